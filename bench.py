@@ -1,0 +1,315 @@
+#!/usr/bin/env python
+"""GROUP BY benchmark on GB300.
+
+Workload (one step = one full GROUP BY pass): the high-cardinality radix
+GROUP BY — 100,000,000 rows, seed 1; k INT64 Zipf(s=1.1) over 20,000,000
+values (ranks mapped into [0, 2^40) by a seeded permutation); x DOUBLE ~
+Normal(100, 25);  SELECT k, COUNT(*), SUM(x), AVG(x) FROM t GROUP BY k,
+materialising the full result in HBM and the ORDER BY COUNT(*) DESC
+LIMIT 10 TopN on it.
+
+  value  — rows/s with the columns resident in HBM (device-timed).
+  e2e    — rows/s through the C ABI with pinned HOST buffers: host→HBM copy
+           of the columns, the GROUP BY, and the device→host copy of the
+           full result, every step.
+
+Inputs (1.6 GB) are larger than L2 (129 MB), so no L2 flush is needed.
+``--impl reference`` times the CPU restatement of the reference's GROUP BY
+(per-thread maps + shard merge, all host cores) on a bounded sample.
+Multi-GPU: the path runs as independent replicas (one full workload per
+rank, no collective); value = rows of all ranks / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GROUP BY rows/s & HBM GB/s at 100M rows; batched queries/s and p99 vs plain"
+N_VALUES = 20_000_000
+EST_GROUPS = 8_000_000  # planner estimate handed to the operator
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--rows", type=int, default=100_000_000)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=20_000_000)
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+        self.idx = gpu_index
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except Exception:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.f.read().splitlines():
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def gen_data(rows):
+    from slothdb_gb300 import datagen
+    t = time.time()
+    k, x = datagen.zipf(rows, seed=1, n_values=N_VALUES)
+    return k, x, time.time() - t
+
+
+def cpu_baseline(k, x, sample_rows, threads=None):
+    """Time the oracle's CPU restatement of the reference GROUP BY on the
+    first `sample_rows` rows with all host threads."""
+    import oracle
+    threads = threads or os.cpu_count() or 1
+    n = min(sample_rows, len(k))
+    ks, xs = k[:n], x[:n]
+    oracle.run_query([3, 4], [0], [("count_star", -1), ("sum", 1), ("avg", 1)], [ks[:100_000], xs[:100_000]],
+                     nthreads=threads)
+    t = time.perf_counter()
+    oracle.run_query([3, 4], [0], [("count_star", -1), ("sum", 1), ("avg", 1)], [ks, xs], nthreads=threads,
+                     est_groups=N_VALUES // 4)
+    dt = time.perf_counter() - t
+    return {"value": n / dt, "unit": "rows/s", "cores": threads, "kind": "port",
+            "sample": "first %d rows of the 100M-row workload, one pass, %d threads (%.2f s)" % (n, threads, dt)}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    sample = min(args.cpu_sample // 2, args.rows)
+    k, x, _ = gen_data(max(sample, 1))
+    import oracle
+    aggs = [("count_star", -1), ("sum", 1), ("avg", 1)]
+    times = []
+    for i in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        oracle.run_query([3, 4], [0], aggs, [k, x], nthreads=threads, est_groups=N_VALUES // 4)
+        dt = time.perf_counter() - t
+        if i >= args.warmup:
+            times.append(dt)
+    per = statistics.mean(times)
+    val = sample / per
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "rows/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic",
+            "config": {"workload": "zipf-groupby-100M (bounded sample of %d rows per step)" % sample,
+                       "rows": sample, "distinct_values": N_VALUES, "aggs": "COUNT(*),SUM(x),AVG(x)"},
+            "cpu_baseline": {"value": val, "unit": "rows/s", "cores": threads, "kind": "port",
+                             "sample": "first %d rows of the 100M-row workload per step" % sample},
+            "e2e": {"value": val, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    ws, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from slothdb_gb300 import capi
+    capi.load(build_if_missing=True)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    rows = args.rows
+    k, x, gen_s = gen_data(rows)
+    dk = torch.from_numpy(k).cuda()
+    dx = torch.from_numpy(x).cuda()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    aggs = [("count_star", -1), ("sum", 1), ("avg", 1)]
+    g = capi.GroupBy([capi.BIGINT, capi.DOUBLE], [0], aggs, est_groups=EST_GROUPS)
+    g.set_topn(1, False, 10)
+
+    def step_device():
+        g.reset()
+        g.ingest([dk, dx], nrows=rows, device=True, stream=sp)
+        g.finalize(stream=sp)
+
+    for _ in range(args.warmup):
+        step_device()
+    torch.cuda.synchronize()
+    # one profiled pass for per-kernel device times (CUDA events on `sp`)
+    g.set_profiling(True)
+    step_device()
+    prof = g.profile()
+    g.set_profiling(False)
+    launches_before = g.launches()
+
+    clocks = Clocks(local)
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        step_device()
+        launches += g.launches()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    # full result size: run once without TopN to count groups
+    g2 = capi.GroupBy([capi.BIGINT, capi.DOUBLE], [0], aggs, est_groups=EST_GROUPS)
+    g2.ingest([dk, dx], nrows=rows, device=True, stream=sp)
+    g2.finalize(stream=sp)
+    import ctypes as C
+    rr = capi.Result()
+    capi.check(g2.lib.gb_agg_result_device(g2.h, C.byref(rr)))
+    n_groups = int(rr.n_rows)
+    g2.close()
+
+    in_bytes = rows * 16
+    out_bytes = n_groups * 32
+    alg_bytes = in_bytes + out_bytes
+    value = rows * ws / (ms / 1e3)
+
+    # roofline: dominant kernel = the ingest kernel
+    ing = prof.get("k_ingest", (1, float("nan")))
+    ing_ms = ing[1] / max(1, ing[0])
+    achieved = in_bytes / (ing_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": achieved / hbm_peak, "traffic": None,
+                "kernel": "k_ingest", "kernel_ms": ing_ms,
+                "peak_source": peak_src,
+                "step_GBps": alg_bytes / (ms / 1e3) / 1e9,
+                "step_frac": alg_bytes / (ms / 1e3) / 1e9 / hbm_peak,
+                "kernels_ms": {kname: v[1] / max(1, v[0]) for kname, v in prof.items()}}
+
+    # e2e through the C ABI with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        pk = capi.PinnedBuffer(rows * 8)
+        px = capi.PinnedBuffer(rows * 8)
+        pk.view(np.int64)[:] = k
+        px.view(np.float64)[:] = x
+        ge = capi.GroupBy([capi.BIGINT, capi.DOUBLE], [0], aggs, est_groups=EST_GROUPS)
+        d2h = 0
+
+        def step_e2e():
+            ge.reset()
+            ge.ingest([pk.ptr, px.ptr], nrows=rows, stream=sp)  # host (pinned) pointers
+            ge.finalize(stream=sp)
+            res = ge.result()
+            return sum(a.nbytes for a, _ in res)
+
+        for _ in range(2):
+            d2h = step_e2e()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(max(1, args.steps // 2)):
+            d2h = step_e2e()
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - t0) / max(1, args.steps // 2)
+        e2e = {"value": rows * ws / e2e_s, "unit": "rows/s", "h2d_bytes_per_step": in_bytes,
+               "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3}
+        ge.close()
+        pk.close()
+        px.close()
+
+    cpu = None
+    if rank == 0:
+        cpu = cpu_baseline(k, x, args.cpu_sample)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic",
+                "config": {"workload": "zipf-groupby-100M", "rows": rows, "distinct_values": N_VALUES,
+                           "observed_groups": n_groups, "key": "INT64 Zipf(1.1)", "aggs": "COUNT(*),SUM(x),AVG(x)",
+                           "topn": "ORDER BY COUNT(*) DESC LIMIT 10 (+ full result in HBM)",
+                           "l2": "inputs 1.6 GB > L2 129 MB (no flush needed)",
+                           "parallelism": "replicas" if ws > 1 else "single",
+                           "est_groups_hint": EST_GROUPS, "datagen_s": round(gen_s, 1)},
+                "algorithmic_bytes_per_step": alg_bytes,
+                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+                "gpu_launches": launches}
+        print(json.dumps(line), flush=True)
+    g.close()
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

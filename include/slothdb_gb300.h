@@ -1,0 +1,207 @@
+/*
+ * slothdb_gb300.h — C ABI of the GB300 GROUP BY execution path.
+ *
+ * One handle (gb_agg) executes one GROUP BY: it is created from a plan
+ * description (group columns, aggregates, simple scan predicates), is fed
+ * row batches (typed column vectors or raw Parquet row groups), and is
+ * finalised into a typed result table.  Every entry point returns a
+ * gb_status; gb_last_error() gives the message of the calling thread's most
+ * recent failure.  There is no CPU fallback: a shape the GPU path does not
+ * implement is rejected with GB_ERR_UNSUPPORTED.
+ *
+ * Handles are thread-compatible (one thread at a time per handle).  Host
+ * pointers passed in are borrowed for the duration of the call; result
+ * buffers are owned by the handle until the next reset/destroy.
+ *
+ * Every function names the reference (SlothDB) interface it replaces; paths
+ * are relative to the reference project root.
+ */
+#ifndef SLOTHDB_GB300_H
+#define SLOTHDB_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GB_ABI_VERSION 1
+
+typedef enum gb_status {
+    GB_OK = 0,
+    GB_ERR_INVALID = 1,      /* bad argument or malformed plan                */
+    GB_ERR_OOM = 2,          /* device or pinned-host allocation failed       */
+    GB_ERR_UNSUPPORTED = 3,  /* shape not implemented on the GPU path         */
+    GB_ERR_TIMEOUT = 4,      /* a bounded device wait gave up                 */
+    GB_ERR_CUDA = 5,         /* CUDA runtime error                            */
+    GB_ERR_CORRUPT = 6,      /* malformed Parquet page / footer               */
+    GB_ERR_STATE = 7,        /* call out of order (e.g. result before finalize) */
+    GB_ERR_BUDGET = 8        /* admission refused: over the memory budget     */
+} gb_status;
+
+/* Column types, named after the reference's LogicalTypeId values that the
+ * GROUP BY path accepts (include/slothdb/common/types/logical_type.hpp). */
+typedef enum gb_type {
+    GB_T_SMALLINT = 1,  /* int16  */
+    GB_T_INTEGER = 2,   /* int32  */
+    GB_T_BIGINT = 3,    /* int64  */
+    GB_T_DOUBLE = 4,    /* double */
+    GB_T_VARCHAR = 5    /* bytes + int64 offsets[n+1] */
+} gb_type;
+
+/* Aggregates the binder resolves for GROUP BY
+ * (src/binder/binder.cpp:1345-1391): COUNT → BIGINT; SUM(int) → BIGINT;
+ * SUM(double) → DOUBLE; AVG → DOUBLE; MIN/MAX → input type. */
+typedef enum gb_agg_kind {
+    GB_AGG_COUNT_STAR = 0,
+    GB_AGG_COUNT = 1,
+    GB_AGG_SUM = 2,
+    GB_AGG_AVG = 3,
+    GB_AGG_MIN = 4,
+    GB_AGG_MAX = 5
+} gb_agg_kind;
+
+/* Comparison of a SimplePredicate (src/execution/physical_planner.cpp:110-135). */
+typedef enum gb_cmp {
+    GB_CMP_EQ = 0, GB_CMP_NE = 1, GB_CMP_LT = 2,
+    GB_CMP_LE = 3, GB_CMP_GT = 4, GB_CMP_GE = 5
+} gb_cmp;
+
+typedef struct gb_agg_desc {
+    int32_t kind;   /* gb_agg_kind */
+    int32_t col;    /* input column index; -1 for COUNT(*) */
+} gb_agg_desc;
+
+/* col OP constant.  Integer columns compare in int64 (the reference widens
+ * to int64 before comparing, physical_planner.cpp:466-479, 693-716); DOUBLE
+ * columns compare against d_const. */
+typedef struct gb_filter {
+    int32_t col;
+    int32_t op;      /* gb_cmp */
+    int64_t i_const;
+    double d_const;
+} gb_filter;
+
+#define GB_SPEC_COL_NULLABLE_BITS 0  /* see gb_agg_spec.nullable_mask */
+
+typedef struct gb_agg_spec {
+    uint32_t n_cols;            /* input schema width                        */
+    const int32_t *col_types;   /* gb_type per input column                  */
+    uint32_t n_groups;          /* 1 or 2 group columns                      */
+    const int32_t *group_cols;
+    uint32_t n_aggs;
+    const gb_agg_desc *aggs;
+    uint32_t n_filters;         /* conjunction of predicates (WHERE)         */
+    const gb_filter *filters;
+    uint64_t nullable_mask;     /* bit c set: column c may carry NULLs       */
+    uint64_t est_groups;        /* planner estimate; 0 = unknown             */
+} gb_agg_spec;
+
+/* One input column vector.  Validity uses the reference's ValidityMask
+ * layout (include/slothdb/common/types/validity_mask.hpp:9-69): 64-bit
+ * words, bit (i % 64) of word (i / 64) set = row i valid; NULL = all valid. */
+typedef struct gb_col {
+    const void *data;
+    const uint64_t *validity;
+    const int64_t *offsets;     /* VARCHAR only: n+1 byte offsets into data  */
+} gb_col;
+
+typedef enum gb_mem { GB_MEM_HOST = 0, GB_MEM_DEVICE = 1 } gb_mem;
+
+/* Result table: [group columns..., aggregate columns...], the output slot
+ * order of PhysicalHashAggregate (physical_planner.cpp:6017-6021). */
+typedef struct gb_result {
+    uint64_t n_rows;
+    uint32_t n_cols;
+    const int32_t *types;             /* gb_type per output column          */
+    const void *const *data;          /* per column                         */
+    const int64_t *const *offsets;    /* VARCHAR columns, else NULL         */
+    const uint64_t *const *validity;  /* NULL entry = all valid             */
+} gb_result;
+
+typedef struct gb_agg gb_agg;
+
+/* Thread-local message of the last failed call ("" if none). */
+const char *gb_last_error(void);
+int gb_abi_version(void);
+
+/* Replaces PhysicalHashAggregate(groups, aggregates, result_types)
+ * (src/execution/physical_planner.cpp:6011-6015) as constructed by
+ * PhysicalPlanner::PlanAggregate (physical_planner.cpp:14356-14362). */
+gb_status gb_agg_create(const gb_agg_spec *spec, gb_agg **out);
+
+/* Replaces PhysicalHashAggregate::SetTopNHint (physical_planner.cpp:6022-6027):
+ * keep only the best `limit` rows by output column `col_idx` (output slot
+ * space; ties broken by group key ascending). */
+gb_status gb_agg_set_topn(gb_agg *h, uint32_t col_idx, int32_t ascending, uint64_t limit);
+
+/* Replaces PhysicalHashAggregate::SetRowLimit (physical_planner.cpp:6032). */
+gb_status gb_agg_set_row_limit(gb_agg *h, uint64_t limit);
+
+/* Replaces the child GetData(DataChunk&) consumption of the chunk loops
+ * (physical_planner.cpp:7933-8021, 12291-12516): aggregates `nrows` rows of
+ * the spec's input columns.  May be called repeatedly; states accumulate.
+ * mem = GB_MEM_HOST copies the vectors to HBM inside the call (pinned
+ * host memory is copied directly, overlapped with the aggregation);
+ * GB_MEM_DEVICE reads device-resident vectors.  `stream` is a cudaStream_t
+ * (NULL = legacy default stream). */
+gb_status gb_agg_ingest(gb_agg *h, const gb_col *cols, uint64_t nrows, int32_t mem, void *stream);
+
+/* Replaces the merge + emit of ComputeAggregates (physical_planner.cpp:
+ * 7871-7908 merge, 8027-8173 direct emit / TopN, agg_emit_helpers.cpp:26-165). */
+gb_status gb_agg_finalize(gb_agg *h, void *stream);
+
+/* Replaces PhysicalHashAggregate::GetData emission (physical_planner.cpp:
+ * 6040-6060): host copies of the result columns, owned by the handle. */
+gb_status gb_agg_result(gb_agg *h, gb_result *out);
+
+/* Device-resident view of the same result (no copy). */
+gb_status gb_agg_result_device(gb_agg *h, gb_result *out);
+
+/* Rewinds the handle to the empty state, keeping its device allocations
+ * (re-execution of the same plan: PhysicalHashAggregate::Init,
+ * physical_planner.cpp:6034-6038). */
+gb_status gb_agg_reset(gb_agg *h);
+
+void gb_agg_destroy(gb_agg *h);
+
+/* Number of kernels this handle launched since create/reset (for launch
+ * accounting). */
+uint64_t gb_agg_kernel_launches(const gb_agg *h);
+
+/* Per-kernel device time of this handle, measured with CUDA events on the
+ * stream each kernel is launched on (enabled by gb_agg_set_profiling; no
+ * reference counterpart: the reference's SLOTH_PROFILE counters,
+ * include/slothdb/storage/parquet.hpp:22-44, are host timers). */
+typedef struct gb_kernel_stat {
+    char name[32];
+    uint64_t launches;
+    double ms;
+} gb_kernel_stat;
+
+gb_status gb_agg_set_profiling(gb_agg *h, int32_t on);
+uint32_t gb_agg_profile(const gb_agg *h, gb_kernel_stat *out, uint32_t max);
+
+/* Replaces GPUEngine::HashAggregate (include/slothdb/execution/gpu/
+ * gpu_engine.hpp:78-84): group int32 keys, SUM and COUNT int32 values.
+ * Host in, host out.  Output arrays hold `*n_out` groups (capacity
+ * `cap`, GB_ERR_INVALID if more groups than cap). */
+gb_status gb_engine_hash_aggregate(const int32_t *keys, const int32_t *values, uint64_t n,
+                                   int32_t *out_keys, int64_t *out_sums, int64_t *out_counts,
+                                   uint64_t cap, uint64_t *n_out);
+
+/* Pinned host memory helpers (so a caller can stage inputs for the
+ * overlapped host→HBM path without linking CUDA itself). */
+gb_status gb_host_alloc(void **ptr, size_t bytes);
+gb_status gb_host_free(void *ptr);
+gb_status gb_device_alloc(void **ptr, size_t bytes);
+gb_status gb_device_free(void *ptr);
+gb_status gb_memcpy(void *dst, const void *src, size_t bytes, int32_t kind /* 0 h2d,1 d2h,2 d2d */);
+gb_status gb_device_sync(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SLOTHDB_GB300_H */

@@ -1,0 +1,288 @@
+"""ctypes binding of include/slothdb_gb300.h and a thin Python host API.
+
+The library is the in-tree ``slothdb_gb300/_build/libslothdb_gb300.so``.
+Loading fails loudly when it is missing: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+GB_OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "OOM", 3: "UNSUPPORTED", 4: "TIMEOUT", 5: "CUDA", 6: "CORRUPT",
+                7: "STATE", 8: "BUDGET"}
+
+SMALLINT, INTEGER, BIGINT, DOUBLE, VARCHAR = 1, 2, 3, 4, 5
+COUNT_STAR, COUNT, SUM, AVG, MIN, MAX = 0, 1, 2, 3, 4, 5
+EQ, NE, LT, LE, GT, GE = 0, 1, 2, 3, 4, 5
+MEM_HOST, MEM_DEVICE = 0, 1
+
+NP_TYPES = {SMALLINT: np.int16, INTEGER: np.int32, BIGINT: np.int64, DOUBLE: np.float64}
+AGG_NAMES = {"count_star": COUNT_STAR, "count": COUNT, "sum": SUM, "avg": AVG, "min": MIN, "max": MAX}
+CMP_NAMES = {"==": EQ, "=": EQ, "!=": NE, "<>": NE, "<": LT, "<=": LE, ">": GT, ">=": GE}
+
+
+class GbError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("%s: %s" % (STATUS_NAMES.get(status, status), msg))
+        self.status = status
+
+
+class AggDesc(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("col", C.c_int32)]
+
+
+class Filter(C.Structure):
+    _fields_ = [("col", C.c_int32), ("op", C.c_int32), ("i_const", C.c_int64), ("d_const", C.c_double)]
+
+
+class AggSpec(C.Structure):
+    _fields_ = [("n_cols", C.c_uint32), ("col_types", C.POINTER(C.c_int32)),
+                ("n_groups", C.c_uint32), ("group_cols", C.POINTER(C.c_int32)),
+                ("n_aggs", C.c_uint32), ("aggs", C.POINTER(AggDesc)),
+                ("n_filters", C.c_uint32), ("filters", C.POINTER(Filter)),
+                ("nullable_mask", C.c_uint64), ("est_groups", C.c_uint64)]
+
+
+class Col(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("validity", C.c_void_p), ("offsets", C.c_void_p)]
+
+
+class KernelStat(C.Structure):
+    _fields_ = [("name", C.c_char * 32), ("launches", C.c_uint64), ("ms", C.c_double)]
+
+
+class Result(C.Structure):
+    _fields_ = [("n_rows", C.c_uint64), ("n_cols", C.c_uint32), ("types", C.POINTER(C.c_int32)),
+                ("data", C.POINTER(C.c_void_p)), ("offsets", C.POINTER(C.c_void_p)),
+                ("validity", C.POINTER(C.c_void_p))]
+
+
+# every exported symbol of include/slothdb_gb300.h (checked by tests)
+_SIGS = {
+    "gb_last_error": (C.c_char_p, []),
+    "gb_abi_version": (C.c_int, []),
+    "gb_agg_create": (C.c_int, [C.POINTER(AggSpec), C.POINTER(C.c_void_p)]),
+    "gb_agg_set_topn": (C.c_int, [C.c_void_p, C.c_uint32, C.c_int32, C.c_uint64]),
+    "gb_agg_set_row_limit": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "gb_agg_ingest": (C.c_int, [C.c_void_p, C.POINTER(Col), C.c_uint64, C.c_int32, C.c_void_p]),
+    "gb_agg_finalize": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gb_agg_result": (C.c_int, [C.c_void_p, C.POINTER(Result)]),
+    "gb_agg_result_device": (C.c_int, [C.c_void_p, C.POINTER(Result)]),
+    "gb_agg_reset": (C.c_int, [C.c_void_p]),
+    "gb_agg_destroy": (None, [C.c_void_p]),
+    "gb_agg_kernel_launches": (C.c_uint64, [C.c_void_p]),
+    "gb_agg_set_profiling": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gb_agg_profile": (C.c_uint32, [C.c_void_p, C.POINTER(KernelStat), C.c_uint32]),
+    "gb_engine_hash_aggregate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "gb_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
+    "gb_host_free": (C.c_int, [C.c_void_p]),
+    "gb_device_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
+    "gb_device_free": (C.c_int, [C.c_void_p]),
+    "gb_memcpy": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int32]),
+    "gb_device_sync": (C.c_int, []),
+}
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = False):
+    """Load the CUDA library (no fallback: raises if it cannot be loaded)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = lib_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError("GB300 library not built (%s); run __graft_entry__.build()" % path)
+        _build.build_lib()
+    lib = C.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def declared_symbols():
+    return sorted(_SIGS)
+
+
+def check(status: int):
+    if status != GB_OK:
+        raise GbError(status, load().gb_last_error().decode())
+
+
+def _arr_ptr(a):
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if hasattr(a, "data_ptr"):  # torch tensor
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+class GroupBy:
+    """One GROUP BY handle (gb_agg) — the Python mirror of the operator.
+
+    ``aggs``: list of (kind, col) with kind a name ('count_star', 'count',
+    'sum', 'avg', 'min', 'max') or the gb_agg_kind code; col = -1 for
+    COUNT(*).  ``filters``: list of (col, op, const) with op one of
+    '==', '!=', '<', '<=', '>', '>='.
+    """
+
+    def __init__(self, col_types, group_cols, aggs, filters=(), nullable=(), est_groups=0):
+        self.lib = load()
+        self.col_types = list(col_types)
+        self.group_cols = list(group_cols)
+        self.aggs = [(AGG_NAMES[k] if isinstance(k, str) else int(k), int(c)) for k, c in aggs]
+        self.filters = list(filters)
+        ct = (C.c_int32 * len(self.col_types))(*self.col_types)
+        gc = (C.c_int32 * len(self.group_cols))(*self.group_cols)
+        ag = (AggDesc * len(self.aggs))(*[AggDesc(k, c) for k, c in self.aggs])
+        fl = (Filter * max(1, len(self.filters)))()
+        for i, (col, op, const) in enumerate(self.filters):
+            opc = CMP_NAMES[op] if isinstance(op, str) else int(op)
+            if self.col_types[col] == DOUBLE:
+                fl[i] = Filter(col, opc, 0, float(const))
+            else:
+                fl[i] = Filter(col, opc, int(const), 0.0)
+        mask = 0
+        for c in nullable:
+            mask |= 1 << int(c)
+        spec = AggSpec(len(self.col_types), ct, len(self.group_cols), gc, len(self.aggs), ag,
+                       len(self.filters), fl if self.filters else None, mask, int(est_groups))
+        h = C.c_void_p()
+        check(self.lib.gb_agg_create(C.byref(spec), C.byref(h)))
+        self.h = h
+        self._keep = []
+
+    def set_topn(self, col_idx, ascending, limit):
+        check(self.lib.gb_agg_set_topn(self.h, col_idx, 1 if ascending else 0, limit))
+
+    def set_row_limit(self, limit):
+        check(self.lib.gb_agg_set_row_limit(self.h, limit))
+
+    def ingest(self, cols, nrows=None, validity=None, device=False, stream=None):
+        """cols: numpy arrays (host) or torch CUDA tensors / int device
+        pointers (device=True), one per input column."""
+        n = len(self.col_types)
+        arr = (Col * n)()
+        keep = []
+        for i, a in enumerate(cols):
+            if not device and isinstance(a, np.ndarray):
+                a = np.ascontiguousarray(a, dtype=NP_TYPES[self.col_types[i]])
+                keep.append(a)
+            v = validity[i] if validity is not None else None
+            if v is not None and not device and isinstance(v, np.ndarray):
+                v = np.ascontiguousarray(v, dtype=np.uint64)
+                keep.append(v)
+            arr[i] = Col(_arr_ptr(a), _arr_ptr(v), None)
+        if nrows is None:
+            nrows = len(cols[0])
+        check(self.lib.gb_agg_ingest(self.h, arr, int(nrows), MEM_DEVICE if device else MEM_HOST,
+                                     C.c_void_p(stream) if stream else None))
+
+    def finalize(self, stream=None):
+        check(self.lib.gb_agg_finalize(self.h, C.c_void_p(stream) if stream else None))
+
+    def result(self):
+        """Host copy of the result: list of (values ndarray, valid bool ndarray)."""
+        r = Result()
+        check(self.lib.gb_agg_result(self.h, C.byref(r)))
+        out = []
+        n = int(r.n_rows)
+        for c in range(r.n_cols):
+            t = r.types[c]
+            dt = np.dtype(NP_TYPES[t])
+            if n:
+                buf = (C.c_char * (n * dt.itemsize)).from_address(r.data[c])
+                vals = np.frombuffer(buf, dtype=dt).copy()
+                vw = np.frombuffer((C.c_char * (((n + 63) // 64) * 8)).from_address(r.validity[c]),
+                                   dtype=np.uint64)
+                bits = np.unpackbits(vw.view(np.uint8), bitorder="little")[:n].astype(bool)
+            else:
+                vals = np.zeros(0, dtype=dt)
+                bits = np.zeros(0, dtype=bool)
+            out.append((vals, bits))
+        return out
+
+    def set_profiling(self, on=True):
+        check(self.lib.gb_agg_set_profiling(self.h, 1 if on else 0))
+
+    def profile(self):
+        """{kernel name: (launches, total ms)} measured with CUDA events."""
+        arr = (KernelStat * 32)()
+        n = self.lib.gb_agg_profile(self.h, arr, 32)
+        return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].ms)) for i in range(min(n, 32))}
+
+    def launches(self):
+        return int(self.lib.gb_agg_kernel_launches(self.h))
+
+    def reset(self):
+        check(self.lib.gb_agg_reset(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gb_agg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def validity_words(valid_bool: np.ndarray) -> np.ndarray:
+    """bool[n] → ValidityMask words (uint64, bit i%64 of word i/64)."""
+    n = len(valid_bool)
+    pad = np.zeros(((n + 63) // 64) * 64, dtype=bool)
+    pad[:n] = valid_bool
+    return np.packbits(pad, bitorder="little").view(np.uint64).copy()
+
+
+class PinnedBuffer:
+    """Page-locked host buffer from gb_host_alloc, viewable as numpy."""
+
+    def __init__(self, nbytes):
+        self.lib = load()
+        p = C.c_void_p()
+        check(self.lib.gb_host_alloc(C.byref(p), int(nbytes)))
+        self.ptr = p.value
+        self.nbytes = int(nbytes)
+
+    def view(self, dtype, count=None):
+        dt = np.dtype(dtype)
+        if count is None:
+            count = self.nbytes // dt.itemsize
+        buf = (C.c_char * (count * dt.itemsize)).from_address(self.ptr)
+        return np.frombuffer(buf, dtype=dt)
+
+    def close(self):
+        if self.ptr:
+            self.lib.gb_host_free(C.c_void_p(self.ptr))
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,1459 @@
+// gb_agg.cu — single-query GROUP BY on GB300: plan compilation, the
+// persistent hash-aggregation kernel, table growth, result compaction
+// (emit), the fused TopN select, and the C ABI of include/slothdb_gb300.h.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gb_agg_host.h"
+#include "gb_kernels.cuh"
+
+namespace gb {
+
+// ----------------------------------------------------------------- errors
+static thread_local std::string g_err;
+
+void set_error(const char *fmt, ...) {
+    char buf[1024];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+}
+
+gb_status cuda_fail(cudaError_t e, const char *what) {
+    set_error("CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
+    if (e == cudaErrorMemoryAllocation) return GB_ERR_OOM;
+    return GB_ERR_CUDA;
+}
+
+int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+// ================================================================ kernels
+__global__ void k_table_init(u64 *slots, u64 nslots, int stride, const __grid_constant__ Plan P) {
+    u64 total = nslots * (u64)stride;
+    for (u64 i = blockIdx.x * (u64)blockDim.x + threadIdx.x; i < total; i += (u64)gridDim.x * blockDim.x) {
+        int w = (int)(i % (u64)stride);
+        u64 v;
+        if (w == 0) v = EMPTY_KEY;
+        else if (w - 1 < P.words) v = P.word_init[w - 1];
+        else v = 0;
+        slots[i] = v;
+    }
+}
+
+struct IngestArgs {
+    u64 n_rows;
+    u32 tile_rows;
+    u32 n_tiles;      // tiles remaining from first_tile
+    u32 first_tile;
+    int32_t smem_slots;
+    int32_t smem_probe;
+    int32_t pad;
+};
+
+// Persistent ingest: CTAs claim tiles of rows until none are left or the
+// spill buffer nears its threshold (then the host grows the table, merges
+// the spill records and relaunches from the first unclaimed tile).
+template <bool PRECOMBINE>
+__global__ void __launch_bounds__(512) k_ingest(const __grid_constant__ Plan P, const TableRef T, const IngestArgs A) {
+    extern __shared__ u64 smem[];
+    __shared__ u32 s_tile;
+    __shared__ u32 s_new;
+    SmemTable sm;
+    sm.S = A.smem_slots;
+    sm.probe = A.smem_probe;
+    sm.keys = smem;
+    sm.st = smem + sm.S;
+    if (threadIdx.x == 0) s_new = 0;
+    smem_init(P, sm);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            u32 t = ~0u;
+            if (*(volatile u32 *)&T.ctl->stop == 0) {
+                u32 c = atomicAdd(&T.ctl->tile_counter, 1u);
+                if (c < A.n_tiles) t = c;
+            }
+            s_tile = t;
+        }
+        __syncthreads();
+        const u32 t = s_tile;
+        __syncthreads();
+        if (t == ~0u) break;
+        const u64 t0 = (u64)(A.first_tile + t) * A.tile_rows;
+        const u64 t1 = min(A.n_rows, t0 + A.tile_rows);
+        for (u64 base = t0 + (u64)warp * 32; base < t1; base += (u64)nwarps * 32)
+            warp_rows<PRECOMBINE>(P, T, sm, base, t1, &s_new);
+        if (threadIdx.x == 0 && *(volatile u32 *)&T.ctl->spill_count > T.spill_threshold)
+            atomicExch(&T.ctl->stop, 1u);
+    }
+    __syncthreads();
+    smem_flush(P, T, sm, &s_new);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_new) atomicAdd(&T.ctl->n_groups, s_new);
+}
+
+// Re-insert every used slot of `old` into the (larger, initialised) table.
+__global__ void k_rehash(const __grid_constant__ Plan P, const u64 *old, u64 old_cap, int stride, const TableRef T) {
+    __shared__ u32 s_new;
+    if (threadIdx.x == 0) s_new = 0;
+    __syncthreads();
+    for (u64 s = blockIdx.x * (u64)blockDim.x + threadIdx.x; s < old_cap + 2; s += (u64)gridDim.x * blockDim.x) {
+        const u64 *src = old + s * (u64)stride;
+        if (s >= old_cap) {
+            if (src[1] == 0) continue;
+            u64 *dst = T.slots + (T.cap + (s - old_cap)) * (u64)T.stride;
+            for (int w = 0; w < P.words; w++) dst[1 + w] = src[1 + w];
+            continue;
+        }
+        u64 k = src[0];
+        if (k == EMPTY_KEY) continue;
+        long long d = g_slot(T, k, mix64(k), &s_new);
+        if (d < 0) {
+            u64 v[GB_MAX_OPS];
+            for (int i = 0; i < P.n_ops; i++) v[i] = src[1 + P.ops[i].word];
+            spill_record(P, T, k, src[1], v);
+            continue;
+        }
+        u64 *dst = T.slots + (u64)d * (u64)T.stride;
+        for (int w = 0; w < P.words; w++) dst[1 + w] = src[1 + w];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_new) atomicAdd(&T.ctl->n_groups, s_new);
+}
+
+// Merge spill records [0, n) into the table; records that still do not fit
+// are re-spilled at the tail (index >= n), so the host can loop.
+__global__ void k_merge_records(const __grid_constant__ Plan P, const u64 *recs, u32 n, const TableRef T) {
+    __shared__ u32 s_new;
+    if (threadIdx.x == 0) s_new = 0;
+    __syncthreads();
+    for (u64 i = blockIdx.x * (u64)blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
+        const u64 *rec = recs + i * (u64)(1 + P.words);
+        u64 v[GB_MAX_OPS];
+        for (int j = 0; j < P.n_ops; j++) v[j] = rec[1 + P.ops[j].word];
+        global_fold(P, T, rec[0], rec[1], v, &s_new);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_new) atomicAdd(&T.ctl->n_groups, s_new);
+}
+
+// ------------------------------------------------------------ emit
+struct EmitAgg {
+    int32_t kind;      // gb_agg_kind
+    int32_t in_type;   // gb_type of the input column (-1 for COUNT(*))
+    int32_t out_type;  // gb_type of the output column
+    int32_t val_word;  // state word of the value (-1 none)
+    int32_t cnt_word;  // state word of the non-NULL count
+    int32_t pad;
+};
+
+struct EmitArgs {
+    EmitAgg aggs[GB_MAX_AGGS];
+    void *out[2 + GB_MAX_AGGS];        // device column buffers
+    uint64_t *valid[2 + GB_MAX_AGGS];  // validity words (pre-set to all ones)
+    int32_t n_aggs;
+    int32_t n_keys;
+    u64 out_cap;
+};
+
+__device__ __forceinline__ void store_int(void *base, int type, u64 i, i64 v) {
+    switch (type) {
+    case GB_T_SMALLINT: ((int16_t *)base)[i] = (int16_t)v; break;
+    case GB_T_INTEGER: ((int32_t *)base)[i] = (int32_t)v; break;
+    default: ((long long *)base)[i] = v; break;
+    }
+}
+
+__device__ __forceinline__ void clear_valid(uint64_t *vw, u64 i) {
+    atomicAnd((unsigned long long *)(vw + (i >> 6)), ~(1ull << (i & 63)));
+}
+
+__device__ __forceinline__ i64 sext(u64 x, int bits) {
+    if (bits >= 64) return (i64)x;
+    u64 m = 1ull << (bits - 1);
+    x &= (1ull << bits) - 1ull;
+    return (i64)((x ^ m) - m);
+}
+
+// Compact used slots into dense result columns (the direct emit of
+// physical_planner.cpp:8027-8173 with agg_emit_helpers.cpp:26-165 rules).
+__global__ void k_compact(const __grid_constant__ Plan P, const u64 *slots, u64 cap, int stride,
+                          const __grid_constant__ EmitArgs E, Ctl *ctl) {
+    const int lane = threadIdx.x & 31;
+    const u64 total = cap + 2;
+    const u64 step = (u64)gridDim.x * blockDim.x;
+    for (u64 base = blockIdx.x * (u64)blockDim.x + threadIdx.x - lane; base < total; base += step) {
+        const u64 s = base + lane;
+        bool occ = false;
+        const u64 *sl = slots + s * (u64)stride;
+        if (s < cap) occ = sl[0] != EMPTY_KEY;
+        else if (s < total) occ = sl[1] != 0;
+        const unsigned m = __ballot_sync(FULL, occ);
+        if (m == 0) continue;
+        u32 wbase = 0;
+        if (lane == 0) wbase = atomicAdd(&ctl->out_count, (u32)__popc(m));
+        wbase = __shfl_sync(FULL, wbase, 0);
+        if (!occ) continue;
+        const u64 o = wbase + __popc(m & ((1u << lane) - 1u));
+        if (o >= E.out_cap) {
+            atomicOr(&ctl->err, (u32)ERR_OUT_OVERFLOW);
+            continue;
+        }
+        // keys
+        const u64 pk = (s < cap) ? sl[0] : (s == cap ? EMPTY_KEY : 0ull);
+        const bool null_key = (s == cap + 1);
+        if (P.key_mode == KEY_SINGLE || P.key_mode == KEY_STRING) {
+            store_int(E.out[0], P.key_type[0], o, (i64)pk);
+            if (null_key) clear_valid(E.valid[0], o);
+        } else if (P.key_mode == KEY_PACKED) {
+            const int bb = P.key_bits_b, ba = P.key_bits_a;
+            i64 a = sext(pk >> bb, ba), b = sext(pk, bb);
+            bool na = (pk >> (ba + bb)) & 1ull, nb = (pk >> (ba + bb + 1)) & 1ull;
+            store_int(E.out[0], P.key_type[0], o, a);
+            store_int(E.out[1], P.key_type[1], o, b);
+            if (na) clear_valid(E.valid[0], o);
+            if (nb) clear_valid(E.valid[1], o);
+        } else {
+            store_int(E.out[0], P.key_type[0], o, (i64)(int32_t)(uint32_t)(pk >> 32));
+            store_int(E.out[1], P.key_type[1], o, (i64)(int32_t)(uint32_t)pk);
+        }
+        const u64 *w = sl + 1;
+        for (int a = 0; a < E.n_aggs; a++) {
+            const EmitAgg &g = E.aggs[a];
+            void *dst = E.out[E.n_keys + a];
+            uint64_t *vw = E.valid[E.n_keys + a];
+            const u64 cnt = w[g.cnt_word];
+            switch (g.kind) {
+            case GB_AGG_COUNT_STAR:
+            case GB_AGG_COUNT: ((long long *)dst)[o] = (i64)cnt; break;
+            case GB_AGG_SUM:
+                if (cnt == 0) { ((long long *)dst)[o] = 0; clear_valid(vw, o); }
+                else ((long long *)dst)[o] = (i64)w[g.val_word];  // int64 or double bits
+                break;
+            case GB_AGG_AVG:
+                if (cnt == 0) { ((double *)dst)[o] = 0.0; clear_valid(vw, o); }
+                else {
+                    double sum = (g.in_type == GB_T_DOUBLE) ? __longlong_as_double((i64)w[g.val_word])
+                                                            : (double)(i64)w[g.val_word];
+                    ((double *)dst)[o] = sum / (double)cnt;
+                }
+                break;
+            default:  // MIN / MAX
+                if (cnt == 0) { store_int(dst, g.out_type == GB_T_DOUBLE ? GB_T_BIGINT : g.out_type, o, 0); clear_valid(vw, o); }
+                else if (g.out_type == GB_T_DOUBLE) ((double *)dst)[o] = dec_f64((i64)w[g.val_word]);
+                else store_int(dst, g.out_type, o, (i64)w[g.val_word]);
+                break;
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------ TopN
+// Order code: a pair (primary, secondary) of u64 where smaller is better.
+struct TopnArgs {
+    const void *order_col;
+    int32_t order_type;   // gb_type of the order column
+    int32_t ascending;
+    const uint64_t *order_valid;
+    const void *key0;
+    const void *key1;
+    int32_t key_type0, key_type1;
+    int32_t n_keys;
+    int32_t K;            // <= 1024
+};
+
+__device__ __forceinline__ u64 ord_u64(i64 v) { return (u64)v ^ 0x8000000000000000ull; }
+
+__device__ __forceinline__ i64 load_any_int(const void *p, int type, u64 i) {
+    switch (type) {
+    case GB_T_SMALLINT: return ((const int16_t *)p)[i];
+    case GB_T_INTEGER: return ((const int32_t *)p)[i];
+    default: return ((const long long *)p)[i];
+    }
+}
+
+__device__ __forceinline__ void topn_code(const TopnArgs &A, u64 i, u64 &p, u64 &s) {
+    u64 prim;
+    bool valid = A.order_valid == nullptr || ((A.order_valid[i >> 6] >> (i & 63)) & 1ull);
+    if (!valid) prim = 0;  // NULL orders first ascending, last descending
+    else if (A.order_type == GB_T_DOUBLE) prim = ord_u64(enc_f64(((const double *)A.order_col)[i]));
+    else prim = ord_u64(load_any_int(A.order_col, A.order_type, i));
+    p = A.ascending ? prim : ~prim;
+    if (A.n_keys == 1) {
+        s = ord_u64(load_any_int(A.key0, A.key_type0, i));
+    } else {
+        u64 a = ord_u64(load_any_int(A.key0, A.key_type0, i)) >> 32;
+        u64 b = ord_u64(load_any_int(A.key1, A.key_type1, i)) >> 32;
+        if (A.key_type0 == GB_T_BIGINT || A.key_type1 == GB_T_BIGINT) {
+            a = ord_u64(load_any_int(A.key0, A.key_type0, i));
+            b = 0;
+        }
+        s = (a << 32) | (b & 0xffffffffull);
+    }
+}
+
+__device__ __forceinline__ bool code_less(u64 ap, u64 as, u64 bp, u64 bs) {
+    return ap < bp || (ap == bp && as < bs);
+}
+
+// Bitonic sort of n (power of two) entries in shared memory, ascending.
+__device__ void smem_bitonic(u64 *P_, u64 *S_, u32 *I_, int n) {
+    for (int k = 2; k <= n; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < n; i += blockDim.x) {
+                int ixj = i ^ j;
+                if (ixj > i) {
+                    bool up = ((i & k) == 0);
+                    bool gt = code_less(P_[ixj], S_[ixj], P_[i], S_[i]);
+                    if (gt == up) {
+                        u64 tp = P_[i]; P_[i] = P_[ixj]; P_[ixj] = tp;
+                        u64 ts = S_[i]; S_[i] = S_[ixj]; S_[ixj] = ts;
+                        u32 ti = I_[i]; I_[i] = I_[ixj]; I_[ixj] = ti;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// Each CTA selects the K best of its slice of items; items are either
+// result rows (ids == nullptr) or a candidate list of row ids (~0u = none).
+// Survivors of the running threshold go to a candidate buffer; when it
+// fills, best ∪ candidates is bitonic-sorted and the best K kept.
+__global__ void __launch_bounds__(512) k_topn(const __grid_constant__ TopnArgs A, const u32 *ids, u64 n,
+                                              u32 *out_ids, u32 *out_n, int sortn) {
+    extern __shared__ u64 tsm[];
+    u64 *Pp = tsm;
+    u64 *Ss = tsm + sortn;
+    u32 *Ii = (u32 *)(tsm + 2 * sortn);
+    __shared__ int s_nbest, s_ncand;
+    __shared__ u64 s_thr_p, s_thr_s;
+    const int K = A.K;
+    if (threadIdx.x == 0) { s_nbest = 0; s_ncand = 0; s_thr_p = ~0ull; s_thr_s = ~0ull; }
+    // entries [0, K) = best (sorted), [K, 2K) = candidates, rest padding
+    for (int i = threadIdx.x; i < sortn; i += blockDim.x) { Pp[i] = ~0ull; Ss[i] = ~0ull; Ii[i] = ~0u; }
+    __syncthreads();
+    const u64 per = (n + gridDim.x - 1) / gridDim.x;
+    const u64 lo = blockIdx.x * per, hi = min(n, lo + per);
+    for (u64 base = lo; base < hi; base += blockDim.x) {
+        const u64 it = base + threadIdx.x;
+        u64 cp = ~0ull, cs = ~0ull;
+        u32 row = ~0u;
+        bool want = false;
+        if (it < hi) {
+            row = ids ? ids[it] : (u32)it;
+            if (row != ~0u) {
+                topn_code(A, row, cp, cs);
+                want = s_nbest < K || code_less(cp, cs, s_thr_p, s_thr_s);
+            }
+        }
+        while (__syncthreads_or(want)) {
+            if (want) {
+                int pos = atomicAdd(&s_ncand, 1);
+                if (pos < K) {
+                    Pp[K + pos] = cp; Ss[K + pos] = cs; Ii[K + pos] = row;
+                    want = false;
+                }
+            }
+            __syncthreads();
+            if (s_ncand >= K) {
+                smem_bitonic(Pp, Ss, Ii, sortn);
+                if (threadIdx.x == 0) {
+                    s_nbest = min(s_nbest + K, K);
+                    s_ncand = 0;
+                    s_thr_p = Pp[K - 1];
+                    s_thr_s = Ss[K - 1];
+                }
+                for (int i = K + threadIdx.x; i < sortn; i += blockDim.x) { Pp[i] = ~0ull; Ss[i] = ~0ull; Ii[i] = ~0u; }
+                __syncthreads();
+                if (want) want = code_less(cp, cs, s_thr_p, s_thr_s);
+            }
+        }
+    }
+    __syncthreads();
+    if (s_ncand > 0) {
+        smem_bitonic(Pp, Ss, Ii, sortn);
+        if (threadIdx.x == 0) s_nbest = min(s_nbest + s_ncand, K);
+        __syncthreads();
+    }
+    const int nb = s_nbest;
+    for (int i = threadIdx.x; i < K; i += blockDim.x) out_ids[(u64)blockIdx.x * K + i] = (i < nb) ? Ii[i] : ~0u;
+    if (threadIdx.x == 0) out_n[blockIdx.x] = nb;
+}
+
+// Gather rows `ids[0..k)` of the dense result into TopN output buffers.
+__global__ void k_gather_rows(const u32 *ids, u32 k, int ncols, const __grid_constant__ EmitArgs src,
+                              const __grid_constant__ EmitArgs dst, const int32_t *types) {
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < k; i += gridDim.x * blockDim.x) {
+        u32 r = ids[i];
+        if (r == ~0u) continue;
+        for (int c = 0; c < ncols; c++) {
+            int t = types[c];
+            int sz = (t == GB_T_SMALLINT) ? 2 : (t == GB_T_INTEGER ? 4 : 8);
+            const char *sp = (const char *)src.out[c] + (u64)r * sz;
+            char *dp = (char *)dst.out[c] + (u64)i * sz;
+            for (int b = 0; b < sz; b++) dp[b] = sp[b];
+            bool v = (src.valid[c][r >> 6] >> (r & 63)) & 1ull;
+            if (!v) clear_valid(dst.valid[c], i);
+        }
+    }
+}
+
+}  // namespace gb
+
+// ======================================================================= host
+using namespace gb;
+
+static int type_size(int t) {
+    switch (t) {
+    case GB_T_SMALLINT: return 2;
+    case GB_T_INTEGER: return 4;
+    case GB_T_BIGINT: return 8;
+    case GB_T_DOUBLE: return 8;
+    default: return 0;
+    }
+}
+
+static int type_bits(int t) { return type_size(t) * 8; }
+
+static u64 next_pow2(u64 x) {
+    u64 p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    gb_status ensure(size_t bytes) {
+        if (bytes <= n) return GB_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        size_t want = std::max(bytes, (size_t)256);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e != cudaSuccess) { p = nullptr; return cuda_fail(e, "cudaMalloc"); }
+        n = want;
+        return GB_OK;
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct HostBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    gb_status ensure(size_t bytes) {
+        if (bytes <= n) return GB_OK;
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+        size_t want = std::max(bytes, (size_t)256);
+        cudaError_t e = cudaMallocHost(&p, want);
+        if (e != cudaSuccess) { p = nullptr; return cuda_fail(e, "cudaMallocHost"); }
+        n = want;
+        return GB_OK;
+    }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct gb_agg {
+    // spec copy
+    std::vector<int32_t> col_types;
+    std::vector<int32_t> group_cols;
+    std::vector<gb_agg_desc> aggs;
+    std::vector<gb_filter> filters;
+    uint64_t nullable_mask = 0;
+    uint64_t est_groups = 0;
+
+    Plan plan{};
+    std::vector<EmitAgg> emit;
+    std::vector<int32_t> out_types;  // per output column
+
+    // HBM table
+    DevBuf table, table_old, spill, ctl_buf;
+    u64 cap = 0;
+    u32 spill_cap = 0, spill_threshold = 0;
+    u64 n_groups = 0;
+    // dense result
+    std::vector<DevBuf> out_cols, out_valid;
+    u64 out_cap = 0;
+    u64 n_rows_out = 0;
+    // topn
+    bool topn = false;
+    u32 topn_col = 0;
+    bool topn_asc = false;
+    u64 topn_limit = 0;
+    u64 row_limit = 0;
+    DevBuf topn_ids_a, topn_ids_b, topn_cnt;
+    std::vector<DevBuf> top_cols, top_valid;
+    DevBuf types_dev;
+    bool topn_applied = false;
+    // host result
+    std::vector<HostBuf> host_cols, host_valid;
+    std::vector<const void *> res_ptrs;
+    std::vector<const uint64_t *> res_valid;
+    std::vector<const int64_t *> res_offsets;
+    // host staging
+    std::vector<DevBuf> stage[2];
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr};
+    // tuning
+    int block = 512;
+    int ctas_per_sm = 2;
+    int smem_slots = 4096;
+    int smem_probe = 8;
+    int gmax_probe = 256;
+    bool precombine = true;
+    u32 tile_rows = 8192;
+    // profiling (CUDA events around each kernel, resolved at sync points)
+    bool profiling = false;
+    struct ProfEv { int stat; cudaEvent_t a, b; };
+    std::vector<ProfEv> prof_pending;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<gb_kernel_stat> stats;
+    // accounting / state
+    u64 launches = 0;
+    bool finalized = false;
+    bool has_result = false;
+    Ctl ctl_host{};
+};
+
+static TableRef table_ref(gb_agg *h) {
+    TableRef T;
+    T.slots = (u64 *)h->table.p;
+    T.cap = h->cap;
+    T.stride = h->plan.stride;
+    T.gmax_probe = h->gmax_probe;
+    T.ctl = (Ctl *)h->ctl_buf.p;
+    T.spill = (u64 *)h->spill.p;
+    T.spill_cap = h->spill_cap;
+    T.spill_threshold = h->spill_threshold;
+    return T;
+}
+
+static cudaEvent_t prof_event(gb_agg *h) {
+    if (!h->ev_pool.empty()) {
+        cudaEvent_t e = h->ev_pool.back();
+        h->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+static int prof_stat(gb_agg *h, const char *name) {
+    for (size_t i = 0; i < h->stats.size(); i++)
+        if (strncmp(h->stats[i].name, name, sizeof(h->stats[i].name)) == 0) return (int)i;
+    gb_kernel_stat s{};
+    strncpy(s.name, name, sizeof(s.name) - 1);
+    h->stats.push_back(s);
+    return (int)h->stats.size() - 1;
+}
+
+// Bracket one kernel launch with events on its stream (profiling only).
+struct ProfScope {
+    gb_agg *h;
+    cudaStream_t st;
+    int stat;
+    cudaEvent_t a = nullptr;
+    ProfScope(gb_agg *h_, const char *name, cudaStream_t st_) : h(h_), st(st_), stat(-1) {
+        if (!h->profiling) return;
+        stat = prof_stat(h, name);
+        a = prof_event(h);
+        cudaEventRecord(a, st);
+    }
+    ~ProfScope() {
+        if (!h->profiling) return;
+        cudaEvent_t b = prof_event(h);
+        cudaEventRecord(b, st);
+        h->prof_pending.push_back({stat, a, b});
+    }
+};
+
+// Resolve pending event pairs (the stream has been synchronised).
+static void prof_collect(gb_agg *h) {
+    for (auto &p : h->prof_pending) {
+        float ms = 0.f;
+        if (cudaEventSynchronize(p.b) == cudaSuccess && cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            h->stats[p.stat].launches++;
+            h->stats[p.stat].ms += ms;
+        }
+        h->ev_pool.push_back(p.a);
+        h->ev_pool.push_back(p.b);
+    }
+    h->prof_pending.clear();
+}
+
+static int grid_for(u64 work, int block, int max_ctas) {
+    u64 g = (work + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > (u64)max_ctas) g = max_ctas;
+    return (int)g;
+}
+
+static gb_status init_table(gb_agg *h, DevBuf &buf, u64 cap, cudaStream_t st) {
+    size_t bytes = (size_t)(cap + 2) * h->plan.stride * 8;
+    gb_status s = buf.ensure(bytes);
+    if (s) return s;
+    u64 words = (cap + 2) * (u64)h->plan.stride;
+    {
+        ProfScope ps(h, "k_table_init", st);
+        k_table_init<<<grid_for(words, 256, sm_count() * 8), 256, 0, st>>>((u64 *)buf.p, cap + 2, h->plan.stride,
+                                                                           h->plan);
+    }
+    h->launches++;
+    GB_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+static gb_status read_ctl(gb_agg *h, cudaStream_t st) {
+    GB_CUDA(cudaMemcpyAsync(&h->ctl_host, h->ctl_buf.p, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    return GB_OK;
+}
+
+static gb_status check_err(gb_agg *h) {
+    u32 e = h->ctl_host.err;
+    if (e & ERR_NULL_IN_WIDE_KEY) {
+        set_error("NULL in a two-column key whose packed width leaves no NULL bits (two 32-bit keys)");
+        return GB_ERR_UNSUPPORTED;
+    }
+    if (e & ERR_SPILL_OVERFLOW) {
+        set_error("spill buffer overflow (internal invariant violated)");
+        return GB_ERR_OOM;
+    }
+    if (e & ERR_OUT_OVERFLOW) {
+        set_error("result buffer overflow (internal invariant violated)");
+        return GB_ERR_CUDA;
+    }
+    return GB_OK;
+}
+
+// Grow the HBM table to new_cap (rehash) and merge `pending` spill records
+// (already at the front of the spill buffer).  Loops until nothing spills.
+static gb_status grow_and_merge(gb_agg *h, u64 new_cap, u32 pending, cudaStream_t st) {
+    Ctl *dctl = (Ctl *)h->ctl_buf.p;
+    const int recw = 1 + h->plan.words;
+    for (int round = 0; round < 40; round++) {
+        if (new_cap > h->cap) {
+            std::swap(h->table, h->table_old);
+            u64 old_cap = h->cap;
+            gb_status s = init_table(h, h->table, new_cap, st);
+            if (s) return s;
+            h->cap = new_cap;
+            // move pending records out of the way: they live at [0, pending)
+            // and rehash spills append after them.
+            GB_CUDA(cudaMemsetAsync(&dctl->n_groups, 0, sizeof(u32), st));
+            GB_CUDA(cudaMemcpyAsync(&dctl->spill_count, &pending, sizeof(u32), cudaMemcpyHostToDevice, st));
+            TableRef T = table_ref(h);
+            k_rehash<<<grid_for(old_cap + 2, 256, sm_count() * 8), 256, 0, st>>>(h->plan, (const u64 *)h->table_old.p,
+                                                                                 old_cap, h->plan.stride, T);
+            h->launches++;
+            GB_CUDA(cudaGetLastError());
+        }
+        if (pending == 0) {
+            gb_status s = read_ctl(h, st);
+            if (s) return s;
+            if ((s = check_err(h))) return s;
+            h->n_groups = h->ctl_host.n_groups;
+            u32 sp = h->ctl_host.spill_count;
+            if (sp == 0) return GB_OK;
+            pending = sp;  // rehash itself spilled: grow again
+            new_cap = h->cap * 2;
+            continue;
+        }
+        // merge [0, pending) — re-spills land at [pending, ...)
+        TableRef T = table_ref(h);
+        GB_CUDA(cudaMemcpyAsync(&dctl->spill_count, &pending, sizeof(u32), cudaMemcpyHostToDevice, st));
+        k_merge_records<<<grid_for(pending, 256, sm_count() * 8), 256, 0, st>>>(h->plan, (const u64 *)h->spill.p,
+                                                                              pending, T);
+        h->launches++;
+        GB_CUDA(cudaGetLastError());
+        gb_status s = read_ctl(h, st);
+        if (s) return s;
+        if ((s = check_err(h))) return s;
+        u32 total = h->ctl_host.spill_count;
+        u32 again = total - pending;
+        h->n_groups = h->ctl_host.n_groups;
+        if (again == 0) {
+            GB_CUDA(cudaMemsetAsync(&dctl->spill_count, 0, sizeof(u32), st));
+            return GB_OK;
+        }
+        // compact the re-spilled tail to the front
+        GB_CUDA(cudaMemcpyAsync(h->spill.p, (u64 *)h->spill.p + (size_t)pending * recw, (size_t)again * recw * 8,
+                                cudaMemcpyDeviceToDevice, st));
+        pending = again;
+        new_cap = h->cap * 2;
+    }
+    set_error("hash table growth did not converge");
+    return GB_ERR_OOM;
+}
+
+static gb_status ensure_capacity(gb_agg *h, cudaStream_t st) {
+    // keep the load factor <= 0.5 for the next batch
+    if (h->n_groups * 2 > h->cap) {
+        u64 nc = h->cap;
+        while (h->n_groups * 2 > nc) nc *= 2;
+        return grow_and_merge(h, nc, 0, st);
+    }
+    return GB_OK;
+}
+
+static gb_status run_ingest(gb_agg *h, u64 n_rows, cudaStream_t st) {
+    if (n_rows == 0) return GB_OK;
+    Ctl *dctl = (Ctl *)h->ctl_buf.p;
+    const int words = h->plan.words;
+    u32 tile_rows = h->tile_rows;
+    const int max_ctas = sm_count() * h->ctas_per_sm;
+    // small inputs: shrink tiles so every CTA gets work
+    u64 want_tiles = (u64)max_ctas * 4;
+    if (n_rows / tile_rows < want_tiles) {
+        u64 tr = (n_rows + want_tiles - 1) / want_tiles;
+        tr = ((tr + 511) / 512) * 512;
+        tile_rows = (u32)std::max<u64>(1024, std::min<u64>(tr, h->tile_rows));
+    }
+    const u64 n_tiles_total = (n_rows + tile_rows - 1) / tile_rows;
+    int grid = (int)std::min<u64>((u64)max_ctas, n_tiles_total);
+    int S = h->smem_slots;
+    size_t smem = (size_t)S * 8 * (1 + words);
+    // spill capacity: threshold + what in-flight tiles and the final flush can add
+    u64 margin = (u64)grid * ((u64)tile_rows + (u64)S) + 1024;
+    u64 need_cap = (1u << 20) + margin;
+    if (h->spill_cap < need_cap) {
+        gb_status s = h->spill.ensure((size_t)need_cap * (1 + words) * 8);
+        if (s) return s;
+        h->spill_cap = (u32)need_cap;
+    }
+    h->spill_threshold = (u32)(h->spill_cap - margin);
+    static bool attr_set[2] = {false, false};
+    if (!attr_set[0]) {
+        cudaFuncSetAttribute(k_ingest<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_ingest<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        attr_set[0] = attr_set[1] = true;
+    }
+    u64 first = 0;
+    while (first < n_tiles_total) {
+        GB_CUDA(cudaMemsetAsync(&dctl->spill_count, 0, 4 * 4, st));  // spill_count, tile_counter, stop, err
+        IngestArgs A;
+        A.n_rows = n_rows;
+        A.tile_rows = tile_rows;
+        A.first_tile = (u32)first;
+        A.n_tiles = (u32)(n_tiles_total - first);
+        A.smem_slots = S;
+        A.smem_probe = h->smem_probe;
+        A.pad = 0;
+        TableRef T = table_ref(h);
+        int g = (int)std::min<u64>((u64)grid, n_tiles_total - first);
+        {
+            ProfScope ps(h, "k_ingest", st);
+            if (h->precombine) k_ingest<true><<<g, h->block, smem, st>>>(h->plan, T, A);
+            else k_ingest<false><<<g, h->block, smem, st>>>(h->plan, T, A);
+        }
+        h->launches++;
+        GB_CUDA(cudaGetLastError());
+        gb_status s = read_ctl(h, st);
+        if (s) return s;
+        if ((s = check_err(h))) return s;
+        h->n_groups = h->ctl_host.n_groups;
+        u64 claimed = std::min<u64>(h->ctl_host.tile_counter, n_tiles_total - first);
+        first += claimed;
+        u32 sp = h->ctl_host.spill_count;
+        if (sp > 0) {
+            u64 nc = h->cap * 2;
+            while ((h->n_groups + sp) * 2 > nc) nc *= 2;
+            s = grow_and_merge(h, nc, sp, st);
+            if (s) return s;
+        }
+        if ((s = ensure_capacity(h, st))) return s;
+    }
+    return GB_OK;
+}
+
+// ---------------------------------------------------------------- compile
+static gb_status compile_plan(gb_agg *h) {
+    Plan &P = h->plan;
+    memset(&P, 0, sizeof P);
+    const int nc = (int)h->col_types.size();
+    if (nc <= 0 || nc > GB_MAX_COLS) {
+        set_error("n_cols must be in [1, %d]", GB_MAX_COLS);
+        return GB_ERR_INVALID;
+    }
+    for (int c = 0; c < nc; c++) {
+        int t = h->col_types[c];
+        if (t < GB_T_SMALLINT || t > GB_T_VARCHAR) {
+            set_error("column %d: unknown type %d", c, t);
+            return GB_ERR_INVALID;
+        }
+        P.cols[c].type = t;
+    }
+    P.n_cols = nc;
+    const int ng = (int)h->group_cols.size();
+    if (ng < 1 || ng > 2) {
+        set_error("GROUP BY needs 1 or 2 key columns on the GPU path (got %d)", ng);
+        return ng < 1 ? GB_ERR_INVALID : GB_ERR_UNSUPPORTED;
+    }
+    for (int i = 0; i < ng; i++) {
+        int c = h->group_cols[i];
+        if (c < 0 || c >= nc) {
+            set_error("group column %d out of range", c);
+            return GB_ERR_INVALID;
+        }
+        int t = h->col_types[c];
+        if (t == GB_T_DOUBLE) {
+            set_error("DOUBLE group keys are not supported on the GPU path");
+            return GB_ERR_UNSUPPORTED;
+        }
+        P.key_col[i] = c;
+        P.key_type[i] = t;
+    }
+    P.n_keys = ng;
+    if (ng == 1) {
+        P.key_mode = (h->col_types[P.key_col[0]] == GB_T_VARCHAR) ? KEY_STRING : KEY_SINGLE;
+        if (P.key_mode == KEY_STRING) {
+            set_error("VARCHAR keys go through the batched/string path (gb_batch); not the single-query ingest");
+            return GB_ERR_UNSUPPORTED;
+        }
+    } else {
+        if (P.key_type[0] == GB_T_VARCHAR || P.key_type[1] == GB_T_VARCHAR) {
+            set_error("VARCHAR in a two-column key is not supported on the GPU path");
+            return GB_ERR_UNSUPPORTED;
+        }
+        int ba = type_bits(P.key_type[0]), bb = type_bits(P.key_type[1]);
+        if (ba + bb + 2 <= 64) {
+            P.key_mode = KEY_PACKED;
+            P.key_bits_a = ba;
+            P.key_bits_b = bb;
+        } else if (ba + bb == 64) {
+            P.key_mode = KEY_WIDE;
+        } else {
+            set_error("two-column key wider than 64 bits (BIGINT in a pair) is not supported on the GPU path");
+            return GB_ERR_UNSUPPORTED;
+        }
+    }
+    for (size_t i = 0; i < h->filters.size(); i++) {
+        const gb_filter &f = h->filters[i];
+        if (f.col < 0 || f.col >= nc || f.op < 0 || f.op > 5 || h->col_types[f.col] == GB_T_VARCHAR) {
+            set_error("filter %zu invalid (column, operator or VARCHAR predicate)", i);
+            return GB_ERR_INVALID;
+        }
+        if (i >= GB_MAX_FILTERS) {
+            set_error("too many filters (max %d)", GB_MAX_FILTERS);
+            return GB_ERR_UNSUPPORTED;
+        }
+        P.filters[i].col = f.col;
+        P.filters[i].op = f.op;
+        P.filters[i].ic = f.i_const;
+        P.filters[i].dc = f.d_const;
+    }
+    P.n_filters = (int)h->filters.size();
+
+    // state words: 0 = row count; ops deduplicated per (kind, column)
+    int words = 1;
+    P.word_init[0] = 0;
+    auto find_or_add_op = [&](int kind, int col) -> int {
+        for (int i = 0; i < P.n_ops; i++)
+            if (P.ops[i].kind == kind && P.ops[i].col == col) return P.ops[i].word;
+        if (P.n_ops >= GB_MAX_OPS || words >= GB_MAX_WORDS) return -1;
+        Op &o = P.ops[P.n_ops++];
+        o.kind = (uint8_t)kind;
+        o.col = (uint8_t)col;
+        o.word = (uint8_t)words;
+        u64 init = 0;
+        if (kind == OP_MIN_I || kind == OP_MIN_F) init = 0x7fffffffffffffffull;
+        if (kind == OP_MAX_I || kind == OP_MAX_F) init = 0x8000000000000000ull;
+        P.word_init[words] = init;
+        return words++;
+    };
+    h->emit.clear();
+    h->out_types.clear();
+    for (int i = 0; i < ng; i++) h->out_types.push_back(P.key_type[i]);
+    if (h->aggs.empty() || h->aggs.size() > GB_MAX_AGGS) {
+        set_error("need 1..%d aggregates", GB_MAX_AGGS);
+        return GB_ERR_INVALID;
+    }
+    for (size_t a = 0; a < h->aggs.size(); a++) {
+        const gb_agg_desc &d = h->aggs[a];
+        EmitAgg e{};
+        e.kind = d.kind;
+        e.val_word = -1;
+        e.cnt_word = 0;
+        e.in_type = -1;
+        if (d.kind == GB_AGG_COUNT_STAR) {
+            e.out_type = GB_T_BIGINT;
+        } else {
+            if (d.col < 0 || d.col >= nc || d.kind < 0 || d.kind > GB_AGG_MAX) {
+                set_error("aggregate %zu: invalid kind or column", a);
+                return GB_ERR_INVALID;
+            }
+            int t = h->col_types[d.col];
+            e.in_type = t;
+            if (t == GB_T_VARCHAR) {
+                set_error("aggregate %zu over VARCHAR is not supported on the GPU path", a);
+                return GB_ERR_UNSUPPORTED;
+            }
+            bool nullable = (h->nullable_mask >> d.col) & 1ull;
+            int cntw = 0;
+            if (nullable) cntw = find_or_add_op(OP_CNT_NN, d.col);
+            if (cntw < 0) goto too_many;
+            e.cnt_word = cntw;
+            bool isf = (t == GB_T_DOUBLE);
+            switch (d.kind) {
+            case GB_AGG_COUNT: e.out_type = GB_T_BIGINT; break;
+            case GB_AGG_SUM:
+                e.out_type = isf ? GB_T_DOUBLE : GB_T_BIGINT;
+                e.val_word = find_or_add_op(isf ? OP_ADD_F : OP_ADD_I, d.col);
+                break;
+            case GB_AGG_AVG:
+                e.out_type = GB_T_DOUBLE;
+                e.val_word = find_or_add_op(isf ? OP_ADD_F : OP_ADD_I, d.col);
+                break;
+            case GB_AGG_MIN:
+                e.out_type = t;
+                e.val_word = find_or_add_op(isf ? OP_MIN_F : OP_MIN_I, d.col);
+                break;
+            case GB_AGG_MAX:
+                e.out_type = t;
+                e.val_word = find_or_add_op(isf ? OP_MAX_F : OP_MAX_I, d.col);
+                break;
+            }
+            if (d.kind != GB_AGG_COUNT && e.val_word < 0) goto too_many;
+        }
+        h->emit.push_back(e);
+        h->out_types.push_back(e.out_type);
+    }
+    P.words = words;
+    {
+        int need = words + 1;
+        int stride = need <= 4 ? (int)next_pow2(need) : ((need + 3) / 4) * 4;
+        P.stride = stride;
+    }
+    return GB_OK;
+too_many:
+    set_error("too many distinct aggregate states (max %d)", GB_MAX_OPS);
+    return GB_ERR_UNSUPPORTED;
+}
+
+static gb_status alloc_outputs(gb_agg *h, u64 rows) {
+    size_t nout = h->out_types.size();
+    h->out_cols.resize(nout);
+    h->out_valid.resize(nout);
+    for (size_t c = 0; c < nout; c++) {
+        gb_status s = h->out_cols[c].ensure((size_t)rows * type_size(h->out_types[c]) + 64);
+        if (s) return s;
+        s = h->out_valid[c].ensure(((size_t)rows + 63) / 64 * 8 + 64);
+        if (s) return s;
+    }
+    h->out_cap = rows;
+    return GB_OK;
+}
+
+static void fill_emit(gb_agg *h, EmitArgs &E, std::vector<DevBuf> &cols, std::vector<DevBuf> &valid, u64 cap) {
+    memset(&E, 0, sizeof E);
+    E.n_aggs = (int)h->emit.size();
+    E.n_keys = h->plan.n_keys;
+    for (int a = 0; a < E.n_aggs; a++) E.aggs[a] = h->emit[a];
+    for (size_t c = 0; c < cols.size(); c++) {
+        E.out[c] = cols[c].p;
+        E.valid[c] = (uint64_t *)valid[c].p;
+    }
+    E.out_cap = cap;
+}
+
+// ------------------------------------------------------------ TopN host
+static gb_status run_topn(gb_agg *h, cudaStream_t st) {
+    const u64 n = h->n_rows_out;
+    const int K = (int)h->topn_limit;
+    const size_t nout = h->out_types.size();
+    TopnArgs A{};
+    A.order_col = h->out_cols[h->topn_col].p;
+    A.order_type = h->out_types[h->topn_col];
+    A.order_valid = (const uint64_t *)h->out_valid[h->topn_col].p;
+    A.ascending = h->topn_asc ? 1 : 0;
+    A.n_keys = h->plan.n_keys;
+    A.key0 = h->out_cols[0].p;
+    A.key_type0 = h->out_types[0];
+    if (A.n_keys > 1) {
+        A.key1 = h->out_cols[1].p;
+        A.key_type1 = h->out_types[1];
+    }
+    A.K = K;
+    int sortn = (int)next_pow2((u64)2 * K);
+    if (sortn < 64) sortn = 64;
+    size_t smem = (size_t)sortn * (8 + 8 + 4);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_topn, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024);
+        attr = true;
+    }
+    int grid = (int)std::min<u64>((u64)sm_count() * 2, std::max<u64>(1, n / 4096));
+    gb_status s;
+    if ((s = h->topn_ids_a.ensure((size_t)grid * K * 4))) return s;
+    if ((s = h->topn_ids_b.ensure((size_t)K * 4 + 64))) return s;
+    if ((s = h->topn_cnt.ensure((size_t)grid * 4 + 64))) return s;
+    GB_CUDA(cudaMemsetAsync(h->topn_ids_a.p, 0xff, (size_t)grid * K * 4, st));
+    {
+        ProfScope ps(h, "k_topn", st);
+        k_topn<<<grid, 512, smem, st>>>(A, nullptr, n, (u32 *)h->topn_ids_a.p, (u32 *)h->topn_cnt.p, sortn);
+    }
+    h->launches++;
+    GB_CUDA(cudaGetLastError());
+    // second pass over the grid*K candidate ids (padding ids are skipped)
+    k_topn<<<1, 512, smem, st>>>(A, (const u32 *)h->topn_ids_a.p, (u64)grid * K, (u32 *)h->topn_ids_b.p,
+                                 (u32 *)h->topn_cnt.p, sortn);
+    h->launches++;
+    GB_CUDA(cudaGetLastError());
+    u32 kf = 0;
+    GB_CUDA(cudaMemcpyAsync(&kf, h->topn_cnt.p, 4, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    // gather rows into top_cols
+    h->top_cols.resize(nout);
+    h->top_valid.resize(nout);
+    for (size_t c = 0; c < nout; c++) {
+        if ((s = h->top_cols[c].ensure((size_t)K * 8 + 64))) return s;
+        if ((s = h->top_valid[c].ensure(((size_t)K + 63) / 64 * 8 + 64))) return s;
+        GB_CUDA(cudaMemsetAsync(h->top_valid[c].p, 0xff, ((size_t)K + 63) / 64 * 8 + 8, st));
+    }
+    if ((s = h->types_dev.ensure(nout * 4))) return s;
+    GB_CUDA(cudaMemcpyAsync(h->types_dev.p, h->out_types.data(), nout * 4, cudaMemcpyHostToDevice, st));
+    EmitArgs src, dst;
+    fill_emit(h, src, h->out_cols, h->out_valid, h->out_cap);
+    fill_emit(h, dst, h->top_cols, h->top_valid, K);
+    if (kf > 0) {
+        k_gather_rows<<<1, 256, 0, st>>>((const u32 *)h->topn_ids_b.p, kf, (int)nout, src, dst,
+                                         (const int32_t *)h->types_dev.p);
+        h->launches++;
+        GB_CUDA(cudaGetLastError());
+    }
+    h->n_rows_out = kf;
+    h->topn_applied = true;
+    return GB_OK;
+}
+
+// =================================================================== C ABI
+extern "C" {
+
+const char *gb_last_error(void) { return g_err.c_str(); }
+int gb_abi_version(void) { return GB_ABI_VERSION; }
+
+gb_status gb_agg_create(const gb_agg_spec *spec, gb_agg **out) {
+    if (!spec || !out) {
+        set_error("null spec/out");
+        return GB_ERR_INVALID;
+    }
+    *out = nullptr;
+    if (spec->n_cols == 0 || !spec->col_types || spec->n_groups == 0 || !spec->group_cols || spec->n_aggs == 0 ||
+        !spec->aggs || (spec->n_filters && !spec->filters)) {
+        set_error("incomplete spec");
+        return GB_ERR_INVALID;
+    }
+    gb_agg *h = new gb_agg();
+    h->col_types.assign(spec->col_types, spec->col_types + spec->n_cols);
+    h->group_cols.assign(spec->group_cols, spec->group_cols + spec->n_groups);
+    h->aggs.assign(spec->aggs, spec->aggs + spec->n_aggs);
+    if (spec->n_filters) h->filters.assign(spec->filters, spec->filters + spec->n_filters);
+    h->nullable_mask = spec->nullable_mask;
+    h->est_groups = spec->est_groups;
+    gb_status s = compile_plan(h);
+    if (s) {
+        delete h;
+        return s;
+    }
+    gb_apply_tuning(h);
+    u64 est = h->est_groups ? h->est_groups : (1u << 15);
+    h->cap = std::max<u64>(1024, next_pow2(est * 2));
+    if ((s = h->ctl_buf.ensure(sizeof(Ctl)))) {
+        delete h;
+        return s;
+    }
+    cudaError_t e = cudaMemset(h->ctl_buf.p, 0, sizeof(Ctl));
+    if (e != cudaSuccess) {
+        delete h;
+        return cuda_fail(e, "cudaMemset");
+    }
+    if ((s = init_table(h, h->table, h->cap, 0))) {
+        delete h;
+        return s;
+    }
+    *out = h;
+    return GB_OK;
+}
+
+gb_status gb_agg_set_topn(gb_agg *h, uint32_t col_idx, int32_t ascending, uint64_t limit) {
+    if (!h) return GB_ERR_INVALID;
+    if (col_idx >= h->out_types.size()) {
+        set_error("TopN column %u out of range", col_idx);
+        return GB_ERR_INVALID;
+    }
+    h->topn = true;
+    h->topn_col = col_idx;
+    h->topn_asc = ascending != 0;
+    h->topn_limit = limit;
+    return GB_OK;
+}
+
+gb_status gb_agg_set_row_limit(gb_agg *h, uint64_t limit) {
+    if (!h) return GB_ERR_INVALID;
+    h->row_limit = limit;
+    return GB_OK;
+}
+
+gb_status gb_agg_ingest(gb_agg *h, const gb_col *cols, uint64_t nrows, int32_t mem, void *stream) {
+    if (!h || (!cols && nrows)) {
+        set_error("null handle/columns");
+        return GB_ERR_INVALID;
+    }
+    if (h->finalized) {
+        set_error("ingest after finalize (call gb_agg_reset first)");
+        return GB_ERR_STATE;
+    }
+    if (nrows == 0) return GB_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int nc = h->plan.n_cols;
+    for (int c = 0; c < nc; c++) {
+        if (!cols[c].data) {
+            set_error("column %d has no data pointer", c);
+            return GB_ERR_INVALID;
+        }
+        if (cols[c].validity && !((h->nullable_mask >> c) & 1ull)) {
+            set_error("column %d carries a validity mask but the spec declares it NOT NULL", c);
+            return GB_ERR_INVALID;
+        }
+    }
+    if (mem == GB_MEM_DEVICE) {
+        for (int c = 0; c < nc; c++) {
+            h->plan.cols[c].data = cols[c].data;
+            h->plan.cols[c].valid = cols[c].validity;
+            h->plan.cols[c].offsets = cols[c].offsets;
+        }
+        gb_status s = run_ingest(h, nrows, st);
+        prof_collect(h);
+        return s;
+    }
+    if (mem != GB_MEM_HOST) {
+        set_error("mem must be GB_MEM_HOST or GB_MEM_DEVICE");
+        return GB_ERR_INVALID;
+    }
+    // Host vectors: double-buffered chunks, copy of chunk i+1 overlaps the
+    // aggregation of chunk i.
+    if (!h->copy_stream) {
+        GB_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; b++) {
+            GB_CUDA(cudaEventCreateWithFlags(&h->ev_copied[b], cudaEventDisableTiming));
+            GB_CUDA(cudaEventCreateWithFlags(&h->ev_done[b], cudaEventDisableTiming));
+        }
+    }
+    const u64 chunk = std::min<u64>(nrows, (u64)16 << 20);
+    for (int b = 0; b < 2; b++) {
+        h->stage[b].resize(2 * nc);
+        for (int c = 0; c < nc; c++) {
+            gb_status s = h->stage[b][c].ensure((size_t)chunk * type_size(h->col_types[c]) + 64);
+            if (s) return s;
+            if (cols[c].validity) {
+                s = h->stage[b][nc + c].ensure((size_t)(chunk / 64 + 2) * 8);
+                if (s) return s;
+            }
+        }
+    }
+    const u64 nchunks = (nrows + chunk - 1) / chunk;
+    auto issue_copy = [&](u64 i) -> gb_status {
+        int b = (int)(i & 1);
+        u64 r0 = i * chunk, r1 = std::min<u64>(nrows, r0 + chunk);
+        if (i >= 2) GB_CUDA(cudaStreamWaitEvent(h->copy_stream, h->ev_done[b], 0));
+        for (int c = 0; c < nc; c++) {
+            int ts = type_size(h->col_types[c]);
+            GB_CUDA(cudaMemcpyAsync(h->stage[b][c].p, (const char *)cols[c].data + r0 * ts, (r1 - r0) * ts,
+                                    cudaMemcpyHostToDevice, h->copy_stream));
+            if (cols[c].validity) {
+                // chunk boundaries are multiples of 64 rows (chunk = 16Mi)
+                GB_CUDA(cudaMemcpyAsync(h->stage[b][nc + c].p, cols[c].validity + r0 / 64, ((r1 - r0) + 63) / 64 * 8,
+                                        cudaMemcpyHostToDevice, h->copy_stream));
+            }
+        }
+        GB_CUDA(cudaEventRecord(h->ev_copied[b], h->copy_stream));
+        return GB_OK;
+    };
+    gb_status s = issue_copy(0);
+    if (s) return s;
+    for (u64 i = 0; i < nchunks; i++) {
+        int b = (int)(i & 1);
+        if (i + 1 < nchunks && (s = issue_copy(i + 1))) return s;
+        GB_CUDA(cudaStreamWaitEvent(st, h->ev_copied[b], 0));
+        u64 r0 = i * chunk, r1 = std::min<u64>(nrows, r0 + chunk);
+        for (int c = 0; c < nc; c++) {
+            h->plan.cols[c].data = h->stage[b][c].p;
+            h->plan.cols[c].valid = cols[c].validity ? (const uint64_t *)h->stage[b][nc + c].p : nullptr;
+            h->plan.cols[c].offsets = nullptr;
+        }
+        if ((s = run_ingest(h, r1 - r0, st))) return s;
+        GB_CUDA(cudaEventRecord(h->ev_done[b], st));
+    }
+    prof_collect(h);
+    return GB_OK;
+}
+
+gb_status gb_agg_finalize(gb_agg *h, void *stream) {
+    if (!h) return GB_ERR_INVALID;
+    if (h->finalized) return GB_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    gb_status s;
+    if ((s = alloc_outputs(h, h->cap + 2))) return s;
+    for (size_t c = 0; c < h->out_valid.size(); c++)
+        GB_CUDA(cudaMemsetAsync(h->out_valid[c].p, 0xff, h->out_valid[c].n, st));
+    Ctl *dctl = (Ctl *)h->ctl_buf.p;
+    GB_CUDA(cudaMemsetAsync(&dctl->out_count, 0, 4, st));
+    GB_CUDA(cudaMemsetAsync(&dctl->err, 0, 4, st));
+    EmitArgs E;
+    fill_emit(h, E, h->out_cols, h->out_valid, h->out_cap);
+    {
+        ProfScope ps(h, "k_compact", st);
+        k_compact<<<grid_for(h->cap + 2, 256, sm_count() * 8), 256, 0, st>>>(h->plan, (const u64 *)h->table.p,
+                                                                             h->cap, h->plan.stride, E, dctl);
+    }
+    h->launches++;
+    GB_CUDA(cudaGetLastError());
+    if ((s = read_ctl(h, st))) return s;
+    if ((s = check_err(h))) return s;
+    h->n_rows_out = h->ctl_host.out_count;
+    h->topn_applied = false;
+    if (h->topn && h->topn_limit > 0 && h->topn_limit <= 1024 && h->n_rows_out > 0) {
+        if ((s = run_topn(h, st))) return s;
+    }
+    h->finalized = true;
+    h->has_result = false;
+    prof_collect(h);
+    return GB_OK;
+}
+
+static void fill_result_view(gb_agg *h, gb_result *out, bool host) {
+    size_t nout = h->out_types.size();
+    h->res_ptrs.resize(nout);
+    h->res_valid.resize(nout);
+    h->res_offsets.assign(nout, nullptr);
+    for (size_t c = 0; c < nout; c++) {
+        if (host) {
+            h->res_ptrs[c] = h->host_cols[c].p;
+            h->res_valid[c] = (const uint64_t *)h->host_valid[c].p;
+        } else {
+            auto &cols = h->topn_applied ? h->top_cols : h->out_cols;
+            auto &val = h->topn_applied ? h->top_valid : h->out_valid;
+            h->res_ptrs[c] = cols[c].p;
+            h->res_valid[c] = (const uint64_t *)val[c].p;
+        }
+    }
+    out->n_rows = h->n_rows_out;
+    out->n_cols = (uint32_t)nout;
+    out->types = h->out_types.data();
+    out->data = h->res_ptrs.data();
+    out->offsets = h->res_offsets.data();
+    out->validity = h->res_valid.data();
+}
+
+gb_status gb_agg_result(gb_agg *h, gb_result *out) {
+    if (!h || !out) return GB_ERR_INVALID;
+    if (!h->finalized) {
+        set_error("result before finalize");
+        return GB_ERR_STATE;
+    }
+    if (!h->has_result) {
+        size_t nout = h->out_types.size();
+        h->host_cols.resize(nout);
+        h->host_valid.resize(nout);
+        u64 n = h->n_rows_out;
+        if (h->row_limit && n > h->row_limit) n = h->row_limit;
+        auto &cols = h->topn_applied ? h->top_cols : h->out_cols;
+        auto &val = h->topn_applied ? h->top_valid : h->out_valid;
+        for (size_t c = 0; c < nout; c++) {
+            size_t bytes = (size_t)n * type_size(h->out_types[c]);
+            size_t vbytes = ((size_t)n + 63) / 64 * 8;
+            gb_status s;
+            if ((s = h->host_cols[c].ensure(bytes + 8))) return s;
+            if ((s = h->host_valid[c].ensure(vbytes + 8))) return s;
+            if (bytes) GB_CUDA(cudaMemcpyAsync(h->host_cols[c].p, cols[c].p, bytes, cudaMemcpyDeviceToHost, 0));
+            if (vbytes) GB_CUDA(cudaMemcpyAsync(h->host_valid[c].p, val[c].p, vbytes, cudaMemcpyDeviceToHost, 0));
+        }
+        GB_CUDA(cudaStreamSynchronize(0));
+        h->n_rows_out = n;
+        h->has_result = true;
+    }
+    fill_result_view(h, out, true);
+    return GB_OK;
+}
+
+gb_status gb_agg_result_device(gb_agg *h, gb_result *out) {
+    if (!h || !out) return GB_ERR_INVALID;
+    if (!h->finalized) {
+        set_error("result before finalize");
+        return GB_ERR_STATE;
+    }
+    fill_result_view(h, out, false);
+    return GB_OK;
+}
+
+gb_status gb_agg_reset(gb_agg *h) {
+    if (!h) return GB_ERR_INVALID;
+    gb_status s = init_table(h, h->table, h->cap, 0);
+    if (s) return s;
+    GB_CUDA(cudaMemset(h->ctl_buf.p, 0, sizeof(Ctl)));
+    h->n_groups = 0;
+    h->finalized = false;
+    h->has_result = false;
+    h->topn_applied = false;
+    h->n_rows_out = 0;
+    h->launches = 0;
+    return GB_OK;
+}
+
+void gb_agg_destroy(gb_agg *h) {
+    if (!h) return;
+    cudaDeviceSynchronize();
+    h->table.release();
+    h->table_old.release();
+    h->spill.release();
+    h->ctl_buf.release();
+    for (auto &b : h->out_cols) b.release();
+    for (auto &b : h->out_valid) b.release();
+    for (auto &b : h->top_cols) b.release();
+    for (auto &b : h->top_valid) b.release();
+    h->topn_ids_a.release();
+    h->topn_ids_b.release();
+    h->topn_cnt.release();
+    h->types_dev.release();
+    for (auto &b : h->host_cols) b.release();
+    for (auto &b : h->host_valid) b.release();
+    for (int i = 0; i < 2; i++) {
+        for (auto &b : h->stage[i]) b.release();
+        if (h->ev_copied[i]) cudaEventDestroy(h->ev_copied[i]);
+        if (h->ev_done[i]) cudaEventDestroy(h->ev_done[i]);
+    }
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+    for (auto &p : h->prof_pending) {
+        cudaEventDestroy(p.a);
+        cudaEventDestroy(p.b);
+    }
+    for (auto e : h->ev_pool) cudaEventDestroy(e);
+    delete h;
+}
+
+uint64_t gb_agg_kernel_launches(const gb_agg *h) { return h ? h->launches : 0; }
+
+gb_status gb_agg_set_profiling(gb_agg *h, int32_t on) {
+    if (!h) return GB_ERR_INVALID;
+    h->profiling = on != 0;
+    if (!on) h->stats.clear();
+    return GB_OK;
+}
+
+uint32_t gb_agg_profile(const gb_agg *h, gb_kernel_stat *out, uint32_t max) {
+    if (!h) return 0;
+    uint32_t n = (uint32_t)std::min<size_t>(max, h->stats.size());
+    for (uint32_t i = 0; i < n; i++) out[i] = h->stats[i];
+    return (uint32_t)h->stats.size();
+}
+
+gb_status gb_engine_hash_aggregate(const int32_t *keys, const int32_t *values, uint64_t n, int32_t *out_keys,
+                                   int64_t *out_sums, int64_t *out_counts, uint64_t cap, uint64_t *n_out) {
+    if ((!keys || !values) && n) return GB_ERR_INVALID;
+    int32_t types[2] = {GB_T_INTEGER, GB_T_INTEGER};
+    int32_t gcols[1] = {0};
+    gb_agg_desc aggs[2] = {{GB_AGG_SUM, 1}, {GB_AGG_COUNT_STAR, -1}};
+    gb_agg_spec spec{};
+    spec.n_cols = 2;
+    spec.col_types = types;
+    spec.n_groups = 1;
+    spec.group_cols = gcols;
+    spec.n_aggs = 2;
+    spec.aggs = aggs;
+    gb_agg *h = nullptr;
+    gb_status s = gb_agg_create(&spec, &h);
+    if (s) return s;
+    gb_col cols[2] = {{keys, nullptr, nullptr}, {values, nullptr, nullptr}};
+    if (!(s = gb_agg_ingest(h, cols, n, GB_MEM_HOST, nullptr)) && !(s = gb_agg_finalize(h, nullptr))) {
+        gb_result r;
+        if (!(s = gb_agg_result(h, &r))) {
+            if (r.n_rows > cap) {
+                set_error("%llu groups exceed output capacity %llu", (unsigned long long)r.n_rows,
+                          (unsigned long long)cap);
+                s = GB_ERR_INVALID;
+            } else {
+                memcpy(out_keys, r.data[0], r.n_rows * 4);
+                memcpy(out_sums, r.data[1], r.n_rows * 8);
+                memcpy(out_counts, r.data[2], r.n_rows * 8);
+                *n_out = r.n_rows;
+            }
+        }
+    }
+    gb_agg_destroy(h);
+    return s;
+}
+
+gb_status gb_host_alloc(void **ptr, size_t bytes) {
+    if (!ptr) return GB_ERR_INVALID;
+    GB_CUDA(cudaMallocHost(ptr, bytes ? bytes : 1));
+    return GB_OK;
+}
+gb_status gb_host_free(void *ptr) {
+    GB_CUDA(cudaFreeHost(ptr));
+    return GB_OK;
+}
+gb_status gb_device_alloc(void **ptr, size_t bytes) {
+    if (!ptr) return GB_ERR_INVALID;
+    GB_CUDA(cudaMalloc(ptr, bytes ? bytes : 1));
+    return GB_OK;
+}
+gb_status gb_device_free(void *ptr) {
+    GB_CUDA(cudaFree(ptr));
+    return GB_OK;
+}
+gb_status gb_memcpy(void *dst, const void *src, size_t bytes, int32_t kind) {
+    cudaMemcpyKind k = kind == 0 ? cudaMemcpyHostToDevice : (kind == 1 ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice);
+    GB_CUDA(cudaMemcpy(dst, src, bytes, k));
+    return GB_OK;
+}
+gb_status gb_device_sync(void) {
+    GB_CUDA(cudaDeviceSynchronize());
+    return GB_OK;
+}
+
+}  // extern "C"
+
+// tuning hook (defaults here; the autotuner overrides per shape)
+void gb_apply_tuning(gb_agg *h) {
+    const int words = h->plan.words;
+    // shared table: 2x the estimated groups, at most ~96 KB so two CTAs fit
+    u64 est = h->est_groups ? h->est_groups : 4096;
+    u64 S = next_pow2(est * 2);
+    u64 max_s = (96 * 1024) / (8 * (1 + words));
+    u64 max_p2 = 1;
+    while (max_p2 * 2 <= max_s) max_p2 *= 2;
+    if (S > max_p2) S = max_p2;
+    if (S < 256) S = 256;
+    h->smem_slots = (int)S;
+    h->ctas_per_sm = 2;
+    h->block = 512;
+}

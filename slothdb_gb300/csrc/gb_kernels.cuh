@@ -1,0 +1,272 @@
+// gb_kernels.cuh — the hash-aggregation device code shared by the single
+// query path (gb_agg.cu) and the batched persistent path (gb_batch.cu).
+//
+// Row pipeline per warp (32 consecutive rows, coalesced column loads):
+//   filter predicates → packed 64-bit group key → __match_any_sync groups the
+//   lanes holding the same key → segmented shuffle reduction combines their
+//   partial states into the lowest lane (the "leader") → the leader folds
+//   the combined partial into the CTA's shared-memory open-addressing table
+//   with shared-memory atomics → if the shared table has no room the partial
+//   goes to the HBM table with global atomics → if the HBM table is too full
+//   (probe bound) the partial is spilled as a record and merged after the
+//   host grows the table.  At CTA exit the shared table is flushed into the
+//   HBM table.
+//
+// This restates the reference's per-row probe + AggState update
+// (src/execution/physical_planner.cpp:7933-8021 in-memory loop, 7698-7820
+// fused Parquet loop) with a three-level GPU memory hierarchy in place of
+// the per-thread ankerl maps and their shard merge (7871-7908).
+#pragma once
+
+#include "gb_internal.cuh"
+
+namespace gb {
+
+struct Ctl {
+    u32 n_groups;      // groups inserted in the HBM table
+    u32 spill_count;   // spill records written
+    u32 tile_counter;  // tiles claimed by persistent CTAs
+    u32 stop;          // set when the spill buffer nears its threshold
+    u32 err;           // ErrFlag bits
+    u32 out_count;     // rows written by compaction
+    u32 aux0, aux1;
+};
+
+struct TableRef {
+    u64 *slots;        // (cap + 2) * stride words
+    u64 cap;           // power of two
+    int32_t stride;
+    int32_t gmax_probe;
+    Ctl *ctl;
+    u64 *spill;        // spill_cap records of (1 + words) words
+    u32 spill_cap;
+    u32 spill_threshold;
+};
+
+// ----------------------------------------------------------------- keys
+// Returns 0 = ordinary key in pk, 1 = pk equals EMPTY_KEY (out-of-band slot
+// cap+0), 2 = NULL key (slot cap+1), 3 = NULL in a full-width pair key
+// (unsupported; flagged).
+__device__ __forceinline__ int make_key(const Plan &P, u64 r, u64 &pk) {
+    if (P.key_mode == KEY_SINGLE || P.key_mode == KEY_STRING) {
+        const DevCol &c = P.cols[P.key_col[0]];
+        if (!row_valid(c.valid, r)) { pk = 0; return 2; }
+        pk = (u64)load_int(c, r);
+        return pk == EMPTY_KEY ? 1 : 0;
+    }
+    const DevCol &ca = P.cols[P.key_col[0]];
+    const DevCol &cb = P.cols[P.key_col[1]];
+    bool va = row_valid(ca.valid, r), vb = row_valid(cb.valid, r);
+    u64 a = va ? (u64)load_int(ca, r) : 0ull;
+    u64 b = vb ? (u64)load_int(cb, r) : 0ull;
+    if (P.key_mode == KEY_PACKED) {
+        const int bb = P.key_bits_b, ba = P.key_bits_a;
+        const u64 mb = (bb >= 64) ? ~0ull : ((1ull << bb) - 1ull);
+        const u64 ma = (ba >= 64) ? ~0ull : ((1ull << ba) - 1ull);
+        pk = ((a & ma) << bb) | (b & mb) | ((u64)(!va) << (ba + bb)) | ((u64)(!vb) << (ba + bb + 1));
+        return 0;
+    }
+    if (!va || !vb) { pk = 0; return 3; }
+    pk = ((a & 0xffffffffull) << 32) | (b & 0xffffffffull);
+    return pk == EMPTY_KEY ? 1 : 0;
+}
+
+__device__ __forceinline__ bool pass_filters(const Plan &P, u64 r) {
+    for (int i = 0; i < P.n_filters; i++) {
+        const Filter &f = P.filters[i];
+        const DevCol &c = P.cols[f.col];
+        if (!row_valid(c.valid, r)) return false;
+        if (c.type == GB_T_DOUBLE) {
+            if (!cmp_f(f.op, load_f64(c, r), f.dc)) return false;
+        } else {
+            if (!cmp_i(f.op, load_int(c, r), f.ic)) return false;
+        }
+    }
+    return true;
+}
+
+// Per-op partial contributions of row r (identity where the input is NULL).
+__device__ __forceinline__ void load_vals(const Plan &P, u64 r, u64 *v) {
+#pragma unroll
+    for (int i = 0; i < GB_MAX_OPS; i++) {
+        if (i < P.n_ops) {
+            const Op o = P.ops[i];
+            const DevCol &c = P.cols[o.col];
+            const bool ok = row_valid(c.valid, r);
+            u64 x = P.word_init[o.word];
+            if (ok) {
+                switch (o.kind) {
+                case OP_ADD_F: x = (u64)__double_as_longlong(load_f64(c, r)); break;
+                case OP_MIN_F:
+                case OP_MAX_F: x = (u64)enc_f64(load_f64(c, r)); break;
+                case OP_CNT_NN: x = 1ull; break;
+                default: x = (u64)load_int(c, r); break;
+                }
+            }
+            v[i] = x;
+        }
+    }
+}
+
+// ------------------------------------------------------------ HBM table
+// Find or claim the slot of pk.  Returns the slot index or -1 if the probe
+// bound was reached.  `new_groups` counts claimed slots (CTA-local).
+__device__ __forceinline__ long long g_slot(const TableRef &T, u64 pk, u64 h, u32 *new_groups) {
+    u64 s = h & (T.cap - 1);
+    for (int p = 0; p < T.gmax_probe; p++) {
+        u64 *kp = T.slots + s * (u64)T.stride;
+        u64 k = *(volatile u64 *)kp;
+        if (k == pk) return (long long)s;
+        if (k == EMPTY_KEY) {
+            u64 old = atomicCAS(kp, EMPTY_KEY, pk);
+            if (old == EMPTY_KEY) {
+                atomicAdd(new_groups, 1u);
+                return (long long)s;
+            }
+            if (old == pk) return (long long)s;
+        }
+        s = (s + 1) & (T.cap - 1);
+    }
+    return -1;
+}
+
+__device__ __forceinline__ void apply_state(const Plan &P, u64 *w, u64 cnt, const u64 *v) {
+    if (cnt) atomicAdd(w, cnt);
+#pragma unroll
+    for (int i = 0; i < GB_MAX_OPS; i++) {
+        if (i < P.n_ops) {
+            const Op o = P.ops[i];
+            op_apply(o.kind, w + o.word, v[i], P.word_init[o.word]);
+        }
+    }
+}
+
+__device__ __forceinline__ void spill_record(const Plan &P, const TableRef &T, u64 pk, u64 cnt, const u64 *v) {
+    u32 idx = atomicAdd(&T.ctl->spill_count, 1u);
+    if (idx >= T.spill_cap) {
+        atomicOr(&T.ctl->err, (u32)ERR_SPILL_OVERFLOW);
+        return;
+    }
+    u64 *rec = T.spill + (u64)idx * (u64)(1 + P.words);
+    rec[0] = pk;
+    rec[1] = cnt;
+    for (int i = 0; i < P.n_ops; i++) rec[1 + P.ops[i].word] = v[i];
+}
+
+// Fold a combined partial into the HBM table (or spill it).
+__device__ __forceinline__ void global_fold(const Plan &P, const TableRef &T, u64 pk, u64 cnt, const u64 *v,
+                                            u32 *new_groups) {
+    long long s = g_slot(T, pk, mix64(pk), new_groups);
+    if (s < 0) {
+        spill_record(P, T, pk, cnt, v);
+        return;
+    }
+    apply_state(P, T.slots + (u64)s * (u64)T.stride + 1, cnt, v);
+}
+
+// Out-of-band slots (EMPTY_KEY-valued key, NULL key) are folded directly.
+__device__ __forceinline__ void special_fold(const Plan &P, const TableRef &T, int kind, u64 cnt, const u64 *v) {
+    u64 *w = T.slots + (T.cap + (u64)(kind - 1)) * (u64)T.stride + 1;
+    apply_state(P, w, cnt, v);
+}
+
+// ------------------------------------------------------ shared-memory table
+struct SmemTable {
+    u64 *keys;   // S keys
+    u64 *st;     // S * words state words
+    int S;       // power of two (0 = disabled)
+    int probe;   // probe bound
+};
+
+__device__ __forceinline__ void smem_init(const Plan &P, SmemTable &t) {
+    for (int i = threadIdx.x; i < t.S; i += blockDim.x) {
+        t.keys[i] = EMPTY_KEY;
+        for (int w = 0; w < P.words; w++) t.st[(u64)i * P.words + w] = P.word_init[w];
+    }
+}
+
+// Returns true if folded into shared memory.
+__device__ __forceinline__ bool smem_fold(const Plan &P, SmemTable &t, u64 pk, u64 h, u64 cnt, const u64 *v) {
+    if (t.S == 0) return false;
+    u32 s = (u32)(h >> 40) & (u32)(t.S - 1);
+    volatile u64 *vk = t.keys;
+    for (int p = 0; p < t.probe; p++) {
+        u64 k = vk[s];
+        bool hit = (k == pk);
+        if (!hit && k == EMPTY_KEY) {
+            u64 old = atomicCAS(&t.keys[s], EMPTY_KEY, pk);
+            hit = (old == EMPTY_KEY || old == pk);
+        }
+        if (hit) {
+            apply_state(P, t.st + (u64)s * P.words, cnt, v);
+            return true;
+        }
+        s = (s + 1) & (u32)(t.S - 1);
+    }
+    return false;
+}
+
+__device__ __forceinline__ void smem_flush(const Plan &P, const TableRef &T, SmemTable &t, u32 *new_groups) {
+    for (int i = threadIdx.x; i < t.S; i += blockDim.x) {
+        u64 k = t.keys[i];
+        if (k == EMPTY_KEY) continue;
+        const u64 *st = t.st + (u64)i * P.words;
+        u64 v[GB_MAX_OPS];
+#pragma unroll
+        for (int j = 0; j < GB_MAX_OPS; j++)
+            if (j < P.n_ops) v[j] = st[P.ops[j].word];
+        global_fold(P, T, k, st[0], v, new_groups);
+    }
+}
+
+// ------------------------------------------------------- warp row step
+// Processes rows [base, base+32) ∩ [.., end) of the current batch; rows
+// index the column vectors (row_ids != nullptr: gather through ids).
+template <bool PRECOMBINE>
+__device__ __forceinline__ void warp_rows(const Plan &P, const TableRef &T, SmemTable &sm, u64 base, u64 end,
+                                          u32 *new_groups) {
+    const int lane = threadIdx.x & 31;
+    const u64 r = base + lane;
+    bool act = r < end;
+    if (act && P.n_filters) act = pass_filters(P, r);
+    u64 pk = 0;
+    u64 v[GB_MAX_OPS];
+#pragma unroll
+    for (int i = 0; i < GB_MAX_OPS; i++) v[i] = 0;
+    if (act) {
+        int kind = make_key(P, r, pk);
+        load_vals(P, r, v);
+        if (kind != 0) {
+            if (kind == 3) atomicOr(&T.ctl->err, (u32)ERR_NULL_IN_WIDE_KEY);
+            else special_fold(P, T, kind, 1, v);
+            act = false;
+        }
+    }
+    const unsigned am = __ballot_sync(FULL, act);
+    if (am == 0) return;
+    u64 cnt = 1;
+    if (PRECOMBINE) {
+        unsigned peers = __match_any_sync(FULL, pk) & am;
+        const bool leader = act && ((__ffs(peers) - 1) == lane);
+        unsigned rem = leader ? (peers & ~(1u << lane)) : 0u;
+        cnt = __popc(peers);
+        const int maxit = __reduce_max_sync(FULL, (unsigned)__popc(rem));
+        for (int it = 0; it < maxit; it++) {
+            const int src = rem ? (__ffs(rem) - 1) : lane;
+            rem &= rem - 1u;
+#pragma unroll
+            for (int i = 0; i < GB_MAX_OPS; i++) {
+                if (i < P.n_ops) {
+                    u64 o = __shfl_sync(FULL, v[i], src);
+                    if (src != lane) v[i] = op_combine(P.ops[i].kind, v[i], o);
+                }
+            }
+        }
+        act = leader;
+    }
+    if (!act) return;
+    const u64 h = mix64(pk);
+    if (!smem_fold(P, sm, pk, h, cnt, v)) global_fold(P, T, pk, cnt, v, new_groups);
+}
+
+}  // namespace gb

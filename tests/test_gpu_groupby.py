@@ -1,0 +1,230 @@
+"""GPU parity: the CUDA GROUP BY (through the C ABI) against the oracle on
+identical seeded inputs.  Integer results bit-exact; DOUBLE SUM/AVG within
+1e-12 relative error of the FP64 compensated sum."""
+import numpy as np
+import pytest
+
+import oracle
+from slothdb_gb300 import capi, datagen
+from slothdb_gb300.capi import BIGINT, DOUBLE, INTEGER, SMALLINT
+from util import compare, gpu_to_dict
+
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("oracle_lib", "gblib")]
+
+REL_TOL = 1e-12
+
+
+def run_gpu(col_types, group_cols, aggs, cols, filters=(), nulls=None, est_groups=0, device=False,
+            chunks=None, topn=None):
+    nullable = [i for i, m in enumerate(nulls or []) if m is not None]
+    g = capi.GroupBy(col_types, group_cols, aggs, filters=filters, nullable=nullable, est_groups=est_groups)
+    try:
+        if topn:
+            g.set_topn(*topn)
+        n = len(cols[0])
+        validity = None
+        if nulls is not None:
+            validity = [capi.validity_words(~m) if m is not None else None for m in nulls]
+        bounds = [(0, n)] if not chunks else [(i, min(n, i + chunks)) for i in range(0, max(n, 1), chunks)]
+        for lo, hi in bounds:
+            if hi <= lo and n > 0:
+                continue
+            part = [c[lo:hi] for c in cols]
+            vpart = None
+            if validity is not None:
+                assert lo % 64 == 0
+                vpart = [v[lo // 64:(hi + 63) // 64] if v is not None else None for v in validity]
+            if device:
+                import torch
+                tens = [torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in part]
+                vt = None
+                if vpart is not None:
+                    vt = [torch.from_numpy(v.view(np.int64)).cuda() if v is not None else None for v in vpart]
+                torch.cuda.synchronize()
+                g.ingest(tens, nrows=hi - lo, validity=vt, device=True)
+                torch.cuda.synchronize()
+            else:
+                g.ingest(part, nrows=hi - lo, validity=vpart)
+        g.finalize()
+        res = g.result()
+        launches = g.launches()
+    finally:
+        g.close()
+    n_keys = len(group_cols)
+    out_types = [col_types[c] for c in group_cols] + [oracle.agg_out_type(oracle.AGG_NAMES[k] if isinstance(k, str)
+                                                                          else k, col_types[c] if c >= 0 else 0)
+                                                      for k, c in aggs]
+    d = gpu_to_dict(res, n_keys, out_types)
+    d["launches"] = launches
+    return d
+
+
+def check(col_types, group_cols, aggs, cols, **kw):
+    nulls = kw.get("nulls")
+    filters = kw.get("filters", ())
+    orc = oracle.run_query(col_types, group_cols, aggs, cols, filters=filters, nulls=nulls)
+    gpu = run_gpu(col_types, group_cols, aggs, cols, **kw)
+    assert gpu["launches"] > 0
+    return compare(gpu, orc, rel_tol=REL_TOL), gpu, orc
+
+
+PLAIN_AGGS = [("count_star", -1), ("sum", 1), ("min", 1), ("max", 1)]
+
+
+def test_plain_workload_1m_host_and_device():
+    k, v = datagen.plain(1_000_000, seed=0)
+    check([INTEGER, BIGINT], [0], PLAIN_AGGS, [k, v])
+    check([INTEGER, BIGINT], [0], PLAIN_AGGS, [k, v], device=True)
+
+
+@pytest.mark.parametrize("n", [0, 1, 31, 32, 33, 2047, 2048, 2049, 122_880 + 7])
+def test_ragged_sizes(n):
+    k, v = datagen.plain(max(n, 1), seed=11, n_keys=97)
+    k, v = k[:n], v[:n]
+    if n == 0:
+        gpu = run_gpu([INTEGER, BIGINT], [0], PLAIN_AGGS, [k, v])
+        assert len(gpu["keys"][0]) == 0
+        return
+    check([INTEGER, BIGINT], [0], PLAIN_AGGS, [k, v])
+
+
+def test_all_distinct_and_single_group():
+    n = 300_000
+    rng = np.random.default_rng(3)
+    k = rng.permutation(n).astype(np.int64) * 7919 - 10**12
+    v = rng.integers(-10**9, 10**9, n, dtype=np.int64)
+    check([BIGINT, BIGINT], [0], PLAIN_AGGS, [k, v], est_groups=n)
+    check([BIGINT, BIGINT], [0], PLAIN_AGGS, [np.full(n, 42, np.int64), v])
+
+
+def test_table_growth_from_tiny_estimate():
+    """500K distinct keys into a table sized for 16 groups: spill records,
+    rehash and replay must lose nothing."""
+    n = 1_500_000
+    rng = np.random.default_rng(4)
+    k = rng.integers(0, 500_000, n, dtype=np.int64)
+    v = rng.integers(0, 10**6, n, dtype=np.int64)
+    check([BIGINT, BIGINT], [0], PLAIN_AGGS, [k, v], est_groups=16)
+
+
+def test_zipf_double_sum_avg_tolerance():
+    k, x = datagen.zipf(2_000_000, seed=1, n_values=400_000)
+    err, gpu, orc = check([BIGINT, DOUBLE], [0], [("count_star", -1), ("sum", 1), ("avg", 1)], [k, x],
+                          est_groups=400_000)
+    assert err <= REL_TOL
+
+
+def test_zipf_topn_count_desc():
+    k, x = datagen.zipf(2_000_000, seed=1, n_values=400_000)
+    aggs = [("count_star", -1), ("sum", 1), ("avg", 1)]
+    gpu = run_gpu([BIGINT, DOUBLE], [0], aggs, [k, x], topn=(1, False, 10), est_groups=400_000)
+    orc = oracle.run_query([BIGINT, DOUBLE], [0], aggs, [k, x])
+    cnt = orc["aggs"][0][0]
+    order = np.lexsort((orc["keys"][0], -cnt))[:10]
+    assert np.array_equal(gpu["keys"][0], orc["keys"][0][order])
+    assert np.array_equal(gpu["aggs"][0][0], cnt[order])
+    ref_sum = orc["aggs"][1][2][order]
+    assert np.max(np.abs(gpu["aggs"][1][0] - ref_sum) / np.abs(ref_sum)) <= REL_TOL
+
+
+def test_topn_ties_key_ascending_and_asc_order():
+    # the reference's ORDER BY cnt DESC, dept tie case (test_aggregation.cpp:196-212) on int keys
+    k = np.array([7, 7, 3, 3, 9], dtype=np.int32)
+    v = np.arange(5, dtype=np.int64)
+    gpu = run_gpu([INTEGER, BIGINT], [0], [("count_star", -1)], [k, v], topn=(1, False, 3))
+    assert gpu["keys"][0].tolist() == [3, 7, 9]
+    assert gpu["aggs"][0][0].tolist() == [2, 2, 1]
+    gpu = run_gpu([INTEGER, BIGINT], [0], [("sum", 1)], [k, v], topn=(1, True, 2))
+    assert gpu["keys"][0].tolist() == [7, 9]
+
+
+def test_nulls_in_keys_and_values():
+    n = 200_000
+    rng = np.random.default_rng(6)
+    k = rng.integers(0, 1000, n, dtype=np.int32)
+    v = rng.integers(-10**6, 10**6, n, dtype=np.int64)
+    kn = rng.random(n) < 0.01
+    vn = rng.random(n) < 0.2
+    # a group whose values are all NULL (SUM/MIN/MAX → NULL)
+    k[:50] = 5000
+    vn[:50] = True
+    kn[:50] = False
+    check([INTEGER, BIGINT], [0], [("count_star", -1), ("count", 1), ("sum", 1), ("avg", 1), ("min", 1), ("max", 1)],
+          [k, v], nulls=[kn, vn], chunks=65536)
+
+
+def test_composite_int32_int16_key_batched_shape():
+    a, b, s, m = datagen.composite(400_000, 50_000, seed=3)
+    check([INTEGER, SMALLINT, BIGINT, INTEGER], [0, 1], [("count_star", -1), ("sum", 2), ("max", 3)], [a, b, s, m])
+
+
+def test_composite_with_nulls_and_wide_pair():
+    n = 100_000
+    rng = np.random.default_rng(8)
+    a = rng.integers(-50, 50, n, dtype=np.int32)
+    b = rng.integers(-3, 3, n, dtype=np.int16)
+    an = rng.random(n) < 0.05
+    bn = rng.random(n) < 0.05
+    s = rng.integers(0, 100, n, dtype=np.int64)
+    check([INTEGER, SMALLINT, BIGINT], [0, 1], [("count_star", -1), ("sum", 2)], [a, b, s], nulls=[an, bn, None])
+    c = rng.integers(-(2**31), 2**31 - 1, n, dtype=np.int32)
+    d = rng.integers(-5, 5, n, dtype=np.int32)
+    check([INTEGER, INTEGER, BIGINT], [0, 1], [("count_star", -1), ("min", 2)], [c, d, s])
+
+
+def test_filters_int_and_double():
+    n = 500_000
+    rng = np.random.default_rng(9)
+    k = rng.integers(0, 5000, n, dtype=np.int32)
+    f = rng.integers(0, 1000, n, dtype=np.int16)
+    v = rng.integers(-10**9, 10**9 + 1, n, dtype=np.int64)
+    x = rng.normal(0, 1, n)
+    check([INTEGER, SMALLINT, BIGINT, DOUBLE], [0], [("sum", 2), ("count_star", -1)], [k, f, v, x],
+          filters=[(1, "<", 100)])
+    check([INTEGER, SMALLINT, BIGINT, DOUBLE], [0], [("sum", 2), ("min", 3), ("max", 3)], [k, f, v, x],
+          filters=[(3, ">=", 0.5), (1, "!=", 7)])
+
+
+def test_special_key_values_and_smallint():
+    k = np.array([np.iinfo(np.int64).min, 0, -1, np.iinfo(np.int64).max, np.iinfo(np.int64).min, -1], dtype=np.int64)
+    v = np.arange(6, dtype=np.int64)
+    check([BIGINT, BIGINT], [0], PLAIN_AGGS, [k, v])
+    ks = np.array([-32768, 32767, 0, -32768], dtype=np.int16)
+    vd = np.array([-1.5, 2.25, -0.0, 7.0])
+    check([SMALLINT, DOUBLE], [0], [("min", 1), ("max", 1), ("sum", 1), ("count", 1)], [ks, vd])
+
+
+def test_many_chunks_accumulate():
+    k, v = datagen.plain(100_000, seed=12)
+    check([INTEGER, BIGINT], [0], PLAIN_AGGS, [k, v], chunks=2048)
+
+
+def test_engine_hash_aggregate_known_answer(gblib):
+    import ctypes as C
+    keys = np.array([1, 2, 1, 2, 1], dtype=np.int32)
+    vals = np.array([10, 20, 30, 40, 50], dtype=np.int32)
+    ok = np.zeros(8, np.int32)
+    os_ = np.zeros(8, np.int64)
+    oc = np.zeros(8, np.int64)
+    n = C.c_uint64()
+    capi.check(gblib.gb_engine_hash_aggregate(keys.ctypes.data, vals.ctypes.data, 5, ok.ctypes.data,
+                                              os_.ctypes.data, oc.ctypes.data, 8, C.byref(n)))
+    got = {int(ok[i]): (int(os_[i]), int(oc[i])) for i in range(n.value)}
+    assert got == {1: (90, 3), 2: (60, 2)}
+
+
+def test_reset_reuses_handle():
+    k, v = datagen.plain(50_000, seed=13)
+    g = capi.GroupBy([INTEGER, BIGINT], [0], PLAIN_AGGS)
+    try:
+        outs = []
+        for _ in range(2):
+            g.ingest([k, v])
+            g.finalize()
+            outs.append(g.result())
+            g.reset()
+        o0, o1 = (np.argsort(o[0][0]) for o in outs)
+        for c in range(5):
+            assert np.array_equal(outs[0][c][0][o0], outs[1][c][0][o1])
+    finally:
+        g.close()
