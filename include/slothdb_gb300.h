@@ -191,6 +191,26 @@ gb_status gb_engine_hash_aggregate(const int32_t *keys, const int32_t *values, u
                                    int32_t *out_keys, int64_t *out_sums, int64_t *out_counts,
                                    uint64_t cap, uint64_t *n_out);
 
+/* Allocation-free GROUP BY for callers that cannot allocate device memory
+ * on their query path (an engine that hands out device memory only from
+ * its own pre-reserved arena, a plugin host that forbids allocation inside
+ * operator calls, or a latency-critical path where cudaMalloc/cudaFree
+ * would synchronise the device).  No counterpart in the reference: it is
+ * the GPU engine's HashAggregate shape (int64 keys; SUM and COUNT of int64
+ * values) on DEVICE buffers, with all scratch in fixed-size device arrays
+ * inside the library (about 8.1 MiB, held by every GPU that loads the
+ * library until the process exits).  Limits: out_cap <= GB_NOALLOC_MAX_GROUPS
+ * and at most that many distinct keys, n <= 2^31 rows; beyond them the call
+ * fails with a message and writes no result count.  The first call on a
+ * device resolves the scratch addresses (cudaGetSymbolAddress), so make it
+ * before any stream capture.  All calls share the scratch, which each call
+ * clears first: calls that overlap on the GPU race and must be serialised.
+ * Outputs: *n_out groups in out_keys/out_sums/out_counts (device). */
+#define GB_NOALLOC_MAX_GROUPS 131072
+gb_status gb_hash_aggregate_noalloc(const int64_t *keys, const int64_t *values, uint64_t n,
+                                    int64_t *out_keys, int64_t *out_sums, int64_t *out_counts,
+                                    uint64_t out_cap, uint64_t *n_out, void *stream);
+
 /* Pinned host memory helpers (so a caller can stage inputs for the
  * overlapped host→HBM path without linking CUDA itself). */
 gb_status gb_host_alloc(void **ptr, size_t bytes);

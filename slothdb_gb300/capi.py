@@ -80,6 +80,8 @@ _SIGS = {
     "gb_agg_profile": (C.c_uint32, [C.c_void_p, C.POINTER(KernelStat), C.c_uint32]),
     "gb_engine_hash_aggregate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                            C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "gb_hash_aggregate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64), C.c_void_p]),
     "gb_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
     "gb_host_free": (C.c_int, [C.c_void_p]),
     "gb_device_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
