@@ -170,6 +170,19 @@ void gb_agg_destroy(gb_agg *h);
  * accounting). */
 uint64_t gb_agg_kernel_launches(const gb_agg *h);
 
+/* Execution options of a handle, set before its first ingest (the
+ * autotuner's knobs; no reference counterpart beyond the hard-coded thread
+ * counts of physical_planner.cpp:7320-7641):
+ *   "mode"        0 auto, 1 hash (shared + HBM tables), 2 radix partitions
+ *   "smem_slots"  shared pre-aggregation table slots (power of two, hash)
+ *   "precombine"  warp pre-combine of duplicate keys (0/1, hash)
+ *   "ctas_per_sm" persistent CTAs per SM (hash)
+ *   "tile_rows"   rows per claimed tile (hash)
+ *   "hot_slots"   heavy-hitter table slots (power of two, radix) */
+gb_status gb_agg_set_option(gb_agg *h, const char *name, int64_t value);
+/* 1 = radix mode, 0 = hash mode. */
+int32_t gb_agg_get_mode(const gb_agg *h);
+
 /* Per-kernel device time of this handle, measured with CUDA events on the
  * stream each kernel is launched on (enabled by gb_agg_set_profiling; no
  * reference counterpart: the reference's SLOTH_PROFILE counters,

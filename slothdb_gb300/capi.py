@@ -76,6 +76,8 @@ _SIGS = {
     "gb_agg_reset": (C.c_int, [C.c_void_p]),
     "gb_agg_destroy": (None, [C.c_void_p]),
     "gb_agg_kernel_launches": (C.c_uint64, [C.c_void_p]),
+    "gb_agg_set_option": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
+    "gb_agg_get_mode": (C.c_int32, [C.c_void_p]),
     "gb_agg_set_profiling": (C.c_int, [C.c_void_p, C.c_int32]),
     "gb_agg_profile": (C.c_uint32, [C.c_void_p, C.POINTER(KernelStat), C.c_uint32]),
     "gb_engine_hash_aggregate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
@@ -144,7 +146,7 @@ class GroupBy:
     '==', '!=', '<', '<=', '>', '>='.
     """
 
-    def __init__(self, col_types, group_cols, aggs, filters=(), nullable=(), est_groups=0):
+    def __init__(self, col_types, group_cols, aggs, filters=(), nullable=(), est_groups=0, options=None):
         self.lib = load()
         self.col_types = list(col_types)
         self.group_cols = list(group_cols)
@@ -169,6 +171,8 @@ class GroupBy:
         check(self.lib.gb_agg_create(C.byref(spec), C.byref(h)))
         self.h = h
         self._keep = []
+        for k, v in (options or {}).items():
+            self.set_option(k, v)
 
     def set_topn(self, col_idx, ascending, limit):
         check(self.lib.gb_agg_set_topn(self.h, col_idx, 1 if ascending else 0, limit))
@@ -219,6 +223,12 @@ class GroupBy:
                 bits = np.zeros(0, dtype=bool)
             out.append((vals, bits))
         return out
+
+    def set_option(self, name, value):
+        check(self.lib.gb_agg_set_option(self.h, name.encode(), int(value)))
+
+    def mode(self):
+        return int(self.lib.gb_agg_get_mode(self.h))
 
     def set_profiling(self, on=True):
         check(self.lib.gb_agg_set_profiling(self.h, 1 if on else 0))

@@ -10,6 +10,7 @@
 
 #include "gb_agg_host.h"
 #include "gb_kernels.cuh"
+#include "gb_radix.h"
 
 namespace gb {
 
@@ -153,44 +154,6 @@ __global__ void k_merge_records(const __grid_constant__ Plan P, const u64 *recs,
     if (threadIdx.x == 0 && s_new) atomicAdd(&T.ctl->n_groups, s_new);
 }
 
-// ------------------------------------------------------------ emit
-struct EmitAgg {
-    int32_t kind;      // gb_agg_kind
-    int32_t in_type;   // gb_type of the input column (-1 for COUNT(*))
-    int32_t out_type;  // gb_type of the output column
-    int32_t val_word;  // state word of the value (-1 none)
-    int32_t cnt_word;  // state word of the non-NULL count
-    int32_t pad;
-};
-
-struct EmitArgs {
-    EmitAgg aggs[GB_MAX_AGGS];
-    void *out[2 + GB_MAX_AGGS];        // device column buffers
-    uint64_t *valid[2 + GB_MAX_AGGS];  // validity words (pre-set to all ones)
-    int32_t n_aggs;
-    int32_t n_keys;
-    u64 out_cap;
-};
-
-__device__ __forceinline__ void store_int(void *base, int type, u64 i, i64 v) {
-    switch (type) {
-    case GB_T_SMALLINT: ((int16_t *)base)[i] = (int16_t)v; break;
-    case GB_T_INTEGER: ((int32_t *)base)[i] = (int32_t)v; break;
-    default: ((long long *)base)[i] = v; break;
-    }
-}
-
-__device__ __forceinline__ void clear_valid(uint64_t *vw, u64 i) {
-    atomicAnd((unsigned long long *)(vw + (i >> 6)), ~(1ull << (i & 63)));
-}
-
-__device__ __forceinline__ i64 sext(u64 x, int bits) {
-    if (bits >= 64) return (i64)x;
-    u64 m = 1ull << (bits - 1);
-    x &= (1ull << bits) - 1ull;
-    return (i64)((x ^ m) - m);
-}
-
 // Compact used slots into dense result columns (the direct emit of
 // physical_planner.cpp:8027-8173 with agg_emit_helpers.cpp:26-165 rules).
 __global__ void k_compact(const __grid_constant__ Plan P, const u64 *slots, u64 cap, int stride,
@@ -215,52 +178,8 @@ __global__ void k_compact(const __grid_constant__ Plan P, const u64 *slots, u64 
             atomicOr(&ctl->err, (u32)ERR_OUT_OVERFLOW);
             continue;
         }
-        // keys
         const u64 pk = (s < cap) ? sl[0] : (s == cap ? EMPTY_KEY : 0ull);
-        const bool null_key = (s == cap + 1);
-        if (P.key_mode == KEY_SINGLE || P.key_mode == KEY_STRING) {
-            store_int(E.out[0], P.key_type[0], o, (i64)pk);
-            if (null_key) clear_valid(E.valid[0], o);
-        } else if (P.key_mode == KEY_PACKED) {
-            const int bb = P.key_bits_b, ba = P.key_bits_a;
-            i64 a = sext(pk >> bb, ba), b = sext(pk, bb);
-            bool na = (pk >> (ba + bb)) & 1ull, nb = (pk >> (ba + bb + 1)) & 1ull;
-            store_int(E.out[0], P.key_type[0], o, a);
-            store_int(E.out[1], P.key_type[1], o, b);
-            if (na) clear_valid(E.valid[0], o);
-            if (nb) clear_valid(E.valid[1], o);
-        } else {
-            store_int(E.out[0], P.key_type[0], o, (i64)(int32_t)(uint32_t)(pk >> 32));
-            store_int(E.out[1], P.key_type[1], o, (i64)(int32_t)(uint32_t)pk);
-        }
-        const u64 *w = sl + 1;
-        for (int a = 0; a < E.n_aggs; a++) {
-            const EmitAgg &g = E.aggs[a];
-            void *dst = E.out[E.n_keys + a];
-            uint64_t *vw = E.valid[E.n_keys + a];
-            const u64 cnt = w[g.cnt_word];
-            switch (g.kind) {
-            case GB_AGG_COUNT_STAR:
-            case GB_AGG_COUNT: ((long long *)dst)[o] = (i64)cnt; break;
-            case GB_AGG_SUM:
-                if (cnt == 0) { ((long long *)dst)[o] = 0; clear_valid(vw, o); }
-                else ((long long *)dst)[o] = (i64)w[g.val_word];  // int64 or double bits
-                break;
-            case GB_AGG_AVG:
-                if (cnt == 0) { ((double *)dst)[o] = 0.0; clear_valid(vw, o); }
-                else {
-                    double sum = (g.in_type == GB_T_DOUBLE) ? __longlong_as_double((i64)w[g.val_word])
-                                                            : (double)(i64)w[g.val_word];
-                    ((double *)dst)[o] = sum / (double)cnt;
-                }
-                break;
-            default:  // MIN / MAX
-                if (cnt == 0) { store_int(dst, g.out_type == GB_T_DOUBLE ? GB_T_BIGINT : g.out_type, o, 0); clear_valid(vw, o); }
-                else if (g.out_type == GB_T_DOUBLE) ((double *)dst)[o] = dec_f64((i64)w[g.val_word]);
-                else store_int(dst, g.out_type, o, (i64)w[g.val_word]);
-                break;
-            }
-        }
+        emit_group(P, E, o, pk, s == cap + 1, sl + 1);
     }
 }
 
@@ -522,6 +441,16 @@ struct gb_agg {
     std::vector<DevBuf> stage[2];
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t ev_copied[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr};
+    // radix mode (high-cardinality keys)
+    int mode = 0;          // 0 = hash, 1 = radix
+    int mode_option = 0;   // 0 = auto, 1 = force hash, 2 = force radix
+    RadixPlan rplan{};
+    bool r_ready = false;
+    DevBuf r_skeys, r_scnt, r_hist, r_hot_keys, r_hot_part, r_cursor, r_part, r_part2, r_ovf;
+    u64 r_cap_p = 0;
+    u32 r_ovf_cap = 0;
+    int r_grid = 0;
+    u64 rows_ingested = 0;
     // tuning
     int block = 512;
     int ctas_per_sm = 2;
@@ -791,6 +720,184 @@ static gb_status run_ingest(gb_agg *h, u64 n_rows, cudaStream_t st) {
             if (s) return s;
         }
         if ((s = ensure_capacity(h, st))) return s;
+    }
+    return GB_OK;
+}
+
+
+// ------------------------------------------------------------- radix mode
+static RadixRef radix_ref(gb_agg *h) {
+    RadixRef X;
+    X.part = (u64 *)h->r_part.p;
+    X.cap_p = h->r_cap_p;
+    X.cursor = (u32 *)h->r_cursor.p;
+    X.ovf = (u64 *)h->r_ovf.p;
+    X.ovf_cap = h->r_ovf_cap;
+    // tiles still in flight after the threshold trips add at most grid * tile rows
+    const u64 inflight = (u64)h->r_grid * radix_tile_rows(h->rplan) + 4096;
+    X.ovf_threshold = h->r_ovf_cap > inflight ? (u32)(h->r_ovf_cap - inflight) : 0u;
+    X.hot_keys = (const u64 *)h->r_hot_keys.p;
+    X.hot_part = (u64 *)h->r_hot_part.p;
+    return X;
+}
+
+static gb_status radix_begin(gb_agg *h, u64 n, cudaStream_t st) {
+    const RadixPlan &R = h->rplan;
+    const u64 np = 1ull << R.pbits;
+    const int W = h->plan.words;
+    const int TV = 1 + R.V;
+    gb_status s;
+    // sample the first batch
+    u64 m = std::min<u64>(n, 1u << 18);
+    u64 scap = 1024;
+    while (scap < 2 * m) scap <<= 1;
+    if ((s = h->r_skeys.ensure(scap * 8)) || (s = h->r_scnt.ensure(scap * 4)) || (s = h->r_hist.ensure(260 * 4)) ||
+        (s = h->r_hot_keys.ensure((size_t)R.HS * 8)))
+        return s;
+    GB_CUDA(cudaMemsetAsync(h->r_skeys.p, 0xff, scap * 8, st));
+    GB_CUDA(cudaMemsetAsync(h->r_scnt.p, 0, scap * 4, st));
+    GB_CUDA(cudaMemsetAsync(h->r_hist.p, 0, 260 * 4, st));
+    GB_CUDA(cudaMemsetAsync(h->r_hot_keys.p, 0xff, (size_t)R.HS * 8, st));
+    {
+        ProfScope ps(h, "k_sample", st);
+        if ((s = radix_launch_sample(h->plan, R, n, (u64 *)h->r_skeys.p, (u32 *)h->r_scnt.p, scap,
+                                     (u32 *)h->r_hist.p, (u64 *)h->r_hot_keys.p, st, &h->launches)))
+            return s;
+    }
+    u32 hot_rows = 0;
+    GB_CUDA(cudaMemcpyAsync(&hot_rows, (u32 *)h->r_hist.p + 256, 4, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    u64 sampled = std::max<u64>(1, std::min<u64>(n, m));
+    double hot_frac = std::min(1.0, (double)hot_rows / (double)sampled);
+    double tail = (double)n * (1.0 - hot_frac);
+    u64 cap_p = (u64)(tail / (double)np * 1.25) + 2048;
+    cap_p = (cap_p + 31) / 32 * 32;
+    if (cap_p > h->r_cap_p || !h->r_part.p) h->r_cap_p = cap_p;
+    if ((s = h->r_part.ensure((size_t)np * h->r_cap_p * TV * 8))) return s;
+    if ((s = h->r_cursor.ensure((size_t)np * CURSOR_PAD * 4))) return s;
+    GB_CUDA(cudaMemsetAsync(h->r_cursor.p, 0, (size_t)np * CURSOR_PAD * 4, st));
+    h->r_grid = sm_count();
+    if ((s = h->r_hot_part.ensure((size_t)h->r_grid * R.HS * W * 8))) return s;
+    if ((s = radix_fill_identity((u64 *)h->r_hot_part.p, (u64)h->r_grid * R.HS * W, W, h->plan, st))) return s;
+    h->launches++;
+    u32 ovf_cap = (1u << 21) + (u32)(h->r_grid * radix_tile_rows(R)) + 4096;
+    if (h->r_ovf_cap < ovf_cap) {
+        if ((s = h->r_ovf.ensure((size_t)ovf_cap * (TV + 1) * 8))) return s;
+        h->r_ovf_cap = ovf_cap;
+    }
+    h->r_ready = true;
+    return GB_OK;
+}
+
+// Grow the partition regions so every partition can take its overflow,
+// then append the overflow tuples.
+static gb_status radix_grow(gb_agg *h, u32 novf, cudaStream_t st) {
+    const RadixPlan &R = h->rplan;
+    const u64 np = 1ull << R.pbits;
+    const int TV = 1 + R.V;
+    std::vector<u32> cur((size_t)np * CURSOR_PAD);
+    GB_CUDA(cudaMemcpyAsync(cur.data(), h->r_cursor.p, cur.size() * 4, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    u64 need = 0;
+    for (u64 p = 0; p < np; p++) {
+        u64 c = cur[p * CURSOR_PAD];
+        need = std::max<u64>(need, c);
+        cur[p * CURSOR_PAD] = (u32)std::min<u64>(c, h->r_cap_p);  // tuples actually in the region
+    }
+    u64 ncap = std::max<u64>(h->r_cap_p * 2, need + need / 4 + 1024);
+    ncap = (ncap + 31) / 32 * 32;
+    gb_status s = h->r_part2.ensure((size_t)np * ncap * TV * 8);
+    if (s) return s;
+    GB_CUDA(cudaMemcpy2DAsync(h->r_part2.p, ncap * TV * 8, h->r_part.p, h->r_cap_p * TV * 8, h->r_cap_p * TV * 8, np,
+                              cudaMemcpyDeviceToDevice, st));
+    std::swap(h->r_part, h->r_part2);
+    h->r_part2.release();
+    h->r_cap_p = ncap;
+    GB_CUDA(cudaMemcpyAsync(h->r_cursor.p, cur.data(), cur.size() * 4, cudaMemcpyHostToDevice, st));
+    RadixRef X = radix_ref(h);
+    if ((s = radix_launch_drain(X, R.V, novf, st))) return s;
+    h->launches++;
+    Ctl *dctl = (Ctl *)h->ctl_buf.p;
+    GB_CUDA(cudaMemsetAsync(&dctl->aux0, 0, 4, st));
+    return GB_OK;
+}
+
+static gb_status radix_ingest(gb_agg *h, u64 n, cudaStream_t st) {
+    if (n == 0) return GB_OK;
+    gb_status s;
+    if (!h->r_ready && (s = radix_begin(h, n, st))) return s;
+    Ctl *dctl = (Ctl *)h->ctl_buf.p;
+    const u32 tr = radix_tile_rows(h->rplan);
+    const u64 n_tiles = (n + tr - 1) / tr;
+    u64 first = 0;
+    while (first < n_tiles) {
+        GB_CUDA(cudaMemsetAsync(&dctl->spill_count, 0, 4 * 4, st));
+        GB_CUDA(cudaMemsetAsync(&dctl->aux0, 0, 4, st));
+        RadixTile A;
+        A.n_rows = n;
+        A.first_tile = (u32)first;
+        A.n_tiles = (u32)(n_tiles - first);
+        TableRef T = table_ref(h);
+        RadixRef X = radix_ref(h);
+        {
+            ProfScope ps(h, "k_partition", st);
+            if ((s = radix_launch_p1(h->plan, h->rplan, X, T, A, h->r_grid, st))) return s;
+        }
+        h->launches++;
+        if ((s = read_ctl(h, st))) return s;
+        if ((s = check_err(h))) return s;
+        first += std::min<u64>(h->ctl_host.tile_counter, n_tiles - first);
+        if (h->ctl_host.aux0 > 0 && (s = radix_grow(h, h->ctl_host.aux0, st))) return s;
+    }
+    return GB_OK;
+}
+
+static gb_status alloc_outputs(gb_agg *h, u64 rows);
+static void fill_emit(gb_agg *h, EmitArgs &E, std::vector<DevBuf> &cols, std::vector<DevBuf> &valid, u64 cap);
+
+static gb_status radix_emit(gb_agg *h, cudaStream_t st) {
+    const RadixPlan &R = h->rplan;
+    const u64 np = 1ull << R.pbits;
+    gb_status s;
+    Ctl *dctl = (Ctl *)h->ctl_buf.p;
+    // capacity bound: tuples in partitions + hot keys + HBM-table slots
+    u64 tuples = 0;
+    if (h->r_ready) {
+        std::vector<u32> cur((size_t)np * CURSOR_PAD);
+        GB_CUDA(cudaMemcpyAsync(cur.data(), h->r_cursor.p, cur.size() * 4, cudaMemcpyDeviceToHost, st));
+        GB_CUDA(cudaStreamSynchronize(st));
+        for (u64 p = 0; p < np; p++) tuples += std::min<u64>(cur[p * CURSOR_PAD], h->r_cap_p);
+    }
+    u64 cap = tuples + (u64)R.HS + h->cap + 2;
+    if ((s = alloc_outputs(h, cap))) return s;
+    for (size_t c = 0; c < h->out_valid.size(); c++)
+        GB_CUDA(cudaMemsetAsync(h->out_valid[c].p, 0xff, (cap + 63) / 64 * 8, st));
+    GB_CUDA(cudaMemsetAsync(&dctl->spill_count, 0, 4 * 4, st));
+    GB_CUDA(cudaMemsetAsync(&dctl->out_count, 0, 4, st));
+    EmitArgs E;
+    fill_emit(h, E, h->out_cols, h->out_valid, h->out_cap);
+    if (h->r_ready) {
+        TableRef T = table_ref(h);
+        RadixRef X = radix_ref(h);
+        {
+            ProfScope ps(h, "k_part_agg", st);
+            if ((s = radix_launch_p2(h->plan, R, X, T, E, st))) return s;
+        }
+        {
+            ProfScope ps(h, "k_hot_emit", st);
+            if ((s = radix_launch_p3(h->plan, R, X, h->r_grid, dctl, E, st))) return s;
+        }
+        h->launches += 2;
+        if ((s = read_ctl(h, st))) return s;
+        if ((s = check_err(h))) return s;
+        h->n_groups = h->ctl_host.n_groups;
+        if (h->ctl_host.spill_count > 0) {
+            u32 sp = h->ctl_host.spill_count;
+            u64 nc = h->cap * 2;
+            while ((h->n_groups + sp) * 2 > nc) nc *= 2;
+            // T's groups are keys of partition tuples, so `cap` still bounds the result
+            if ((s = grow_and_merge(h, nc, sp, st))) return s;
+        }
     }
     return GB_OK;
 }
@@ -1086,7 +1193,7 @@ gb_status gb_agg_create(const gb_agg_spec *spec, gb_agg **out) {
     }
     gb_apply_tuning(h);
     u64 est = h->est_groups ? h->est_groups : (1u << 15);
-    h->cap = std::max<u64>(1024, next_pow2(est * 2));
+    h->cap = h->mode == 1 ? 4096 : std::max<u64>(1024, next_pow2(est * 2));
     if ((s = h->ctl_buf.ensure(sizeof(Ctl)))) {
         delete h;
         return s;
@@ -1151,7 +1258,8 @@ gb_status gb_agg_ingest(gb_agg *h, const gb_col *cols, uint64_t nrows, int32_t m
             h->plan.cols[c].valid = cols[c].validity;
             h->plan.cols[c].offsets = cols[c].offsets;
         }
-        gb_status s = run_ingest(h, nrows, st);
+        gb_status s = h->mode == 1 ? radix_ingest(h, nrows, st) : run_ingest(h, nrows, st);
+        h->rows_ingested += nrows;
         prof_collect(h);
         return s;
     }
@@ -1210,7 +1318,8 @@ gb_status gb_agg_ingest(gb_agg *h, const gb_col *cols, uint64_t nrows, int32_t m
             h->plan.cols[c].valid = cols[c].validity ? (const uint64_t *)h->stage[b][nc + c].p : nullptr;
             h->plan.cols[c].offsets = nullptr;
         }
-        if ((s = run_ingest(h, r1 - r0, st))) return s;
+        if ((s = (h->mode == 1 ? radix_ingest(h, r1 - r0, st) : run_ingest(h, r1 - r0, st)))) return s;
+        h->rows_ingested += r1 - r0;
         GB_CUDA(cudaEventRecord(h->ev_done[b], st));
     }
     prof_collect(h);
@@ -1222,11 +1331,15 @@ gb_status gb_agg_finalize(gb_agg *h, void *stream) {
     if (h->finalized) return GB_OK;
     cudaStream_t st = (cudaStream_t)stream;
     gb_status s;
-    if ((s = alloc_outputs(h, h->cap + 2))) return s;
-    for (size_t c = 0; c < h->out_valid.size(); c++)
-        GB_CUDA(cudaMemsetAsync(h->out_valid[c].p, 0xff, h->out_valid[c].n, st));
     Ctl *dctl = (Ctl *)h->ctl_buf.p;
-    GB_CUDA(cudaMemsetAsync(&dctl->out_count, 0, 4, st));
+    if (h->mode == 1) {
+        if ((s = radix_emit(h, st))) return s;
+    } else {
+        if ((s = alloc_outputs(h, h->cap + 2))) return s;
+        for (size_t c = 0; c < h->out_valid.size(); c++)
+            GB_CUDA(cudaMemsetAsync(h->out_valid[c].p, 0xff, (h->out_cap + 63) / 64 * 8, st));
+        GB_CUDA(cudaMemsetAsync(&dctl->out_count, 0, 4, st));
+    }
     GB_CUDA(cudaMemsetAsync(&dctl->err, 0, 4, st));
     EmitArgs E;
     fill_emit(h, E, h->out_cols, h->out_valid, h->out_cap);
@@ -1321,6 +1434,8 @@ gb_status gb_agg_reset(gb_agg *h) {
     if (s) return s;
     GB_CUDA(cudaMemset(h->ctl_buf.p, 0, sizeof(Ctl)));
     h->n_groups = 0;
+    h->r_ready = false;
+    h->rows_ingested = 0;
     h->finalized = false;
     h->has_result = false;
     h->topn_applied = false;
@@ -1340,6 +1455,9 @@ void gb_agg_destroy(gb_agg *h) {
     for (auto &b : h->out_valid) b.release();
     for (auto &b : h->top_cols) b.release();
     for (auto &b : h->top_valid) b.release();
+    for (DevBuf *b : {&h->r_skeys, &h->r_scnt, &h->r_hist, &h->r_hot_keys, &h->r_hot_part, &h->r_cursor, &h->r_part,
+                      &h->r_part2, &h->r_ovf})
+        b->release();
     h->topn_ids_a.release();
     h->topn_ids_b.release();
     h->topn_cnt.release();
@@ -1361,6 +1479,58 @@ void gb_agg_destroy(gb_agg *h) {
 }
 
 uint64_t gb_agg_kernel_launches(const gb_agg *h) { return h ? h->launches : 0; }
+
+gb_status gb_agg_set_option(gb_agg *h, const char *name, int64_t value) {
+    if (!h || !name) return GB_ERR_INVALID;
+    if (h->rows_ingested || h->finalized) {
+        set_error("options must be set before the first ingest (or after reset)");
+        return GB_ERR_STATE;
+    }
+    std::string n(name);
+    if (n == "mode") {
+        if (value < 0 || value > 2) {
+            set_error("mode must be 0 (auto), 1 (hash) or 2 (radix)");
+            return GB_ERR_INVALID;
+        }
+        h->mode_option = (int)value;
+        int old_mode = h->mode;
+        gb_apply_tuning(h);
+        if (h->mode_option == 2 && h->mode != 1) {
+            set_error("plan not eligible for radix mode (nullable value column or too many value columns)");
+            return GB_ERR_UNSUPPORTED;
+        }
+        if (h->mode != old_mode) {
+            u64 est = h->est_groups ? h->est_groups : (1u << 15);
+            h->cap = h->mode == 1 ? 4096 : std::max<u64>(1024, next_pow2(est * 2));
+            gb_status s = init_table(h, h->table, h->cap, 0);
+            if (s) return s;
+            GB_CUDA(cudaDeviceSynchronize());
+        }
+    } else if (n == "smem_slots") {
+        if (value < 0 || value > 8192 || (value & (value - 1))) {
+            set_error("smem_slots must be 0 or a power of two <= 8192");
+            return GB_ERR_INVALID;
+        }
+        h->smem_slots = (int)value;
+    } else if (n == "precombine") {
+        h->precombine = value != 0;
+    } else if (n == "ctas_per_sm") {
+        if (value < 1 || value > 4) return GB_ERR_INVALID;
+        h->ctas_per_sm = (int)value;
+    } else if (n == "tile_rows") {
+        if (value < 512 || value > (1 << 20) || value % 512) return GB_ERR_INVALID;
+        h->tile_rows = (u32)value;
+    } else if (n == "hot_slots") {
+        if (h->mode != 1 || value < 0 || value > h->rplan.HS || (value & (value - 1))) return GB_ERR_INVALID;
+        h->rplan.HS = (int)value;
+    } else {
+        set_error("unknown option '%s'", name);
+        return GB_ERR_INVALID;
+    }
+    return GB_OK;
+}
+
+int32_t gb_agg_get_mode(const gb_agg *h) { return h ? h->mode : -1; }
 
 gb_status gb_agg_set_profiling(gb_agg *h, int32_t on) {
     if (!h) return GB_ERR_INVALID;
@@ -1456,4 +1626,10 @@ void gb_apply_tuning(gb_agg *h) {
     h->smem_slots = (int)S;
     h->ctas_per_sm = 2;
     h->block = 512;
+    // radix mode for high-cardinality keys
+    h->mode = 0;
+    bool want_radix = h->mode_option == 2 || (h->mode_option == 0 && h->est_groups >= (1u << 20));
+    if (want_radix && radix_prepare(h->plan, h->rplan, std::max<u64>(h->est_groups, 1u << 16), h->nullable_mask) ==
+                          GB_OK)
+        h->mode = 1;
 }

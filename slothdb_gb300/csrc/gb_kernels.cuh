@@ -269,4 +269,104 @@ __device__ __forceinline__ void warp_rows(const Plan &P, const TableRef &T, Smem
     if (!smem_fold(P, sm, pk, h, cnt, v)) global_fold(P, T, pk, cnt, v, new_groups);
 }
 
+// ------------------------------------------------------------ emit
+struct EmitAgg {
+    int32_t kind;      // gb_agg_kind
+    int32_t in_type;   // gb_type of the input column (-1 for COUNT(*))
+    int32_t out_type;  // gb_type of the output column
+    int32_t val_word;  // state word of the value (-1 none)
+    int32_t cnt_word;  // state word of the non-NULL count
+    int32_t pad;
+};
+
+struct EmitArgs {
+    EmitAgg aggs[GB_MAX_AGGS];
+    void *out[2 + GB_MAX_AGGS];        // device column buffers
+    uint64_t *valid[2 + GB_MAX_AGGS];  // validity words (pre-set to all ones)
+    int32_t n_aggs;
+    int32_t n_keys;
+    u64 out_cap;
+};
+
+__device__ __forceinline__ void store_int(void *base, int type, u64 i, i64 v) {
+    switch (type) {
+    case GB_T_SMALLINT: ((int16_t *)base)[i] = (int16_t)v; break;
+    case GB_T_INTEGER: ((int32_t *)base)[i] = (int32_t)v; break;
+    default: ((long long *)base)[i] = v; break;
+    }
+}
+
+__device__ __forceinline__ void clear_valid(uint64_t *vw, u64 i) {
+    atomicAnd((unsigned long long *)(vw + (i >> 6)), ~(1ull << (i & 63)));
+}
+
+__device__ __forceinline__ i64 sext(u64 x, int bits) {
+    if (bits >= 64) return (i64)x;
+    u64 m = 1ull << (bits - 1);
+    x &= (1ull << bits) - 1ull;
+    return (i64)((x ^ m) - m);
+}
+
+
+// Write one group's result row `o` (key columns + finalised aggregates,
+// agg_emit_helpers.cpp:26-98 rules).  `w` = the group's state words.
+__device__ __forceinline__ void emit_group(const Plan &P, const EmitArgs &E, u64 o, u64 pk, bool null_key,
+                                           const u64 *w) {
+    if (P.key_mode == KEY_SINGLE || P.key_mode == KEY_STRING) {
+        store_int(E.out[0], P.key_type[0], o, (i64)pk);
+        if (null_key) clear_valid(E.valid[0], o);
+    } else if (P.key_mode == KEY_PACKED) {
+        const int bb = P.key_bits_b, ba = P.key_bits_a;
+        i64 a = sext(pk >> bb, ba), b = sext(pk, bb);
+        bool na = (pk >> (ba + bb)) & 1ull, nb = (pk >> (ba + bb + 1)) & 1ull;
+        store_int(E.out[0], P.key_type[0], o, a);
+        store_int(E.out[1], P.key_type[1], o, b);
+        if (na) clear_valid(E.valid[0], o);
+        if (nb) clear_valid(E.valid[1], o);
+    } else {
+        store_int(E.out[0], P.key_type[0], o, (i64)(int32_t)(uint32_t)(pk >> 32));
+        store_int(E.out[1], P.key_type[1], o, (i64)(int32_t)(uint32_t)pk);
+    }
+    for (int a = 0; a < E.n_aggs; a++) {
+        const EmitAgg &g = E.aggs[a];
+        void *dst = E.out[E.n_keys + a];
+        uint64_t *vw = E.valid[E.n_keys + a];
+        const u64 cnt = w[g.cnt_word];
+        switch (g.kind) {
+        case GB_AGG_COUNT_STAR:
+        case GB_AGG_COUNT: ((long long *)dst)[o] = (i64)cnt; break;
+        case GB_AGG_SUM:
+            if (cnt == 0) { ((long long *)dst)[o] = 0; clear_valid(vw, o); }
+            else ((long long *)dst)[o] = (i64)w[g.val_word];  // int64 or double bits
+            break;
+        case GB_AGG_AVG:
+            if (cnt == 0) { ((double *)dst)[o] = 0.0; clear_valid(vw, o); }
+            else {
+                double sum = (g.in_type == GB_T_DOUBLE) ? __longlong_as_double((i64)w[g.val_word])
+                                                        : (double)(i64)w[g.val_word];
+                ((double *)dst)[o] = sum / (double)cnt;
+            }
+            break;
+        default:  // MIN / MAX
+            if (cnt == 0) {
+                store_int(dst, g.out_type == GB_T_DOUBLE ? GB_T_BIGINT : g.out_type, o, 0);
+                clear_valid(vw, o);
+            } else if (g.out_type == GB_T_DOUBLE) ((double *)dst)[o] = dec_f64((i64)w[g.val_word]);
+            else store_int(dst, g.out_type, o, (i64)w[g.val_word]);
+            break;
+        }
+    }
+}
+
+// Reserve `n` output rows for a warp's occupied lanes (ballot + one atomic).
+__device__ __forceinline__ u64 warp_out_slot(Ctl *ctl, bool occ, unsigned active) {
+    const int lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(active, occ);
+    u32 base = 0;
+    const int leader = __ffs(active) - 1;
+    if (lane == leader && m) base = atomicAdd(&ctl->out_count, (u32)__popc(m));
+    base = __shfl_sync(active, base, leader);
+    return (u64)base + __popc(m & ((1u << lane) - 1u));
+}
+
 }  // namespace gb

@@ -15,9 +15,12 @@ REL_TOL = 1e-12
 
 
 def run_gpu(col_types, group_cols, aggs, cols, filters=(), nulls=None, est_groups=0, device=False,
-            chunks=None, topn=None):
+            chunks=None, topn=None, mode=0):
     nullable = [i for i, m in enumerate(nulls or []) if m is not None]
-    g = capi.GroupBy(col_types, group_cols, aggs, filters=filters, nullable=nullable, est_groups=est_groups)
+    g = capi.GroupBy(col_types, group_cols, aggs, filters=filters, nullable=nullable, est_groups=est_groups,
+                     options={"mode": mode} if mode else None)
+    if mode == 2:
+        assert g.mode() == 1
     try:
         if topn:
             g.set_topn(*topn)
@@ -69,32 +72,36 @@ def check(col_types, group_cols, aggs, cols, **kw):
 
 
 PLAIN_AGGS = [("count_star", -1), ("sum", 1), ("min", 1), ("max", 1)]
+HASH, RADIX = 1, 2
 
 
-def test_plain_workload_1m_host_and_device():
+@pytest.mark.parametrize("mode", [HASH, RADIX])
+def test_plain_workload_1m_host_and_device(mode):
     k, v = datagen.plain(1_000_000, seed=0)
-    check([INTEGER, BIGINT], [0], PLAIN_AGGS, [k, v])
-    check([INTEGER, BIGINT], [0], PLAIN_AGGS, [k, v], device=True)
+    check([INTEGER, BIGINT], [0], PLAIN_AGGS, [k, v], mode=mode)
+    check([INTEGER, BIGINT], [0], PLAIN_AGGS, [k, v], device=True, mode=mode)
 
 
+@pytest.mark.parametrize("mode", [HASH, RADIX])
 @pytest.mark.parametrize("n", [0, 1, 31, 32, 33, 2047, 2048, 2049, 122_880 + 7])
-def test_ragged_sizes(n):
+def test_ragged_sizes(n, mode):
     k, v = datagen.plain(max(n, 1), seed=11, n_keys=97)
     k, v = k[:n], v[:n]
     if n == 0:
-        gpu = run_gpu([INTEGER, BIGINT], [0], PLAIN_AGGS, [k, v])
+        gpu = run_gpu([INTEGER, BIGINT], [0], PLAIN_AGGS, [k, v], mode=mode)
         assert len(gpu["keys"][0]) == 0
         return
-    check([INTEGER, BIGINT], [0], PLAIN_AGGS, [k, v])
+    check([INTEGER, BIGINT], [0], PLAIN_AGGS, [k, v], mode=mode)
 
 
-def test_all_distinct_and_single_group():
+@pytest.mark.parametrize("mode", [HASH, RADIX])
+def test_all_distinct_and_single_group(mode):
     n = 300_000
     rng = np.random.default_rng(3)
     k = rng.permutation(n).astype(np.int64) * 7919 - 10**12
     v = rng.integers(-10**9, 10**9, n, dtype=np.int64)
-    check([BIGINT, BIGINT], [0], PLAIN_AGGS, [k, v], est_groups=n)
-    check([BIGINT, BIGINT], [0], PLAIN_AGGS, [np.full(n, 42, np.int64), v])
+    check([BIGINT, BIGINT], [0], PLAIN_AGGS, [k, v], est_groups=n, mode=mode)
+    check([BIGINT, BIGINT], [0], PLAIN_AGGS, [np.full(n, 42, np.int64), v], mode=mode)
 
 
 def test_table_growth_from_tiny_estimate():
@@ -107,17 +114,29 @@ def test_table_growth_from_tiny_estimate():
     check([BIGINT, BIGINT], [0], PLAIN_AGGS, [k, v], est_groups=16)
 
 
-def test_zipf_double_sum_avg_tolerance():
+def test_radix_partition_growth_over_many_chunks():
+    """The first chunk sizes the partitions; later chunks overflow them, so
+    the overflow list, partition regrowth and drain must keep every row."""
+    n = 1_500_000
+    rng = np.random.default_rng(14)
+    k = rng.integers(0, 400_000, n, dtype=np.int64)
+    v = rng.integers(0, 10**6, n, dtype=np.int64)
+    check([BIGINT, BIGINT], [0], PLAIN_AGGS, [k, v], est_groups=16, chunks=65536, mode=RADIX)
+
+
+@pytest.mark.parametrize("mode", [HASH, RADIX])
+def test_zipf_double_sum_avg_tolerance(mode):
     k, x = datagen.zipf(2_000_000, seed=1, n_values=400_000)
     err, gpu, orc = check([BIGINT, DOUBLE], [0], [("count_star", -1), ("sum", 1), ("avg", 1)], [k, x],
-                          est_groups=400_000)
+                          est_groups=400_000, mode=mode)
     assert err <= REL_TOL
 
 
-def test_zipf_topn_count_desc():
+@pytest.mark.parametrize("mode", [HASH, RADIX])
+def test_zipf_topn_count_desc(mode):
     k, x = datagen.zipf(2_000_000, seed=1, n_values=400_000)
     aggs = [("count_star", -1), ("sum", 1), ("avg", 1)]
-    gpu = run_gpu([BIGINT, DOUBLE], [0], aggs, [k, x], topn=(1, False, 10), est_groups=400_000)
+    gpu = run_gpu([BIGINT, DOUBLE], [0], aggs, [k, x], topn=(1, False, 10), est_groups=400_000, mode=mode)
     orc = oracle.run_query([BIGINT, DOUBLE], [0], aggs, [k, x])
     cnt = orc["aggs"][0][0]
     order = np.lexsort((orc["keys"][0], -cnt))[:10]
@@ -153,9 +172,11 @@ def test_nulls_in_keys_and_values():
           [k, v], nulls=[kn, vn], chunks=65536)
 
 
-def test_composite_int32_int16_key_batched_shape():
+@pytest.mark.parametrize("mode", [HASH, RADIX])
+def test_composite_int32_int16_key_batched_shape(mode):
     a, b, s, m = datagen.composite(400_000, 50_000, seed=3)
-    check([INTEGER, SMALLINT, BIGINT, INTEGER], [0, 1], [("count_star", -1), ("sum", 2), ("max", 3)], [a, b, s, m])
+    check([INTEGER, SMALLINT, BIGINT, INTEGER], [0, 1], [("count_star", -1), ("sum", 2), ("max", 3)], [a, b, s, m],
+          mode=mode)
 
 
 def test_composite_with_nulls_and_wide_pair():
@@ -172,7 +193,8 @@ def test_composite_with_nulls_and_wide_pair():
     check([INTEGER, INTEGER, BIGINT], [0, 1], [("count_star", -1), ("min", 2)], [c, d, s])
 
 
-def test_filters_int_and_double():
+@pytest.mark.parametrize("mode", [HASH, RADIX])
+def test_filters_int_and_double(mode):
     n = 500_000
     rng = np.random.default_rng(9)
     k = rng.integers(0, 5000, n, dtype=np.int32)
@@ -180,18 +202,30 @@ def test_filters_int_and_double():
     v = rng.integers(-10**9, 10**9 + 1, n, dtype=np.int64)
     x = rng.normal(0, 1, n)
     check([INTEGER, SMALLINT, BIGINT, DOUBLE], [0], [("sum", 2), ("count_star", -1)], [k, f, v, x],
-          filters=[(1, "<", 100)])
+          filters=[(1, "<", 100)], mode=mode)
     check([INTEGER, SMALLINT, BIGINT, DOUBLE], [0], [("sum", 2), ("min", 3), ("max", 3)], [k, f, v, x],
-          filters=[(3, ">=", 0.5), (1, "!=", 7)])
+          filters=[(3, ">=", 0.5), (1, "!=", 7)], mode=mode)
 
 
-def test_special_key_values_and_smallint():
+@pytest.mark.parametrize("mode", [HASH, RADIX])
+def test_special_key_values_and_smallint(mode):
     k = np.array([np.iinfo(np.int64).min, 0, -1, np.iinfo(np.int64).max, np.iinfo(np.int64).min, -1], dtype=np.int64)
     v = np.arange(6, dtype=np.int64)
-    check([BIGINT, BIGINT], [0], PLAIN_AGGS, [k, v])
+    check([BIGINT, BIGINT], [0], PLAIN_AGGS, [k, v], mode=mode)
     ks = np.array([-32768, 32767, 0, -32768], dtype=np.int16)
     vd = np.array([-1.5, 2.25, -0.0, 7.0])
-    check([SMALLINT, DOUBLE], [0], [("min", 1), ("max", 1), ("sum", 1), ("count", 1)], [ks, vd])
+    check([SMALLINT, DOUBLE], [0], [("min", 1), ("max", 1), ("sum", 1), ("count", 1)], [ks, vd], mode=mode)
+
+
+def test_radix_null_keys_and_mode_rejection():
+    n = 100_000
+    rng = np.random.default_rng(15)
+    k = rng.integers(0, 20_000, n, dtype=np.int64)
+    kn = rng.random(n) < 0.02
+    v = rng.integers(0, 100, n, dtype=np.int64)
+    check([BIGINT, BIGINT], [0], PLAIN_AGGS, [k, v], nulls=[kn, None], mode=RADIX)
+    with pytest.raises(capi.GbError):
+        capi.GroupBy([BIGINT, BIGINT], [0], PLAIN_AGGS, nullable=[1], options={"mode": RADIX})
 
 
 def test_many_chunks_accumulate():
