@@ -156,30 +156,38 @@ __global__ void k_merge_records(const __grid_constant__ Plan P, const u64 *recs,
 
 // Compact used slots into dense result columns (the direct emit of
 // physical_planner.cpp:8027-8173 with agg_emit_helpers.cpp:26-165 rules).
+// Each CTA takes chunks of COMPACT_PER * blockDim slots; one output
+// reservation per chunk.
+#define COMPACT_PER 8
 __global__ void k_compact(const __grid_constant__ Plan P, const u64 *slots, u64 cap, int stride,
                           const __grid_constant__ EmitArgs E, Ctl *ctl) {
-    const int lane = threadIdx.x & 31;
     const u64 total = cap + 2;
-    const u64 step = (u64)gridDim.x * blockDim.x;
-    for (u64 base = blockIdx.x * (u64)blockDim.x + threadIdx.x - lane; base < total; base += step) {
-        const u64 s = base + lane;
-        bool occ = false;
-        const u64 *sl = slots + s * (u64)stride;
-        if (s < cap) occ = sl[0] != EMPTY_KEY;
-        else if (s < total) occ = sl[1] != 0;
-        const unsigned m = __ballot_sync(FULL, occ);
-        if (m == 0) continue;
-        u32 wbase = 0;
-        if (lane == 0) wbase = atomicAdd(&ctl->out_count, (u32)__popc(m));
-        wbase = __shfl_sync(FULL, wbase, 0);
-        if (!occ) continue;
-        const u64 o = wbase + __popc(m & ((1u << lane) - 1u));
-        if (o >= E.out_cap) {
-            atomicOr(&ctl->err, (u32)ERR_OUT_OVERFLOW);
-            continue;
+    const u64 chunk = (u64)COMPACT_PER * blockDim.x;
+    for (u64 c0 = blockIdx.x * chunk; c0 < total; c0 += (u64)gridDim.x * chunk) {
+        u32 mine = 0;
+#pragma unroll
+        for (int j = 0; j < COMPACT_PER; j++) {
+            const u64 s = c0 + (u64)j * blockDim.x + threadIdx.x;
+            if (s >= total) break;
+            const u64 *sl = slots + s * (u64)stride;
+            mine += (s < cap) ? (sl[0] != EMPTY_KEY) : (sl[1] != 0);
         }
-        const u64 pk = (s < cap) ? sl[0] : (s == cap ? EMPTY_KEY : 0ull);
-        emit_group(P, E, o, pk, s == cap + 1, sl + 1);
+        u64 o = block_out_base(ctl, mine);
+#pragma unroll
+        for (int j = 0; j < COMPACT_PER; j++) {
+            const u64 s = c0 + (u64)j * blockDim.x + threadIdx.x;
+            if (s >= total) break;
+            const u64 *sl = slots + s * (u64)stride;
+            const bool occ = (s < cap) ? (sl[0] != EMPTY_KEY) : (sl[1] != 0);
+            if (!occ) continue;
+            if (o >= E.out_cap) {
+                atomicOr(&ctl->err, (u32)ERR_OUT_OVERFLOW);
+                continue;
+            }
+            const u64 pk = (s < cap) ? sl[0] : (s == cap ? EMPTY_KEY : 0ull);
+            emit_group(P, E, o, pk, s == cap + 1, sl + 1);
+            o++;
+        }
     }
 }
 
@@ -368,7 +376,13 @@ struct DevBuf {
         n = 0;
         size_t want = std::max(bytes, (size_t)256);
         cudaError_t e = cudaMalloc(&p, want);
-        if (e != cudaSuccess) { p = nullptr; return cuda_fail(e, "cudaMalloc"); }
+        if (e != cudaSuccess) {
+            p = nullptr;
+            (void)cudaGetLastError();  // do not leave the failure as the runtime's last error
+            char what[96];
+            snprintf(what, sizeof what, "cudaMalloc(%zu bytes)", want);
+            return cuda_fail(e, what);
+        }
         n = want;
         return GB_OK;
     }
@@ -447,6 +461,10 @@ struct gb_agg {
     RadixPlan rplan{};
     bool r_ready = false;
     DevBuf r_skeys, r_scnt, r_hist, r_hot_keys, r_hot_part, r_cursor, r_part, r_part2, r_ovf;
+    DevBuf r_off, r_cap, r_off2, r_cap2;    // per-partition region start / capacity (device)
+    DevBuf r_hot_idx, r_hot_list, r_hstate;
+    std::vector<u64> h_off;                 // host copies
+    std::vector<u32> h_capv;
     u64 r_cap_p = 0;
     u32 r_ovf_cap = 0;
     int r_grid = 0;
@@ -729,7 +747,8 @@ static gb_status run_ingest(gb_agg *h, u64 n_rows, cudaStream_t st) {
 static RadixRef radix_ref(gb_agg *h) {
     RadixRef X;
     X.part = (u64 *)h->r_part.p;
-    X.cap_p = h->r_cap_p;
+    X.part_off = (const u64 *)h->r_off.p;
+    X.part_cap = (const u32 *)h->r_cap.p;
     X.cursor = (u32 *)h->r_cursor.p;
     X.ovf = (u64 *)h->r_ovf.p;
     X.ovf_cap = h->r_ovf_cap;
@@ -737,6 +756,8 @@ static RadixRef radix_ref(gb_agg *h) {
     const u64 inflight = (u64)h->r_grid * radix_tile_rows(h->rplan) + 4096;
     X.ovf_threshold = h->r_ovf_cap > inflight ? (u32)(h->r_ovf_cap - inflight) : 0u;
     X.hot_keys = (const u64 *)h->r_hot_keys.p;
+    X.hot_idx = (const uint16_t *)h->r_hot_idx.p;
+    X.hot_list = (const u64 *)h->r_hot_list.p;
     X.hot_part = (u64 *)h->r_hot_part.p;
     return X;
 }
@@ -751,34 +772,47 @@ static gb_status radix_begin(gb_agg *h, u64 n, cudaStream_t st) {
     u64 m = std::min<u64>(n, 1u << 18);
     u64 scap = 1024;
     while (scap < 2 * m) scap <<= 1;
-    if ((s = h->r_skeys.ensure(scap * 8)) || (s = h->r_scnt.ensure(scap * 4)) || (s = h->r_hist.ensure(260 * 4)) ||
-        (s = h->r_hot_keys.ensure((size_t)R.HS * 8)))
+    if ((s = h->r_skeys.ensure(scap * 8)) || (s = h->r_scnt.ensure(scap * 4)) ||
+        (s = h->r_hist.ensure(HIST_BINS * 4)) || (s = h->r_hstate.ensure(16)) ||
+        (s = h->r_hot_keys.ensure((size_t)R.HS * 8)) || (s = h->r_hot_idx.ensure((size_t)R.HS * 2)) ||
+        (s = h->r_hot_list.ensure((size_t)R.nh * 8)))
         return s;
-    GB_CUDA(cudaMemsetAsync(h->r_skeys.p, 0xff, scap * 8, st));
+    if ((s = radix_fill_u64((u64 *)h->r_skeys.p, scap, EMPTY_KEY, st))) return s;
     GB_CUDA(cudaMemsetAsync(h->r_scnt.p, 0, scap * 4, st));
-    GB_CUDA(cudaMemsetAsync(h->r_hist.p, 0, 260 * 4, st));
-    GB_CUDA(cudaMemsetAsync(h->r_hot_keys.p, 0xff, (size_t)R.HS * 8, st));
+    GB_CUDA(cudaMemsetAsync(h->r_hist.p, 0, HIST_BINS * 4, st));
+    GB_CUDA(cudaMemsetAsync(h->r_hstate.p, 0, 16, st));
+    GB_CUDA(cudaMemsetAsync(h->r_hot_idx.p, 0, (size_t)R.HS * 2, st));
+    if ((s = radix_fill_u64((u64 *)h->r_hot_keys.p, R.HS, EMPTY_KEY, st))) return s;
+    h->launches += 2;
     {
         ProfScope ps(h, "k_sample", st);
         if ((s = radix_launch_sample(h->plan, R, n, (u64 *)h->r_skeys.p, (u32 *)h->r_scnt.p, scap,
-                                     (u32 *)h->r_hist.p, (u64 *)h->r_hot_keys.p, st, &h->launches)))
+                                     (u32 *)h->r_hist.p, (u32 *)h->r_hstate.p, (u64 *)h->r_hot_keys.p,
+                                     (uint16_t *)h->r_hot_idx.p, (u64 *)h->r_hot_list.p, st, &h->launches)))
             return s;
     }
-    u32 hot_rows = 0;
-    GB_CUDA(cudaMemcpyAsync(&hot_rows, (u32 *)h->r_hist.p + 256, 4, cudaMemcpyDeviceToHost, st));
+    u32 hst[4] = {0, 0, 0, 0};
+    GB_CUDA(cudaMemcpyAsync(hst, h->r_hstate.p, 16, cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
+    u32 hot_rows = hst[2];
     u64 sampled = std::max<u64>(1, std::min<u64>(n, m));
     double hot_frac = std::min(1.0, (double)hot_rows / (double)sampled);
     double tail = (double)n * (1.0 - hot_frac);
     u64 cap_p = (u64)(tail / (double)np * 1.25) + 2048;
     cap_p = (cap_p + 31) / 32 * 32;
-    if (cap_p > h->r_cap_p || !h->r_part.p) h->r_cap_p = cap_p;
-    if ((s = h->r_part.ensure((size_t)np * h->r_cap_p * TV * 8))) return s;
+    h->r_cap_p = cap_p;
+    h->h_off.assign(np + 1, 0);
+    h->h_capv.assign(np, (u32)cap_p);
+    for (u64 p = 0; p < np; p++) h->h_off[p + 1] = h->h_off[p] + cap_p;
+    if ((s = h->r_part.ensure((size_t)h->h_off[np] * TV * 8))) return s;
+    if ((s = h->r_off.ensure((np + 1) * 8)) || (s = h->r_cap.ensure(np * 4))) return s;
+    GB_CUDA(cudaMemcpyAsync(h->r_off.p, h->h_off.data(), (np + 1) * 8, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(h->r_cap.p, h->h_capv.data(), np * 4, cudaMemcpyHostToDevice, st));
     if ((s = h->r_cursor.ensure((size_t)np * CURSOR_PAD * 4))) return s;
     GB_CUDA(cudaMemsetAsync(h->r_cursor.p, 0, (size_t)np * CURSOR_PAD * 4, st));
     h->r_grid = sm_count();
-    if ((s = h->r_hot_part.ensure((size_t)h->r_grid * R.HS * W * 8))) return s;
-    if ((s = radix_fill_identity((u64 *)h->r_hot_part.p, (u64)h->r_grid * R.HS * W, W, h->plan, st))) return s;
+    if ((s = h->r_hot_part.ensure((size_t)h->r_grid * R.nh * W * 8))) return s;
+    if ((s = radix_fill_identity((u64 *)h->r_hot_part.p, (u64)h->r_grid * R.nh * W, W, h->plan, st))) return s;
     h->launches++;
     u32 ovf_cap = (1u << 21) + (u32)(h->r_grid * radix_tile_rows(R)) + 4096;
     if (h->r_ovf_cap < ovf_cap) {
@@ -789,8 +823,9 @@ static gb_status radix_begin(gb_agg *h, u64 n, cudaStream_t st) {
     return GB_OK;
 }
 
-// Grow the partition regions so every partition can take its overflow,
-// then append the overflow tuples.
+// Grow the regions of the partitions that overflowed (each to what it
+// needs, so one skewed partition does not inflate the others), move the
+// filled prefixes, then append the overflow tuples.
 static gb_status radix_grow(gb_agg *h, u32 novf, cudaStream_t st) {
     const RadixPlan &R = h->rplan;
     const u64 np = 1ull << R.pbits;
@@ -798,25 +833,46 @@ static gb_status radix_grow(gb_agg *h, u32 novf, cudaStream_t st) {
     std::vector<u32> cur((size_t)np * CURSOR_PAD);
     GB_CUDA(cudaMemcpyAsync(cur.data(), h->r_cursor.p, cur.size() * 4, cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
-    u64 need = 0;
+    std::vector<u64> noff(np + 1, 0);
+    std::vector<u32> ncap(np);
     for (u64 p = 0; p < np; p++) {
-        u64 c = cur[p * CURSOR_PAD];
-        need = std::max<u64>(need, c);
-        cur[p * CURSOR_PAD] = (u32)std::min<u64>(c, h->r_cap_p);  // tuples actually in the region
+        const u64 want = cur[p * CURSOR_PAD];
+        u64 c = h->h_capv[p];
+        if (want > c) c = std::max<u64>(c * 2, want + want / 4 + 256);
+        c = (c + 31) / 32 * 32;
+        if (c > 0xffffffffull) {
+            set_error("partition %llu exceeds 2^32 tuples", (unsigned long long)p);
+            return GB_ERR_UNSUPPORTED;
+        }
+        ncap[p] = (u32)c;
+        noff[p + 1] = noff[p] + c;
     }
-    u64 ncap = std::max<u64>(h->r_cap_p * 2, need + need / 4 + 1024);
-    ncap = (ncap + 31) / 32 * 32;
-    gb_status s = h->r_part2.ensure((size_t)np * ncap * TV * 8);
-    if (s) return s;
-    GB_CUDA(cudaMemcpy2DAsync(h->r_part2.p, ncap * TV * 8, h->r_part.p, h->r_cap_p * TV * 8, h->r_cap_p * TV * 8, np,
-                              cudaMemcpyDeviceToDevice, st));
-    std::swap(h->r_part, h->r_part2);
-    h->r_part2.release();
-    h->r_cap_p = ncap;
+    gb_status s;
+    if ((s = h->r_part2.ensure((size_t)noff[np] * TV * 8)) || (s = h->r_off2.ensure((np + 1) * 8)) ||
+        (s = h->r_cap2.ensure(np * 4)))
+        return s;
+    GB_CUDA(cudaMemcpyAsync(h->r_off2.p, noff.data(), (np + 1) * 8, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(h->r_cap2.p, ncap.data(), np * 4, cudaMemcpyHostToDevice, st));
+    RadixRef from = radix_ref(h);
+    RadixRef to = from;
+    to.part = (u64 *)h->r_part2.p;
+    to.part_off = (const u64 *)h->r_off2.p;
+    to.part_cap = (const u32 *)h->r_cap2.p;
+    if ((s = radix_launch_move(from, to, R.V, (int)np, st))) return s;
+    h->launches++;
+    // cursors := tuples actually stored in each region
+    for (u64 p = 0; p < np; p++) cur[p * CURSOR_PAD] = std::min<u32>(cur[p * CURSOR_PAD], h->h_capv[p]);
     GB_CUDA(cudaMemcpyAsync(h->r_cursor.p, cur.data(), cur.size() * 4, cudaMemcpyHostToDevice, st));
+    std::swap(h->r_part, h->r_part2);
+    std::swap(h->r_off, h->r_off2);
+    std::swap(h->r_cap, h->r_cap2);
+    h->h_off.swap(noff);
+    h->h_capv.swap(ncap);
     RadixRef X = radix_ref(h);
     if ((s = radix_launch_drain(X, R.V, novf, st))) return s;
     h->launches++;
+    GB_CUDA(cudaStreamSynchronize(st));
+    h->r_part2.release();
     Ctl *dctl = (Ctl *)h->ctl_buf.p;
     GB_CUDA(cudaMemsetAsync(&dctl->aux0, 0, 4, st));
     return GB_OK;
@@ -866,10 +922,20 @@ static gb_status radix_emit(gb_agg *h, cudaStream_t st) {
         std::vector<u32> cur((size_t)np * CURSOR_PAD);
         GB_CUDA(cudaMemcpyAsync(cur.data(), h->r_cursor.p, cur.size() * 4, cudaMemcpyDeviceToHost, st));
         GB_CUDA(cudaStreamSynchronize(st));
-        for (u64 p = 0; p < np; p++) tuples += std::min<u64>(cur[p * CURSOR_PAD], h->r_cap_p);
+        for (u64 p = 0; p < np; p++) tuples += std::min<u64>(cur[p * CURSOR_PAD], h->h_capv[p]);
     }
-    u64 cap = tuples + (u64)R.HS + h->cap + 2;
+    u64 cap = tuples + (u64)R.nh + h->cap + 2;
     if ((s = alloc_outputs(h, cap))) return s;
+    // a partition whose groups overflow its shared table folds the rest into
+    // the HBM table, which spills (at most once per tuple) when full
+    {
+        const u64 need = tuples + 4096;
+        if (h->spill_cap < need) {
+            if ((s = h->spill.ensure((size_t)need * (1 + h->plan.words) * 8))) return s;
+            h->spill_cap = (u32)need;
+        }
+        h->spill_threshold = h->spill_cap;
+    }
     for (size_t c = 0; c < h->out_valid.size(); c++)
         GB_CUDA(cudaMemsetAsync(h->out_valid[c].p, 0xff, (cap + 63) / 64 * 8, st));
     GB_CUDA(cudaMemsetAsync(&dctl->spill_count, 0, 4 * 4, st));
@@ -885,7 +951,7 @@ static gb_status radix_emit(gb_agg *h, cudaStream_t st) {
         }
         {
             ProfScope ps(h, "k_hot_emit", st);
-            if ((s = radix_launch_p3(h->plan, R, X, h->r_grid, dctl, E, st))) return s;
+            if ((s = radix_launch_p3(h->plan, R, X, h->r_grid, (const u32 *)h->r_hstate.p, dctl, E, st))) return s;
         }
         h->launches += 2;
         if ((s = read_ctl(h, st))) return s;
@@ -1345,8 +1411,8 @@ gb_status gb_agg_finalize(gb_agg *h, void *stream) {
     fill_emit(h, E, h->out_cols, h->out_valid, h->out_cap);
     {
         ProfScope ps(h, "k_compact", st);
-        k_compact<<<grid_for(h->cap + 2, 256, sm_count() * 8), 256, 0, st>>>(h->plan, (const u64 *)h->table.p,
-                                                                             h->cap, h->plan.stride, E, dctl);
+        k_compact<<<grid_for((h->cap + 2 + COMPACT_PER - 1) / COMPACT_PER, 256, sm_count() * 4), 256, 0, st>>>(
+            h->plan, (const u64 *)h->table.p, h->cap, h->plan.stride, E, dctl);
     }
     h->launches++;
     GB_CUDA(cudaGetLastError());
@@ -1456,7 +1522,8 @@ void gb_agg_destroy(gb_agg *h) {
     for (auto &b : h->top_cols) b.release();
     for (auto &b : h->top_valid) b.release();
     for (DevBuf *b : {&h->r_skeys, &h->r_scnt, &h->r_hist, &h->r_hot_keys, &h->r_hot_part, &h->r_cursor, &h->r_part,
-                      &h->r_part2, &h->r_ovf})
+                      &h->r_part2, &h->r_ovf, &h->r_off, &h->r_cap, &h->r_off2, &h->r_cap2, &h->r_hot_idx,
+                      &h->r_hot_list, &h->r_hstate})
         b->release();
     h->topn_ids_a.release();
     h->topn_ids_b.release();
@@ -1521,8 +1588,10 @@ gb_status gb_agg_set_option(gb_agg *h, const char *name, int64_t value) {
         if (value < 512 || value > (1 << 20) || value % 512) return GB_ERR_INVALID;
         h->tile_rows = (u32)value;
     } else if (n == "hot_slots") {
-        if (h->mode != 1 || value < 0 || value > h->rplan.HS || (value & (value - 1))) return GB_ERR_INVALID;
+        if (h->mode != 1 || value < 64 || value > h->rplan.HS || (value & (value - 1))) return GB_ERR_INVALID;
         h->rplan.HS = (int)value;
+        h->rplan.nh = std::min<int>(h->rplan.nh, (int)value / 2);
+        h->rplan.nsup = std::min<int>(h->rplan.nsup, h->rplan.nh);
     } else {
         set_error("unknown option '%s'", name);
         return GB_ERR_INVALID;

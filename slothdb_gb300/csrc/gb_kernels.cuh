@@ -358,6 +358,42 @@ __device__ __forceinline__ void emit_group(const Plan &P, const EmitArgs &E, u64
     }
 }
 
+// Block-cooperative output reservation: every thread of the block passes the
+// number of rows it will emit and gets the index of its first one; one global
+// atomic per block (a per-warp atomic on the single counter serialises).
+// Must be called by all threads of the block, blockDim.x a multiple of 32.
+__device__ __forceinline__ u64 block_out_base(Ctl *ctl, u32 mine) {
+    __shared__ u32 s_warp[32];
+    __shared__ u32 s_total;
+    __shared__ unsigned long long s_base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    u32 x = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const u32 y = __shfl_up_sync(FULL, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        u32 w = lane < nwarps ? s_warp[lane] : 0u;
+        u32 incl = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane < nwarps) s_warp[lane] = incl - w;
+        if (lane == 31) s_total = incl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_base = s_total ? atomicAdd(&ctl->out_count, s_total) : 0u;
+    __syncthreads();
+    const u64 r = s_base + s_warp[warp] + (x - mine);
+    __syncthreads();  // s_warp / s_base are reused by the next call
+    return r;
+}
+
 // Reserve `n` output rows for a warp's occupied lanes (ballot + one atomic).
 __device__ __forceinline__ u64 warp_out_slot(Ctl *ctl, bool occ, unsigned active) {
     const int lane = threadIdx.x & 31;

@@ -6,22 +6,31 @@
 // map, src/execution/simple_i64_count_map.hpp:20-109) generalised to every
 // aggregate of the plan, with a heavy-hitter stage in front:
 //
-//   S  sample:  a strided sample of the keys is counted; keys whose sample
-//               count clears a threshold form the "hot" set (at most HS/2).
-//   P1 scatter: persistent CTAs stream the rows (coalesced loads); a hot key
-//               is folded into the CTA's shared-memory hot table; any other
-//               row is scattered as a (key, values) tuple into partition
-//               p = top bits of its hash.  Per tile, partition slots are
-//               reserved with one global atomic per touched partition.
-//   P2 agg:     one CTA per partition folds the partition's tuples into a
-//               shared-memory open-addressing table and emits its groups.
-//   P3 hot:     per-CTA hot partials are reduced in a fixed order and the
-//               hot groups are emitted.
+//   S  sample:  a strided sample of the keys is counted; the NH most frequent
+//               keys become "hot" (dense hot index), the NSUP most frequent of
+//               them "super-hot".
+//   P1 scatter: persistent CTAs stream the rows.  A super-hot row is folded
+//               into its warp's PRIVATE state (warp pre-combine + plain
+//               read-modify-write); a warm hot row is forwarded through a
+//               shared-memory inbox to the warp that owns its hot index, which
+//               folds it without atomics; any other row is appended as a
+//               (key, values) tuple to partition p = top hash bits, into a
+//               per-CTA lease of that partition's region (one global atomic
+//               per lease of RADIX_LEASE tuples).
+//   P2 agg:     one CTA per partition; its shared table is split into 32
+//               sub-tables, one per warp, and each tuple is forwarded to the
+//               warp owning its key, so state words are updated without
+//               atomics.
+//   P3 hot:     per-CTA hot partials are reduced in a fixed order (hence a
+//               deterministic DOUBLE sum for hot keys) and emitted.
 //
-// A key is either hot for the whole query or never, and lives in exactly one
-// partition, so every group is emitted exactly once.  Bounded probes fall
-// back to the HBM hash table (whose groups are emitted by the compaction
-// kernel), which keeps the result exact whatever the key distribution.
+// Shared-memory 64-bit atomics are avoided on every hot path: on sm_103a
+// they are compare-and-swap loops that collapse under the Zipf head's
+// contention, while 32-bit shared atomics are native.  A key is hot for the
+// whole query or never, and lives in exactly one partition and one warp's
+// sub-table, so every group is emitted exactly once.  Bounded probes fall back
+// to the HBM hash table (emitted by the compaction kernel), which keeps the
+// result exact for any key distribution.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -61,95 +70,238 @@ __global__ void k_sample_count(const __grid_constant__ Plan P, u64 n, u64 step, 
 }
 
 __global__ void k_sample_hist(const u64 *skeys, const u32 *scnt, u64 scap, u32 *hist) {
-    __shared__ u32 h[256];
-    for (int i = threadIdx.x; i < 256; i += blockDim.x) h[i] = 0;
+    __shared__ u32 h[HIST_BINS];
+    for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x) h[i] = 0;
     __syncthreads();
     for (u64 s = blockIdx.x * (u64)blockDim.x + threadIdx.x; s < scap; s += (u64)gridDim.x * blockDim.x)
-        if (skeys[s] != EMPTY_KEY) atomicAdd(&h[min(scnt[s], 255u)], 1u);
+        if (skeys[s] != EMPTY_KEY) atomicAdd(&h[min(scnt[s], (u32)(HIST_BINS - 1))], 1u);
     __syncthreads();
-    for (int i = threadIdx.x; i < 256; i += blockDim.x)
+    for (int i = threadIdx.x; i < HIST_BINS; i += blockDim.x)
         if (h[i]) atomicAdd(&hist[i], h[i]);
 }
 
-// Keys with sample count >= t (the smallest t >= min_count that admits at
-// most hot_max keys) go into the hot table.  hist[256] += sampled rows
-// covered by hot keys, for sizing the partitions.
-__global__ void k_hot_build(const u64 *skeys, const u32 *scnt, u64 scap, u32 *hist, u32 min_count, u32 hot_max,
-                            u64 *hot_keys, int HS) {
-    __shared__ u32 s_t;
-    __shared__ u32 s_rows;
+// The smallest t >= floor_t admitting at most `cap` keys with sample count
+// >= t (HIST_BINS = none).
+__device__ __forceinline__ u32 count_threshold(const u32 *hist, u32 cap, u32 floor_t) {
+    u32 cum = 0, t = HIST_BINS;
+    for (int c = HIST_BINS - 1; c >= (int)floor_t; c--) {
+        if (cum + hist[c] > cap) break;
+        cum += hist[c];
+        t = c;
+    }
+    return t;
+}
+
+// Build the hot table (HS slots: key, dense hot index) and the hot list.
+// hstate[0] = super-hot keys assigned, hstate[1] = warm keys assigned,
+// hstate[2] = sampled rows covered by hot keys.
+__global__ void k_hot_build(const u64 *skeys, const u32 *scnt, u64 scap, const u32 *hist, u32 *hstate, int NSUP,
+                            int NH, u64 *hot_keys, uint16_t *hot_idx, u64 *hot_list, int HS) {
+    __shared__ u32 s_t, s_ts;
     if (threadIdx.x == 0) {
-        u32 cum = 0, t = 256;
-        for (int c = 255; c >= (int)min_count; c--) {
-            if (cum + hist[c] > hot_max) break;
-            cum += hist[c];
-            t = c;
-        }
-        s_t = t;
-        s_rows = 0;
+        s_t = count_threshold(hist, (u32)NH, 2);
+        s_ts = count_threshold(hist, (u32)NSUP, max(2u, s_t));
     }
     __syncthreads();
-    const u32 t = s_t;
+    const u32 t = s_t, ts = s_ts;
+    if (t >= HIST_BINS) return;
     for (u64 s = blockIdx.x * (u64)blockDim.x + threadIdx.x; s < scap; s += (u64)gridDim.x * blockDim.x) {
-        u64 k = skeys[s];
-        if (k == EMPTY_KEY || scnt[s] < t || t > 255) continue;
-        atomicAdd(&s_rows, scnt[s]);
+        const u64 k = skeys[s];
+        if (k == EMPTY_KEY) continue;
+        const u32 c = min(scnt[s], (u32)(HIST_BINS - 1));
+        if (c < t) continue;
+        u32 idx;
+        if (c >= ts && ts < HIST_BINS) {
+            idx = atomicAdd(&hstate[0], 1u);
+            if (idx >= (u32)NSUP) continue;  // cannot happen: the threshold admits <= NSUP
+        } else {
+            idx = atomicAdd(&hstate[1], 1u) + (u32)NSUP;
+            if (idx >= (u32)NH) continue;
+        }
+        atomicAdd(&hstate[2], scnt[s]);
+        hot_list[idx] = k;
         u32 h = hot_slot(mix64(k), HS);
         for (int p = 0; p < HS; p++) {
-            u64 old = atomicCAS(&hot_keys[h], EMPTY_KEY, k);
-            if (old == EMPTY_KEY || old == k) break;
+            const u64 old = atomicCAS(&hot_keys[h], EMPTY_KEY, k);
+            if (old == EMPTY_KEY) {
+                hot_idx[h] = (uint16_t)idx;
+                break;
+            }
             h = (h + 1) & (u32)(HS - 1);
         }
     }
-    __syncthreads();
-    if (threadIdx.x == 0 && s_rows) atomicAdd(&hist[256], s_rows);
 }
 
-// ------------------------------------------------------------- P1 scatter
+// ------------------------------------------------------------- helpers
+template <int VV>
 __device__ __forceinline__ void tuple_vals(const Plan &P, const RadixPlan &R, u64 r, u64 *tv) {
 #pragma unroll
-    for (int j = 0; j < RADIX_MAX_V; j++) {
-        if (j < R.V) {
-            const DevCol &c = P.cols[R.vcol[j]];
-            tv[j] = (c.type == GB_T_DOUBLE) ? (u64)__double_as_longlong(load_f64(c, r)) : (u64)load_int(c, r);
-        }
+    for (int j = 0; j < VV; j++) {
+        const DevCol &c = P.cols[R.vcol[j]];
+        tv[j] = (c.type == GB_T_DOUBLE) ? (u64)__double_as_longlong(load_f64(c, r)) : (u64)load_int(c, r);
     }
+}
+
+template <int VV>
+__device__ __forceinline__ u64 tv_pick(const u64 *tv, int j) {
+    if (VV == 1) return tv[0];
+    if (VV == 2) return j == 0 ? tv[0] : tv[1];
+    return j == 0 ? tv[0] : (j == 1 ? tv[1] : tv[2]);
 }
 
 // Per-op contributions of one tuple (value columns are NOT NULL here).
+template <int VV, int NOPS>
 __device__ __forceinline__ void tuple_contrib(const Plan &P, const RadixPlan &R, const u64 *tv, u64 *v) {
 #pragma unroll
-    for (int i = 0; i < GB_MAX_OPS; i++) {
-        if (i < P.n_ops) {
-            const u64 x = tv[R.op_v[i]];
-            switch (P.ops[i].kind) {
-            case OP_MIN_F:
-            case OP_MAX_F: v[i] = (u64)enc_f64(__longlong_as_double((i64)x)); break;
-            case OP_CNT_NN: v[i] = 1ull; break;
-            default: v[i] = x; break;
-            }
+    for (int i = 0; i < NOPS; i++) {
+        const u64 x = tv_pick<VV>(tv, R.op_v[i]);
+        switch (P.ops[i].kind) {
+        case OP_MIN_F:
+        case OP_MAX_F: v[i] = (u64)enc_f64(__longlong_as_double((i64)x)); break;
+        case OP_CNT_NN: v[i] = 1ull; break;
+        default: v[i] = x; break;
         }
     }
 }
 
-template <int ROWS, int VV>
-__global__ void __launch_bounds__(1024, 1) k_partition(const __grid_constant__ Plan P, const __grid_constant__ RadixPlan R,
-                                                       const RadixRef X, const TableRef T, const RadixTile A) {
-    extern __shared__ u64 rsm[];
-    const int HS = R.HS, W = P.words, NP = 1 << R.pbits;
-    u64 *hk = rsm;                         // HS hot keys
-    u64 *hs = rsm + HS;                    // HS * W hot states
-    u32 *s_hist = (u32 *)(hs + (u64)HS * W);
-    u32 *s_base = s_hist + NP;
-    __shared__ u32 s_tile;
-    for (int i = threadIdx.x; i < HS; i += blockDim.x) {
-        hk[i] = X.hot_keys ? X.hot_keys[i] : EMPTY_KEY;
-        for (int w = 0; w < W; w++) hs[(u64)i * W + w] = P.word_init[w];
+// Plain (non-atomic) fold of a combined partial into state words owned by
+// the calling lane.
+template <int NOPS>
+__device__ __forceinline__ void fold_plain(const Plan &P, u64 *w, u64 cnt, const u64 *v) {
+    w[0] += cnt;
+#pragma unroll
+    for (int i = 0; i < NOPS; i++) w[P.ops[i].word] = op_combine(P.ops[i].kind, w[P.ops[i].word], v[i]);
+}
+
+template <int NOPS>
+__device__ __forceinline__ void fold_atomic(const Plan &P, u64 *w, u64 cnt, const u64 *v) {
+    atomicAdd(w, cnt);
+#pragma unroll
+    for (int i = 0; i < NOPS; i++) op_apply(P.ops[i].kind, w + P.ops[i].word, v[i], P.word_init[P.ops[i].word]);
+}
+
+template <int NOPS>
+__device__ __forceinline__ void global_fold_n(const Plan &P, const TableRef &T, u64 pk, u64 cnt, const u64 *v,
+                                              u32 *new_groups) {
+    u64 vv[GB_MAX_OPS];
+#pragma unroll
+    for (int i = 0; i < GB_MAX_OPS; i++) vv[i] = i < NOPS ? v[i < NOPS ? i : 0] : 0;
+    global_fold(P, T, pk, cnt, vv, new_groups);
+}
+
+// Warp segmented combine: lanes with equal `id` (among `act` lanes) fold
+// their partials into the lowest such lane (the leader).  Returns the leader
+// flag; cnt = group size.
+template <int NOPS>
+__device__ __forceinline__ bool warp_combine(const Plan &P, bool act, u64 id, u64 *v, u64 &cnt) {
+    const int lane = threadIdx.x & 31;
+    const unsigned am = __ballot_sync(FULL, act);
+    const unsigned peers = __match_any_sync(FULL, id) & am;
+    const bool leader = act && ((__ffs(peers) - 1) == lane);
+    unsigned rem = leader ? (peers & ~(1u << lane)) : 0u;
+    const int maxit = __reduce_max_sync(FULL, (unsigned)__popc(rem));
+    for (int it = 0; it < maxit; it++) {
+        const int src = rem ? (__ffs(rem) - 1) : lane;
+        rem &= rem - 1u;
+#pragma unroll
+        for (int q = 0; q < NOPS; q++) {
+            const u64 o = __shfl_sync(FULL, v[q], src);
+            if (src != lane) v[q] = op_combine(P.ops[q].kind, v[q], o);
+        }
     }
-    for (int i = threadIdx.x; i < NP; i += blockDim.x) s_hist[i] = 0;
+    cnt = __popc(peers);
+    return leader;
+}
+
+template <int VV>
+__device__ __forceinline__ void put_tuple(u64 *dst, u64 pk, const u64 *tv) {
+    dst[0] = pk;
+#pragma unroll
+    for (int q = 0; q < VV; q++) dst[1 + q] = tv[q];
+}
+
+template <int VV>
+__device__ __forceinline__ void put_overflow(const RadixRef &X, const TableRef &T, u32 p, u64 pk, const u64 *tv) {
+    const u32 o = atomicAdd(&T.ctl->aux0, 1u);
+    if (o < X.ovf_cap) {
+        u64 *od = X.ovf + (u64)o * (VV + 2);
+        od[0] = p;
+        put_tuple<VV>(od + 1, pk, tv);
+    } else {
+        atomicOr(&T.ctl->err, (u32)ERR_SPILL_OVERFLOW);
+    }
+}
+
+// Write one tuple at region position `pos` of partition p (or overflow).
+template <int VV>
+__device__ __forceinline__ void store_at(const RadixRef &X, const TableRef &T, u32 p, u32 pos, u64 pk, const u64 *tv) {
+    if (pos < __ldg(&X.part_cap[p])) put_tuple<VV>(X.part + ((u64)__ldg(&X.part_off[p]) + pos) * (1 + VV), pk, tv);
+    else put_overflow<VV>(X, T, p, pk, tv);
+}
+
+// ------------------------------------------------------------- P1 scatter
+// Block: P1_WARPS warps, ROWS rows per thread per tile.  The NPRIV hottest
+// keys have a private state per warp (u32 count + W-1 words, plain updates
+// after a warp pre-combine); the other hot keys share one state per CTA
+// (native u32 count atomics; their word atomics are rarely contended).
+template <int ROWS, int VV, int NOPS>
+__global__ void __launch_bounds__(P1_WARPS * 32, 1)
+    k_partition(const __grid_constant__ Plan P, const __grid_constant__ RadixPlan R, const RadixRef X,
+                const TableRef T, const RadixTile A) {
+    extern __shared__ u64 rsm[];
+    constexpr int TV = 1 + VV;
+    constexpr int NT = P1_WARPS * 32;
+    const int HS = R.HS, W = P.words, NP = 1 << R.pbits, NH = R.nh, NPRIV = R.nsup, NWARM = R.nh - R.nsup;
+    const int B = R.wcb;
+    const int WM = W - 1;  // state words besides the count
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    u64 *hk = rsm;                                        // [HS] hot keys
+    u64 *pw = hk + HS;                                    // [P1_WARPS][NPRIV][WM] private words
+    u64 *sw = pw + (size_t)P1_WARPS * NPRIV * WM;         // [NWARM][WM] shared words
+    u64 *wbuf = sw + (size_t)NWARM * WM;                  // [NP][B][TV] write-combining buffers
+    u32 *pc = (u32 *)(wbuf + (size_t)NP * B * TV);        // [P1_WARPS][NPRIV] private counts
+    u32 *sc = pc + P1_WARPS * NPRIV;                      // [NWARM] shared counts
+    u32 *bcnt = sc + NWARM;                               // [NP] buffered tuples
+    u32 *sbase = bcnt + NP;                               // [NP] flush base this tile
+    u32 *snf = sbase + NP;                                // [NP] tuples flushed this tile
+    uint16_t *hix = (uint16_t *)(snf + NP);               // [HS] hot index
+    __shared__ u32 s_tile;
+    for (int i = threadIdx.x; i < HS; i += NT) {
+        hk[i] = X.hot_keys[i];
+        hix[i] = X.hot_idx[i];
+    }
+    for (int i = threadIdx.x; i < P1_WARPS * NPRIV; i += NT) {
+        pc[i] = 0;
+        for (int w = 0; w < WM; w++) pw[(size_t)i * WM + w] = P.word_init[1 + w];
+    }
+    for (int i = threadIdx.x; i < NWARM; i += NT) {
+        sc[i] = 0;
+        for (int w = 0; w < WM; w++) sw[(size_t)i * WM + w] = P.word_init[1 + w];
+    }
+    for (int i = threadIdx.x; i < NP; i += NT) bcnt[i] = 0;
     __syncthreads();
-    const int TV = 1 + R.V;
-    for (;;) {
+    u32 *mypc = pc + warp * NPRIV;
+    u64 *mypw = pw + (size_t)warp * NPRIV * WM;
+    // the REG_HOT hottest keys accumulate in this lane's registers: no
+    // conflicts, no warp collectives
+    constexpr int NV = NOPS > 0 ? NOPS : 1;
+    u32 rc[REG_HOT];
+    u64 rw[REG_HOT][NV];
+#pragma unroll
+    for (int k = 0; k < REG_HOT; k++) {
+        rc[k] = 0;
+#pragma unroll
+        for (int i = 0; i < NV; i++) rw[k][i] = i < NOPS ? P.word_init[P.ops[i < NOPS ? i : 0].word] : 0;
+    }
+    // the next tile is claimed one tile ahead so the claim's latency overlaps work
+    if (threadIdx.x == 0) {
+        u32 c = atomicAdd(&T.ctl->tile_counter, 1u);
+        s_tile = c < A.n_tiles ? c : ~0u;
+    }
+    __syncthreads();
+    u32 tile = s_tile;
+    __syncthreads();
+    while (tile != ~0u) {
         if (threadIdx.x == 0) {
             u32 t = ~0u;
             if (*(volatile u32 *)&T.ctl->stop == 0) {
@@ -158,98 +310,184 @@ __global__ void __launch_bounds__(1024, 1) k_partition(const __grid_constant__ P
             }
             s_tile = t;
         }
-        __syncthreads();
-        const u32 tile = s_tile;
-        __syncthreads();
-        if (tile == ~0u) break;
-        const u64 t0 = (u64)(A.first_tile + tile) * (u64)(ROWS * blockDim.x);
-        const u64 t1 = min(A.n_rows, t0 + (u64)(ROWS * blockDim.x));
+        const u64 t0 = (u64)(A.first_tile + tile) * (u64)(ROWS * NT);
+        const u64 t1 = min(A.n_rows, t0 + (u64)(ROWS * NT));
         u64 pk[ROWS];
         u64 tv[ROWS][VV];
-        u32 pr[ROWS];  // partition << 16 | rank, ~0u = not a tail row
+        u32 pend[ROWS];  // partition + 1 of a tuple that did not fit the buffer
+        u32 pslot[ROWS];
+        int kinds[ROWS];
+        bool acts[ROWS];
+        // issue every load of the tile before any dependent work
 #pragma unroll
         for (int j = 0; j < ROWS; j++) {
-            const u64 r = t0 + (u64)j * blockDim.x + threadIdx.x;
-            pr[j] = ~0u;
-            if (r >= t1) continue;
-            if (P.n_filters && !pass_filters(P, r)) continue;
-            const int kind = make_key(P, r, pk[j]);
-            u64 tvf[RADIX_MAX_V];
-            tuple_vals(P, R, r, tvf);
-#pragma unroll
-            for (int q = 0; q < VV; q++) tv[j][q] = tvf[q];
-            u64 v[GB_MAX_OPS];
-            tuple_contrib(P, R, tvf, v);
-            if (kind != 0) {
-                if (kind == 3) atomicOr(&T.ctl->err, (u32)ERR_NULL_IN_WIDE_KEY);
-                else special_fold(P, T, kind, 1, v);
-                continue;
+            const u64 r = t0 + (u64)j * NT + threadIdx.x;
+            acts[j] = r < t1;
+            kinds[j] = 0;
+            pk[j] = 0;
+            if (acts[j]) {
+                kinds[j] = make_key(P, r, pk[j]);
+                tuple_vals<VV>(P, R, r, tv[j]);
             }
-            const u64 h = mix64(pk[j]);
-            bool hot = false;
-            if (HS) {
-                u32 s = hot_slot(h, HS);
-                for (int p = 0; p < R.hot_probe; p++) {
-                    const u64 k = hk[s];
-                    if (k == pk[j]) {
-                        apply_state(P, hs + (u64)s * W, 1, v);
-                        hot = true;
-                        break;
+        }
+#pragma unroll
+        for (int j = 0; j < ROWS; j++) {
+            const u64 r = t0 + (u64)j * NT + threadIdx.x;
+            pend[j] = 0;
+            pslot[j] = 0;
+            bool act = acts[j];
+            if (act && P.n_filters) act = pass_filters(P, r);
+            bool priv = false;
+            u32 hidx = 0;
+            u64 v[NOPS > 0 ? NOPS : 1];
+#pragma unroll
+            for (int q = 0; q < (NOPS > 0 ? NOPS : 1); q++) v[q] = 0;
+            if (act) {
+                const int kind = kinds[j];
+                tuple_contrib<VV, NOPS>(P, R, tv[j], v);
+                if (kind != 0) {
+                    if (kind == 3) {
+                        atomicOr(&T.ctl->err, (u32)ERR_NULL_IN_WIDE_KEY);
+                    } else {
+                        u64 *w = T.slots + (T.cap + (u64)(kind - 1)) * (u64)T.stride + 1;
+                        fold_atomic<NOPS>(P, w, 1, v);
                     }
-                    if (k == EMPTY_KEY) break;
-                    s = (s + 1) & (u32)(HS - 1);
+                } else {
+                    const u64 h = mix64(pk[j]);
+                    bool hot = false;
+                    if (HS) {
+                        u32 s = hot_slot(h, HS);
+                        for (int q = 0; q < R.hot_probe; q++) {
+                            const u64 k = hk[s];
+                            if (k == pk[j]) {
+                                hidx = hix[s];
+                                hot = true;
+                                break;
+                            }
+                            if (k == EMPTY_KEY) break;
+                            s = (s + 1) & (u32)(HS - 1);
+                        }
+                    }
+                    if (hot) {
+                        if (hidx < (u32)REG_HOT) {
+#pragma unroll
+                            for (int k = 0; k < REG_HOT; k++) {
+                                if (hidx == (u32)k) {
+                                    rc[k]++;
+#pragma unroll
+                                    for (int i = 0; i < NOPS; i++) rw[k][i] = op_combine(P.ops[i].kind, rw[k][i], v[i]);
+                                }
+                            }
+                        } else if ((int)hidx < NPRIV) {
+                            // warp-private state: only lanes of this warp contend
+                            atomicAdd(&mypc[hidx], 1u);
+#pragma unroll
+                            for (int i = 0; i < NOPS; i++)
+                                op_apply(P.ops[i].kind, mypw + (size_t)hidx * WM + (P.ops[i].word - 1), v[i],
+                                         P.word_init[P.ops[i].word]);
+                        } else {
+                            const u32 wi = hidx - NPRIV;
+                            atomicAdd(&sc[wi], 1u);
+#pragma unroll
+                            for (int i = 0; i < NOPS; i++)
+                                op_apply(P.ops[i].kind, sw + (size_t)wi * WM + (P.ops[i].word - 1), v[i],
+                                         P.word_init[P.ops[i].word]);
+                        }
+                    } else {
+                        const u32 p = part_of(h, R.pbits);
+                        const u32 slot = atomicAdd(&bcnt[p], 1u);
+                        if (slot < (u32)B) {
+                            put_tuple<VV>(wbuf + ((size_t)p * B + slot) * TV, pk[j], tv[j]);
+                        } else {
+                            pend[j] = p + 1;
+                            pslot[j] = slot;
+                        }
+                    }
                 }
             }
-            if (!hot) {
-                const u32 p = part_of(h, R.pbits);
-                const u32 rank = atomicAdd(&s_hist[p], 1u);
-                pr[j] = (p << 16) | rank;
+            (void)priv;
+        }
+        __syncthreads();
+        // flush full buffers: whole multiples of B tuples, aligned
+        for (int p = threadIdx.x; p < NP; p += NT) {
+            const u32 c = bcnt[p];
+            if (c >= (u32)B) {
+                const u32 nf = (c / (u32)B) * (u32)B;
+                const u32 base = atomicAdd(&X.cursor[(u64)p * CURSOR_PAD], nf);
+                sbase[p] = base;
+                snf[p] = nf;
+                bcnt[p] = c - nf;
+                const u64 *src = wbuf + (size_t)p * B * TV;
+                if (base + (u32)B <= __ldg(&X.part_cap[p])) {
+                    u64 *dst = X.part + ((u64)__ldg(&X.part_off[p]) + base) * TV;
+                    for (int q = 0; q < B * TV; q += 2)
+                        *(ulonglong2 *)(dst + q) = *(const ulonglong2 *)(src + q);
+                } else {
+                    for (int q = 0; q < B; q++) store_at<VV>(X, T, p, base + q, src[q * TV], src + q * TV + 1);
+                }
             }
         }
         __syncthreads();
-        for (int p = threadIdx.x; p < NP; p += blockDim.x) {
-            const u32 c = s_hist[p];
-            if (c) {
-                s_base[p] = atomicAdd(&X.cursor[(u64)p * CURSOR_PAD], c);
-                s_hist[p] = 0;
-            }
-        }
-        __syncthreads();
+        // tuples beyond the buffer: inside the flushed range they go straight
+        // to HBM, the rest become the buffer's new head
 #pragma unroll
         for (int j = 0; j < ROWS; j++) {
-            if (pr[j] == ~0u) continue;
-            const u32 p = pr[j] >> 16;
-            const u64 pos = (u64)s_base[p] + (pr[j] & 0xffffu);
-            if (pos < X.cap_p) {
-                u64 *dst = X.part + ((u64)p * X.cap_p + pos) * TV;
-                dst[0] = pk[j];
-#pragma unroll
-                for (int q = 0; q < VV; q++) dst[1 + q] = tv[j][q];
-            } else {
-                const u32 o = atomicAdd(&T.ctl->aux0, 1u);
-                if (o < X.ovf_cap) {
-                    u64 *dst = X.ovf + (u64)o * (TV + 1);
-                    dst[0] = p;
-                    dst[1] = pk[j];
-#pragma unroll
-                    for (int q = 0; q < VV; q++) dst[2 + q] = tv[j][q];
-                } else {
-                    atomicOr(&T.ctl->err, (u32)ERR_SPILL_OVERFLOW);
-                }
-            }
+            if (!pend[j]) continue;
+            const u32 p = pend[j] - 1;
+            const u32 slot = pslot[j];
+            if (slot < snf[p]) store_at<VV>(X, T, p, sbase[p] + slot, pk[j], tv[j]);
+            else put_tuple<VV>(wbuf + ((size_t)p * B + (slot - snf[p])) * TV, pk[j], tv[j]);
         }
         if (threadIdx.x == 0 && *(volatile u32 *)&T.ctl->aux0 > X.ovf_threshold) atomicExch(&T.ctl->stop, 1u);
+        __syncthreads();
+        tile = s_tile;
+        __syncthreads();
+    }
+    // final partial buffers: padded to B with holes (EMPTY_KEY) so every
+    // flush stays aligned; P2 skips the holes
+    for (int p = threadIdx.x; p < NP; p += NT) {
+        const u32 c = bcnt[p];
+        if (c == 0) continue;
+        const u32 base = atomicAdd(&X.cursor[(u64)p * CURSOR_PAD], (u32)B);
+        u64 *src = wbuf + (size_t)p * B * TV;
+        for (u32 q = c; q < (u32)B; q++) src[q * TV] = EMPTY_KEY;
+        for (int q = 0; q < B; q++) {
+            const u32 pos = base + q;
+            if (pos < __ldg(&X.part_cap[p]))
+                put_tuple<VV>(X.part + ((u64)__ldg(&X.part_off[p]) + pos) * TV, src[q * TV], src + q * TV + 1);
+            else if (q < (int)c)
+                put_overflow<VV>(X, T, p, src[q * TV], src + q * TV + 1);
+        }
+    }
+    // this lane's register accumulators join its warp's private states
+#pragma unroll
+    for (int k = 0; k < REG_HOT; k++) {
+        if (k < NPRIV && rc[k]) {
+            atomicAdd(&mypc[k], rc[k]);
+#pragma unroll
+            for (int i = 0; i < NOPS; i++)
+                op_apply(P.ops[i].kind, mypw + (size_t)k * WM + (P.ops[i].word - 1), rw[k][i],
+                         P.word_init[P.ops[i].word]);
+        }
     }
     __syncthreads();
-    // fold this CTA's hot partial states into its slice (launches of one
-    // handle run in stream order, so the read-modify-write is race free)
-    if (HS) {
-        u64 *hp = X.hot_part + (u64)blockIdx.x * HS * W;
-        for (u64 i = threadIdx.x; i < (u64)HS * W; i += blockDim.x) {
-            const int w = (int)(i % W);
-            const u64 a = hp[i], b = hs[i];
-            hp[i] = (w == 0) ? a + b : op_combine(R.word_kind[w], a, b);
+    // fold private and shared hot states into this CTA's slice
+    u64 *hp = X.hot_part + (u64)blockIdx.x * NH * W;
+    for (int i = threadIdx.x; i < NH; i += NT) {
+        u64 acc[GB_MAX_WORDS];
+        for (int w = 0; w < W; w++) acc[w] = hp[(size_t)i * W + w];
+        if (i < NPRIV) {
+            for (int wp = 0; wp < P1_WARPS; wp++) {
+                acc[0] += pc[wp * NPRIV + i];
+                const u64 *s = pw + ((size_t)wp * NPRIV + i) * WM;
+                for (int w = 1; w < W; w++) acc[w] = op_combine(R.word_kind[w], acc[w], s[w - 1]);
+            }
+        } else {
+            acc[0] += sc[i - NPRIV];
+            const u64 *s = sw + (size_t)(i - NPRIV) * WM;
+            for (int w = 1; w < W; w++) acc[w] = op_combine(R.word_kind[w], acc[w], s[w - 1]);
         }
+        for (int w = 0; w < W; w++) hp[(size_t)i * W + w] = acc[w];
     }
 }
 
@@ -260,102 +498,173 @@ __global__ void k_part_drain(const RadixRef X, int V, u32 n) {
         const u64 *src = X.ovf + i * (TV + 1);
         const u32 p = (u32)src[0];
         const u64 pos = atomicAdd(&X.cursor[(u64)p * CURSOR_PAD], 1u);
-        u64 *dst = X.part + ((u64)p * X.cap_p + pos) * TV;
+        u64 *dst = X.part + (X.part_off[p] + pos) * TV;
         for (int q = 0; q < TV; q++) dst[q] = src[1 + q];
     }
 }
 
+// Copy each partition's filled prefix into the (larger) regions of `to`.
+__global__ void k_part_move(const RadixRef from, const RadixRef to, int V) {
+    const int TV = 1 + V;
+    const u32 p = blockIdx.x;
+    const u64 n = (u64)min(from.cursor[(u64)p * CURSOR_PAD], from.part_cap[p]) * TV;
+    const u64 *src = from.part + from.part_off[p] * TV;
+    u64 *dst = to.part + to.part_off[p] * TV;
+    for (u64 i = threadIdx.x; i < n; i += blockDim.x) dst[i] = src[i];
+}
+
+__global__ void k_fill_u64(u64 *dst, u64 n, u64 value) {
+    for (u64 i = blockIdx.x * (u64)blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) dst[i] = value;
+}
+
 // ------------------------------------------------------------- P2 aggregate
-__global__ void __launch_bounds__(1024, 1) k_part_agg(const __grid_constant__ Plan P, const __grid_constant__ RadixPlan R,
-                                                      const RadixRef X, const TableRef T,
-                                                      const __grid_constant__ EmitArgs E, int SP) {
+// One CTA per partition: a shared open-addressing table (u64 keys, u32
+// counts, W-1 state words).  Warps pre-combine duplicate keys, then fold with
+// native u32 count atomics and (rarely contended) word atomics; no barriers
+// in the main loop.
+template <int VV, int NOPS>
+__global__ void __launch_bounds__(RADIX_BLOCK, 1)
+    k_part_agg(const __grid_constant__ Plan P, const __grid_constant__ RadixPlan R, const RadixRef X,
+               const TableRef T, const __grid_constant__ EmitArgs E, int SP) {
     extern __shared__ u64 rsm[];
-    const int W = P.words, TV = 1 + R.V;
-    u64 *keys = rsm;
-    u64 *st = rsm + SP;
+    constexpr int TV = 1 + VV;
+    constexpr int NV = NOPS > 0 ? NOPS : 1;
+    const int W = P.words, WM = W - 1;
+    const int lane = threadIdx.x & 31;
+    u64 *keys = rsm;                          // [SP]
+    u64 *wd = keys + SP;                      // [SP][WM]
+    u32 *cn = (u32 *)(wd + (size_t)SP * WM);  // [SP]
     __shared__ u32 s_new;
     for (int i = threadIdx.x; i < SP; i += blockDim.x) {
         keys[i] = EMPTY_KEY;
-        for (int w = 0; w < W; w++) st[(u64)i * W + w] = P.word_init[w];
+        cn[i] = 0;
+        for (int w = 0; w < WM; w++) wd[(size_t)i * WM + w] = P.word_init[1 + w];
     }
     if (threadIdx.x == 0) s_new = 0;
     __syncthreads();
     const u32 p = blockIdx.x;
-    const u64 n = min((u64)X.cursor[(u64)p * CURSOR_PAD], X.cap_p);
-    const u64 *base = X.part + (u64)p * X.cap_p * TV;
+    const u64 n = min((u64)X.cursor[(u64)p * CURSOR_PAD], (u64)X.part_cap[p]);
+    const u64 *base = X.part + X.part_off[p] * TV;
     volatile u64 *vk = keys;
-    for (u64 i = threadIdx.x; i < n; i += blockDim.x) {
-        const u64 *tp = base + i * TV;
-        const u64 pk = tp[0];
-        u64 tv[RADIX_MAX_V];
+    for (u64 b0 = threadIdx.x - lane; b0 < n; b0 += blockDim.x) {
+        const u64 i = b0 + lane;
+        bool act = false;
+        u64 pk = EMPTY_KEY ^ (u64)(lane + 1);
+        u64 v[NV];
 #pragma unroll
-        for (int q = 0; q < RADIX_MAX_V; q++)
-            if (q < R.V) tv[q] = tp[1 + q];
-        u64 v[GB_MAX_OPS];
-        tuple_contrib(P, R, tv, v);
-        const u64 h = mix64(pk);
-        u32 s = agg_slot(h, SP);
+        for (int q = 0; q < NV; q++) v[q] = 0;
+        if (i < n) {
+            const u64 *tp = base + i * TV;
+            const u64 k = tp[0];
+            if (k != EMPTY_KEY) {
+                u64 tv[VV];
+#pragma unroll
+                for (int q = 0; q < VV; q++) tv[q] = tp[1 + q];
+                tuple_contrib<VV, NOPS>(P, R, tv, v);
+                pk = k;
+                act = true;
+            }
+        }
+        // pre-combine lanes with equal keys: match on 32 hash bits (cheaper
+        // than a 64-bit match), then keep only lanes whose full key equals
+        // their group leader's; the others stay leaders of themselves
+        const u64 hh = mix64(pk);
+        const unsigned am = __ballot_sync(FULL, act);
+        unsigned peers = __match_any_sync(FULL, (unsigned)hh) & am;
+        const int ldr = __ffs(peers) - 1;
+        const u64 lkey = __shfl_sync(FULL, pk, ldr < 0 ? lane : ldr);
+        const bool same = act && lkey == pk;
+        peers &= __ballot_sync(FULL, same);
+        const bool leader = act && (!same || ldr == lane);
+        if (!same) peers = act ? (1u << lane) : 0u;
+        unsigned rem = (leader && same) ? (peers & ~(1u << lane)) : 0u;
+        const int maxit = __reduce_max_sync(FULL, (unsigned)__popc(rem));
+        for (int it = 0; it < maxit; it++) {
+            const int src = rem ? (__ffs(rem) - 1) : lane;
+            rem &= rem - 1u;
+#pragma unroll
+            for (int q = 0; q < NOPS; q++) {
+                const u64 o = __shfl_sync(FULL, v[q], src);
+                if (src != lane) v[q] = op_combine(P.ops[q].kind, v[q], o);
+            }
+        }
+        if (!leader) continue;
+        const u64 cnt = __popc(peers);
+        u32 s = agg_slot(hh, SP);
         bool done = false;
         for (int q = 0; q < R.agg_probe; q++) {
             u64 k = vk[s];
             if (k == EMPTY_KEY) {
-                u64 old = atomicCAS(&keys[s], EMPTY_KEY, pk);
-                if (old == EMPTY_KEY || old == pk) k = pk;
-                else k = old;
+                const u64 old = atomicCAS(&keys[s], EMPTY_KEY, pk);
+                k = (old == EMPTY_KEY) ? pk : old;
             }
             if (k == pk) {
-                apply_state(P, st + (u64)s * W, 1, v);
+                atomicAdd(&cn[s], (u32)cnt);
+#pragma unroll
+                for (int o = 0; o < NOPS; o++)
+                    op_apply(P.ops[o].kind, wd + (size_t)s * WM + (P.ops[o].word - 1), v[o],
+                             P.word_init[P.ops[o].word]);
                 done = true;
                 break;
             }
             s = (s + 1) & (u32)(SP - 1);
         }
-        if (!done) global_fold(P, T, pk, 1, v, &s_new);
+        if (!done) global_fold_n<NOPS>(P, T, pk, cnt, v, &s_new);
     }
     __syncthreads();
-    const int lane = threadIdx.x & 31;
-    for (int b = threadIdx.x - lane; b < SP; b += blockDim.x) {
-        const int s = b + lane;
-        const bool occ = keys[s] != EMPTY_KEY;
-        const u64 o = warp_out_slot(T.ctl, occ, FULL);
-        if (!occ) continue;
+    // emit: one output reservation per CTA
+    u32 mine = 0;
+    for (int s = threadIdx.x; s < SP; s += blockDim.x) mine += keys[s] != EMPTY_KEY;
+    u64 o = block_out_base(T.ctl, mine);
+    for (int s = threadIdx.x; s < SP; s += blockDim.x) {
+        if (keys[s] == EMPTY_KEY) continue;
         if (o >= E.out_cap) {
             atomicOr(&T.ctl->err, (u32)ERR_OUT_OVERFLOW);
             continue;
         }
-        emit_group(P, E, o, keys[s], false, st + (u64)s * W);
+        u64 w[GB_MAX_WORDS];
+        w[0] = cn[s];
+        for (int q = 0; q < WM; q++) w[1 + q] = wd[(size_t)s * WM + q];
+        emit_group(P, E, o, keys[s], false, w);
+        o++;
     }
     __syncthreads();
     if (threadIdx.x == 0 && s_new) atomicAdd(&T.ctl->n_groups, s_new);
 }
 
 // ------------------------------------------------------------- P3 hot
+// One warp per hot key: lanes fold the per-CTA slices lane, lane+32, ... and
+// a fixed shuffle tree combines them (deterministic order).  Output rows are
+// reserved per block.
 __global__ void k_hot_emit(const __grid_constant__ Plan P, const __grid_constant__ RadixPlan R, const RadixRef X,
-                           int G, Ctl *ctl, const __grid_constant__ EmitArgs E) {
-    const int W = P.words, HS = R.HS;
-    const int lane = threadIdx.x & 31;
-    for (u64 b = blockIdx.x * (u64)blockDim.x + threadIdx.x - lane; b < (u64)HS;
-         b += (u64)gridDim.x * blockDim.x) {
-        const u64 s = b + lane;
+                           int G, const u32 *hstate, Ctl *ctl, const __grid_constant__ EmitArgs E) {
+    const int W = P.words, NH = R.nh, NSUP = R.nsup;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const u32 nsup = min(hstate[0], (u32)NSUP), nwarm = min(hstate[1], (u32)(NH - NSUP));
+    for (u64 k0 = (u64)blockIdx.x * nwarps; k0 < (u64)NH; k0 += (u64)gridDim.x * nwarps) {
+        const u64 s = k0 + warp;
+        const bool used = s < (u64)NH && (s < nsup || (s >= (u64)NSUP && s < (u64)NSUP + nwarm));
         u64 w[GB_MAX_WORDS];
-        bool occ = false;
-        const u64 key = s < (u64)HS ? X.hot_keys[s] : EMPTY_KEY;
-        if (key != EMPTY_KEY) {
-            for (int q = 0; q < W; q++) w[q] = P.word_init[q];
-            for (int g = 0; g < G; g++) {
-                const u64 *hp = X.hot_part + ((u64)g * HS + s) * W;
+        for (int q = 0; q < W; q++) w[q] = P.word_init[q];
+        if (used) {
+            for (int g = lane; g < G; g += 32) {
+                const u64 *hp = X.hot_part + ((u64)g * NH + s) * W;
                 w[0] += hp[0];
                 for (int q = 1; q < W; q++) w[q] = op_combine(R.word_kind[q], w[q], hp[q]);
             }
-            occ = w[0] != 0;
+            for (int o = 16; o > 0; o >>= 1) {
+                w[0] += __shfl_xor_sync(FULL, w[0], o);
+                for (int q = 1; q < W; q++) w[q] = op_combine(R.word_kind[q], w[q], __shfl_xor_sync(FULL, w[q], o));
+            }
         }
-        const u64 o = warp_out_slot(ctl, occ, FULL);
+        const bool occ = used && w[0] != 0 && lane == 0;
+        u64 o = block_out_base(ctl, occ ? 1u : 0u);
         if (!occ) continue;
         if (o >= E.out_cap) {
             atomicOr(&ctl->err, (u32)ERR_OUT_OVERFLOW);
             continue;
         }
-        emit_group(P, E, o, key, false, w);
+        emit_group(P, E, o, X.hot_list[s], false, w);
     }
 }
 
@@ -376,10 +685,26 @@ static int grid_of(u64 work, int block, int cap) {
     return (int)std::max<u64>(1, std::min<u64>(g, (u64)cap));
 }
 
+size_t radix_p1_smem(const Plan &P, const RadixPlan &R) {
+    const size_t WM = P.words - 1, NP = (size_t)1 << R.pbits, V = R.V;
+    const size_t NWARM = R.nh - R.nsup;
+    return (size_t)R.HS * 8 + (size_t)P1_WARPS * R.nsup * WM * 8 + NWARM * WM * 8 + NP * R.wcb * (1 + V) * 8 +
+           (size_t)P1_WARPS * R.nsup * 4 + NWARM * 4 + 3 * NP * 4 + (size_t)R.HS * 2;
+}
+
+size_t radix_p2_smem(const Plan &P, const RadixPlan &R) {
+    const size_t WM = P.words - 1, SP = (size_t)R.sub;
+    return SP * 8 + SP * WM * 8 + SP * 4;
+}
+
+u32 radix_tile_rows(const RadixPlan &R) { return (u32)((R.V == 3 ? RADIX_ROWS / 2 : RADIX_ROWS) * P1_WARPS * 32); }
+
+static const size_t kSmemBudget = 224 * 1024;  // <= the 227 KiB opt-in minus static shared memory
+
 gb_status radix_prepare(const Plan &P, RadixPlan &R, u64 est_groups, u64 nullable_mask) {
     memset(&R, 0, sizeof R);
     if (P.key_mode == KEY_STRING) return GB_ERR_UNSUPPORTED;
-    // tuple values: distinct NOT NULL op columns
+    if (P.n_ops > RADIX_MAX_OPS) return GB_ERR_UNSUPPORTED;
     for (int i = 0; i < P.n_ops; i++) {
         const int c = P.ops[i].col;
         if ((nullable_mask >> c) & 1ull) return GB_ERR_UNSUPPORTED;
@@ -392,66 +717,122 @@ gb_status radix_prepare(const Plan &P, RadixPlan &R, u64 est_groups, u64 nullabl
         R.op_v[i] = j;
         R.word_kind[P.ops[i].word] = P.ops[i].kind;
     }
+    if (R.V == 0) {  // COUNT(*) only: the tuple carries one unused value
+        R.vcol[0] = P.key_col[0];
+        R.V = 1;
+    }
     if (P.words > GB_MAX_WORDS) return GB_ERR_UNSUPPORTED;
-    // partitions: ~3K groups each so a partition fits a shared table at
-    // load <= 0.5
-    u64 want = (est_groups + 3071) / 3072;
-    u64 np = pow2_at_least(std::max<u64>(want, 64));
+    // P2: one shared table of `sub` slots per partition
+    int sp = 8192;
+    R.sub = sp;
+    while (sp > 512 && radix_p2_smem(P, R) > kSmemBudget) {
+        sp /= 2;
+        R.sub = sp;
+    }
+    R.agg_probe = 64;
+    // partitions so that a partition's groups fill its table to <= ~0.7
+    const u64 per_part = (u64)sp * 7 / 10;
+    u64 np = pow2_at_least(std::max<u64>((est_groups + per_part - 1) / per_part, 64));
     np = std::min<u64>(np, 4096);
     int pb = 0;
     while ((1ull << pb) < np) pb++;
     R.pbits = pb;
-    // hot table: as many slots as fit next to the partition counters
-    const size_t budget = 200 * 1024 - 2 * np * 4;
-    u64 hs = 1;
-    while ((hs * 2) * 8 * (1 + (u64)P.words) <= budget) hs *= 2;
-    R.HS = (int)std::min<u64>(hs, 8192);
+    R.wcb = 4;  // write-combining tuples per partition per flush
+    // P1: hot set of nh keys, the nsup hottest private per warp; shrink to fit
+    R.HS = 8192;
+    R.nh = 4096;
+    R.nsup = 64;
     R.hot_probe = 8;
-    R.agg_probe = 64;
+    while (radix_p1_smem(P, R) > kSmemBudget) {
+        if (R.pbits > 10) R.pbits--;
+        else if (R.nh > 1024) {
+            R.nh /= 2;
+            R.HS /= 2;
+        } else if (R.pbits > 8) R.pbits--;
+        else if (R.nsup > 16) R.nsup /= 2;
+        else if (R.nh > 64) {
+            R.nh /= 2;
+            R.HS /= 2;
+        } else if (R.pbits > 6) R.pbits--;
+        else return GB_ERR_UNSUPPORTED;
+    }
+    R.qcap = 0;
+    R.qcap2 = 0;
     return GB_OK;
 }
 
-u32 radix_tile_rows(const RadixPlan &R) { return (u32)((R.V == 3 ? RADIX_ROWS / 2 : RADIX_ROWS) * RADIX_BLOCK); }
-
-size_t radix_p1_smem(const Plan &P, const RadixPlan &R) {
-    return (size_t)R.HS * 8 * (1 + P.words) + (size_t)2 * (1u << R.pbits) * 4;
-}
-
-int radix_sp(const Plan &P) {
-    u64 sp = 1;
-    while ((sp * 2) * 8 * (1 + (u64)P.words) <= 200 * 1024) sp *= 2;
-    return (int)std::min<u64>(sp, 8192);
-}
-
 gb_status radix_launch_sample(const Plan &P, const RadixPlan &R, u64 n, u64 *skeys, u32 *scnt, u64 scap,
-                              u32 *hist, u64 *hot_keys, cudaStream_t st, u64 *launches) {
+                              u32 *hist, u32 *hstate, u64 *hot_keys, uint16_t *hot_idx, u64 *hot_list,
+                              cudaStream_t st, u64 *launches) {
     const u64 m = std::min<u64>(n, scap / 2);
     const u64 step = std::max<u64>(1, n / std::max<u64>(m, 1));
     const int sms = sm_count();
     k_sample_count<<<grid_of(m, 256, sms * 4), 256, 0, st>>>(P, n, step, m, skeys, scnt, scap);
     k_sample_hist<<<grid_of(scap, 256, sms * 2), 256, 0, st>>>(skeys, scnt, scap, hist);
-    k_hot_build<<<grid_of(scap, 256, sms * 2), 256, 0, st>>>(skeys, scnt, scap, hist, 2, (u32)(R.HS / 2), hot_keys,
-                                                            R.HS);
+    k_hot_build<<<grid_of(scap, 256, sms * 2), 256, 0, st>>>(skeys, scnt, scap, hist, hstate, R.nsup, R.nh,
+                                                            hot_keys, hot_idx, hot_list, R.HS);
     *launches += 3;
     GB_CUDA(cudaGetLastError());
     return GB_OK;
 }
 
+// Raise a kernel's dynamic shared-memory limit to what the device allows
+// next to the kernel's static shared memory.
+template <typename F>
+static gb_status allow_max_smem(F f) {
+    int dev = 0, optin = 0;
+    GB_CUDA(cudaGetDevice(&dev));
+    GB_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes a;
+    GB_CUDA(cudaFuncGetAttributes(&a, f));
+    GB_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)a.sharedSizeBytes));
+    return GB_OK;
+}
+
+typedef void (*P1Fn)(Plan, RadixPlan, RadixRef, TableRef, RadixTile);
+typedef void (*P2Fn)(Plan, RadixPlan, RadixRef, TableRef, EmitArgs, int);
+
+template <int VV, int NOPS>
+static void p1_table(P1Fn *t) {
+    t[VV * (RADIX_MAX_OPS + 1) + NOPS] = (P1Fn)k_partition<(VV == 3 ? RADIX_ROWS / 2 : RADIX_ROWS), VV, NOPS>;
+}
+template <int VV, int NOPS>
+static void p2_table(P2Fn *t) {
+    t[VV * (RADIX_MAX_OPS + 1) + NOPS] = (P2Fn)k_part_agg<VV, NOPS>;
+}
+
+template <int VV>
+static void fill_tables(P1Fn *t1, P2Fn *t2) {
+    p1_table<VV, 0>(t1); p1_table<VV, 1>(t1); p1_table<VV, 2>(t1); p1_table<VV, 3>(t1); p1_table<VV, 4>(t1);
+    p2_table<VV, 0>(t2); p2_table<VV, 1>(t2); p2_table<VV, 2>(t2); p2_table<VV, 3>(t2); p2_table<VV, 4>(t2);
+}
+
+static P1Fn g_p1[4 * (RADIX_MAX_OPS + 1)];
+static P2Fn g_p2[4 * (RADIX_MAX_OPS + 1)];
+
+static gb_status radix_set_attributes() {
+    static bool done = false;
+    if (done) return GB_OK;
+    fill_tables<1>(g_p1, g_p2);
+    fill_tables<2>(g_p1, g_p2);
+    fill_tables<3>(g_p1, g_p2);
+    for (int v = 1; v <= 3; v++)
+        for (int o = 0; o <= RADIX_MAX_OPS; o++) {
+            gb_status s;
+            if ((s = allow_max_smem(g_p1[v * (RADIX_MAX_OPS + 1) + o]))) return s;
+            if ((s = allow_max_smem(g_p2[v * (RADIX_MAX_OPS + 1) + o]))) return s;
+        }
+    done = true;
+    return GB_OK;
+}
+
 gb_status radix_launch_p1(const Plan &P, const RadixPlan &R, const RadixRef &X, const TableRef &T,
                           const RadixTile &A, int grid, cudaStream_t st) {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_partition<RADIX_ROWS, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-        cudaFuncSetAttribute(k_partition<RADIX_ROWS, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-        cudaFuncSetAttribute(k_partition<RADIX_ROWS / 2, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             220 * 1024);
-        cudaFuncSetAttribute(k_part_agg, cudaFuncAttributeMaxDynamicSharedMemorySize, 220 * 1024);
-        attr = true;
-    }
+    gb_status s = radix_set_attributes();
+    if (s) return s;
     const size_t smem = radix_p1_smem(P, R);
-    if (R.V == 1) k_partition<RADIX_ROWS, 1><<<grid, RADIX_BLOCK, smem, st>>>(P, R, X, T, A);
-    else if (R.V == 2) k_partition<RADIX_ROWS, 2><<<grid, RADIX_BLOCK, smem, st>>>(P, R, X, T, A);
-    else k_partition<RADIX_ROWS / 2, 3><<<grid, RADIX_BLOCK, smem, st>>>(P, R, X, T, A);
+    P1Fn f = g_p1[R.V * (RADIX_MAX_OPS + 1) + P.n_ops];
+    f<<<grid, P1_WARPS * 32, smem, st>>>(P, R, X, T, A);
     GB_CUDA(cudaGetLastError());
     return GB_OK;
 }
@@ -464,17 +845,32 @@ gb_status radix_launch_drain(const RadixRef &X, int V, u32 n, cudaStream_t st) {
 
 gb_status radix_launch_p2(const Plan &P, const RadixPlan &R, const RadixRef &X, const TableRef &T, const EmitArgs &E,
                           cudaStream_t st) {
-    const int SP = radix_sp(P);
-    const size_t smem = (size_t)SP * 8 * (1 + P.words);
-    k_part_agg<<<1 << R.pbits, RADIX_BLOCK, smem, st>>>(P, R, X, T, E, SP);
+    gb_status s = radix_set_attributes();
+    if (s) return s;
+    const size_t smem = radix_p2_smem(P, R);
+    const int np = 1 << R.pbits;
+    P2Fn f = g_p2[R.V * (RADIX_MAX_OPS + 1) + P.n_ops];
+    f<<<np, RADIX_BLOCK, smem, st>>>(P, R, X, T, E, R.sub);
     GB_CUDA(cudaGetLastError());
     return GB_OK;
 }
 
-gb_status radix_launch_p3(const Plan &P, const RadixPlan &R, const RadixRef &X, int G, Ctl *ctl, const EmitArgs &E,
-                          cudaStream_t st) {
-    if (R.HS == 0) return GB_OK;
-    k_hot_emit<<<grid_of(R.HS, 256, sm_count() * 2), 256, 0, st>>>(P, R, X, G, ctl, E);
+gb_status radix_launch_p3(const Plan &P, const RadixPlan &R, const RadixRef &X, int G, const u32 *hstate, Ctl *ctl,
+                          const EmitArgs &E, cudaStream_t st) {
+    if (R.nh == 0) return GB_OK;
+    k_hot_emit<<<grid_of((u64)R.nh * 32, 256, sm_count() * 4), 256, 0, st>>>(P, R, X, G, hstate, ctl, E);
+    GB_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+gb_status radix_launch_move(const RadixRef &from, const RadixRef &to, int V, int np, cudaStream_t st) {
+    k_part_move<<<np, 256, 0, st>>>(from, to, V);
+    GB_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+gb_status radix_fill_u64(u64 *dst, u64 n, u64 value, cudaStream_t st) {
+    k_fill_u64<<<grid_of(n, 256, sm_count() * 8), 256, 0, st>>>(dst, n, value);
     GB_CUDA(cudaGetLastError());
     return GB_OK;
 }
