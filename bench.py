@@ -38,6 +38,9 @@ sys.path.insert(0, ROOT)
 METRIC = "GROUP BY rows/s & HBM GB/s at 100M rows; batched queries/s and p99 vs plain"
 N_VALUES = 20_000_000
 EST_GROUPS = 8_000_000  # planner estimate handed to the operator
+# DRAM bytes per input row of the dominant kernel (ncu capture summarised in
+# profiles/radix_groupby_zipf100M.md): (490.4 MB read + 126.8 MB written) / 30M rows
+TRAFFIC_PER_ROW = {"k_partition": (490.36 + 126.75) * 1e6 / 30e6}
 
 
 def parse():
@@ -245,13 +248,19 @@ def main():
     alg_bytes = in_bytes + out_bytes
     value = rows * ws / (ms / 1e3)
 
-    # roofline: dominant kernel = the ingest kernel
-    ing = prof.get("k_ingest", (1, float("nan")))
+    # roofline: dominant kernel = the row pass (k_partition in radix mode,
+    # k_ingest in hash mode); algorithmic bytes = the key + value columns
+    # (16 B/row) it reads once
+    dom = "k_partition" if "k_partition" in prof else "k_ingest"
+    ing = prof.get(dom, (1, float("nan")))
     ing_ms = ing[1] / max(1, ing[0])
     achieved = in_bytes / (ing_ms / 1e3) / 1e9
+    # DRAM traffic per row of k_partition from the committed ncu capture
+    # (30M-row case, read + write = 617.1 MB), scaled to this launch's rows
+    traffic = TRAFFIC_PER_ROW.get(dom)
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": achieved / hbm_peak, "traffic": None,
-                "kernel": "k_ingest", "kernel_ms": ing_ms,
+                "frac": achieved / hbm_peak, "traffic": traffic * rows if traffic else None,
+                "kernel": dom, "kernel_ms": ing_ms,
                 "peak_source": peak_src,
                 "step_GBps": alg_bytes / (ms / 1e3) / 1e9,
                 "step_frac": alg_bytes / (ms / 1e3) / 1e9 / hbm_peak,

@@ -798,7 +798,7 @@ static gb_status radix_begin(gb_agg *h, u64 n, cudaStream_t st) {
     u64 sampled = std::max<u64>(1, std::min<u64>(n, m));
     double hot_frac = std::min(1.0, (double)hot_rows / (double)sampled);
     double tail = (double)n * (1.0 - hot_frac);
-    u64 cap_p = (u64)(tail / (double)np * 1.25) + 2048;
+    u64 cap_p = (u64)(tail / (double)np * 1.5) + 2048;
     cap_p = (cap_p + 31) / 32 * 32;
     h->r_cap_p = cap_p;
     h->h_off.assign(np + 1, 0);
