@@ -204,6 +204,35 @@ gb_status gb_engine_hash_aggregate(const int32_t *keys, const int32_t *values, u
                                    int32_t *out_keys, int64_t *out_sums, int64_t *out_counts,
                                    uint64_t cap, uint64_t *n_out);
 
+/* ---------------------------------------------------------------- Parquet
+ * A Parquet file held in host memory (read or mmap'd by the caller).
+ * gb_pq_open parses the footer and every page header into a page index —
+ * replaces ParquetReader's metadata/page walk (src/storage/parquet.cpp:
+ * 92-470 thrift + page headers, 1107-1366 metadata, 2475-2706 ReadColumnInto).
+ * Supported: uncompressed column chunks, REQUIRED flat columns of INT32
+ * (INT(16) annotation → SMALLINT), INT64 and DOUBLE, PLAIN or dictionary
+ * (RLE / bit-packed hybrid) encoded, data page v1 and v2. */
+typedef struct gb_pq_file gb_pq_file;
+gb_status gb_pq_open(const uint8_t *bytes, uint64_t size, gb_pq_file **out);
+uint32_t gb_pq_num_row_groups(const gb_pq_file *f);
+uint64_t gb_pq_num_rows(const gb_pq_file *f);
+uint32_t gb_pq_num_columns(const gb_pq_file *f);
+gb_status gb_pq_column_info(const gb_pq_file *f, uint32_t col, char *name, uint32_t name_cap, int32_t *type);
+/* Copies the whole file into HBM once (a resident table). */
+gb_status gb_pq_upload(gb_pq_file *f, void *stream);
+void gb_pq_close(gb_pq_file *f);
+
+/* Replaces the RG-consumer path of the fused Parquet aggregate
+ * (PhysicalParquetScan::SetRGConsumer / RunParallelRGs / DecodeRowGroupInto,
+ * physical_planner.cpp:1060-1062, 1070-1135, 1175-1203, consumed by the
+ * TLSingle loop 7613-7931): row groups [rg_begin, rg_end) are decoded on the
+ * GPU (dictionary RLE/bit-unpack + gather, PLAIN loads), filtered by the
+ * spec's predicates and aggregated.  Spec column c reads file column
+ * col_map[c].  mem = GB_MEM_DEVICE reads the gb_pq_upload'ed copy;
+ * GB_MEM_HOST copies the row groups' bytes to HBM inside the call. */
+gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg_begin, uint32_t rg_end, const int32_t *col_map,
+                                int32_t mem, void *stream);
+
 /* Allocation-free GROUP BY for callers that cannot allocate device memory
  * on their query path (an engine that hands out device memory only from
  * its own pre-reserved arena, a plugin host that forbids allocation inside

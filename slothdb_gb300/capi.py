@@ -84,6 +84,15 @@ _SIGS = {
                                            C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
     "gb_hash_aggregate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64), C.c_void_p]),
+    "gb_pq_open": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
+    "gb_pq_num_row_groups": (C.c_uint32, [C.c_void_p]),
+    "gb_pq_num_rows": (C.c_uint64, [C.c_void_p]),
+    "gb_pq_num_columns": (C.c_uint32, [C.c_void_p]),
+    "gb_pq_column_info": (C.c_int, [C.c_void_p, C.c_uint32, C.c_char_p, C.c_uint32, C.POINTER(C.c_int32)]),
+    "gb_pq_upload": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gb_pq_close": (None, [C.c_void_p]),
+    "gb_agg_ingest_parquet": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_int32),
+                                        C.c_int32, C.c_void_p]),
     "gb_host_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
     "gb_host_free": (C.c_int, [C.c_void_p]),
     "gb_device_alloc": (C.c_int, [C.POINTER(C.c_void_p), C.c_size_t]),
@@ -269,6 +278,60 @@ def validity_words(valid_bool: np.ndarray) -> np.ndarray:
     pad = np.zeros(((n + 63) // 64) * 64, dtype=bool)
     pad[:n] = valid_bool
     return np.packbits(pad, bitorder="little").view(np.uint64).copy()
+
+
+class ParquetFile:
+    """A Parquet file in host memory, parsed by the library (gb_pq_open)."""
+
+    def __init__(self, data):
+        self.lib = load()
+        if isinstance(data, (bytes, bytearray)):
+            self._buf = np.frombuffer(data, dtype=np.uint8)
+        else:
+            self._buf = np.ascontiguousarray(data, dtype=np.uint8)
+        h = C.c_void_p()
+        check(self.lib.gb_pq_open(self._buf.ctypes.data, len(self._buf), C.byref(h)))
+        self.h = h
+
+    @property
+    def num_row_groups(self):
+        return int(self.lib.gb_pq_num_row_groups(self.h))
+
+    @property
+    def num_rows(self):
+        return int(self.lib.gb_pq_num_rows(self.h))
+
+    def columns(self):
+        out = []
+        for i in range(int(self.lib.gb_pq_num_columns(self.h))):
+            name = C.create_string_buffer(256)
+            t = C.c_int32()
+            check(self.lib.gb_pq_column_info(self.h, i, name, 256, C.byref(t)))
+            out.append((name.value.decode(), int(t.value)))
+        return out
+
+    def upload(self, stream=None):
+        check(self.lib.gb_pq_upload(self.h, C.c_void_p(stream) if stream else None))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gb_pq_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def ingest_parquet(g, pf, col_map, rg_begin=0, rg_end=None, device=False, stream=None):
+    """Feed row groups of ParquetFile `pf` to GroupBy `g` (spec column c reads
+    file column col_map[c])."""
+    rg_end = pf.num_row_groups if rg_end is None else rg_end
+    cm = (C.c_int32 * len(col_map))(*col_map)
+    check(g.lib.gb_agg_ingest_parquet(g.h, pf.h, rg_begin, rg_end, cm, MEM_DEVICE if device else MEM_HOST,
+                                      C.c_void_p(stream) if stream else None))
 
 
 class PinnedBuffer:

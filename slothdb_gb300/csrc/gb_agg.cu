@@ -1513,6 +1513,7 @@ gb_status gb_agg_reset(gb_agg *h) {
 void gb_agg_destroy(gb_agg *h) {
     if (!h) return;
     cudaDeviceSynchronize();
+    gb_pq_release_scratch(h);
     h->table.release();
     h->table_old.release();
     h->spill.release();
@@ -1680,6 +1681,32 @@ gb_status gb_device_sync(void) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------ Parquet ingest hooks
+gb_status gb_agg_view(gb_agg *h, AggView *v) {
+    if (!h || !v) return GB_ERR_INVALID;
+    if (h->finalized) {
+        set_error("ingest after finalize (call gb_agg_reset first)");
+        return GB_ERR_STATE;
+    }
+    v->n_cols = h->plan.n_cols;
+    v->col_types = h->col_types.data();
+    v->n_filters = h->plan.n_filters;
+    for (int i = 0; i < h->plan.n_filters; i++) v->filters[i] = h->plan.filters[i];
+    return GB_OK;
+}
+
+void gb_agg_count_launch(gb_agg *h, int n) { h->launches += (u64)n; }
+
+gb_status gb_agg_ingest_prefiltered(gb_agg *h, const gb_col *cols, uint64_t nrows, void *stream) {
+    const int nf = h->plan.n_filters;
+    h->plan.n_filters = 0;
+    const uint64_t saved_mask = h->nullable_mask;
+    gb_status s = gb_agg_ingest(h, cols, nrows, GB_MEM_DEVICE, stream);
+    h->plan.n_filters = nf;
+    h->nullable_mask = saved_mask;
+    return s;
+}
 
 // tuning hook (defaults here; the autotuner overrides per shape)
 void gb_apply_tuning(gb_agg *h) {

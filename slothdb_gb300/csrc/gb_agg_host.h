@@ -5,3 +5,19 @@
 // Applies default (or autotuned) launch parameters to a freshly compiled
 // handle: shared-table slots, CTAs per SM, block size.
 void gb_apply_tuning(gb_agg *h);
+
+#include "gb_internal.cuh"
+
+// A read-only view of the handle's spec for the Parquet ingest.
+struct AggView {
+    int n_cols;
+    const int32_t *col_types;
+    int n_filters;
+    gb::Filter filters[GB_MAX_FILTERS];
+};
+gb_status gb_agg_view(gb_agg *h, AggView *v);
+void gb_agg_count_launch(gb_agg *h, int n);
+// Device-resident columns whose rows already passed the spec's filters.
+gb_status gb_agg_ingest_prefiltered(gb_agg *h, const gb_col *cols, uint64_t nrows, void *stream);
+// Frees the per-handle Parquet scratch (called by gb_agg_destroy).
+void gb_pq_release_scratch(gb_agg *h);

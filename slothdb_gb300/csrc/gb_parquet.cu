@@ -1,0 +1,935 @@
+// gb_parquet.cu — Parquet row groups straight into the GROUP BY on GB300.
+//
+// Host: the footer and every page header are parsed from the file bytes
+// (thrift compact protocol) into a page index — the GPU-side restatement of
+// ParquetReader's metadata walk (src/storage/parquet.cpp:92-184 ThriftRd,
+// 187-382 / 1107-1366 metadata, 385-470 page headers, 2475-2706
+// ReadColumnInto's page loop).
+//
+// Device, per batch of row groups:
+//   k_pq_runs   one CTA per dictionary-encoded data page: the page is staged in
+//               shared memory and its RLE / bit-packed run headers are walked
+//               into a run table (RleDecoder::FetchRun, parquet.cpp:485-512).
+//   k_pq_scan   row chunks: every needed column is decoded at each row — PLAIN
+//               values loaded in place from the page, dictionary indices
+//               located through the run table and bit-unpacked from the page
+//               (RleDecoder::Next / NextBatch, parquet.cpp:514-608) then
+//               gathered from the dictionary page (DecodeDataPageTyped,
+//               parquet.cpp:2119-2210; an index past the dictionary yields 0)
+//               — the scan filter is evaluated on the decoded values
+//               (BuildTypedKeepMask, physical_planner.cpp:505-720) and the
+//               passing rows are compacted into typed columns.
+//   The compacted columns then go through the ordinary aggregation ingest.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "gb_agg_host.h"
+#include "gb_kernels.cuh"
+
+namespace gb {
+
+// ------------------------------------------------------------ thrift reader
+struct TReader {
+    const uint8_t *p;
+    size_t n, pos;
+    bool bad = false;
+    TReader(const uint8_t *p_, size_t n_, size_t pos_ = 0) : p(p_), n(n_), pos(pos_) {}
+    uint8_t byte() {
+        if (pos >= n) {
+            bad = true;
+            return 0;
+        }
+        return p[pos++];
+    }
+    uint64_t varint() {
+        uint64_t v = 0;
+        for (int sh = 0; sh < 64; sh += 7) {
+            uint8_t b = byte();
+            v |= (uint64_t)(b & 0x7f) << sh;
+            if (!(b & 0x80) || bad) return v;
+        }
+        bad = true;
+        return v;
+    }
+    int64_t zz() {
+        uint64_t v = varint();
+        return (int64_t)(v >> 1) ^ -(int64_t)(v & 1);
+    }
+    // next field of the current struct; false at STOP
+    bool field(int &fid, int &type, int &last) {
+        uint8_t b = byte();
+        if (bad || b == 0) return false;
+        type = b & 0x0f;
+        int delta = b >> 4;
+        fid = delta ? last + delta : (int)(int16_t)zz();
+        last = fid;
+        return true;
+    }
+    void list_header(int &etype, uint64_t &size) {
+        uint8_t b = byte();
+        etype = b & 0x0f;
+        size = (b >> 4) == 15 ? varint() : (b >> 4);
+    }
+    std::string binary() {
+        uint64_t len = varint();
+        if (bad || pos + len > n) {
+            bad = true;
+            return std::string();
+        }
+        std::string s((const char *)p + pos, (size_t)len);
+        pos += len;
+        return s;
+    }
+    void skip(int type, int depth = 0) {
+        if (depth > 32) {
+            bad = true;
+            return;
+        }
+        switch (type) {
+        case 1:
+        case 2: break;  // bool in the field header
+        case 3: byte(); break;
+        case 4:
+        case 5:
+        case 6: varint(); break;
+        case 7: pos += 8; break;
+        case 8: {
+            uint64_t len = varint();
+            pos += len;
+            break;
+        }
+        case 9:
+        case 10: {
+            int et;
+            uint64_t sz;
+            list_header(et, sz);
+            for (uint64_t i = 0; i < sz && !bad; i++) skip(et, depth + 1);
+            break;
+        }
+        case 11: {
+            uint64_t sz = varint();
+            if (sz) {
+                uint8_t kv = byte();
+                for (uint64_t i = 0; i < sz && !bad; i++) {
+                    skip(kv >> 4, depth + 1);
+                    skip(kv & 0x0f, depth + 1);
+                }
+            }
+            break;
+        }
+        case 12: {
+            int fid, t, last = 0;
+            while (field(fid, t, last)) skip(t, depth + 1);
+            break;
+        }
+        default: bad = true;
+        }
+        if (pos > n) bad = true;
+    }
+};
+
+}  // namespace gb
+
+using namespace gb;
+
+// ----------------------------------------------------------- host structures
+struct PqPage {
+    int32_t kind;        // 0 PLAIN, 1 dictionary indices
+    int32_t col;         // file column
+    uint32_t rg;
+    uint32_t first_row;  // within the row group
+    uint32_t n_values;
+    uint32_t bytes;      // payload bytes
+    uint64_t off;        // payload offset in the file
+};
+
+struct PqChunk {
+    int64_t num_values = 0;
+    uint64_t start = 0, size = 0;  // byte range of the column chunk
+    int32_t codec = 0;
+    int64_t dict_off = -1;  // dictionary payload offset (-1 = none)
+    uint32_t dict_n = 0;
+    uint32_t page_begin = 0, page_end = 0;  // into pages (data pages only)
+};
+
+struct PqColumn {
+    std::string name;
+    int32_t ptype = -1;  // parquet physical type
+    int32_t gtype = 0;   // gb_type (0 = unsupported)
+    int32_t repetition = 0;
+    int32_t width = 0;   // bytes per PLAIN value
+};
+
+struct gb_pq_file {
+    const uint8_t *host = nullptr;
+    uint64_t size = 0;
+    std::vector<PqColumn> cols;
+    std::vector<uint64_t> rg_rows;
+    std::vector<std::vector<PqChunk>> chunks;  // [rg][col]
+    std::vector<PqPage> pages;
+    uint64_t num_rows = 0;
+    void *dev = nullptr;  // device copy of the file (gb_pq_upload)
+};
+
+static gb_status pq_corrupt(const char *what) {
+    set_error("malformed Parquet: %s", what);
+    return GB_ERR_CORRUPT;
+}
+
+static gb_status parse_footer(gb_pq_file *f) {
+    const uint8_t *b = f->host;
+    const uint64_t n = f->size;
+    if (n < 12 || memcmp(b, "PAR1", 4) != 0 || memcmp(b + n - 4, "PAR1", 4) != 0) return pq_corrupt("magic");
+    uint32_t flen;
+    memcpy(&flen, b + n - 8, 4);
+    if ((uint64_t)flen + 12 > n) return pq_corrupt("footer length");
+    TReader r(b, n - 8, n - 8 - flen);
+    int fid, type, last = 0;
+    std::vector<PqColumn> schema;
+    while (r.field(fid, type, last)) {
+        if (fid == 2 && type == 9) {  // schema
+            int et;
+            uint64_t sz;
+            r.list_header(et, sz);
+            for (uint64_t i = 0; i < sz && !r.bad; i++) {
+                PqColumn c;
+                int nchild = 0, conv = -1, int_bits = 0;
+                int f2, t2, l2 = 0;
+                while (r.field(f2, t2, l2)) {
+                    if (f2 == 1 && t2 == 5) c.ptype = (int)r.zz();
+                    else if (f2 == 3 && t2 == 5) c.repetition = (int)r.zz();
+                    else if (f2 == 4 && t2 == 8) c.name = r.binary();
+                    else if (f2 == 5 && t2 == 5) nchild = (int)r.zz();
+                    else if (f2 == 6 && t2 == 5) conv = (int)r.zz();
+                    else if (f2 == 10 && t2 == 12) {  // LogicalType union
+                        int f3, t3, l3 = 0;
+                        while (r.field(f3, t3, l3)) {
+                            if (f3 == 10 && t3 == 12) {  // INTEGER
+                                int f4, t4, l4 = 0;
+                                while (r.field(f4, t4, l4)) {
+                                    if (f4 == 1 && t4 == 3) int_bits = (int8_t)r.byte();
+                                    else r.skip(t4);
+                                }
+                            } else r.skip(t3);
+                        }
+                    } else r.skip(t2);
+                }
+                if (i == 0) continue;  // root
+                if (nchild > 0) {
+                    set_error("nested Parquet schemas are not supported on the GPU path");
+                    return GB_ERR_UNSUPPORTED;
+                }
+                switch (c.ptype) {
+                case 1:
+                    c.gtype = (conv == 16 || int_bits == 16) ? GB_T_SMALLINT : GB_T_INTEGER;
+                    c.width = 4;
+                    break;
+                case 2: c.gtype = GB_T_BIGINT; c.width = 8; break;
+                case 5: c.gtype = GB_T_DOUBLE; c.width = 8; break;
+                default: c.gtype = 0; c.width = 0; break;
+                }
+                schema.push_back(c);
+            }
+        } else if (fid == 3 && type == 6) {
+            f->num_rows = (uint64_t)r.zz();
+        } else if (fid == 4 && type == 9) {  // row groups
+            int et;
+            uint64_t sz;
+            r.list_header(et, sz);
+            for (uint64_t g = 0; g < sz && !r.bad; g++) {
+                std::vector<PqChunk> cc;
+                uint64_t rows = 0;
+                int f2, t2, l2 = 0;
+                while (r.field(f2, t2, l2)) {
+                    if (f2 == 1 && t2 == 9) {
+                        int et2;
+                        uint64_t sz2;
+                        r.list_header(et2, sz2);
+                        for (uint64_t c = 0; c < sz2 && !r.bad; c++) {
+                            PqChunk ch;
+                            int64_t data_off = -1, dict_off = -1, comp = 0;
+                            int f3, t3, l3 = 0;
+                            while (r.field(f3, t3, l3)) {
+                                if (f3 == 3 && t3 == 12) {  // ColumnMetaData
+                                    int f4, t4, l4 = 0;
+                                    while (r.field(f4, t4, l4)) {
+                                        if (f4 == 4 && t4 == 5) ch.codec = (int)r.zz();
+                                        else if (f4 == 5 && t4 == 6) ch.num_values = r.zz();
+                                        else if (f4 == 7 && t4 == 6) comp = r.zz();
+                                        else if (f4 == 9 && t4 == 6) data_off = r.zz();
+                                        else if (f4 == 11 && t4 == 6) dict_off = r.zz();
+                                        else r.skip(t4);
+                                    }
+                                } else r.skip(t3);
+                            }
+                            int64_t start = (dict_off >= 0 && dict_off < data_off) ? dict_off : data_off;
+                            if (start < 0 || comp < 0 || (uint64_t)(start + comp) > n) return pq_corrupt("column chunk range");
+                            ch.start = (uint64_t)start;
+                            ch.size = (uint64_t)comp;
+                            cc.push_back(ch);
+                        }
+                    } else if (f2 == 3 && t2 == 6) {
+                        rows = (uint64_t)r.zz();
+                    } else r.skip(t2);
+                }
+                f->chunks.push_back(cc);
+                f->rg_rows.push_back(rows);
+            }
+        } else {
+            r.skip(type);
+        }
+    }
+    if (r.bad) return pq_corrupt("footer thrift");
+    if (schema.empty()) return pq_corrupt("schema has no columns");
+    uint64_t total = 0;
+    for (uint64_t rows : f->rg_rows) total += rows;
+    if (total != f->num_rows) return pq_corrupt("row-group rows do not add up to num_rows");
+    f->cols = schema;
+    for (auto &cc : f->chunks)
+        if (cc.size() != f->cols.size()) return pq_corrupt("row group column count");
+    return GB_OK;
+}
+
+// Walk one column chunk's page headers.
+static gb_status parse_pages(gb_pq_file *f, uint32_t rg, uint32_t col) {
+    PqChunk &ch = f->chunks[rg][col];
+    uint64_t pos = ch.start, end = ch.start + ch.size;
+    uint32_t row = 0;
+    ch.page_begin = (uint32_t)f->pages.size();
+    while (pos < end) {
+        TReader r(f->host, end, pos);
+        int fid, type, last = 0;
+        int ptype = -1, enc = -1;
+        int64_t csize = -1, nvals = -1, dict_n = -1;
+        while (r.field(fid, type, last)) {
+            if (fid == 1 && type == 5) ptype = (int)r.zz();
+            else if (fid == 3 && type == 5) csize = r.zz();
+            else if ((fid == 5 || fid == 8) && type == 12) {  // data page v1 / v2
+                int f2, t2, l2 = 0;
+                int64_t def_len = 0, rep_len = 0;
+                while (r.field(f2, t2, l2)) {
+                    if (f2 == 1 && t2 == 5) nvals = r.zz();
+                    else if (fid == 5 && f2 == 2 && t2 == 5) enc = (int)r.zz();
+                    else if (fid == 8 && f2 == 4 && t2 == 5) enc = (int)r.zz();
+                    else if (fid == 8 && f2 == 5 && t2 == 5) def_len = r.zz();
+                    else if (fid == 8 && f2 == 6 && t2 == 5) rep_len = r.zz();
+                    else r.skip(t2);
+                }
+                if (def_len || rep_len) {
+                    set_error("Parquet data page v2 with repetition/definition levels is not supported");
+                    return GB_ERR_UNSUPPORTED;
+                }
+            } else if (fid == 7 && type == 12) {
+                int f2, t2, l2 = 0;
+                while (r.field(f2, t2, l2)) {
+                    if (f2 == 1 && t2 == 5) dict_n = r.zz();
+                    else r.skip(t2);
+                }
+            } else r.skip(type);
+        }
+        if (r.bad || csize < 0 || r.pos + (uint64_t)csize > end) return pq_corrupt("page header");
+        const uint64_t payload = r.pos;
+        if (ptype == 2) {
+            if (dict_n < 0) return pq_corrupt("dictionary page header");
+            ch.dict_off = (int64_t)payload;
+            ch.dict_n = (uint32_t)dict_n;
+            if ((uint64_t)dict_n * f->cols[col].width > (uint64_t)csize) return pq_corrupt("dictionary size");
+        } else if (ptype == 0 || ptype == 3) {
+            if (nvals < 0) return pq_corrupt("data page header");
+            PqPage pg;
+            pg.col = (int32_t)col;
+            pg.rg = rg;
+            pg.first_row = row;
+            pg.n_values = (uint32_t)nvals;
+            pg.bytes = (uint32_t)csize;
+            pg.off = payload;
+            if (enc == 0) {
+                pg.kind = 0;
+                if ((uint64_t)nvals * f->cols[col].width > (uint64_t)csize) return pq_corrupt("PLAIN page size");
+            } else if (enc == 2 || enc == 8) {
+                pg.kind = 1;
+                if (csize < 1) return pq_corrupt("dictionary-index page");
+            } else {
+                set_error("Parquet encoding %d is not supported on the GPU path", enc);
+                return GB_ERR_UNSUPPORTED;
+            }
+            f->pages.push_back(pg);
+            row += (uint32_t)nvals;
+        }
+        pos = payload + (uint64_t)csize;
+    }
+    ch.page_end = (uint32_t)f->pages.size();
+    if (row != f->rg_rows[rg]) return pq_corrupt("page values do not add up to the row group");
+    return GB_OK;
+}
+
+// ================================================================= kernels
+struct DPage {
+    uint64_t off;       // payload offset in the device file
+    uint64_t dict_off;  // dictionary payload offset
+    uint32_t first_row, n_values, bytes, dict_n;
+    uint32_t run_base, run_cap;  // run-table slice (dictionary pages)
+    int32_t kind, width;
+};
+
+struct DRun {
+    uint32_t start;  // first value index of the run within the page
+    uint32_t off;    // payload byte of the packed values (0xffffffff = RLE)
+    uint32_t cnt;
+    uint32_t val;    // RLE value
+};
+
+#define PQ_WIN 16384
+
+// One CTA per dictionary-index page: stage windows of the payload in shared
+// memory; thread 0 walks the run headers.  Run counts/bit width per page go
+// to page_runs[p] = {n_runs, bit_width}.
+__global__ void k_pq_runs(const uint8_t *file, const DPage *pages, const uint32_t *dict_pages, DRun *runs,
+                          uint32_t *page_runs, Ctl *ctl) {
+    __shared__ uint8_t win[PQ_WIN + 16];
+    __shared__ uint64_t s_pos;   // absolute payload position of the walk
+    __shared__ uint32_t s_vals, s_runs, s_done, s_bw;
+    const uint32_t pidx = dict_pages[blockIdx.x];
+    const DPage pg = pages[pidx];
+    if (threadIdx.x == 0) {
+        s_pos = 0;
+        s_vals = 0;
+        s_runs = 0;
+        s_done = 0;
+        s_bw = file[pg.off];
+        if (s_bw > 32) {
+            atomicOr(&ctl->err, (u32)ERR_CORRUPT);
+            s_done = 1;
+        }
+        s_pos = 1;
+    }
+    __syncthreads();
+    while (!s_done) {
+        const uint64_t w0 = s_pos;
+        const uint64_t wn = min((uint64_t)PQ_WIN, (uint64_t)pg.bytes - w0);
+        for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) win[i] = file[pg.off + w0 + i];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint32_t bw = s_bw;
+            const uint32_t vb = (bw + 7) / 8;
+            uint64_t pos = w0;
+            uint32_t vals = s_vals, nr = s_runs;
+            bool done = false, err = false;
+            while (!done) {
+                if (vals >= pg.n_values || pos >= pg.bytes) {
+                    done = true;
+                    break;
+                }
+                // a header (<= 10 bytes) plus an RLE value must lie inside the window
+                if (pos + 16 > w0 + wn && w0 + wn < pg.bytes) break;
+                uint64_t hdr = 0;
+                int sh = 0;
+                uint64_t q = pos;
+                for (;;) {
+                    if (q >= pg.bytes || sh > 35) {
+                        err = true;
+                        break;
+                    }
+                    const uint8_t b = win[q - w0];
+                    q++;
+                    hdr |= (uint64_t)(b & 0x7f) << sh;
+                    if (!(b & 0x80)) break;
+                    sh += 7;
+                }
+                if (err) break;
+                DRun rn;
+                rn.start = vals;
+                if (hdr & 1) {
+                    const uint64_t cnt = (hdr >> 1) * 8;
+                    const uint64_t plen = (hdr >> 1) * (uint64_t)bw;
+                    rn.off = (uint32_t)q;
+                    rn.cnt = (uint32_t)min(cnt, (uint64_t)(pg.n_values - vals));
+                    rn.val = 0;
+                    q += plen;
+                    if (q > pg.bytes) {
+                        // truncated packed run: the reference decodes what is there
+                        // and leaves the rest unset (RleDecoder::NextBatch refill)
+                        const uint64_t have = ((uint64_t)pg.bytes - rn.off) * 8 / (bw ? bw : 1);
+                        rn.cnt = (uint32_t)min((uint64_t)rn.cnt, have);
+                        done = true;
+                    }
+                } else {
+                    const uint64_t cnt = hdr >> 1;
+                    if (q + vb > pg.bytes) {
+                        done = true;
+                        break;
+                    }
+                    uint32_t v = 0;
+                    for (uint32_t b = 0; b < vb; b++) v |= (uint32_t)win[q - w0 + b] << (8 * b);
+                    q += vb;
+                    rn.off = 0xffffffffu;
+                    rn.cnt = (uint32_t)min(cnt, (uint64_t)(pg.n_values - vals));
+                    rn.val = v;
+                }
+                if (rn.cnt) {
+                    if (nr >= pg.run_cap) {
+                        err = true;
+                        break;
+                    }
+                    runs[pg.run_base + nr] = rn;
+                    nr++;
+                    vals += rn.cnt;
+                }
+                pos = q;
+            }
+            if (err) {
+                atomicOr(&ctl->err, (u32)ERR_CORRUPT);
+                done = true;
+            }
+            s_pos = pos;
+            s_vals = vals;
+            s_runs = nr;
+            s_done = done;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        page_runs[2 * pidx] = s_runs;
+        page_runs[2 * pidx + 1] = s_bw;
+    }
+}
+
+
+// Locate the page of `col` holding row r of the chunk's row group:
+// pages [pb, pe) are sorted by first_row.
+__device__ __forceinline__ uint32_t find_page(const DPage *pages, uint32_t pb, uint32_t pe, uint32_t r) {
+    uint32_t lo = pb, hi = pe;  // last page with first_row <= r
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (pages[mid].first_row <= r) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Decode one value of a page at value index i (as int64 / double bits).
+__device__ __forceinline__ u64 decode_at(const uint8_t *file, const DPage &pg, const DRun *runs,
+                                         const uint32_t *page_runs, uint32_t pidx, uint32_t i) {
+    if (pg.kind == 0) {
+        const uint8_t *src = file + pg.off + (u64)i * pg.width;
+        if (pg.width == 4) {
+            int32_t v;
+            memcpy(&v, src, 4);
+            return (u64)(i64)v;
+        }
+        u64 v;
+        memcpy(&v, src, 8);
+        return v;
+    }
+    const uint32_t nr = page_runs[2 * pidx], bw = page_runs[2 * pidx + 1];
+    const DRun *rr = runs + pg.run_base;
+    uint32_t lo = 0, hi = nr;  // last run with start <= i
+    if (nr == 0) return 0;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (rr[mid].start <= i) lo = mid;
+        else hi = mid;
+    }
+    const DRun rn = rr[lo];
+    uint32_t idx;
+    if (i >= rn.start + rn.cnt) {
+        idx = 0xffffffffu;  // past the decoded values (truncated page): left unset → 0
+    } else if (rn.off == 0xffffffffu) {
+        idx = rn.val;
+    } else {
+        const u64 bit = (u64)(i - rn.start) * bw;
+        const uint8_t *b = file + pg.off + rn.off + (bit >> 3);
+        u64 w = 0;
+        const uint32_t nb = (uint32_t)(((bit & 7) + bw + 7) >> 3);
+        for (uint32_t k = 0; k < nb; k++) w |= (u64)b[k] << (8 * k);
+        idx = (uint32_t)((w >> (bit & 7)) & (bw >= 32 ? 0xffffffffull : ((1ull << bw) - 1ull)));
+    }
+    if (idx >= pg.dict_n) return 0;  // the reference maps an out-of-range index to 0
+    const uint8_t *src = file + pg.dict_off + (u64)idx * pg.width;
+    if (pg.width == 4) {
+        int32_t v;
+        memcpy(&v, src, 4);
+        return (u64)(i64)v;
+    }
+    u64 v;
+    memcpy(&v, src, 8);
+    return v;
+}
+
+struct PqChunkArg {
+    uint32_t rg;          // index into the batch's row groups
+    uint32_t row0, nrows; // rows [row0, row0 + nrows) of the row group
+};
+
+struct PqScan {
+    int32_t n_cols;
+    int32_t out_type[GB_MAX_COLS];   // gb_type of each compacted output column
+    int32_t n_filters;
+    Filter filters[GB_MAX_FILTERS];
+    void *out[GB_MAX_COLS];
+    u64 out_cap;
+};
+
+// Row chunks of one batch.  Pass 1 decodes only the filter columns and keeps
+// a row flag; pass 2 decodes the needed columns of the surviving rows only
+// (late materialisation) into the compacted output.
+// col_pages[2 * (rg * n_cols + c)] = {page begin, page end} in `pages`.
+#define PQ_CHUNK 4096
+__device__ __forceinline__ u64 decode_col(const uint8_t *file, const DPage *pages, const DRun *runs,
+                                          const uint32_t *page_runs, const uint32_t *col_pages, int n_cols,
+                                          uint32_t rg, int c, uint32_t r) {
+    const uint32_t pb = col_pages[2 * (rg * n_cols + c)], pe = col_pages[2 * (rg * n_cols + c) + 1];
+    const uint32_t pi = find_page(pages, pb, pe, r);
+    const DPage &pg = pages[pi];
+    return decode_at(file, pg, runs, page_runs, pi, r - pg.first_row);
+}
+
+__global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPage *pages, const DRun *runs,
+                                                 const uint32_t *page_runs, const uint32_t *col_pages,
+                                                 const PqChunkArg *chunks, uint32_t n_chunks,
+                                                 const __grid_constant__ PqScan S, Ctl *ctl) {
+    constexpr int PER = PQ_CHUNK / 256;
+    for (uint32_t ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
+        const PqChunkArg ch = chunks[ci];
+        bool keep[PER];
+        u32 mine = 0;
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            const uint32_t rr = (uint32_t)j * 256 + threadIdx.x;
+            keep[j] = rr < ch.nrows;
+            if (!keep[j]) continue;
+            const uint32_t r = ch.row0 + rr;
+            for (int q = 0; q < S.n_filters && keep[j]; q++) {
+                const Filter &f = S.filters[q];
+                const u64 x = decode_col(file, pages, runs, page_runs, col_pages, S.n_cols, ch.rg, f.col, r);
+                if (S.out_type[f.col] == GB_T_DOUBLE) keep[j] = cmp_f(f.op, __longlong_as_double((i64)x), f.dc);
+                else keep[j] = cmp_i(f.op, (i64)x, f.ic);
+            }
+            mine += keep[j];
+        }
+        u64 o = block_out_base(ctl, mine);
+#pragma unroll
+        for (int j = 0; j < PER; j++) {
+            if (!keep[j]) continue;
+            if (o >= S.out_cap) {
+                atomicOr(&ctl->err, (u32)ERR_OUT_OVERFLOW);
+                continue;
+            }
+            const uint32_t r = ch.row0 + (uint32_t)j * 256 + threadIdx.x;
+            for (int c = 0; c < S.n_cols; c++) {
+                const u64 x = decode_col(file, pages, runs, page_runs, col_pages, S.n_cols, ch.rg, c, r);
+                switch (S.out_type[c]) {
+                case GB_T_SMALLINT: ((int16_t *)S.out[c])[o] = (int16_t)(i64)x; break;
+                case GB_T_INTEGER: ((int32_t *)S.out[c])[o] = (int32_t)(i64)x; break;
+                default: ((u64 *)S.out[c])[o] = x; break;
+                }
+            }
+            o++;
+        }
+    }
+}
+
+// ================================================================== C ABI
+static gb_status pq_fail_if_err(Ctl &c) {
+    if (c.err & ERR_CORRUPT) {
+        set_error("malformed Parquet page data (RLE / bit-packed run outside its page)");
+        return GB_ERR_CORRUPT;
+    }
+    if (c.err & ERR_OUT_OVERFLOW) {
+        set_error("Parquet scan output overflow (internal invariant violated)");
+        return GB_ERR_CUDA;
+    }
+    return GB_OK;
+}
+
+extern "C" {
+
+gb_status gb_pq_open(const uint8_t *bytes, uint64_t size, gb_pq_file **out) {
+    if (!bytes || !out) {
+        set_error("null argument");
+        return GB_ERR_INVALID;
+    }
+    *out = nullptr;
+    gb_pq_file *f = new gb_pq_file();
+    f->host = bytes;
+    f->size = size;
+    gb_status s = parse_footer(f);
+    for (uint32_t g = 0; !s && g < f->chunks.size(); g++)
+        for (uint32_t c = 0; !s && c < f->cols.size(); c++) {
+            if (f->chunks[g][c].codec != 0) {
+                set_error("compressed Parquet column chunks (codec %d) are not supported on the GPU path",
+                          f->chunks[g][c].codec);
+                s = GB_ERR_UNSUPPORTED;
+                break;
+            }
+            s = parse_pages(f, g, c);
+        }
+    if (s) {
+        delete f;
+        return s;
+    }
+    *out = f;
+    return GB_OK;
+}
+
+uint32_t gb_pq_num_row_groups(const gb_pq_file *f) { return f ? (uint32_t)f->rg_rows.size() : 0; }
+uint64_t gb_pq_num_rows(const gb_pq_file *f) { return f ? f->num_rows : 0; }
+uint32_t gb_pq_num_columns(const gb_pq_file *f) { return f ? (uint32_t)f->cols.size() : 0; }
+
+gb_status gb_pq_column_info(const gb_pq_file *f, uint32_t col, char *name, uint32_t name_cap, int32_t *type) {
+    if (!f || col >= f->cols.size()) return GB_ERR_INVALID;
+    if (name && name_cap) {
+        strncpy(name, f->cols[col].name.c_str(), name_cap - 1);
+        name[name_cap - 1] = 0;
+    }
+    if (type) *type = f->cols[col].gtype;
+    return GB_OK;
+}
+
+gb_status gb_pq_upload(gb_pq_file *f, void *stream) {
+    if (!f) return GB_ERR_INVALID;
+    if (f->dev) return GB_OK;
+    GB_CUDA(cudaMalloc(&f->dev, f->size));
+    GB_CUDA(cudaMemcpyAsync(f->dev, f->host, f->size, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    GB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return GB_OK;
+}
+
+void gb_pq_close(gb_pq_file *f) {
+    if (!f) return;
+    if (f->dev) cudaFree(f->dev);
+    delete f;
+}
+
+}  // extern "C"
+
+// The aggregate-side ingest lives here so the handle's internals stay in
+// gb_agg.cu: gb_agg_ingest_parquet decodes + filters + compacts a batch of row
+// groups, then hands the compacted device columns to gb_agg_ingest.
+struct PqScratch {
+    void *file_dev = nullptr;
+    size_t file_cap = 0;
+    void *pages = nullptr, *runs = nullptr, *page_runs = nullptr, *dict_pages = nullptr, *col_pages = nullptr,
+         *chunks = nullptr, *ctl = nullptr;
+    size_t pages_cap = 0, runs_cap = 0, page_runs_cap = 0, dict_pages_cap = 0, col_pages_cap = 0, chunks_cap = 0,
+           ctl_cap = 0;
+    void *out[GB_MAX_COLS] = {};
+    size_t out_cap_rows = 0;
+};
+
+static gb_status grow(void *&p, size_t &cap, size_t need) {
+    if (need <= cap) return GB_OK;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max(need, (size_t)4096);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        return cuda_fail(e, "cudaMalloc (parquet scratch)");
+    }
+    cap = want;
+    return GB_OK;
+}
+
+static std::mutex g_pq_mu;
+static std::map<gb_agg *, PqScratch *> g_pq_scratch;
+
+static PqScratch *g_scratch_for(gb_agg *h) {
+    std::lock_guard<std::mutex> lk(g_pq_mu);
+    auto it = g_pq_scratch.find(h);
+    if (it != g_pq_scratch.end()) return it->second;
+    PqScratch *s = new PqScratch();
+    g_pq_scratch[h] = s;
+    return s;
+}
+
+void gb_pq_release_scratch(gb_agg *h) {
+    PqScratch *s = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_pq_mu);
+        auto it = g_pq_scratch.find(h);
+        if (it == g_pq_scratch.end()) return;
+        s = it->second;
+        g_pq_scratch.erase(it);
+    }
+    for (void *p : {s->file_dev, s->pages, s->runs, s->page_runs, s->dict_pages, s->col_pages, s->chunks, s->ctl})
+        if (p) cudaFree(p);
+    for (void *p : s->out)
+        if (p) cudaFree(p);
+    delete s;
+}
+
+extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg_begin, uint32_t rg_end,
+                                           const int32_t *col_map, int32_t mem, void *stream) {
+    if (!h || !f || !col_map || rg_end > f->rg_rows.size() || rg_begin > rg_end) {
+        set_error("invalid arguments to gb_agg_ingest_parquet");
+        return GB_ERR_INVALID;
+    }
+    if (rg_begin == rg_end) return GB_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    AggView v;
+    gb_status s = gb_agg_view(h, &v);
+    if (s) return s;
+    const int nc = v.n_cols;
+    if (nc > 8) {
+        set_error("at most 8 Parquet columns per GROUP BY on the GPU path");
+        return GB_ERR_UNSUPPORTED;
+    }
+    for (int c = 0; c < nc; c++) {
+        const int fc = col_map[c];
+        if (fc < 0 || fc >= (int)f->cols.size()) {
+            set_error("column map entry %d out of range", c);
+            return GB_ERR_INVALID;
+        }
+        const PqColumn &pc = f->cols[fc];
+        if (pc.gtype == 0) {
+            set_error("Parquet column '%s' has a physical type the GPU path does not decode", pc.name.c_str());
+            return GB_ERR_UNSUPPORTED;
+        }
+        if (pc.repetition != 0) {
+            set_error("Parquet column '%s' is OPTIONAL/REPEATED; the GPU path reads REQUIRED columns", pc.name.c_str());
+            return GB_ERR_UNSUPPORTED;
+        }
+        const int want = v.col_types[c];
+        const bool ok = want == pc.gtype || (want == GB_T_INTEGER && pc.gtype == GB_T_SMALLINT) ||
+                        (want == GB_T_BIGINT && (pc.gtype == GB_T_INTEGER || pc.gtype == GB_T_SMALLINT)) ||
+                        (want == GB_T_SMALLINT && pc.gtype == GB_T_INTEGER);
+        if (!ok) {
+            set_error("column %d: spec type %d does not match Parquet column '%s'", c, want, pc.name.c_str());
+            return GB_ERR_INVALID;
+        }
+    }
+    PqScratch *S = g_scratch_for(h);
+    // device bytes: the uploaded file, or this batch's byte range copied now
+    uint64_t lo = ~0ull, hi = 0;
+    for (uint32_t g = rg_begin; g < rg_end; g++)
+        for (int c = 0; c < nc; c++) {
+            const PqChunk &ch = f->chunks[g][col_map[c]];
+            lo = std::min(lo, ch.start);
+            hi = std::max(hi, ch.start + ch.size);
+        }
+    const uint8_t *dfile;
+    uint64_t base = 0;
+    if (mem == GB_MEM_DEVICE) {
+        if (!f->dev) {
+            set_error("gb_pq_upload the file before ingesting with GB_MEM_DEVICE");
+            return GB_ERR_STATE;
+        }
+        dfile = (const uint8_t *)f->dev;
+    } else {
+        if ((s = grow(S->file_dev, S->file_cap, hi - lo))) return s;
+        GB_CUDA(cudaMemcpyAsync(S->file_dev, f->host + lo, hi - lo, cudaMemcpyHostToDevice, st));
+        dfile = (const uint8_t *)S->file_dev;
+        base = lo;
+    }
+    // page table of the batch (offsets relative to dfile)
+    std::vector<DPage> pages;
+    std::vector<uint32_t> dict_pages, col_pages;
+    std::vector<PqChunkArg> chunks;
+    uint64_t rows = 0;
+    uint32_t run_total = 0;
+    for (uint32_t g = rg_begin; g < rg_end; g++) {
+        for (int c = 0; c < nc; c++) {
+            const PqChunk &ch = f->chunks[g][col_map[c]];
+            const PqColumn &pc = f->cols[col_map[c]];
+            col_pages.push_back((uint32_t)pages.size());
+            for (uint32_t p = ch.page_begin; p < ch.page_end; p++) {
+                const PqPage &pp = f->pages[p];
+                DPage d{};
+                d.off = pp.off - base;
+                d.first_row = pp.first_row;
+                d.n_values = pp.n_values;
+                d.bytes = pp.bytes;
+                d.kind = pp.kind;
+                d.width = pc.width;
+                if (pp.kind == 1) {
+                    if (ch.dict_off < 0) {
+                        set_error("dictionary-encoded page without a dictionary page");
+                        return GB_ERR_CORRUPT;
+                    }
+                    d.dict_off = (uint64_t)ch.dict_off - base;
+                    d.dict_n = ch.dict_n;
+                    d.run_base = run_total;
+                    d.run_cap = std::min<uint32_t>(pp.n_values, pp.bytes) + 1;
+                    run_total += d.run_cap;
+                    dict_pages.push_back((uint32_t)pages.size());
+                }
+                pages.push_back(d);
+            }
+            col_pages.push_back((uint32_t)pages.size());
+        }
+        for (uint64_t r0 = 0; r0 < f->rg_rows[g]; r0 += PQ_CHUNK)
+            chunks.push_back({g - rg_begin, (uint32_t)r0, (uint32_t)std::min<uint64_t>(PQ_CHUNK, f->rg_rows[g] - r0)});
+        rows += f->rg_rows[g];
+    }
+    if ((s = grow(S->pages, S->pages_cap, pages.size() * sizeof(DPage))) ||
+        (s = grow(S->runs, S->runs_cap, (size_t)run_total * sizeof(DRun) + 16)) ||
+        (s = grow(S->page_runs, S->page_runs_cap, pages.size() * 8 + 16)) ||
+        (s = grow(S->dict_pages, S->dict_pages_cap, dict_pages.size() * 4 + 16)) ||
+        (s = grow(S->col_pages, S->col_pages_cap, col_pages.size() * 4)) ||
+        (s = grow(S->chunks, S->chunks_cap, chunks.size() * sizeof(PqChunkArg))) ||
+        (s = grow(S->ctl, S->ctl_cap, sizeof(Ctl))))
+        return s;
+    GB_CUDA(cudaMemcpyAsync(S->pages, pages.data(), pages.size() * sizeof(DPage), cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(S->col_pages, col_pages.data(), col_pages.size() * 4, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(S->chunks, chunks.data(), chunks.size() * sizeof(PqChunkArg), cudaMemcpyHostToDevice, st));
+    if (!dict_pages.empty())
+        GB_CUDA(cudaMemcpyAsync(S->dict_pages, dict_pages.data(), dict_pages.size() * 4, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemsetAsync(S->ctl, 0, sizeof(Ctl), st));
+    Ctl *dctl = (Ctl *)S->ctl;
+    if (!dict_pages.empty()) {
+        k_pq_runs<<<(unsigned)dict_pages.size(), 128, 0, st>>>(dfile, (const DPage *)S->pages,
+                                                               (const uint32_t *)S->dict_pages, (DRun *)S->runs,
+                                                               (uint32_t *)S->page_runs, dctl);
+        GB_CUDA(cudaGetLastError());
+        gb_agg_count_launch(h, 1);
+    }
+    // compacted output columns (batch rows bound the survivors)
+    if (S->out_cap_rows < rows) {
+        for (int c = 0; c < GB_MAX_COLS; c++)
+            if (S->out[c]) {
+                cudaFree(S->out[c]);
+                S->out[c] = nullptr;
+            }
+        S->out_cap_rows = 0;
+        for (int c = 0; c < nc; c++) {
+            cudaError_t e = cudaMalloc(&S->out[c], rows * 8 + 64);
+            if (e != cudaSuccess) {
+                (void)cudaGetLastError();
+                return cuda_fail(e, "cudaMalloc (parquet columns)");
+            }
+        }
+        S->out_cap_rows = rows;
+    }
+    PqScan P;
+    memset(&P, 0, sizeof P);
+    P.n_cols = nc;
+    for (int c = 0; c < nc; c++) {
+        P.out_type[c] = v.col_types[c];
+        P.out[c] = S->out[c];
+    }
+    P.n_filters = v.n_filters;
+    for (int q = 0; q < v.n_filters; q++) P.filters[q] = v.filters[q];
+    P.out_cap = S->out_cap_rows;
+    {
+        const int grid = (int)std::min<size_t>(chunks.size(), (size_t)sm_count() * 8);
+        k_pq_scan<<<std::max(grid, 1), 256, 0, st>>>(dfile, (const DPage *)S->pages, (const DRun *)S->runs,
+                                                     (const uint32_t *)S->page_runs, (const uint32_t *)S->col_pages,
+                                                     (const PqChunkArg *)S->chunks, (uint32_t)chunks.size(), P, dctl);
+        GB_CUDA(cudaGetLastError());
+        gb_agg_count_launch(h, 1);
+    }
+    Ctl c;
+    GB_CUDA(cudaMemcpyAsync(&c, dctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if ((s = pq_fail_if_err(c))) return s;
+    // the survivors go through the ordinary ingest (filters already applied)
+    gb_col cols[GB_MAX_COLS];
+    for (int q = 0; q < nc; q++) cols[q] = {S->out[q], nullptr, nullptr};
+    return gb_agg_ingest_prefiltered(h, cols, c.out_count, stream);
+}

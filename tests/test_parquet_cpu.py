@@ -1,0 +1,69 @@
+"""Parquet on the host: the project writer (checked against pyarrow when it is
+installed), the oracle's RleDecoder restatement on the writer's encoding, and
+the library's footer / page-header parser (no GPU needed)."""
+import io
+
+import numpy as np
+import pytest
+
+import oracle
+from slothdb_gb300 import capi
+from slothdb_gb300 import parquet as pq
+
+pytestmark = pytest.mark.usefixtures("oracle_lib", "gblib")
+
+
+@pytest.mark.parametrize("bw", [1, 2, 3, 5, 7, 8, 9, 13, 16, 17, 20, 24, 31, 32])
+def test_rle_hybrid_roundtrip_through_oracle(bw):
+    rng = np.random.default_rng(bw)
+    n = 10_007  # not a multiple of 8 or 32: ragged tail
+    hi = (1 << bw) - 1 if bw < 32 else 0xFFFFFFFF
+    lens = rng.geometric(0.2, n)
+    vals = rng.integers(0, hi, len(lens), dtype=np.uint64, endpoint=True).astype(np.uint32)
+    x = np.repeat(vals, lens)[:n]
+    x[100:180] = x[100]  # a long RLE run
+    enc = pq.rle_hybrid(x, bw)
+    dec = oracle.rle_decode(enc, bw, n)
+    assert np.array_equal(dec, x)
+
+
+def test_writer_matches_pyarrow():
+    pa = pytest.importorskip("pyarrow.parquet")
+    data, key, f, v = pq.filter_groupby_file(n_rows=250_000, row_group_rows=100_000, page_rows=16_384)
+    t = pa.read_table(io.BytesIO(data))
+    assert np.array_equal(t.column("key").to_numpy(), key)
+    assert np.array_equal(t.column("f").to_numpy(), f)
+    assert np.array_equal(t.column("v").to_numpy(), v)
+    assert str(t.schema.field("f").type) == "int16"
+
+
+def test_library_parses_footer_and_pages():
+    data, key, f, v = pq.filter_groupby_file(n_rows=250_000, row_group_rows=100_000, page_rows=16_384)
+    pf = capi.ParquetFile(data)
+    assert pf.num_row_groups == 3
+    assert pf.num_rows == 250_000
+    assert pf.columns() == [("key", capi.INTEGER), ("f", capi.SMALLINT), ("v", capi.BIGINT)]
+    pf.close()
+
+
+@pytest.mark.parametrize("damage", ["magic", "footer_len", "truncated", "page_size"])
+def test_malformed_files_are_rejected(damage):
+    data, _, _, _ = pq.filter_groupby_file(n_rows=20_000, row_group_rows=10_000, page_rows=4096)
+    b = bytearray(data)
+    if damage == "magic":
+        b[-1] = ord("X")
+    elif damage == "footer_len":
+        b[-8:-4] = (len(b) * 2).to_bytes(4, "little")
+    elif damage == "truncated":
+        b = b[: len(b) // 2] + b[-8:]
+    elif damage == "page_size":
+        # first data page header of column 'f' lies after the key chunk; grow its
+        # compressed_page_size varint so the page runs past the chunk
+        flen = int.from_bytes(b[-8:-4], "little")
+        assert flen > 0
+        i = 4
+        # corrupt the dictionary page header's size field (first header in the file)
+        b[i + 3] = 0x7F
+    with pytest.raises(capi.GbError) as e:
+        capi.ParquetFile(bytes(b))
+    assert e.value.status in (6,)  # GB_ERR_CORRUPT
