@@ -196,16 +196,27 @@ class GroupBy:
         arr = (Col * n)()
         keep = []
         for i, a in enumerate(cols):
-            if not device and isinstance(a, np.ndarray):
+            offs = None
+            if self.col_types[i] == VARCHAR:
+                # (offsets int64[n+1], bytes uint8) — numpy arrays or device tensors
+                offs, a = a
+                if not device:
+                    offs = np.ascontiguousarray(offs, dtype=np.int64)
+                    a = np.ascontiguousarray(a, dtype=np.uint8)
+                    if len(a) == 0:
+                        a = np.zeros(1, dtype=np.uint8)
+                    keep += [offs, a]
+            elif not device and isinstance(a, np.ndarray):
                 a = np.ascontiguousarray(a, dtype=NP_TYPES[self.col_types[i]])
                 keep.append(a)
             v = validity[i] if validity is not None else None
             if v is not None and not device and isinstance(v, np.ndarray):
                 v = np.ascontiguousarray(v, dtype=np.uint64)
                 keep.append(v)
-            arr[i] = Col(_arr_ptr(a), _arr_ptr(v), None)
+            arr[i] = Col(_arr_ptr(a), _arr_ptr(v), _arr_ptr(offs))
         if nrows is None:
-            nrows = len(cols[0])
+            c0 = cols[0]
+            nrows = len(c0[0]) - 1 if self.col_types[0] == VARCHAR else len(c0)
         check(self.lib.gb_agg_ingest(self.h, arr, int(nrows), MEM_DEVICE if device else MEM_HOST,
                                      C.c_void_p(stream) if stream else None))
 
@@ -220,6 +231,20 @@ class GroupBy:
         n = int(r.n_rows)
         for c in range(r.n_cols):
             t = r.types[c]
+            if t == VARCHAR:
+                if n:
+                    offs = np.frombuffer((C.c_char * ((n + 1) * 8)).from_address(r.offsets[c]), dtype=np.int64).copy()
+                    nb = int(offs[-1])
+                    data = bytes((C.c_char * max(nb, 1)).from_address(r.data[c]))[:nb]
+                    vals = np.array([data[offs[i]:offs[i + 1]] for i in range(n)], dtype=object)
+                    vw = np.frombuffer((C.c_char * (((n + 63) // 64) * 8)).from_address(r.validity[c]),
+                                       dtype=np.uint64)
+                    bits = np.unpackbits(vw.view(np.uint8), bitorder="little")[:n].astype(bool)
+                else:
+                    vals = np.zeros(0, dtype=object)
+                    bits = np.zeros(0, dtype=bool)
+                out.append((vals, bits))
+                continue
             dt = np.dtype(NP_TYPES[t])
             if n:
                 buf = (C.c_char * (n * dt.itemsize)).from_address(r.data[c])

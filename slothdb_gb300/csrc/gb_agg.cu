@@ -11,6 +11,7 @@
 #include "gb_agg_host.h"
 #include "gb_kernels.cuh"
 #include "gb_radix.h"
+#include "gb_strdict.h"
 
 namespace gb {
 
@@ -469,6 +470,13 @@ struct gb_agg {
     u32 r_ovf_cap = 0;
     int r_grid = 0;
     u64 rows_ingested = 0;
+    // VARCHAR group key: device string dictionary (string -> dense id)
+    int str_col = -1;
+    DevBuf sd_hash, sd_ref, sd_id, sd_refid, sd_ctr, sd_arena, sd_old_hash, sd_old_ref, sd_old_id, sd_old_refid;
+    DevBuf sd_ids, sd_retry_a, sd_retry_b;
+    u64 sd_cap = 0, sd_arena_cap = 0;
+    DevBuf out_str_offs, out_str_bytes, str_lens, scan_tmp;
+    HostBuf host_str_offs, host_str_bytes;
     // tuning
     int block = 512;
     int ctas_per_sm = 2;
@@ -968,6 +976,143 @@ static gb_status radix_emit(gb_agg *h, cudaStream_t st) {
     return GB_OK;
 }
 
+
+// ------------------------------------------------------------- VARCHAR keys
+static StrDictRef strdict_ref(gb_agg *h) {
+    StrDictRef D;
+    D.hash = (u64 *)h->sd_hash.p;
+    D.ref = (u64 *)h->sd_ref.p;
+    D.id = (u64 *)h->sd_id.p;
+    D.ref_by_id = (u64 *)h->sd_refid.p;
+    u64 *ctr = (u64 *)h->sd_ctr.p;  // [0] next id, [1] arena used, [2] err (u32)
+    D.next_id = ctr;
+    D.arena_used = ctr + 1;
+    D.err = (u32 *)(ctr + 2);
+    D.cap = h->sd_cap;
+    D.arena = (uint8_t *)h->sd_arena.p;
+    D.arena_cap = h->sd_arena_cap;
+    D.max_probe = 64;
+    return D;
+}
+
+static gb_status strdict_init(gb_agg *h, u64 cap, cudaStream_t st) {
+    gb_status s;
+    if ((s = h->sd_hash.ensure(cap * 8)) || (s = h->sd_ref.ensure(cap * 8)) || (s = h->sd_id.ensure(cap * 8)) ||
+        (s = h->sd_refid.ensure(cap * 8)) || (s = h->sd_ctr.ensure(64)))
+        return s;
+    if ((s = strdict_fill((u64 *)h->sd_hash.p, cap, EMPTY_KEY, st)) || (s = strdict_fill((u64 *)h->sd_ref.p, cap, ~0ull, st)))
+        return s;
+    GB_CUDA(cudaMemsetAsync(h->sd_ctr.p, 0, 64, st));
+    h->sd_cap = cap;
+    h->launches += 2;
+    return GB_OK;
+}
+
+// Grow the dictionary table (ids are kept; slots move).
+static gb_status strdict_grow(gb_agg *h, u64 ncap, cudaStream_t st) {
+    std::swap(h->sd_hash, h->sd_old_hash);
+    std::swap(h->sd_ref, h->sd_old_ref);
+    std::swap(h->sd_id, h->sd_old_id);
+    const u64 old_cap = h->sd_cap;
+    gb_status s;
+    if ((s = h->sd_hash.ensure(ncap * 8)) || (s = h->sd_ref.ensure(ncap * 8)) || (s = h->sd_id.ensure(ncap * 8)))
+        return s;
+    if ((s = strdict_fill((u64 *)h->sd_hash.p, ncap, EMPTY_KEY, st)) || (s = strdict_fill((u64 *)h->sd_ref.p, ncap, ~0ull, st)))
+        return s;
+    // ref_by_id grows with the table (ids < claimed slots <= cap)
+    if (h->sd_refid.n < ncap * 8) {
+        if ((s = h->sd_old_refid.ensure(ncap * 8))) return s;
+        GB_CUDA(cudaMemcpyAsync(h->sd_old_refid.p, h->sd_refid.p, old_cap * 8, cudaMemcpyDeviceToDevice, st));
+        std::swap(h->sd_refid, h->sd_old_refid);
+    }
+    h->sd_cap = ncap;
+    StrDictRef D = strdict_ref(h);
+    if ((s = strdict_launch_rehash((const u64 *)h->sd_old_hash.p, (const u64 *)h->sd_old_ref.p,
+                                   (const u64 *)h->sd_old_id.p, old_cap, D, st)))
+        return s;
+    h->launches += 3;
+    return GB_OK;
+}
+
+// Encode a VARCHAR column (device bytes/offsets; offsets rebased by off_base)
+// into h->sd_ids.  batch_bytes bounds the bytes a new string can add.
+static gb_status strdict_encode(gb_agg *h, const uint8_t *bytes, const int64_t *offs, int64_t off_base,
+                                const uint64_t *valid, u64 n, u64 batch_bytes, cudaStream_t st) {
+    gb_status s;
+    if (!h->sd_cap) {
+        u64 cap = 1024;
+        while (cap < 2 * std::max<u64>(h->est_groups, 512)) cap <<= 1;
+        if ((s = strdict_init(h, cap, st))) return s;
+    }
+    // the arena can take every string of this batch
+    u64 used = 0;
+    GB_CUDA(cudaMemcpyAsync(&used, (u64 *)h->sd_ctr.p + 1, 8, cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if (used + batch_bytes + 64 > h->sd_arena_cap) {
+        const u64 ncap = std::max<u64>((used + batch_bytes) * 3 / 2 + 4096, h->sd_arena_cap * 2);
+        DevBuf nb;
+        if ((s = nb.ensure(ncap))) return s;
+        if (used) GB_CUDA(cudaMemcpyAsync(nb.p, h->sd_arena.p, used, cudaMemcpyDeviceToDevice, st));
+        GB_CUDA(cudaStreamSynchronize(st));
+        h->sd_arena.release();
+        h->sd_arena = nb;
+        h->sd_arena_cap = ncap;
+    }
+    if ((s = h->sd_ids.ensure(n * 8 + 8)) || (s = h->sd_retry_a.ensure(n * 4 + 8)) ||
+        (s = h->sd_retry_b.ensure(n * 4 + 8)))
+        return s;
+    const u32 *rows = nullptr;
+    u64 count = n;
+    u32 *retry = (u32 *)h->sd_retry_a.p;
+    u32 *other = (u32 *)h->sd_retry_b.p;
+    Ctl *dctl = (Ctl *)h->ctl_buf.p;
+    for (int round = 0; round < 40 && count; round++) {
+        GB_CUDA(cudaMemsetAsync(&dctl->aux1, 0, 4, st));
+        StrDictRef D = strdict_ref(h);
+        {
+            ProfScope ps(h, "k_strdict_encode", st);
+            if ((s = strdict_launch_encode(D, bytes, offs, off_base, valid, count, rows, (long long *)h->sd_ids.p, retry,
+                                           &dctl->aux1, &dctl->aux0, st)))
+                return s;
+        }
+        h->launches++;
+        u32 nretry = 0, err = 0;
+        GB_CUDA(cudaMemcpyAsync(&nretry, &dctl->aux1, 4, cudaMemcpyDeviceToHost, st));
+        GB_CUDA(cudaMemcpyAsync(&err, (u64 *)h->sd_ctr.p + 2, 4, cudaMemcpyDeviceToHost, st));
+        GB_CUDA(cudaStreamSynchronize(st));
+        if (err & ERR_TIMEOUT) {
+            set_error("string dictionary: a bounded wait for a published string gave up");
+            return GB_ERR_TIMEOUT;
+        }
+        if (!nretry) return GB_OK;
+        if ((s = strdict_grow(h, h->sd_cap * 2, st))) return s;
+        rows = retry;
+        count = nretry;
+        std::swap(retry, other);
+    }
+    set_error("string dictionary growth did not converge");
+    return GB_ERR_OOM;
+}
+
+// Turn the emitted ids of a VARCHAR key column into offsets + bytes.
+static gb_status strdict_emit(gb_agg *h, const long long *ids, u64 n, cudaStream_t st) {
+    gb_status s;
+    if ((s = h->str_lens.ensure(n * 8 + 8)) || (s = h->out_str_offs.ensure(n * 8 + 16)) ||
+        (s = h->scan_tmp.ensure(((n + 1023) / 1024 + 1) * 8)))
+        return s;
+    StrDictRef D = strdict_ref(h);
+    if ((s = strdict_launch_lengths(D, ids, n, (int64_t *)h->str_lens.p, st))) return s;
+    int64_t total = 0;
+    if ((s = device_exclusive_scan((const int64_t *)h->str_lens.p, (int64_t *)h->out_str_offs.p, n,
+                                   (int64_t *)h->scan_tmp.p, st, &total)))
+        return s;
+    if ((s = h->out_str_bytes.ensure((size_t)total + 16))) return s;
+    if ((s = strdict_launch_gather(D, ids, n, (const int64_t *)h->out_str_offs.p, (uint8_t *)h->out_str_bytes.p, st)))
+        return s;
+    h->launches += 4;
+    return GB_OK;
+}
+
 // ---------------------------------------------------------------- compile
 static gb_status compile_plan(gb_agg *h) {
     Plan &P = h->plan;
@@ -1009,8 +1154,15 @@ static gb_status compile_plan(gb_agg *h) {
     if (ng == 1) {
         P.key_mode = (h->col_types[P.key_col[0]] == GB_T_VARCHAR) ? KEY_STRING : KEY_SINGLE;
         if (P.key_mode == KEY_STRING) {
-            set_error("VARCHAR keys go through the batched/string path (gb_batch); not the single-query ingest");
-            return GB_ERR_UNSUPPORTED;
+            // the aggregation keys on a hidden BIGINT column of string ids
+            if (nc + 1 > GB_MAX_COLS) {
+                set_error("too many columns for a VARCHAR key (max %d)", GB_MAX_COLS - 1);
+                return GB_ERR_UNSUPPORTED;
+            }
+            h->str_col = P.key_col[0];
+            P.cols[nc].type = GB_T_BIGINT;
+            P.key_col[0] = nc;
+            P.key_type[0] = GB_T_BIGINT;
         }
     } else {
         if (P.key_type[0] == GB_T_VARCHAR || P.key_type[1] == GB_T_VARCHAR) {
@@ -1065,7 +1217,7 @@ static gb_status compile_plan(gb_agg *h) {
     };
     h->emit.clear();
     h->out_types.clear();
-    for (int i = 0; i < ng; i++) h->out_types.push_back(P.key_type[i]);
+    for (int i = 0; i < ng; i++) h->out_types.push_back(P.key_mode == KEY_STRING ? GB_T_VARCHAR : P.key_type[i]);
     if (h->aggs.empty() || h->aggs.size() > GB_MAX_AGGS) {
         set_error("need 1..%d aggregates", GB_MAX_AGGS);
         return GB_ERR_INVALID;
@@ -1121,6 +1273,7 @@ static gb_status compile_plan(gb_agg *h) {
         h->out_types.push_back(e.out_type);
     }
     P.words = words;
+    if (P.key_mode == KEY_STRING) P.n_cols = nc + 1;
     {
         int need = words + 1;
         int stride = need <= 4 ? (int)next_pow2(need) : ((need + 3) / 4) * 4;
@@ -1137,7 +1290,8 @@ static gb_status alloc_outputs(gb_agg *h, u64 rows) {
     h->out_cols.resize(nout);
     h->out_valid.resize(nout);
     for (size_t c = 0; c < nout; c++) {
-        gb_status s = h->out_cols[c].ensure((size_t)rows * type_size(h->out_types[c]) + 64);
+        const int tsz = h->out_types[c] == GB_T_VARCHAR ? 8 : type_size(h->out_types[c]);
+        gb_status s = h->out_cols[c].ensure((size_t)rows * tsz + 64);
         if (s) return s;
         s = h->out_valid[c].ensure(((size_t)rows + 63) / 64 * 8 + 64);
         if (s) return s;
@@ -1307,10 +1461,14 @@ gb_status gb_agg_ingest(gb_agg *h, const gb_col *cols, uint64_t nrows, int32_t m
     }
     if (nrows == 0) return GB_OK;
     cudaStream_t st = (cudaStream_t)stream;
-    const int nc = h->plan.n_cols;
+    const int nc = (int)h->col_types.size();  // spec columns (the plan may add a hidden id column)
     for (int c = 0; c < nc; c++) {
-        if (!cols[c].data) {
+        if (!cols[c].data && !(h->col_types[c] == GB_T_VARCHAR && cols[c].offsets)) {
             set_error("column %d has no data pointer", c);
+            return GB_ERR_INVALID;
+        }
+        if (h->col_types[c] == GB_T_VARCHAR && !cols[c].offsets) {
+            set_error("VARCHAR column %d needs offsets", c);
             return GB_ERR_INVALID;
         }
         if (cols[c].validity && !((h->nullable_mask >> c) & 1ull)) {
@@ -1318,13 +1476,26 @@ gb_status gb_agg_ingest(gb_agg *h, const gb_col *cols, uint64_t nrows, int32_t m
             return GB_ERR_INVALID;
         }
     }
+    gb_status s;
     if (mem == GB_MEM_DEVICE) {
         for (int c = 0; c < nc; c++) {
             h->plan.cols[c].data = cols[c].data;
             h->plan.cols[c].valid = cols[c].validity;
             h->plan.cols[c].offsets = cols[c].offsets;
         }
-        gb_status s = h->mode == 1 ? radix_ingest(h, nrows, st) : run_ingest(h, nrows, st);
+        if (h->str_col >= 0) {
+            const gb_col &sc = cols[h->str_col];
+            int64_t ends[2];
+            GB_CUDA(cudaMemcpyAsync(&ends[0], sc.offsets, 8, cudaMemcpyDeviceToHost, st));
+            GB_CUDA(cudaMemcpyAsync(&ends[1], sc.offsets + nrows, 8, cudaMemcpyDeviceToHost, st));
+            GB_CUDA(cudaStreamSynchronize(st));
+            if ((s = strdict_encode(h, (const uint8_t *)sc.data, sc.offsets, 0, sc.validity, nrows,
+                                    (u64)(ends[1] - ends[0]), st)))
+                return s;
+            h->plan.cols[nc].data = h->sd_ids.p;
+            h->plan.cols[nc].valid = nullptr;
+        }
+        s = h->mode == 1 ? radix_ingest(h, nrows, st) : run_ingest(h, nrows, st);
         h->rows_ingested += nrows;
         prof_collect(h);
         return s;
@@ -1344,14 +1515,14 @@ gb_status gb_agg_ingest(gb_agg *h, const gb_col *cols, uint64_t nrows, int32_t m
     }
     const u64 chunk = std::min<u64>(nrows, (u64)16 << 20);
     for (int b = 0; b < 2; b++) {
-        h->stage[b].resize(2 * nc);
+        h->stage[b].resize(3 * nc);
         for (int c = 0; c < nc; c++) {
-            gb_status s = h->stage[b][c].ensure((size_t)chunk * type_size(h->col_types[c]) + 64);
-            if (s) return s;
-            if (cols[c].validity) {
-                s = h->stage[b][nc + c].ensure((size_t)(chunk / 64 + 2) * 8);
-                if (s) return s;
+            if (h->col_types[c] == GB_T_VARCHAR) {
+                if ((s = h->stage[b][2 * nc + c].ensure((size_t)(chunk + 1) * 8))) return s;
+            } else if ((s = h->stage[b][c].ensure((size_t)chunk * type_size(h->col_types[c]) + 64))) {
+                return s;
             }
+            if (cols[c].validity && (s = h->stage[b][nc + c].ensure((size_t)(chunk / 64 + 2) * 8))) return s;
         }
     }
     const u64 nchunks = (nrows + chunk - 1) / chunk;
@@ -1360,9 +1531,24 @@ gb_status gb_agg_ingest(gb_agg *h, const gb_col *cols, uint64_t nrows, int32_t m
         u64 r0 = i * chunk, r1 = std::min<u64>(nrows, r0 + chunk);
         if (i >= 2) GB_CUDA(cudaStreamWaitEvent(h->copy_stream, h->ev_done[b], 0));
         for (int c = 0; c < nc; c++) {
-            int ts = type_size(h->col_types[c]);
-            GB_CUDA(cudaMemcpyAsync(h->stage[b][c].p, (const char *)cols[c].data + r0 * ts, (r1 - r0) * ts,
-                                    cudaMemcpyHostToDevice, h->copy_stream));
+            if (h->col_types[c] == GB_T_VARCHAR) {
+                const int64_t *ho = cols[c].offsets;
+                const u64 nb = (u64)(ho[r1] - ho[r0]);
+                if (h->stage[b][c].n < nb + 16) {
+                    GB_CUDA(cudaStreamSynchronize(h->copy_stream));
+                    GB_CUDA(cudaDeviceSynchronize());
+                    gb_status s2 = h->stage[b][c].ensure(nb + 16);
+                    if (s2) return s2;
+                }
+                GB_CUDA(cudaMemcpyAsync(h->stage[b][c].p, (const char *)cols[c].data + ho[r0], nb,
+                                        cudaMemcpyHostToDevice, h->copy_stream));
+                GB_CUDA(cudaMemcpyAsync(h->stage[b][2 * nc + c].p, ho + r0, (r1 - r0 + 1) * 8, cudaMemcpyHostToDevice,
+                                        h->copy_stream));
+            } else {
+                int ts = type_size(h->col_types[c]);
+                GB_CUDA(cudaMemcpyAsync(h->stage[b][c].p, (const char *)cols[c].data + r0 * ts, (r1 - r0) * ts,
+                                        cudaMemcpyHostToDevice, h->copy_stream));
+            }
             if (cols[c].validity) {
                 // chunk boundaries are multiples of 64 rows (chunk = 16Mi)
                 GB_CUDA(cudaMemcpyAsync(h->stage[b][nc + c].p, cols[c].validity + r0 / 64, ((r1 - r0) + 63) / 64 * 8,
@@ -1372,7 +1558,7 @@ gb_status gb_agg_ingest(gb_agg *h, const gb_col *cols, uint64_t nrows, int32_t m
         GB_CUDA(cudaEventRecord(h->ev_copied[b], h->copy_stream));
         return GB_OK;
     };
-    gb_status s = issue_copy(0);
+    s = issue_copy(0);
     if (s) return s;
     for (u64 i = 0; i < nchunks; i++) {
         int b = (int)(i & 1);
@@ -1383,6 +1569,15 @@ gb_status gb_agg_ingest(gb_agg *h, const gb_col *cols, uint64_t nrows, int32_t m
             h->plan.cols[c].data = h->stage[b][c].p;
             h->plan.cols[c].valid = cols[c].validity ? (const uint64_t *)h->stage[b][nc + c].p : nullptr;
             h->plan.cols[c].offsets = nullptr;
+        }
+        if (h->str_col >= 0) {
+            const int c = h->str_col;
+            const int64_t *ho = cols[c].offsets;
+            if ((s = strdict_encode(h, (const uint8_t *)h->stage[b][c].p, (const int64_t *)h->stage[b][2 * nc + c].p,
+                                    ho[r0], h->plan.cols[c].valid, r1 - r0, (u64)(ho[r1] - ho[r0]), st)))
+                return s;
+            h->plan.cols[nc].data = h->sd_ids.p;
+            h->plan.cols[nc].valid = nullptr;
         }
         if ((s = (h->mode == 1 ? radix_ingest(h, r1 - r0, st) : run_ingest(h, r1 - r0, st)))) return s;
         h->rows_ingested += r1 - r0;
@@ -1420,7 +1615,11 @@ gb_status gb_agg_finalize(gb_agg *h, void *stream) {
     if ((s = check_err(h))) return s;
     h->n_rows_out = h->ctl_host.out_count;
     h->topn_applied = false;
-    if (h->topn && h->topn_limit > 0 && h->topn_limit <= 1024 && h->n_rows_out > 0) {
+    if (h->str_col >= 0) {
+        // VARCHAR keys: the TopN hint is not applied (the ORDER BY above sorts
+        // the full result); ids become offsets + bytes
+        if ((s = strdict_emit(h, (const long long *)h->out_cols[0].p, h->n_rows_out, st))) return s;
+    } else if (h->topn && h->topn_limit > 0 && h->topn_limit <= 1024 && h->n_rows_out > 0) {
         if ((s = run_topn(h, st))) return s;
     }
     h->finalized = true;
@@ -1435,6 +1634,12 @@ static void fill_result_view(gb_agg *h, gb_result *out, bool host) {
     h->res_valid.resize(nout);
     h->res_offsets.assign(nout, nullptr);
     for (size_t c = 0; c < nout; c++) {
+        if (h->out_types[c] == GB_T_VARCHAR) {
+            h->res_ptrs[c] = host ? h->host_str_bytes.p : h->out_str_bytes.p;
+            h->res_offsets[c] = (const int64_t *)(host ? h->host_str_offs.p : h->out_str_offs.p);
+            h->res_valid[c] = (const uint64_t *)(host ? h->host_valid[c].p : h->out_valid[c].p);
+            continue;
+        }
         if (host) {
             h->res_ptrs[c] = h->host_cols[c].p;
             h->res_valid[c] = (const uint64_t *)h->host_valid[c].p;
@@ -1468,13 +1673,22 @@ gb_status gb_agg_result(gb_agg *h, gb_result *out) {
         auto &cols = h->topn_applied ? h->top_cols : h->out_cols;
         auto &val = h->topn_applied ? h->top_valid : h->out_valid;
         for (size_t c = 0; c < nout; c++) {
-            size_t bytes = (size_t)n * type_size(h->out_types[c]);
             size_t vbytes = ((size_t)n + 63) / 64 * 8;
             gb_status s;
-            if ((s = h->host_cols[c].ensure(bytes + 8))) return s;
             if ((s = h->host_valid[c].ensure(vbytes + 8))) return s;
-            if (bytes) GB_CUDA(cudaMemcpyAsync(h->host_cols[c].p, cols[c].p, bytes, cudaMemcpyDeviceToHost, 0));
             if (vbytes) GB_CUDA(cudaMemcpyAsync(h->host_valid[c].p, val[c].p, vbytes, cudaMemcpyDeviceToHost, 0));
+            if (h->out_types[c] == GB_T_VARCHAR) {
+                if ((s = h->host_str_offs.ensure((n + 1) * 8))) return s;
+                GB_CUDA(cudaMemcpy(h->host_str_offs.p, h->out_str_offs.p, (n + 1) * 8, cudaMemcpyDeviceToHost));
+                const int64_t nb = ((const int64_t *)h->host_str_offs.p)[n];
+                if ((s = h->host_str_bytes.ensure((size_t)nb + 8))) return s;
+                if (nb) GB_CUDA(cudaMemcpy(h->host_str_bytes.p, h->out_str_bytes.p, nb, cudaMemcpyDeviceToHost));
+                if ((s = h->host_cols[c].ensure(8))) return s;
+                continue;
+            }
+            size_t bytes = (size_t)n * type_size(h->out_types[c]);
+            if ((s = h->host_cols[c].ensure(bytes + 8))) return s;
+            if (bytes) GB_CUDA(cudaMemcpyAsync(h->host_cols[c].p, cols[c].p, bytes, cudaMemcpyDeviceToHost, 0));
         }
         GB_CUDA(cudaStreamSynchronize(0));
         h->n_rows_out = n;
@@ -1500,6 +1714,7 @@ gb_status gb_agg_reset(gb_agg *h) {
     if (s) return s;
     GB_CUDA(cudaMemset(h->ctl_buf.p, 0, sizeof(Ctl)));
     h->n_groups = 0;
+    h->sd_cap = 0;  // the string dictionary is rebuilt by the next ingest
     h->r_ready = false;
     h->rows_ingested = 0;
     h->finalized = false;
@@ -1522,6 +1737,12 @@ void gb_agg_destroy(gb_agg *h) {
     for (auto &b : h->out_valid) b.release();
     for (auto &b : h->top_cols) b.release();
     for (auto &b : h->top_valid) b.release();
+    for (DevBuf *b : {&h->sd_hash, &h->sd_ref, &h->sd_id, &h->sd_refid, &h->sd_ctr, &h->sd_arena, &h->sd_old_hash,
+                      &h->sd_old_ref, &h->sd_old_id, &h->sd_old_refid, &h->sd_ids, &h->sd_retry_a, &h->sd_retry_b,
+                      &h->out_str_offs, &h->out_str_bytes, &h->str_lens, &h->scan_tmp})
+        b->release();
+    h->host_str_offs.release();
+    h->host_str_bytes.release();
     for (DevBuf *b : {&h->r_skeys, &h->r_scnt, &h->r_hist, &h->r_hot_keys, &h->r_hot_part, &h->r_cursor, &h->r_part,
                       &h->r_part2, &h->r_ovf, &h->r_off, &h->r_cap, &h->r_off2, &h->r_cap2, &h->r_hot_idx,
                       &h->r_hot_list, &h->r_hstate})

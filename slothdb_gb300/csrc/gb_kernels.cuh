@@ -52,6 +52,7 @@ __device__ __forceinline__ int make_key(const Plan &P, u64 r, u64 &pk) {
         const DevCol &c = P.cols[P.key_col[0]];
         if (!row_valid(c.valid, r)) { pk = 0; return 2; }
         pk = (u64)load_int(c, r);
+        if (P.key_mode == KEY_STRING && (i64)pk < 0) { pk = 0; return 2; }  // NULL string → id -1
         return pk == EMPTY_KEY ? 1 : 0;
     }
     const DevCol &ca = P.cols[P.key_col[0]];

@@ -24,7 +24,7 @@ def run_gpu(col_types, group_cols, aggs, cols, filters=(), nulls=None, est_group
     try:
         if topn:
             g.set_topn(*topn)
-        n = len(cols[0])
+        n = (len(cols[0][0]) - 1) if col_types[0] == capi.VARCHAR else len(cols[0])
         validity = None
         if nulls is not None:
             validity = [capi.validity_words(~m) if m is not None else None for m in nulls]
@@ -32,14 +32,15 @@ def run_gpu(col_types, group_cols, aggs, cols, filters=(), nulls=None, est_group
         for lo, hi in bounds:
             if hi <= lo and n > 0:
                 continue
-            part = [c[lo:hi] for c in cols]
+            part = [_slice(c, t, lo, hi) for c, t in zip(cols, col_types)]
             vpart = None
             if validity is not None:
                 assert lo % 64 == 0
                 vpart = [v[lo // 64:(hi + 63) // 64] if v is not None else None for v in validity]
             if device:
                 import torch
-                tens = [torch.from_numpy(np.ascontiguousarray(p)).cuda() for p in part]
+                tens = [(torch.from_numpy(p[0]).cuda(), torch.from_numpy(p[1]).cuda()) if t == capi.VARCHAR
+                        else torch.from_numpy(np.ascontiguousarray(p)).cuda() for p, t in zip(part, col_types)]
                 vt = None
                 if vpart is not None:
                     vt = [torch.from_numpy(v.view(np.int64)).cuda() if v is not None else None for v in vpart]
@@ -60,6 +61,15 @@ def run_gpu(col_types, group_cols, aggs, cols, filters=(), nulls=None, est_group
     d = gpu_to_dict(res, n_keys, out_types)
     d["launches"] = launches
     return d
+
+
+def _slice(c, t, lo, hi):
+    if t == capi.VARCHAR:
+        offs, data = c
+        o = offs[lo:hi + 1]
+        return (np.ascontiguousarray(o - o[0]), np.ascontiguousarray(data[o[0]:o[-1]]) if o[-1] > o[0]
+                else np.zeros(1, np.uint8))
+    return c[lo:hi]
 
 
 def check(col_types, group_cols, aggs, cols, **kw):
@@ -262,3 +272,37 @@ def test_reset_reuses_handle():
             assert np.array_equal(outs[0][c][0][o0], outs[1][c][0][o1])
     finally:
         g.close()
+
+
+VARCHAR = capi.VARCHAR
+
+
+@pytest.mark.parametrize("device", [False, True])
+def test_varchar_key_batched_shape(device):
+    """VARCHAR key of length 8..32 over [a-z0-9]: COUNT(*), SUM(INT64), MAX(INT32)."""
+    (offs, data), s, m = datagen.varchar_table(300_000, 20_000, seed=31)
+    check([VARCHAR, BIGINT, INTEGER], [0], [("count_star", -1), ("sum", 1), ("max", 2)], [(offs, data), s, m],
+          device=device, est_groups=1000)
+
+
+def test_varchar_nulls_empty_and_long_strings():
+    rng = np.random.default_rng(32)
+    pool = [b"", b"a", b"ab", b"x" * 12, b"x" * 13, b"prefix-shared-1", b"prefix-shared-2",
+            bytes(rng.integers(0, 256, 300, dtype=np.uint8))]
+    n = 50_000
+    pick = rng.integers(0, len(pool), n)
+    strs = [pool[i] for i in pick]
+    lens = np.array([len(x) for x in strs], dtype=np.int64)
+    offs = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(lens, out=offs[1:])
+    data = np.frombuffer(b"".join(strs), dtype=np.uint8)
+    kn = rng.random(n) < 0.05
+    v = rng.integers(0, 100, n, dtype=np.int64)
+    check([VARCHAR, BIGINT], [0], [("count_star", -1), ("sum", 1)], [(offs, data), v], nulls=[kn, None],
+          chunks=8192)
+
+
+def test_varchar_dictionary_growth():
+    """100K distinct strings into a dictionary sized for 16: retries + rehash."""
+    (offs, data), s, m = datagen.varchar_table(400_000, 100_000, seed=33)
+    check([VARCHAR, BIGINT, INTEGER], [0], [("count_star", -1), ("sum", 1)], [(offs, data), s, m], est_groups=16)
