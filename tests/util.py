@@ -11,7 +11,8 @@ def _order(keys, key_null):
     cols = []
     for k, kn in zip(reversed(keys), reversed(key_null)):
         if k.dtype == object:
-            # strings: rank by sorted unique values
+            # strings: rank by sorted unique values (NULL entries ranked first)
+            k = np.array([b"" if n else x for x, n in zip(k, kn)], dtype=object)
             uniq = sorted(set(k.tolist()))
             pos = {s: i for i, s in enumerate(uniq)}
             k = np.array([pos[s] for s in k.tolist()], dtype=np.int64)
@@ -48,7 +49,9 @@ def compare(gpu, orc, rel_tol=REL_TOL_F64, check_order=False):
         assert np.array_equal(gn, on), "key NULL flags differ (col %d)" % i
         gk, ok = gpu["keys"][i][go], orc["keys"][i][oo]
         if ok.dtype == object:
-            assert list(gk) == list(ok), "string keys differ"
+            gl = [b"" if n else x for x, n in zip(gk, gn)]
+            ol = [b"" if n else x for x, n in zip(ok, on)]
+            assert gl == ol, "string keys differ"
         else:
             assert np.array_equal(np.where(gn, 0, gk.astype(np.int64)), np.where(on, 0, ok.astype(np.int64))), \
                 "keys differ (col %d)" % i
