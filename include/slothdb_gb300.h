@@ -233,6 +233,34 @@ void gb_pq_close(gb_pq_file *f);
 gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg_begin, uint32_t rg_end, const int32_t *col_map,
                                 int32_t mem, void *stream);
 
+/* ----------------------------------------------------------------- batches
+ * Many independent GROUP BY queries over device-resident tables, executed
+ * together.  The reference runs each such query on its own, through the
+ * generic chunk loop of its hash aggregate (composite / VARCHAR keys,
+ * src/execution/physical_planner.cpp:12291-12516, AppendGroupKey
+ * 6185-6206); gb_batch_add takes the same gb_agg_spec a single query takes,
+ * and gb_batch_result returns what gb_agg_result would for that query.
+ * gb_batch_run executes every query with a few launches in total — table
+ * init, VARCHAR key encoding, one persistent aggregation kernel over a
+ * device work queue of (query, tile) items, compaction — captured as a CUDA
+ * graph on the first run and replayed on later runs.  A query that needs a
+ * host decision (hash-table growth, string-dictionary growth) is re-run on
+ * its own afterwards; gb_batch_slow_queries counts them for the last run.
+ * Column pointers (gb_col) must be device memory and stay valid, with the
+ * same row counts, for every run of the batch.  Options ("graph" 0/1,
+ * "ctas_per_sm" 1..4, "smem_slots" 0 or a power of two <= 4096,
+ * "precombine" 0/1) take effect at the next run. */
+typedef struct gb_batch gb_batch;
+gb_status gb_batch_create(gb_batch **out);
+gb_status gb_batch_add(gb_batch *b, const gb_agg_spec *spec, const gb_col *cols, uint64_t nrows, uint32_t *query_index);
+gb_status gb_batch_set_option(gb_batch *b, const char *name, int64_t value);
+gb_status gb_batch_run(gb_batch *b, void *stream);
+uint32_t gb_batch_size(const gb_batch *b);
+gb_status gb_batch_result(gb_batch *b, uint32_t query_index, gb_result *out);
+uint32_t gb_batch_slow_queries(const gb_batch *b);
+uint64_t gb_batch_kernel_launches(const gb_batch *b);
+void gb_batch_destroy(gb_batch *b);
+
 /* Allocation-free GROUP BY for callers that cannot allocate device memory
  * on their query path (an engine that hands out device memory only from
  * its own pre-reserved arena, a plugin host that forbids allocation inside

@@ -82,6 +82,16 @@ _SIGS = {
     "gb_agg_profile": (C.c_uint32, [C.c_void_p, C.POINTER(KernelStat), C.c_uint32]),
     "gb_engine_hash_aggregate": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                            C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "gb_batch_create": (C.c_int, [C.POINTER(C.c_void_p)]),
+    "gb_batch_add": (C.c_int, [C.c_void_p, C.POINTER(AggSpec), C.POINTER(Col), C.c_uint64,
+                               C.POINTER(C.c_uint32)]),
+    "gb_batch_set_option": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
+    "gb_batch_run": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gb_batch_size": (C.c_uint32, [C.c_void_p]),
+    "gb_batch_result": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Result)]),
+    "gb_batch_slow_queries": (C.c_uint32, [C.c_void_p]),
+    "gb_batch_kernel_launches": (C.c_uint64, [C.c_void_p]),
+    "gb_batch_destroy": (None, [C.c_void_p]),
     "gb_hash_aggregate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64), C.c_void_p]),
     "gb_pq_open": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
@@ -146,6 +156,64 @@ def _arr_ptr(a):
     return a.ctypes.data
 
 
+def _make_spec(col_types, group_cols, aggs, filters=(), nullable=(), est_groups=0):
+    """gb_agg_spec for a query; returns (spec, arrays the spec points into)."""
+    col_types = list(col_types)
+    group_cols = list(group_cols)
+    aggs = [(AGG_NAMES[k] if isinstance(k, str) else int(k), int(c)) for k, c in aggs]
+    filters = list(filters)
+    ct = (C.c_int32 * len(col_types))(*col_types)
+    gc = (C.c_int32 * len(group_cols))(*group_cols)
+    ag = (AggDesc * len(aggs))(*[AggDesc(k, c) for k, c in aggs])
+    fl = (Filter * max(1, len(filters)))()
+    for i, (col, op, const) in enumerate(filters):
+        opc = CMP_NAMES[op] if isinstance(op, str) else int(op)
+        if col_types[col] == DOUBLE:
+            fl[i] = Filter(col, opc, 0, float(const))
+        else:
+            fl[i] = Filter(col, opc, int(const), 0.0)
+    mask = 0
+    for c in nullable:
+        mask |= 1 << int(c)
+    spec = AggSpec(len(col_types), ct, len(group_cols), gc, len(aggs), ag,
+                   len(filters), fl if filters else None, mask, int(est_groups))
+    return spec, (ct, gc, ag, fl)
+
+
+def _read_result(r):
+    """Host gb_result -> list of (values ndarray, valid bool ndarray)."""
+    out = []
+    n = int(r.n_rows)
+    for c in range(r.n_cols):
+        t = r.types[c]
+        if t == VARCHAR:
+            if n:
+                offs = np.frombuffer((C.c_char * ((n + 1) * 8)).from_address(r.offsets[c]), dtype=np.int64).copy()
+                nb = int(offs[-1])
+                data = bytes((C.c_char * max(nb, 1)).from_address(r.data[c]))[:nb]
+                vals = np.array([data[offs[i]:offs[i + 1]] for i in range(n)], dtype=object)
+                vw = np.frombuffer((C.c_char * (((n + 63) // 64) * 8)).from_address(r.validity[c]),
+                                   dtype=np.uint64)
+                bits = np.unpackbits(vw.view(np.uint8), bitorder="little")[:n].astype(bool)
+            else:
+                vals = np.zeros(0, dtype=object)
+                bits = np.zeros(0, dtype=bool)
+            out.append((vals, bits))
+            continue
+        dt = np.dtype(NP_TYPES[t])
+        if n:
+            buf = (C.c_char * (n * dt.itemsize)).from_address(r.data[c])
+            vals = np.frombuffer(buf, dtype=dt).copy()
+            vw = np.frombuffer((C.c_char * (((n + 63) // 64) * 8)).from_address(r.validity[c]),
+                               dtype=np.uint64)
+            bits = np.unpackbits(vw.view(np.uint8), bitorder="little")[:n].astype(bool)
+        else:
+            vals = np.zeros(0, dtype=dt)
+            bits = np.zeros(0, dtype=bool)
+        out.append((vals, bits))
+    return out
+
+
 class GroupBy:
     """One GROUP BY handle (gb_agg) — the Python mirror of the operator.
 
@@ -159,23 +227,7 @@ class GroupBy:
         self.lib = load()
         self.col_types = list(col_types)
         self.group_cols = list(group_cols)
-        self.aggs = [(AGG_NAMES[k] if isinstance(k, str) else int(k), int(c)) for k, c in aggs]
-        self.filters = list(filters)
-        ct = (C.c_int32 * len(self.col_types))(*self.col_types)
-        gc = (C.c_int32 * len(self.group_cols))(*self.group_cols)
-        ag = (AggDesc * len(self.aggs))(*[AggDesc(k, c) for k, c in self.aggs])
-        fl = (Filter * max(1, len(self.filters)))()
-        for i, (col, op, const) in enumerate(self.filters):
-            opc = CMP_NAMES[op] if isinstance(op, str) else int(op)
-            if self.col_types[col] == DOUBLE:
-                fl[i] = Filter(col, opc, 0, float(const))
-            else:
-                fl[i] = Filter(col, opc, int(const), 0.0)
-        mask = 0
-        for c in nullable:
-            mask |= 1 << int(c)
-        spec = AggSpec(len(self.col_types), ct, len(self.group_cols), gc, len(self.aggs), ag,
-                       len(self.filters), fl if self.filters else None, mask, int(est_groups))
+        spec, self._spec_keep = _make_spec(col_types, group_cols, aggs, filters, nullable, est_groups)
         h = C.c_void_p()
         check(self.lib.gb_agg_create(C.byref(spec), C.byref(h)))
         self.h = h
@@ -227,36 +279,7 @@ class GroupBy:
         """Host copy of the result: list of (values ndarray, valid bool ndarray)."""
         r = Result()
         check(self.lib.gb_agg_result(self.h, C.byref(r)))
-        out = []
-        n = int(r.n_rows)
-        for c in range(r.n_cols):
-            t = r.types[c]
-            if t == VARCHAR:
-                if n:
-                    offs = np.frombuffer((C.c_char * ((n + 1) * 8)).from_address(r.offsets[c]), dtype=np.int64).copy()
-                    nb = int(offs[-1])
-                    data = bytes((C.c_char * max(nb, 1)).from_address(r.data[c]))[:nb]
-                    vals = np.array([data[offs[i]:offs[i + 1]] for i in range(n)], dtype=object)
-                    vw = np.frombuffer((C.c_char * (((n + 63) // 64) * 8)).from_address(r.validity[c]),
-                                       dtype=np.uint64)
-                    bits = np.unpackbits(vw.view(np.uint8), bitorder="little")[:n].astype(bool)
-                else:
-                    vals = np.zeros(0, dtype=object)
-                    bits = np.zeros(0, dtype=bool)
-                out.append((vals, bits))
-                continue
-            dt = np.dtype(NP_TYPES[t])
-            if n:
-                buf = (C.c_char * (n * dt.itemsize)).from_address(r.data[c])
-                vals = np.frombuffer(buf, dtype=dt).copy()
-                vw = np.frombuffer((C.c_char * (((n + 63) // 64) * 8)).from_address(r.validity[c]),
-                                   dtype=np.uint64)
-                bits = np.unpackbits(vw.view(np.uint8), bitorder="little")[:n].astype(bool)
-            else:
-                vals = np.zeros(0, dtype=dt)
-                bits = np.zeros(0, dtype=bool)
-            out.append((vals, bits))
-        return out
+        return _read_result(r)
 
     def set_option(self, name, value):
         check(self.lib.gb_agg_set_option(self.h, name.encode(), int(value)))
@@ -295,6 +318,67 @@ class GroupBy:
 
     def __exit__(self, *a):
         self.close()
+
+
+class Batch:
+    """Many GROUP BY queries over device-resident tables run together
+    (gb_batch): ``add`` takes a query's spec and its device columns (torch
+    CUDA tensors or int device pointers; VARCHAR as (offsets, bytes)),
+    ``run`` executes all of them, ``result(i)`` reads query i's result."""
+
+    def __init__(self, options=None):
+        self.lib = load()
+        h = C.c_void_p()
+        check(self.lib.gb_batch_create(C.byref(h)))
+        self.h = h
+        self._keep = []
+        for k, v in (options or {}).items():
+            self.set_option(k, v)
+
+    def add(self, col_types, group_cols, aggs, cols, nrows, validity=None, filters=(), nullable=(), est_groups=0):
+        spec, keep = _make_spec(col_types, group_cols, aggs, filters, nullable, est_groups)
+        arr = (Col * len(col_types))()
+        for i, a in enumerate(cols):
+            offs = None
+            if col_types[i] == VARCHAR:
+                offs, a = a
+            v = validity[i] if validity is not None else None
+            arr[i] = Col(_arr_ptr(a), _arr_ptr(v), _arr_ptr(offs))
+        q = C.c_uint32()
+        check(self.lib.gb_batch_add(self.h, C.byref(spec), arr, int(nrows), C.byref(q)))
+        self._keep.append((keep, cols, validity))
+        return int(q.value)
+
+    def set_option(self, name, value):
+        check(self.lib.gb_batch_set_option(self.h, name.encode(), int(value)))
+
+    def run(self, stream=None):
+        check(self.lib.gb_batch_run(self.h, C.c_void_p(stream) if stream else None))
+
+    def __len__(self):
+        return int(self.lib.gb_batch_size(self.h))
+
+    def result(self, q):
+        r = Result()
+        check(self.lib.gb_batch_result(self.h, int(q), C.byref(r)))
+        return _read_result(r)
+
+    def slow_queries(self):
+        return int(self.lib.gb_batch_slow_queries(self.h))
+
+    def launches(self):
+        return int(self.lib.gb_batch_kernel_launches(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def validity_words(valid_bool: np.ndarray) -> np.ndarray:

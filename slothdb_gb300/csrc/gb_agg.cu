@@ -1950,3 +1950,5 @@ void gb_apply_tuning(gb_agg *h) {
                           GB_OK)
         h->mode = 1;
 }
+
+#include "gb_batch.cuh"

@@ -1,0 +1,516 @@
+// gb_batch.cuh — many independent GROUP BY queries in one pass (included at
+// the end of gb_agg.cu, whose handle internals it reuses).
+//
+// The reference runs such queries one after another, each through its own
+// PhysicalHashAggregate (src/execution/physical_planner.cpp:12291-12516 for
+// composite / VARCHAR keys).  Here every query keeps its own gb_agg handle
+// (plan, HBM table, outputs, string dictionary), and the batch executes:
+//
+//   k_batch_init     one launch: every query's table to its identity state;
+//   k_batch_strdict  one launch: VARCHAR keys of every VARCHAR query → ids;
+//   k_batch_ingest   one persistent launch over a device work queue of
+//                    (query, tile) items, tiles of uneven queries interleaved;
+//                    each item copies its query's plan into shared memory and
+//                    runs the same warp pipeline as the single-query kernel;
+//   k_batch_compact  one launch: every query's table → its dense result.
+//
+// The sequence is captured once in a CUDA graph and replayed.  The graph is
+// the fast path: a query that needs a host decision (table spill, string
+// dictionary growth) is re-run on its own handle afterwards.
+
+#define BATCH_TILE 16384
+
+struct BQuery {
+    Plan P;
+    TableRef T;
+    EmitArgs E;
+    StrDictRef D;
+    const uint8_t *sbytes;
+    const int64_t *soffs;
+    const uint64_t *svalid;
+    long long *ids;
+    u32 *sretry;
+    u64 n_rows;
+    u64 table_words;
+    int32_t smem_slots;
+    int32_t is_str;
+};
+
+struct BItem {
+    u32 q;
+    u32 idx;
+};
+
+__device__ __forceinline__ void copy_words(void *dst, const void *src, int bytes) {
+    const u32 *s = (const u32 *)src;
+    u32 *d = (u32 *)dst;
+    for (int i = threadIdx.x; i < bytes / 4; i += blockDim.x) d[i] = s[i];
+}
+
+// Item (q, idx) covers words [idx * 65536, (idx+1) * 65536) of the query's
+// init range: the table words, then the validity words of every output column
+// (all ones; the emit clears the bits of NULL results).
+__global__ void k_batch_init(const BQuery *qs, const BItem *items, u32 n_items) {
+    for (u32 it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const BItem w = items[it];
+        const BQuery &q = qs[w.q];
+        const int stride = q.P.stride;
+        const u64 vwords = (q.E.out_cap + 63) / 64;
+        const u64 total = q.table_words + (u64)(q.E.n_keys + q.E.n_aggs) * vwords;
+        const u64 lo = (u64)w.idx * 65536, hi = min(total, lo + 65536);
+        for (u64 i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+            if (i >= q.table_words) {
+                const u64 j = i - q.table_words;
+                q.E.valid[j / vwords][j % vwords] = ~0ull;
+                continue;
+            }
+            const int wd = (int)(i % (u64)stride);
+            u64 v;
+            if (wd == 0) v = EMPTY_KEY;
+            else if (wd - 1 < q.P.words) v = q.P.word_init[wd - 1];
+            else v = 0;
+            q.T.slots[i] = v;
+        }
+    }
+}
+
+__global__ void k_batch_strdict(const BQuery *qs, const BItem *items, u32 n_items) {
+    __shared__ StrDictRef D;
+    __shared__ u32 s_new;
+    for (u32 it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const BItem w = items[it];
+        const BQuery &q = qs[w.q];
+        if (threadIdx.x == 0) {
+            D = q.D;
+            s_new = 0;
+        }
+        __syncthreads();
+        const u64 lo = (u64)w.idx * 8192, hi = min(q.n_rows, lo + 8192);
+        for (u64 r = lo + threadIdx.x; r < hi; r += blockDim.x) {
+            if (q.svalid && !((q.svalid[r >> 6] >> (r & 63)) & 1ull)) {
+                q.ids[r] = -1;
+                continue;
+            }
+            const int64_t a = q.soffs[r], b = q.soffs[r + 1];
+            const u32 len = (u32)(b - a);
+            const uint8_t *s = q.sbytes + a;
+            const long long id = strdict_find_or_insert(D, s, len, str_hash(s, len), &s_new);
+            q.ids[r] = id;
+            if (id < 0) atomicAdd(&q.T.ctl->aux1, 1u);  // needs the host: the query re-runs on its handle
+        }
+        __syncthreads();
+    }
+}
+
+template <bool PRECOMBINE>
+__global__ void __launch_bounds__(512) k_batch_ingest(const BQuery *qs, const BItem *items, u32 n_items, Ctl *bctl,
+                                                      int smem_bytes) {
+    extern __shared__ u64 bsm[];
+    __shared__ Plan sP;
+    __shared__ TableRef sT;
+    __shared__ u32 s_item, s_new, s_skip;
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            u32 t = ~0u;
+            const u32 c = atomicAdd(&bctl->tile_counter, 1u);
+            if (c < n_items) t = c;
+            s_item = t;
+            s_new = 0;
+            // a query stopped by its spill threshold skips its remaining tiles
+            // (the host re-runs it on its own handle)
+            s_skip = t != ~0u && *(volatile u32 *)&qs[items[t].q].T.ctl->stop != 0;
+        }
+        __syncthreads();
+        const u32 it = s_item;
+        if (it == ~0u) break;
+        if (s_skip) {
+            __syncthreads();
+            continue;
+        }
+        const BItem w = items[it];
+        const BQuery &q = qs[w.q];
+        copy_words(&sP, &q.P, (int)sizeof(Plan));
+        copy_words(&sT, &q.T, (int)sizeof(TableRef));
+        __syncthreads();
+        SmemTable sm;
+        sm.S = q.smem_slots;
+        while (sm.S && (size_t)sm.S * 8 * (1 + sP.words) > (size_t)smem_bytes) sm.S >>= 1;
+        sm.probe = 8;
+        sm.keys = bsm;
+        sm.st = bsm + sm.S;
+        smem_init(sP, sm);
+        __syncthreads();
+        const u64 t0 = (u64)w.idx * BATCH_TILE, t1 = min(q.n_rows, t0 + BATCH_TILE);
+        for (u64 base = t0 + (u64)warp * 32; base < t1; base += (u64)nwarps * 32)
+            warp_rows<PRECOMBINE>(sP, sT, sm, base, t1, &s_new);
+        __syncthreads();
+        smem_flush(sP, sT, sm, &s_new);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (s_new) atomicAdd(&sT.ctl->n_groups, s_new);
+            if (*(volatile u32 *)&sT.ctl->spill_count > sT.spill_threshold) atomicExch(&sT.ctl->stop, 1u);
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void k_batch_compact(const BQuery *qs, const BItem *items, u32 n_items) {
+    __shared__ EmitArgs sE;
+    __shared__ Plan sP;
+    for (u32 it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const BItem w = items[it];
+        const BQuery &q = qs[w.q];
+        copy_words(&sE, &q.E, (int)sizeof(EmitArgs));
+        copy_words(&sP, &q.P, (int)sizeof(Plan));
+        __syncthreads();
+        const u64 cap = q.T.cap, total = cap + 2;
+        const int stride = q.T.stride;
+        const u64 c0 = (u64)w.idx * (COMPACT_PER * 256);
+        u32 mine = 0;
+#pragma unroll
+        for (int j = 0; j < COMPACT_PER; j++) {
+            const u64 s = c0 + (u64)j * blockDim.x + threadIdx.x;
+            if (s >= total) break;
+            const u64 *sl = q.T.slots + s * (u64)stride;
+            mine += (s < cap) ? (sl[0] != EMPTY_KEY) : (sl[1] != 0);
+        }
+        u64 o = block_out_base(q.T.ctl, mine);
+#pragma unroll
+        for (int j = 0; j < COMPACT_PER; j++) {
+            const u64 s = c0 + (u64)j * blockDim.x + threadIdx.x;
+            if (s >= total) break;
+            const u64 *sl = q.T.slots + s * (u64)stride;
+            const bool occ = (s < cap) ? (sl[0] != EMPTY_KEY) : (sl[1] != 0);
+            if (!occ) continue;
+            if (o >= sE.out_cap) {
+                atomicOr(&q.T.ctl->err, (u32)ERR_OUT_OVERFLOW);
+                continue;
+            }
+            const u64 pk = (s < cap) ? sl[0] : (s == cap ? EMPTY_KEY : 0ull);
+            emit_group(sP, sE, o, pk, s == cap + 1, sl + 1);
+            o++;
+        }
+        __syncthreads();
+    }
+}
+
+// ================================================================== host
+struct gb_batch {
+    std::vector<gb_agg *> handles;
+    std::vector<std::vector<gb_col>> cols;
+    std::vector<u64> rows;
+    DevBuf qdesc, items_init, items_str, items_ingest, items_compact, bctl, qctl;
+    HostBuf qctl_host;
+    u32 n_init = 0, n_str = 0, n_ingest = 0, n_compact = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    bool prepared = false;
+    bool use_graph = true;
+    int ctas_per_sm = 2;
+    int smem_slots_max = 2048;
+    bool precombine = true;
+    u64 launches = 0;
+    std::vector<int> slow;  // queries re-run on their handle in the last run
+};
+
+static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
+    const u32 nq = (u32)b->handles.size();
+    std::vector<BQuery> qs(nq);
+    std::vector<BItem> it_init, it_str, it_ing, it_cmp;
+    gb_status s;
+    if ((s = b->qctl.ensure((size_t)nq * sizeof(Ctl) + 64)) || (s = b->bctl.ensure(sizeof(Ctl))) ||
+        (s = b->qctl_host.ensure((size_t)nq * sizeof(Ctl) + 64)))
+        return s;
+    for (u32 q = 0; q < nq; q++) {
+        gb_agg *h = b->handles[q];
+        const u64 n = b->rows[q];
+        const int nc = (int)h->col_types.size();
+        for (int c = 0; c < nc; c++) {
+            h->plan.cols[c].data = b->cols[q][c].data;
+            h->plan.cols[c].valid = b->cols[q][c].validity;
+            h->plan.cols[c].offsets = b->cols[q][c].offsets;
+        }
+        BQuery &d = qs[q];
+        memset(&d, 0, sizeof d);
+        d.n_rows = n;
+        d.is_str = h->str_col >= 0;
+        if (d.is_str) {
+            // dictionary and arena sized for the whole query: no growth in the graph
+            const gb_col &sc = b->cols[q][h->str_col];
+            int64_t ends[2];
+            GB_CUDA(cudaMemcpy(&ends[0], sc.offsets, 8, cudaMemcpyDeviceToHost));
+            GB_CUDA(cudaMemcpy(&ends[1], sc.offsets + n, 8, cudaMemcpyDeviceToHost));
+            u64 cap = 1024;
+            while (cap < 2 * std::max<u64>(h->est_groups, 512)) cap <<= 1;
+            cap = std::max(cap, h->sd_cap);  // a re-run on the handle may have grown it
+            if ((s = strdict_init(h, cap, st))) return s;
+            const u64 need = (u64)(ends[1] - ends[0]) + 64;
+            if (h->sd_arena_cap < need) {
+                if ((s = h->sd_arena.ensure(need))) return s;
+                h->sd_arena_cap = need;
+            }
+            if ((s = h->sd_ids.ensure(n * 8 + 8))) return s;
+            h->plan.cols[nc].data = h->sd_ids.p;
+            h->plan.cols[nc].valid = nullptr;
+            d.D = strdict_ref(h);
+            d.sbytes = (const uint8_t *)sc.data;
+            d.soffs = sc.offsets;
+            d.svalid = sc.validity;
+            d.ids = (long long *)h->sd_ids.p;
+            for (u64 c = 0; c * 8192 < n; c++) it_str.push_back({q, (u32)c});
+        }
+        // HBM table, spill buffer, outputs of the handle
+        const int words = h->plan.words;
+        const u64 need_spill = (1u << 16) + 4096;
+        if (h->spill_cap < need_spill) {
+            if ((s = h->spill.ensure((size_t)need_spill * (1 + words) * 8))) return s;
+            h->spill_cap = (u32)need_spill;
+        }
+        if ((s = alloc_outputs(h, h->cap + 2))) return s;
+        d.P = h->plan;
+        d.T = table_ref(h);
+        d.T.ctl = (Ctl *)b->qctl.p + q;
+        d.T.spill_threshold = h->spill_cap / 2;
+        fill_emit(h, d.E, h->out_cols, h->out_valid, h->out_cap);
+        d.table_words = (h->cap + 2) * (u64)h->plan.stride;
+        d.smem_slots = h->mode == 0 ? std::min(h->smem_slots, b->smem_slots_max) : 0;
+        if (h->est_groups > 65536) d.smem_slots = 0;  // a shared table only pays for small group counts
+        const u64 init_words = d.table_words + (u64)(d.E.n_keys + d.E.n_aggs) * ((d.E.out_cap + 63) / 64);
+        for (u64 c = 0; c * 65536 < init_words; c++) it_init.push_back({q, (u32)c});
+        for (u64 c = 0; c * BATCH_TILE < n; c++) it_ing.push_back({q, (u32)c});
+        for (u64 c = 0; c * (COMPACT_PER * 256) < h->cap + 2; c++) it_cmp.push_back({q, (u32)c});
+    }
+    // interleave the tiles of different queries (uneven sizes balance across CTAs)
+    std::vector<BItem> mixed;
+    mixed.reserve(it_ing.size());
+    {
+        std::vector<std::vector<BItem>> per(nq);
+        for (auto &x : it_ing) per[x.q].push_back(x);
+        size_t k = 0;
+        bool any = true;
+        while (any) {
+            any = false;
+            for (u32 q = 0; q < nq; q++)
+                if (k < per[q].size()) {
+                    mixed.push_back(per[q][k]);
+                    any = true;
+                }
+            k++;
+        }
+    }
+    it_ing.swap(mixed);
+    if ((s = b->qdesc.ensure(qs.size() * sizeof(BQuery) + 64)) ||
+        (s = b->items_init.ensure(it_init.size() * sizeof(BItem) + 64)) ||
+        (s = b->items_str.ensure(it_str.size() * sizeof(BItem) + 64)) ||
+        (s = b->items_ingest.ensure(it_ing.size() * sizeof(BItem) + 64)) ||
+        (s = b->items_compact.ensure(it_cmp.size() * sizeof(BItem) + 64)))
+        return s;
+    GB_CUDA(cudaMemcpy(b->qdesc.p, qs.data(), qs.size() * sizeof(BQuery), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(b->items_init.p, it_init.data(), it_init.size() * sizeof(BItem), cudaMemcpyHostToDevice));
+    if (!it_str.empty())
+        GB_CUDA(cudaMemcpy(b->items_str.p, it_str.data(), it_str.size() * sizeof(BItem), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(b->items_ingest.p, it_ing.data(), it_ing.size() * sizeof(BItem), cudaMemcpyHostToDevice));
+    GB_CUDA(cudaMemcpy(b->items_compact.p, it_cmp.data(), it_cmp.size() * sizeof(BItem), cudaMemcpyHostToDevice));
+    b->n_init = (u32)it_init.size();
+    b->n_str = (u32)it_str.size();
+    b->n_ingest = (u32)it_ing.size();
+    b->n_compact = (u32)it_cmp.size();
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_batch_ingest<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+        cudaFuncSetAttribute(k_batch_ingest<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+        attr = true;
+    }
+    b->prepared = true;
+    return GB_OK;
+}
+
+// Dynamic shared memory of one k_batch_ingest CTA so that `ctas` CTAs fit on
+// an SM (about 227 KB usable per SM, less each CTA's static shared memory).
+static int batch_smem_bytes(int ctas) {
+    int b = (227 * 1024) / std::max(1, ctas) - 4096;
+    b = std::min(b, 96 * 1024);
+    return b & ~4095;
+}
+
+// The graph body: every launch of one batch execution.
+static gb_status batch_enqueue(gb_batch *b, cudaStream_t st) {
+    const u32 nq = (u32)b->handles.size();
+    const int sms = sm_count();
+    GB_CUDA(cudaMemsetAsync(b->qctl.p, 0, (size_t)nq * sizeof(Ctl), st));
+    GB_CUDA(cudaMemsetAsync(b->bctl.p, 0, sizeof(Ctl), st));
+    for (u32 q = 0; q < nq; q++) {
+        gb_agg *h = b->handles[q];
+        if (h->str_col < 0) continue;
+        const u64 cap = h->sd_cap;
+        gb_status s;
+        if ((s = strdict_fill((u64 *)h->sd_hash.p, cap, EMPTY_KEY, st)) ||
+            (s = strdict_fill((u64 *)h->sd_ref.p, cap, ~0ull, st)))
+            return s;
+        GB_CUDA(cudaMemsetAsync(h->sd_ctr.p, 0, 64, st));
+    }
+    k_batch_init<<<std::max(1, std::min((int)b->n_init, sms * 8)), 256, 0, st>>>((const BQuery *)b->qdesc.p,
+                                                                               (const BItem *)b->items_init.p, b->n_init);
+    GB_CUDA(cudaGetLastError());
+    if (b->n_str) {
+        k_batch_strdict<<<std::min((int)b->n_str, sms * 8), 256, 0, st>>>((const BQuery *)b->qdesc.p,
+                                                                       (const BItem *)b->items_str.p, b->n_str);
+        GB_CUDA(cudaGetLastError());
+    }
+    const int smem_bytes = batch_smem_bytes(b->ctas_per_sm);
+    const int grid = std::max(1, std::min((int)b->n_ingest, sms * b->ctas_per_sm));
+    if (b->precombine)
+        k_batch_ingest<true><<<grid, 512, smem_bytes, st>>>((const BQuery *)b->qdesc.p, (const BItem *)b->items_ingest.p,
+                                                           b->n_ingest, (Ctl *)b->bctl.p, smem_bytes);
+    else
+        k_batch_ingest<false><<<grid, 512, smem_bytes, st>>>((const BQuery *)b->qdesc.p,
+                                                            (const BItem *)b->items_ingest.p, b->n_ingest,
+                                                            (Ctl *)b->bctl.p, smem_bytes);
+    GB_CUDA(cudaGetLastError());
+    k_batch_compact<<<std::max(1, std::min((int)b->n_compact, sms * 8)), 256, 0, st>>>(
+        (const BQuery *)b->qdesc.p, (const BItem *)b->items_compact.p, b->n_compact);
+    GB_CUDA(cudaGetLastError());
+    GB_CUDA(cudaMemcpyAsync(b->qctl_host.p, b->qctl.p, (size_t)nq * sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    return GB_OK;
+}
+
+extern "C" {
+
+gb_status gb_batch_create(gb_batch **out) {
+    if (!out) return GB_ERR_INVALID;
+    *out = new gb_batch();
+    return GB_OK;
+}
+
+gb_status gb_batch_add(gb_batch *b, const gb_agg_spec *spec, const gb_col *cols, uint64_t nrows, uint32_t *qidx) {
+    if (!b || !spec || (!cols && nrows)) return GB_ERR_INVALID;
+    gb_agg *h = nullptr;
+    gb_status s = gb_agg_create(spec, &h);
+    if (s) return s;
+    if (h->mode == 1) {  // the batch runs the hash pipeline for every query
+        h->mode = 0;
+        u64 est = h->est_groups ? h->est_groups : (1u << 15);
+        h->cap = std::max<u64>(1024, next_pow2(est * 2));
+        if ((s = init_table(h, h->table, h->cap, 0))) {
+            gb_agg_destroy(h);
+            return s;
+        }
+    }
+    b->handles.push_back(h);
+    b->cols.emplace_back(cols, cols + spec->n_cols);
+    b->rows.push_back(nrows);
+    b->prepared = false;
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    if (qidx) *qidx = (uint32_t)(b->handles.size() - 1);
+    return GB_OK;
+}
+
+gb_status gb_batch_set_option(gb_batch *b, const char *name, int64_t value) {
+    if (!b || !name) return GB_ERR_INVALID;
+    std::string n(name);
+    if (n == "graph") b->use_graph = value != 0;
+    else if (n == "ctas_per_sm" && value >= 1 && value <= 4) b->ctas_per_sm = (int)value;
+    else if (n == "smem_slots" && value >= 0 && value <= 4096 && !(value & (value - 1))) b->smem_slots_max = (int)value;
+    else if (n == "precombine") b->precombine = value != 0;
+    else {
+        set_error("unknown or invalid batch option '%s'", name);
+        return GB_ERR_INVALID;
+    }
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    return GB_OK;
+}
+
+gb_status gb_batch_run(gb_batch *b, void *stream) {
+    if (!b) return GB_ERR_INVALID;
+    cudaStream_t st = (cudaStream_t)stream;
+    gb_status s;
+    if (!b->prepared && (s = batch_prepare(b, st))) return s;
+    const u32 nq = (u32)b->handles.size();
+    if (b->use_graph) {
+        if (!b->exec) {
+            cudaStream_t cs;
+            GB_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+            GB_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+            gb_status es = batch_enqueue(b, cs);
+            cudaGraph_t g = nullptr;
+            cudaError_t e = cudaStreamEndCapture(cs, &g);
+            cudaStreamDestroy(cs);
+            if (es) return es;
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+            if (b->graph) cudaGraphDestroy(b->graph);
+            b->graph = g;
+            GB_CUDA(cudaGraphInstantiate(&b->exec, g, 0));
+        }
+        GB_CUDA(cudaGraphLaunch(b->exec, st));
+        b->launches += 4 + (b->n_str ? 1 : 0);
+    } else {
+        if ((s = batch_enqueue(b, st))) return s;
+        b->launches += 4 + (b->n_str ? 1 : 0);
+    }
+    GB_CUDA(cudaStreamSynchronize(st));
+    const Ctl *qc = (const Ctl *)b->qctl_host.p;
+    b->slow.clear();
+    for (u32 q = 0; q < nq; q++) {
+        gb_agg *h = b->handles[q];
+        const Ctl &c = qc[q];
+        const bool bad = c.spill_count || c.err || c.aux1 || c.out_count > h->out_cap;
+        if (bad) {
+            // host decisions needed (spill / dictionary growth): the whole query
+            // re-runs on its own handle
+            b->slow.push_back((int)q);
+            if ((s = gb_agg_reset(h))) return s;
+            if ((s = gb_agg_ingest(h, b->cols[q].data(), b->rows[q], GB_MEM_DEVICE, stream))) return s;
+            if ((s = gb_agg_finalize(h, stream))) return s;
+            continue;
+        }
+        h->n_groups = c.n_groups;
+        h->n_rows_out = c.out_count;
+        h->topn_applied = false;
+        h->finalized = true;
+        h->has_result = false;
+        if (h->str_col >= 0 && (s = strdict_emit(h, (const long long *)h->out_cols[0].p, h->n_rows_out, st))) return s;
+    }
+    if (b->handles.size() && b->slow.size() < nq) GB_CUDA(cudaStreamSynchronize(st));
+    if (!b->slow.empty()) {
+        // a re-run may have grown tables / dictionaries: the next run prepares
+        // (and captures) again with the new sizes
+        b->prepared = false;
+        if (b->exec) {
+            cudaGraphExecDestroy(b->exec);
+            b->exec = nullptr;
+        }
+    }
+    return GB_OK;
+}
+
+uint32_t gb_batch_size(const gb_batch *b) { return b ? (uint32_t)b->handles.size() : 0; }
+
+gb_status gb_batch_result(gb_batch *b, uint32_t q, gb_result *out) {
+    if (!b || q >= b->handles.size()) return GB_ERR_INVALID;
+    return gb_agg_result(b->handles[q], out);
+}
+
+uint32_t gb_batch_slow_queries(const gb_batch *b) { return b ? (uint32_t)b->slow.size() : 0; }
+
+uint64_t gb_batch_kernel_launches(const gb_batch *b) { return b ? b->launches : 0; }
+
+void gb_batch_destroy(gb_batch *b) {
+    if (!b) return;
+    cudaDeviceSynchronize();
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (auto *h : b->handles) gb_agg_destroy(h);
+    for (DevBuf *d : {&b->qdesc, &b->items_init, &b->items_str, &b->items_ingest, &b->items_compact, &b->bctl, &b->qctl})
+        d->release();
+    b->qctl_host.release();
+    delete b;
+}
+
+}  // extern "C"

@@ -136,3 +136,59 @@ def varchar_table(n: int, n_groups: int, seed: int):
     s = rng.integers(0, 10**6, n, dtype=np.int64)
     m = rng.integers(-(2**31), 2**31 - 1, n, dtype=np.int32)
     return (offs, data), s, m
+
+
+def batch_shapes(n_tables: int = 256, seed: int = 3, rows_exp=(4.0, 7.0), groups_exp=(2.0, 6.0),
+                 varchar_frac: float = 0.25):
+    """Shapes of a batch of independent GROUP BY tables: rows = floor(10^U(rows_exp)),
+    groups = floor(10^U(groups_exp)) (log-uniform), a varchar_frac share of the
+    tables (at seeded positions) keyed by VARCHAR, the rest by (INT32, INT16).
+    Returns a list of dicts {kind, rows, groups, seed}."""
+    rng = np.random.default_rng(seed)
+    rows = np.floor(10 ** rng.uniform(rows_exp[0], rows_exp[1], n_tables)).astype(np.int64)
+    groups = np.floor(10 ** rng.uniform(groups_exp[0], groups_exp[1], n_tables)).astype(np.int64)
+    n_str = int(round(varchar_frac * n_tables))
+    is_str = np.zeros(n_tables, dtype=bool)
+    is_str[rng.permutation(n_tables)[:n_str]] = True
+    return [dict(kind="varchar" if is_str[i] else "composite", rows=int(rows[i]), groups=int(max(1, groups[i])),
+                 seed=seed * 100_003 + i) for i in range(n_tables)]
+
+
+def batch_table_host(shape):
+    """numpy columns of one batch table (composite: a, b, s, m; varchar:
+    (offsets, bytes), s, m)."""
+    if shape["kind"] == "composite":
+        return list(composite(shape["rows"], shape["groups"], shape["seed"]))
+    (offs, data), s, m = varchar_table(shape["rows"], shape["groups"], shape["seed"])
+    return [(offs, data), s, m]
+
+
+def batch_table_device(shape, device="cuda"):
+    """The same table shape generated on the GPU (torch's generator: other
+    values than batch_table_host, same distributions) — for full-size runs."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(shape["seed"])
+    n, ng = shape["rows"], shape["groups"]
+    s = torch.randint(0, 10**6, (n,), generator=g, device=device, dtype=torch.int64)
+    m = torch.randint(-(2**31), 2**31 - 1, (n,), generator=g, device=device, dtype=torch.int64).to(torch.int32)
+    if shape["kind"] == "composite":
+        a = torch.randint(0, max(1, ng // 64), (n,), generator=g, device=device, dtype=torch.int32)
+        b = torch.randint(0, 64, (n,), generator=g, device=device, dtype=torch.int16)
+        return [a, b, s, m]
+    rng = np.random.default_rng(shape["seed"])
+    poffs, pdata = varchar_pool(ng, rng)
+    poffs_d = torch.from_numpy(poffs).to(device)
+    pdata_d = torch.from_numpy(pdata).to(device)
+    pick = torch.randint(0, ng, (n,), generator=g, device=device, dtype=torch.int64)
+    lens = poffs_d[pick + 1] - poffs_d[pick]
+    offs = torch.zeros(n + 1, dtype=torch.int64, device=device)
+    torch.cumsum(lens, 0, out=offs[1:])
+    total = int(offs[-1].item())
+    starts = torch.repeat_interleave(poffs_d[pick] - offs[:-1], lens, output_size=total)
+    data = pdata_d[starts + torch.arange(total, device=device, dtype=torch.int64)]
+    return [(offs, data), s, m]
+
+
+BATCH_COMPOSITE = dict(col_types=[2, 1, 3, 2], group_cols=[0, 1], aggs=[("count_star", -1), ("sum", 2), ("max", 3)])
+BATCH_VARCHAR = dict(col_types=[5, 3, 2], group_cols=[0], aggs=[("count_star", -1), ("sum", 1), ("max", 2)])

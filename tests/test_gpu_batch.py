@@ -1,0 +1,176 @@
+"""GPU parity of the batched path: many independent GROUP BY queries
+(composite (INT32, INT16) keys and VARCHAR keys; COUNT(*), SUM(INT64),
+MAX(INT32)) executed together through gb_batch, each result checked against
+the oracle and against the same query run alone.  Bit-exact."""
+import numpy as np
+import pytest
+
+import oracle
+from slothdb_gb300 import capi, datagen
+from util import as_expected, compare, gpu_to_dict
+
+pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("oracle_lib", "gblib")]
+
+COMP = datagen.BATCH_COMPOSITE
+STR = datagen.BATCH_VARCHAR
+
+
+def _q(shape):
+    return COMP if shape["kind"] == "composite" else STR
+
+
+def _out_types(q):
+    return [q["col_types"][c] for c in q["group_cols"]] + [
+        oracle.agg_out_type(oracle.AGG_NAMES[k], q["col_types"][c] if c >= 0 else 0) for k, c in q["aggs"]]
+
+
+def _to_device(cols, col_types):
+    import torch
+    out = []
+    for c, t in zip(cols, col_types):
+        if t == capi.VARCHAR:
+            offs, data = c
+            data = data if len(data) else np.zeros(1, np.uint8)
+            out.append((torch.from_numpy(np.ascontiguousarray(offs)).cuda(),
+                        torch.from_numpy(np.ascontiguousarray(data)).cuda()))
+        else:
+            out.append(torch.from_numpy(np.ascontiguousarray(c)).cuda())
+    torch.cuda.synchronize()
+    return out
+
+
+def _orc(shape, cols, nulls=None):
+    q = _q(shape)
+    return oracle.run_query(q["col_types"], q["group_cols"], q["aggs"], cols, nulls=nulls)
+
+
+def _gpu(res, shape):
+    q = _q(shape)
+    return gpu_to_dict(res, len(q["group_cols"]), _out_types(q))
+
+
+def _build(shapes, est=None, options=None):
+    b = capi.Batch(options)
+    host, dev = [], []
+    for i, sh in enumerate(shapes):
+        q = _q(sh)
+        cols = datagen.batch_table_host(sh)
+        d = _to_device(cols, q["col_types"])
+        host.append(cols)
+        dev.append(d)
+        e = sh["groups"] if est is None else est[i]
+        assert b.add(q["col_types"], q["group_cols"], q["aggs"], d, sh["rows"], est_groups=e) == i
+    return b, host, dev
+
+
+def test_batch_mixed_queries_match_oracle_and_replay():
+    shapes = datagen.batch_shapes(n_tables=24, seed=7, rows_exp=(3.0, 5.3), groups_exp=(1.0, 4.5))
+    b, host, dev = _build(shapes)
+    try:
+        assert len(b) == 24
+        b.run()
+        first = []
+        for i, sh in enumerate(shapes):
+            r = b.result(i)
+            first.append(r)
+            compare(_gpu(r, sh), _orc(sh, host[i]))
+        assert b.launches() > 0
+        # replay of the captured graph: same results
+        b.run()
+        assert b.slow_queries() == 0
+        for i, sh in enumerate(shapes):
+            compare(_gpu(b.result(i), sh), as_expected(_gpu(first[i], sh)), rel_tol=0.0)
+    finally:
+        b.close()
+
+
+@pytest.mark.parametrize("options", [{"graph": 0}, {"smem_slots": 0, "precombine": 0}, {"ctas_per_sm": 1,
+                                                                                        "smem_slots": 512}])
+def test_batch_options(options):
+    shapes = datagen.batch_shapes(n_tables=10, seed=8, rows_exp=(3.0, 5.0), groups_exp=(1.0, 4.0))
+    b, host, _ = _build(shapes, options=options)
+    try:
+        for _ in range(2):
+            b.run()
+            for i, sh in enumerate(shapes):
+                compare(_gpu(b.result(i), sh), _orc(sh, host[i]))
+    finally:
+        b.close()
+
+
+def test_batch_result_same_as_alone():
+    """Each query's batched result equals the same query run on its own."""
+    shapes = datagen.batch_shapes(n_tables=8, seed=9, rows_exp=(4.0, 5.5), groups_exp=(2.0, 4.5))
+    b, host, dev = _build(shapes)
+    try:
+        b.run()
+        for i, sh in enumerate(shapes):
+            q = _q(sh)
+            g = capi.GroupBy(q["col_types"], q["group_cols"], q["aggs"], est_groups=sh["groups"])
+            try:
+                g.ingest(dev[i], nrows=sh["rows"], device=True)
+                g.finalize()
+                alone = g.result()
+            finally:
+                g.close()
+            compare(_gpu(b.result(i), sh), as_expected(_gpu(alone, sh)), rel_tol=0.0)
+    finally:
+        b.close()
+
+
+def test_batch_underestimated_groups_take_the_slow_path():
+    """est_groups far below the real count: the batched table overflows, the
+    query re-runs on its own handle, and the next run fits in the batch."""
+    shapes = [dict(kind="composite", rows=200_000, groups=60_000, seed=11),
+              dict(kind="varchar", rows=150_000, groups=40_000, seed=12),
+              dict(kind="composite", rows=5_000, groups=100, seed=13)]
+    b, host, _ = _build(shapes, est=[16, 16, 100])
+    try:
+        b.run()
+        assert b.slow_queries() >= 2
+        for i, sh in enumerate(shapes):
+            compare(_gpu(b.result(i), sh), _orc(sh, host[i]))
+        b.run()
+        assert b.slow_queries() == 0
+        for i, sh in enumerate(shapes):
+            compare(_gpu(b.result(i), sh), _orc(sh, host[i]))
+    finally:
+        b.close()
+
+
+def test_batch_empty_tiny_and_nullable():
+    import torch
+    rng = np.random.default_rng(21)
+    b = capi.Batch()
+    try:
+        # empty table
+        e = [torch.zeros(1, dtype=torch.int32, device="cuda"), torch.zeros(1, dtype=torch.int16, device="cuda"),
+             torch.zeros(1, dtype=torch.int64, device="cuda"), torch.zeros(1, dtype=torch.int32, device="cuda")]
+        b.add(COMP["col_types"], COMP["group_cols"], COMP["aggs"], e, 0, est_groups=10)
+        # one row
+        one = datagen.batch_table_host(dict(kind="varchar", rows=1, groups=1, seed=5))
+        b.add(STR["col_types"], STR["group_cols"], STR["aggs"], _to_device(one, STR["col_types"]), 1, est_groups=1)
+        # nullable key and value columns
+        n = 70_001
+        a = rng.integers(0, 300, n, dtype=np.int32)
+        kb = rng.integers(0, 64, n, dtype=np.int16)
+        s = rng.integers(0, 10**6, n, dtype=np.int64)
+        m = rng.integers(-(2**31), 2**31 - 1, n, dtype=np.int32)
+        an = rng.random(n) < 0.05
+        mn = rng.random(n) < 0.3
+        va = capi.validity_words(~an)
+        vm = capi.validity_words(~mn)
+        d = _to_device([a, kb, s, m], COMP["col_types"])
+        vd = [torch.from_numpy(va.view(np.int64)).cuda(), None, None, torch.from_numpy(vm.view(np.int64)).cuda()]
+        b.add(COMP["col_types"], COMP["group_cols"], COMP["aggs"], d, n, validity=vd, nullable=[0, 3],
+              est_groups=20_000)
+        torch.cuda.synchronize()
+        b.run()
+        r0 = b.result(0)
+        assert len(r0[0][0]) == 0
+        compare(_gpu(b.result(1), dict(kind="varchar")), _orc(dict(kind="varchar"), one))
+        orc = oracle.run_query(COMP["col_types"], COMP["group_cols"], COMP["aggs"], [a, kb, s, m],
+                               nulls=[an, None, None, mn])
+        compare(_gpu(b.result(2), dict(kind="composite")), orc)
+    finally:
+        b.close()
