@@ -243,6 +243,11 @@ def run_batch(args):
                 mismatches += 1
                 break
     slow = b.slow_queries()
+    b.set_option("profiling", 1)
+    b.run(stream=sp)
+    prof = {k: v[1] / max(1, v[0]) for k, v in b.profile().items()}
+    b.set_option("profiling", 0)
+    b.run(stream=sp)
     clocks = Clocks(local)
     clocks.start()
     launches0 = b.launches()
@@ -266,6 +271,7 @@ def run_batch(args):
             "plain": {"value": nq / (ms_plain / 1e3), "unit": "queries/s", "ms_per_step": ms_plain,
                       "steps": plain_steps},
             "speedup_vs_plain": ms_plain / ms_batch, "parity_mismatches": mismatches, "slow_queries": slow,
+            "kernels_ms": prof,
             "clocks": clk, "gpu_launches": launches}
     print(json.dumps(line), flush=True)
     b.close()

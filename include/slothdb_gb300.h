@@ -249,7 +249,10 @@ gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg_begin, uin
  * Column pointers (gb_col) must be device memory and stay valid, with the
  * same row counts, for every run of the batch.  Options ("graph" 0/1,
  * "ctas_per_sm" 1..4, "smem_slots" 0 or a power of two <= 4096,
- * "precombine" 0/1) take effect at the next run. */
+ * "precombine" 0/1, "profiling" 0/1, "order" 0 query-major tiles / 1
+ * interleaved) take effect at the next run; with
+ * profiling on, runs skip the graph and gb_batch_profile reports CUDA-event
+ * times of the four kernels. */
 typedef struct gb_batch gb_batch;
 gb_status gb_batch_create(gb_batch **out);
 gb_status gb_batch_add(gb_batch *b, const gb_agg_spec *spec, const gb_col *cols, uint64_t nrows, uint32_t *query_index);
@@ -259,6 +262,7 @@ uint32_t gb_batch_size(const gb_batch *b);
 gb_status gb_batch_result(gb_batch *b, uint32_t query_index, gb_result *out);
 uint32_t gb_batch_slow_queries(const gb_batch *b);
 uint64_t gb_batch_kernel_launches(const gb_batch *b);
+uint32_t gb_batch_profile(const gb_batch *b, gb_kernel_stat *out, uint32_t max);
 void gb_batch_destroy(gb_batch *b);
 
 /* Allocation-free GROUP BY for callers that cannot allocate device memory

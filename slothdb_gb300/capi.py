@@ -91,6 +91,7 @@ _SIGS = {
     "gb_batch_result": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Result)]),
     "gb_batch_slow_queries": (C.c_uint32, [C.c_void_p]),
     "gb_batch_kernel_launches": (C.c_uint64, [C.c_void_p]),
+    "gb_batch_profile": (C.c_uint32, [C.c_void_p, C.POINTER(KernelStat), C.c_uint32]),
     "gb_batch_destroy": (None, [C.c_void_p]),
     "gb_hash_aggregate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64), C.c_void_p]),
@@ -368,6 +369,12 @@ class Batch:
 
     def launches(self):
         return int(self.lib.gb_batch_kernel_launches(self.h))
+
+    def profile(self):
+        """{kernel name: (launches, total ms)} of the profiled runs."""
+        arr = (KernelStat * 8)()
+        n = self.lib.gb_batch_profile(self.h, arr, 8)
+        return {arr[i].name.decode(): (int(arr[i].launches), float(arr[i].ms)) for i in range(min(n, 8))}
 
     def close(self):
         if getattr(self, "h", None):

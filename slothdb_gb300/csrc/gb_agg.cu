@@ -1048,6 +1048,8 @@ static gb_status strdict_encode(gb_agg *h, const uint8_t *bytes, const int64_t *
     u64 used = 0;
     GB_CUDA(cudaMemcpyAsync(&used, (u64 *)h->sd_ctr.p + 1, 8, cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
+    // arena entries are padded to 8 bytes: at most 7 more per non-empty string
+    batch_bytes += 7 * std::min<u64>(n, batch_bytes);
     if (used + batch_bytes + 64 > h->sd_arena_cap) {
         const u64 ncap = std::max<u64>((used + batch_bytes) * 3 / 2 + 4096, h->sd_arena_cap * 2);
         DevBuf nb;

@@ -9,7 +9,8 @@
 //   k_batch_init     one launch: every query's table to its identity state;
 //   k_batch_strdict  one launch: VARCHAR keys of every VARCHAR query → ids;
 //   k_batch_ingest   one persistent launch over a device work queue of
-//                    (query, tile) items, tiles of uneven queries interleaved;
+//                    (query, tile) items (query-major, so one table at a
+//                    time is hot in L2; uneven sizes balance dynamically);
 //                    each item copies its query's plan into shared memory and
 //                    runs the same warp pipeline as the single-query kernel;
 //   k_batch_compact  one launch: every query's table → its dense result.
@@ -32,6 +33,7 @@ struct BQuery {
     u32 *sretry;
     u64 n_rows;
     u64 table_words;
+    u64 init_words;  // table words, output validity words, dictionary words
     int32_t smem_slots;
     int32_t is_str;
 };
@@ -49,27 +51,36 @@ __device__ __forceinline__ void copy_words(void *dst, const void *src, int bytes
 
 // Item (q, idx) covers words [idx * 65536, (idx+1) * 65536) of the query's
 // init range: the table words, then the validity words of every output column
-// (all ones; the emit clears the bits of NULL results).
+// (all ones; the emit clears the bits of NULL results), then for a VARCHAR
+// key the dictionary's hash slots (free), ref slots (unpublished) and its
+// eight counter words (zero).
 __global__ void k_batch_init(const BQuery *qs, const BItem *items, u32 n_items) {
     for (u32 it = blockIdx.x; it < n_items; it += gridDim.x) {
         const BItem w = items[it];
         const BQuery &q = qs[w.q];
         const int stride = q.P.stride;
         const u64 vwords = (q.E.out_cap + 63) / 64;
-        const u64 total = q.table_words + (u64)(q.E.n_keys + q.E.n_aggs) * vwords;
-        const u64 lo = (u64)w.idx * 65536, hi = min(total, lo + 65536);
+        const u64 n0 = q.table_words, n1 = n0 + (u64)(q.E.n_keys + q.E.n_aggs) * vwords;
+        const u64 dc = q.is_str ? q.D.cap : 0;
+        const u64 lo = (u64)w.idx * 65536, hi = min(q.init_words, lo + 65536);
         for (u64 i = lo + threadIdx.x; i < hi; i += blockDim.x) {
-            if (i >= q.table_words) {
-                const u64 j = i - q.table_words;
+            if (i < n0) {
+                const int wd = (int)(i % (u64)stride);
+                u64 v;
+                if (wd == 0) v = EMPTY_KEY;
+                else if (wd - 1 < q.P.words) v = q.P.word_init[wd - 1];
+                else v = 0;
+                q.T.slots[i] = v;
+            } else if (i < n1) {
+                const u64 j = i - n0;
                 q.E.valid[j / vwords][j % vwords] = ~0ull;
-                continue;
+            } else if (i < n1 + dc) {
+                q.D.hash[i - n1] = EMPTY_KEY;
+            } else if (i < n1 + 2 * dc) {
+                q.D.ref[i - n1 - dc] = REF_PENDING;
+            } else {
+                q.D.next_id[i - n1 - 2 * dc] = 0;  // next id, arena used, error word, spare
             }
-            const int wd = (int)(i % (u64)stride);
-            u64 v;
-            if (wd == 0) v = EMPTY_KEY;
-            else if (wd - 1 < q.P.words) v = q.P.word_init[wd - 1];
-            else v = 0;
-            q.T.slots[i] = v;
         }
     }
 }
@@ -77,6 +88,7 @@ __global__ void k_batch_init(const BQuery *qs, const BItem *items, u32 n_items) 
 __global__ void k_batch_strdict(const BQuery *qs, const BItem *items, u32 n_items) {
     __shared__ StrDictRef D;
     __shared__ u32 s_new;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     for (u32 it = blockIdx.x; it < n_items; it += gridDim.x) {
         const BItem w = items[it];
         const BQuery &q = qs[w.q];
@@ -86,15 +98,17 @@ __global__ void k_batch_strdict(const BQuery *qs, const BItem *items, u32 n_item
         }
         __syncthreads();
         const u64 lo = (u64)w.idx * 8192, hi = min(q.n_rows, lo + 8192);
-        for (u64 r = lo + threadIdx.x; r < hi; r += blockDim.x) {
-            if (q.svalid && !((q.svalid[r >> 6] >> (r & 63)) & 1ull)) {
+        for (u64 base = lo + (u64)warp * 32; base < hi; base += (u64)nwarps * 32) {
+            const u64 r = base + lane;
+            bool act = r < hi;
+            if (act && q.svalid && !((q.svalid[r >> 6] >> (r & 63)) & 1ull)) {
                 q.ids[r] = -1;
-                continue;
+                act = false;
             }
-            const int64_t a = q.soffs[r], b = q.soffs[r + 1];
-            const u32 len = (u32)(b - a);
-            const uint8_t *s = q.sbytes + a;
-            const long long id = strdict_find_or_insert(D, s, len, str_hash(s, len), &s_new);
+            const int64_t a = act ? q.soffs[r] : 0;
+            const u32 len = act ? (u32)(q.soffs[r + 1] - a) : 0u;
+            const long long id = strdict_warp_encode(D, q.sbytes + a, len, act, &s_new);
+            if (!act) continue;
             q.ids[r] = id;
             if (id < 0) atomicAdd(&q.T.ctl->aux1, 1u);  // needs the host: the query re-runs on its handle
         }
@@ -210,6 +224,15 @@ struct gb_batch {
     int ctas_per_sm = 2;
     int smem_slots_max = 2048;
     bool precombine = true;
+    bool profiling = false;
+    int order = 0;  // 0 query-major tiles, 1 interleaved
+    struct BatchProf {
+        const char *name;
+        cudaEvent_t a = nullptr, b = nullptr;
+        bool pending = false;
+        double ms = 0;
+        u64 n = 0;
+    } prof[4] = {{"k_batch_init"}, {"k_batch_strdict"}, {"k_batch_ingest"}, {"k_batch_compact"}};
     u64 launches = 0;
     std::vector<int> slow;  // queries re-run on their handle in the last run
 };
@@ -245,7 +268,9 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
             while (cap < 2 * std::max<u64>(h->est_groups, 512)) cap <<= 1;
             cap = std::max(cap, h->sd_cap);  // a re-run on the handle may have grown it
             if ((s = strdict_init(h, cap, st))) return s;
-            const u64 need = (u64)(ends[1] - ends[0]) + 64;
+            // arena entries are padded to 8 bytes: at most 7 more per non-empty string
+            const u64 sbytes = (u64)(ends[1] - ends[0]);
+            const u64 need = sbytes + 7 * std::min<u64>(n, sbytes) + 64;
             if (h->sd_arena_cap < need) {
                 if ((s = h->sd_arena.ensure(need))) return s;
                 h->sd_arena_cap = need;
@@ -276,15 +301,17 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
         d.table_words = (h->cap + 2) * (u64)h->plan.stride;
         d.smem_slots = h->mode == 0 ? std::min(h->smem_slots, b->smem_slots_max) : 0;
         if (h->est_groups > 65536) d.smem_slots = 0;  // a shared table only pays for small group counts
-        const u64 init_words = d.table_words + (u64)(d.E.n_keys + d.E.n_aggs) * ((d.E.out_cap + 63) / 64);
-        for (u64 c = 0; c * 65536 < init_words; c++) it_init.push_back({q, (u32)c});
+        d.init_words = d.table_words + (u64)(d.E.n_keys + d.E.n_aggs) * ((d.E.out_cap + 63) / 64) +
+                       (d.is_str ? 2 * d.D.cap + 8 : 0);
+        for (u64 c = 0; c * 65536 < d.init_words; c++) it_init.push_back({q, (u32)c});
         for (u64 c = 0; c * BATCH_TILE < n; c++) it_ing.push_back({q, (u32)c});
         for (u64 c = 0; c * (COMPACT_PER * 256) < h->cap + 2; c++) it_cmp.push_back({q, (u32)c});
     }
-    // interleave the tiles of different queries (uneven sizes balance across CTAs)
+    // Tile order: query-major by default (the CTAs sweep one query's table
+    // at a time, which keeps it in L2); "order" 1 interleaves the queries.
     std::vector<BItem> mixed;
     mixed.reserve(it_ing.size());
-    {
+    if (b->order == 1) {
         std::vector<std::vector<BItem>> per(nq);
         for (auto &x : it_ing) per[x.q].push_back(x);
         size_t k = 0;
@@ -299,7 +326,7 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
             k++;
         }
     }
-    it_ing.swap(mixed);
+    if (b->order == 1) it_ing.swap(mixed);
     if ((s = b->qdesc.ensure(qs.size() * sizeof(BQuery) + 64)) ||
         (s = b->items_init.ensure(it_init.size() * sizeof(BItem) + 64)) ||
         (s = b->items_str.ensure(it_str.size() * sizeof(BItem) + 64)) ||
@@ -334,32 +361,53 @@ static int batch_smem_bytes(int ctas) {
     return b & ~4095;
 }
 
+// Profiling (graph off): events around each of the four kernels.
+using BatchProf = gb_batch::BatchProf;
+
+static void batch_prof(gb_batch *b, int i, cudaStream_t st, bool begin) {
+    if (!b->profiling) return;
+    BatchProf &p = b->prof[i];
+    if (!p.a) {
+        cudaEventCreate(&p.a);
+        cudaEventCreate(&p.b);
+    }
+    cudaEventRecord(begin ? p.a : p.b, st);
+    if (!begin) p.pending = true;
+}
+
+static void batch_prof_collect(gb_batch *b) {
+    for (auto &p : b->prof) {
+        if (!p.pending) continue;
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
+            p.ms += ms;
+            p.n++;
+        }
+        p.pending = false;
+    }
+}
+
 // The graph body: every launch of one batch execution.
 static gb_status batch_enqueue(gb_batch *b, cudaStream_t st) {
     const u32 nq = (u32)b->handles.size();
     const int sms = sm_count();
     GB_CUDA(cudaMemsetAsync(b->qctl.p, 0, (size_t)nq * sizeof(Ctl), st));
     GB_CUDA(cudaMemsetAsync(b->bctl.p, 0, sizeof(Ctl), st));
-    for (u32 q = 0; q < nq; q++) {
-        gb_agg *h = b->handles[q];
-        if (h->str_col < 0) continue;
-        const u64 cap = h->sd_cap;
-        gb_status s;
-        if ((s = strdict_fill((u64 *)h->sd_hash.p, cap, EMPTY_KEY, st)) ||
-            (s = strdict_fill((u64 *)h->sd_ref.p, cap, ~0ull, st)))
-            return s;
-        GB_CUDA(cudaMemsetAsync(h->sd_ctr.p, 0, 64, st));
-    }
+    batch_prof(b, 0, st, true);
     k_batch_init<<<std::max(1, std::min((int)b->n_init, sms * 8)), 256, 0, st>>>((const BQuery *)b->qdesc.p,
                                                                                (const BItem *)b->items_init.p, b->n_init);
     GB_CUDA(cudaGetLastError());
+    batch_prof(b, 0, st, false);
     if (b->n_str) {
+        batch_prof(b, 1, st, true);
         k_batch_strdict<<<std::min((int)b->n_str, sms * 8), 256, 0, st>>>((const BQuery *)b->qdesc.p,
                                                                        (const BItem *)b->items_str.p, b->n_str);
         GB_CUDA(cudaGetLastError());
+        batch_prof(b, 1, st, false);
     }
     const int smem_bytes = batch_smem_bytes(b->ctas_per_sm);
     const int grid = std::max(1, std::min((int)b->n_ingest, sms * b->ctas_per_sm));
+    batch_prof(b, 2, st, true);
     if (b->precombine)
         k_batch_ingest<true><<<grid, 512, smem_bytes, st>>>((const BQuery *)b->qdesc.p, (const BItem *)b->items_ingest.p,
                                                            b->n_ingest, (Ctl *)b->bctl.p, smem_bytes);
@@ -368,9 +416,12 @@ static gb_status batch_enqueue(gb_batch *b, cudaStream_t st) {
                                                             (const BItem *)b->items_ingest.p, b->n_ingest,
                                                             (Ctl *)b->bctl.p, smem_bytes);
     GB_CUDA(cudaGetLastError());
+    batch_prof(b, 2, st, false);
+    batch_prof(b, 3, st, true);
     k_batch_compact<<<std::max(1, std::min((int)b->n_compact, sms * 8)), 256, 0, st>>>(
         (const BQuery *)b->qdesc.p, (const BItem *)b->items_compact.p, b->n_compact);
     GB_CUDA(cudaGetLastError());
+    batch_prof(b, 3, st, false);
     GB_CUDA(cudaMemcpyAsync(b->qctl_host.p, b->qctl.p, (size_t)nq * sizeof(Ctl), cudaMemcpyDeviceToHost, st));
     return GB_OK;
 }
@@ -385,8 +436,12 @@ gb_status gb_batch_create(gb_batch **out) {
 
 gb_status gb_batch_add(gb_batch *b, const gb_agg_spec *spec, const gb_col *cols, uint64_t nrows, uint32_t *qidx) {
     if (!b || !spec || (!cols && nrows)) return GB_ERR_INVALID;
+    // a table never has more groups than rows: size it for min(estimate, rows)
+    gb_agg_spec sp = *spec;
+    const u64 est = sp.est_groups ? sp.est_groups : (1u << 15);
+    sp.est_groups = std::max<u64>(1, std::min<u64>(est, nrows));
     gb_agg *h = nullptr;
-    gb_status s = gb_agg_create(spec, &h);
+    gb_status s = gb_agg_create(&sp, &h);
     if (s) return s;
     if (h->mode == 1) {  // the batch runs the hash pipeline for every query
         h->mode = 0;
@@ -416,6 +471,11 @@ gb_status gb_batch_set_option(gb_batch *b, const char *name, int64_t value) {
     else if (n == "ctas_per_sm" && value >= 1 && value <= 4) b->ctas_per_sm = (int)value;
     else if (n == "smem_slots" && value >= 0 && value <= 4096 && !(value & (value - 1))) b->smem_slots_max = (int)value;
     else if (n == "precombine") b->precombine = value != 0;
+    else if (n == "profiling") b->profiling = value != 0;
+    else if (n == "order" && (value == 0 || value == 1)) {
+        b->order = (int)value;
+        b->prepared = false;
+    }
     else {
         set_error("unknown or invalid batch option '%s'", name);
         return GB_ERR_INVALID;
@@ -433,7 +493,7 @@ gb_status gb_batch_run(gb_batch *b, void *stream) {
     gb_status s;
     if (!b->prepared && (s = batch_prepare(b, st))) return s;
     const u32 nq = (u32)b->handles.size();
-    if (b->use_graph) {
+    if (b->use_graph && !b->profiling) {
         if (!b->exec) {
             cudaStream_t cs;
             GB_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
@@ -449,12 +509,12 @@ gb_status gb_batch_run(gb_batch *b, void *stream) {
             GB_CUDA(cudaGraphInstantiate(&b->exec, g, 0));
         }
         GB_CUDA(cudaGraphLaunch(b->exec, st));
-        b->launches += 4 + (b->n_str ? 1 : 0);
     } else {
         if ((s = batch_enqueue(b, st))) return s;
-        b->launches += 4 + (b->n_str ? 1 : 0);
     }
+    b->launches += 3 + (b->n_str ? 1 : 0);
     GB_CUDA(cudaStreamSynchronize(st));
+    batch_prof_collect(b);
     const Ctl *qc = (const Ctl *)b->qctl_host.p;
     b->slow.clear();
     for (u32 q = 0; q < nq; q++) {
@@ -501,11 +561,31 @@ uint32_t gb_batch_slow_queries(const gb_batch *b) { return b ? (uint32_t)b->slow
 
 uint64_t gb_batch_kernel_launches(const gb_batch *b) { return b ? b->launches : 0; }
 
+uint32_t gb_batch_profile(const gb_batch *b, gb_kernel_stat *out, uint32_t max) {
+    if (!b) return 0;
+    uint32_t n = 0;
+    for (const auto &p : b->prof) {
+        if (!p.n) continue;
+        if (out && n < max) {
+            memset(&out[n], 0, sizeof out[n]);
+            strncpy(out[n].name, p.name, sizeof(out[n].name) - 1);
+            out[n].launches = p.n;
+            out[n].ms = p.ms;
+        }
+        n++;
+    }
+    return n;
+}
+
 void gb_batch_destroy(gb_batch *b) {
     if (!b) return;
     cudaDeviceSynchronize();
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
+    for (auto &p : b->prof) {
+        if (p.a) cudaEventDestroy(p.a);
+        if (p.b) cudaEventDestroy(p.b);
+    }
     for (auto *h : b->handles) gb_agg_destroy(h);
     for (DevBuf *d : {&b->qdesc, &b->items_init, &b->items_str, &b->items_ingest, &b->items_compact, &b->bctl, &b->qctl})
         d->release();

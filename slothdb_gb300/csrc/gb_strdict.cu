@@ -20,24 +20,33 @@
 namespace gb {
 
 // Encode rows [0, n) (or the rows listed in `rows`) of a VARCHAR column into
-// ids; rows that found no slot are appended to `retry` for the host to
-// re-run after growing the table / arena.
+// ids, one row per lane of warp-uniform groups of 32; rows that found no slot
+// are appended to `retry` for the host to re-run after growing the table /
+// arena.
 __global__ void k_strdict_encode(const StrDictRef D, const uint8_t *bytes, const int64_t *offsets, int64_t off_base,
                                  const uint64_t *valid, u64 n, const u32 *rows, long long *ids, u32 *retry,
                                  u32 *retry_n, u32 *new_strs_total) {
     __shared__ u32 s_new;
     if (threadIdx.x == 0) s_new = 0;
     __syncthreads();
-    for (u64 i = blockIdx.x * (u64)blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
-        const u64 r = rows ? rows[i] : i;
-        if (valid && !((valid[r >> 6] >> (r & 63)) & 1ull)) {
-            ids[r] = -1;  // NULL key: the aggregation treats it as the NULL group
-            continue;
+    const int lane = threadIdx.x & 31;
+    const u64 warp = (blockIdx.x * (u64)blockDim.x + threadIdx.x) >> 5;
+    const u64 nwarps = ((u64)gridDim.x * blockDim.x) >> 5;
+    for (u64 base = warp * 32; base < n; base += nwarps * 32) {
+        const u64 i = base + lane;
+        bool act = i < n;
+        u64 r = 0;
+        if (act) {
+            r = rows ? rows[i] : i;
+            if (valid && !((valid[r >> 6] >> (r & 63)) & 1ull)) {
+                ids[r] = -1;  // NULL key: the aggregation treats it as the NULL group
+                act = false;
+            }
         }
-        const int64_t a = offsets[r] - off_base, b = offsets[r + 1] - off_base;
-        const u32 len = (u32)(b - a);
-        const uint8_t *s = bytes + a;
-        const long long id = strdict_find_or_insert(D, s, len, str_hash(s, len), &s_new);
+        const int64_t a = act ? offsets[r] - off_base : 0;
+        const u32 len = act ? (u32)(offsets[r + 1] - off_base - a) : 0u;
+        const long long id = strdict_warp_encode(D, bytes + a, len, act, &s_new);
+        if (!act) continue;
         if (id >= 0) {
             ids[r] = id;
         } else {

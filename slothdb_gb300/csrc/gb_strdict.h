@@ -22,78 +22,214 @@ constexpr u64 REF_PENDING = ~0ull;
 constexpr u64 DEAD_OFF = (1ull << 40) - 1;
 constexpr int SPIN_LIMIT = 1 << 20;
 
+// Bytes [8j, 8j+8) of the string at p (little-endian, zero past len), read
+// with aligned 8-byte loads of only the words that hold bytes of the string
+// (an aligned word never crosses a page, so nothing outside the pages of the
+// string is touched).
+__device__ __forceinline__ u64 str_chunk(const uint8_t *p, u32 len, u32 j) {
+    const uintptr_t a = (uintptr_t)p + 8u * j;
+    const u32 nb = min(8u, len - 8u * j);
+    const u64 *w = (const u64 *)(a & ~(uintptr_t)7);
+    const u32 lo = (u32)(a & 7);
+    u64 v = __ldg(w) >> (8 * lo);
+    if (lo && lo + nb > 8) v |= __ldg(w + 1) << (64 - 8 * lo);
+    if (nb < 8) v &= (1ull << (8 * nb)) - 1ull;
+    return v;
+}
+
+// FNV-1a over the 8-byte chunks (one final step for the partial, possibly
+// empty, last chunk), then the 64-bit finaliser.
 __device__ __forceinline__ u64 str_hash(const uint8_t *p, u32 len) {
-    // FNV-1a over 8-byte words, then the 64-bit finaliser
     u64 h = 0xcbf29ce484222325ull ^ ((u64)len * 0x9e3779b97f4a7c15ull);
-    u32 i = 0;
-    for (; i + 8 <= len; i += 8) {
-        u64 w = 0;
-#pragma unroll
-        for (int b = 0; b < 8; b++) w |= (u64)p[i + b] << (8 * b);
-        h = (h ^ w) * 0x100000001b3ull;
-    }
-    u64 w = 0;
-    for (u32 b = 0; i + b < len; b++) w |= (u64)p[i + b] << (8 * b);
-    h = (h ^ w) * 0x100000001b3ull;
+    const u32 full = len >> 3;
+    for (u32 j = 0; j < full; j++) h = (h ^ str_chunk(p, len, j)) * 0x100000001b3ull;
+    const u64 tail = (len & 7) ? str_chunk(p, len, full) : 0ull;
+    h = (h ^ tail) * 0x100000001b3ull;
     return mix64(h);
 }
 
-__device__ __forceinline__ bool bytes_equal(const uint8_t *a, const uint8_t *b, u32 len) {
-    for (u32 i = 0; i < len; i++)
-        if (a[i] != b[i]) return false;
+__device__ __forceinline__ u64 dict_hash_value(u64 h) { return h == EMPTY_KEY ? h ^ 1ull : h; }
+
+// Arena entries start at 8-byte offsets and hold the string's chunks (zero
+// padded), so a comparison is one aligned load per chunk.
+__device__ __forceinline__ bool arena_equal(const StrDictRef &D, u64 r, const uint8_t *s, u32 len) {
+    const u32 rlen = (u32)(r & 0xffffffu);
+    const u64 roff = r >> 24;
+    if (rlen != len || roff + ((len + 7u) & ~7u) > D.arena_cap) return false;
+    const u64 *aw = (const u64 *)(D.arena + roff);
+    const u32 nc = (len + 7) >> 3;
+    for (u32 j = 0; j < nc; j++)
+        if (aw[j] != str_chunk(s, len, j)) return false;
     return true;
 }
 
-// Returns the slot index (= string id), or -1 if the probe bound was reached
-// (table too full) or the arena is exhausted, or -2 on a timeout.
-__device__ __forceinline__ long long strdict_find_or_insert(const StrDictRef &D, const uint8_t *s, u32 len, u64 h, u32 *new_strs) {
-    u64 slot = h & (D.cap - 1);
-    for (int p = 0; p < D.max_probe; p++) {
+// Write the string into its arena entry, then its id, then publish the ref.
+__device__ __forceinline__ void strdict_publish(const StrDictRef &D, u64 slot, const uint8_t *s, u32 len, u64 off,
+                                                u64 id) {
+    u64 *aw = (u64 *)(D.arena + off);
+    const u32 nc = (len + 7) >> 3;
+    for (u32 j = 0; j < nc; j++) aw[j] = str_chunk(s, len, j);
+    const u64 rv = (off << 24) | (u64)len;
+    D.id[slot] = id;
+    D.ref_by_id[id] = rv;
+    __threadfence();
+    atomicExch((unsigned long long *)(D.ref + slot), (unsigned long long)rv);
+}
+
+__device__ __forceinline__ void strdict_kill(const StrDictRef &D, u64 slot, u32 len) {
+    atomicExch((unsigned long long *)(D.ref + slot), (unsigned long long)((DEAD_OFF << 24) | (u64)len));
+}
+
+// Bounded wait for a claimed slot's ref; REF_PENDING after the limit.
+__device__ __forceinline__ u64 strdict_wait_ref(const StrDictRef &D, u64 slot) {
+    u64 r = *(volatile u64 *)(D.ref + slot);
+    int spin = 0;
+    while (r == REF_PENDING) {
+        if (++spin > SPIN_LIMIT) {
+            atomicOr(D.err, (u32)ERR_TIMEOUT);
+            return REF_PENDING;
+        }
+        __nanosleep(32);
+        r = *(volatile u64 *)(D.ref + slot);
+    }
+    __threadfence();
+    return r;
+}
+
+// One thread: find the string's id or insert it, probing from probe step p0.
+// Returns the id, -1 if the probe bound was reached (table too full) or the
+// arena is exhausted, or -2 on a timeout.  A thread holds a claimed slot only
+// between its CAS and its publish, and never waits in between.
+__device__ __forceinline__ long long strdict_find_or_insert(const StrDictRef &D, const uint8_t *s, u32 len, u64 h,
+                                                            u32 *new_strs, int p0 = 0) {
+    const u64 hv = dict_hash_value(h);
+    u64 slot = (h + (u64)p0) & (D.cap - 1);
+    for (int p = p0; p < D.max_probe; p++) {
         u64 *hk = D.hash + slot;
         u64 k = *(volatile u64 *)hk;
         if (k == EMPTY_KEY) {
-            const u64 old = atomicCAS(hk, EMPTY_KEY, h == EMPTY_KEY ? h ^ 1ull : h);
+            const u64 old = atomicCAS((unsigned long long *)hk, EMPTY_KEY, hv);
             if (old == EMPTY_KEY) {
-                // claimed: copy the bytes into the arena, assign the id, then
-                // publish ref (readers wait for it)
-                const u64 off = atomicAdd(D.arena_used, (u64)len);
-                if (off + len > D.arena_cap || len >= (1u << 24)) {
-                    // dead slot: an offset past the arena never matches
-                    atomicExch(D.ref + slot, (DEAD_OFF << 24) | (u64)len);
+                const u64 plen = (len + 7u) & ~7u;
+                const u64 off = atomicAdd((unsigned long long *)D.arena_used, (unsigned long long)plen);
+                if (off + plen > D.arena_cap || len >= (1u << 24)) {
+                    strdict_kill(D, slot, len);  // an offset past the arena never matches
                     return -1;
                 }
-                for (u32 i = 0; i < len; i++) D.arena[off + i] = s[i];
-                const u64 id = atomicAdd(D.next_id, 1ull);
-                const u64 rv = (off << 24) | (u64)len;
-                D.id[slot] = id;
-                D.ref_by_id[id] = rv;
-                __threadfence();
-                atomicExch(D.ref + slot, rv);
+                const u64 id = atomicAdd((unsigned long long *)D.next_id, 1ull);
+                strdict_publish(D, slot, s, len, off, id);
                 atomicAdd(new_strs, 1u);
                 return (long long)id;
             }
             k = old;
         }
-        if (k == (h == EMPTY_KEY ? h ^ 1ull : h)) {
-            u64 r = *(volatile u64 *)(D.ref + slot);
-            int spin = 0;
-            while (r == REF_PENDING) {
-                if (++spin > SPIN_LIMIT) {
-                    atomicOr(D.err, (u32)ERR_TIMEOUT);
-                    return -2;
-                }
-                __nanosleep(32);
-                r = *(volatile u64 *)(D.ref + slot);
-            }
-            __threadfence();
-            const u32 rlen = (u32)(r & 0xffffffu);
-            const u64 roff = r >> 24;
-            if (rlen == len && roff + rlen <= D.arena_cap && bytes_equal(D.arena + roff, s, len))
-                return (long long)*(volatile u64 *)(D.id + slot);
+        if (k == hv) {
+            const u64 r = strdict_wait_ref(D, slot);
+            if (r == REF_PENDING) return -2;
+            if (arena_equal(D, r, s, len)) return (long long)*(volatile u64 *)(D.id + slot);
         }
         slot = (slot + 1) & (D.cap - 1);
     }
     return -1;
+}
+
+// Warp-cooperative encode, one row per lane (all 32 lanes call it; `act`
+// marks lanes with a row).  Lanes with equal hashes elect a leader that
+// probes; the warp's new strings take their arena bytes and ids with one
+// atomic each per warp and are published before any lane of the warp waits
+// on a slot another warp has claimed but not yet published — so no two warps
+// can wait on each other.  Followers check they hold the leader's bytes (a
+// hash collision falls back to the one-thread path).
+// Returns as strdict_find_or_insert.
+__device__ __forceinline__ long long strdict_warp_encode(const StrDictRef &D, const uint8_t *s, u32 len, bool act,
+                                                         u32 *new_strs) {
+    const int lane = threadIdx.x & 31;
+    const u64 h = act ? str_hash(s, len) : 0ull;
+    const unsigned am = __ballot_sync(0xffffffffu, act);
+    const unsigned peers = __match_any_sync(0xffffffffu, h) & am;
+    const int lead = act ? __ffs(peers) - 1 : lane;
+    const bool leader = act && lead == lane;
+    // phase 1 (leaders): probe without waiting
+    long long id = -1;
+    long long claimed = -1, waitslot = -1;
+    int waitp = 0;
+    if (leader) {
+        const u64 hv = dict_hash_value(h);
+        u64 slot = h & (D.cap - 1);
+        for (int p = 0; p < D.max_probe; p++) {
+            u64 *hk = D.hash + slot;
+            u64 k = *(volatile u64 *)hk;
+            if (k == EMPTY_KEY) {
+                const u64 old = atomicCAS((unsigned long long *)hk, EMPTY_KEY, hv);
+                if (old == EMPTY_KEY) {
+                    claimed = (long long)slot;
+                    break;
+                }
+                k = old;
+            }
+            if (k == hv) {
+                const u64 r = *(volatile u64 *)(D.ref + slot);
+                if (r == REF_PENDING) {
+                    waitslot = (long long)slot;
+                    waitp = p;
+                    break;
+                }
+                __threadfence();
+                if (arena_equal(D, r, s, len)) {
+                    id = (long long)*(volatile u64 *)(D.id + slot);
+                    break;
+                }
+            }
+            slot = (slot + 1) & (D.cap - 1);
+        }
+    }
+    // phase 2 (warp): arena bytes, then ids, for every claimed slot; publish
+    const bool need = claimed >= 0;
+    const unsigned needm = __ballot_sync(0xffffffffu, need);
+    if (needm) {
+        const u32 plen = need ? ((len + 7u) & ~7u) : 0u;
+        u64 incl = plen;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const u64 y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const u64 total = __shfl_sync(0xffffffffu, incl, 31);
+        u64 base = 0;
+        if (lane == 0) base = atomicAdd((unsigned long long *)D.arena_used, (unsigned long long)total);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        const u64 off = base + incl - plen;
+        const bool ok = need && off + plen <= D.arena_cap && len < (1u << 24);
+        const unsigned okm = __ballot_sync(0xffffffffu, ok);
+        u64 idb = 0;
+        if (lane == 0 && okm) idb = atomicAdd((unsigned long long *)D.next_id, (unsigned long long)__popc(okm));
+        idb = __shfl_sync(0xffffffffu, idb, 0);
+        if (ok) {
+            id = (long long)(idb + __popc(okm & ((1u << lane) - 1u)));
+            strdict_publish(D, (u64)claimed, s, len, off, (u64)id);
+        } else if (need) {
+            strdict_kill(D, (u64)claimed, len);
+            id = -1;
+        }
+        if (lane == 0 && okm) atomicAdd(new_strs, (u32)__popc(okm));
+    }
+    // phase 3 (leaders): wait for slots claimed by other warps
+    if (waitslot >= 0) {
+        const u64 r = strdict_wait_ref(D, (u64)waitslot);
+        if (r == REF_PENDING) id = -2;
+        else if (arena_equal(D, r, s, len)) id = (long long)*(volatile u64 *)(D.id + waitslot);
+        else id = strdict_find_or_insert(D, s, len, h, new_strs, waitp + 1);
+    }
+    // followers take the leader's id when they hold the same bytes
+    const long long lid = __shfl_sync(0xffffffffu, id, lead);
+    const uint8_t *ls = (const uint8_t *)__shfl_sync(0xffffffffu, (unsigned long long)(uintptr_t)s, lead);
+    const u32 llen = __shfl_sync(0xffffffffu, len, lead);
+    if (act && !leader) {
+        bool same = llen == len;
+        for (u32 j = 0; same && j < ((len + 7) >> 3); j++) same = str_chunk(s, len, j) == str_chunk(ls, len, j);
+        id = same ? lid : strdict_find_or_insert(D, s, len, h, new_strs);
+    }
+    return id;
 }
 
 
