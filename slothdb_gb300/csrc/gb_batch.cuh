@@ -20,8 +20,27 @@
 // dictionary growth) is re-run on its own handle afterwards.
 
 #define BATCH_TILE 16384
+#define FAST_MAX_OPS 4
+
+// Integer-plan description kept in registers by the fast tile path (no
+// filters; keys SINGLE / PACKED / STRING; ops ADD_I, MIN_I, MAX_I, CNT_NN over
+// integer columns).  kdesc = key_mode | kt0 << 4 | kt1 << 8 | bits_b << 16 |
+// bits_a << 24; op[i] = kind | type << 4 | table word << 8 | shared word << 16
+// | wide << 24, wide = a MIN/MAX over BIGINT (64-bit shared word).
+struct FastPlan {
+    const void *kp[2];
+    const uint64_t *kv[2];
+    const void *vp[FAST_MAX_OPS];
+    const uint64_t *vv[FAST_MAX_OPS];
+    u32 kdesc;
+    u32 op[FAST_MAX_OPS];
+    int32_t n_ops;
+    int32_t swords;    // 32-bit words per shared state: count, then the ops
+    int32_t eligible;
+};
 
 struct BQuery {
+    FastPlan F;
     Plan P;
     TableRef T;
     EmitArgs E;
@@ -85,7 +104,7 @@ __global__ void k_batch_init(const BQuery *qs, const BItem *items, u32 n_items) 
     }
 }
 
-__global__ void k_batch_strdict(const BQuery *qs, const BItem *items, u32 n_items) {
+__global__ void __launch_bounds__(256, 4) k_batch_strdict(const BQuery *qs, const BItem *items, u32 n_items) {
     __shared__ StrDictRef D;
     __shared__ u32 s_new;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -116,8 +135,263 @@ __global__ void k_batch_strdict(const BQuery *qs, const BItem *items, u32 n_item
     }
 }
 
+// ------------------------------------------------------------- fast tiles
+__device__ __forceinline__ i64 fast_load(const void *p, int t, u64 r) {
+    switch (t) {
+    case GB_T_SMALLINT: return (i64)__ldg((const int16_t *)p + r);
+    case GB_T_INTEGER: return (i64)__ldg((const int32_t *)p + r);
+    default: return (i64)__ldg((const long long *)p + r);
+    }
+}
+
+__device__ __forceinline__ u64 fast_ident(int kind) {
+    return kind == OP_MIN_I ? 0x7fffffffffffffffull : (kind == OP_MAX_I ? 0x8000000000000000ull : 0ull);
+}
+
+// Fold a partial into an HBM state (count at word 0, op i at its word).
+template <int NOPS>
+__device__ __forceinline__ void fast_apply_global(const FastPlan &F, u64 *w, u64 cnt, const u64 *v) {
+    if (cnt) atomicAdd(w, cnt);
+#pragma unroll
+    for (int i = 0; i < NOPS; i++) {
+        const u32 od = F.op[i];
+        const int kind = od & 15;
+        op_apply(kind, w + ((od >> 8) & 255), v[i], fast_ident(kind));
+    }
+}
+
+template <int NOPS>
+__device__ __forceinline__ void fast_global(const FastPlan &F, const TableRef &T, u64 pk, u64 cnt, const u64 *v,
+                                            u32 *new_groups) {
+    const long long s = g_slot(T, pk, mix64(pk), new_groups);
+    if (s < 0) {
+        atomicAdd(&T.ctl->spill_count, 1u);  // the query re-runs on its own handle
+        return;
+    }
+    fast_apply_global<NOPS>(F, T.slots + (u64)s * (u64)T.stride + 1, cnt, v);
+}
+
+// Narrow shared states: count u32; ADD as a (lo, hi) u32 pair with carry;
+// CNT_NN u32; MIN/MAX s32 over SMALLINT/INTEGER, s64 over BIGINT.  Every
+// update is a native 32-bit shared atomic except the 64-bit MIN/MAX.
+template <int NOPS>
+__device__ __forceinline__ void fast_apply_smem(const FastPlan &F, u32 *st, u64 cnt, const u64 *v) {
+    atomicAdd(st, (u32)cnt);
+#pragma unroll
+    for (int i = 0; i < NOPS; i++) {
+        const u32 od = F.op[i];
+        const int kind = od & 15;
+        if (v[i] == fast_ident(kind)) continue;
+        u32 *w = st + ((od >> 16) & 255);
+        const bool wide = (od >> 24) & 1;
+        switch (kind) {
+        case OP_ADD_I: {
+            const u32 lo = (u32)v[i], hi = (u32)(v[i] >> 32);
+            const u32 old = atomicAdd(w, lo);
+            const u32 carry = (old + lo) < old ? 1u : 0u;
+            if (hi + carry) atomicAdd(w + 1, hi + carry);
+            break;
+        }
+        case OP_MIN_I:
+            if (wide) atomicMin((long long *)w, (long long)v[i]);
+            else atomicMin((int *)w, (int)(i64)v[i]);
+            break;
+        case OP_MAX_I:
+            if (wide) atomicMax((long long *)w, (long long)v[i]);
+            else atomicMax((int *)w, (int)(i64)v[i]);
+            break;
+        default:  // CNT_NN
+            atomicAdd(w, (u32)v[i]);
+            break;
+        }
+    }
+}
+
+template <int NOPS>
+__device__ __forceinline__ void fast_smem_init(const FastPlan &F, u64 *keys, u32 *st, int S) {
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+        keys[i] = EMPTY_KEY;
+        u32 *w = st + (u64)i * F.swords;
+        w[0] = 0;
+#pragma unroll
+        for (int j = 0; j < NOPS; j++) {
+            const u32 od = F.op[j];
+            const int kind = od & 15;
+            u32 *x = w + ((od >> 16) & 255);
+            const bool wide = (od >> 24) & 1;
+            if (kind == OP_ADD_I) {
+                x[0] = 0;
+                x[1] = 0;
+            } else if (kind == OP_MIN_I || kind == OP_MAX_I) {
+                if (wide) *(u64 *)x = fast_ident(kind);
+                else x[0] = kind == OP_MIN_I ? 0x7fffffffu : 0x80000000u;
+            } else {
+                x[0] = 0;
+            }
+        }
+    }
+}
+
+template <int NOPS>
+__device__ __forceinline__ void fast_smem_flush(const FastPlan &F, const TableRef &T, const u64 *keys, const u32 *st,
+                                                int S, u32 *new_groups) {
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+        const u64 k = keys[i];
+        if (k == EMPTY_KEY) continue;
+        const u32 *w = st + (u64)i * F.swords;
+        u64 v[NOPS ? NOPS : 1];
+#pragma unroll
+        for (int j = 0; j < NOPS; j++) {
+            const u32 od = F.op[j];
+            const int kind = od & 15;
+            const u32 *x = w + ((od >> 16) & 255);
+            const bool wide = (od >> 24) & 1;
+            if (kind == OP_ADD_I) v[j] = (u64)x[0] | ((u64)x[1] << 32);
+            else if (kind == OP_MIN_I || kind == OP_MAX_I) v[j] = wide ? *(const u64 *)x : (u64)(i64)(int)x[0];
+            else v[j] = x[0];
+        }
+        fast_global<NOPS>(F, T, k, w[0], v, new_groups);
+    }
+}
+
+// Raw column values of one row, loaded one warp step ahead of their use so
+// that the next step's loads are in flight while this step folds.
+template <int NOPS>
+struct FastRaw {
+    i64 a, b;
+    i64 x[NOPS ? NOPS : 1];
+    u32 vbits;  // bit 0/1 key validity, bit 2+i op column validity
+    bool act;
+};
+
+template <int NOPS>
+__device__ __forceinline__ void fast_fetch(const FastPlan &F, u64 r, u64 end, FastRaw<NOPS> &w) {
+    w.act = r < end;
+    w.a = w.b = 0;
+    w.vbits = 0;
+#pragma unroll
+    for (int i = 0; i < NOPS; i++) w.x[i] = 0;
+    if (!w.act) return;
+    const u32 kd = F.kdesc;
+    w.a = fast_load(F.kp[0], (kd >> 4) & 15, r);
+    w.vbits = row_valid(F.kv[0], r) ? 1u : 0u;
+    if ((kd & 15) == KEY_PACKED) {
+        w.b = fast_load(F.kp[1], (kd >> 8) & 15, r);
+        w.vbits |= row_valid(F.kv[1], r) ? 2u : 0u;
+    }
+#pragma unroll
+    for (int i = 0; i < NOPS; i++) {
+        const u32 od = F.op[i];
+        if ((od & 15) != OP_CNT_NN) w.x[i] = fast_load(F.vp[i], (od >> 4) & 15, r);
+        w.vbits |= row_valid(F.vv[i], r) ? (4u << i) : 0u;
+    }
+}
+
+// The packed key of a fetched row, exactly as make_key builds it.
+__device__ __forceinline__ int fast_key_of(u32 kd, i64 a_, i64 b_, u32 vbits, u64 &pk) {
+    const int mode = kd & 15;
+    if (mode != KEY_PACKED) {
+        if (!(vbits & 1u)) { pk = 0; return 2; }
+        pk = (u64)a_;
+        if (mode == KEY_STRING && a_ < 0) { pk = 0; return 2; }
+        return pk == EMPTY_KEY ? 1 : 0;
+    }
+    const int bb = (kd >> 16) & 255, ba = (kd >> 24) & 255;
+    const bool va = vbits & 1u, vb = vbits & 2u;
+    const u64 a = va ? (u64)a_ : 0ull, b = vb ? (u64)b_ : 0ull;
+    const u64 mb = (bb >= 64) ? ~0ull : ((1ull << bb) - 1ull);
+    const u64 ma = (ba >= 64) ? ~0ull : ((1ull << ba) - 1ull);
+    pk = ((a & ma) << bb) | (b & mb) | ((u64)(!va) << (ba + bb)) | ((u64)(!vb) << (ba + bb + 1));
+    return 0;
+}
+
+// One warp step of the fast path on fetched rows.
+template <bool PRECOMBINE, int NOPS>
+__device__ __forceinline__ void fast_rows(const FastPlan &F, const TableRef &T, u64 *keys, u32 *st, int S,
+                                          const FastRaw<NOPS> &w, u32 *new_groups) {
+    const int lane = threadIdx.x & 31;
+    bool act = w.act;
+    u64 pk = 0;
+    u64 v[NOPS ? NOPS : 1];
+#pragma unroll
+    for (int i = 0; i < NOPS; i++) {
+        const int kind = F.op[i] & 15;
+        v[i] = fast_ident(kind);
+        if (act && (w.vbits & (4u << i))) v[i] = kind == OP_CNT_NN ? 1ull : (u64)w.x[i];
+    }
+    if (act) {
+        const int kind = fast_key_of(F.kdesc, w.a, w.b, w.vbits, pk);
+        if (kind != 0) {
+            fast_apply_global<NOPS>(F, T.slots + (T.cap + (u64)(kind - 1)) * (u64)T.stride + 1, 1, v);
+            act = false;
+        }
+    }
+    const unsigned am = __ballot_sync(FULL, act);
+    if (am == 0) return;
+    u64 cnt = 1;
+    if (PRECOMBINE) {
+        const unsigned peers = __match_any_sync(FULL, pk) & am;
+        const bool leader = act && ((__ffs(peers) - 1) == lane);
+        unsigned rem = leader ? (peers & ~(1u << lane)) : 0u;
+        cnt = __popc(peers);
+        const int maxit = __reduce_max_sync(FULL, (unsigned)__popc(rem));
+        for (int it = 0; it < maxit; it++) {
+            const int src = rem ? (__ffs(rem) - 1) : lane;
+            rem &= rem - 1u;
+#pragma unroll
+            for (int i = 0; i < NOPS; i++) {
+                const u64 o = __shfl_sync(FULL, v[i], src);
+                if (src != lane) v[i] = op_combine(F.op[i] & 15, v[i], o);
+            }
+        }
+        act = leader;
+    }
+    if (!act) return;
+    if (S) {
+        const u64 h = mix64(pk);
+        u32 s = (u32)(h >> 40) & (u32)(S - 1);
+        volatile u64 *vk = keys;
+        for (int p = 0; p < 8; p++) {
+            const u64 k = vk[s];
+            bool hit = k == pk;
+            if (!hit && k == EMPTY_KEY) {
+                const u64 old = atomicCAS(&keys[s], EMPTY_KEY, pk);
+                hit = old == EMPTY_KEY || old == pk;
+            }
+            if (hit) {
+                fast_apply_smem<NOPS>(F, st + (u64)s * F.swords, cnt, v);
+                return;
+            }
+            s = (s + 1) & (u32)(S - 1);
+        }
+    }
+    fast_global<NOPS>(F, T, pk, cnt, v, new_groups);
+}
+
+template <bool PRECOMBINE, int NOPS>
+__device__ __forceinline__ void fast_tile(const FastPlan &F, const TableRef &T, u64 *bsm, int smem_bytes, int S,
+                                       u64 t0, u64 t1, u32 *new_groups) {
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    while (S && (size_t)S * (8 + 4 * (size_t)F.swords) > (size_t)smem_bytes) S >>= 1;
+    u64 *keys = bsm;
+    u32 *st = (u32 *)(bsm + S);
+    fast_smem_init<NOPS>(F, keys, st, S);
+    __syncthreads();
+    const u64 step = (u64)nwarps * 32;
+    u64 base = t0 + (u64)warp * 32;
+    FastRaw<NOPS> cur, nxt;
+    fast_fetch<NOPS>(F, base + (threadIdx.x & 31), t1, cur);
+    for (; base < t1; base += step) {
+        fast_fetch<NOPS>(F, base + step + (threadIdx.x & 31), t1, nxt);
+        fast_rows<PRECOMBINE, NOPS>(F, T, keys, st, S, cur, new_groups);
+        cur = nxt;
+    }
+    __syncthreads();
+    fast_smem_flush<NOPS>(F, T, keys, st, S, new_groups);
+}
+
 template <bool PRECOMBINE>
-__global__ void __launch_bounds__(512) k_batch_ingest(const BQuery *qs, const BItem *items, u32 n_items, Ctl *bctl,
+__global__ void __launch_bounds__(512, 2) k_batch_ingest(const BQuery *qs, const BItem *items, u32 n_items, Ctl *bctl,
                                                       int smem_bytes) {
     extern __shared__ u64 bsm[];
     __shared__ Plan sP;
@@ -144,6 +418,25 @@ __global__ void __launch_bounds__(512) k_batch_ingest(const BQuery *qs, const BI
         }
         const BItem w = items[it];
         const BQuery &q = qs[w.q];
+        const u64 t0 = (u64)w.idx * BATCH_TILE, t1 = min(q.n_rows, t0 + BATCH_TILE);
+        if (q.F.eligible) {
+            const FastPlan F = q.F;
+            const TableRef T = q.T;
+            switch (F.n_ops) {
+            case 0: fast_tile<PRECOMBINE, 0>(F, T, bsm, smem_bytes, q.smem_slots, t0, t1, &s_new); break;
+            case 1: fast_tile<PRECOMBINE, 1>(F, T, bsm, smem_bytes, q.smem_slots, t0, t1, &s_new); break;
+            case 2: fast_tile<PRECOMBINE, 2>(F, T, bsm, smem_bytes, q.smem_slots, t0, t1, &s_new); break;
+            case 3: fast_tile<PRECOMBINE, 3>(F, T, bsm, smem_bytes, q.smem_slots, t0, t1, &s_new); break;
+            default: fast_tile<PRECOMBINE, 4>(F, T, bsm, smem_bytes, q.smem_slots, t0, t1, &s_new); break;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                if (s_new) atomicAdd(&T.ctl->n_groups, s_new);
+                if (*(volatile u32 *)&T.ctl->spill_count > T.spill_threshold) atomicExch(&T.ctl->stop, 1u);
+            }
+            __syncthreads();
+            continue;
+        }
         copy_words(&sP, &q.P, (int)sizeof(Plan));
         copy_words(&sT, &q.T, (int)sizeof(TableRef));
         __syncthreads();
@@ -155,7 +448,6 @@ __global__ void __launch_bounds__(512) k_batch_ingest(const BQuery *qs, const BI
         sm.st = bsm + sm.S;
         smem_init(sP, sm);
         __syncthreads();
-        const u64 t0 = (u64)w.idx * BATCH_TILE, t1 = min(q.n_rows, t0 + BATCH_TILE);
         for (u64 base = t0 + (u64)warp * 32; base < t1; base += (u64)nwarps * 32)
             warp_rows<PRECOMBINE>(sP, sT, sm, base, t1, &s_new);
         __syncthreads();
@@ -222,10 +514,11 @@ struct gb_batch {
     bool prepared = false;
     bool use_graph = true;
     int ctas_per_sm = 2;
-    int smem_slots_max = 2048;
+    int smem_slots_max = 4096;
     bool precombine = true;
     bool profiling = false;
     int order = 0;  // 0 query-major tiles, 1 interleaved
+    bool fast = true;  // register-resident integer tiles where the plan allows
     struct BatchProf {
         const char *name;
         cudaEvent_t a = nullptr, b = nullptr;
@@ -236,6 +529,52 @@ struct gb_batch {
     u64 launches = 0;
     std::vector<int> slow;  // queries re-run on their handle in the last run
 };
+
+// The fast-path description of a query's plan (eligible = 0 when the plan
+// has filters, a full-width pair key, floating-point ops or more than
+// FAST_MAX_OPS ops: such queries take the generic tile path).
+static FastPlan make_fast_plan(const Plan &P) {
+    FastPlan F;
+    memset(&F, 0, sizeof F);
+    if (P.n_filters || P.key_mode == KEY_WIDE || P.n_ops > FAST_MAX_OPS) return F;
+    auto is_int = [](int t) { return t == GB_T_SMALLINT || t == GB_T_INTEGER || t == GB_T_BIGINT; };
+    for (int k = 0; k < P.n_keys; k++)
+        if (!is_int(P.cols[P.key_col[k]].type)) return F;
+    const int nk = P.key_mode == KEY_PACKED ? 2 : 1;
+    for (int k = 0; k < nk; k++) {
+        F.kp[k] = P.cols[P.key_col[k]].data;
+        F.kv[k] = P.cols[P.key_col[k]].valid;
+    }
+    const int t1 = nk == 2 ? P.cols[P.key_col[1]].type : 0;
+    F.kdesc = (u32)P.key_mode | ((u32)P.cols[P.key_col[0]].type << 4) | ((u32)t1 << 8);
+    if (P.key_mode == KEY_PACKED) F.kdesc |= ((u32)P.key_bits_b << 16) | ((u32)P.key_bits_a << 24);
+    int sw = 1;
+    for (int i = 0; i < P.n_ops; i++) {
+        const Op &o = P.ops[i];
+        const int t = P.cols[o.col].type;
+        if (o.kind != OP_ADD_I && o.kind != OP_MIN_I && o.kind != OP_MAX_I && o.kind != OP_CNT_NN) return F;
+        if (o.kind != OP_CNT_NN && !is_int(t)) return F;
+        const bool wide = (o.kind == OP_MIN_I || o.kind == OP_MAX_I) && t == GB_T_BIGINT;
+        if (wide && (sw & 1)) sw++;
+        F.op[i] = (u32)o.kind | ((u32)(t & 15) << 4) | ((u32)o.word << 8) | ((u32)sw << 16) | ((u32)wide << 24);
+        sw += (wide || o.kind == OP_ADD_I) ? 2 : 1;
+        F.vp[i] = P.cols[o.col].data;
+        F.vv[i] = P.cols[o.col].valid;
+    }
+    if (sw & 1) sw++;  // 8-byte aligned states (64-bit MIN/MAX words)
+    F.swords = sw;
+    F.n_ops = P.n_ops;
+    F.eligible = 1;
+    return F;
+}
+
+// Dynamic shared memory of one k_batch_ingest CTA so that `ctas` CTAs fit on
+// an SM (about 227 KB usable per SM, less each CTA's static shared memory).
+static int batch_smem_bytes(int ctas) {
+    int b = (227 * 1024) / std::max(1, ctas) - 4096;
+    b = std::min(b, 96 * 1024);
+    return b & ~4095;
+}
 
 static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
     const u32 nq = (u32)b->handles.size();
@@ -294,13 +633,24 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
         }
         if ((s = alloc_outputs(h, h->cap + 2))) return s;
         d.P = h->plan;
+        d.F = b->fast ? make_fast_plan(h->plan) : FastPlan{};
         d.T = table_ref(h);
         d.T.ctl = (Ctl *)b->qctl.p + q;
         d.T.spill_threshold = h->spill_cap / 2;
         fill_emit(h, d.E, h->out_cols, h->out_valid, h->out_cap);
         d.table_words = (h->cap + 2) * (u64)h->plan.stride;
         d.smem_slots = h->mode == 0 ? std::min(h->smem_slots, b->smem_slots_max) : 0;
-        if (h->est_groups > 65536) d.smem_slots = 0;  // a shared table only pays for small group counts
+        if (d.F.eligible) {
+            // narrow shared states: as many slots as fit, used when the
+            // estimated groups fit in them (else rows go straight to HBM)
+            const int per = 8 + 4 * d.F.swords;
+            int S = 1;
+            while (S * 2 * per <= batch_smem_bytes(b->ctas_per_sm)) S *= 2;
+            S = std::min(S, b->smem_slots_max);
+            d.smem_slots = h->est_groups <= (u64)S ? S : 0;
+        } else if (h->est_groups > 65536) {
+            d.smem_slots = 0;  // a shared table only pays for small group counts
+        }
         d.init_words = d.table_words + (u64)(d.E.n_keys + d.E.n_aggs) * ((d.E.out_cap + 63) / 64) +
                        (d.is_str ? 2 * d.D.cap + 8 : 0);
         for (u64 c = 0; c * 65536 < d.init_words; c++) it_init.push_back({q, (u32)c});
@@ -353,13 +703,6 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
     return GB_OK;
 }
 
-// Dynamic shared memory of one k_batch_ingest CTA so that `ctas` CTAs fit on
-// an SM (about 227 KB usable per SM, less each CTA's static shared memory).
-static int batch_smem_bytes(int ctas) {
-    int b = (227 * 1024) / std::max(1, ctas) - 4096;
-    b = std::min(b, 96 * 1024);
-    return b & ~4095;
-}
 
 // Profiling (graph off): events around each of the four kernels.
 using BatchProf = gb_batch::BatchProf;
@@ -472,6 +815,10 @@ gb_status gb_batch_set_option(gb_batch *b, const char *name, int64_t value) {
     else if (n == "smem_slots" && value >= 0 && value <= 4096 && !(value & (value - 1))) b->smem_slots_max = (int)value;
     else if (n == "precombine") b->precombine = value != 0;
     else if (n == "profiling") b->profiling = value != 0;
+    else if (n == "fast") {
+        b->fast = value != 0;
+        b->prepared = false;
+    }
     else if (n == "order" && (value == 0 || value == 1)) {
         b->order = (int)value;
         b->prepared = false;

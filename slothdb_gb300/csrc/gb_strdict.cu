@@ -23,7 +23,7 @@ namespace gb {
 // ids, one row per lane of warp-uniform groups of 32; rows that found no slot
 // are appended to `retry` for the host to re-run after growing the table /
 // arena.
-__global__ void k_strdict_encode(const StrDictRef D, const uint8_t *bytes, const int64_t *offsets, int64_t off_base,
+__global__ void __launch_bounds__(256, 4) k_strdict_encode(const StrDictRef D, const uint8_t *bytes, const int64_t *offsets, int64_t off_base,
                                  const uint64_t *valid, u64 n, const u32 *rows, long long *ids, u32 *retry,
                                  u32 *retry_n, u32 *new_strs_total) {
     __shared__ u32 s_new;

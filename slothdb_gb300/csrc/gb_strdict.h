@@ -80,9 +80,16 @@ __device__ __forceinline__ void strdict_kill(const StrDictRef &D, u64 slot, u32 
     atomicExch((unsigned long long *)(D.ref + slot), (unsigned long long)((DEAD_OFF << 24) | (u64)len));
 }
 
+// Acquire load of a published ref (orders the later arena / id reads after it).
+__device__ __forceinline__ u64 ld_acquire(const u64 *p) {
+    u64 v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
 // Bounded wait for a claimed slot's ref; REF_PENDING after the limit.
 __device__ __forceinline__ u64 strdict_wait_ref(const StrDictRef &D, u64 slot) {
-    u64 r = *(volatile u64 *)(D.ref + slot);
+    u64 r = ld_acquire(D.ref + slot);
     int spin = 0;
     while (r == REF_PENDING) {
         if (++spin > SPIN_LIMIT) {
@@ -90,9 +97,8 @@ __device__ __forceinline__ u64 strdict_wait_ref(const StrDictRef &D, u64 slot) {
             return REF_PENDING;
         }
         __nanosleep(32);
-        r = *(volatile u64 *)(D.ref + slot);
+        r = ld_acquire(D.ref + slot);
     }
-    __threadfence();
     return r;
 }
 
@@ -133,18 +139,78 @@ __device__ __forceinline__ long long strdict_find_or_insert(const StrDictRef &D,
     return -1;
 }
 
+// A string of at most 32 bytes held as four zero-padded chunks in registers
+// (read with at most five aligned 8-byte loads).
+constexpr u32 SHORT_STR = 32;
+
+__device__ __forceinline__ void short_chunks(const uint8_t *p, u32 len, u64 c[4]) {
+    const uintptr_t a = (uintptr_t)p;
+    const u64 *w = (const u64 *)(a & ~(uintptr_t)7);
+    const u32 nw = len ? (u32)(((a + len - 1) >> 3) - (a >> 3) + 1) : 0u;
+    u64 x[5];
+#pragma unroll
+    for (int i = 0; i < 5; i++) x[i] = (u32)i < nw ? __ldg(w + i) : 0ull;
+    const u32 sh = 8u * (u32)(a & 7);
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        u64 v = sh ? ((x[j] >> sh) | (x[j + 1] << (64 - sh))) : x[j];
+        const int nb = (int)len - 8 * j;
+        v = nb >= 8 ? v : (nb <= 0 ? 0ull : (v & ((1ull << (8 * nb)) - 1ull)));
+        c[j] = v;
+    }
+}
+
+// str_hash of a short string from its chunks (same value).
+__device__ __forceinline__ u64 short_hash(const u64 c[4], u32 len) {
+    u64 h = 0xcbf29ce484222325ull ^ ((u64)len * 0x9e3779b97f4a7c15ull);
+    const u32 full = len >> 3;
+#pragma unroll
+    for (u32 j = 0; j < 4; j++)
+        if (j < full) h = (h ^ c[j]) * 0x100000001b3ull;
+    u64 tail = 0;
+#pragma unroll
+    for (u32 j = 0; j < 4; j++)
+        if (j == full) tail = c[j];
+    h = (h ^ tail) * 0x100000001b3ull;  // a whole last chunk leaves tail = 0 (c[j] beyond len is 0)
+    return mix64(h);
+}
+
+__device__ __forceinline__ bool short_arena_equal(const StrDictRef &D, u64 r, const u64 c[4], u32 len) {
+    const u32 rlen = (u32)(r & 0xffffffu);
+    const u64 roff = r >> 24;
+    if (rlen != len || roff + ((len + 7u) & ~7u) > D.arena_cap) return false;
+    const u64 *aw = (const u64 *)(D.arena + roff);
+    const u32 nc = (len + 7) >> 3;
+    bool eq = true;
+#pragma unroll
+    for (u32 j = 0; j < 4; j++)
+        if (j < nc) eq &= aw[j] == c[j];
+    return eq;
+}
+
 // Warp-cooperative encode, one row per lane (all 32 lanes call it; `act`
 // marks lanes with a row).  Lanes with equal hashes elect a leader that
 // probes; the warp's new strings take their arena bytes and ids with one
 // atomic each per warp and are published before any lane of the warp waits
 // on a slot another warp has claimed but not yet published — so no two warps
 // can wait on each other.  Followers check they hold the leader's bytes (a
-// hash collision falls back to the one-thread path).
+// hash collision falls back to the one-thread path).  Strings of at most 32
+// bytes stay in registers; longer ones are re-read chunk by chunk.
 // Returns as strdict_find_or_insert.
 __device__ __forceinline__ long long strdict_warp_encode(const StrDictRef &D, const uint8_t *s, u32 len, bool act,
                                                          u32 *new_strs) {
     const int lane = threadIdx.x & 31;
-    const u64 h = act ? str_hash(s, len) : 0ull;
+    const bool shrt = len <= SHORT_STR;
+    u64 c[4] = {0ull, 0ull, 0ull, 0ull};
+    u64 h = 0;
+    if (act) {
+        if (shrt) {
+            short_chunks(s, len, c);
+            h = short_hash(c, len);
+        } else {
+            h = str_hash(s, len);
+        }
+    }
     const unsigned am = __ballot_sync(0xffffffffu, act);
     const unsigned peers = __match_any_sync(0xffffffffu, h) & am;
     const int lead = act ? __ffs(peers) - 1 : lane;
@@ -168,15 +234,14 @@ __device__ __forceinline__ long long strdict_warp_encode(const StrDictRef &D, co
                 k = old;
             }
             if (k == hv) {
-                const u64 r = *(volatile u64 *)(D.ref + slot);
+                const u64 r = ld_acquire(D.ref + slot);
                 if (r == REF_PENDING) {
                     waitslot = (long long)slot;
                     waitp = p;
                     break;
                 }
-                __threadfence();
-                if (arena_equal(D, r, s, len)) {
-                    id = (long long)*(volatile u64 *)(D.id + slot);
+                if (shrt ? short_arena_equal(D, r, c, len) : arena_equal(D, r, s, len)) {
+                    id = (long long)D.id[slot];
                     break;
                 }
             }
@@ -217,16 +282,24 @@ __device__ __forceinline__ long long strdict_warp_encode(const StrDictRef &D, co
     if (waitslot >= 0) {
         const u64 r = strdict_wait_ref(D, (u64)waitslot);
         if (r == REF_PENDING) id = -2;
-        else if (arena_equal(D, r, s, len)) id = (long long)*(volatile u64 *)(D.id + waitslot);
+        else if (shrt ? short_arena_equal(D, r, c, len) : arena_equal(D, r, s, len)) id = (long long)D.id[waitslot];
         else id = strdict_find_or_insert(D, s, len, h, new_strs, waitp + 1);
     }
     // followers take the leader's id when they hold the same bytes
     const long long lid = __shfl_sync(0xffffffffu, id, lead);
-    const uint8_t *ls = (const uint8_t *)__shfl_sync(0xffffffffu, (unsigned long long)(uintptr_t)s, lead);
     const u32 llen = __shfl_sync(0xffffffffu, len, lead);
+    u64 lc[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) lc[j] = __shfl_sync(0xffffffffu, c[j], lead);
+    const uint8_t *ls = (const uint8_t *)__shfl_sync(0xffffffffu, (unsigned long long)(uintptr_t)s, lead);
     if (act && !leader) {
         bool same = llen == len;
-        for (u32 j = 0; same && j < ((len + 7) >> 3); j++) same = str_chunk(s, len, j) == str_chunk(ls, len, j);
+        if (same && shrt) {
+#pragma unroll
+            for (int j = 0; j < 4; j++) same &= lc[j] == c[j];
+        } else {
+            for (u32 j = 0; same && j < ((len + 7) >> 3); j++) same = str_chunk(s, len, j) == str_chunk(ls, len, j);
+        }
         id = same ? lid : strdict_find_or_insert(D, s, len, h, new_strs);
     }
     return id;

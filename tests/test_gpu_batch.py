@@ -84,8 +84,9 @@ def test_batch_mixed_queries_match_oracle_and_replay():
         b.close()
 
 
-@pytest.mark.parametrize("options", [{"graph": 0}, {"smem_slots": 0, "precombine": 0}, {"ctas_per_sm": 1,
-                                                                                        "smem_slots": 512}])
+@pytest.mark.parametrize("options", [{"graph": 0}, {"smem_slots": 0, "precombine": 0},
+                                     {"ctas_per_sm": 1, "smem_slots": 512}, {"fast": 0}, {"order": 1},
+                                     {"fast": 0, "precombine": 0}])
 def test_batch_options(options):
     shapes = datagen.batch_shapes(n_tables=10, seed=8, rows_exp=(3.0, 5.0), groups_exp=(1.0, 4.0))
     b, host, _ = _build(shapes, options=options)
