@@ -178,7 +178,8 @@ uint64_t gb_agg_kernel_launches(const gb_agg *h);
  *   "precombine"  warp pre-combine of duplicate keys (0/1, hash)
  *   "ctas_per_sm" persistent CTAs per SM (hash)
  *   "tile_rows"   rows per claimed tile (hash)
- *   "hot_slots"   heavy-hitter table slots (power of two, radix) */
+ *   "hot_slots"   heavy-hitter table slots (power of two, radix)
+ *   "radix_bits"  log2 of the partition count, 6..12 (radix) */
 gb_status gb_agg_set_option(gb_agg *h, const char *name, int64_t value);
 /* 1 = radix mode, 0 = hash mode. */
 int32_t gb_agg_get_mode(const gb_agg *h);
@@ -250,7 +251,8 @@ gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg_begin, uin
  * same row counts, for every run of the batch.  Options ("graph" 0/1,
  * "ctas_per_sm" 1..4, "smem_slots" 0 or a power of two <= 4096,
  * "precombine" 0/1, "profiling" 0/1, "order" 0 query-major tiles / 1
- * interleaved) take effect at the next run; with
+ * interleaved, "tile_rows" a power of two in [1024, 2^20], "fast" 0/1 for
+ * the register-resident integer tile path) take effect at the next run; with
  * profiling on, runs skip the graph and gb_batch_profile reports CUDA-event
  * times of the four kernels. */
 typedef struct gb_batch gb_batch;

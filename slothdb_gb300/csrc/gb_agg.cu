@@ -1811,6 +1811,16 @@ gb_status gb_agg_set_option(gb_agg *h, const char *name, int64_t value) {
     } else if (n == "tile_rows") {
         if (value < 512 || value > (1 << 20) || value % 512) return GB_ERR_INVALID;
         h->tile_rows = (u32)value;
+    } else if (n == "radix_bits") {
+        if (h->mode != 1) {
+            set_error("radix_bits applies to radix mode only");
+            return GB_ERR_INVALID;
+        }
+        gb_status s = radix_set_bits(h->plan, h->rplan, (int)value);
+        if (s) {
+            set_error("radix_bits must be 6..12 and fit the partition pass's shared memory");
+            return s;
+        }
     } else if (n == "hot_slots") {
         if (h->mode != 1 || value < 64 || value > h->rplan.HS || (value & (value - 1))) return GB_ERR_INVALID;
         h->rplan.HS = (int)value;

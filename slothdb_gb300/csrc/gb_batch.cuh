@@ -19,7 +19,7 @@
 // the fast path: a query that needs a host decision (table spill, string
 // dictionary growth) is re-run on its own handle afterwards.
 
-#define BATCH_TILE 16384
+#define BATCH_TILE 16384  // default rows per work item (option "tile_rows")
 #define FAST_MAX_OPS 4
 
 // Integer-plan description kept in registers by the fast tile path (no
@@ -55,6 +55,8 @@ struct BQuery {
     u64 init_words;  // table words, output validity words, dictionary words
     int32_t smem_slots;
     int32_t is_str;
+    int32_t pre;        // fast path: combine equal keys within a warp first
+    u32 tile_rows;
 };
 
 struct BItem {
@@ -418,16 +420,27 @@ __global__ void __launch_bounds__(512, 2) k_batch_ingest(const BQuery *qs, const
         }
         const BItem w = items[it];
         const BQuery &q = qs[w.q];
-        const u64 t0 = (u64)w.idx * BATCH_TILE, t1 = min(q.n_rows, t0 + BATCH_TILE);
+        const u64 t0 = (u64)w.idx * q.tile_rows, t1 = min(q.n_rows, t0 + q.tile_rows);
         if (q.F.eligible) {
             const FastPlan F = q.F;
             const TableRef T = q.T;
-            switch (F.n_ops) {
-            case 0: fast_tile<PRECOMBINE, 0>(F, T, bsm, smem_bytes, q.smem_slots, t0, t1, &s_new); break;
-            case 1: fast_tile<PRECOMBINE, 1>(F, T, bsm, smem_bytes, q.smem_slots, t0, t1, &s_new); break;
-            case 2: fast_tile<PRECOMBINE, 2>(F, T, bsm, smem_bytes, q.smem_slots, t0, t1, &s_new); break;
-            case 3: fast_tile<PRECOMBINE, 3>(F, T, bsm, smem_bytes, q.smem_slots, t0, t1, &s_new); break;
-            default: fast_tile<PRECOMBINE, 4>(F, T, bsm, smem_bytes, q.smem_slots, t0, t1, &s_new); break;
+            const int S = q.smem_slots;
+            if (PRECOMBINE && q.pre) {
+                switch (F.n_ops) {
+                case 0: fast_tile<true, 0>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
+                case 1: fast_tile<true, 1>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
+                case 2: fast_tile<true, 2>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
+                case 3: fast_tile<true, 3>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
+                default: fast_tile<true, 4>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
+                }
+            } else {
+                switch (F.n_ops) {
+                case 0: fast_tile<false, 0>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
+                case 1: fast_tile<false, 1>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
+                case 2: fast_tile<false, 2>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
+                case 3: fast_tile<false, 3>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
+                default: fast_tile<false, 4>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
+                }
             }
             __syncthreads();
             if (threadIdx.x == 0) {
@@ -519,6 +532,7 @@ struct gb_batch {
     bool profiling = false;
     int order = 0;  // 0 query-major tiles, 1 interleaved
     bool fast = true;  // register-resident integer tiles where the plan allows
+    u32 tile_rows = BATCH_TILE;
     struct BatchProf {
         const char *name;
         cudaEvent_t a = nullptr, b = nullptr;
@@ -648,13 +662,17 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
             while (S * 2 * per <= batch_smem_bytes(b->ctas_per_sm)) S *= 2;
             S = std::min(S, b->smem_slots_max);
             d.smem_slots = h->est_groups <= (u64)S ? S : 0;
+            // narrow shared atomics beat the warp key match; without a shared
+            // table, few groups mean hot HBM slots, which the match relieves
+            d.pre = d.smem_slots == 0 && h->est_groups <= 4096;
         } else if (h->est_groups > 65536) {
             d.smem_slots = 0;  // a shared table only pays for small group counts
         }
         d.init_words = d.table_words + (u64)(d.E.n_keys + d.E.n_aggs) * ((d.E.out_cap + 63) / 64) +
                        (d.is_str ? 2 * d.D.cap + 8 : 0);
         for (u64 c = 0; c * 65536 < d.init_words; c++) it_init.push_back({q, (u32)c});
-        for (u64 c = 0; c * BATCH_TILE < n; c++) it_ing.push_back({q, (u32)c});
+        d.tile_rows = b->tile_rows;
+        for (u64 c = 0; c * b->tile_rows < n; c++) it_ing.push_back({q, (u32)c});
         for (u64 c = 0; c * (COMPACT_PER * 256) < h->cap + 2; c++) it_cmp.push_back({q, (u32)c});
     }
     // Tile order: query-major by default (the CTAs sweep one query's table
@@ -815,7 +833,10 @@ gb_status gb_batch_set_option(gb_batch *b, const char *name, int64_t value) {
     else if (n == "smem_slots" && value >= 0 && value <= 4096 && !(value & (value - 1))) b->smem_slots_max = (int)value;
     else if (n == "precombine") b->precombine = value != 0;
     else if (n == "profiling") b->profiling = value != 0;
-    else if (n == "fast") {
+    else if (n == "tile_rows" && value >= 1024 && value <= (1 << 20) && !(value & (value - 1))) {
+        b->tile_rows = (u32)value;
+        b->prepared = false;
+    } else if (n == "fast") {
         b->fast = value != 0;
         b->prepared = false;
     }

@@ -761,6 +761,16 @@ gb_status radix_prepare(const Plan &P, RadixPlan &R, u64 est_groups, u64 nullabl
     return GB_OK;
 }
 
+// Override the partition count (2^bits partitions) chosen by radix_prepare.
+gb_status radix_set_bits(const Plan &P, RadixPlan &R, int bits) {
+    if (bits < 6 || bits > 12) return GB_ERR_INVALID;
+    RadixPlan t = R;
+    t.pbits = bits;
+    if (radix_p1_smem(P, t) > kSmemBudget) return GB_ERR_UNSUPPORTED;
+    R = t;
+    return GB_OK;
+}
+
 gb_status radix_launch_sample(const Plan &P, const RadixPlan &R, u64 n, u64 *skeys, u32 *scnt, u64 scap,
                               u32 *hist, u32 *hstate, u64 *hot_keys, uint16_t *hot_idx, u64 *hot_list,
                               cudaStream_t st, u64 *launches) {

@@ -55,6 +55,7 @@ struct RadixTile {
 
 gb_status radix_prepare(const Plan &P, RadixPlan &R, u64 est_groups, u64 nullable_mask);
 size_t radix_p1_smem(const Plan &P, const RadixPlan &R);
+gb_status radix_set_bits(const Plan &P, RadixPlan &R, int bits);
 size_t radix_p2_smem(const Plan &P, const RadixPlan &R);
 u32 radix_tile_rows(const RadixPlan &R);
 gb_status radix_launch_sample(const Plan &P, const RadixPlan &R, u64 n, u64 *skeys, u32 *scnt, u64 scap, u32 *hist,
