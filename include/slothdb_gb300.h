@@ -250,7 +250,8 @@ gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg_begin, uin
  * Column pointers (gb_col) must be device memory and stay valid, with the
  * same row counts, for every run of the batch.  Options ("graph" 0/1,
  * "ctas_per_sm" 1..4, "smem_slots" 0 or a power of two <= 4096,
- * "precombine" 0/1, "profiling" 0/1, "order" 0 query-major tiles / 1
+ * "precombine" 0 never / 1 per query / 2 always, "profiling" 0/1, "order" 0
+ * query-major tiles / 1
  * interleaved, "tile_rows" a power of two in [1024, 2^20], "fast" 0/1 for
  * the register-resident integer tile path) take effect at the next run; with
  * profiling on, runs skip the graph and gb_batch_profile reports CUDA-event

@@ -8,11 +8,13 @@
 //
 //   k_batch_init     one launch: every query's table to its identity state;
 //   k_batch_strdict  one launch: VARCHAR keys of every VARCHAR query → ids;
-//   k_batch_ingest   one persistent launch over a device work queue of
-//                    (query, tile) items (query-major, so one table at a
-//                    time is hot in L2; uneven sizes balance dynamically);
-//                    each item copies its query's plan into shared memory and
-//                    runs the same warp pipeline as the single-query kernel;
+//   k_batch_fast /   one persistent launch per plan class over a device
+//   k_batch_generic  work queue of (query, tile) items (query-major, so one
+//                    table at a time is hot in L2; uneven sizes balance
+//                    dynamically).  Integer plans run a specialised,
+//                    register-resident pipeline with narrow shared-memory
+//                    states; any other plan runs the single-query pipeline
+//                    with its plan copied into shared memory per item;
 //   k_batch_compact  one launch: every query's table → its dense result.
 //
 // The sequence is captured once in a CUDA graph and replayed.  The graph is
@@ -20,11 +22,12 @@
 // dictionary growth) is re-run on its own handle afterwards.
 
 #define BATCH_TILE 16384  // default rows per work item (option "tile_rows")
-#define FAST_MAX_OPS 4
+#define FAST_MAX_OPS 2
+#define FAST_MAX_FILTERS 2
 
-// Integer-plan description kept in registers by the fast tile path (no
-// filters; keys SINGLE / PACKED / STRING; ops ADD_I, MIN_I, MAX_I, CNT_NN over
-// integer columns).  kdesc = key_mode | kt0 << 4 | kt1 << 8 | bits_b << 16 |
+// Integer-plan description kept in registers by the fast tile path (up to
+// FAST_MAX_FILTERS predicates on integer or DOUBLE columns; keys SINGLE /
+// PACKED / STRING; ops ADD_I, MIN_I, MAX_I, CNT_NN over integer columns).  kdesc = key_mode | kt0 << 4 | kt1 << 8 | bits_b << 16 |
 // bits_a << 24; op[i] = kind | type << 4 | table word << 8 | shared word << 16
 // | wide << 24, wide = a MIN/MAX over BIGINT (64-bit shared word).
 struct FastPlan {
@@ -34,13 +37,24 @@ struct FastPlan {
     const uint64_t *vv[FAST_MAX_OPS];
     u32 kdesc;
     u32 op[FAST_MAX_OPS];
+    int32_t n_filters;
     int32_t n_ops;
     int32_t swords;    // 32-bit words per shared state: count, then the ops
     int32_t eligible;
+    int32_t nulls;     // some key, op or filter column has a validity mask
+};
+
+// Predicates of the fast path (read from shared memory, once per row).
+struct FastFilters {
+    const void *fp[FAST_MAX_FILTERS];
+    const uint64_t *fv[FAST_MAX_FILTERS];
+    u64 fk[FAST_MAX_FILTERS];     // constant: int64, or the bits of a double
+    u32 fdesc[FAST_MAX_FILTERS];  // column type | gb_cmp << 4
 };
 
 struct BQuery {
     FastPlan F;
+    FastFilters FF;
     Plan P;
     TableRef T;
     EmitArgs E;
@@ -258,16 +272,18 @@ __device__ __forceinline__ void fast_smem_flush(const FastPlan &F, const TableRe
 
 // Raw column values of one row, loaded one warp step ahead of their use so
 // that the next step's loads are in flight while this step folds.
-template <int NOPS>
+template <int NOPS, bool FILT>
 struct FastRaw {
     i64 a, b;
     i64 x[NOPS ? NOPS : 1];
-    u32 vbits;  // bit 0/1 key validity, bit 2+i op column validity
+    u64 f[FILT ? FAST_MAX_FILTERS : 1];  // filter column values (raw bits)
+    u32 vbits;  // bit 0/1 key validity, bit 2+i op column validity, bit 8+j filter column validity
     bool act;
 };
 
-template <int NOPS>
-__device__ __forceinline__ void fast_fetch(const FastPlan &F, u64 r, u64 end, FastRaw<NOPS> &w) {
+template <int NOPS, bool NULLS, bool FILT>
+__device__ __forceinline__ void fast_fetch(const FastPlan &F, const FastFilters &FF, u64 r, u64 end,
+                                           FastRaw<NOPS, FILT> &w) {
     w.act = r < end;
     w.a = w.b = 0;
     w.vbits = 0;
@@ -276,17 +292,46 @@ __device__ __forceinline__ void fast_fetch(const FastPlan &F, u64 r, u64 end, Fa
     if (!w.act) return;
     const u32 kd = F.kdesc;
     w.a = fast_load(F.kp[0], (kd >> 4) & 15, r);
-    w.vbits = row_valid(F.kv[0], r) ? 1u : 0u;
+    w.vbits = NULLS ? (row_valid(F.kv[0], r) ? 1u : 0u) : ~0u;
     if ((kd & 15) == KEY_PACKED) {
         w.b = fast_load(F.kp[1], (kd >> 8) & 15, r);
-        w.vbits |= row_valid(F.kv[1], r) ? 2u : 0u;
+        if (NULLS) w.vbits |= row_valid(F.kv[1], r) ? 2u : 0u;
     }
 #pragma unroll
     for (int i = 0; i < NOPS; i++) {
         const u32 od = F.op[i];
         if ((od & 15) != OP_CNT_NN) w.x[i] = fast_load(F.vp[i], (od >> 4) & 15, r);
-        w.vbits |= row_valid(F.vv[i], r) ? (4u << i) : 0u;
+        if (NULLS) w.vbits |= row_valid(F.vv[i], r) ? (4u << i) : 0u;
     }
+#pragma unroll
+    for (int j = 0; j < (FILT ? FAST_MAX_FILTERS : 0); j++) {
+        w.f[j] = 0;
+        if (j < F.n_filters) {
+            const int t = FF.fdesc[j] & 15;
+            w.f[j] = t == GB_T_DOUBLE ? (u64)__double_as_longlong(__ldg((const double *)FF.fp[j] + r))
+                                      : (u64)fast_load(FF.fp[j], t, r);
+            if (NULLS) w.vbits |= row_valid(FF.fv[j], r) ? (256u << j) : 0u;
+        }
+    }
+}
+
+// The row passes every predicate (a NULL input fails it, as pass_filters).
+__device__ __forceinline__ bool fast_pass(const FastPlan &F, const FastFilters &FF, const u64 *f, u32 vbits) {
+    bool ok = true;
+#pragma unroll
+    for (int j = 0; j < FAST_MAX_FILTERS; j++) {
+        if (j < F.n_filters) {
+            const u32 fd = FF.fdesc[j];
+            const int op = (fd >> 4) & 15;
+            bool p;
+            if ((fd & 15) == GB_T_DOUBLE)
+                p = cmp_f(op, __longlong_as_double((i64)f[j]), __longlong_as_double((i64)FF.fk[j]));
+            else
+                p = cmp_i(op, (i64)f[j], (i64)FF.fk[j]);
+            ok = ok && p && (vbits & (256u << j));
+        }
+    }
+    return ok;
 }
 
 // The packed key of a fetched row, exactly as make_key builds it.
@@ -308,11 +353,11 @@ __device__ __forceinline__ int fast_key_of(u32 kd, i64 a_, i64 b_, u32 vbits, u6
 }
 
 // One warp step of the fast path on fetched rows.
-template <bool PRECOMBINE, int NOPS>
-__device__ __forceinline__ void fast_rows(const FastPlan &F, const TableRef &T, u64 *keys, u32 *st, int S,
-                                          const FastRaw<NOPS> &w, u32 *new_groups) {
+template <bool PRECOMBINE, int NOPS, bool FILT>
+__device__ __forceinline__ void fast_rows(const FastPlan &F, const FastFilters &FF, const TableRef &T, u64 *keys,
+                                          u32 *st, int S, const FastRaw<NOPS, FILT> &w, u32 *new_groups) {
     const int lane = threadIdx.x & 31;
-    bool act = w.act;
+    bool act = w.act && (!FILT || fast_pass(F, FF, w.f, w.vbits));
     u64 pk = 0;
     u64 v[NOPS ? NOPS : 1];
 #pragma unroll
@@ -370,9 +415,11 @@ __device__ __forceinline__ void fast_rows(const FastPlan &F, const TableRef &T, 
     fast_global<NOPS>(F, T, pk, cnt, v, new_groups);
 }
 
-template <bool PRECOMBINE, int NOPS>
-__device__ __forceinline__ void fast_tile(const FastPlan &F, const TableRef &T, u64 *bsm, int smem_bytes, int S,
-                                       u64 t0, u64 t1, u32 *new_groups) {
+// One tile of the fast path (inlined into its class's kernel: the plan's
+// fields stay in registers).
+template <bool PRECOMBINE, int NOPS, bool NULLS, bool FILT>
+__device__ __forceinline__ void fast_tile(const FastPlan &F, const FastFilters &FF, const TableRef &T, u64 *bsm,
+                                          int smem_bytes, int S, u64 t0, u64 t1, u32 *new_groups) {
     const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     while (S && (size_t)S * (8 + 4 * (size_t)F.swords) > (size_t)smem_bytes) S >>= 1;
     u64 *keys = bsm;
@@ -381,34 +428,50 @@ __device__ __forceinline__ void fast_tile(const FastPlan &F, const TableRef &T, 
     __syncthreads();
     const u64 step = (u64)nwarps * 32;
     u64 base = t0 + (u64)warp * 32;
-    FastRaw<NOPS> cur, nxt;
-    fast_fetch<NOPS>(F, base + (threadIdx.x & 31), t1, cur);
+    FastRaw<NOPS, FILT> cur, nxt;
+    fast_fetch<NOPS, NULLS, FILT>(F, FF, base + (threadIdx.x & 31), t1, cur);
     for (; base < t1; base += step) {
-        fast_fetch<NOPS>(F, base + step + (threadIdx.x & 31), t1, nxt);
-        fast_rows<PRECOMBINE, NOPS>(F, T, keys, st, S, cur, new_groups);
+        fast_fetch<NOPS, NULLS, FILT>(F, FF, base + step + (threadIdx.x & 31), t1, nxt);
+        fast_rows<PRECOMBINE, NOPS, FILT>(F, FF, T, keys, st, S, cur, new_groups);
         cur = nxt;
     }
     __syncthreads();
     fast_smem_flush<NOPS>(F, T, keys, st, S, new_groups);
 }
 
+// One tile of the generic path (any plan; the plan is in shared memory).
 template <bool PRECOMBINE>
-__global__ void __launch_bounds__(512, 2) k_batch_ingest(const BQuery *qs, const BItem *items, u32 n_items, Ctl *bctl,
-                                                      int smem_bytes) {
-    extern __shared__ u64 bsm[];
-    __shared__ Plan sP;
-    __shared__ TableRef sT;
-    __shared__ u32 s_item, s_new, s_skip;
+__device__ __noinline__ void generic_tile(const Plan &sP, const TableRef &sT, u64 *bsm, int S, int smem_bytes, u64 t0,
+                                          u64 t1, u32 *new_groups) {
     const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    SmemTable sm;
+    sm.S = S;
+    while (sm.S && (size_t)sm.S * 8 * (1 + sP.words) > (size_t)smem_bytes) sm.S >>= 1;
+    sm.probe = 8;
+    sm.keys = bsm;
+    sm.st = bsm + sm.S;
+    smem_init(sP, sm);
+    __syncthreads();
+    for (u64 base = t0 + (u64)warp * 32; base < t1; base += (u64)nwarps * 32)
+        warp_rows<PRECOMBINE>(sP, sT, sm, base, t1, new_groups);
+    __syncthreads();
+    smem_flush(sP, sT, sm, new_groups);
+}
+
+// The persistent loop shared by the ingest kernels: claim the next item of
+// this kernel's class, skip queries stopped by their spill threshold (they
+// re-run on their own handle), run `tile` on it, publish the group count.
+template <class Tile>
+__device__ __forceinline__ void batch_item_loop(const BQuery *qs, const BItem *items, u32 n_items, Ctl *cctl,
+                                                Tile tile) {
+    __shared__ u32 s_item, s_new, s_skip;
     for (;;) {
         if (threadIdx.x == 0) {
             u32 t = ~0u;
-            const u32 c = atomicAdd(&bctl->tile_counter, 1u);
+            const u32 c = atomicAdd(&cctl->tile_counter, 1u);
             if (c < n_items) t = c;
             s_item = t;
             s_new = 0;
-            // a query stopped by its spill threshold skips its remaining tiles
-            // (the host re-runs it on its own handle)
             s_skip = t != ~0u && *(volatile u32 *)&qs[items[t].q].T.ctl->stop != 0;
         }
         __syncthreads();
@@ -421,57 +484,74 @@ __global__ void __launch_bounds__(512, 2) k_batch_ingest(const BQuery *qs, const
         const BItem w = items[it];
         const BQuery &q = qs[w.q];
         const u64 t0 = (u64)w.idx * q.tile_rows, t1 = min(q.n_rows, t0 + q.tile_rows);
-        if (q.F.eligible) {
-            const FastPlan F = q.F;
-            const TableRef T = q.T;
-            const int S = q.smem_slots;
-            if (PRECOMBINE && q.pre) {
-                switch (F.n_ops) {
-                case 0: fast_tile<true, 0>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
-                case 1: fast_tile<true, 1>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
-                case 2: fast_tile<true, 2>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
-                case 3: fast_tile<true, 3>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
-                default: fast_tile<true, 4>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
-                }
-            } else {
-                switch (F.n_ops) {
-                case 0: fast_tile<false, 0>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
-                case 1: fast_tile<false, 1>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
-                case 2: fast_tile<false, 2>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
-                case 3: fast_tile<false, 3>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
-                default: fast_tile<false, 4>(F, T, bsm, smem_bytes, S, t0, t1, &s_new); break;
-                }
-            }
-            __syncthreads();
-            if (threadIdx.x == 0) {
-                if (s_new) atomicAdd(&T.ctl->n_groups, s_new);
-                if (*(volatile u32 *)&T.ctl->spill_count > T.spill_threshold) atomicExch(&T.ctl->stop, 1u);
-            }
-            __syncthreads();
-            continue;
-        }
-        copy_words(&sP, &q.P, (int)sizeof(Plan));
-        copy_words(&sT, &q.T, (int)sizeof(TableRef));
-        __syncthreads();
-        SmemTable sm;
-        sm.S = q.smem_slots;
-        while (sm.S && (size_t)sm.S * 8 * (1 + sP.words) > (size_t)smem_bytes) sm.S >>= 1;
-        sm.probe = 8;
-        sm.keys = bsm;
-        sm.st = bsm + sm.S;
-        smem_init(sP, sm);
-        __syncthreads();
-        for (u64 base = t0 + (u64)warp * 32; base < t1; base += (u64)nwarps * 32)
-            warp_rows<PRECOMBINE>(sP, sT, sm, base, t1, &s_new);
-        __syncthreads();
-        smem_flush(sP, sT, sm, &s_new);
+        Ctl *qctl = tile(q, t0, t1, &s_new);
         __syncthreads();
         if (threadIdx.x == 0) {
-            if (s_new) atomicAdd(&sT.ctl->n_groups, s_new);
-            if (*(volatile u32 *)&sT.ctl->spill_count > sT.spill_threshold) atomicExch(&sT.ctl->stop, 1u);
+            if (s_new) atomicAdd(&qctl->n_groups, s_new);
+            if (*(volatile u32 *)&qctl->spill_count > q.T.spill_threshold) atomicExch(&qctl->stop, 1u);
         }
         __syncthreads();
     }
+}
+
+// Fast-path ingest for one plan class (PRECOMBINE, NOPS, NULLS, FILT): a
+// separate kernel per class, so each gets its own register allocation.
+template <bool PRECOMBINE, int NOPS, bool NULLS, bool FILT>
+__global__ void __launch_bounds__(512, 2) k_batch_fast(const BQuery *qs, const BItem *items, u32 n_items, Ctl *cctl,
+                                                    int smem_bytes) {
+    extern __shared__ u64 bsm[];
+    __shared__ FastFilters sFF;
+    batch_item_loop(qs, items, n_items, cctl, [&](const BQuery &q, u64 t0, u64 t1, u32 *s_new) -> Ctl * {
+        if (FILT) {
+            copy_words(&sFF, &q.FF, (int)sizeof(FastFilters));
+            __syncthreads();
+        }
+        const FastPlan F = q.F;
+        const TableRef T = q.T;
+        fast_tile<PRECOMBINE, NOPS, NULLS, FILT>(F, sFF, T, bsm, smem_bytes, q.smem_slots, t0, t1, s_new);
+        return T.ctl;
+    });
+}
+
+// Generic-path ingest (any plan; the plan is copied to shared memory per item).
+template <bool PRECOMBINE>
+__global__ void __launch_bounds__(512, 2) k_batch_generic(const BQuery *qs, const BItem *items, u32 n_items,
+                                                       Ctl *cctl, int smem_bytes) {
+    extern __shared__ u64 bsm[];
+    __shared__ Plan sP;
+    __shared__ TableRef sT;
+    batch_item_loop(qs, items, n_items, cctl, [&](const BQuery &q, u64 t0, u64 t1, u32 *s_new) -> Ctl * {
+        copy_words(&sP, &q.P, (int)sizeof(Plan));
+        copy_words(&sT, &q.T, (int)sizeof(TableRef));
+        __syncthreads();
+        generic_tile<PRECOMBINE>(sP, sT, bsm, q.smem_slots, smem_bytes, t0, t1, s_new);
+        return q.T.ctl;
+    });
+}
+
+// Plan classes: 0 = generic without / 1 = with the warp pre-combine;
+// 2 + (pre * 12 + nops * 4 + nulls * 2 + filt) = a fast-path kernel.
+constexpr int BATCH_CLASSES = 2 + 24;
+
+typedef void (*BatchKernel)(const BQuery *, const BItem *, u32, Ctl *, int);
+
+static BatchKernel batch_kernel(int cls) {
+    static const BatchKernel tab[BATCH_CLASSES] = {
+        k_batch_generic<false>, k_batch_generic<true>,
+        k_batch_fast<false, 0, false, false>, k_batch_fast<false, 0, false, true>,
+        k_batch_fast<false, 0, true, false>, k_batch_fast<false, 0, true, true>,
+        k_batch_fast<false, 1, false, false>, k_batch_fast<false, 1, false, true>,
+        k_batch_fast<false, 1, true, false>, k_batch_fast<false, 1, true, true>,
+        k_batch_fast<false, 2, false, false>, k_batch_fast<false, 2, false, true>,
+        k_batch_fast<false, 2, true, false>, k_batch_fast<false, 2, true, true>,
+        k_batch_fast<true, 0, false, false>, k_batch_fast<true, 0, false, true>,
+        k_batch_fast<true, 0, true, false>, k_batch_fast<true, 0, true, true>,
+        k_batch_fast<true, 1, false, false>, k_batch_fast<true, 1, false, true>,
+        k_batch_fast<true, 1, true, false>, k_batch_fast<true, 1, true, true>,
+        k_batch_fast<true, 2, false, false>, k_batch_fast<true, 2, false, true>,
+        k_batch_fast<true, 2, true, false>, k_batch_fast<true, 2, true, true>,
+    };
+    return tab[cls];
 }
 
 __global__ void k_batch_compact(const BQuery *qs, const BItem *items, u32 n_items) {
@@ -522,13 +602,14 @@ struct gb_batch {
     DevBuf qdesc, items_init, items_str, items_ingest, items_compact, bctl, qctl;
     HostBuf qctl_host;
     u32 n_init = 0, n_str = 0, n_ingest = 0, n_compact = 0;
+    u32 cls_off[BATCH_CLASSES] = {}, cls_n[BATCH_CLASSES] = {};  // ingest items per plan class
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     bool prepared = false;
     bool use_graph = true;
     int ctas_per_sm = 2;
     int smem_slots_max = 4096;
-    bool precombine = true;
+    int precombine = 1;  // 0 never, 1 per query (auto), 2 always
     bool profiling = false;
     int order = 0;  // 0 query-major tiles, 1 interleaved
     bool fast = true;  // register-resident integer tiles where the plan allows
@@ -547,10 +628,11 @@ struct gb_batch {
 // The fast-path description of a query's plan (eligible = 0 when the plan
 // has filters, a full-width pair key, floating-point ops or more than
 // FAST_MAX_OPS ops: such queries take the generic tile path).
-static FastPlan make_fast_plan(const Plan &P) {
+static FastPlan make_fast_plan(const Plan &P, FastFilters &FF) {
     FastPlan F;
     memset(&F, 0, sizeof F);
-    if (P.n_filters || P.key_mode == KEY_WIDE || P.n_ops > FAST_MAX_OPS) return F;
+    memset(&FF, 0, sizeof FF);
+    if (P.n_filters > FAST_MAX_FILTERS || P.key_mode == KEY_WIDE || P.n_ops > FAST_MAX_OPS) return F;
     auto is_int = [](int t) { return t == GB_T_SMALLINT || t == GB_T_INTEGER || t == GB_T_BIGINT; };
     for (int k = 0; k < P.n_keys; k++)
         if (!is_int(P.cols[P.key_col[k]].type)) return F;
@@ -575,6 +657,20 @@ static FastPlan make_fast_plan(const Plan &P) {
         F.vp[i] = P.cols[o.col].data;
         F.vv[i] = P.cols[o.col].valid;
     }
+    for (int j = 0; j < P.n_filters; j++) {
+        const Filter &f = P.filters[j];
+        const int t = P.cols[f.col].type;
+        if (!is_int(t) && t != GB_T_DOUBLE) return F;
+        FF.fp[j] = P.cols[f.col].data;
+        FF.fv[j] = P.cols[f.col].valid;
+        if (t == GB_T_DOUBLE) memcpy(&FF.fk[j], &f.dc, 8);
+        else FF.fk[j] = (u64)f.ic;
+        FF.fdesc[j] = (u32)t | ((u32)f.op << 4);
+    }
+    F.n_filters = P.n_filters;
+    F.nulls = (F.kv[0] || F.kv[1]) ? 1 : 0;
+    for (int i = 0; i < P.n_ops; i++) F.nulls |= F.vv[i] ? 1 : 0;
+    for (int j = 0; j < P.n_filters; j++) F.nulls |= FF.fv[j] ? 1 : 0;
     if (sw & 1) sw++;  // 8-byte aligned states (64-bit MIN/MAX words)
     F.swords = sw;
     F.n_ops = P.n_ops;
@@ -595,7 +691,7 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
     std::vector<BQuery> qs(nq);
     std::vector<BItem> it_init, it_str, it_ing, it_cmp;
     gb_status s;
-    if ((s = b->qctl.ensure((size_t)nq * sizeof(Ctl) + 64)) || (s = b->bctl.ensure(sizeof(Ctl))) ||
+    if ((s = b->qctl.ensure((size_t)nq * sizeof(Ctl) + 64)) || (s = b->bctl.ensure(BATCH_CLASSES * sizeof(Ctl))) ||
         (s = b->qctl_host.ensure((size_t)nq * sizeof(Ctl) + 64)))
         return s;
     for (u32 q = 0; q < nq; q++) {
@@ -647,7 +743,7 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
         }
         if ((s = alloc_outputs(h, h->cap + 2))) return s;
         d.P = h->plan;
-        d.F = b->fast ? make_fast_plan(h->plan) : FastPlan{};
+        if (b->fast) d.F = make_fast_plan(h->plan, d.FF);
         d.T = table_ref(h);
         d.T.ctl = (Ctl *)b->qctl.p + q;
         d.T.spill_threshold = h->spill_cap / 2;
@@ -664,7 +760,7 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
             d.smem_slots = h->est_groups <= (u64)S ? S : 0;
             // narrow shared atomics beat the warp key match; without a shared
             // table, few groups mean hot HBM slots, which the match relieves
-            d.pre = d.smem_slots == 0 && h->est_groups <= 4096;
+            d.pre = b->precombine == 2 || (b->precombine == 1 && d.smem_slots == 0 && h->est_groups <= 4096);
         } else if (h->est_groups > 65536) {
             d.smem_slots = 0;  // a shared table only pays for small group counts
         }
@@ -695,6 +791,23 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
         }
     }
     if (b->order == 1) it_ing.swap(mixed);
+    // group the items by plan class (one persistent kernel per class)
+    {
+        std::vector<int> qcls(nq);
+        for (u32 q = 0; q < nq; q++) {
+            const BQuery &d = qs[q];
+            qcls[q] = d.F.eligible ? 2 + (d.pre ? 12 : 0) + d.F.n_ops * 4 + d.F.nulls * 2 + (d.F.n_filters ? 1 : 0)
+                                   : (b->precombine ? 1 : 0);
+        }
+        std::vector<std::vector<BItem>> per(BATCH_CLASSES);
+        for (auto &x : it_ing) per[qcls[x.q]].push_back(x);
+        it_ing.clear();
+        for (int c = 0; c < BATCH_CLASSES; c++) {
+            b->cls_off[c] = (u32)it_ing.size();
+            b->cls_n[c] = (u32)per[c].size();
+            it_ing.insert(it_ing.end(), per[c].begin(), per[c].end());
+        }
+    }
     if ((s = b->qdesc.ensure(qs.size() * sizeof(BQuery) + 64)) ||
         (s = b->items_init.ensure(it_init.size() * sizeof(BItem) + 64)) ||
         (s = b->items_str.ensure(it_str.size() * sizeof(BItem) + 64)) ||
@@ -713,8 +826,8 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
     b->n_compact = (u32)it_cmp.size();
     static bool attr = false;
     if (!attr) {
-        cudaFuncSetAttribute(k_batch_ingest<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
-        cudaFuncSetAttribute(k_batch_ingest<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
+        for (int c = 0; c < BATCH_CLASSES; c++)
+            cudaFuncSetAttribute(batch_kernel(c), cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024);
         attr = true;
     }
     b->prepared = true;
@@ -743,6 +856,8 @@ static void batch_prof_collect(gb_batch *b) {
         if (cudaEventElapsedTime(&ms, p.a, p.b) == cudaSuccess) {
             p.ms += ms;
             p.n++;
+        } else {
+            (void)cudaGetLastError();  // leave no sticky error behind
         }
         p.pending = false;
     }
@@ -753,7 +868,7 @@ static gb_status batch_enqueue(gb_batch *b, cudaStream_t st) {
     const u32 nq = (u32)b->handles.size();
     const int sms = sm_count();
     GB_CUDA(cudaMemsetAsync(b->qctl.p, 0, (size_t)nq * sizeof(Ctl), st));
-    GB_CUDA(cudaMemsetAsync(b->bctl.p, 0, sizeof(Ctl), st));
+    GB_CUDA(cudaMemsetAsync(b->bctl.p, 0, BATCH_CLASSES * sizeof(Ctl), st));
     batch_prof(b, 0, st, true);
     k_batch_init<<<std::max(1, std::min((int)b->n_init, sms * 8)), 256, 0, st>>>((const BQuery *)b->qdesc.p,
                                                                                (const BItem *)b->items_init.p, b->n_init);
@@ -767,16 +882,15 @@ static gb_status batch_enqueue(gb_batch *b, cudaStream_t st) {
         batch_prof(b, 1, st, false);
     }
     const int smem_bytes = batch_smem_bytes(b->ctas_per_sm);
-    const int grid = std::max(1, std::min((int)b->n_ingest, sms * b->ctas_per_sm));
     batch_prof(b, 2, st, true);
-    if (b->precombine)
-        k_batch_ingest<true><<<grid, 512, smem_bytes, st>>>((const BQuery *)b->qdesc.p, (const BItem *)b->items_ingest.p,
-                                                           b->n_ingest, (Ctl *)b->bctl.p, smem_bytes);
-    else
-        k_batch_ingest<false><<<grid, 512, smem_bytes, st>>>((const BQuery *)b->qdesc.p,
-                                                            (const BItem *)b->items_ingest.p, b->n_ingest,
-                                                            (Ctl *)b->bctl.p, smem_bytes);
-    GB_CUDA(cudaGetLastError());
+    for (int c = 0; c < BATCH_CLASSES; c++) {
+        if (!b->cls_n[c]) continue;
+        const int grid = std::max(1, std::min((int)b->cls_n[c], sms * b->ctas_per_sm));
+        batch_kernel(c)<<<grid, 512, smem_bytes, st>>>((const BQuery *)b->qdesc.p,
+                                                      (const BItem *)b->items_ingest.p + b->cls_off[c], b->cls_n[c],
+                                                      (Ctl *)b->bctl.p + c, smem_bytes);
+        GB_CUDA(cudaGetLastError());
+    }
     batch_prof(b, 2, st, false);
     batch_prof(b, 3, st, true);
     k_batch_compact<<<std::max(1, std::min((int)b->n_compact, sms * 8)), 256, 0, st>>>(
@@ -831,7 +945,10 @@ gb_status gb_batch_set_option(gb_batch *b, const char *name, int64_t value) {
     if (n == "graph") b->use_graph = value != 0;
     else if (n == "ctas_per_sm" && value >= 1 && value <= 4) b->ctas_per_sm = (int)value;
     else if (n == "smem_slots" && value >= 0 && value <= 4096 && !(value & (value - 1))) b->smem_slots_max = (int)value;
-    else if (n == "precombine") b->precombine = value != 0;
+    else if (n == "precombine" && value >= 0 && value <= 2) {
+        b->precombine = (int)value;
+        b->prepared = false;
+    }
     else if (n == "profiling") b->profiling = value != 0;
     else if (n == "tile_rows" && value >= 1024 && value <= (1 << 20) && !(value & (value - 1))) {
         b->tile_rows = (u32)value;
@@ -880,7 +997,9 @@ gb_status gb_batch_run(gb_batch *b, void *stream) {
     } else {
         if ((s = batch_enqueue(b, st))) return s;
     }
-    b->launches += 3 + (b->n_str ? 1 : 0);
+    u32 ncls = 0;
+    for (int c = 0; c < BATCH_CLASSES; c++) ncls += b->cls_n[c] ? 1 : 0;
+    b->launches += 2 + ncls + (b->n_str ? 1 : 0);
     GB_CUDA(cudaStreamSynchronize(st));
     batch_prof_collect(b);
     const Ctl *qc = (const Ctl *)b->qctl_host.p;

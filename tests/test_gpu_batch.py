@@ -86,7 +86,7 @@ def test_batch_mixed_queries_match_oracle_and_replay():
 
 @pytest.mark.parametrize("options", [{"graph": 0}, {"smem_slots": 0, "precombine": 0},
                                      {"ctas_per_sm": 1, "smem_slots": 512}, {"fast": 0}, {"order": 1},
-                                     {"fast": 0, "precombine": 0}])
+                                     {"fast": 0, "precombine": 0}, {"profiling": 1}, {"precombine": 2}])
 def test_batch_options(options):
     shapes = datagen.batch_shapes(n_tables=10, seed=8, rows_exp=(3.0, 5.0), groups_exp=(1.0, 4.0))
     b, host, _ = _build(shapes, options=options)
@@ -95,6 +95,9 @@ def test_batch_options(options):
             b.run()
             for i, sh in enumerate(shapes):
                 compare(_gpu(b.result(i), sh), _orc(sh, host[i]))
+        if options.get("profiling"):
+            prof = b.profile()
+            assert prof["k_batch_ingest"][0] == 2 and prof["k_batch_ingest"][1] > 0
     finally:
         b.close()
 
@@ -173,5 +176,51 @@ def test_batch_empty_tiny_and_nullable():
         orc = oracle.run_query(COMP["col_types"], COMP["group_cols"], COMP["aggs"], [a, kb, s, m],
                                nulls=[an, None, None, mn])
         compare(_gpu(b.result(2), dict(kind="composite")), orc)
+    finally:
+        b.close()
+
+
+def test_batch_filters_int_and_double():
+    """WHERE predicates on the fast path (integer and DOUBLE columns, with
+    and without NULLs) and on the generic path (a DOUBLE SUM)."""
+    import torch
+    rng = np.random.default_rng(31)
+    b = capi.Batch()
+    checks = []
+    try:
+        for i, (kind, flt) in enumerate([("composite", [(2, "<", 300_000)]),
+                                          ("composite", [(3, ">=", 0), (2, "!=", 5)]),
+                                          ("varchar", [(1, "<", 500_000)]),
+                                          ("composite", [(2, "<", -1)])]):   # selects nothing
+            sh = dict(kind=kind, rows=120_000 + 17 * i, groups=3000 + 1000 * i, seed=40 + i)
+            q = _q(sh)
+            cols = datagen.batch_table_host(sh)
+            b.add(q["col_types"], q["group_cols"], q["aggs"], _to_device(cols, q["col_types"]), sh["rows"],
+                  filters=flt, est_groups=sh["groups"])
+            checks.append((sh, oracle.run_query(q["col_types"], q["group_cols"], q["aggs"], cols, filters=flt)))
+        # DOUBLE filter + nullable filter column on the fast path
+        n = 90_001
+        k = rng.integers(0, 700, n, dtype=np.int32)
+        x = rng.normal(100, 25, n)
+        v = rng.integers(-1000, 1000, n, dtype=np.int64)
+        xn = rng.random(n) < 0.1
+        types = [capi.INTEGER, capi.DOUBLE, capi.BIGINT]
+        aggs = [("count_star", -1), ("sum", 2), ("min", 2)]
+        d = _to_device([k, x, v], types)
+        vx = torch.from_numpy(capi.validity_words(~xn).view(np.int64)).cuda()
+        b.add(types, [0], aggs, d, n, validity=[None, vx, None], nullable=[1], filters=[(1, ">", 104.5)],
+              est_groups=700)
+        orc_fast = oracle.run_query(types, [0], aggs, [k, x, v], filters=[(1, ">", 104.5)], nulls=[None, xn, None])
+        # generic path: SUM of a DOUBLE
+        aggs_g = [("count_star", -1), ("sum", 1)]
+        b.add(types, [0], aggs_g, d, n, filters=[(2, "<", 0)], est_groups=700)
+        orc_gen = oracle.run_query(types, [0], aggs_g, [k, x, v], filters=[(2, "<", 0)])
+        torch.cuda.synchronize()
+        b.run()
+        for i, (sh, orc) in enumerate(checks):
+            compare(_gpu(b.result(i), sh), orc)
+        nb = len(checks)
+        compare(gpu_to_dict(b.result(nb), 1, [capi.INTEGER, capi.BIGINT, capi.BIGINT, capi.BIGINT]), orc_fast)
+        compare(gpu_to_dict(b.result(nb + 1), 1, [capi.INTEGER, capi.BIGINT, capi.DOUBLE]), orc_gen)
     finally:
         b.close()
