@@ -52,8 +52,12 @@ def parse():
     ap.add_argument("--rows", type=int, default=100_000_000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=20_000_000)
-    ap.add_argument("--workload", default="zipf100m", choices=["zipf100m", "batch256"])
+    ap.add_argument("--workload", default="zipf100m", choices=["zipf100m", "batch256", "serve"])
     ap.add_argument("--tables", type=int, default=256)
+    ap.add_argument("--duration", type=float, default=20.0, help="serve: seconds of Poisson arrivals")
+    ap.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")
+    ap.add_argument("--scale", type=float, default=1.0, help="serve: resident table scale (1.0 = ~66 GB)")
+    ap.add_argument("--budget-gb", type=float, default=40.0, help="serve: admission budget")
     return ap.parse_args()
 
 
@@ -316,10 +320,222 @@ def run_batch_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _serve_stream(srv, queries, t0_wall):
+    """Submit `queries` at their arrival times (seconds after t0_wall) and
+    wait for all of them; returns (tickets, submit wall times)."""
+    import threading
+    tickets = [None] * len(queries)
+    errors = []
+
+    def submitter():
+        try:
+            for i, q in enumerate(queries):
+                delay = t0_wall + q["at"] - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                tickets[i] = srv.submit(q["table"], q["r0"], q["r1"], q["group_cols"], q["aggs"],
+                                        filters=q["filters"], est_groups=q["est_groups"])
+        except Exception as e:  # surfaced below
+            errors.append(e)
+
+    th = threading.Thread(target=submitter)
+    th.start()
+    th.join()
+    if errors:
+        raise errors[0]
+    for t in tickets:
+        srv.wait(t)
+    return tickets
+
+
+def run_serve(args):
+    """The served query stream: 10 resident tables (~66 GB at --scale 1),
+    Poisson arrivals at --rate q/s for --duration s, each query one of the
+    four GROUP BY shapes over a random row range with WHERE selectivity
+    U[1%, 100%]; admission budget --budget-gb of estimated device bytes.
+    Runs the same stream with continuous batching and one query at a time."""
+    ws, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    from slothdb_gb300 import capi, datagen
+    capi.load(build_if_missing=True)
+    if args.impl == "reference":
+        return run_serve_reference(args)
+    t0 = time.time()
+    tabs, rows_of, res_bytes = [], {}, 0
+    for i, t in enumerate(datagen.SERVE_TABLES):
+        cols, n = datagen.serve_table_device(t, scale=args.scale)
+        tabs.append((datagen.SERVE_TYPES[t["family"]], cols, n))
+        rows_of[i] = n
+        for c in cols:
+            res_bytes += (c[0].numel() * 8 + c[1].numel()) if isinstance(c, tuple) else c.numel() * c.element_size()
+    torch.cuda.synchronize()
+    gen_s = time.time() - t0
+    queries = datagen.serve_queries(args.duration, args.rate, rows_of, seed=4)
+    scanned = 0
+    for q in queries:
+        types, cols, _ = tabs[q["table"]]
+        for c, ty in zip(cols, types):
+            if ty == capi.VARCHAR:  # offsets + string bytes of the range
+                scanned += (q["r1"] - q["r0"]) * 8 + int((c[0][q["r1"]] - c[0][q["r0"]]).item())
+            else:
+                scanned += (q["r1"] - q["r0"]) * c.element_size()
+    out = {}
+    results = {}
+    sample = list(range(0, len(queries), max(1, len(queries) // 24)))
+    for mode, name in [(0, "batched"), (1, "one_at_a_time")]:
+        srv = capi.Server(budget_bytes=int(args.budget_gb * (1 << 30)), max_batch=256, mode=mode)
+        for types, cols, n in tabs:
+            srv.add_table(types, cols, n)
+        # warm-up: a few queries of every shape
+        warm = [q for q in queries[:64]]
+        for q in warm[:16]:
+            t = srv.submit(q["table"], q["r0"], q["r1"], q["group_cols"], q["aggs"], filters=q["filters"],
+                           est_groups=q["est_groups"])
+            srv.wait(t)
+            srv.release(t)
+        st0 = srv.stats()
+        clocks = Clocks(local)
+        clocks.start()
+        w0 = time.perf_counter()
+        tickets = _serve_stream(srv, queries, w0)
+        w1 = time.perf_counter()
+        clk = clocks.stop()
+        lat = []
+        exec_by_shape = {}
+        for i, t in enumerate(tickets):
+            qm, em, bs = srv.times(t)
+            lat.append(qm + em)
+            if mode == 1:
+                exec_by_shape.setdefault(queries[i]["shape"], []).append((em, queries[i]["r1"] - queries[i]["r0"]))
+            if i in sample:
+                results.setdefault(i, []).append(srv.result(t))
+            srv.release(t)
+        st = srv.stats()
+        lat = np.array(lat)
+        out[name] = {"queries_per_s": len(queries) / (w1 - w0), "wall_s": w1 - w0,
+                     "p50_ms": float(np.percentile(lat, 50)), "p95_ms": float(np.percentile(lat, 95)),
+                     "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+                     "batches": st["batches"] - st0["batches"], "busy_ms": st["busy_ms"] - st0["busy_ms"],
+                     "rejected": st["rejected"], "failed": st["failed"],
+                     "peak_admitted_GB": st["peak_admitted_bytes"] / 2**30,
+                     "kernel_launches": st["kernel_launches"] - st0["kernel_launches"], "clocks": clk}
+        if mode == 1:
+            out[name]["per_shape"] = {
+                str(k): {"queries": len(v), "mean_exec_ms": float(np.mean([e for e, _ in v])),
+                         "rows_per_s": float(sum(r for _, r in v) / max(1e-9, sum(e for e, _ in v) / 1e3))}
+                for k, v in sorted(exec_by_shape.items())}
+        srv.close()
+    # per-result identity, mixed (batched) vs alone: integer columns
+    # bit-exact, DOUBLE columns within 1e-12 relative (their sums are
+    # accumulated in a different order on each run)
+    same, worst, why = 0, 0.0, []
+    for i, (rb, ra) in results.items():
+        ok = len(rb[0][0]) == len(ra[0][0])
+        if not ok:
+            why.append("q%d shape %d: %d vs %d groups" % (i, queries[i]["shape"], len(rb[0][0]), len(ra[0][0])))
+        if ok:
+            nk = len(queries[i]["group_cols"])
+            def order(r):
+                return sorted(range(len(r[0][0])), key=lambda j: tuple(
+                    (bool(r[c][1][j]), r[c][0][j] if r[c][1][j] else 0) for c in range(nk)))
+            ob, oa = order(rb), order(ra)
+            for (vb, nb), (va, na) in zip(rb, ra):
+                vb, nb, va, na = vb[ob], nb[ob], va[oa], na[oa]
+                if not np.array_equal(nb, na):
+                    ok = False
+                elif vb.dtype == np.float64:
+                    m = nb
+                    d = np.abs(vb[m] - va[m]) / np.maximum(np.abs(va[m]), 1e-300)
+                    w = float(d.max()) if d.size else 0.0
+                    worst = max(worst, w)
+                    ok = ok and w <= 1e-12
+                else:
+                    ok = ok and bool(np.array_equal(vb[nb], va[na]))
+            if not ok:
+                why.append("q%d shape %d: values differ" % (i, queries[i]["shape"]))
+        same += ok
+    b = out["batched"]
+    line = {"metric": "served GROUP BY queries/s and latency percentiles (Poisson stream, admission budget)",
+            "value": b["queries_per_s"], "unit": "queries/s", "n_gpus": 1, "steps": 1, "warmup": 16,
+            "ms_per_step": b["wall_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic",
+            "config": {"workload": "serve-10-tables", "resident_GB": res_bytes / 1e9, "scale": args.scale,
+                       "queries": len(queries), "rate_qps": args.rate, "duration_s": args.duration,
+                       "budget_GB": args.budget_gb, "scanned_GB": scanned / 1e9,
+                       "shapes": "1M plain / 100M zipf / 200M filtered / 1e4-1e7 composite|varchar",
+                       "datagen_s": round(gen_s, 1)},
+            "p50_ms": b["p50_ms"], "p95_ms": b["p95_ms"], "p99_ms": b["p99_ms"],
+            "batched": b, "one_at_a_time": out["one_at_a_time"],
+            "speedup_vs_one_at_a_time": out["one_at_a_time"]["wall_s"] / b["wall_s"],
+            "identity_alone_vs_mixed": "%d/%d sampled results identical (integers bit-exact, DOUBLE max rel "
+                                        "diff %.1e)" % (same, len(results), worst),
+            "identity_mismatches": why[:6],
+            "gpu_launches": b["kernel_launches"], "clocks": b["clocks"]}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve_reference(args):
+    """The oracle (restatement of the reference's GROUP BY) on a sample of
+    the query mix: the first queries of the stream whose row ranges sum to
+    about 30M rows, host-generated columns of the same families, 1 thread
+    per query (the full stream is infeasible on the CPU)."""
+    import oracle
+    from slothdb_gb300 import datagen
+    rows_of = {i: int(t["rows"] * args.scale) for i, t in enumerate(datagen.SERVE_TABLES)}
+    queries = datagen.serve_queries(args.duration, args.rate, rows_of, seed=4)
+    picked, tot = [], 0
+    for q in queries:
+        n = q["r1"] - q["r0"]
+        if tot + n > 30_000_000:
+            continue
+        picked.append(q)
+        tot += n
+    rng = np.random.default_rng(5)
+
+    def host_cols(q):
+        n = q["r1"] - q["r0"]
+        fam = datagen.SERVE_TABLES[q["table"]]["family"]
+        g = datagen.SERVE_TABLES[q["table"]]["groups"]
+        if fam == "plain":
+            return [rng.integers(0, g, n, dtype=np.int32), rng.integers(0, 10**6, n, dtype=np.int64)]
+        if fam == "zipf":
+            return [rng.integers(0, 2**40, n, dtype=np.int64), rng.normal(100, 25, n)]
+        if fam == "filter":
+            return [rng.integers(0, g, n, dtype=np.int32), rng.integers(0, 1000, n, dtype=np.int16),
+                    rng.integers(-10**9, 10**9, n, dtype=np.int64)]
+        return datagen.batch_table_host(dict(kind=fam, rows=n, groups=g, seed=int(rng.integers(1 << 30))))
+
+    data = [host_cols(q) for q in picked]
+    times = []
+    for i in range(args.warmup + max(1, args.steps)):
+        t = time.perf_counter()
+        for q, cols in zip(picked, data):
+            types = datagen.SERVE_TYPES[datagen.SERVE_TABLES[q["table"]]["family"]]
+            oracle.run_query(types, q["group_cols"], q["aggs"], cols, filters=q["filters"], nthreads=1)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t)
+    per = statistics.mean(times)
+    val = len(picked) / per
+    line = {"impl": "reference", "metric": "served GROUP BY queries/s and latency percentiles (Poisson stream, "
+            "admission budget)", "value": val, "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic",
+            "config": {"workload": "serve-10-tables (bounded sample: %d queries, %d rows)" % (len(picked), tot)},
+            "cpu_baseline": {"value": val, "unit": "queries/s", "cores": 1, "kind": "port",
+                             "sample": "first %d queries of the stream (%d rows), sequential, 1 thread" % (
+                                 len(picked), tot)},
+            "e2e": {"value": val, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "batch256":
         run_batch(args)
+        return
+    if args.workload == "serve":
+        run_serve(args)
         return
     if args.impl == "reference":
         run_reference(args)

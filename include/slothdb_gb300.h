@@ -131,6 +131,18 @@ int gb_abi_version(void);
  * PhysicalPlanner::PlanAggregate (physical_planner.cpp:14356-14362). */
 gb_status gb_agg_create(const gb_agg_spec *spec, gb_agg **out);
 
+/* Device bytes a GROUP BY of `nrows` rows with this spec is expected to hold
+ * (hash table sized from min(est_groups, nrows), result columns, spill
+ * records, string dictionary).  Compiles the plan only; allocates nothing.
+ * Used for admission control; no reference counterpart. */
+gb_status gb_agg_estimate_bytes(const gb_agg_spec *spec, uint64_t nrows, uint64_t *bytes);
+
+/* Replaces the handle's WHERE predicates (same plan otherwise), after create
+ * or reset and before the first ingest — so a pooled handle can serve the
+ * next query of the same shape without reallocating.  No reference
+ * counterpart (the reference builds a new operator per query). */
+gb_status gb_agg_set_filters(gb_agg *h, const gb_filter *filters, uint32_t n_filters);
+
 /* Replaces PhysicalHashAggregate::SetTopNHint (physical_planner.cpp:6022-6027):
  * keep only the best `limit` rows by output column `col_idx` (output slot
  * space; ties broken by group key ascending). */
@@ -261,12 +273,55 @@ gb_status gb_batch_create(gb_batch **out);
 gb_status gb_batch_add(gb_batch *b, const gb_agg_spec *spec, const gb_col *cols, uint64_t nrows, uint32_t *query_index);
 gb_status gb_batch_set_option(gb_batch *b, const char *name, int64_t value);
 gb_status gb_batch_run(gb_batch *b, void *stream);
+/* Removes every query from the batch but keeps its device buffers; the
+ * queries' handles stay in an idle pool and a later gb_batch_add of the same
+ * plan shape and table size reuses one (new filter constants allowed), so a
+ * long-lived batch object allocates nothing in steady state. */
+gb_status gb_batch_clear(gb_batch *b);
 uint32_t gb_batch_size(const gb_batch *b);
 gb_status gb_batch_result(gb_batch *b, uint32_t query_index, gb_result *out);
 uint32_t gb_batch_slow_queries(const gb_batch *b);
 uint64_t gb_batch_kernel_launches(const gb_batch *b);
 uint32_t gb_batch_profile(const gb_batch *b, gb_kernel_stat *out, uint32_t max);
 void gb_batch_destroy(gb_batch *b);
+
+/* ----------------------------------------------------------------- serving
+ * A served stream of GROUP BY queries over tables resident in HBM (no
+ * reference counterpart: the reference plans and runs each query on the
+ * caller's thread, Connection::Query → PhysicalPlanner::PlanAggregate,
+ * physical_planner.cpp:14356-14362).  One dispatcher thread owns the GPU:
+ * queued queries are admitted in arrival order while the sum of their
+ * estimated device bytes (gb_agg_estimate_bytes) stays within
+ * `budget_bytes` (a query whose estimate alone exceeds it fails with
+ * GB_ERR_BUDGET), at most `max_batch` per batch, and run together as one
+ * gb_batch; queries estimated at >= 2^20 groups run alone on their own
+ * handle.  mode 1 runs every query alone, one at a time (the baseline).
+ * Queries that arrive while a batch executes form the next batch.
+ * Tables are registered (device columns, borrowed; validity-masked tables
+ * are sliced at multiples of 64 rows) before the first submit.  A query is
+ * a gb_agg_spec over the table's columns plus a row range.  Results are
+ * host copies owned by the ticket until gb_server_release.  gb_server_wait
+ * returns the query's status (GB_ERR_TIMEOUT if not done within timeout_us;
+ * timeout_us < 0 waits without limit).  gb_server_destroy drains the queue. */
+typedef struct gb_server gb_server;
+typedef struct gb_server_stat {
+    uint64_t batches, completed, rejected, failed, queued;
+    uint64_t peak_admitted_bytes;
+    double busy_ms;
+    uint64_t kernel_launches;
+} gb_server_stat;
+gb_status gb_server_create(uint64_t budget_bytes, uint32_t max_batch, int32_t mode, gb_server **out);
+gb_status gb_server_add_table(gb_server *s, const int32_t *col_types, uint32_t n_cols, const gb_col *cols,
+                              uint64_t nrows, uint32_t *table_id);
+gb_status gb_server_submit(gb_server *s, uint32_t table_id, uint64_t row_begin, uint64_t row_end,
+                           const gb_agg_spec *spec, uint64_t *ticket);
+gb_status gb_server_wait(gb_server *s, uint64_t ticket, int64_t timeout_us);
+gb_status gb_server_result(gb_server *s, uint64_t ticket, gb_result *out);
+gb_status gb_server_query_times(gb_server *s, uint64_t ticket, double *queue_ms, double *exec_ms,
+                                uint32_t *batch_size);
+gb_status gb_server_release(gb_server *s, uint64_t ticket);
+gb_status gb_server_stats(gb_server *s, gb_server_stat *out);
+void gb_server_destroy(gb_server *s);
 
 /* Allocation-free GROUP BY for callers that cannot allocate device memory
  * on their query path (an engine that hands out device memory only from

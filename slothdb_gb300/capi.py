@@ -13,6 +13,8 @@ import numpy as np
 from . import build as _build
 
 GB_OK = 0
+GB_ERR_TIMEOUT = 4
+GB_ERR_BUDGET = 8
 STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "OOM", 3: "UNSUPPORTED", 4: "TIMEOUT", 5: "CUDA", 6: "CORRUPT",
                 7: "STATE", 8: "BUDGET"}
 
@@ -62,6 +64,12 @@ class Result(C.Structure):
                 ("validity", C.POINTER(C.c_void_p))]
 
 
+class ServerStat(C.Structure):
+    _fields_ = [("batches", C.c_uint64), ("completed", C.c_uint64), ("rejected", C.c_uint64),
+                ("failed", C.c_uint64), ("queued", C.c_uint64), ("peak_admitted_bytes", C.c_uint64),
+                ("busy_ms", C.c_double), ("kernel_launches", C.c_uint64)]
+
+
 # every exported symbol of include/slothdb_gb300.h (checked by tests)
 _SIGS = {
     "gb_last_error": (C.c_char_p, []),
@@ -87,12 +95,27 @@ _SIGS = {
                                C.POINTER(C.c_uint32)]),
     "gb_batch_set_option": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
     "gb_batch_run": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gb_batch_clear": (C.c_int, [C.c_void_p]),
     "gb_batch_size": (C.c_uint32, [C.c_void_p]),
     "gb_batch_result": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Result)]),
     "gb_batch_slow_queries": (C.c_uint32, [C.c_void_p]),
     "gb_batch_kernel_launches": (C.c_uint64, [C.c_void_p]),
     "gb_batch_profile": (C.c_uint32, [C.c_void_p, C.POINTER(KernelStat), C.c_uint32]),
     "gb_batch_destroy": (None, [C.c_void_p]),
+    "gb_agg_set_filters": (C.c_int, [C.c_void_p, C.POINTER(Filter), C.c_uint32]),
+    "gb_agg_estimate_bytes": (C.c_int, [C.POINTER(AggSpec), C.c_uint64, C.POINTER(C.c_uint64)]),
+    "gb_server_create": (C.c_int, [C.c_uint64, C.c_uint32, C.c_int32, C.POINTER(C.c_void_p)]),
+    "gb_server_add_table": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_uint32, C.POINTER(Col), C.c_uint64,
+                                      C.POINTER(C.c_uint32)]),
+    "gb_server_submit": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint64, C.c_uint64, C.POINTER(AggSpec),
+                                   C.POINTER(C.c_uint64)]),
+    "gb_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_int64]),
+    "gb_server_result": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(Result)]),
+    "gb_server_query_times": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_uint32)]),
+    "gb_server_release": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "gb_server_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStat)]),
+    "gb_server_destroy": (None, [C.c_void_p]),
     "gb_hash_aggregate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
                                             C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64), C.c_void_p]),
     "gb_pq_open": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_void_p)]),
@@ -285,6 +308,17 @@ class GroupBy:
     def set_option(self, name, value):
         check(self.lib.gb_agg_set_option(self.h, name.encode(), int(value)))
 
+    def set_filters(self, filters):
+        """Replace the WHERE predicates (after create or reset)."""
+        fl = (Filter * max(1, len(filters)))()
+        for i, (col, op, const) in enumerate(filters):
+            opc = CMP_NAMES[op] if isinstance(op, str) else int(op)
+            if self.col_types[col] == DOUBLE:
+                fl[i] = Filter(col, opc, 0, float(const))
+            else:
+                fl[i] = Filter(col, opc, int(const), 0.0)
+        check(self.lib.gb_agg_set_filters(self.h, fl, len(filters)))
+
     def mode(self):
         return int(self.lib.gb_agg_get_mode(self.h))
 
@@ -356,6 +390,10 @@ class Batch:
     def run(self, stream=None):
         check(self.lib.gb_batch_run(self.h, C.c_void_p(stream) if stream else None))
 
+    def clear(self):
+        check(self.lib.gb_batch_clear(self.h))
+        self._keep = []
+
     def __len__(self):
         return int(self.lib.gb_batch_size(self.h))
 
@@ -379,6 +417,87 @@ class Batch:
     def close(self):
         if getattr(self, "h", None):
             self.lib.gb_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def estimate_bytes(col_types, group_cols, aggs, nrows, filters=(), nullable=(), est_groups=0):
+    """Device bytes a GROUP BY of nrows rows is expected to hold."""
+    spec, keep = _make_spec(col_types, group_cols, aggs, filters, nullable, est_groups)
+    out = C.c_uint64()
+    check(load().gb_agg_estimate_bytes(C.byref(spec), int(nrows), C.byref(out)))
+    return int(out.value)
+
+
+class Server:
+    """A served query stream over HBM-resident tables (gb_server).  mode 0 =
+    continuous batching, 1 = one query at a time."""
+
+    def __init__(self, budget_bytes, max_batch=256, mode=0):
+        self.lib = load()
+        h = C.c_void_p()
+        check(self.lib.gb_server_create(int(budget_bytes), int(max_batch), int(mode), C.byref(h)))
+        self.h = h
+        self._keep = []
+        self.tables = []
+
+    def add_table(self, col_types, cols, nrows, validity=None):
+        """cols: torch CUDA tensors / device pointers (VARCHAR: (offsets, bytes))."""
+        arr = (Col * len(col_types))()
+        for i, a in enumerate(cols):
+            offs = None
+            if col_types[i] == VARCHAR:
+                offs, a = a
+            v = validity[i] if validity is not None else None
+            arr[i] = Col(_arr_ptr(a), _arr_ptr(v), _arr_ptr(offs))
+        ct = (C.c_int32 * len(col_types))(*col_types)
+        tid = C.c_uint32()
+        check(self.lib.gb_server_add_table(self.h, ct, len(col_types), arr, int(nrows), C.byref(tid)))
+        self._keep.append((cols, validity))
+        self.tables.append(list(col_types))
+        return int(tid.value)
+
+    def submit(self, table, row_begin, row_end, group_cols, aggs, filters=(), nullable=(), est_groups=0):
+        spec, keep = _make_spec(self.tables[table], group_cols, aggs, filters, nullable, est_groups)
+        t = C.c_uint64()
+        check(self.lib.gb_server_submit(self.h, int(table), int(row_begin), int(row_end), C.byref(spec),
+                                        C.byref(t)))
+        return int(t.value)
+
+    def wait(self, ticket, timeout_us=-1):
+        """True when done (raises on a failed query), False on timeout."""
+        st = self.lib.gb_server_wait(self.h, int(ticket), int(timeout_us))
+        if st == GB_ERR_TIMEOUT:
+            return False
+        check(st)
+        return True
+
+    def result(self, ticket):
+        r = Result()
+        check(self.lib.gb_server_result(self.h, int(ticket), C.byref(r)))
+        return _read_result(r)
+
+    def times(self, ticket):
+        qm, em, bs = C.c_double(), C.c_double(), C.c_uint32()
+        check(self.lib.gb_server_query_times(self.h, int(ticket), C.byref(qm), C.byref(em), C.byref(bs)))
+        return float(qm.value), float(em.value), int(bs.value)
+
+    def release(self, ticket):
+        check(self.lib.gb_server_release(self.h, int(ticket)))
+
+    def stats(self):
+        st = ServerStat()
+        check(self.lib.gb_server_stats(self.h, C.byref(st)))
+        return {f: getattr(st, f) for f, _ in ServerStat._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.gb_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "gb_agg_host.h"
@@ -1116,6 +1117,29 @@ static gb_status strdict_emit(gb_agg *h, const long long *ids, u64 n, cudaStream
 }
 
 // ---------------------------------------------------------------- compile
+// The plan's predicates from h->filters (validated).
+static gb_status compile_filters(gb_agg *h) {
+    Plan &P = h->plan;
+    const int nc = (int)h->col_types.size();
+    for (size_t i = 0; i < h->filters.size(); i++) {
+        const gb_filter &f = h->filters[i];
+        if (f.col < 0 || f.col >= nc || f.op < 0 || f.op > 5 || h->col_types[f.col] == GB_T_VARCHAR) {
+            set_error("filter %zu invalid (column, operator or VARCHAR predicate)", i);
+            return GB_ERR_INVALID;
+        }
+        if (i >= GB_MAX_FILTERS) {
+            set_error("too many filters (max %d)", GB_MAX_FILTERS);
+            return GB_ERR_UNSUPPORTED;
+        }
+        P.filters[i].col = f.col;
+        P.filters[i].op = f.op;
+        P.filters[i].ic = f.i_const;
+        P.filters[i].dc = f.d_const;
+    }
+    P.n_filters = (int)h->filters.size();
+    return GB_OK;
+}
+
 static gb_status compile_plan(gb_agg *h) {
     Plan &P = h->plan;
     memset(&P, 0, sizeof P);
@@ -1183,22 +1207,7 @@ static gb_status compile_plan(gb_agg *h) {
             return GB_ERR_UNSUPPORTED;
         }
     }
-    for (size_t i = 0; i < h->filters.size(); i++) {
-        const gb_filter &f = h->filters[i];
-        if (f.col < 0 || f.col >= nc || f.op < 0 || f.op > 5 || h->col_types[f.col] == GB_T_VARCHAR) {
-            set_error("filter %zu invalid (column, operator or VARCHAR predicate)", i);
-            return GB_ERR_INVALID;
-        }
-        if (i >= GB_MAX_FILTERS) {
-            set_error("too many filters (max %d)", GB_MAX_FILTERS);
-            return GB_ERR_UNSUPPORTED;
-        }
-        P.filters[i].col = f.col;
-        P.filters[i].op = f.op;
-        P.filters[i].ic = f.i_const;
-        P.filters[i].dc = f.d_const;
-    }
-    P.n_filters = (int)h->filters.size();
+    if (gb_status fs = compile_filters(h)) return fs;
 
     // state words: 0 = row count; ops deduplicated per (kind, column)
     int words = 1;
@@ -1390,6 +1399,47 @@ extern "C" {
 const char *gb_last_error(void) { return g_err.c_str(); }
 int gb_abi_version(void) { return GB_ABI_VERSION; }
 
+gb_status gb_agg_estimate_bytes(const gb_agg_spec *spec, uint64_t nrows, uint64_t *bytes) {
+    if (!spec || !bytes || spec->n_cols == 0 || !spec->col_types || spec->n_groups == 0 || !spec->group_cols ||
+        spec->n_aggs == 0 || !spec->aggs || (spec->n_filters && !spec->filters)) {
+        set_error("incomplete spec");
+        return GB_ERR_INVALID;
+    }
+    gb_agg h;  // plan only: nothing is allocated on the device
+    h.col_types.assign(spec->col_types, spec->col_types + spec->n_cols);
+    h.group_cols.assign(spec->group_cols, spec->group_cols + spec->n_groups);
+    h.aggs.assign(spec->aggs, spec->aggs + spec->n_aggs);
+    if (spec->n_filters) h.filters.assign(spec->filters, spec->filters + spec->n_filters);
+    h.nullable_mask = spec->nullable_mask;
+    gb_status s = compile_plan(&h);
+    if (s) return s;
+    const u64 est = std::max<u64>(1, std::min<u64>(spec->est_groups ? spec->est_groups : (1u << 15),
+                                                   std::max<u64>(nrows, 1)));
+    const u64 cap = std::max<u64>(1024, next_pow2(est * 2));
+    u64 b = (cap + 2) * (u64)h.plan.stride * 8;                        // hash table
+    for (int t : h.out_types) b += (cap + 2) * (u64)(t == GB_T_VARCHAR ? 8 : type_size(t)) + (cap + 2) / 8;
+    b += (u64)((1u << 16) + 4096) * (1 + h.plan.words) * 8;            // spill records
+    if (h.str_col >= 0) b += 4 * 2 * cap * 8 + 40 * est + 16 * est;    // dictionary, arena, emitted strings
+    *bytes = b;
+    return GB_OK;
+}
+
+gb_status gb_agg_set_filters(gb_agg *h, const gb_filter *filters, uint32_t n_filters) {
+    if (!h || (n_filters && !filters)) return GB_ERR_INVALID;
+    if (h->rows_ingested || h->finalized) {
+        set_error("filters are replaced after create or reset, before the first ingest");
+        return GB_ERR_STATE;
+    }
+    std::vector<gb_filter> old = h->filters;
+    h->filters.assign(filters, filters + n_filters);
+    if (gb_status s = compile_filters(h)) {
+        h->filters = old;
+        compile_filters(h);
+        return s;
+    }
+    return GB_OK;
+}
+
 gb_status gb_agg_create(const gb_agg_spec *spec, gb_agg **out) {
     if (!spec || !out) {
         set_error("null spec/out");
@@ -1428,6 +1478,13 @@ gb_status gb_agg_create(const gb_agg_spec *spec, gb_agg **out) {
     if ((s = init_table(h, h->table, h->cap, 0))) {
         delete h;
         return s;
+    }
+    // the table is initialised on the legacy stream: finish before the caller
+    // ingests on a stream that does not synchronise with it
+    e = cudaStreamSynchronize(0);
+    if (e != cudaSuccess) {
+        delete h;
+        return cuda_fail(e, "cudaStreamSynchronize");
     }
     *out = h;
     return GB_OK;
@@ -1715,6 +1772,7 @@ gb_status gb_agg_reset(gb_agg *h) {
     gb_status s = init_table(h, h->table, h->cap, 0);
     if (s) return s;
     GB_CUDA(cudaMemset(h->ctl_buf.p, 0, sizeof(Ctl)));
+    GB_CUDA(cudaStreamSynchronize(0));  // before ingests on streams that do not synchronise with it
     h->n_groups = 0;
     h->sd_cap = 0;  // the string dictionary is rebuilt by the next ingest
     h->r_ready = false;

@@ -623,6 +623,7 @@ struct gb_batch {
     } prof[4] = {{"k_batch_init"}, {"k_batch_strdict"}, {"k_batch_ingest"}, {"k_batch_compact"}};
     u64 launches = 0;
     std::vector<int> slow;  // queries re-run on their handle in the last run
+    std::unordered_multimap<std::string, gb_agg *> pool;  // idle handles kept by gb_batch_clear
 };
 
 // The fast-path description of a query's plan (eligible = 0 when the plan
@@ -901,7 +902,73 @@ static gb_status batch_enqueue(gb_batch *b, cudaStream_t st) {
     return GB_OK;
 }
 
+static gb_status cuda_sync_legacy() {
+    GB_CUDA(cudaStreamSynchronize(0));
+    return GB_OK;
+}
+
+// Pool key of a handle: its plan shape (without the filter constants) and
+// the table capacity its estimate gives.
+static std::string batch_pool_key(const gb_agg_spec &sp) {
+    std::string k;
+    auto put = [&](const void *p, size_t n) { k.append((const char *)p, n); };
+    put(&sp.n_cols, 4);
+    put(sp.col_types, 4 * sp.n_cols);
+    put(&sp.n_groups, 4);
+    put(sp.group_cols, 4 * sp.n_groups);
+    put(&sp.n_aggs, 4);
+    put(sp.aggs, sizeof(gb_agg_desc) * sp.n_aggs);
+    put(&sp.n_filters, 4);
+    for (uint32_t i = 0; i < sp.n_filters; i++) {
+        put(&sp.filters[i].col, 4);
+        put(&sp.filters[i].op, 4);
+    }
+    put(&sp.nullable_mask, 8);
+    const u64 cap = std::max<u64>(1024, next_pow2(sp.est_groups * 2));
+    put(&cap, 8);
+    return k;
+}
+
+static std::string batch_pool_key(const gb_agg *h) {
+    gb_agg_spec sp{};
+    sp.n_cols = (uint32_t)h->col_types.size();
+    sp.col_types = h->col_types.data();
+    sp.n_groups = (uint32_t)h->group_cols.size();
+    sp.group_cols = h->group_cols.data();
+    sp.n_aggs = (uint32_t)h->aggs.size();
+    sp.aggs = h->aggs.data();
+    sp.n_filters = (uint32_t)h->filters.size();
+    sp.filters = h->filters.data();
+    sp.nullable_mask = h->nullable_mask;
+    sp.est_groups = h->cap / 2;
+    return batch_pool_key(sp);
+}
+
+constexpr size_t BATCH_POOL_MAX = 4096;
+
 extern "C" {
+
+gb_status gb_batch_clear(gb_batch *b) {
+    if (!b) return GB_ERR_INVALID;
+    cudaDeviceSynchronize();
+    for (auto *h : b->handles) {
+        if (b->pool.size() >= BATCH_POOL_MAX) {
+            gb_agg_destroy(h);
+            continue;
+        }
+        b->pool.emplace(batch_pool_key(h), h);
+    }
+    b->handles.clear();
+    b->cols.clear();
+    b->rows.clear();
+    b->slow.clear();
+    b->prepared = false;
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+    return GB_OK;
+}
 
 gb_status gb_batch_create(gb_batch **out) {
     if (!out) return GB_ERR_INVALID;
@@ -916,13 +983,38 @@ gb_status gb_batch_add(gb_batch *b, const gb_agg_spec *spec, const gb_col *cols,
     const u64 est = sp.est_groups ? sp.est_groups : (1u << 15);
     sp.est_groups = std::max<u64>(1, std::min<u64>(est, nrows));
     gb_agg *h = nullptr;
-    gb_status s = gb_agg_create(&sp, &h);
-    if (s) return s;
+    gb_status s;
+    const std::string key = batch_pool_key(sp);
+    auto it = b->pool.find(key);
+    if (it != b->pool.end()) {
+        // an idle handle of the same plan shape and table size: rebind it
+        h = it->second;
+        b->pool.erase(it);
+        h->filters.assign(sp.filters, sp.filters + sp.n_filters);
+        if ((s = compile_filters(h))) {
+            gb_agg_destroy(h);
+            return s;
+        }
+        h->est_groups = sp.est_groups;
+        h->finalized = h->has_result = h->topn_applied = false;
+        h->rows_ingested = h->n_groups = h->n_rows_out = h->launches = 0;
+        b->handles.push_back(h);
+        b->cols.emplace_back(cols, cols + spec->n_cols);
+        b->rows.push_back(nrows);
+        b->prepared = false;
+        if (b->exec) {
+            cudaGraphExecDestroy(b->exec);
+            b->exec = nullptr;
+        }
+        if (qidx) *qidx = (uint32_t)(b->handles.size() - 1);
+        return GB_OK;
+    }
+    if ((s = gb_agg_create(&sp, &h))) return s;
     if (h->mode == 1) {  // the batch runs the hash pipeline for every query
         h->mode = 0;
         u64 est = h->est_groups ? h->est_groups : (1u << 15);
         h->cap = std::max<u64>(1024, next_pow2(est * 2));
-        if ((s = init_table(h, h->table, h->cap, 0))) {
+        if ((s = init_table(h, h->table, h->cap, 0)) || (s = cuda_sync_legacy())) {
             gb_agg_destroy(h);
             return s;
         }
@@ -1074,6 +1166,7 @@ void gb_batch_destroy(gb_batch *b) {
         if (p.b) cudaEventDestroy(p.b);
     }
     for (auto *h : b->handles) gb_agg_destroy(h);
+    for (auto &e : b->pool) gb_agg_destroy(e.second);
     for (DevBuf *d : {&b->qdesc, &b->items_init, &b->items_str, &b->items_ingest, &b->items_compact, &b->bctl, &b->qctl})
         d->release();
     b->qctl_host.release();

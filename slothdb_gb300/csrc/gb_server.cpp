@@ -1,0 +1,545 @@
+// gb_server.cpp — a served stream of GROUP BY queries over tables resident
+// in HBM.
+//
+// The reference has no server: each query is one Connection::Query call
+// that plans and runs its own PhysicalHashAggregate (physical_planner.cpp:
+// 14356-14362) on the caller's thread.  Here one dispatcher thread owns the
+// GPU and executes the queued queries with continuous batching:
+//
+//   submit   (any thread) appends a query (table, row range, plan) to a FIFO
+//            queue and returns a ticket;
+//   dispatch the dispatcher takes queued queries in arrival order while the
+//            sum of their estimated device bytes (gb_agg_estimate_bytes)
+//            stays within the admission budget and the batch holds at most
+//            max_batch queries; a query whose estimate alone exceeds the
+//            budget is rejected with GB_ERR_BUDGET;
+//   execute  the admitted queries run as one gb_batch (one pass of a few
+//            persistent kernels), except high-cardinality queries (estimated
+//            groups >= 2^20), which run one by one on their own handle (the
+//            radix path); in mode 1 every query runs alone on its own handle
+//            (the one-at-a-time baseline);
+//   complete results are copied to host memory owned by the ticket, the
+//            ticket records queue / execution times, and waiters wake up.
+//
+// Queries that arrive while a batch executes form the next batch.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/slothdb_gb300.h"
+
+namespace gb {
+void set_error(const char *fmt, ...);  // the library's thread-local error message
+}
+
+namespace {
+
+using gb::set_error;
+typedef unsigned long long u64;
+
+constexpr u64 RADIX_GROUPS = 1ull << 20;
+
+u64 now_ns() {
+    return (u64)std::chrono::duration_cast<std::chrono::nanoseconds>(
+               std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+int type_bytes(int t) {
+    switch (t) {
+    case GB_T_SMALLINT: return 2;
+    case GB_T_INTEGER: return 4;
+    default: return 8;
+    }
+}
+
+struct Table {
+    std::vector<int32_t> types;
+    std::vector<gb_col> cols;
+    u64 nrows = 0;
+};
+
+// A host copy of one result.
+struct HostResult {
+    u64 n_rows = 0;
+    std::vector<int32_t> types;
+    std::vector<std::vector<uint8_t>> data;
+    std::vector<std::vector<uint64_t>> valid;
+    std::vector<std::vector<int64_t>> offs;
+    std::vector<const void *> data_p;
+    std::vector<const int64_t *> offs_p;
+    std::vector<const uint64_t *> valid_p;
+};
+
+struct Query {
+    u64 ticket = 0;
+    uint32_t table = 0;
+    u64 r0 = 0, r1 = 0;
+    std::vector<int32_t> col_types, group_cols;
+    std::vector<gb_agg_desc> aggs;
+    std::vector<gb_filter> filters;
+    u64 nullable_mask = 0, est_groups = 0;
+    u64 est_bytes = 0;
+    bool done = false;
+    gb_status status = GB_OK;
+    std::string error;
+    HostResult res;
+    u64 t_submit = 0, t_start = 0, t_done = 0;
+    uint32_t batch_size = 0;
+
+    gb_agg_spec spec() const {
+        gb_agg_spec s{};
+        s.n_cols = (uint32_t)col_types.size();
+        s.col_types = col_types.data();
+        s.n_groups = (uint32_t)group_cols.size();
+        s.group_cols = group_cols.data();
+        s.n_aggs = (uint32_t)aggs.size();
+        s.aggs = aggs.data();
+        s.n_filters = (uint32_t)filters.size();
+        s.filters = filters.empty() ? nullptr : filters.data();
+        s.nullable_mask = nullable_mask;
+        s.est_groups = est_groups;
+        return s;
+    }
+};
+
+
+void copy_result(const gb_result &r, HostResult &out) {
+    const u64 n = r.n_rows;
+    out.n_rows = n;
+    out.types.assign(r.types, r.types + r.n_cols);
+    out.data.assign(r.n_cols, {});
+    out.valid.assign(r.n_cols, {});
+    out.offs.assign(r.n_cols, {});
+    for (uint32_t c = 0; c < r.n_cols; c++) {
+        const u64 vw = (n + 63) / 64;
+        if (r.validity && r.validity[c]) out.valid[c].assign(r.validity[c], r.validity[c] + vw);
+        else out.valid[c].assign(vw, ~0ull);
+        if (r.types[c] == GB_T_VARCHAR) {
+            out.offs[c].assign(r.offsets[c], r.offsets[c] + n + 1);
+            const int64_t nb = out.offs[c][n] - out.offs[c][0];
+            const uint8_t *p = (const uint8_t *)r.data[c] + out.offs[c][0];
+            out.data[c].assign(p, p + nb);
+            for (auto &o : out.offs[c]) o -= r.offsets[c][0];
+        } else {
+            const uint8_t *p = (const uint8_t *)r.data[c];
+            out.data[c].assign(p, p + n * (u64)type_bytes(r.types[c]));
+        }
+    }
+    out.data_p.resize(r.n_cols);
+    out.offs_p.resize(r.n_cols);
+    out.valid_p.resize(r.n_cols);
+    for (uint32_t c = 0; c < r.n_cols; c++) {
+        out.data_p[c] = out.data[c].data();
+        out.offs_p[c] = out.types[c] == GB_T_VARCHAR ? out.offs[c].data() : nullptr;
+        out.valid_p[c] = out.valid[c].data();
+    }
+}
+
+}  // namespace
+
+struct gb_server {
+    u64 budget = 0;
+    uint32_t max_batch = 256;
+    int mode = 0;  // 0 continuous batching, 1 one at a time
+    std::vector<Table> tables;
+    std::deque<Query *> queue;
+    std::unordered_map<u64, std::unique_ptr<Query>> all;
+    u64 next_ticket = 1;
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::thread worker;
+    bool stopping = false;
+    bool started = false;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    gb_batch *batch = nullptr;                              // reused: gb_batch_clear keeps its handles pooled
+    std::unordered_multimap<std::string, gb_agg *> alone;   // idle handles of queries run alone, by plan shape
+    std::deque<std::string> alone_order;
+    // statistics
+    u64 n_batches = 0, n_done = 0, n_rejected = 0, n_failed = 0, peak_admitted = 0, busy_ns = 0, launches = 0;
+};
+
+namespace {
+
+// The columns of rows [r0, r1) of a table (validity slices start at a
+// multiple of 64 rows; checked at submit).
+std::vector<gb_col> slice_cols(const Table &t, u64 r0) {
+    std::vector<gb_col> c(t.cols.size());
+    for (size_t i = 0; i < t.cols.size(); i++) {
+        const gb_col &s = t.cols[i];
+        c[i] = s;
+        if (t.types[i] == GB_T_VARCHAR) {
+            c[i].offsets = s.offsets + r0;  // offsets index the column's whole byte buffer
+        } else {
+            c[i].data = (const uint8_t *)s.data + r0 * (u64)type_bytes(t.types[i]);
+        }
+        if (s.validity) c[i].validity = s.validity + r0 / 64;
+    }
+    return c;
+}
+
+void finish(Query *q, gb_status st, const char *msg) {
+    q->status = st;
+    if (st != GB_OK) q->error = msg ? msg : "";
+}
+
+// Pool key of a query run alone: plan shape without filter constants, and
+// the estimate's power-of-two bucket.
+std::string alone_key(const Query *q) {
+    std::string k;
+    auto put = [&](const void *p, size_t n) { k.append((const char *)p, n); };
+    put(q->col_types.data(), 4 * q->col_types.size());
+    k.push_back('|');
+    put(q->group_cols.data(), 4 * q->group_cols.size());
+    k.push_back('|');
+    put(q->aggs.data(), sizeof(gb_agg_desc) * q->aggs.size());
+    k.push_back('|');
+    for (const gb_filter &f : q->filters) {
+        put(&f.col, 4);
+        put(&f.op, 4);
+    }
+    put(&q->nullable_mask, 8);
+    u64 b = 1;
+    while (b < q->est_groups) b <<= 1;
+    put(&b, 8);
+    return k;
+}
+
+constexpr size_t ALONE_POOL_MAX = 8;  // idle lone handles kept (a radix handle holds GBs)
+
+// One query on its own handle (the radix path for high-cardinality keys,
+// and every query in one-at-a-time mode).  Handles are pooled by plan shape
+// and reused with new predicates (gb_agg_reset + gb_agg_set_filters).
+void run_alone(gb_server *s, Query *q) {
+    const gb_agg_spec sp = q->spec();
+    gb_agg *h = nullptr;
+    gb_status st = GB_OK;
+    const std::string key = alone_key(q);
+    auto it = s->alone.find(key);
+    if (it != s->alone.end()) {
+        h = it->second;
+        s->alone.erase(it);
+        st = gb_agg_reset(h);
+        if (st == GB_OK) st = gb_agg_set_filters(h, sp.filters, sp.n_filters);
+    } else {
+        st = gb_agg_create(&sp, &h);
+    }
+    if (st == GB_OK) {
+        std::vector<gb_col> cols = slice_cols(s->tables[q->table], q->r0);
+        st = gb_agg_ingest(h, cols.data(), q->r1 - q->r0, GB_MEM_DEVICE, s->stream);
+        if (st == GB_OK) st = gb_agg_finalize(h, s->stream);
+        gb_result r{};
+        if (st == GB_OK) st = gb_agg_result(h, &r);
+        if (st == GB_OK) copy_result(r, q->res);
+        s->launches += gb_agg_kernel_launches(h);
+    }
+    finish(q, st, st ? gb_last_error() : nullptr);
+    if (!h) return;
+    if (st != GB_OK) {
+        gb_agg_destroy(h);
+        return;
+    }
+    s->alone.emplace(key, h);
+    s->alone_order.push_back(key);
+    while (s->alone.size() > ALONE_POOL_MAX && !s->alone_order.empty()) {
+        auto e = s->alone.find(s->alone_order.front());
+        s->alone_order.pop_front();
+        if (e != s->alone.end()) {
+            gb_agg_destroy(e->second);
+            s->alone.erase(e);
+        }
+    }
+}
+
+void run_batch(gb_server *s, std::vector<Query *> &qs) {
+    gb_status st = GB_OK;
+    if (!s->batch) {
+        st = gb_batch_create(&s->batch);
+        if (st == GB_OK) gb_batch_set_option(s->batch, "graph", 0);  // one-off batches: capture costs more
+    } else {
+        st = gb_batch_clear(s->batch);
+    }
+    if (st) {
+        for (Query *q : qs) finish(q, st, gb_last_error());
+        return;
+    }
+    gb_batch *b = s->batch;
+    std::vector<Query *> in;
+    for (Query *q : qs) {
+        const gb_agg_spec sp = q->spec();
+        std::vector<gb_col> cols = slice_cols(s->tables[q->table], q->r0);
+        uint32_t idx = 0;
+        gb_status a = gb_batch_add(b, &sp, cols.data(), q->r1 - q->r0, &idx);
+        if (a) finish(q, a, gb_last_error());
+        else in.push_back(q);
+    }
+    if (!in.empty()) {
+        const u64 l0 = gb_batch_kernel_launches(b);
+        st = gb_batch_run(b, s->stream);
+        for (size_t i = 0; i < in.size(); i++) {
+            gb_result r{};
+            gb_status rs = st ? st : gb_batch_result(b, (uint32_t)i, &r);
+            if (rs == GB_OK) copy_result(r, in[i]->res);
+            finish(in[i], rs, rs ? gb_last_error() : nullptr);
+        }
+        s->launches += gb_batch_kernel_launches(b) - l0;
+    }
+}
+
+void dispatcher(gb_server *s) {
+    cudaSetDevice(s->device);
+    for (;;) {
+        std::vector<Query *> take;
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            s->cv_work.wait(lk, [&] { return s->stopping || !s->queue.empty(); });
+            if (s->queue.empty()) break;  // stopping and drained
+            u64 sum = 0;
+            while (!s->queue.empty() && take.size() < s->max_batch) {
+                Query *q = s->queue.front();
+                if (q->est_bytes > s->budget) {
+                    s->queue.pop_front();
+                    finish(q, GB_ERR_BUDGET, "estimated device bytes exceed the admission budget");
+                    q->t_start = q->t_done = now_ns();
+                    q->done = true;
+                    s->n_rejected++;
+                    continue;
+                }
+                if (sum + q->est_bytes > s->budget) break;
+                s->queue.pop_front();
+                take.push_back(q);
+                sum += q->est_bytes;
+            }
+            s->peak_admitted = std::max(s->peak_admitted, sum);
+            s->cv_done.notify_all();
+        }
+        if (take.empty()) continue;
+        const u64 t0 = now_ns();
+        // a query's start / done times: its batch's, or its own when it runs alone
+        auto complete = [&](std::vector<Query *> &qs, u64 ts, u64 td) {
+            std::lock_guard<std::mutex> lk(s->mu);
+            for (Query *q : qs) {
+                q->t_start = ts;
+                q->t_done = td;
+                q->done = true;
+                if (q->status) s->n_failed++;
+                s->n_done++;
+            }
+        };
+        std::vector<Query *> big, small;
+        for (Query *q : take) (s->mode == 1 || q->est_groups >= RADIX_GROUPS ? big : small).push_back(q);
+        if (!small.empty()) {
+            for (Query *q : small) q->batch_size = (uint32_t)small.size();
+            run_batch(s, small);
+            complete(small, t0, now_ns());
+            s->cv_done.notify_all();
+        }
+        for (Query *q : big) {
+            std::vector<Query *> one{q};
+            q->batch_size = 1;
+            const u64 ts = now_ns();
+            run_alone(s, q);
+            complete(one, ts, now_ns());
+            s->cv_done.notify_all();
+        }
+        const u64 t1 = now_ns();
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->n_batches++;
+            s->busy_ns += t1 - t0;
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+gb_status gb_server_create(uint64_t budget_bytes, uint32_t max_batch, int32_t mode, gb_server **out) {
+    if (!out || budget_bytes == 0 || max_batch == 0 || (mode != 0 && mode != 1)) {
+        set_error("invalid server arguments");
+        return GB_ERR_INVALID;
+    }
+    gb_server *s = new gb_server();
+    s->budget = budget_bytes;
+    s->max_batch = max_batch;
+    s->mode = mode;
+    cudaGetDevice(&s->device);
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete s;
+        set_error("cudaStreamCreate failed");
+        return GB_ERR_CUDA;
+    }
+    *out = s;
+    return GB_OK;
+}
+
+gb_status gb_server_add_table(gb_server *s, const int32_t *col_types, uint32_t n_cols, const gb_col *cols,
+                              uint64_t nrows, uint32_t *table_id) {
+    if (!s || !col_types || !cols || n_cols == 0 || !table_id) return GB_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->started) {
+        set_error("tables are registered before the first query");
+        return GB_ERR_STATE;
+    }
+    Table t;
+    t.types.assign(col_types, col_types + n_cols);
+    t.cols.assign(cols, cols + n_cols);
+    t.nrows = nrows;
+    s->tables.push_back(t);
+    *table_id = (uint32_t)(s->tables.size() - 1);
+    return GB_OK;
+}
+
+gb_status gb_server_submit(gb_server *s, uint32_t table_id, uint64_t row_begin, uint64_t row_end,
+                           const gb_agg_spec *spec, uint64_t *ticket) {
+    if (!s || !spec || !ticket) return GB_ERR_INVALID;
+    if (table_id >= s->tables.size()) {
+        set_error("unknown table %u", table_id);
+        return GB_ERR_INVALID;
+    }
+    const Table &t = s->tables[table_id];
+    if (row_begin > row_end || row_end > t.nrows) {
+        set_error("row range [%llu, %llu) outside the table", (u64)row_begin, (u64)row_end);
+        return GB_ERR_INVALID;
+    }
+    if (spec->n_cols != t.types.size() || memcmp(spec->col_types, t.types.data(), 4 * t.types.size()) != 0) {
+        set_error("spec columns do not match the table's");
+        return GB_ERR_INVALID;
+    }
+    bool has_valid = false;
+    for (const gb_col &c : t.cols) has_valid |= c.validity != nullptr;
+    if (has_valid && (row_begin % 64) != 0) {
+        set_error("a table with validity masks is sliced at multiples of 64 rows");
+        return GB_ERR_INVALID;
+    }
+    auto q = std::make_unique<Query>();
+    q->table = table_id;
+    q->r0 = row_begin;
+    q->r1 = row_end;
+    q->col_types.assign(spec->col_types, spec->col_types + spec->n_cols);
+    q->group_cols.assign(spec->group_cols, spec->group_cols + spec->n_groups);
+    q->aggs.assign(spec->aggs, spec->aggs + spec->n_aggs);
+    if (spec->n_filters) q->filters.assign(spec->filters, spec->filters + spec->n_filters);
+    q->nullable_mask = spec->nullable_mask;
+    q->est_groups = spec->est_groups;
+    const gb_agg_spec sp = q->spec();
+    uint64_t bytes = 0;
+    gb_status st = gb_agg_estimate_bytes(&sp, row_end - row_begin, &bytes);
+    if (st) return st;  // an invalid plan is reported at submit
+    q->est_bytes = bytes;
+    q->t_submit = now_ns();
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->stopping) return GB_ERR_STATE;
+    q->ticket = s->next_ticket++;
+    *ticket = q->ticket;
+    s->queue.push_back(q.get());
+    s->all[q->ticket] = std::move(q);
+    if (!s->started) {
+        s->started = true;
+        s->worker = std::thread(dispatcher, s);
+    }
+    s->cv_work.notify_one();
+    return GB_OK;
+}
+
+gb_status gb_server_wait(gb_server *s, uint64_t ticket, int64_t timeout_us) {
+    if (!s) return GB_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->all.find(ticket);
+    if (it == s->all.end()) return GB_ERR_INVALID;
+    Query *q = it->second.get();
+    auto pred = [&] { return q->done; };
+    if (timeout_us < 0) s->cv_done.wait(lk, pred);
+    else if (!s->cv_done.wait_for(lk, std::chrono::microseconds(timeout_us), pred)) return GB_ERR_TIMEOUT;
+    if (q->status) set_error("%s", q->error.c_str());
+    return q->status;
+}
+
+gb_status gb_server_result(gb_server *s, uint64_t ticket, gb_result *out) {
+    if (!s || !out) return GB_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(ticket);
+    if (it == s->all.end()) return GB_ERR_INVALID;
+    Query *q = it->second.get();
+    if (!q->done) return GB_ERR_STATE;
+    if (q->status) {
+        set_error("%s", q->error.c_str());
+        return q->status;
+    }
+    HostResult &r = q->res;
+    out->n_rows = r.n_rows;
+    out->n_cols = (uint32_t)r.types.size();
+    out->types = r.types.data();
+    out->data = r.data_p.data();
+    out->offsets = r.offs_p.data();
+    out->validity = r.valid_p.data();
+    return GB_OK;
+}
+
+gb_status gb_server_query_times(gb_server *s, uint64_t ticket, double *queue_ms, double *exec_ms,
+                                uint32_t *batch_size) {
+    if (!s) return GB_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(ticket);
+    if (it == s->all.end()) return GB_ERR_INVALID;
+    Query *q = it->second.get();
+    if (!q->done) return GB_ERR_STATE;
+    if (queue_ms) *queue_ms = (double)(q->t_start - q->t_submit) / 1e6;
+    if (exec_ms) *exec_ms = (double)(q->t_done - q->t_start) / 1e6;
+    if (batch_size) *batch_size = q->batch_size;
+    return GB_OK;
+}
+
+gb_status gb_server_release(gb_server *s, uint64_t ticket) {
+    if (!s) return GB_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->all.find(ticket);
+    if (it == s->all.end()) return GB_ERR_INVALID;
+    if (!it->second->done) return GB_ERR_STATE;
+    s->all.erase(it);
+    return GB_OK;
+}
+
+gb_status gb_server_stats(gb_server *s, gb_server_stat *out) {
+    if (!s || !out) return GB_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    out->batches = s->n_batches;
+    out->completed = s->n_done;
+    out->rejected = s->n_rejected;
+    out->failed = s->n_failed;
+    out->queued = s->queue.size();
+    out->peak_admitted_bytes = s->peak_admitted;
+    out->busy_ms = (double)s->busy_ns / 1e6;
+    out->kernel_launches = s->launches;
+    return GB_OK;
+}
+
+void gb_server_destroy(gb_server *s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stopping = true;
+    }
+    s->cv_work.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    if (s->batch) gb_batch_destroy(s->batch);
+    for (auto &e : s->alone) gb_agg_destroy(e.second);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
+}  // extern "C"

@@ -192,3 +192,124 @@ def batch_table_device(shape, device="cuda"):
 
 BATCH_COMPOSITE = dict(col_types=[2, 1, 3, 2], group_cols=[0, 1], aggs=[("count_star", -1), ("sum", 2), ("max", 3)])
 BATCH_VARCHAR = dict(col_types=[5, 3, 2], group_cols=[0], aggs=[("count_star", -1), ("sum", 1), ("max", 2)])
+
+
+# ------------------------------------------------------------------ serving
+# Resident tables of the served query stream: the column families of the
+# plain (INT32 key, INT64 value), Zipf (INT64 key, DOUBLE value), filtered
+# (dictionary-run INT32 key, INT16 filter column, INT64 value), composite
+# and VARCHAR workloads, generated on the GPU (torch's generator) at
+# `scale` × about 66 GB.
+SERVE_TABLES = [
+    dict(name="plain", family="plain", rows=500_000_000, groups=1024),
+    dict(name="zipf0", family="zipf", rows=400_000_000, groups=20_000_000),
+    dict(name="zipf1", family="zipf", rows=400_000_000, groups=20_000_000),
+    dict(name="filter0", family="filter", rows=600_000_000, groups=65_536),
+    dict(name="filter1", family="filter", rows=600_000_000, groups=65_536),
+    dict(name="comp0", family="composite", rows=400_000_000, groups=1_000),
+    dict(name="comp1", family="composite", rows=400_000_000, groups=30_000),
+    dict(name="comp2", family="composite", rows=400_000_000, groups=1_000_000),
+    dict(name="vch0", family="varchar", rows=100_000_000, groups=1_000),
+    dict(name="vch1", family="varchar", rows=100_000_000, groups=100_000),
+]
+
+SERVE_TYPES = {
+    "plain": [2, 3],            # k INTEGER, v BIGINT
+    "zipf": [3, 4],             # k BIGINT, x DOUBLE
+    "filter": [2, 1, 3],        # key INTEGER, f SMALLINT, v BIGINT
+    "composite": [2, 1, 3, 2],  # a INTEGER, b SMALLINT, s BIGINT, m INTEGER
+    "varchar": [5, 3, 2],       # key VARCHAR, s BIGINT, m INTEGER
+}
+
+
+def serve_table_device(t, scale=1.0, seed=4, device="cuda"):
+    """Columns of one serving table on the GPU."""
+    import torch
+    n = max(1024, int(t["rows"] * scale))
+    g = torch.Generator(device=device)
+    g.manual_seed(seed * 1000 + SERVE_TABLES.index(t))
+    fam = t["family"]
+    if fam == "plain":
+        k = torch.randint(0, t["groups"], (n,), generator=g, device=device, dtype=torch.int32)
+        v = torch.randint(0, 10**6, (n,), generator=g, device=device, dtype=torch.int64)
+        return [k, v], n
+    if fam == "zipf":
+        cdf = torch.from_numpy(zipf_cdf(t["groups"], 1.1)).to(device)
+        k = torch.empty(n, dtype=torch.int64, device=device)
+        x = torch.empty(n, dtype=torch.float64, device=device)
+        step = 1 << 26
+        for lo in range(0, n, step):
+            hi = min(n, lo + step)
+            u = torch.rand(hi - lo, generator=g, device=device, dtype=torch.float64)
+            r = torch.searchsorted(cdf, u, right=True).clamp_(max=t["groups"] - 1)
+            # ranks spread over [0, 2^40) by an odd multiplier (a bijection mod 2^40)
+            k[lo:hi] = (r * 0x9E3779B97F4A7C15) & ((1 << 40) - 1)
+            x[lo:hi] = torch.randn(hi - lo, generator=g, device=device, dtype=torch.float64) * 25 + 100
+        return [k, x], n
+    if fam == "filter":
+        dict_vals = torch.randint(0, 2**31, (t["groups"],), generator=g, device=device, dtype=torch.int64)
+        idx = torch.empty(n, dtype=torch.int64, device=device)
+        pos = 0
+        while pos < n:  # runs of Geometric(1/4) length, index uniform per run
+            m = min(n - pos, 1 << 26)
+            nr = m // 2 + 1
+            lens = torch.empty(nr, device=device).geometric_(0.25, generator=g).to(torch.int64)
+            vals = torch.randint(0, t["groups"], (nr,), generator=g, device=device, dtype=torch.int64)
+            run = torch.repeat_interleave(vals, lens)[:m]
+            idx[pos:pos + len(run)] = run
+            pos += len(run)
+        key = dict_vals[idx].to(torch.int32)
+        del idx
+        f = torch.randint(0, 1000, (n,), generator=g, device=device, dtype=torch.int16)
+        v = torch.randint(-10**9, 10**9 + 1, (n,), generator=g, device=device, dtype=torch.int64)
+        return [key, f, v], n
+    shape = dict(kind="composite" if fam == "composite" else "varchar", rows=n, groups=t["groups"],
+                 seed=seed * 1000 + SERVE_TABLES.index(t))
+    return batch_table_device(shape, device=device), n
+
+
+def serve_queries(duration_s, rate, rows_of, seed=4):
+    """Poisson arrivals at `rate` q/s for `duration_s`; each query has the
+    shape of one of the four GROUP BY workloads (uniformly chosen) over a
+    random row range of a table of that family, with a WHERE clause of
+    selectivity U[1%, 100%].  rows_of: table index -> resident rows."""
+    from statistics import NormalDist
+    rng = np.random.default_rng(seed)
+    fam_tables = {}
+    for i, t in enumerate(SERVE_TABLES):
+        fam_tables.setdefault(t["family"], []).append(i)
+    out = []
+    t_at = 0.0
+    while True:
+        t_at += rng.exponential(1.0 / rate)
+        if t_at >= duration_s:
+            break
+        shape = int(rng.integers(1, 5))
+        sel = float(rng.uniform(0.01, 1.0))
+        if shape == 1:
+            ti, rows = fam_tables["plain"][0], 1_000_000
+            q = dict(group_cols=[0], aggs=[("count_star", -1), ("sum", 1), ("min", 1), ("max", 1)],
+                     filters=[(1, "<", int(sel * 10**6))], est_groups=1024)
+        elif shape == 2:
+            ti, rows = int(rng.choice(fam_tables["zipf"])), 100_000_000
+            thr = 100.0 + 25.0 * NormalDist().inv_cdf(min(sel, 0.999999))
+            q = dict(group_cols=[0], aggs=[("count_star", -1), ("sum", 1), ("avg", 1)],
+                     filters=[(1, "<", thr)], est_groups=8_000_000)
+        elif shape == 3:
+            ti, rows = int(rng.choice(fam_tables["filter"])), 200_000_000
+            q = dict(group_cols=[0], aggs=[("sum", 2), ("count_star", -1)],
+                     filters=[(1, "<", int(sel * 1000))], est_groups=65_536)
+        else:
+            fam = "varchar" if rng.random() < 0.25 else "composite"
+            ti = int(rng.choice(fam_tables[fam]))
+            rows = int(10 ** rng.uniform(4, 7))
+            spec = BATCH_VARCHAR if fam == "varchar" else BATCH_COMPOSITE
+            q = dict(group_cols=spec["group_cols"], aggs=spec["aggs"],
+                     filters=[(1 if fam == "varchar" else 2, "<", int(sel * 10**6))],
+                     est_groups=SERVE_TABLES[ti]["groups"])
+        n = rows_of[ti]
+        rows = min(rows, n)
+        r0 = int(rng.integers(0, n - rows + 1)) // 64 * 64
+        q.update(table=ti, r0=r0, r1=r0 + rows, shape=shape, at=t_at)
+        out.append(q)
+    return out

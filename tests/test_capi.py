@@ -5,6 +5,8 @@ import os
 import re
 import subprocess
 
+import pytest
+
 from conftest import ROOT
 
 
@@ -48,3 +50,18 @@ def test_invalid_spec_rejected_without_gpu_work(gblib):
     h = C.c_void_p()
     assert gblib.gb_agg_create(None, C.byref(h)) == 1  # GB_ERR_INVALID
     assert b"null spec" in gblib.gb_last_error()
+
+
+def test_estimate_bytes_host_only(gblib):
+    """gb_agg_estimate_bytes compiles the plan only (no GPU needed)."""
+    from slothdb_gb300 import capi
+    comp = ([capi.INTEGER, capi.SMALLINT, capi.BIGINT, capi.INTEGER], [0, 1], [("count_star", -1), ("sum", 2)])
+    a = capi.estimate_bytes(*comp, nrows=10_000, est_groups=1000)
+    b = capi.estimate_bytes(*comp, nrows=10_000_000, est_groups=1_000_000)
+    c = capi.estimate_bytes(*comp, nrows=500, est_groups=1_000_000)   # groups bounded by rows
+    assert 0 < c <= a < b
+    s = capi.estimate_bytes([capi.VARCHAR, capi.BIGINT], [0], [("count_star", -1)], nrows=10_000, est_groups=1000)
+    assert s > capi.estimate_bytes([capi.BIGINT, capi.BIGINT], [0], [("count_star", -1)], nrows=10_000,
+                                   est_groups=1000)
+    with pytest.raises(capi.GbError):
+        capi.estimate_bytes([capi.VARCHAR, capi.BIGINT], [0], [("sum", 0)], nrows=10)   # SUM over VARCHAR

@@ -224,3 +224,50 @@ def test_batch_filters_int_and_double():
         compare(gpu_to_dict(b.result(nb + 1), 1, [capi.INTEGER, capi.BIGINT, capi.DOUBLE]), orc_gen)
     finally:
         b.close()
+
+
+def test_batch_clear_reuses_handles_with_new_filters():
+    """gb_batch_clear keeps the queries' handles; the next adds of the same
+    shape reuse them with new predicates and still match the oracle."""
+    shapes = [dict(kind="composite", rows=50_000 + i * 1000, groups=2000, seed=80 + i) for i in range(3)] + \
+             [dict(kind="varchar", rows=40_000, groups=900, seed=90)]
+    host = [datagen.batch_table_host(sh) for sh in shapes]
+    dev = [_to_device(c, _q(sh)["col_types"]) for c, sh in zip(host, shapes)]
+    b = capi.Batch()
+    try:
+        for rnd, thr in enumerate([300_000, 800_000, 50_000]):
+            if rnd:
+                b.clear()
+            for sh, d in zip(shapes, dev):
+                q = _q(sh)
+                fcol = 2 if sh["kind"] == "composite" else 1
+                b.add(q["col_types"], q["group_cols"], q["aggs"], d, sh["rows"], filters=[(fcol, "<", thr)],
+                      est_groups=sh["groups"])
+            b.run()
+            for i, (sh, cols) in enumerate(zip(shapes, host)):
+                q = _q(sh)
+                fcol = 2 if sh["kind"] == "composite" else 1
+                compare(_gpu(b.result(i), sh), oracle.run_query(q["col_types"], q["group_cols"], q["aggs"], cols,
+                                                                filters=[(fcol, "<", thr)]))
+    finally:
+        b.close()
+
+
+def test_set_filters_on_a_reset_handle():
+    k, v = datagen.plain(200_000, seed=5)
+    import torch
+    dk, dv = torch.from_numpy(k).cuda(), torch.from_numpy(v).cuda()
+    aggs = [("count_star", -1), ("sum", 1)]
+    g = capi.GroupBy([capi.INTEGER, capi.BIGINT], [0], aggs, filters=[(1, "<", 1000)])
+    try:
+        for thr in (1000, 500_000):
+            g.reset()
+            g.set_filters([(1, "<", thr)])
+            g.ingest([dk, dv], nrows=len(k), device=True)
+            g.finalize()
+            compare(gpu_to_dict(g.result(), 1, [capi.INTEGER, capi.BIGINT, capi.BIGINT]),
+                    oracle.run_query([capi.INTEGER, capi.BIGINT], [0], aggs, [k, v], filters=[(1, "<", thr)]))
+        with pytest.raises(capi.GbError):
+            g.set_filters([(1, "<", 5)])   # after finalize, before reset
+    finally:
+        g.close()
