@@ -52,7 +52,8 @@ def parse():
     ap.add_argument("--rows", type=int, default=100_000_000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=20_000_000)
-    ap.add_argument("--workload", default="zipf100m", choices=["zipf100m", "batch256", "serve"])
+    ap.add_argument("--workload", default="zipf100m", choices=["zipf100m", "batch256", "serve", "parquet200m"])
+    ap.add_argument("--pq-rows", type=int, default=200_000_000, help="parquet200m: rows in the file")
     ap.add_argument("--tables", type=int, default=256)
     ap.add_argument("--duration", type=float, default=20.0, help="serve: seconds of Poisson arrivals")
     ap.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")
@@ -529,6 +530,156 @@ def run_serve_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_parquet(args):
+    """Fused Parquet decode + filter + GROUP BY: an uncompressed file of
+    --pq-rows rows in 1M-row row groups (key INT32 dictionary of 65,536
+    values, RLE/bit-packed indices at bit width 16 with runs of mean 4;
+    f INT16 PLAIN; v INT64 PLAIN), SELECT key, SUM(v), COUNT(*) WHERE
+    f < 100 GROUP BY key.  value = rows/s with the file resident in HBM;
+    e2e = rows/s from the file in pinned host memory (row groups copied to
+    HBM inside the call)."""
+    ws, rank, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    from slothdb_gb300 import capi
+    from slothdb_gb300 import parquet as pq
+    capi.load(build_if_missing=True)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    rows = args.pq_rows
+    t0 = time.time()
+    data, key, f, v = pq.filter_groupby_file(n_rows=rows, row_group_rows=1_000_000)
+    gen_s = time.time() - t0
+    if args.impl == "reference":
+        return run_parquet_reference(args, key, f, v, rows)
+    file_bytes = len(data)
+    types = [capi.INTEGER, capi.SMALLINT, capi.BIGINT]
+    aggs = [("sum", 2), ("count_star", -1)]
+    filters = [(1, "<", 100)]
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    pf = capi.ParquetFile(data)
+    pf.upload(stream=sp)
+    g = capi.GroupBy(types, [0], aggs, filters=filters, est_groups=65_536)
+
+    def step(device=True, gg=g, ff=pf):
+        gg.reset()
+        capi.ingest_parquet(gg, ff, [0, 1, 2], device=device, stream=sp)
+        gg.finalize(stream=sp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # parity at full size against the oracle on the decoded columns
+    import oracle
+    orc = oracle.run_query(types, [0], aggs, [key, f.astype(np.int16), v], filters=filters,
+                           nthreads=os.cpu_count() or 1)
+    res = g.result()
+    got = dict(zip(res[0][0].tolist(), zip(res[1][0].tolist(), res[2][0].tolist())))
+    ok = len(got) == len(orc["keys"][0]) and all(
+        got.get(int(k_)) == (int(s_), int(c_)) for k_, s_, c_ in zip(orc["keys"][0], orc["aggs"][0][0],
+                                                                     orc["aggs"][1][0]))
+    g.set_profiling(True)
+    step()
+    prof = {k: vv[1] / max(1, vv[0]) for k, vv in g.profile().items()}
+    g.set_profiling(False)
+    clocks = Clocks(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        step()
+        launches += g.launches()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    scan_ms = prof.get("k_pq_scan", float("nan"))
+    achieved = file_bytes / (scan_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": None, "kernel": "k_pq_scan", "kernel_ms": scan_ms,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+                "step_GBps": file_bytes / (ms / 1e3) / 1e9, "step_frac": file_bytes / (ms / 1e3) / 1e9 / hbm_peak,
+                "kernels_ms": prof}
+    # e2e: the file in pinned host memory
+    pin = capi.PinnedBuffer(file_bytes)
+    pin.view(np.uint8)[:] = np.frombuffer(data, dtype=np.uint8)
+    pfh = capi.ParquetFile(pin.view(np.uint8))
+    ge = capi.GroupBy(types, [0], aggs, filters=filters, est_groups=65_536)
+    for _ in range(2):
+        step(device=False, gg=ge, ff=pfh)
+    torch.cuda.synchronize()
+    tt = time.perf_counter()
+    ne = max(1, args.steps // 2)
+    d2h = 0
+    for _ in range(ne):
+        step(device=False, gg=ge, ff=pfh)
+        d2h = sum(a.nbytes for a, _ in ge.result())
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - tt) / ne
+    ge.close()
+    pfh.close()
+    pin.close()
+    cpu = None
+    if rank == 0:
+        n = min(args.cpu_sample, rows)
+        thr = os.cpu_count() or 1
+        tc = time.perf_counter()
+        oracle.run_query(types, [0], aggs, [key[:n], f[:n].astype(np.int16), v[:n]], filters=filters, nthreads=thr)
+        dt = time.perf_counter() - tc
+        cpu = {"value": n / dt, "unit": "rows/s", "cores": thr, "kind": "port",
+               "sample": "first %d decoded rows, filter + GROUP BY (no page decode), %d threads" % (n, thr)}
+    line = {"metric": "fused Parquet decode+filter+GROUP BY rows/s (200M rows, 1M-row RGs)",
+            "value": rows / (ms / 1e3), "unit": "rows/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32+int64", "data": "synthetic",
+            "config": {"workload": "parquet-filter-groupby-%dM" % (rows // 1_000_000), "rows": rows,
+                       "file_bytes": file_bytes, "row_group_rows": 1_000_000, "dict": 65_536,
+                       "predicate": "f < 100", "l2": "file %.1f GB > L2 129 MB (no flush needed)" % (file_bytes / 1e9),
+                       "datagen_s": round(gen_s, 1)},
+            "parity": "bit-exact vs oracle" if ok else "MISMATCH vs oracle",
+            "roofline": roofline, "cpu_baseline": cpu,
+            "e2e": {"value": rows / e2e_s, "unit": "rows/s", "h2d_bytes_per_step": file_bytes,
+                    "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3},
+            "clocks": clk, "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+    g.close()
+    pf.close()
+
+
+def run_parquet_reference(args, key, f, v, rows):
+    """The oracle's filter + GROUP BY over the decoded columns of a bounded
+    sample (page decode not included), all host threads."""
+    import oracle
+    n = min(args.cpu_sample, rows)
+    thr = os.cpu_count() or 1
+    types = [2, 1, 3]
+    times = []
+    for i in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        oracle.run_query(types, [0], [("sum", 2), ("count_star", -1)], [key[:n], f[:n].astype(np.int16), v[:n]],
+                         filters=[(1, "<", 100)], nthreads=thr)
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t)
+    per = statistics.mean(times)
+    val = n / per
+    line = {"impl": "reference", "metric": "fused Parquet decode+filter+GROUP BY rows/s (200M rows, 1M-row RGs)",
+            "value": val, "unit": "rows/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32+int64", "data": "synthetic",
+            "config": {"workload": "parquet-filter-groupby (bounded sample of %d decoded rows)" % n},
+            "cpu_baseline": {"value": val, "unit": "rows/s", "cores": thr, "kind": "port",
+                             "sample": "first %d decoded rows per step" % n},
+            "e2e": {"value": val, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.workload == "batch256":
@@ -536,6 +687,9 @@ def main():
         return
     if args.workload == "serve":
         run_serve(args)
+        return
+    if args.workload == "parquet200m":
+        run_parquet(args)
         return
     if args.impl == "reference":
         run_reference(args)

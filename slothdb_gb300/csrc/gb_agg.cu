@@ -1999,6 +1999,26 @@ gb_status gb_agg_ingest_prefiltered(gb_agg *h, const gb_col *cols, uint64_t nrow
     return s;
 }
 
+struct gb_prof_mark {
+    int stat;
+    cudaEvent_t a;
+};
+
+gb_prof_mark *gb_agg_prof_begin(gb_agg *h, const char *name, cudaStream_t st) {
+    if (!h->profiling) return nullptr;
+    gb_prof_mark *m = new gb_prof_mark{prof_stat(h, name), prof_event(h)};
+    cudaEventRecord(m->a, st);
+    return m;
+}
+
+void gb_agg_prof_end(gb_agg *h, gb_prof_mark *m, cudaStream_t st) {
+    if (!m) return;
+    cudaEvent_t b = prof_event(h);
+    cudaEventRecord(b, st);
+    h->prof_pending.push_back({m->stat, m->a, b});
+    delete m;
+}
+
 // tuning hook (defaults here; the autotuner overrides per shape)
 void gb_apply_tuning(gb_agg *h) {
     const int words = h->plan.words;

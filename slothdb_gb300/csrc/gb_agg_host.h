@@ -19,5 +19,10 @@ gb_status gb_agg_view(gb_agg *h, AggView *v);
 void gb_agg_count_launch(gb_agg *h, int n);
 // Device-resident columns whose rows already passed the spec's filters.
 gb_status gb_agg_ingest_prefiltered(gb_agg *h, const gb_col *cols, uint64_t nrows, void *stream);
+// Profiling events around a kernel launched outside gb_agg.cu (no-ops
+// unless the handle's profiling is on).
+struct gb_prof_mark;
+gb_prof_mark *gb_agg_prof_begin(gb_agg *h, const char *name, cudaStream_t st);
+void gb_agg_prof_end(gb_agg *h, gb_prof_mark *m, cudaStream_t st);
 // Frees the per-handle Parquet scratch (called by gb_agg_destroy).
 void gb_pq_release_scratch(gb_agg *h);

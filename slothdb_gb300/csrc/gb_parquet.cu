@@ -883,9 +883,11 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
     GB_CUDA(cudaMemsetAsync(S->ctl, 0, sizeof(Ctl), st));
     Ctl *dctl = (Ctl *)S->ctl;
     if (!dict_pages.empty()) {
+        gb_prof_mark *pm = gb_agg_prof_begin(h, "k_pq_runs", st);
         k_pq_runs<<<(unsigned)dict_pages.size(), 128, 0, st>>>(dfile, (const DPage *)S->pages,
                                                                (const uint32_t *)S->dict_pages, (DRun *)S->runs,
                                                                (uint32_t *)S->page_runs, dctl);
+        gb_agg_prof_end(h, pm, st);
         GB_CUDA(cudaGetLastError());
         gb_agg_count_launch(h, 1);
     }
@@ -918,9 +920,11 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
     P.out_cap = S->out_cap_rows;
     {
         const int grid = (int)std::min<size_t>(chunks.size(), (size_t)sm_count() * 8);
+        gb_prof_mark *pm = gb_agg_prof_begin(h, "k_pq_scan", st);
         k_pq_scan<<<std::max(grid, 1), 256, 0, st>>>(dfile, (const DPage *)S->pages, (const DRun *)S->runs,
                                                      (const uint32_t *)S->page_runs, (const uint32_t *)S->col_pages,
                                                      (const PqChunkArg *)S->chunks, (uint32_t)chunks.size(), P, dctl);
+        gb_agg_prof_end(h, pm, st);
         GB_CUDA(cudaGetLastError());
         gb_agg_count_launch(h, 1);
     }
