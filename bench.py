@@ -62,6 +62,22 @@ def parse():
     return ap.parse_args()
 
 
+def max_over_ranks(ms, device="cuda"):
+    """The slowest rank's time (replicas: every rank runs a full workload)."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return ms
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world_size, ms):
+    """Units of all ranks / the max-over-ranks time (weak scaling)."""
+    return units_per_rank * world_size / (ms / 1e3)
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -753,11 +769,7 @@ def main():
     if ws > 1:
         torch.distributed.barrier()
     clk = clocks.stop()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps)
     # full result size: run once without TopN to count groups
     g2 = capi.GroupBy([capi.BIGINT, capi.DOUBLE], [0], aggs, est_groups=EST_GROUPS)
     g2.ingest([dk, dx], nrows=rows, device=True, stream=sp)
@@ -771,7 +783,7 @@ def main():
     in_bytes = rows * 16
     out_bytes = n_groups * 32
     alg_bytes = in_bytes + out_bytes
-    value = rows * ws / (ms / 1e3)
+    value = whole_job_rate(rows, ws, ms)
 
     # roofline: dominant kernel = the row pass (k_partition in radix mode,
     # k_ingest in hash mode); algorithmic bytes = the key + value columns

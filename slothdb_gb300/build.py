@@ -17,6 +17,7 @@ import sys
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(ROOT, "slothdb_gb300")
 CSRC = os.path.join(PKG, "csrc")
+OPDIR = os.path.join(PKG, "operator")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(BUILD, "libslothdb_gb300.so")
 ORACLE_DIR = os.path.join(ROOT, "oracle")
@@ -37,15 +38,17 @@ def _nvcc() -> str:
 
 def _sources(exts):
     out = []
-    for name in sorted(os.listdir(CSRC)):
-        if os.path.splitext(name)[1] in exts:
-            out.append(os.path.join(CSRC, name))
+    for d in (CSRC, OPDIR):
+        for name in sorted(os.listdir(d)):
+            if os.path.splitext(name)[1] in exts:
+                out.append(os.path.join(d, name))
     return out
 
 
 def _headers():
     hs = [os.path.join(ROOT, "include", n) for n in os.listdir(os.path.join(ROOT, "include"))]
-    hs += [os.path.join(CSRC, n) for n in os.listdir(CSRC) if n.endswith((".h", ".cuh", ".hpp"))]
+    for d in (CSRC, OPDIR):
+        hs += [os.path.join(d, n) for n in os.listdir(d) if n.endswith((".h", ".cuh", ".hpp"))]
     return hs
 
 
@@ -75,7 +78,9 @@ def build_lib(verbose: bool = False, force: bool = False) -> str:
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
         cmd = [nvcc] + ARCH + NVCC_FLAGS + inc + ["-c", src, "-o", obj]
-        if src.endswith(".cpp"):
+        if src.startswith(OPDIR):  # host-only C++ over the C ABI
+            cmd = [os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-fPIC"] + inc + ["-c", src, "-o", obj]
+        elif src.endswith(".cpp"):
             cmd = [nvcc, "-x", "cu"] + ARCH + NVCC_FLAGS + inc + ["-c", src, "-o", obj]
         _run(cmd)
         if verbose:
@@ -88,6 +93,24 @@ def build_lib(verbose: bool = False, force: bool = False) -> str:
     _run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcudart_static", "-lpthread", "-ldl", "-lrt"])
     os.replace(tmp, LIB)
     return LIB
+
+
+OPERATOR_TEST = os.path.join(BUILD, "test_gpu_operator")
+
+
+def build_operator_test(force: bool = False) -> str:
+    """The C++ test program of the operator mirror (tests/cpp), linked
+    against the library."""
+    src = os.path.join(ROOT, "tests", "cpp", "test_gpu_operator.cpp")
+    lib = build_lib()
+    deps = [src, lib, os.path.join(OPDIR, "gpu_operator.hpp")]
+    if not force and _newer(OPERATOR_TEST, deps):
+        return OPERATOR_TEST
+    tmp = OPERATOR_TEST + ".tmp"
+    _run([os.environ.get("CXX", "g++"), "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"), "-I", OPDIR, src,
+          "-o", tmp, "-L", BUILD, "-lslothdb_gb300", "-Wl,-rpath," + BUILD, "-lpthread"])
+    os.replace(tmp, OPERATOR_TEST)
+    return OPERATOR_TEST
 
 
 def build_oracle(force: bool = False) -> str:

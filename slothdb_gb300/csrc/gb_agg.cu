@@ -1642,6 +1642,8 @@ gb_status gb_agg_ingest(gb_agg *h, const gb_col *cols, uint64_t nrows, int32_t m
         h->rows_ingested += r1 - r0;
         GB_CUDA(cudaEventRecord(h->ev_done[b], st));
     }
+    // the caller may reuse its host buffers once the call returns
+    GB_CUDA(cudaStreamSynchronize(h->copy_stream));
     prof_collect(h);
     return GB_OK;
 }
