@@ -810,9 +810,15 @@ static gb_status radix_begin(gb_agg *h, u64 n, cudaStream_t st) {
     u64 cap_p = (u64)(tail / (double)np * 1.5) + 2048;
     cap_p = (cap_p + 31) / 32 * 32;
     h->r_cap_p = cap_p;
-    h->h_off.assign(np + 1, 0);
+    // a re-execution of the handle keeps the per-partition capacities its
+    // earlier runs grew to (skewed partitions stay large), so the regions
+    // are not regrown and moved on every run
+    std::vector<u32> prev;
+    if (h->h_capv.size() == np) prev.swap(h->h_capv);
     h->h_capv.assign(np, (u32)cap_p);
-    for (u64 p = 0; p < np; p++) h->h_off[p + 1] = h->h_off[p] + cap_p;
+    for (u64 p = 0; p < prev.size(); p++) h->h_capv[p] = std::max<u32>(h->h_capv[p], prev[p]);
+    h->h_off.assign(np + 1, 0);
+    for (u64 p = 0; p < np; p++) h->h_off[p + 1] = h->h_off[p] + h->h_capv[p];
     if ((s = h->r_part.ensure((size_t)h->h_off[np] * TV * 8))) return s;
     if ((s = h->r_off.ensure((np + 1) * 8)) || (s = h->r_cap.ensure(np * 4))) return s;
     GB_CUDA(cudaMemcpyAsync(h->r_off.p, h->h_off.data(), (np + 1) * 8, cudaMemcpyHostToDevice, st));
@@ -881,7 +887,6 @@ static gb_status radix_grow(gb_agg *h, u32 novf, cudaStream_t st) {
     if ((s = radix_launch_drain(X, R.V, novf, st))) return s;
     h->launches++;
     GB_CUDA(cudaStreamSynchronize(st));
-    h->r_part2.release();
     Ctl *dctl = (Ctl *)h->ctl_buf.p;
     GB_CUDA(cudaMemsetAsync(&dctl->aux0, 0, 4, st));
     return GB_OK;

@@ -6,8 +6,8 @@
 
 #define RADIX_MAX_V 3
 #define RADIX_MAX_OPS 4
-#define RADIX_ROWS 8
-#define P1_WARPS 16   // P1 block = 512 threads
+#define RADIX_ROWS 4
+#define P1_WARPS 32   // P1 block = 1024 threads (64 registers each: 32 warps per SM)
 #define REG_HOT 4     // hottest keys accumulated in per-lane registers
 #define RADIX_BLOCK 1024
 #define RADIX_LEASE 16   // tuples per partition lease (one global atomic each)
