@@ -244,7 +244,10 @@ __device__ __forceinline__ void store_at(const RadixRef &X, const TableRef &T, u
 // keys have a private state per warp (u32 count + W-1 words, plain updates
 // after a warp pre-combine); the other hot keys share one state per CTA
 // (native u32 count atomics; their word atomics are rarely contended).
-template <int ROWS, int VV, int NOPS>
+// SPEC != 0: the plan is one non-NULL BIGINT key, one non-NULL value column,
+// one op (SPEC = OP_ADD_F or OP_ADD_I) and no predicates — every per-row plan
+// interpretation (key packing, type and op switches) is compiled away.
+template <int ROWS, int VV, int NOPS, int SPEC = 0>
 __global__ void __launch_bounds__(P1_WARPS * 32, 1)
     k_partition(const __grid_constant__ Plan P, const __grid_constant__ RadixPlan R, const RadixRef X,
                 const TableRef T, const RadixTile A) {
@@ -326,8 +329,14 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
             kinds[j] = 0;
             pk[j] = 0;
             if (acts[j]) {
-                kinds[j] = make_key(P, r, pk[j]);
-                tuple_vals<VV>(P, R, r, tv[j]);
+                if (SPEC) {
+                    pk[j] = (u64)__ldg((const long long *)P.cols[P.key_col[0]].data + r);
+                    kinds[j] = pk[j] == EMPTY_KEY ? 1 : 0;
+                    tv[j][0] = (u64)__ldg((const long long *)P.cols[R.vcol[0]].data + r);
+                } else {
+                    kinds[j] = make_key(P, r, pk[j]);
+                    tuple_vals<VV>(P, R, r, tv[j]);
+                }
             }
         }
 #pragma unroll
@@ -336,7 +345,7 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
             pend[j] = 0;
             pslot[j] = 0;
             bool act = acts[j];
-            if (act && P.n_filters) act = pass_filters(P, r);
+            if (!SPEC && act && P.n_filters) act = pass_filters(P, r);
             bool priv = false;
             u32 hidx = 0;
             u64 v[NOPS > 0 ? NOPS : 1];
@@ -344,7 +353,8 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
             for (int q = 0; q < (NOPS > 0 ? NOPS : 1); q++) v[q] = 0;
             if (act) {
                 const int kind = kinds[j];
-                tuple_contrib<VV, NOPS>(P, R, tv[j], v);
+                if (SPEC) v[0] = tv[j][0];
+                else tuple_contrib<VV, NOPS>(P, R, tv[j], v);
                 if (kind != 0) {
                     if (kind == 3) {
                         atomicOr(&T.ctl->err, (u32)ERR_NULL_IN_WIDE_KEY);
@@ -375,7 +385,8 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
                                 if (hidx == (u32)k) {
                                     rc[k]++;
 #pragma unroll
-                                    for (int i = 0; i < NOPS; i++) rw[k][i] = op_combine(P.ops[i].kind, rw[k][i], v[i]);
+                                    for (int i = 0; i < NOPS; i++)
+                                        rw[k][i] = op_combine(SPEC ? SPEC : P.ops[i].kind, rw[k][i], v[i]);
                                 }
                             }
                         } else if ((int)hidx < NPRIV) {
@@ -383,14 +394,14 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
                             atomicAdd(&mypc[hidx], 1u);
 #pragma unroll
                             for (int i = 0; i < NOPS; i++)
-                                op_apply(P.ops[i].kind, mypw + (size_t)hidx * WM + (P.ops[i].word - 1), v[i],
-                                         P.word_init[P.ops[i].word]);
+                                op_apply(SPEC ? SPEC : P.ops[i].kind, mypw + (size_t)hidx * WM + (P.ops[i].word - 1),
+                                         v[i], P.word_init[P.ops[i].word]);
                         } else {
                             const u32 wi = hidx - NPRIV;
                             atomicAdd(&sc[wi], 1u);
 #pragma unroll
                             for (int i = 0; i < NOPS; i++)
-                                op_apply(P.ops[i].kind, sw + (size_t)wi * WM + (P.ops[i].word - 1), v[i],
+                                op_apply(SPEC ? SPEC : P.ops[i].kind, sw + (size_t)wi * WM + (P.ops[i].word - 1), v[i],
                                          P.word_init[P.ops[i].word]);
                         }
                     } else {
@@ -819,6 +830,18 @@ static void fill_tables(P1Fn *t1, P2Fn *t2) {
 
 static P1Fn g_p1[4 * (RADIX_MAX_OPS + 1)];
 static P2Fn g_p2[4 * (RADIX_MAX_OPS + 1)];
+static P1Fn g_p1_spec_f, g_p1_spec_i;  // specialised P1: BIGINT key, one SUM (DOUBLE / integer)
+
+// The specialised P1 applies: one non-NULL BIGINT key, one non-NULL value
+// column, one ADD op, no predicates.
+static int p1_spec(const Plan &P, const RadixPlan &R) {
+    if (P.key_mode != KEY_SINGLE || P.cols[P.key_col[0]].type != GB_T_BIGINT || P.cols[P.key_col[0]].valid) return 0;
+    if (R.V != 1 || P.n_ops != 1 || P.n_filters || P.cols[R.vcol[0]].valid) return 0;
+    const int t = P.cols[R.vcol[0]].type;
+    if (P.ops[0].kind == OP_ADD_F && t == GB_T_DOUBLE) return OP_ADD_F;
+    if (P.ops[0].kind == OP_ADD_I && t == GB_T_BIGINT) return OP_ADD_I;
+    return 0;
+}
 
 static gb_status radix_set_attributes() {
     static bool done = false;
@@ -826,6 +849,10 @@ static gb_status radix_set_attributes() {
     fill_tables<1>(g_p1, g_p2);
     fill_tables<2>(g_p1, g_p2);
     fill_tables<3>(g_p1, g_p2);
+    g_p1_spec_f = (P1Fn)k_partition<RADIX_ROWS, 1, 1, OP_ADD_F>;
+    g_p1_spec_i = (P1Fn)k_partition<RADIX_ROWS, 1, 1, OP_ADD_I>;
+    for (P1Fn f : {g_p1_spec_f, g_p1_spec_i})
+        if (gb_status s = allow_max_smem(f)) return s;
     for (int v = 1; v <= 3; v++)
         for (int o = 0; o <= RADIX_MAX_OPS; o++) {
             gb_status s;
@@ -842,6 +869,9 @@ gb_status radix_launch_p1(const Plan &P, const RadixPlan &R, const RadixRef &X, 
     if (s) return s;
     const size_t smem = radix_p1_smem(P, R);
     P1Fn f = g_p1[R.V * (RADIX_MAX_OPS + 1) + P.n_ops];
+    const int spec = p1_spec(P, R);
+    if (spec == OP_ADD_F) f = g_p1_spec_f;
+    else if (spec == OP_ADD_I) f = g_p1_spec_i;
     f<<<grid, P1_WARPS * 32, smem, st>>>(P, R, X, T, A);
     GB_CUDA(cudaGetLastError());
     return GB_OK;
