@@ -40,6 +40,12 @@
 
 namespace gb {
 
+// P2 pre-combines equal keys within a warp before folding (1) or folds
+// every tuple on its own (0).
+#ifndef P2_PRECOMBINE
+#define P2_PRECOMBINE 1
+#endif
+
 __device__ __forceinline__ u32 part_of(u64 h, int pbits) { return pbits ? (u32)(h >> (64 - pbits)) : 0u; }
 __device__ __forceinline__ u32 hot_slot(u64 h, int HS) { return (u32)h & (u32)(HS - 1); }
 __device__ __forceinline__ u32 agg_slot(u64 h, int SP) { return (u32)(h >> 20) & (u32)(SP - 1); }
@@ -576,10 +582,37 @@ __global__ void __launch_bounds__(RADIX_BLOCK, 1)
                 act = true;
             }
         }
+        const u64 hh = mix64(pk);
+        if (!P2_PRECOMBINE) {
+            // tail keys rarely repeat within 32 consecutive tuples: fold each
+            // tuple on its own
+            if (!act) continue;
+            const u64 cnt = 1;
+            u32 s = agg_slot(hh, SP);
+            bool done = false;
+            for (int q = 0; q < R.agg_probe; q++) {
+                u64 k = vk[s];
+                if (k == EMPTY_KEY) {
+                    const u64 old = atomicCAS(&keys[s], EMPTY_KEY, pk);
+                    k = (old == EMPTY_KEY) ? pk : old;
+                }
+                if (k == pk) {
+                    atomicAdd(&cn[s], (u32)cnt);
+#pragma unroll
+                    for (int o = 0; o < NOPS; o++)
+                        op_apply(P.ops[o].kind, wd + (size_t)s * WM + (P.ops[o].word - 1), v[o],
+                                 P.word_init[P.ops[o].word]);
+                    done = true;
+                    break;
+                }
+                s = (s + 1) & (u32)(SP - 1);
+            }
+            if (!done) global_fold_n<NOPS>(P, T, pk, cnt, v, &s_new);
+            continue;
+        }
         // pre-combine lanes with equal keys: match on 32 hash bits (cheaper
         // than a 64-bit match), then keep only lanes whose full key equals
         // their group leader's; the others stay leaders of themselves
-        const u64 hh = mix64(pk);
         const unsigned am = __ballot_sync(FULL, act);
         unsigned peers = __match_any_sync(FULL, (unsigned)hh) & am;
         const int ldr = __ffs(peers) - 1;
@@ -755,7 +788,10 @@ gb_status radix_prepare(const Plan &P, RadixPlan &R, u64 est_groups, u64 nullabl
     R.nsup = 64;
     R.hot_probe = 8;
     while (radix_p1_smem(P, R) > kSmemBudget) {
+        // keep the hot set large (a key left out of it lands in P2, where its
+        // repeats contend): shrink the warp-private tier first
         if (R.pbits > 10) R.pbits--;
+        else if (R.nsup > 32) R.nsup -= 16;
         else if (R.nh > 1024) {
             R.nh /= 2;
             R.HS /= 2;
