@@ -636,7 +636,7 @@ def run_parquet(args):
     d2h = 0
     for _ in range(ne):
         step(device=False, gg=ge, ff=pfh)
-        d2h = sum(a.nbytes for a, _ in ge.result())
+        d2h = ge.result_host_bytes()[1]
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - tt) / ne
     ge.close()
@@ -817,8 +817,7 @@ def main():
             ge.reset()
             ge.ingest([pk.ptr, px.ptr], nrows=rows, stream=sp)  # host (pinned) pointers
             ge.finalize(stream=sp)
-            res = ge.result()
-            return sum(a.nbytes for a, _ in res)
+            return ge.result_host_bytes()[1]  # gb_agg_result: full result into host memory
 
         for _ in range(2):
             d2h = step_e2e()

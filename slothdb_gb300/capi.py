@@ -305,6 +305,23 @@ class GroupBy:
         check(self.lib.gb_agg_result(self.h, C.byref(r)))
         return _read_result(r)
 
+    def result_host_bytes(self):
+        """gb_agg_result only (the library's device→host copy into its own
+        pinned buffers, no Python conversion); returns (rows, bytes copied)."""
+        r = Result()
+        check(self.lib.gb_agg_result(self.h, C.byref(r)))
+        n = int(r.n_rows)
+        nbytes = 0
+        for c in range(r.n_cols):
+            t = r.types[c]
+            nbytes += (n + 63) // 64 * 8
+            if t == VARCHAR:
+                offs = np.frombuffer((C.c_char * ((n + 1) * 8)).from_address(r.offsets[c]), dtype=np.int64)
+                nbytes += (n + 1) * 8 + int(offs[-1]) if n else 0
+            else:
+                nbytes += n * np.dtype(NP_TYPES[t]).itemsize
+        return n, nbytes
+
     def set_option(self, name, value):
         check(self.lib.gb_agg_set_option(self.h, name.encode(), int(value)))
 

@@ -512,19 +512,38 @@ __device__ __forceinline__ uint32_t find_page(const DPage *pages, uint32_t pb, u
 }
 
 // Decode one value of a page at value index i (as int64 / double bits).
+// `bw` bits (bw <= 32) starting at bit `bit` of the byte string at p, read
+// with aligned 8-byte loads of the words that hold them.
+__device__ __forceinline__ uint32_t load_bits(const uint8_t *p, u64 bit, uint32_t bw) {
+    const uintptr_t a = (uintptr_t)p + (uintptr_t)(bit >> 3);
+    const u64 *w = (const u64 *)(a & ~(uintptr_t)7);
+    const uint32_t sh = (uint32_t)(a & 7) * 8 + (uint32_t)(bit & 7);  // bit offset within *w
+    u64 v = __ldg(w) >> sh;
+    if (sh + bw > 64) v |= __ldg(w + 1) << (64 - sh);
+    return (uint32_t)(v & (bw >= 32 ? 0xffffffffull : ((1ull << bw) - 1ull)));
+}
+
+// A PLAIN value at any byte address: aligned loads of the words that hold
+// its bytes, joined by a funnel shift (a misaligned 4- or 8-byte load would
+// fault).  The words read hold bytes of the value only.
+__device__ __forceinline__ u64 load_plain(const uint8_t *p, int width) {
+    const uintptr_t a = (uintptr_t)p;
+    if (width == 4) {
+        const uint32_t *w = (const uint32_t *)(a & ~(uintptr_t)3);
+        const uint32_t sh = (uint32_t)(a & 3) * 8;
+        const uint32_t lo = __ldg(w);
+        const uint32_t v = sh ? __funnelshift_r(lo, __ldg(w + 1), sh) : lo;
+        return (u64)(i64)(int32_t)v;
+    }
+    const u64 *w = (const u64 *)(a & ~(uintptr_t)7);
+    const uint32_t sh = (uint32_t)(a & 7) * 8;
+    const u64 lo = __ldg(w);
+    return sh ? ((lo >> sh) | (__ldg(w + 1) << (64 - sh))) : lo;
+}
+
 __device__ __forceinline__ u64 decode_at(const uint8_t *file, const DPage &pg, const DRun *runs,
                                          const uint32_t *page_runs, uint32_t pidx, uint32_t i) {
-    if (pg.kind == 0) {
-        const uint8_t *src = file + pg.off + (u64)i * pg.width;
-        if (pg.width == 4) {
-            int32_t v;
-            memcpy(&v, src, 4);
-            return (u64)(i64)v;
-        }
-        u64 v;
-        memcpy(&v, src, 8);
-        return v;
-    }
+    if (pg.kind == 0) return load_plain(file + pg.off + (u64)i * pg.width, pg.width);
     const uint32_t nr = page_runs[2 * pidx], bw = page_runs[2 * pidx + 1];
     const DRun *rr = runs + pg.run_base;
     uint32_t lo = 0, hi = nr;  // last run with start <= i
@@ -541,23 +560,10 @@ __device__ __forceinline__ u64 decode_at(const uint8_t *file, const DPage &pg, c
     } else if (rn.off == 0xffffffffu) {
         idx = rn.val;
     } else {
-        const u64 bit = (u64)(i - rn.start) * bw;
-        const uint8_t *b = file + pg.off + rn.off + (bit >> 3);
-        u64 w = 0;
-        const uint32_t nb = (uint32_t)(((bit & 7) + bw + 7) >> 3);
-        for (uint32_t k = 0; k < nb; k++) w |= (u64)b[k] << (8 * k);
-        idx = (uint32_t)((w >> (bit & 7)) & (bw >= 32 ? 0xffffffffull : ((1ull << bw) - 1ull)));
+        idx = load_bits(file + pg.off + rn.off, (u64)(i - rn.start) * bw, bw);
     }
     if (idx >= pg.dict_n) return 0;  // the reference maps an out-of-range index to 0
-    const uint8_t *src = file + pg.dict_off + (u64)idx * pg.width;
-    if (pg.width == 4) {
-        int32_t v;
-        memcpy(&v, src, 4);
-        return (u64)(i64)v;
-    }
-    u64 v;
-    memcpy(&v, src, 8);
-    return v;
+    return load_plain(file + pg.dict_off + (u64)idx * pg.width, pg.width);
 }
 
 struct PqChunkArg {
@@ -588,15 +594,163 @@ __device__ __forceinline__ u64 decode_col(const uint8_t *file, const DPage *page
     return decode_at(file, pg, runs, page_runs, pi, r - pg.first_row);
 }
 
+// Per chunk, shared memory holds each column's pages that overlap the chunk
+// (PQ_MAXP at most; more falls back to the global page search) and, for the
+// first dictionary-encoded column, the runs of those pages that overlap the
+// chunk (PQ_MAXR at most; more falls back to the global run search), so a
+// row's decode searches a few shared entries instead of global arrays.
+#define PQ_MAXP 8
+#define PQ_MAXR 2048
+
+
+struct PqChunkView {
+    uint32_t np[GB_MAX_COLS];              // pages overlapping the chunk (0 = fallback)
+    uint32_t pfirst[GB_MAX_COLS][PQ_MAXP];  // their first rows
+    uint32_t pidx[GB_MAX_COLS][PQ_MAXP];    // their page indices
+    int32_t dcol;                           // dictionary column with staged runs (-1: none)
+    uint32_t rbeg[PQ_MAXP], rcnt[PQ_MAXP];  // staged run windows per page of dcol
+};
+
+__device__ __forceinline__ uint32_t run_search(const DRun *rr, uint32_t lo, uint32_t hi, uint32_t i) {
+    while (hi - lo > 1) {  // last run with start <= i
+        const uint32_t mid = (lo + hi) >> 1;
+        if (rr[mid].start <= i) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Value i of dictionary page pg, its run found in `rr[lo, hi)`.
+__device__ __forceinline__ u64 dict_value(const uint8_t *file, const DPage &pg, const DRun *rr, uint32_t lo,
+                                          uint32_t hi, uint32_t bw, uint32_t i) {
+    if (hi <= lo) return 0;
+    const DRun rn = rr[run_search(rr, lo, hi, i)];
+    uint32_t idx;
+    if (i < rn.start || i >= rn.start + rn.cnt) {
+        idx = 0xffffffffu;  // past the decoded values (truncated page): left unset → 0
+    } else if (rn.off == 0xffffffffu) {
+        idx = rn.val;
+    } else {
+        idx = load_bits(file + pg.off + rn.off, (u64)(i - rn.start) * bw, bw);
+    }
+    if (idx >= pg.dict_n) return 0;  // the reference maps an out-of-range index to 0
+    return load_plain(file + pg.dict_off + (u64)idx * pg.width, pg.width);
+}
+
+// Row r (row-group relative) of column c through the chunk's staged view.
+__device__ __forceinline__ u64 decode_staged(const uint8_t *file, const DPage *pages, const DRun *runs,
+                                             const uint32_t *page_runs, const uint32_t *col_pages, int n_cols,
+                                             uint32_t rg, int c, uint32_t r, const PqChunkView &V,
+                                             const DRun *srun) {
+    const uint32_t np = V.np[c];
+    if (np == 0) return decode_col(file, pages, runs, page_runs, col_pages, n_cols, rg, c, r);
+    uint32_t k = 0;
+    while (k + 1 < np && V.pfirst[c][k + 1] <= r) k++;
+    const uint32_t pi = V.pidx[c][k];
+    const DPage &pg = pages[pi];
+    const uint32_t i = r - pg.first_row;
+    if (pg.kind != 0 && c == V.dcol)
+        return dict_value(file, pg, srun + V.rbeg[k], 0, V.rcnt[k], page_runs[2 * pi + 1], i);
+    return decode_at(file, pg, runs, page_runs, pi, i);
+}
+
 __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPage *pages, const DRun *runs,
                                                  const uint32_t *page_runs, const uint32_t *col_pages,
                                                  const PqChunkArg *chunks, uint32_t n_chunks,
                                                  const __grid_constant__ PqScan S, Ctl *ctl) {
     constexpr int PER = PQ_CHUNK / 256;
+    __shared__ PqChunkView V;
+    __shared__ DRun srun[PQ_MAXR];
+    __shared__ uint32_t s_rlo[PQ_MAXP];
     for (uint32_t ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
         const PqChunkArg ch = chunks[ci];
+        const uint32_t rlast = ch.row0 + (ch.nrows ? ch.nrows - 1 : 0);
+        // (a) each column's pages overlapping the chunk
+        if (threadIdx.x < (unsigned)S.n_cols) {
+            const int c = threadIdx.x;
+            const uint32_t pb = col_pages[2 * (ch.rg * S.n_cols + c)], pe = col_pages[2 * (ch.rg * S.n_cols + c) + 1];
+            uint32_t n = 0;
+            if (pe > pb) {
+                uint32_t p = find_page(pages, pb, pe, ch.row0);
+                for (; p < pe && pages[p].first_row <= rlast; p++) {
+                    if (n == PQ_MAXP) {
+                        n = 0;  // too many pages: per-row global search
+                        break;
+                    }
+                    V.pfirst[c][n] = pages[p].first_row;
+                    V.pidx[c][n] = p;
+                    n++;
+                }
+            }
+            V.np[c] = n;
+        }
+        if (threadIdx.x == 0) V.dcol = -1;
+        __syncthreads();
+        // (b) the first dictionary column's runs overlapping the chunk
+        if (threadIdx.x == 0) {
+            int dc = -1;
+            for (int c = 0; c < S.n_cols && dc < 0; c++)
+                if (V.np[c] && pages[V.pidx[c][0]].kind != 0) dc = c;
+            uint32_t tot = 0;
+            if (dc >= 0) {
+                for (uint32_t k = 0; k < V.np[dc]; k++) {
+                    const uint32_t pi = V.pidx[dc][k];
+                    const DPage &pg = pages[pi];
+                    if (pg.kind == 0) {  // a PLAIN page of the column has no runs
+                        s_rlo[k] = 0;
+                        V.rbeg[k] = tot;
+                        V.rcnt[k] = 0;
+                        continue;
+                    }
+                    const uint32_t nr = page_runs[2 * pi];
+                    const DRun *rr = runs + pg.run_base;
+                    const uint32_t i0 = ch.row0 > pg.first_row ? ch.row0 - pg.first_row : 0;
+                    const uint32_t i1 = rlast - pg.first_row;  // inclusive (clipped by the run search)
+                    uint32_t lo = nr ? run_search(rr, 0, nr, i0) : 0;
+                    uint32_t hi = nr ? run_search(rr, 0, nr, i1) + 1 : 0;
+                    s_rlo[k] = pg.run_base + lo;
+                    V.rbeg[k] = tot;
+                    V.rcnt[k] = hi - lo;
+                    tot += hi - lo;
+                }
+                if (tot <= PQ_MAXR) V.dcol = dc;
+            }
+        }
+        __syncthreads();
+        if (V.dcol >= 0) {
+            const int dc = V.dcol;
+            for (uint32_t k = 0; k < V.np[dc]; k++)
+                for (uint32_t t = threadIdx.x; t < V.rcnt[k]; t += blockDim.x) srun[V.rbeg[k] + t] = runs[s_rlo[k] + t];
+        }
+        __syncthreads();
         bool keep[PER];
         u32 mine = 0;
+        // one predicate on a PLAIN column inside one page (the common case):
+        // every load of the chunk is issued before any compare
+        const int fc = S.n_filters == 1 ? S.filters[0].col : -1;
+        if (fc >= 0 && V.np[fc] == 1 && pages[V.pidx[fc][0]].kind == 0) {
+            const DPage pg = pages[V.pidx[fc][0]];
+            const Filter f = S.filters[0];
+            const uint8_t *base = file + pg.off;  // page payloads start at any byte
+            u64 xv[PER];
+#pragma unroll
+            for (int j = 0; j < PER; j++) {
+                const uint32_t rr = (uint32_t)j * 256 + threadIdx.x;
+                xv[j] = 0;
+                if (rr < ch.nrows) {
+                    const uint32_t i = ch.row0 + rr - pg.first_row;
+                    xv[j] = load_plain(base + (u64)i * pg.width, pg.width);
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < PER; j++) {
+                const uint32_t rr = (uint32_t)j * 256 + threadIdx.x;
+                keep[j] = rr < ch.nrows && (S.out_type[fc] == GB_T_DOUBLE
+                                                ? cmp_f(f.op, __longlong_as_double((i64)xv[j]), f.dc)
+                                                : cmp_i(f.op, (i64)xv[j], f.ic));
+                mine += keep[j];
+            }
+        } else {
 #pragma unroll
         for (int j = 0; j < PER; j++) {
             const uint32_t rr = (uint32_t)j * 256 + threadIdx.x;
@@ -605,11 +759,12 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
             const uint32_t r = ch.row0 + rr;
             for (int q = 0; q < S.n_filters && keep[j]; q++) {
                 const Filter &f = S.filters[q];
-                const u64 x = decode_col(file, pages, runs, page_runs, col_pages, S.n_cols, ch.rg, f.col, r);
+                const u64 x = decode_staged(file, pages, runs, page_runs, col_pages, S.n_cols, ch.rg, f.col, r, V, srun);
                 if (S.out_type[f.col] == GB_T_DOUBLE) keep[j] = cmp_f(f.op, __longlong_as_double((i64)x), f.dc);
                 else keep[j] = cmp_i(f.op, (i64)x, f.ic);
             }
             mine += keep[j];
+        }
         }
         u64 o = block_out_base(ctl, mine);
 #pragma unroll
@@ -621,7 +776,7 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
             }
             const uint32_t r = ch.row0 + (uint32_t)j * 256 + threadIdx.x;
             for (int c = 0; c < S.n_cols; c++) {
-                const u64 x = decode_col(file, pages, runs, page_runs, col_pages, S.n_cols, ch.rg, c, r);
+                const u64 x = decode_staged(file, pages, runs, page_runs, col_pages, S.n_cols, ch.rg, c, r, V, srun);
                 switch (S.out_type[c]) {
                 case GB_T_SMALLINT: ((int16_t *)S.out[c])[o] = (int16_t)(i64)x; break;
                 case GB_T_INTEGER: ((int32_t *)S.out[c])[o] = (int32_t)(i64)x; break;
@@ -630,6 +785,7 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
             }
             o++;
         }
+        __syncthreads();  // the chunk view is rebuilt for the next chunk
     }
 }
 
