@@ -280,6 +280,8 @@ gb_status gb_batch_run(gb_batch *b, void *stream);
 gb_status gb_batch_clear(gb_batch *b);
 uint32_t gb_batch_size(const gb_batch *b);
 gb_status gb_batch_result(gb_batch *b, uint32_t query_index, gb_result *out);
+/* Device-resident view of query i's result (valid until the next run/clear). */
+gb_status gb_batch_result_device(gb_batch *b, uint32_t query_index, gb_result *out);
 uint32_t gb_batch_slow_queries(const gb_batch *b);
 uint64_t gb_batch_kernel_launches(const gb_batch *b);
 uint32_t gb_batch_profile(const gb_batch *b, gb_kernel_stat *out, uint32_t max);

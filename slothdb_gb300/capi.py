@@ -98,6 +98,7 @@ _SIGS = {
     "gb_batch_clear": (C.c_int, [C.c_void_p]),
     "gb_batch_size": (C.c_uint32, [C.c_void_p]),
     "gb_batch_result": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Result)]),
+    "gb_batch_result_device": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(Result)]),
     "gb_batch_slow_queries": (C.c_uint32, [C.c_void_p]),
     "gb_batch_kernel_launches": (C.c_uint64, [C.c_void_p]),
     "gb_batch_profile": (C.c_uint32, [C.c_void_p, C.POINTER(KernelStat), C.c_uint32]),

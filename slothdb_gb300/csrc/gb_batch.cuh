@@ -1136,6 +1136,11 @@ gb_status gb_batch_result(gb_batch *b, uint32_t q, gb_result *out) {
     return gb_agg_result(b->handles[q], out);
 }
 
+gb_status gb_batch_result_device(gb_batch *b, uint32_t q, gb_result *out) {
+    if (!b || q >= b->handles.size()) return GB_ERR_INVALID;
+    return gb_agg_result_device(b->handles[q], out);
+}
+
 uint32_t gb_batch_slow_queries(const gb_batch *b) { return b ? (uint32_t)b->slow.size() : 0; }
 
 uint64_t gb_batch_kernel_launches(const gb_batch *b) { return b ? b->launches : 0; }

@@ -31,6 +31,7 @@
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <map>
 #include <memory>
 #include <mutex>
 #include <string>
@@ -71,13 +72,61 @@ struct Table {
     u64 nrows = 0;
 };
 
-// A host copy of one result.
+// Page-locked host blocks recycled between results (size classes of powers
+// of two), so a result is copied once, device → pinned host, at full link
+// bandwidth, with no allocation in steady state.
+class PinnedPool {
+public:
+    struct Block {
+        void *p;
+        size_t cls;
+    };
+    Block get(size_t bytes) {
+        size_t cls = 4096;
+        while (cls < bytes) cls <<= 1;
+        {
+            std::lock_guard<std::mutex> lk(mu_);
+            auto it = free_.find(cls);
+            if (it != free_.end()) {
+                Block b{it->second, cls};
+                free_.erase(it);
+                free_bytes_ -= cls;
+                return b;
+            }
+        }
+        void *p = nullptr;
+        if (cudaMallocHost(&p, cls) != cudaSuccess) {
+            (void)cudaGetLastError();
+            return {nullptr, 0};
+        }
+        return {p, cls};
+    }
+    void put(const Block &b) {
+        if (!b.p) return;
+        std::lock_guard<std::mutex> lk(mu_);
+        if (free_bytes_ + b.cls > kKeepBytes) {
+            cudaFreeHost(b.p);
+            return;
+        }
+        free_.emplace(b.cls, b.p);
+        free_bytes_ += b.cls;
+    }
+    ~PinnedPool() {
+        for (auto &e : free_) cudaFreeHost(e.second);
+    }
+
+private:
+    static constexpr size_t kKeepBytes = (size_t)8 << 30;  // idle pinned memory kept for reuse
+    std::mutex mu_;
+    std::multimap<size_t, void *> free_;
+    size_t free_bytes_ = 0;
+};
+
+// A host copy of one result, in pinned blocks of the pool.
 struct HostResult {
     u64 n_rows = 0;
     std::vector<int32_t> types;
-    std::vector<std::vector<uint8_t>> data;
-    std::vector<std::vector<uint64_t>> valid;
-    std::vector<std::vector<int64_t>> offs;
+    std::vector<PinnedPool::Block> blocks;
     std::vector<const void *> data_p;
     std::vector<const int64_t *> offs_p;
     std::vector<const uint64_t *> valid_p;
@@ -116,38 +165,6 @@ struct Query {
 };
 
 
-void copy_result(const gb_result &r, HostResult &out) {
-    const u64 n = r.n_rows;
-    out.n_rows = n;
-    out.types.assign(r.types, r.types + r.n_cols);
-    out.data.assign(r.n_cols, {});
-    out.valid.assign(r.n_cols, {});
-    out.offs.assign(r.n_cols, {});
-    for (uint32_t c = 0; c < r.n_cols; c++) {
-        const u64 vw = (n + 63) / 64;
-        if (r.validity && r.validity[c]) out.valid[c].assign(r.validity[c], r.validity[c] + vw);
-        else out.valid[c].assign(vw, ~0ull);
-        if (r.types[c] == GB_T_VARCHAR) {
-            out.offs[c].assign(r.offsets[c], r.offsets[c] + n + 1);
-            const int64_t nb = out.offs[c][n] - out.offs[c][0];
-            const uint8_t *p = (const uint8_t *)r.data[c] + out.offs[c][0];
-            out.data[c].assign(p, p + nb);
-            for (auto &o : out.offs[c]) o -= r.offsets[c][0];
-        } else {
-            const uint8_t *p = (const uint8_t *)r.data[c];
-            out.data[c].assign(p, p + n * (u64)type_bytes(r.types[c]));
-        }
-    }
-    out.data_p.resize(r.n_cols);
-    out.offs_p.resize(r.n_cols);
-    out.valid_p.resize(r.n_cols);
-    for (uint32_t c = 0; c < r.n_cols; c++) {
-        out.data_p[c] = out.data[c].data();
-        out.offs_p[c] = out.types[c] == GB_T_VARCHAR ? out.offs[c].data() : nullptr;
-        out.valid_p[c] = out.valid[c].data();
-    }
-}
-
 }  // namespace
 
 struct gb_server {
@@ -165,6 +182,7 @@ struct gb_server {
     bool started = false;
     cudaStream_t stream = nullptr;
     int device = 0;
+    PinnedPool pinned;                                      // host result blocks
     gb_batch *batch = nullptr;                              // reused: gb_batch_clear keeps its handles pooled
     std::unordered_multimap<std::string, gb_agg *> alone;   // idle handles of queries run alone, by plan shape
     std::deque<std::string> alone_order;
@@ -173,6 +191,71 @@ struct gb_server {
 };
 
 namespace {
+
+// Copy a device-resident result into pinned blocks: fixed-width columns,
+// validity words and VARCHAR offsets first, then the string bytes.
+gb_status copy_result_device(const gb_result &r, HostResult &out, PinnedPool &pool, cudaStream_t st) {
+    const u64 n = r.n_rows;
+    out.n_rows = n;
+    out.types.assign(r.types, r.types + r.n_cols);
+    out.data_p.assign(r.n_cols, nullptr);
+    out.offs_p.assign(r.n_cols, nullptr);
+    out.valid_p.assign(r.n_cols, nullptr);
+    const u64 vw = (n + 63) / 64;
+    auto take = [&](size_t bytes) -> void * {
+        PinnedPool::Block b = pool.get(std::max<size_t>(bytes, 8));
+        if (b.p) out.blocks.push_back(b);
+        return b.p;
+    };
+    for (uint32_t c = 0; c < r.n_cols; c++) {
+        uint64_t *v = (uint64_t *)take(vw * 8);
+        if (!v) return GB_ERR_OOM;
+        if (r.validity && r.validity[c]) {
+            if (vw && cudaMemcpyAsync(v, r.validity[c], vw * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+                return GB_ERR_CUDA;
+        } else {
+            for (u64 i = 0; i < vw; i++) v[i] = ~0ull;
+        }
+        out.valid_p[c] = v;
+        if (r.types[c] == GB_T_VARCHAR) {
+            int64_t *o = (int64_t *)take((n + 1) * 8);
+            if (!o) return GB_ERR_OOM;
+            if (cudaMemcpyAsync(o, r.offsets[c], (n + 1) * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+                return GB_ERR_CUDA;
+            out.offs_p[c] = o;
+        } else if (n) {
+            void *d = take(n * (u64)type_bytes(r.types[c]));
+            if (!d) return GB_ERR_OOM;
+            if (cudaMemcpyAsync(d, r.data[c], n * (u64)type_bytes(r.types[c]), cudaMemcpyDeviceToHost, st) !=
+                cudaSuccess)
+                return GB_ERR_CUDA;
+            out.data_p[c] = d;
+        }
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess) return GB_ERR_CUDA;
+    for (uint32_t c = 0; c < r.n_cols; c++) {
+        if (r.types[c] != GB_T_VARCHAR) continue;
+        const int64_t *o = out.offs_p[c];
+        const u64 nb = (u64)(o[n] - o[0]);
+        void *d = take(nb + 8);
+        if (!d) return GB_ERR_OOM;
+        if (nb && cudaMemcpyAsync(d, (const uint8_t *)r.data[c] + o[0], nb, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+            return GB_ERR_CUDA;
+        out.data_p[c] = d;
+        if (o[0]) {  // offsets relative to the copied bytes
+            int64_t *w = const_cast<int64_t *>(o);
+            const int64_t b0 = o[0];
+            for (u64 i = 0; i <= n; i++) w[i] -= b0;
+        }
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess) return GB_ERR_CUDA;
+    return GB_OK;
+}
+
+void release_result(HostResult &r, PinnedPool &pool) {
+    for (const auto &b : r.blocks) pool.put(b);
+    r.blocks.clear();
+}
 
 // The columns of rows [r0, r1) of a table (validity slices start at a
 // multiple of 64 rows; checked at submit).
@@ -242,8 +325,8 @@ void run_alone(gb_server *s, Query *q) {
         st = gb_agg_ingest(h, cols.data(), q->r1 - q->r0, GB_MEM_DEVICE, s->stream);
         if (st == GB_OK) st = gb_agg_finalize(h, s->stream);
         gb_result r{};
-        if (st == GB_OK) st = gb_agg_result(h, &r);
-        if (st == GB_OK) copy_result(r, q->res);
+        if (st == GB_OK) st = gb_agg_result_device(h, &r);
+        if (st == GB_OK) st = copy_result_device(r, q->res, s->pinned, s->stream);
         s->launches += gb_agg_kernel_launches(h);
     }
     finish(q, st, st ? gb_last_error() : nullptr);
@@ -291,8 +374,8 @@ void run_batch(gb_server *s, std::vector<Query *> &qs) {
         st = gb_batch_run(b, s->stream);
         for (size_t i = 0; i < in.size(); i++) {
             gb_result r{};
-            gb_status rs = st ? st : gb_batch_result(b, (uint32_t)i, &r);
-            if (rs == GB_OK) copy_result(r, in[i]->res);
+            gb_status rs = st ? st : gb_batch_result_device(b, (uint32_t)i, &r);
+            if (rs == GB_OK) rs = copy_result_device(r, in[i]->res, s->pinned, s->stream);
             finish(in[i], rs, rs ? gb_last_error() : nullptr);
         }
         s->launches += gb_batch_kernel_launches(b) - l0;
@@ -486,7 +569,7 @@ gb_status gb_server_result(gb_server *s, uint64_t ticket, gb_result *out) {
     out->types = r.types.data();
     out->data = r.data_p.data();
     out->offsets = r.offs_p.data();
-    out->validity = r.valid_p.data();
+    out->validity = r.valid_p.data();  // pinned blocks owned by the ticket
     return GB_OK;
 }
 
@@ -510,6 +593,7 @@ gb_status gb_server_release(gb_server *s, uint64_t ticket) {
     auto it = s->all.find(ticket);
     if (it == s->all.end()) return GB_ERR_INVALID;
     if (!it->second->done) return GB_ERR_STATE;
+    release_result(it->second->res, s->pinned);
     s->all.erase(it);
     return GB_OK;
 }
@@ -538,6 +622,7 @@ void gb_server_destroy(gb_server *s) {
     if (s->worker.joinable()) s->worker.join();
     if (s->batch) gb_batch_destroy(s->batch);
     for (auto &e : s->alone) gb_agg_destroy(e.second);
+    for (auto &e : s->all) release_result(e.second->res, s->pinned);
     if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }
