@@ -600,7 +600,7 @@ __device__ __forceinline__ u64 decode_col(const uint8_t *file, const DPage *page
 // chunk (PQ_MAXR at most; more falls back to the global run search), so a
 // row's decode searches a few shared entries instead of global arrays.
 #define PQ_MAXP 8
-#define PQ_MAXR 2048
+#define PQ_MAXR 1024
 
 
 struct PqChunkView {
@@ -661,6 +661,7 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
     constexpr int PER = PQ_CHUNK / 256;
     __shared__ PqChunkView V;
     __shared__ DRun srun[PQ_MAXR];
+    __shared__ uint32_t s_surv[8][PER * 32];  // per warp: its surviving rows
     __shared__ uint32_t s_rlo[PQ_MAXP];
     for (uint32_t ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
         const PqChunkArg ch = chunks[ci];
@@ -766,26 +767,37 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
             mine += keep[j];
         }
         }
-        u64 o = block_out_base(ctl, mine);
+        // late materialisation with full warps: each warp lists its
+        // survivors in shared memory, then decodes them 32 at a time
+        (void)mine;
+        const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+        u32 cnt = 0;
 #pragma unroll
         for (int j = 0; j < PER; j++) {
-            if (!keep[j]) continue;
-            if (o >= S.out_cap) {
+            const unsigned bm = __ballot_sync(FULL, keep[j]);
+            if (keep[j]) s_surv[wid][cnt + __popc(bm & ((1u << lane) - 1u))] = ch.row0 + (uint32_t)j * 256 + threadIdx.x;
+            cnt += __popc(bm);
+        }
+        u64 o = block_out_base(ctl, lane == 0 ? cnt : 0u);
+        o = __shfl_sync(FULL, o, 0);
+        __syncwarp();
+        for (u32 e = lane; e < cnt; e += 32) {
+            const u64 oe = o + e;
+            if (oe >= S.out_cap) {
                 atomicOr(&ctl->err, (u32)ERR_OUT_OVERFLOW);
                 continue;
             }
-            const uint32_t r = ch.row0 + (uint32_t)j * 256 + threadIdx.x;
+            const uint32_t r = s_surv[wid][e];
             for (int c = 0; c < S.n_cols; c++) {
                 const u64 x = decode_staged(file, pages, runs, page_runs, col_pages, S.n_cols, ch.rg, c, r, V, srun);
                 switch (S.out_type[c]) {
-                case GB_T_SMALLINT: ((int16_t *)S.out[c])[o] = (int16_t)(i64)x; break;
-                case GB_T_INTEGER: ((int32_t *)S.out[c])[o] = (int32_t)(i64)x; break;
-                default: ((u64 *)S.out[c])[o] = x; break;
+                case GB_T_SMALLINT: ((int16_t *)S.out[c])[oe] = (int16_t)(i64)x; break;
+                case GB_T_INTEGER: ((int32_t *)S.out[c])[oe] = (int32_t)(i64)x; break;
+                default: ((u64 *)S.out[c])[oe] = x; break;
                 }
             }
-            o++;
         }
-        __syncthreads();  // the chunk view is rebuilt for the next chunk
+        __syncthreads();  // the chunk view and survivor lists are rebuilt for the next chunk
     }
 }
 
