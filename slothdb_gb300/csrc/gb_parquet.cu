@@ -173,6 +173,13 @@ struct gb_pq_file {
     std::vector<PqPage> pages;
     uint64_t num_rows = 0;
     void *dev = nullptr;  // device copy of the file (gb_pq_upload)
+    // page index of the uploaded file, built on the GPU by the first
+    // device-resident scan and kept with the file (like Parquet's offset
+    // index): every page's descriptor and every dictionary page's run table
+    std::mutex idx_mu;
+    bool idx_ready = false;
+    void *idx_pages = nullptr, *idx_runs = nullptr, *idx_page_runs = nullptr;
+    std::vector<uint32_t> idx_col_pages;  // [(rg * n_cols + col) * 2] = {begin, end}
 };
 
 static gb_status pq_corrupt(const char *what) {
@@ -814,6 +821,99 @@ static gb_status pq_fail_if_err(Ctl &c) {
     return GB_OK;
 }
 
+// Page descriptors of row groups [rg_begin, rg_end) and the given file
+// columns (offsets relative to `base`), with run-table slots for the
+// dictionary pages; col_pages gets one {begin, end} pair per (rg, column).
+static gb_status pq_page_table(const gb_pq_file *f, uint32_t rg_begin, uint32_t rg_end, const int32_t *cols, int nc,
+                               uint64_t base, std::vector<DPage> &pages, std::vector<uint32_t> &dict_pages,
+                               std::vector<uint32_t> &col_pages, uint32_t &run_total) {
+    for (uint32_t g = rg_begin; g < rg_end; g++) {
+        for (int c = 0; c < nc; c++) {
+            const PqChunk &ch = f->chunks[g][cols[c]];
+            const PqColumn &pc = f->cols[cols[c]];
+            col_pages.push_back((uint32_t)pages.size());
+            for (uint32_t p = ch.page_begin; p < ch.page_end; p++) {
+                const PqPage &pp = f->pages[p];
+                DPage d{};
+                d.off = pp.off - base;
+                d.first_row = pp.first_row;
+                d.n_values = pp.n_values;
+                d.bytes = pp.bytes;
+                d.kind = pp.kind;
+                d.width = pc.width;
+                if (pp.kind == 1) {
+                    if (ch.dict_off < 0) {
+                        set_error("dictionary-encoded page without a dictionary page");
+                        return GB_ERR_CORRUPT;
+                    }
+                    d.dict_off = (uint64_t)ch.dict_off - base;
+                    d.dict_n = ch.dict_n;
+                    d.run_base = run_total;
+                    d.run_cap = std::min<uint32_t>(pp.n_values, pp.bytes) + 1;
+                    run_total += d.run_cap;
+                    dict_pages.push_back((uint32_t)pages.size());
+                }
+                pages.push_back(d);
+            }
+            col_pages.push_back((uint32_t)pages.size());
+        }
+    }
+    return GB_OK;
+}
+
+// Build the uploaded file's page index once: descriptors of every page and
+// the run table of every dictionary page (k_pq_runs over the whole file).
+static gb_status pq_build_index(gb_pq_file *f, cudaStream_t st) {
+    std::lock_guard<std::mutex> lk(f->idx_mu);
+    if (f->idx_ready) return GB_OK;
+    const int nfc = (int)f->cols.size();
+    std::vector<int32_t> all(nfc);
+    for (int c = 0; c < nfc; c++) all[c] = c;
+    std::vector<DPage> pages;
+    std::vector<uint32_t> dict_pages, col_pages;
+    uint32_t run_total = 0;
+    gb_status s = pq_page_table(f, 0, (uint32_t)f->rg_rows.size(), all.data(), nfc, 0, pages, dict_pages, col_pages,
+                                run_total);
+    if (s) return s;
+    void *dp = nullptr, *ctl = nullptr;
+    auto fail = [&](cudaError_t e, const char *what) {
+        for (void *p : {f->idx_pages, f->idx_runs, f->idx_page_runs, dp, ctl})
+            if (p) cudaFree(p);
+        f->idx_pages = f->idx_runs = f->idx_page_runs = nullptr;
+        (void)cudaGetLastError();
+        return cuda_fail(e, what);
+    };
+    cudaError_t e;
+    if ((e = cudaMalloc(&f->idx_pages, std::max<size_t>(pages.size() * sizeof(DPage), 16))) ||
+        (e = cudaMalloc(&f->idx_runs, (size_t)run_total * sizeof(DRun) + 16)) ||
+        (e = cudaMalloc(&f->idx_page_runs, pages.size() * 8 + 16)) ||
+        (e = cudaMalloc(&dp, dict_pages.size() * 4 + 16)) || (e = cudaMalloc(&ctl, sizeof(Ctl))))
+        return fail(e, "cudaMalloc (Parquet page index)");
+    if ((e = cudaMemcpyAsync(f->idx_pages, pages.data(), pages.size() * sizeof(DPage), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(dp, dict_pages.data(), dict_pages.size() * 4, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemsetAsync(ctl, 0, sizeof(Ctl), st)))
+        return fail(e, "cudaMemcpy (Parquet page index)");
+    if (!dict_pages.empty()) {
+        k_pq_runs<<<(unsigned)dict_pages.size(), 128, 0, st>>>((const uint8_t *)f->dev, (const DPage *)f->idx_pages,
+                                                               (const uint32_t *)dp, (DRun *)f->idx_runs,
+                                                               (uint32_t *)f->idx_page_runs, (Ctl *)ctl);
+        if ((e = cudaGetLastError())) return fail(e, "k_pq_runs");
+    }
+    Ctl c;
+    if ((e = cudaMemcpyAsync(&c, ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st)) || (e = cudaStreamSynchronize(st)))
+        return fail(e, "k_pq_runs");
+    cudaFree(dp);
+    cudaFree(ctl);
+    if ((s = pq_fail_if_err(c))) {
+        for (void *p : {f->idx_pages, f->idx_runs, f->idx_page_runs}) cudaFree(p);
+        f->idx_pages = f->idx_runs = f->idx_page_runs = nullptr;
+        return s;
+    }
+    f->idx_col_pages.swap(col_pages);
+    f->idx_ready = true;
+    return GB_OK;
+}
+
 extern "C" {
 
 gb_status gb_pq_open(const uint8_t *bytes, uint64_t size, gb_pq_file **out) {
@@ -870,6 +970,8 @@ gb_status gb_pq_upload(gb_pq_file *f, void *stream) {
 void gb_pq_close(gb_pq_file *f) {
     if (!f) return;
     if (f->dev) cudaFree(f->dev);
+    for (void *p : {f->idx_pages, f->idx_runs, f->idx_page_runs})
+        if (p) cudaFree(p);
     delete f;
 }
 
@@ -995,70 +1097,63 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
         dfile = (const uint8_t *)S->file_dev;
         base = lo;
     }
-    // page table of the batch (offsets relative to dfile)
-    std::vector<DPage> pages;
-    std::vector<uint32_t> dict_pages, col_pages;
     std::vector<PqChunkArg> chunks;
     uint64_t rows = 0;
-    uint32_t run_total = 0;
     for (uint32_t g = rg_begin; g < rg_end; g++) {
-        for (int c = 0; c < nc; c++) {
-            const PqChunk &ch = f->chunks[g][col_map[c]];
-            const PqColumn &pc = f->cols[col_map[c]];
-            col_pages.push_back((uint32_t)pages.size());
-            for (uint32_t p = ch.page_begin; p < ch.page_end; p++) {
-                const PqPage &pp = f->pages[p];
-                DPage d{};
-                d.off = pp.off - base;
-                d.first_row = pp.first_row;
-                d.n_values = pp.n_values;
-                d.bytes = pp.bytes;
-                d.kind = pp.kind;
-                d.width = pc.width;
-                if (pp.kind == 1) {
-                    if (ch.dict_off < 0) {
-                        set_error("dictionary-encoded page without a dictionary page");
-                        return GB_ERR_CORRUPT;
-                    }
-                    d.dict_off = (uint64_t)ch.dict_off - base;
-                    d.dict_n = ch.dict_n;
-                    d.run_base = run_total;
-                    d.run_cap = std::min<uint32_t>(pp.n_values, pp.bytes) + 1;
-                    run_total += d.run_cap;
-                    dict_pages.push_back((uint32_t)pages.size());
-                }
-                pages.push_back(d);
-            }
-            col_pages.push_back((uint32_t)pages.size());
-        }
         for (uint64_t r0 = 0; r0 < f->rg_rows[g]; r0 += PQ_CHUNK)
             chunks.push_back({g - rg_begin, (uint32_t)r0, (uint32_t)std::min<uint64_t>(PQ_CHUNK, f->rg_rows[g] - r0)});
         rows += f->rg_rows[g];
     }
-    if ((s = grow(S->pages, S->pages_cap, pages.size() * sizeof(DPage))) ||
-        (s = grow(S->runs, S->runs_cap, (size_t)run_total * sizeof(DRun) + 16)) ||
-        (s = grow(S->page_runs, S->page_runs_cap, pages.size() * 8 + 16)) ||
-        (s = grow(S->dict_pages, S->dict_pages_cap, dict_pages.size() * 4 + 16)) ||
-        (s = grow(S->col_pages, S->col_pages_cap, col_pages.size() * 4)) ||
-        (s = grow(S->chunks, S->chunks_cap, chunks.size() * sizeof(PqChunkArg))) ||
+    const void *d_pages, *d_runs, *d_page_runs;
+    std::vector<uint32_t> col_pages;
+    if ((s = grow(S->chunks, S->chunks_cap, chunks.size() * sizeof(PqChunkArg) + 16)) ||
         (s = grow(S->ctl, S->ctl_cap, sizeof(Ctl))))
         return s;
-    GB_CUDA(cudaMemcpyAsync(S->pages, pages.data(), pages.size() * sizeof(DPage), cudaMemcpyHostToDevice, st));
-    GB_CUDA(cudaMemcpyAsync(S->col_pages, col_pages.data(), col_pages.size() * 4, cudaMemcpyHostToDevice, st));
-    GB_CUDA(cudaMemcpyAsync(S->chunks, chunks.data(), chunks.size() * sizeof(PqChunkArg), cudaMemcpyHostToDevice, st));
-    if (!dict_pages.empty())
-        GB_CUDA(cudaMemcpyAsync(S->dict_pages, dict_pages.data(), dict_pages.size() * 4, cudaMemcpyHostToDevice, st));
     GB_CUDA(cudaMemsetAsync(S->ctl, 0, sizeof(Ctl), st));
     Ctl *dctl = (Ctl *)S->ctl;
-    if (!dict_pages.empty()) {
-        gb_prof_mark *pm = gb_agg_prof_begin(h, "k_pq_runs", st);
-        k_pq_runs<<<(unsigned)dict_pages.size(), 128, 0, st>>>(dfile, (const DPage *)S->pages,
-                                                               (const uint32_t *)S->dict_pages, (DRun *)S->runs,
-                                                               (uint32_t *)S->page_runs, dctl);
-        gb_agg_prof_end(h, pm, st);
-        GB_CUDA(cudaGetLastError());
-        gb_agg_count_launch(h, 1);
+    if (mem == GB_MEM_DEVICE) {
+        // the resident file's page index (built once), columns picked per call
+        if ((s = pq_build_index(f, st))) return s;
+        const int nfc = (int)f->cols.size();
+        for (uint32_t g = rg_begin; g < rg_end; g++)
+            for (int c = 0; c < nc; c++) {
+                col_pages.push_back(f->idx_col_pages[2 * (g * nfc + col_map[c])]);
+                col_pages.push_back(f->idx_col_pages[2 * (g * nfc + col_map[c]) + 1]);
+            }
+        d_pages = f->idx_pages;
+        d_runs = f->idx_runs;
+        d_page_runs = f->idx_page_runs;
+    } else {
+        // this batch's page table (offsets relative to its byte range) and runs
+        std::vector<DPage> pages;
+        std::vector<uint32_t> dict_pages;
+        uint32_t run_total = 0;
+        if ((s = pq_page_table(f, rg_begin, rg_end, col_map, nc, base, pages, dict_pages, col_pages, run_total)))
+            return s;
+        if ((s = grow(S->pages, S->pages_cap, pages.size() * sizeof(DPage) + 16)) ||
+            (s = grow(S->runs, S->runs_cap, (size_t)run_total * sizeof(DRun) + 16)) ||
+            (s = grow(S->page_runs, S->page_runs_cap, pages.size() * 8 + 16)) ||
+            (s = grow(S->dict_pages, S->dict_pages_cap, dict_pages.size() * 4 + 16)))
+            return s;
+        GB_CUDA(cudaMemcpyAsync(S->pages, pages.data(), pages.size() * sizeof(DPage), cudaMemcpyHostToDevice, st));
+        if (!dict_pages.empty()) {
+            GB_CUDA(cudaMemcpyAsync(S->dict_pages, dict_pages.data(), dict_pages.size() * 4, cudaMemcpyHostToDevice,
+                                    st));
+            gb_prof_mark *pm = gb_agg_prof_begin(h, "k_pq_runs", st);
+            k_pq_runs<<<(unsigned)dict_pages.size(), 128, 0, st>>>(dfile, (const DPage *)S->pages,
+                                                                   (const uint32_t *)S->dict_pages, (DRun *)S->runs,
+                                                                   (uint32_t *)S->page_runs, dctl);
+            gb_agg_prof_end(h, pm, st);
+            GB_CUDA(cudaGetLastError());
+            gb_agg_count_launch(h, 1);
+        }
+        d_pages = S->pages;
+        d_runs = S->runs;
+        d_page_runs = S->page_runs;
     }
+    if ((s = grow(S->col_pages, S->col_pages_cap, col_pages.size() * 4 + 16))) return s;
+    GB_CUDA(cudaMemcpyAsync(S->col_pages, col_pages.data(), col_pages.size() * 4, cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync(S->chunks, chunks.data(), chunks.size() * sizeof(PqChunkArg), cudaMemcpyHostToDevice, st));
     // compacted output columns (batch rows bound the survivors)
     if (S->out_cap_rows < rows) {
         for (int c = 0; c < GB_MAX_COLS; c++)
@@ -1089,8 +1184,8 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
     {
         const int grid = (int)std::min<size_t>(chunks.size(), (size_t)sm_count() * 8);
         gb_prof_mark *pm = gb_agg_prof_begin(h, "k_pq_scan", st);
-        k_pq_scan<<<std::max(grid, 1), 256, 0, st>>>(dfile, (const DPage *)S->pages, (const DRun *)S->runs,
-                                                     (const uint32_t *)S->page_runs, (const uint32_t *)S->col_pages,
+        k_pq_scan<<<std::max(grid, 1), 256, 0, st>>>(dfile, (const DPage *)d_pages, (const DRun *)d_runs,
+                                                     (const uint32_t *)d_page_runs, (const uint32_t *)S->col_pages,
                                                      (const PqChunkArg *)S->chunks, (uint32_t)chunks.size(), P, dctl);
         gb_agg_prof_end(h, pm, st);
         GB_CUDA(cudaGetLastError());
