@@ -9,28 +9,28 @@
 //   S  sample:  a strided sample of the keys is counted; the NH most frequent
 //               keys become "hot" (dense hot index), the NSUP most frequent of
 //               them "super-hot".
-//   P1 scatter: persistent CTAs stream the rows.  A super-hot row is folded
-//               into its warp's PRIVATE state (warp pre-combine + plain
-//               read-modify-write); a warm hot row is forwarded through a
-//               shared-memory inbox to the warp that owns its hot index, which
-//               folds it without atomics; any other row is appended as a
-//               (key, values) tuple to partition p = top hash bits, into a
-//               per-CTA lease of that partition's region (one global atomic
-//               per lease of RADIX_LEASE tuples).
-//   P2 agg:     one CTA per partition; its shared table is split into 32
-//               sub-tables, one per warp, and each tuple is forwarded to the
-//               warp owning its key, so state words are updated without
-//               atomics.
+//   P1 scatter: persistent CTAs (32 warps, 4 rows per thread per tile) stream
+//               the rows.  A row of one of the REG_HOT hottest keys is folded
+//               into per-lane registers; a super-hot row into its warp's
+//               private shared state; another hot row into the CTA's shared
+//               state (shared atomics); any other row is appended as a (key,
+//               values) tuple to partition p = top hash bits through a
+//               per-CTA write-combining buffer of wcb tuples per partition,
+//               flushed in aligned groups (one global atomic per flush).
+//               Partition regions have per-partition capacities; a region
+//               that overflows is grown (and its tuples moved) by the host,
+//               and a re-execution keeps the grown capacities.
+//   P2 agg:     one CTA per partition: a shared open-addressing table, a warp
+//               pre-combine of equal keys (32-bit hash match checked on the
+//               full key), shared atomics; a table that overflows folds the
+//               rest into the HBM hash table.
 //   P3 hot:     per-CTA hot partials are reduced in a fixed order (hence a
 //               deterministic DOUBLE sum for hot keys) and emitted.
 //
-// Shared-memory 64-bit atomics are avoided on every hot path: on sm_103a
-// they are compare-and-swap loops that collapse under the Zipf head's
-// contention, while 32-bit shared atomics are native.  A key is hot for the
-// whole query or never, and lives in exactly one partition and one warp's
-// sub-table, so every group is emitted exactly once.  Bounded probes fall back
-// to the HBM hash table (emitted by the compaction kernel), which keeps the
-// result exact for any key distribution.
+// A key is hot for the whole query or never, and lives in exactly one
+// partition, so every group is emitted exactly once.  Bounded probes fall
+// back to the HBM hash table (emitted by the compaction kernel), which keeps
+// the result exact for any key distribution.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -352,7 +352,6 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
             pslot[j] = 0;
             bool act = acts[j];
             if (!SPEC && act && P.n_filters) act = pass_filters(P, r);
-            bool priv = false;
             u32 hidx = 0;
             u64 v[NOPS > 0 ? NOPS : 1];
 #pragma unroll
@@ -422,7 +421,6 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
                     }
                 }
             }
-            (void)priv;
         }
         __syncthreads();
         // flush full buffers: whole multiples of B tuples, aligned
@@ -803,8 +801,6 @@ gb_status radix_prepare(const Plan &P, RadixPlan &R, u64 est_groups, u64 nullabl
         } else if (R.pbits > 6) R.pbits--;
         else return GB_ERR_UNSUPPORTED;
     }
-    R.qcap = 0;
-    R.qcap2 = 0;
     return GB_OK;
 }
 

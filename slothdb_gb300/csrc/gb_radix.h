@@ -10,7 +10,6 @@
 #define P1_WARPS 32   // P1 block = 1024 threads (64 registers each: 32 warps per SM)
 #define REG_HOT 4     // hottest keys accumulated in per-lane registers
 #define RADIX_BLOCK 1024
-#define RADIX_LEASE 16   // tuples per partition lease (one global atomic each)
 #define CURSOR_PAD 32    // partition cursors 128 bytes apart (spread over L2 slices)
 #define HIST_BINS 1024   // sample-count histogram bins
 
@@ -25,8 +24,6 @@ struct RadixPlan {
     int32_t HS;                         // hot hash-table slots (power of two)
     int32_t nh;                         // hot keys (dense indices [0, nh))
     int32_t nsup;                       // super-hot keys: indices [0, nsup)
-    int32_t qcap;                       // P1 warm inbox entries per warp
-    int32_t qcap2;                      // P2 inbox entries per warp
     int32_t sub;                        // P2 shared-table slots (power of two)
     int32_t wcb;                        // P1 write-combining tuples per partition
     int32_t hot_probe;
