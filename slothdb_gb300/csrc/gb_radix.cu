@@ -246,10 +246,10 @@ __device__ __forceinline__ void store_at(const RadixRef &X, const TableRef &T, u
 }
 
 // ------------------------------------------------------------- P1 scatter
-// Block: P1_WARPS warps, ROWS rows per thread per tile.  The NPRIV hottest
-// keys have a private state per warp (u32 count + W-1 words, plain updates
-// after a warp pre-combine); the other hot keys share one state per CTA
-// (native u32 count atomics; their word atomics are rarely contended).
+// Block: P1_WARPS warps, ROWS rows per thread per tile.  The REG_HOT hottest
+// keys accumulate in per-lane registers; the next NPRIV - REG_HOT have a
+// private state per warp (u32 count + W-1 words; only this warp's lanes
+// contend on its atomics); the other hot keys share one state per CTA.
 // SPEC != 0: the plan is one non-NULL BIGINT key, one non-NULL value column,
 // one op (SPEC = OP_ADD_F or OP_ADD_I) and no predicates — every per-row plan
 // interpretation (key packing, type and op switches) is compiled away.
