@@ -291,6 +291,7 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
     __syncthreads();
     u32 *mypc = pc + warp * NPRIV;
     u64 *mypw = pw + (size_t)warp * NPRIV * WM;
+    u64 *hpart = X.hot_part + (u64)blockIdx.x * NH * W;  // this CTA's hot slice (identity-initialised)
     // the REG_HOT hottest keys accumulate in this lane's registers: no
     // conflicts, no warp collectives
     constexpr int NV = NOPS > 0 ? NOPS : 1;
@@ -394,19 +395,30 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
                                         rw[k][i] = op_combine(SPEC ? SPEC : P.ops[i].kind, rw[k][i], v[i]);
                                 }
                             }
+                        } else if (SPEC) {
+                            // the count stays in shared memory (native 32-bit
+                            // atomics); the sum is a fire-and-forget reduction
+                            // into this CTA's hot slice in L2 (native 64-bit
+                            // adds there; a shared 64-bit atomic would be a
+                            // compare-and-swap loop)
+                            if ((int)hidx < NPRIV) atomicAdd(&mypc[hidx], 1u);
+                            else atomicAdd(&sc[hidx - NPRIV], 1u);
+                            u64 *hw = hpart + (size_t)hidx * W + P.ops[0].word;
+                            if (SPEC == OP_ADD_F) atomicAdd((double *)hw, __longlong_as_double((i64)v[0]));
+                            else atomicAdd((unsigned long long *)hw, (unsigned long long)v[0]);
                         } else if ((int)hidx < NPRIV) {
                             // warp-private state: only lanes of this warp contend
                             atomicAdd(&mypc[hidx], 1u);
 #pragma unroll
                             for (int i = 0; i < NOPS; i++)
-                                op_apply(SPEC ? SPEC : P.ops[i].kind, mypw + (size_t)hidx * WM + (P.ops[i].word - 1),
-                                         v[i], P.word_init[P.ops[i].word]);
+                                op_apply(P.ops[i].kind, mypw + (size_t)hidx * WM + (P.ops[i].word - 1), v[i],
+                                         P.word_init[P.ops[i].word]);
                         } else {
                             const u32 wi = hidx - NPRIV;
                             atomicAdd(&sc[wi], 1u);
 #pragma unroll
                             for (int i = 0; i < NOPS; i++)
-                                op_apply(SPEC ? SPEC : P.ops[i].kind, sw + (size_t)wi * WM + (P.ops[i].word - 1), v[i],
+                                op_apply(P.ops[i].kind, sw + (size_t)wi * WM + (P.ops[i].word - 1), v[i],
                                          P.word_init[P.ops[i].word]);
                         }
                     } else {
@@ -486,8 +498,13 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
         }
     }
     __syncthreads();
-    // fold private and shared hot states into this CTA's slice
-    u64 *hp = X.hot_part + (u64)blockIdx.x * NH * W;
+    // fold private and shared hot states into this CTA's slice (after the
+    // slice's L2 reductions of the specialised kernel are visible)
+    if (SPEC) {
+        __threadfence();
+        __syncthreads();
+    }
+    u64 *hp = hpart;
     for (int i = threadIdx.x; i < NH; i += NT) {
         u64 acc[GB_MAX_WORDS];
         for (int w = 0; w < W; w++) acc[w] = hp[(size_t)i * W + w];
