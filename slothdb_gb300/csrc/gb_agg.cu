@@ -465,6 +465,7 @@ struct gb_agg {
     DevBuf r_skeys, r_scnt, r_hist, r_hot_keys, r_hot_part, r_cursor, r_part, r_part2, r_ovf;
     DevBuf r_off, r_cap, r_off2, r_cap2;    // per-partition region start / capacity (device)
     DevBuf r_hot_idx, r_hot_list, r_hstate;
+    DevBuf r_p2w;                           // P2 state words folded in L2 (plans whose ops are all DOUBLE SUM)
     std::vector<u64> h_off;                 // host copies
     std::vector<u32> h_capv;
     u64 r_cap_p = 0;
@@ -768,6 +769,7 @@ static RadixRef radix_ref(gb_agg *h) {
     X.hot_idx = (const uint16_t *)h->r_hot_idx.p;
     X.hot_list = (const u64 *)h->r_hot_list.p;
     X.hot_part = (u64 *)h->r_hot_part.p;
+    X.p2_words = nullptr;
     return X;
 }
 
@@ -959,6 +961,10 @@ static gb_status radix_emit(gb_agg *h, cudaStream_t st) {
     if (h->r_ready) {
         TableRef T = table_ref(h);
         RadixRef X = radix_ref(h);
+        if (radix_p2_global_words(h->plan, R)) {
+            if ((s = h->r_p2w.ensure((size_t)np * R.sub * (h->plan.words - 1) * 8))) return s;
+            X.p2_words = (u64 *)h->r_p2w.p;
+        }
         {
             ProfScope ps(h, "k_part_agg", st);
             if ((s = radix_launch_p2(h->plan, R, X, T, E, st))) return s;
@@ -1812,7 +1818,7 @@ void gb_agg_destroy(gb_agg *h) {
     h->host_str_bytes.release();
     for (DevBuf *b : {&h->r_skeys, &h->r_scnt, &h->r_hist, &h->r_hot_keys, &h->r_hot_part, &h->r_cursor, &h->r_part,
                       &h->r_part2, &h->r_ovf, &h->r_off, &h->r_cap, &h->r_off2, &h->r_cap2, &h->r_hot_idx,
-                      &h->r_hot_list, &h->r_hstate})
+                      &h->r_hot_list, &h->r_hstate, &h->r_p2w})
         b->release();
     h->topn_ids_a.release();
     h->topn_ids_b.release();

@@ -553,8 +553,10 @@ __global__ void k_fill_u64(u64 *dst, u64 n, u64 value) {
 // One CTA per partition: a shared open-addressing table (u64 keys, u32
 // counts, W-1 state words).  Warps pre-combine duplicate keys, then fold with
 // native u32 count atomics and (rarely contended) word atomics; no barriers
-// in the main loop.
-template <int VV, int NOPS>
+// in the main loop.  GW: every op is a DOUBLE SUM, whose shared-memory atomic
+// is a compare-and-swap loop; the state words then live in the partition's
+// slice of X.p2_words (L2-resident) and fold as fire-and-forget L2 reductions.
+template <int VV, int NOPS, bool GW>
 __global__ void __launch_bounds__(RADIX_BLOCK, 1)
     k_part_agg(const __grid_constant__ Plan P, const __grid_constant__ RadixPlan R, const RadixRef X,
                const TableRef T, const __grid_constant__ EmitArgs E, int SP) {
@@ -563,9 +565,9 @@ __global__ void __launch_bounds__(RADIX_BLOCK, 1)
     constexpr int NV = NOPS > 0 ? NOPS : 1;
     const int W = P.words, WM = W - 1;
     const int lane = threadIdx.x & 31;
-    u64 *keys = rsm;                          // [SP]
-    u64 *wd = keys + SP;                      // [SP][WM]
-    u32 *cn = (u32 *)(wd + (size_t)SP * WM);  // [SP]
+    u64 *keys = rsm;  // [SP]
+    u64 *wd = GW ? X.p2_words + (size_t)blockIdx.x * SP * WM : keys + SP;  // [SP][WM]
+    u32 *cn = GW ? (u32 *)(keys + SP) : (u32 *)(wd + (size_t)SP * WM);   // [SP]
     __shared__ u32 s_new;
     for (int i = threadIdx.x; i < SP; i += blockDim.x) {
         keys[i] = EMPTY_KEY;
@@ -670,6 +672,7 @@ __global__ void __launch_bounds__(RADIX_BLOCK, 1)
         }
         if (!done) global_fold_n<NOPS>(P, T, pk, cnt, v, &s_new);
     }
+    if (GW) __threadfence();  // the reductions reach L2 before the emit reads them
     __syncthreads();
     // emit: one output reservation per CTA
     u32 mine = 0;
@@ -683,7 +686,7 @@ __global__ void __launch_bounds__(RADIX_BLOCK, 1)
         }
         u64 w[GB_MAX_WORDS];
         w[0] = cn[s];
-        for (int q = 0; q < WM; q++) w[1 + q] = wd[(size_t)s * WM + q];
+        for (int q = 0; q < WM; q++) w[1 + q] = GW ? __ldcg(wd + (size_t)s * WM + q) : wd[(size_t)s * WM + q];
         emit_group(P, E, o, keys[s], false, w);
         o++;
     }
@@ -754,6 +757,13 @@ size_t radix_p1_smem(const Plan &P, const RadixPlan &R) {
 size_t radix_p2_smem(const Plan &P, const RadixPlan &R) {
     const size_t WM = P.words - 1, SP = (size_t)R.sub;
     return SP * 8 + SP * WM * 8 + SP * 4;
+}
+
+bool radix_p2_global_words(const Plan &P, const RadixPlan &R) {
+    if (P.n_ops < 1 || P.n_ops > 2 || R.V != 1) return false;
+    for (int i = 0; i < P.n_ops; i++)
+        if (P.ops[i].kind != OP_ADD_F) return false;
+    return true;
 }
 
 u32 radix_tile_rows(const RadixPlan &R) { return (u32)((R.V == 3 ? RADIX_ROWS / 2 : RADIX_ROWS) * P1_WARPS * 32); }
@@ -868,7 +878,7 @@ static void p1_table(P1Fn *t) {
 }
 template <int VV, int NOPS>
 static void p2_table(P2Fn *t) {
-    t[VV * (RADIX_MAX_OPS + 1) + NOPS] = (P2Fn)k_part_agg<VV, NOPS>;
+    t[VV * (RADIX_MAX_OPS + 1) + NOPS] = (P2Fn)k_part_agg<VV, NOPS, false>;
 }
 
 template <int VV>
@@ -880,6 +890,7 @@ static void fill_tables(P1Fn *t1, P2Fn *t2) {
 static P1Fn g_p1[4 * (RADIX_MAX_OPS + 1)];
 static P2Fn g_p2[4 * (RADIX_MAX_OPS + 1)];
 static P1Fn g_p1_spec_f, g_p1_spec_i;  // specialised P1: BIGINT key, one SUM (DOUBLE / integer)
+static P2Fn g_p2_gw[RADIX_MAX_OPS + 1];  // P2 with the state words in L2 (ops all DOUBLE SUM), one value column
 
 // The specialised P1 applies: one non-NULL BIGINT key, one non-NULL value
 // column, one ADD op, no predicates.
@@ -900,8 +911,12 @@ static gb_status radix_set_attributes() {
     fill_tables<3>(g_p1, g_p2);
     g_p1_spec_f = (P1Fn)k_partition<RADIX_ROWS, 1, 1, OP_ADD_F>;
     g_p1_spec_i = (P1Fn)k_partition<RADIX_ROWS, 1, 1, OP_ADD_I>;
+    g_p2_gw[1] = (P2Fn)k_part_agg<1, 1, true>;
+    g_p2_gw[2] = (P2Fn)k_part_agg<1, 2, true>;
     for (P1Fn f : {g_p1_spec_f, g_p1_spec_i})
         if (gb_status s = allow_max_smem(f)) return s;
+    for (int o = 1; o <= 2; o++)
+        if (gb_status s = allow_max_smem(g_p2_gw[o])) return s;
     for (int v = 1; v <= 3; v++)
         for (int o = 0; o <= RADIX_MAX_OPS; o++) {
             gb_status s;
@@ -936,9 +951,13 @@ gb_status radix_launch_p2(const Plan &P, const RadixPlan &R, const RadixRef &X, 
                           cudaStream_t st) {
     gb_status s = radix_set_attributes();
     if (s) return s;
-    const size_t smem = radix_p2_smem(P, R);
+    size_t smem = radix_p2_smem(P, R);
     const int np = 1 << R.pbits;
     P2Fn f = g_p2[R.V * (RADIX_MAX_OPS + 1) + P.n_ops];
+    if (X.p2_words && radix_p2_global_words(P, R)) {
+        f = g_p2_gw[P.n_ops];
+        smem = (size_t)R.sub * 12;
+    }
     f<<<np, RADIX_BLOCK, smem, st>>>(P, R, X, T, E, R.sub);
     GB_CUDA(cudaGetLastError());
     return GB_OK;

@@ -42,6 +42,7 @@ struct RadixRef {
     const uint16_t *hot_idx;  // HS dense hot index
     const u64 *hot_list;      // nh keys by hot index
     u64 *hot_part;            // [grid][nh][words] per-CTA hot partials
+    u64 *p2_words;            // [np][sub][words - 1] P2 state words when they fold in L2 (or null)
 };
 
 struct RadixTile {
@@ -54,6 +55,7 @@ gb_status radix_prepare(const Plan &P, RadixPlan &R, u64 est_groups, u64 nullabl
 size_t radix_p1_smem(const Plan &P, const RadixPlan &R);
 gb_status radix_set_bits(const Plan &P, RadixPlan &R, int bits);
 size_t radix_p2_smem(const Plan &P, const RadixPlan &R);
+bool radix_p2_global_words(const Plan &P, const RadixPlan &R);
 u32 radix_tile_rows(const RadixPlan &R);
 gb_status radix_launch_sample(const Plan &P, const RadixPlan &R, u64 n, u64 *skeys, u32 *scnt, u64 scap, u32 *hist,
                               u32 *hstate, u64 *hot_keys, uint16_t *hot_idx, u64 *hot_list, cudaStream_t st,
