@@ -1892,6 +1892,12 @@ gb_status gb_agg_set_option(gb_agg *h, const char *name, int64_t value) {
             set_error("radix_bits must be 6..12 and fit the partition pass's shared memory");
             return s;
         }
+    } else if (n == "radix_precombine") {
+        if (h->mode != 1 || value < 0 || value > 1) {
+            set_error("radix_precombine applies to radix mode only and is 0 or 1");
+            return GB_ERR_INVALID;
+        }
+        h->rplan.p2_pre = (int)value;
     } else if (n == "hot_slots") {
         if (h->mode != 1 || value < 64 || value > h->rplan.HS || (value & (value - 1))) return GB_ERR_INVALID;
         h->rplan.HS = (int)value;

@@ -40,12 +40,6 @@
 
 namespace gb {
 
-// P2 pre-combines equal keys within a warp before folding (1) or folds
-// every tuple on its own (0).
-#ifndef P2_PRECOMBINE
-#define P2_PRECOMBINE 1
-#endif
-
 __device__ __forceinline__ u32 part_of(u64 h, int pbits) { return pbits ? (u32)(h >> (64 - pbits)) : 0u; }
 __device__ __forceinline__ u32 hot_slot(u64 h, int HS) { return (u32)h & (u32)(HS - 1); }
 __device__ __forceinline__ u32 agg_slot(u64 h, int SP) { return (u32)(h >> 20) & (u32)(SP - 1); }
@@ -600,7 +594,7 @@ __global__ void __launch_bounds__(RADIX_BLOCK, 1)
             }
         }
         const u64 hh = mix64(pk);
-        if (!P2_PRECOMBINE) {
+        if (!R.p2_pre) {
             // tail keys rarely repeat within 32 consecutive tuples: fold each
             // tuple on its own
             if (!act) continue;
@@ -799,6 +793,8 @@ gb_status radix_prepare(const Plan &P, RadixPlan &R, u64 est_groups, u64 nullabl
         R.sub = sp;
     }
     R.agg_probe = 64;
+    // a table whose words fold in L2 takes repeated keys cheaply: no pre-combine
+    R.p2_pre = radix_p2_global_words(P, R) ? 0 : 1;
     // partitions so that a partition's groups fill its table to <= ~0.7
     const u64 per_part = (u64)sp * 7 / 10;
     u64 np = pow2_at_least(std::max<u64>((est_groups + per_part - 1) / per_part, 64));

@@ -28,6 +28,7 @@ struct RadixPlan {
     int32_t wcb;                        // P1 write-combining tuples per partition
     int32_t hot_probe;
     int32_t agg_probe;
+    int32_t p2_pre;                     // P2: warps pre-combine equal keys (1) or fold each tuple (0)
 };
 
 struct RadixRef {

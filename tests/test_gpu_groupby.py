@@ -15,10 +15,11 @@ REL_TOL = 1e-12
 
 
 def run_gpu(col_types, group_cols, aggs, cols, filters=(), nulls=None, est_groups=0, device=False,
-            chunks=None, topn=None, mode=0):
+            chunks=None, topn=None, mode=0, options=None):
     nullable = [i for i, m in enumerate(nulls or []) if m is not None]
+    opts = dict({"mode": mode} if mode else {}, **(options or {}))
     g = capi.GroupBy(col_types, group_cols, aggs, filters=filters, nullable=nullable, est_groups=est_groups,
-                     options={"mode": mode} if mode else None)
+                     options=opts or None)
     if mode == 2:
         assert g.mode() == 1
     try:
@@ -139,6 +140,26 @@ def test_zipf_double_sum_avg_tolerance(mode):
     k, x = datagen.zipf(2_000_000, seed=1, n_values=400_000)
     err, gpu, orc = check([BIGINT, DOUBLE], [0], [("count_star", -1), ("sum", 1), ("avg", 1)], [k, x],
                           est_groups=400_000, mode=mode)
+    assert err <= REL_TOL
+
+
+@pytest.mark.parametrize("pre", [0, 1])
+@pytest.mark.parametrize("vtype", [DOUBLE, BIGINT])
+def test_radix_partition_pass_with_and_without_precombine(vtype, pre):
+    """The per-partition pass folds repeated tail keys with the warp
+    pre-combine and tuple by tuple (DOUBLE SUM words fold in L2, BIGINT SUM
+    words in shared memory); a WHERE clause takes the generic partition pass."""
+    k, x = datagen.zipf(2_000_000, seed=5, n_values=400_000)
+    if vtype == BIGINT:
+        # per-group sums stay below 2^53, where the reference's double
+        # accumulation is exact
+        x = np.random.default_rng(5).integers(-10**6, 10**6, len(k), dtype=np.int64)
+    aggs = [("count_star", -1), ("sum", 1), ("avg", 1)]
+    opts = {"radix_precombine": pre}
+    err, _, _ = check([BIGINT, vtype], [0], aggs, [k, x], est_groups=400_000, mode=RADIX, options=opts)
+    assert err <= REL_TOL
+    err, _, _ = check([BIGINT, vtype], [0], aggs, [k, x], est_groups=400_000, mode=RADIX, options=opts,
+                      filters=[(1, ">", 0)], device=True)
     assert err <= REL_TOL
 
 
