@@ -52,15 +52,23 @@ typedef enum gb_type {
 
 /* Aggregates the binder resolves for GROUP BY
  * (src/binder/binder.cpp:1345-1391): COUNT → BIGINT; SUM(int) → BIGINT;
- * SUM(double) → DOUBLE; AVG → DOUBLE; MIN/MAX → input type. */
+ * SUM(double) → DOUBLE; AVG → DOUBLE; MIN/MAX → input type.
+ * COUNT(DISTINCT col) → BIGINT: the number of distinct non-NULL values of an
+ * integer column in the group (the per-group value sets of
+ * src/execution/int_group_agg.cpp:89-92, union sizes at 154-270); 0 for a
+ * group whose values are all NULL.  It runs in hash mode only (not radix,
+ * not gb_batch_*); at most GB_MAX_DISTINCT distinct columns per query. */
 typedef enum gb_agg_kind {
     GB_AGG_COUNT_STAR = 0,
     GB_AGG_COUNT = 1,
     GB_AGG_SUM = 2,
     GB_AGG_AVG = 3,
     GB_AGG_MIN = 4,
-    GB_AGG_MAX = 5
+    GB_AGG_MAX = 5,
+    GB_AGG_COUNT_DISTINCT = 6
 } gb_agg_kind;
+
+#define GB_MAX_DISTINCT 2
 
 /* Comparison of a SimplePredicate (src/execution/physical_planner.cpp:110-135). */
 typedef enum gb_cmp {

@@ -21,9 +21,10 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
 SMALLINT, INTEGER, BIGINT, DOUBLE, VARCHAR = 1, 2, 3, 4, 5
-COUNT_STAR, COUNT, SUM, AVG, MIN, MAX = 0, 1, 2, 3, 4, 5
+COUNT_STAR, COUNT, SUM, AVG, MIN, MAX, COUNT_DISTINCT = 0, 1, 2, 3, 4, 5, 6
 NP_TYPES = {SMALLINT: np.int16, INTEGER: np.int32, BIGINT: np.int64, DOUBLE: np.float64}
-AGG_NAMES = {"count_star": COUNT_STAR, "count": COUNT, "sum": SUM, "avg": AVG, "min": MIN, "max": MAX}
+AGG_NAMES = {"count_star": COUNT_STAR, "count": COUNT, "sum": SUM, "avg": AVG, "min": MIN, "max": MAX,
+             "count_distinct": COUNT_DISTINCT}
 CMP_NAMES = {"==": 0, "=": 0, "!=": 1, "<>": 1, "<": 2, "<=": 3, ">": 4, ">=": 5}
 
 _lib = None
@@ -59,7 +60,7 @@ def _p(a):
 
 def agg_out_type(kind, in_type):
     """Binder return type (src/binder/binder.cpp:1345-1391)."""
-    if kind in (COUNT_STAR, COUNT):
+    if kind in (COUNT_STAR, COUNT, COUNT_DISTINCT):
         return BIGINT
     if kind == SUM:
         return DOUBLE if in_type == DOUBLE else BIGINT

@@ -23,6 +23,10 @@
  *      (TLSingle): src/execution/physical_planner.cpp:7613-7931, 7871-7908
  *  - RLE/bit-packed hybrid decoding: src/storage/parquet.cpp:476-609
  *    (RleDecoder::FetchRun / Next)
+ *  - COUNT(DISTINCT col): each group keeps the set of the non-NULL int64
+ *    values of col (src/execution/int_group_agg.cpp:89-92) and emits its
+ *    size (the union of the per-thread sets, int_group_agg.cpp:154-270);
+ *    here one set of (group, value) pairs per aggregate, single-threaded.
  *
  * Deliberate divergence: a NULL group key forms its own group (SQL
  * semantics).  The reference's in-memory chunk loop reads the key's raw
@@ -38,7 +42,7 @@
 #include <string.h>
 
 enum { T_SMALLINT = 1, T_INTEGER = 2, T_BIGINT = 3, T_DOUBLE = 4, T_VARCHAR = 5 };
-enum { A_COUNT_STAR = 0, A_COUNT = 1, A_SUM = 2, A_AVG = 3, A_MIN = 4, A_MAX = 5 };
+enum { A_COUNT_STAR = 0, A_COUNT = 1, A_SUM = 2, A_AVG = 3, A_MIN = 4, A_MAX = 5, A_COUNT_DISTINCT = 6 };
 enum { C_EQ = 0, C_NE, C_LT, C_LE, C_GT, C_GE };
 
 typedef struct {
@@ -147,17 +151,73 @@ static inline int64_t read_int(int type, const void *d, int64_t r) {
     }
 }
 
+/* set of (group index, value) pairs: COUNT(DISTINCT) */
+typedef struct {
+    int64_t *g;
+    int64_t *v;
+    uint8_t *used;
+    uint64_t cap;
+    int64_t n;
+} pset;
+
+static int pset_init(pset *p, uint64_t cap) {
+    p->cap = 64;
+    while (p->cap < cap) p->cap <<= 1;
+    p->g = (int64_t *)malloc(p->cap * 8);
+    p->v = (int64_t *)malloc(p->cap * 8);
+    p->used = (uint8_t *)calloc(p->cap, 1);
+    p->n = 0;
+    return (p->g && p->v && p->used) ? 0 : -1;
+}
+
+static void pset_free(pset *p) {
+    free(p->g);
+    free(p->v);
+    free(p->used);
+}
+
+/* returns 1 when (g, v) was not in the set (and inserts it), 0 if present,
+ * -1 on allocation failure */
+static int pset_insert(pset *p, int64_t g, int64_t v) {
+    if ((uint64_t)(p->n + 1) * 2 > p->cap) {
+        pset q;
+        if (pset_init(&q, p->cap * 2)) return -1;
+        for (uint64_t i = 0; i < p->cap; i++) {
+            if (!p->used[i]) continue;
+            uint64_t s = or_mix(or_mix((uint64_t)p->g[i]) ^ (uint64_t)p->v[i]) & (q.cap - 1);
+            while (q.used[s]) s = (s + 1) & (q.cap - 1);
+            q.used[s] = 1;
+            q.g[s] = p->g[i];
+            q.v[s] = p->v[i];
+        }
+        q.n = p->n;
+        pset_free(p);
+        *p = q;
+    }
+    uint64_t s = or_mix(or_mix((uint64_t)g) ^ (uint64_t)v) & (p->cap - 1);
+    while (p->used[s]) {
+        if (p->g[s] == g && p->v[s] == v) return 0;
+        s = (s + 1) & (p->cap - 1);
+    }
+    p->used[s] = 1;
+    p->g[s] = g;
+    p->v[s] = v;
+    p->n++;
+    return 1;
+}
+
 typedef struct {
     int32_t n_aggs;
     const int32_t *kind;
     const int32_t *in_type;
     const void *const *data;
     const uint8_t *const *nul; /* per agg: 1 = NULL, or NULL pointer */
+    pset *dset;                /* per agg (COUNT(DISTINCT) only), or NULL */
 } or_aggs;
 
 /* The per-row AggState update of the in-memory chunk loop
- * (physical_planner.cpp:7988-8017). */
-static inline void update_states(or_state *st, const or_aggs *A, int64_t r) {
+ * (physical_planner.cpp:7988-8017); g = the row's group index. */
+static inline int update_states(or_state *st, const or_aggs *A, int64_t r, int64_t g) {
     for (int a = 0; a < A->n_aggs; a++) {
         or_state *s = &st[a];
         int k = A->kind[a];
@@ -168,6 +228,12 @@ static inline void update_states(or_state *st, const or_aggs *A, int64_t r) {
         if (A->nul[a] && A->nul[a][r]) continue;
         if (k == A_COUNT) {
             s->count++;
+            continue;
+        }
+        if (k == A_COUNT_DISTINCT) {
+            int isnew = pset_insert(&A->dset[a], g, read_int(A->in_type[a], A->data[a], r));
+            if (isnew < 0) return -1;
+            s->count += isnew;
             continue;
         }
         double val = read_double(A->in_type[a], A->data[a], r);
@@ -193,6 +259,23 @@ static inline void update_states(or_state *st, const or_aggs *A, int64_t r) {
             }
         }
     }
+    return 0;
+}
+
+/* one pair set per COUNT(DISTINCT) aggregate (zeroed entries for the others) */
+static pset *dsets_new(int32_t n_aggs, const int32_t *kind) {
+    pset *d = (pset *)calloc((size_t)(n_aggs > 0 ? n_aggs : 1), sizeof(pset));
+    if (!d) return NULL;
+    for (int a = 0; a < n_aggs; a++)
+        if (kind[a] == A_COUNT_DISTINCT && pset_init(&d[a], 64)) return NULL;
+    return d;
+}
+
+static void dsets_free(pset *d, int32_t n_aggs, const int32_t *kind) {
+    if (!d) return;
+    for (int a = 0; a < n_aggs; a++)
+        if (kind[a] == A_COUNT_DISTINCT) pset_free(&d[a]);
+    free(d);
 }
 
 /* Merge partial states (shard merge of the per-thread maps,
@@ -228,14 +311,15 @@ static void emit_group(int64_t g, int64_t cap, const or_state *st, const or_aggs
         const or_state *s = &st[a];
         int64_t o = (int64_t)a * cap + g;
         int k = A->kind[a];
-        int isf = (k != A_COUNT_STAR && k != A_COUNT) && A->in_type[a] == T_DOUBLE;
+        int isf = (k != A_COUNT_STAR && k != A_COUNT && k != A_COUNT_DISTINCT) && A->in_type[a] == T_DOUBLE;
         out_null[o] = 0;
         out_i[o] = 0;
         out_d[o] = 0.0;
         out_comp[o] = 0.0;
         switch (k) {
         case A_COUNT_STAR:
-        case A_COUNT: out_i[o] = s->count; break;
+        case A_COUNT:
+        case A_COUNT_DISTINCT: out_i[o] = s->count; break;
         case A_SUM:
             if (s->count == 0) { out_null[o] = 1; break; }
             if (isf) out_d[o] = s->sum;
@@ -328,7 +412,7 @@ static int run_range(or_table *t, int64_t r0, int64_t r1, const int64_t *keys, c
         int nul = key_null ? key_null[r] : 0;
         int64_t g = tab_group(t, A->n_aggs, nul ? 0 : (uint64_t)keys[r], nul);
         if (g < 0) return -1;
-        update_states(&t->st[(size_t)g * A->n_aggs], A, r);
+        if (update_states(&t->st[(size_t)g * A->n_aggs], A, r, g)) return -1;
     }
     return 0;
 }
@@ -387,14 +471,20 @@ int64_t or_groupby(int64_t n, const int64_t *keys, const uint8_t *key_null, cons
                    const uint8_t *const *agg_null, int32_t nthreads, int64_t est_groups, int64_t cap,
                    int64_t *out_keys, uint8_t *out_key_null, int64_t *out_i, double *out_d, uint8_t *out_null,
                    double *out_comp) {
-    or_aggs A = {n_aggs, agg_kind, agg_in_type, agg_data, agg_null};
+    or_aggs A = {n_aggs, agg_kind, agg_in_type, agg_data, agg_null, NULL};
     if (nthreads < 1) nthreads = 1;
     if (nthreads > 256) nthreads = 256;
+    int has_distinct = 0;
+    for (int a = 0; a < n_aggs; a++) has_distinct |= agg_kind[a] == A_COUNT_DISTINCT;
+    if (has_distinct) nthreads = 1; /* the value sets are kept single-threaded */
     int64_t ng = 0;
     if (nthreads == 1) {
         or_table t;
         if (tab_init(&t, n_aggs, est_groups)) return -1;
-        if (run_range(&t, 0, n, keys, key_null, keep, &A)) { tab_free(&t); return -1; }
+        if (has_distinct && !(A.dset = dsets_new(n_aggs, agg_kind))) { tab_free(&t); return -1; }
+        int rc = run_range(&t, 0, n, keys, key_null, keep, &A);
+        dsets_free(A.dset, n_aggs, agg_kind);
+        if (rc) { tab_free(&t); return -1; }
         ng = t.ng;
         if (ng > cap) { tab_free(&t); return -ng - 2; }
         for (int64_t g = 0; g < ng; g++) {
@@ -474,7 +564,9 @@ int64_t or_groupby_str(int64_t n, const int64_t *offsets, const uint8_t *bytes, 
                        const uint8_t *keep, int32_t n_aggs, const int32_t *agg_kind, const int32_t *agg_in_type,
                        const void *const *agg_data, const uint8_t *const *agg_null, int64_t cap, int64_t *out_rep,
                        uint8_t *out_key_null, int64_t *out_i, double *out_d, uint8_t *out_null, double *out_comp) {
-    or_aggs A = {n_aggs, agg_kind, agg_in_type, agg_data, agg_null};
+    or_aggs A = {n_aggs, agg_kind, agg_in_type, agg_data, agg_null, NULL};
+    A.dset = dsets_new(n_aggs, agg_kind);
+    if (!A.dset) return -1;
     uint64_t mcap = 64;
     while (mcap < (uint64_t)(cap > 0 ? cap : 1) * 2) mcap <<= 1;
     int64_t *slot = (int64_t *)malloc(mcap * 8); /* group index or -1 */
@@ -520,7 +612,7 @@ int64_t or_groupby_str(int64_t n, const int64_t *offsets, const uint8_t *bytes, 
             }
             if (g < 0) { ng = cap + 1; break; }
         }
-        update_states(&st[(size_t)g * n_aggs], &A, r);
+        if (update_states(&st[(size_t)g * n_aggs], &A, r, g)) { ng = -1; break; }
     }
     if (ng <= cap) {
         for (int64_t g = 0; g < ng; g++) {
@@ -529,6 +621,7 @@ int64_t or_groupby_str(int64_t n, const int64_t *offsets, const uint8_t *bytes, 
             emit_group(g, cap, &st[(size_t)g * n_aggs], &A, out_i, out_d, out_null, out_comp);
         }
     }
+    dsets_free(A.dset, n_aggs, agg_kind);
     free(slot);
     free(sh);
     free(rep);

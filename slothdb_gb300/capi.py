@@ -19,12 +19,13 @@ STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "OOM", 3: "UNSUPPORTED", 4: "TIMEOUT",
                 7: "STATE", 8: "BUDGET"}
 
 SMALLINT, INTEGER, BIGINT, DOUBLE, VARCHAR = 1, 2, 3, 4, 5
-COUNT_STAR, COUNT, SUM, AVG, MIN, MAX = 0, 1, 2, 3, 4, 5
+COUNT_STAR, COUNT, SUM, AVG, MIN, MAX, COUNT_DISTINCT = 0, 1, 2, 3, 4, 5, 6
 EQ, NE, LT, LE, GT, GE = 0, 1, 2, 3, 4, 5
 MEM_HOST, MEM_DEVICE = 0, 1
 
 NP_TYPES = {SMALLINT: np.int16, INTEGER: np.int32, BIGINT: np.int64, DOUBLE: np.float64}
-AGG_NAMES = {"count_star": COUNT_STAR, "count": COUNT, "sum": SUM, "avg": AVG, "min": MIN, "max": MAX}
+AGG_NAMES = {"count_star": COUNT_STAR, "count": COUNT, "sum": SUM, "avg": AVG, "min": MIN, "max": MAX,
+             "count_distinct": COUNT_DISTINCT}
 CMP_NAMES = {"==": EQ, "=": EQ, "!=": NE, "<>": NE, "<": LT, "<=": LE, ">": GT, ">=": GE}
 
 
@@ -243,8 +244,8 @@ class GroupBy:
     """One GROUP BY handle (gb_agg) — the Python mirror of the operator.
 
     ``aggs``: list of (kind, col) with kind a name ('count_star', 'count',
-    'sum', 'avg', 'min', 'max') or the gb_agg_kind code; col = -1 for
-    COUNT(*).  ``filters``: list of (col, op, const) with op one of
+    'sum', 'avg', 'min', 'max', 'count_distinct') or the gb_agg_kind code;
+    col = -1 for COUNT(*).  ``filters``: list of (col, op, const) with op one of
     '==', '!=', '<', '<=', '>', '>='.
     """
 

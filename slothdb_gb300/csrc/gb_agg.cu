@@ -76,12 +76,13 @@ __global__ void __launch_bounds__(512) k_ingest(const __grid_constant__ Plan P, 
     extern __shared__ u64 smem[];
     __shared__ u32 s_tile;
     __shared__ u32 s_new;
+    __shared__ u32 s_pairs;
     SmemTable sm;
     sm.S = A.smem_slots;
     sm.probe = A.smem_probe;
     sm.keys = smem;
     sm.st = smem + sm.S;
-    if (threadIdx.x == 0) s_new = 0;
+    if (threadIdx.x == 0) s_new = s_pairs = 0;
     smem_init(P, sm);
     __syncthreads();
     const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -101,7 +102,7 @@ __global__ void __launch_bounds__(512) k_ingest(const __grid_constant__ Plan P, 
         const u64 t0 = (u64)(A.first_tile + t) * A.tile_rows;
         const u64 t1 = min(A.n_rows, t0 + A.tile_rows);
         for (u64 base = t0 + (u64)warp * 32; base < t1; base += (u64)nwarps * 32)
-            warp_rows<PRECOMBINE>(P, T, sm, base, t1, &s_new);
+            warp_rows<PRECOMBINE>(P, T, sm, base, t1, &s_new, &s_pairs);
         if (threadIdx.x == 0 && *(volatile u32 *)&T.ctl->spill_count > T.spill_threshold)
             atomicExch(&T.ctl->stop, 1u);
     }
@@ -109,6 +110,20 @@ __global__ void __launch_bounds__(512) k_ingest(const __grid_constant__ Plan P, 
     smem_flush(P, T, sm, &s_new);
     __syncthreads();
     if (threadIdx.x == 0 && s_new) atomicAdd(&T.ctl->n_groups, s_new);
+    if (threadIdx.x == 0 && s_pairs) atomicAdd(P.dmeta, (unsigned long long)s_pairs);
+}
+
+// Re-insert every pair of the old sets into the new (larger, emptied) ones.
+__global__ void k_dset_rehash(const u64 *old_sets, u64 old_mask, int n_sets, u64 *new_sets, u64 new_mask,
+                              unsigned long long *meta) {
+    const u64 old_slots = old_mask + 1, new_slots = new_mask + 1;
+    const u64 total = old_slots * (u64)n_sets;
+    for (u64 i = blockIdx.x * (u64)blockDim.x + threadIdx.x; i < total; i += (u64)gridDim.x * blockDim.x) {
+        const u64 g = old_sets[2 * i], v = old_sets[2 * i + 1];
+        if (g == EMPTY_KEY && v == EMPTY_KEY) continue;
+        const int d = (int)(i / old_slots);
+        dset_insert(new_sets + 2 * new_slots * d, new_mask, g, v, meta, d);
+    }
 }
 
 // Re-insert every used slot of `old` into the (larger, initialised) table.
@@ -472,6 +487,12 @@ struct gb_agg {
     u32 r_ovf_cap = 0;
     int r_grid = 0;
     u64 rows_ingested = 0;
+    // COUNT(DISTINCT): (group, value) pair sets, one per distinct column
+    DevBuf dsets, dsets_old, null_sets, null_sets_old, dmeta;
+    u64 dslots = 0;               // slots per set (power of two; 0 = none yet)
+    u64 dpairs = 0;               // pairs inserted (host copy)
+    bool dist_null_sets = false;  // NULL-key group of a nullable BIGINT key in twin sets
+    unsigned long long dmeta_host[2 + GB_MAX_DISTINCT] = {};
     // VARCHAR group key: device string dictionary (string -> dense id)
     int str_col = -1;
     DevBuf sd_hash, sd_ref, sd_id, sd_refid, sd_ctr, sd_arena, sd_old_hash, sd_old_ref, sd_old_id, sd_old_refid;
@@ -682,8 +703,71 @@ static gb_status ensure_capacity(gb_agg *h, cudaStream_t st) {
     return GB_OK;
 }
 
+// COUNT(DISTINCT): size the pair sets for `n_rows` more rows (load <= 1/2
+// even if every row brings a new pair), rehashing what they hold, and point
+// the plan at them.
+static gb_status dist_reserve(gb_agg *h, u64 n_rows, cudaStream_t st) {
+    Plan &P = h->plan;
+    const int nd = P.n_dist;
+    if ((P.dsets && P.dmask + 1 == h->dslots) && h->dslots >= 2 * (h->dpairs + n_rows)) return GB_OK;
+    gb_status s;
+    if ((s = h->dmeta.ensure(sizeof(h->dmeta_host)))) return s;
+    if (h->dslots == 0) GB_CUDA(cudaMemsetAsync(h->dmeta.p, 0, sizeof(h->dmeta_host), st));
+    u64 slots = std::max<u64>(1024, h->dslots);
+    while (slots < 2 * (h->dpairs + n_rows)) slots *= 2;
+    const size_t bytes = (size_t)slots * 16 * nd;
+    if (slots != h->dslots) {
+        std::swap(h->dsets, h->dsets_old);
+        std::swap(h->null_sets, h->null_sets_old);
+        if ((s = h->dsets.ensure(bytes))) return s;
+        if ((s = radix_fill_u64((u64 *)h->dsets.p, (u64)slots * 2 * nd, EMPTY_KEY, st))) return s;
+        if (h->dist_null_sets) {
+            if ((s = h->null_sets.ensure(bytes))) return s;
+            if ((s = radix_fill_u64((u64 *)h->null_sets.p, (u64)slots * 2 * nd, EMPTY_KEY, st))) return s;
+        }
+        if (h->dslots) {
+            const u64 old_mask = h->dslots - 1, total = h->dslots * (u64)nd;
+            const int grid = grid_for(total, 256, sm_count() * 8);
+            k_dset_rehash<<<grid, 256, 0, st>>>((const u64 *)h->dsets_old.p, old_mask, nd, (u64 *)h->dsets.p,
+                                                slots - 1, (unsigned long long *)h->dmeta.p);
+            h->launches++;
+            if (h->dist_null_sets) {
+                k_dset_rehash<<<grid, 256, 0, st>>>((const u64 *)h->null_sets_old.p, old_mask, nd,
+                                                    (u64 *)h->null_sets.p, slots - 1, (unsigned long long *)h->dmeta.p);
+                h->launches++;
+            }
+            GB_CUDA(cudaGetLastError());
+        }
+        h->dsets_old.release();
+        h->null_sets_old.release();
+        h->dslots = slots;
+    }
+    P.dsets = (u64 *)h->dsets.p;
+    P.null_sets = h->dist_null_sets ? (u64 *)h->null_sets.p : nullptr;
+    P.dmeta = (unsigned long long *)h->dmeta.p;
+    P.dmask = slots - 1;
+    return GB_OK;
+}
+
+// Empty the pair sets (reset).
+static gb_status dist_clear(gb_agg *h, cudaStream_t st) {
+    h->dpairs = 0;
+    memset(h->dmeta_host, 0, sizeof(h->dmeta_host));
+    if (!h->dslots) return GB_OK;
+    const u64 words = h->dslots * 2 * (u64)h->plan.n_dist;
+    gb_status s;
+    if ((s = radix_fill_u64((u64 *)h->dsets.p, words, EMPTY_KEY, st))) return s;
+    if (h->dist_null_sets && (s = radix_fill_u64((u64 *)h->null_sets.p, words, EMPTY_KEY, st))) return s;
+    GB_CUDA(cudaMemsetAsync(h->dmeta.p, 0, sizeof(h->dmeta_host), st));
+    return GB_OK;
+}
+
 static gb_status run_ingest(gb_agg *h, u64 n_rows, cudaStream_t st) {
     if (n_rows == 0) return GB_OK;
+    if (h->plan.n_dist) {
+        gb_status s = dist_reserve(h, n_rows, st);
+        if (s) return s;
+    }
     Ctl *dctl = (Ctl *)h->ctl_buf.p;
     const int words = h->plan.words;
     u32 tile_rows = h->tile_rows;
@@ -734,9 +818,18 @@ static gb_status run_ingest(gb_agg *h, u64 n_rows, cudaStream_t st) {
         }
         h->launches++;
         GB_CUDA(cudaGetLastError());
+        if (h->plan.n_dist)
+            GB_CUDA(cudaMemcpyAsync(h->dmeta_host, h->dmeta.p, sizeof(h->dmeta_host), cudaMemcpyDeviceToHost, st));
         gb_status s = read_ctl(h, st);
         if (s) return s;
         if ((s = check_err(h))) return s;
+        if (h->plan.n_dist) {
+            if (h->dmeta_host[1]) {
+                set_error("COUNT(DISTINCT) pair set overflow (internal invariant violated)");
+                return GB_ERR_CUDA;
+            }
+            h->dpairs = h->dmeta_host[0];
+        }
         h->n_groups = h->ctl_host.n_groups;
         u64 claimed = std::min<u64>(h->ctl_host.tile_counter, n_tiles_total - first);
         first += claimed;
@@ -1254,7 +1347,7 @@ static gb_status compile_plan(gb_agg *h) {
         if (d.kind == GB_AGG_COUNT_STAR) {
             e.out_type = GB_T_BIGINT;
         } else {
-            if (d.col < 0 || d.col >= nc || d.kind < 0 || d.kind > GB_AGG_MAX) {
+            if (d.col < 0 || d.col >= nc || d.kind < 0 || d.kind > GB_AGG_COUNT_DISTINCT) {
                 set_error("aggregate %zu: invalid kind or column", a);
                 return GB_ERR_INVALID;
             }
@@ -1263,6 +1356,19 @@ static gb_status compile_plan(gb_agg *h) {
             if (t == GB_T_VARCHAR) {
                 set_error("aggregate %zu over VARCHAR is not supported on the GPU path", a);
                 return GB_ERR_UNSUPPORTED;
+            }
+            if (d.kind == GB_AGG_COUNT_DISTINCT) {
+                // NULLs never enter the value set: no non-NULL count word
+                if (t == GB_T_DOUBLE) {
+                    set_error("COUNT(DISTINCT) over DOUBLE is not supported on the GPU path");
+                    return GB_ERR_UNSUPPORTED;
+                }
+                e.out_type = GB_T_BIGINT;
+                e.val_word = find_or_add_op(OP_DIST, d.col);
+                if (e.val_word < 0) goto too_many;
+                h->emit.push_back(e);
+                h->out_types.push_back(e.out_type);
+                continue;
             }
             bool nullable = (h->nullable_mask >> d.col) & 1ull;
             int cntw = 0;
@@ -1295,6 +1401,18 @@ static gb_status compile_plan(gb_agg *h) {
         h->out_types.push_back(e.out_type);
     }
     P.words = words;
+    P.n_dist = 0;
+    for (int i = 0; i < P.n_ops; i++) {
+        P.ops[i].dset = 0;
+        if (P.ops[i].kind == OP_DIST) P.ops[i].dset = (uint8_t)P.n_dist++;
+    }
+    if (P.n_dist > GB_MAX_DISTINCT) {
+        set_error("at most %d COUNT(DISTINCT) columns per query", GB_MAX_DISTINCT);
+        return GB_ERR_UNSUPPORTED;
+    }
+    // the NULL-key group of a nullable BIGINT key has no spare key value
+    h->dist_null_sets = P.n_dist && P.key_mode == KEY_SINGLE && P.key_type[0] == GB_T_BIGINT &&
+                        ((h->nullable_mask >> P.key_col[0]) & 1ull);
     if (P.key_mode == KEY_STRING) P.n_cols = nc + 1;
     {
         int need = words + 1;
@@ -1431,6 +1549,9 @@ gb_status gb_agg_estimate_bytes(const gb_agg_spec *spec, uint64_t nrows, uint64_
     for (int t : h.out_types) b += (cap + 2) * (u64)(t == GB_T_VARCHAR ? 8 : type_size(t)) + (cap + 2) / 8;
     b += (u64)((1u << 16) + 4096) * (1 + h.plan.words) * 8;            // spill records
     if (h.str_col >= 0) b += 4 * 2 * cap * 8 + 40 * est + 16 * est;    // dictionary, arena, emitted strings
+    if (h.plan.n_dist)                                                   // (group, value) pair sets
+        b += std::max<u64>(1024, next_pow2(2 * std::max<u64>(nrows, 1))) * 16 * h.plan.n_dist *
+             (h.dist_null_sets ? 2 : 1);
     *bytes = b;
     return GB_OK;
 }
@@ -1784,6 +1905,7 @@ gb_status gb_agg_reset(gb_agg *h) {
     if (!h) return GB_ERR_INVALID;
     gb_status s = init_table(h, h->table, h->cap, 0);
     if (s) return s;
+    if ((s = dist_clear(h, 0))) return s;
     GB_CUDA(cudaMemset(h->ctl_buf.p, 0, sizeof(Ctl)));
     GB_CUDA(cudaStreamSynchronize(0));  // before ingests on streams that do not synchronise with it
     h->n_groups = 0;
@@ -1818,7 +1940,8 @@ void gb_agg_destroy(gb_agg *h) {
     h->host_str_bytes.release();
     for (DevBuf *b : {&h->r_skeys, &h->r_scnt, &h->r_hist, &h->r_hot_keys, &h->r_hot_part, &h->r_cursor, &h->r_part,
                       &h->r_part2, &h->r_ovf, &h->r_off, &h->r_cap, &h->r_off2, &h->r_cap2, &h->r_hot_idx,
-                      &h->r_hot_list, &h->r_hstate, &h->r_p2w})
+                      &h->r_hot_list, &h->r_hstate, &h->r_p2w, &h->dsets, &h->dsets_old, &h->null_sets,
+                      &h->null_sets_old, &h->dmeta})
         b->release();
     h->topn_ids_a.release();
     h->topn_ids_b.release();

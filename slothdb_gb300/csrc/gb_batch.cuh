@@ -453,7 +453,7 @@ __device__ __noinline__ void generic_tile(const Plan &sP, const TableRef &sT, u6
     smem_init(sP, sm);
     __syncthreads();
     for (u64 base = t0 + (u64)warp * 32; base < t1; base += (u64)nwarps * 32)
-        warp_rows<PRECOMBINE>(sP, sT, sm, base, t1, new_groups);
+        warp_rows<PRECOMBINE>(sP, sT, sm, base, t1, new_groups, nullptr);  // no OP_DIST in a batch
     __syncthreads();
     smem_flush(sP, sT, sm, new_groups);
 }
@@ -978,6 +978,11 @@ gb_status gb_batch_create(gb_batch **out) {
 
 gb_status gb_batch_add(gb_batch *b, const gb_agg_spec *spec, const gb_col *cols, uint64_t nrows, uint32_t *qidx) {
     if (!b || !spec || (!cols && nrows)) return GB_ERR_INVALID;
+    for (uint32_t a = 0; a < spec->n_aggs && spec->aggs; a++)
+        if (spec->aggs[a].kind == GB_AGG_COUNT_DISTINCT) {
+            set_error("COUNT(DISTINCT) runs on its own handle (gb_agg_*), not in a batch");
+            return GB_ERR_UNSUPPORTED;
+        }
     // a table never has more groups than rows: size it for min(estimate, rows)
     gb_agg_spec sp = *spec;
     const u64 est = sp.est_groups ? sp.est_groups : (1u << 15);

@@ -52,6 +52,7 @@ enum OpKind : uint8_t {
     OP_MIN_F = 5,   // ordered-int64-encoded double
     OP_MAX_F = 6,
     OP_CNT_NN = 7,  // count of non-NULL values of a column
+    OP_DIST = 8,    // distinct non-NULL values: contributes 1 per new (group, value) pair
 };
 
 enum KeyMode : int32_t {
@@ -73,7 +74,7 @@ struct Op {
     uint8_t kind;
     uint8_t col;
     uint8_t word;  // state word index (1..words-1)
-    uint8_t pad;
+    uint8_t dset;  // OP_DIST: index of the op's pair set
 };
 
 struct Filter {
@@ -96,8 +97,15 @@ struct Plan {
     int32_t key_bits_a;   // KEY_PACKED: width of the first key
     int32_t words;        // state words (word 0 = row count)
     int32_t stride;       // words per table slot incl. key, power of two
-    int32_t pad_;
+    int32_t n_dist;       // OP_DIST ops (COUNT(DISTINCT) columns)
     uint64_t word_init[GB_MAX_WORDS];
+    // COUNT(DISTINCT): per OP_DIST op a set of (group key, value) pairs,
+    // 16-byte slots of which dmask + 1 per set; the NULL-key group of a
+    // nullable BIGINT key keeps its pairs in twin sets (null_sets, or null)
+    u64 *dsets;
+    u64 *null_sets;
+    unsigned long long *dmeta;  // [0] pairs inserted, [1] overflow flag, [2 + d] marker pair of set d seen
+    u64 dmask;
 };
 
 // --------------------------------------------------------------- device utils

@@ -109,6 +109,81 @@ __device__ __forceinline__ void load_vals(const Plan &P, u64 r, u64 *v) {
     }
 }
 
+// ------------------------------------------------------------ distinct pairs
+// COUNT(DISTINCT v) keeps, per distinct column, one open-addressing set of
+// (group key, value) pairs in HBM.  A slot is claimed by one 128-bit
+// compare-and-swap, so a pair is never half-written and no thread waits on
+// another; the set is sized by the host to a load factor <= 1/2 before each
+// ingest, so a probe always meets an empty slot.  The empty marker is the
+// pair (EMPTY_KEY, EMPTY_KEY); the real pair equal to it (the INT64_MIN key
+// with the INT64_MIN value) is tracked by a flag word instead.
+#define DIST_NULL_KEY 0x4000000000000000ull  // NULL-key group of a key narrower than 64 bits
+
+__device__ __forceinline__ void cas128(u64 *p, u64 cmp_lo, u64 cmp_hi, u64 new_lo, u64 new_hi, u64 &old_lo,
+                                       u64 &old_hi) {
+    asm volatile(
+        "{\n\t.reg .b128 c, n, o;\n\t"
+        "mov.b128 c, {%2, %3};\n\t"
+        "mov.b128 n, {%4, %5};\n\t"
+        "atom.global.cas.b128 o, [%6], c, n;\n\t"
+        "mov.b128 {%0, %1}, o;\n\t}"
+        : "=l"(old_lo), "=l"(old_hi)
+        : "l"(cmp_lo), "l"(cmp_hi), "l"(new_lo), "l"(new_hi), "l"(p)
+        : "memory");
+}
+
+__device__ __forceinline__ u64 pair_hash(u64 g, u64 v) { return mix64(mix64(g) ^ v); }
+
+// Insert (g, v) into the set at `set` (mask + 1 slots).  Returns true when
+// the pair is new.  meta: the plan's dmeta words; d: the set's index.
+__device__ __forceinline__ bool dset_insert(u64 *set, u64 mask, u64 g, u64 v, unsigned long long *meta, int d) {
+    if (g == EMPTY_KEY && v == EMPTY_KEY) return atomicExch(meta + 2 + d, 1ull) == 0ull;
+    u64 s = pair_hash(g, v) & mask;
+    for (u64 q = 0; q <= mask; q++) {
+        u64 lo, hi;
+        cas128(set + 2 * s, EMPTY_KEY, EMPTY_KEY, g, v, lo, hi);
+        if (lo == EMPTY_KEY && hi == EMPTY_KEY) return true;
+        if (lo == g && hi == v) return false;
+        s = (s + 1) & mask;
+    }
+    atomicExch(meta + 1, 1ull);  // full: the host sized it wrongly
+    return false;
+}
+
+// Replace each OP_DIST contribution of row r (key pk of kind `kind`, as
+// make_key returns) by 1 if its (group, value) pair is new, else 0.
+__device__ __forceinline__ void dist_vals(const Plan &P, u64 r, int kind, u64 pk, u64 *v, u32 *new_pairs) {
+#pragma unroll
+    for (int i = 0; i < GB_MAX_OPS; i++) {
+        if (i < P.n_ops && P.ops[i].kind == OP_DIST) {
+            const Op o = P.ops[i];
+            const DevCol &c = P.cols[o.col];
+            u64 x = 0;
+            if (row_valid(c.valid, r)) {
+                const u64 val = (u64)load_int(c, r);
+                const u64 slots = P.dmask + 1;
+                u64 *set = P.dsets + 2 * slots * o.dset;
+                u64 g = pk;
+                if (kind == 1) {
+                    g = EMPTY_KEY;
+                } else if (kind == 2) {
+                    if (P.null_sets) {
+                        set = P.null_sets + 2 * slots * o.dset;
+                        g = 0;
+                    } else {
+                        g = DIST_NULL_KEY;
+                    }
+                }
+                if (dset_insert(set, P.dmask, g, val, P.dmeta, o.dset)) {
+                    x = 1;
+                    atomicAdd(new_pairs, 1u);
+                }
+            }
+            v[i] = x;
+        }
+    }
+}
+
 // ------------------------------------------------------------ HBM table
 // Find or claim the slot of pk.  Returns the slot index or -1 if the probe
 // bound was reached.  `new_groups` counts claimed slots (CTA-local).
@@ -225,7 +300,7 @@ __device__ __forceinline__ void smem_flush(const Plan &P, const TableRef &T, Sme
 // index the column vectors (row_ids != nullptr: gather through ids).
 template <bool PRECOMBINE>
 __device__ __forceinline__ void warp_rows(const Plan &P, const TableRef &T, SmemTable &sm, u64 base, u64 end,
-                                          u32 *new_groups) {
+                                          u32 *new_groups, u32 *new_pairs) {
     const int lane = threadIdx.x & 31;
     const u64 r = base + lane;
     bool act = r < end;
@@ -237,6 +312,7 @@ __device__ __forceinline__ void warp_rows(const Plan &P, const TableRef &T, Smem
     if (act) {
         int kind = make_key(P, r, pk);
         load_vals(P, r, v);
+        if (P.n_dist && kind != 3) dist_vals(P, r, kind, pk, v, new_pairs);
         if (kind != 0) {
             if (kind == 3) atomicOr(&T.ctl->err, (u32)ERR_NULL_IN_WIDE_KEY);
             else special_fold(P, T, kind, 1, v);
@@ -336,6 +412,7 @@ __device__ __forceinline__ void emit_group(const Plan &P, const EmitArgs &E, u64
         switch (g.kind) {
         case GB_AGG_COUNT_STAR:
         case GB_AGG_COUNT: ((long long *)dst)[o] = (i64)cnt; break;
+        case GB_AGG_COUNT_DISTINCT: ((long long *)dst)[o] = (i64)w[g.val_word]; break;
         case GB_AGG_SUM:
             if (cnt == 0) { ((long long *)dst)[o] = 0; clear_valid(vw, o); }
             else ((long long *)dst)[o] = (i64)w[g.val_word];  // int64 or double bits

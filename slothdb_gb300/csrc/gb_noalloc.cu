@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(512) k_ingest_noalloc(const __grid_constant__ 
     const int warp = threadIdx.x >> 5;
     const u64 warps_total = (u64)gridDim.x * (blockDim.x >> 5);
     for (u64 base = ((u64)blockIdx.x * (blockDim.x >> 5) + warp) * 32; base < n; base += warps_total * 32)
-        warp_rows<true>(P, T, sm, base, n, &s_new);
+        warp_rows<true>(P, T, sm, base, n, &s_new, nullptr);  // COUNT and SUM only: no OP_DIST
     __syncthreads();
     smem_flush(P, T, sm, &s_new);
     __syncthreads();

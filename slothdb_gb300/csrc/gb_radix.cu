@@ -766,7 +766,7 @@ static const size_t kSmemBudget = 224 * 1024;  // <= the 227 KiB opt-in minus st
 
 gb_status radix_prepare(const Plan &P, RadixPlan &R, u64 est_groups, u64 nullable_mask) {
     memset(&R, 0, sizeof R);
-    if (P.key_mode == KEY_STRING) return GB_ERR_UNSUPPORTED;
+    if (P.key_mode == KEY_STRING || P.n_dist) return GB_ERR_UNSUPPORTED;
     if (P.n_ops > RADIX_MAX_OPS) return GB_ERR_UNSUPPORTED;
     for (int i = 0; i < P.n_ops; i++) {
         const int c = P.ops[i].col;

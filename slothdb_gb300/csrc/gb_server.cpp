@@ -16,7 +16,8 @@
 //   execute  the admitted queries run as one gb_batch (one pass of a few
 //            persistent kernels), except high-cardinality queries (estimated
 //            groups >= 2^20), which run one by one on their own handle (the
-//            radix path); in mode 1 every query runs alone on its own handle
+//            radix path), and COUNT(DISTINCT) queries, which run alone on a
+//            hash handle; in mode 1 every query runs alone on its own handle
 //            (the one-at-a-time baseline);
 //   complete results are copied to host memory owned by the ticket, the
 //            ticket records queue / execution times, and waiters wake up.
@@ -147,6 +148,12 @@ struct Query {
     HostResult res;
     u64 t_submit = 0, t_start = 0, t_done = 0;
     uint32_t batch_size = 0;
+
+    bool distinct() const {
+        for (const gb_agg_desc &a : aggs)
+            if (a.kind == GB_AGG_COUNT_DISTINCT) return true;
+        return false;
+    }
 
     gb_agg_spec spec() const {
         gb_agg_spec s{};
@@ -423,7 +430,8 @@ void dispatcher(gb_server *s) {
             }
         };
         std::vector<Query *> big, small;
-        for (Query *q : take) (s->mode == 1 || q->est_groups >= RADIX_GROUPS ? big : small).push_back(q);
+        for (Query *q : take)
+            (s->mode == 1 || q->est_groups >= RADIX_GROUPS || q->distinct() ? big : small).push_back(q);
         if (!small.empty()) {
             for (Query *q : small) q->batch_size = (uint32_t)small.size();
             run_batch(s, small);

@@ -65,3 +65,23 @@ def test_estimate_bytes_host_only(gblib):
                                    est_groups=1000)
     with pytest.raises(capi.GbError):
         capi.estimate_bytes([capi.VARCHAR, capi.BIGINT], [0], [("sum", 0)], nrows=10)   # SUM over VARCHAR
+
+
+def test_count_distinct_plan_host_only(gblib):
+    """COUNT(DISTINCT) plans compile on the host: pair sets add to the
+    estimate (twice for a nullable BIGINT key); DOUBLE input and a third
+    distinct column are refused."""
+    from slothdb_gb300 import capi
+    base = capi.estimate_bytes([capi.INTEGER, capi.BIGINT], [0], [("count_star", -1)], nrows=100_000,
+                               est_groups=1000)
+    d = capi.estimate_bytes([capi.INTEGER, capi.BIGINT], [0], [("count_distinct", 1)], nrows=100_000,
+                            est_groups=1000)
+    assert d >= base + 2 * 100_000 * 16
+    dn = capi.estimate_bytes([capi.BIGINT, capi.BIGINT], [0], [("count_distinct", 1)], nrows=100_000,
+                             est_groups=1000, nullable=[0])
+    assert dn >= d + 2 * 100_000 * 16
+    with pytest.raises(capi.GbError):
+        capi.estimate_bytes([capi.INTEGER, capi.DOUBLE], [0], [("count_distinct", 1)], nrows=10)
+    with pytest.raises(capi.GbError):
+        capi.estimate_bytes([capi.INTEGER, capi.BIGINT, capi.BIGINT, capi.BIGINT], [0],
+                            [("count_distinct", 1), ("count_distinct", 2), ("count_distinct", 3)], nrows=10)

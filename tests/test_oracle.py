@@ -110,3 +110,32 @@ def test_double_sum_compensated():
     exact = math.fsum(x.tolist())
     assert abs(r["aggs"][0][2][0] - exact) <= 1e-15 * abs(exact) * 4
     assert abs(r["aggs"][0][0][0] - exact) / exact < 1e-12
+
+
+def test_count_distinct_known_answers():
+    # SELECT DISTINCT x over (1, 1, 2, 2, 3) has 3 rows
+    # (test/unit/execution/test_advanced_sql.cpp:11-18): as COUNT(DISTINCT x)
+    # under one constant key
+    x = np.array([1, 1, 2, 2, 3], dtype=np.int32)
+    r = _q([2, 2], [0], [("count_distinct", 1)], [np.zeros(5, np.int32), x])
+    assert r["aggs"][0][0].tolist() == [3]
+    assert r["out_types"][1] == oracle.BIGINT
+    # per group, NULL values never counted; an all-NULL group counts 0
+    k = np.array([1, 1, 1, 2, 2, 3, 3], dtype=np.int32)
+    v = np.array([7, 7, 8, 5, 6, 9, 9], dtype=np.int64)
+    vn = np.array([0, 0, 0, 0, 1, 1, 1], dtype=bool)
+    r = _q([2, 3], [0], [("count_distinct", 1), ("count_star", -1)], [k, v], nulls=[None, vn])
+    got = dict(zip(r["keys"][0].tolist(), zip(r["aggs"][0][0].tolist(), r["aggs"][1][0].tolist())))
+    assert got == {1: (2, 3), 2: (1, 2), 3: (0, 2)}
+
+
+def test_count_distinct_matches_numpy_sets():
+    rng = np.random.default_rng(21)
+    n = 50_000
+    k = rng.integers(0, 300, n, dtype=np.int32)
+    v = rng.integers(-40, 40, n, dtype=np.int64) * (10**15)
+    r = _q([2, 3], [0], [("count_distinct", 1)], [k, v], nthreads=4)  # the value sets keep it single-threaded
+    pairs = np.unique(np.stack([k.astype(np.int64), v], axis=1), axis=0)
+    keys, counts = np.unique(pairs[:, 0], return_counts=True)
+    got = dict(zip(r["keys"][0].tolist(), r["aggs"][0][0].tolist()))
+    assert got == dict(zip(keys.tolist(), counts.tolist()))
