@@ -53,7 +53,8 @@ def parse():
     ap.add_argument("--rows", type=int, default=100_000_000)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=20_000_000)
-    ap.add_argument("--workload", default="zipf100m", choices=["zipf100m", "batch256", "serve", "parquet200m"])
+    ap.add_argument("--workload", default="zipf100m", choices=["zipf100m", "batch256", "serve", "parquet200m",
+                                                                      "distinct100m"])
     ap.add_argument("--pq-rows", type=int, default=200_000_000, help="parquet200m: rows in the file")
     ap.add_argument("--tables", type=int, default=256)
     ap.add_argument("--duration", type=float, default=20.0, help="serve: seconds of Poisson arrivals")
@@ -697,8 +698,172 @@ def run_parquet_reference(args, key, f, v, rows):
     print(json.dumps(line), flush=True)
 
 
+DISTINCT_GROUPS, DISTINCT_VALUES = 100_000, 2000
+
+
+def distinct_data(rows):
+    """k INT32 uniform over 100,000 groups, v INT32 uniform over 2,000
+    values (seed 5): ~787 distinct values per group, ~79M distinct pairs."""
+    rng = np.random.default_rng(5)
+    k = rng.integers(0, DISTINCT_GROUPS, rows, dtype=np.int32)
+    v = rng.integers(0, DISTINCT_VALUES, rows, dtype=np.int32)
+    return k, v
+
+
+def run_distinct(args):
+    """SELECT k, COUNT(DISTINCT v), COUNT(*) FROM t GROUP BY k over --rows
+    rows (hash GROUP BY + (group, value) pair sets in HBM).  value = rows/s
+    with the columns resident in HBM; parity at full size against exact
+    per-group value sets built with numpy."""
+    ws, rank, local = dist_env()
+    rows = args.rows
+    t0 = time.time()
+    k, v = distinct_data(rows)
+    gen_s = time.time() - t0
+    types = [2, 2]
+    aggs = [("count_distinct", 1), ("count_star", -1)]
+    if args.impl == "reference":
+        return run_distinct_reference(args, k, v, types, aggs)
+    import torch
+    torch.cuda.set_device(local)
+    from slothdb_gb300 import capi
+    capi.load(build_if_missing=True)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    dk = torch.from_numpy(k).cuda()
+    dv = torch.from_numpy(v).cuda()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    sp = stream.cuda_stream
+    g = capi.GroupBy(types, [0], aggs, est_groups=DISTINCT_GROUPS)
+
+    def step():
+        g.reset()
+        g.ingest([dk, dv], nrows=rows, device=True, stream=sp)
+        g.finalize(stream=sp)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    # parity at full size: exact per-group distinct counts from a bitmap of
+    # the (group, value) pairs
+    res = g.result()
+    seen = np.bincount(k.astype(np.int64) * DISTINCT_VALUES + v, minlength=DISTINCT_GROUPS * DISTINCT_VALUES)
+    exp_d = (seen.reshape(DISTINCT_GROUPS, DISTINCT_VALUES) > 0).sum(axis=1)
+    exp_c = np.bincount(k, minlength=DISTINCT_GROUPS)
+    del seen
+    o = np.argsort(res[0][0])
+    gk = res[0][0][o].astype(np.int64)
+    ok = (np.array_equal(gk, np.nonzero(exp_c)[0]) and np.array_equal(res[1][0][o], exp_d[gk])
+          and np.array_equal(res[2][0][o], exp_c[gk]))
+    g.set_profiling(True)
+    step()
+    prof = {kk: vv[1] / max(1, vv[0]) for kk, vv in g.profile().items()}
+    g.set_profiling(False)
+    clocks = Clocks(local)
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    launches = 0
+    for _ in range(args.steps):
+        step()
+        launches += g.launches()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    in_bytes = rows * 8
+    ing_ms = prof.get("k_ingest", float("nan"))
+    achieved = in_bytes / (ing_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                "traffic": None, "kernel": "k_ingest", "kernel_ms": ing_ms,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback", "kernels_ms": prof}
+    e2e = None
+    if not args.no_e2e:
+        pk = capi.PinnedBuffer(rows * 4)
+        pv = capi.PinnedBuffer(rows * 4)
+        pk.view(np.int32)[:] = k
+        pv.view(np.int32)[:] = v
+        ge = capi.GroupBy(types, [0], aggs, est_groups=DISTINCT_GROUPS)
+        d2h = 0
+
+        def step_e2e():
+            ge.reset()
+            ge.ingest([pk.ptr, pv.ptr], nrows=rows, stream=sp)
+            ge.finalize(stream=sp)
+            return ge.result_host_bytes()[1]
+
+        for _ in range(2):
+            d2h = step_e2e()
+        torch.cuda.synchronize()
+        tt = time.perf_counter()
+        ne = max(1, args.steps // 2)
+        for _ in range(ne):
+            d2h = step_e2e()
+        torch.cuda.synchronize()
+        e2e_s = (time.perf_counter() - tt) / ne
+        e2e = {"value": rows / e2e_s, "unit": "rows/s", "h2d_bytes_per_step": in_bytes, "d2h_bytes_per_step": d2h,
+               "ms_per_step": e2e_s * 1e3}
+        ge.close()
+        pk.close()
+        pv.close()
+    cpu = None
+    if rank == 0:
+        import oracle
+        n = min(args.cpu_sample, rows)
+        tc = time.perf_counter()
+        oracle.run_query(types, [0], aggs, [k[:n], v[:n]])
+        dt = time.perf_counter() - tc
+        cpu = {"value": n / dt, "unit": "rows/s", "cores": 1, "kind": "port",
+               "sample": "first %d rows, per-group value sets (single-threaded, %.2f s)" % (n, dt)}
+    line = {"metric": "COUNT(DISTINCT) GROUP BY rows/s (100M rows, 100K groups)", "value": rows / (ms / 1e3),
+            "unit": "rows/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
+            "config": {"workload": "count-distinct-groupby-%dM" % (rows // 1_000_000), "rows": rows,
+                       "groups": DISTINCT_GROUPS, "values": DISTINCT_VALUES, "distinct_pairs": int(exp_d.sum()),
+                       "aggs": "COUNT(DISTINCT v),COUNT(*)",
+                       "l2": "inputs %.1f GB + pair sets > L2 129 MB (no flush needed)" % (in_bytes / 1e9),
+                       "datagen_s": round(gen_s, 1)},
+            "parity": "bit-exact vs exact value sets" if ok else "MISMATCH vs exact value sets",
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk, "gpu_launches": launches}
+    print(json.dumps(line), flush=True)
+    g.close()
+
+
+def run_distinct_reference(args, k, v, types, aggs):
+    """The oracle's per-group value sets over a bounded sample (single thread:
+    the sets are not merged across threads)."""
+    import oracle
+    n = min(args.cpu_sample, len(k))
+    times = []
+    for i in range(args.warmup + args.steps):
+        t = time.perf_counter()
+        oracle.run_query(types, [0], aggs, [k[:n], v[:n]])
+        if i >= args.warmup:
+            times.append(time.perf_counter() - t)
+    per = statistics.mean(times)
+    val = n / per
+    line = {"impl": "reference", "metric": "COUNT(DISTINCT) GROUP BY rows/s (100M rows, 100K groups)",
+            "value": val, "unit": "rows/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int32", "data": "synthetic",
+            "config": {"workload": "count-distinct-groupby (bounded sample of %d rows)" % n},
+            "cpu_baseline": {"value": val, "unit": "rows/s", "cores": 1, "kind": "port",
+                             "sample": "first %d rows per step" % n},
+            "e2e": {"value": val, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "distinct100m":
+        run_distinct(args)
+        return
     if args.workload == "batch256":
         run_batch(args)
         return
