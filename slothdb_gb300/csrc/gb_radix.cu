@@ -384,11 +384,20 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
                             for (int k = 0; k < REG_HOT; k++) {
                                 if (hidx == (u32)k) {
                                     rc[k]++;
+                                    if (SPEC != OP_ADD_F) {
 #pragma unroll
-                                    for (int i = 0; i < NOPS; i++)
-                                        rw[k][i] = op_combine(SPEC ? SPEC : P.ops[i].kind, rw[k][i], v[i]);
+                                        for (int i = 0; i < NOPS; i++)
+                                            rw[k][i] = op_combine(SPEC ? SPEC : P.ops[i].kind, rw[k][i], v[i]);
+                                    }
                                 }
                             }
+                            // FP64 runs at a small fraction of the integer rate on
+                            // this part, and a warp's register adds cost one FP64
+                            // instruction per hot key present: the DOUBLE sum of
+                            // a register-tier row goes to the L2 slice instead
+                            if (SPEC == OP_ADD_F)
+                                atomicAdd((double *)(hpart + (size_t)hidx * W + P.ops[0].word),
+                                          __longlong_as_double((i64)v[0]));
                         } else if (SPEC) {
                             // the count stays in shared memory (native 32-bit
                             // atomics); the sum is a fire-and-forget reduction
