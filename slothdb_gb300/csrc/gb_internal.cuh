@@ -109,6 +109,17 @@ struct Plan {
 };
 
 // --------------------------------------------------------------- device utils
+// Hint: start pulling [p, p + bytes) into L2 with one bulk prefetch (no data
+// returned, nothing to wait for).  Skipped unless p is 16-byte aligned; the
+// size is rounded down to 16 bytes, so the range never leaves [p, p + bytes).
+__device__ __forceinline__ void l2_prefetch(const void *p, u64 bytes) {
+    if ((((u64)p) & 15) || bytes < 16) return;
+    if (bytes > (1ull << 30)) bytes = 1ull << 30;
+    u64 g;
+    asm("cvta.to.global.u64 %0, %1;" : "=l"(g) : "l"(p));
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(g), "r"((unsigned)(bytes & ~15ull)) : "memory");
+}
+
 __device__ __forceinline__ u64 mix64(u64 k) {
     // murmur3 fmix64 finaliser
     k ^= k >> 33;

@@ -313,6 +313,14 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
                 if (c < A.n_tiles) t = c;
             }
             s_tile = t;
+            if (SPEC && t != ~0u) {
+                // the next tile's key and value columns head for L2 while
+                // this tile is processed
+                const u64 n0 = (u64)(A.first_tile + t) * (u64)(ROWS * NT);
+                const u64 nb = (min(A.n_rows, n0 + (u64)(ROWS * NT)) - n0) * 8;
+                l2_prefetch((const long long *)P.cols[P.key_col[0]].data + n0, nb);
+                l2_prefetch((const long long *)P.cols[R.vcol[0]].data + n0, nb);
+            }
         }
         const u64 t0 = (u64)(A.first_tile + tile) * (u64)(ROWS * NT);
         const u64 t1 = min(A.n_rows, t0 + (u64)(ROWS * NT));
@@ -578,10 +586,16 @@ __global__ void __launch_bounds__(RADIX_BLOCK, 1)
         for (int w = 0; w < WM; w++) wd[(size_t)i * WM + w] = P.word_init[1 + w];
     }
     if (threadIdx.x == 0) s_new = 0;
-    __syncthreads();
     const u32 p = blockIdx.x;
     const u64 n = min((u64)X.cursor[(u64)p * CURSOR_PAD], (u64)X.part_cap[p]);
     const u64 *base = X.part + X.part_off[p] * TV;
+    if (threadIdx.x < 32) {
+        // the partition's tuples head for L2 in 32 KB pieces, one per lane
+        const u64 bytes = n * TV * 8, piece = 32768;
+        for (u64 o = (u64)threadIdx.x * piece; o < bytes; o += 32 * piece)
+            l2_prefetch((const char *)base + o, min(piece, bytes - o));
+    }
+    __syncthreads();
     volatile u64 *vk = keys;
     for (u64 b0 = threadIdx.x - lane; b0 < n; b0 += blockDim.x) {
         const u64 i = b0 + lane;
