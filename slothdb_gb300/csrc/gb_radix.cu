@@ -313,14 +313,6 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
                 if (c < A.n_tiles) t = c;
             }
             s_tile = t;
-            if (SPEC && t != ~0u) {
-                // the next tile's key and value columns head for L2 while
-                // this tile is processed
-                const u64 n0 = (u64)(A.first_tile + t) * (u64)(ROWS * NT);
-                const u64 nb = (min(A.n_rows, n0 + (u64)(ROWS * NT)) - n0) * 8;
-                l2_prefetch((const long long *)P.cols[P.key_col[0]].data + n0, nb);
-                l2_prefetch((const long long *)P.cols[R.vcol[0]].data + n0, nb);
-            }
         }
         const u64 t0 = (u64)(A.first_tile + tile) * (u64)(ROWS * NT);
         const u64 t1 = min(A.n_rows, t0 + (u64)(ROWS * NT));
@@ -387,36 +379,32 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
                         }
                     }
                     if (hot) {
-                        if (hidx < (u32)REG_HOT) {
+                        if (SPEC) {
+                            // one path for every hot tier (lanes of a warp hit
+                            // different tiers; separate paths would run one after
+                            // another): branch-free register counts for the
+                            // REG_HOT hottest keys, one native 32-bit shared
+                            // atomic for the other counts, and the sum as one
+                            // fire-and-forget reduction into this CTA's hot slice
+                            // in L2 (no FP64 arithmetic on the SM, no shared
+                            // 64-bit compare-and-swap loop)
+#pragma unroll
+                            for (int k = 0; k < REG_HOT; k++) rc[k] += hidx == (u32)k ? 1u : 0u;
+                            if (hidx >= (u32)REG_HOT)
+                                atomicAdd((int)hidx < NPRIV ? mypc + hidx : sc + (hidx - NPRIV), 1u);
+                            u64 *hw = hpart + (size_t)hidx * W + P.ops[0].word;
+                            if (SPEC == OP_ADD_F) atomicAdd((double *)hw, __longlong_as_double((i64)v[0]));
+                            else atomicAdd((unsigned long long *)hw, (unsigned long long)v[0]);
+                        } else if (hidx < (u32)REG_HOT) {
 #pragma unroll
                             for (int k = 0; k < REG_HOT; k++) {
                                 if (hidx == (u32)k) {
                                     rc[k]++;
-                                    if (SPEC != OP_ADD_F) {
 #pragma unroll
-                                        for (int i = 0; i < NOPS; i++)
-                                            rw[k][i] = op_combine(SPEC ? SPEC : P.ops[i].kind, rw[k][i], v[i]);
-                                    }
+                                    for (int i = 0; i < NOPS; i++)
+                                        rw[k][i] = op_combine(P.ops[i].kind, rw[k][i], v[i]);
                                 }
                             }
-                            // FP64 runs at a small fraction of the integer rate on
-                            // this part, and a warp's register adds cost one FP64
-                            // instruction per hot key present: the DOUBLE sum of
-                            // a register-tier row goes to the L2 slice instead
-                            if (SPEC == OP_ADD_F)
-                                atomicAdd((double *)(hpart + (size_t)hidx * W + P.ops[0].word),
-                                          __longlong_as_double((i64)v[0]));
-                        } else if (SPEC) {
-                            // the count stays in shared memory (native 32-bit
-                            // atomics); the sum is a fire-and-forget reduction
-                            // into this CTA's hot slice in L2 (native 64-bit
-                            // adds there; a shared 64-bit atomic would be a
-                            // compare-and-swap loop)
-                            if ((int)hidx < NPRIV) atomicAdd(&mypc[hidx], 1u);
-                            else atomicAdd(&sc[hidx - NPRIV], 1u);
-                            u64 *hw = hpart + (size_t)hidx * W + P.ops[0].word;
-                            if (SPEC == OP_ADD_F) atomicAdd((double *)hw, __longlong_as_double((i64)v[0]));
-                            else atomicAdd((unsigned long long *)hw, (unsigned long long)v[0]);
                         } else if ((int)hidx < NPRIV) {
                             // warp-private state: only lanes of this warp contend
                             atomicAdd(&mypc[hidx], 1u);
