@@ -38,10 +38,10 @@ sys.path.insert(0, ROOT)
 METRIC = "GROUP BY rows/s & HBM GB/s at 100M rows; batched queries/s and p99 vs plain"
 N_VALUES = 20_000_000
 EST_GROUPS = 8_000_000  # planner estimate handed to the operator
-# DRAM bytes per input row of the dominant kernel (ncu capture of the 30M-row
-# case summarised in profiles/radix_groupby_zipf100M.md): (490.6 MB read +
-# 126.6 MB written) / 30M rows
-TRAFFIC_PER_ROW = {"k_partition": (490.61 + 126.64) * 1e6 / 30e6}
+# DRAM bytes per input row of the dominant kernel (one ncu capture of the
+# 30M-row case of the same workload): (490.7 MB read + 127.5 MB written) /
+# 30M rows
+TRAFFIC_PER_ROW = {"k_partition": (490.74 + 127.53) * 1e6 / 30e6}
 
 
 def parse():

@@ -1025,14 +1025,11 @@ static gb_status radix_emit(gb_agg *h, cudaStream_t st) {
     const u64 np = 1ull << R.pbits;
     gb_status s;
     Ctl *dctl = (Ctl *)h->ctl_buf.p;
-    // capacity bound: tuples in partitions + hot keys + HBM-table slots
+    // capacity bound: tuples the partition regions hold (their capacities,
+    // known on the host: no device round trip) + hot keys + HBM-table slots
     u64 tuples = 0;
-    if (h->r_ready) {
-        std::vector<u32> cur((size_t)np * CURSOR_PAD);
-        GB_CUDA(cudaMemcpyAsync(cur.data(), h->r_cursor.p, cur.size() * 4, cudaMemcpyDeviceToHost, st));
-        GB_CUDA(cudaStreamSynchronize(st));
-        for (u64 p = 0; p < np; p++) tuples += std::min<u64>(cur[p * CURSOR_PAD], h->h_capv[p]);
-    }
+    if (h->r_ready)
+        for (u64 p = 0; p < np; p++) tuples += h->h_capv[p];
     u64 cap = tuples + (u64)R.nh + h->cap + 2;
     if ((s = alloc_outputs(h, cap))) return s;
     // a partition whose groups overflow its shared table folds the rest into

@@ -17,7 +17,7 @@
 //
 // The engine types below are minimal stand-ins with the reference's names so
 // that this operator and its tests compile on their own; inside SlothDB the
-// operator uses the engine's own types (INTEGRATION.md shows the binding).
+// operator uses the engine's own types in their place.
 // Group keys and aggregate arguments are input column indices — the planner
 // places a projection below the operator for expressions.  Failures throw
 // GpuAggregateError (SlothDB converts it to InternalException); there is no
