@@ -17,6 +17,7 @@
 #include <cstring>
 #include <map>
 #include <random>
+#include <set>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -277,6 +278,43 @@ static void test_errors_are_reported() {
     REQUIRE(threw);
 }
 
+static void test_count_distinct() {
+    // SELECT DISTINCT x over (1, 1, 2, 2, 3) has 3 rows
+    // (test_advanced_sql.cpp:11-18): COUNT(DISTINCT x) under a constant key
+    auto src = std::make_unique<ColumnSource>(std::vector<LogicalType>{INTEGER_T, INTEGER_T}, 5);
+    src->ints = {{0, 0, 0, 0, 0}, {1, 1, 2, 2, 3}};
+    PhysicalGpuHashAggregate agg({0}, {{GB_AGG_COUNT_DISTINCT, 1}}, {INTEGER_T, BIGINT_T}, {INTEGER_T, INTEGER_T});
+    agg.children.push_back(std::move(src));
+    agg.Init();
+    auto rows = pull(agg);
+    REQUIRE(rows.size() == 1 && rows[0].cells[1] == "3");
+    // grouped: NULL values never counted, a group of NULL values counts 0
+    const idx_t n = 3000;
+    auto src2 = std::make_unique<ColumnSource>(std::vector<LogicalType>{INTEGER_T, BIGINT_T}, n);
+    src2->ints.assign(2, std::vector<int64_t>(n));
+    src2->nulls.assign(2, std::vector<bool>(n, false));
+    std::map<std::string, std::set<int64_t>> want;
+    for (idx_t i = 0; i < n; i++) {
+        const int64_t k = (int64_t)(i % 7), v = (int64_t)((i * 13) % 50);
+        src2->ints[0][i] = k;
+        src2->ints[1][i] = v;
+        src2->nulls[1][i] = (i % 9) == 0 || k == 6;
+        auto &w = want[std::to_string(k)];
+        if (!src2->nulls[1][i]) w.insert(v);
+    }
+    PhysicalGpuHashAggregate agg2({0}, {{GB_AGG_COUNT_DISTINCT, 1}, {GB_AGG_COUNT_STAR, -1}},
+                                  {INTEGER_T, BIGINT_T, BIGINT_T}, {INTEGER_T, BIGINT_T});
+    agg2.children.push_back(std::move(src2));
+    agg2.Init();
+    auto rows2 = pull(agg2);
+    REQUIRE(rows2.size() == want.size());
+    for (auto &r : rows2) {
+        auto it = want.find(r.cells[0]);
+        REQUIRE(it != want.end());
+        if (it != want.end()) REQUIRE(r.cells[1] == std::to_string(it->second.size()));
+    }
+}
+
 int main() {
     test_hash_aggregate_known_answer();
     test_emp_group_by_dept();
@@ -284,6 +322,7 @@ int main() {
     test_plain_million_rows_and_reexecution();
     test_nulls_filter_and_topn();
     test_errors_are_reported();
+    test_count_distinct();
     if (g_fail) {
         std::fprintf(stderr, "%d check(s) failed\n", g_fail);
         return 1;
