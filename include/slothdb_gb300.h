@@ -199,7 +199,10 @@ uint64_t gb_agg_kernel_launches(const gb_agg *h);
  *   "ctas_per_sm" persistent CTAs per SM (hash)
  *   "tile_rows"   rows per claimed tile (hash)
  *   "hot_slots"   heavy-hitter table slots (power of two, radix)
- *   "radix_bits"  log2 of the partition count, 6..12 (radix) */
+ *   "radix_bits"  log2 of the partition count, 6..12 (radix)
+ *   "radix_precombine"  1 = the partition pass combines a warp's equal keys
+ *                 before folding, 0 = folds tuple by tuple (radix; default 0
+ *                 when every op is a DOUBLE SUM, else 1) */
 gb_status gb_agg_set_option(gb_agg *h, const char *name, int64_t value);
 /* 1 = radix mode, 0 = hash mode. */
 int32_t gb_agg_get_mode(const gb_agg *h);

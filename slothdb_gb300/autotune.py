@@ -103,7 +103,8 @@ def groupby_candidates(est_groups: int, radix_ok: bool = True):
                 c.append({"mode": 1, "smem_slots": smem, "tile_rows": tile, "ctas_per_sm": ctas})
     if radix_ok and est_groups >= (1 << 16):
         for bits in (8, 10, 12):
-            c.append({"mode": 2, "radix_bits": bits})
+            for pre in (0, 1):
+                c.append({"mode": 2, "radix_bits": bits, "radix_precombine": pre})
     return c
 
 

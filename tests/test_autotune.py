@@ -48,7 +48,7 @@ def test_pick_best_skips_failing_candidates():
 
 
 def test_candidate_sets_are_valid_option_names():
-    names = {"mode", "smem_slots", "tile_rows", "ctas_per_sm", "radix_bits"}
+    names = {"mode", "smem_slots", "tile_rows", "ctas_per_sm", "radix_bits", "radix_precombine"}
     for c in autotune.groupby_candidates(1 << 20):
         assert set(c) <= names
     assert any(c.get("mode") == 2 for c in autotune.groupby_candidates(1 << 20))
