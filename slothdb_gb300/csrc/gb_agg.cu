@@ -2119,7 +2119,8 @@ gb_status gb_agg_view(gb_agg *h, AggView *v) {
         set_error("ingest after finalize (call gb_agg_reset first)");
         return GB_ERR_STATE;
     }
-    v->n_cols = h->plan.n_cols;
+    v->n_cols = (int)h->col_types.size();
+    v->str_col = h->str_col;
     v->col_types = h->col_types.data();
     v->n_filters = h->plan.n_filters;
     for (int i = 0; i < h->plan.n_filters; i++) v->filters[i] = h->plan.filters[i];
@@ -2136,6 +2137,43 @@ gb_status gb_agg_ingest_prefiltered(gb_agg *h, const gb_col *cols, uint64_t nrow
     h->plan.n_filters = nf;
     h->nullable_mask = saved_mask;
     return s;
+}
+
+gb_status gb_agg_ingest_prefiltered_ids(gb_agg *h, const gb_col *cols, uint64_t nrows, const int64_t *ids,
+                                        void *stream) {
+    if (!h || h->str_col < 0 || h->finalized) {
+        set_error("string ids need a handle with a VARCHAR group key that is not finalised");
+        return GB_ERR_STATE;
+    }
+    if (nrows == 0) return GB_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int nc = (int)h->col_types.size();
+    for (int c = 0; c < nc; c++) {
+        h->plan.cols[c].data = cols[c].data;
+        h->plan.cols[c].valid = nullptr;
+        h->plan.cols[c].offsets = cols[c].offsets;
+    }
+    h->plan.cols[nc].data = ids;
+    h->plan.cols[nc].valid = nullptr;
+    const int nf = h->plan.n_filters;
+    h->plan.n_filters = 0;
+    gb_status s = h->mode == 1 ? radix_ingest(h, nrows, st) : run_ingest(h, nrows, st);
+    h->plan.n_filters = nf;
+    h->rows_ingested += nrows;
+    prof_collect(h);
+    return s;
+}
+
+gb_status gb_agg_encode_strings(gb_agg *h, const uint8_t *bytes, const int64_t *offsets, uint64_t n,
+                                uint64_t total_bytes, void *stream, const int64_t **ids) {
+    if (!h || h->str_col < 0) {
+        set_error("string encode needs a handle with a VARCHAR group key");
+        return GB_ERR_STATE;
+    }
+    gb_status s = strdict_encode(h, bytes, offsets, 0, nullptr, n, total_bytes, (cudaStream_t)stream);
+    if (s) return s;
+    *ids = (const int64_t *)h->sd_ids.p;
+    return GB_OK;
 }
 
 struct gb_prof_mark {

@@ -10,7 +10,8 @@ void gb_apply_tuning(gb_agg *h);
 
 // A read-only view of the handle's spec for the Parquet ingest.
 struct AggView {
-    int n_cols;
+    int n_cols;           // spec columns
+    int str_col;          // the VARCHAR group key's column (-1: none)
     const int32_t *col_types;
     int n_filters;
     gb::Filter filters[GB_MAX_FILTERS];
@@ -19,6 +20,15 @@ gb_status gb_agg_view(gb_agg *h, AggView *v);
 void gb_agg_count_launch(gb_agg *h, int n);
 // Device-resident columns whose rows already passed the spec's filters.
 gb_status gb_agg_ingest_prefiltered(gb_agg *h, const gb_col *cols, uint64_t nrows, void *stream);
+// As above for a VARCHAR group key whose rows arrive as this handle's string
+// ids (`ids`, one per row) instead of strings: no per-row encode.
+gb_status gb_agg_ingest_prefiltered_ids(gb_agg *h, const gb_col *cols, uint64_t nrows, const int64_t *ids,
+                                        void *stream);
+// Encode `n` strings (offsets[n + 1] into `bytes`, device) into the handle's
+// string dictionary; on success *ids points at their ids (device, valid
+// until the handle's next encode).
+gb_status gb_agg_encode_strings(gb_agg *h, const uint8_t *bytes, const int64_t *offsets, uint64_t n,
+                                uint64_t total_bytes, void *stream, const int64_t **ids);
 // Profiling events around a kernel launched outside gb_agg.cu (no-ops
 // unless the handle's profiling is on).
 struct gb_prof_mark;

@@ -153,6 +153,7 @@ struct PqChunk {
     int32_t codec = 0;
     int64_t dict_off = -1;  // dictionary payload offset (-1 = none)
     uint32_t dict_n = 0;
+    uint32_t dict_bytes = 0;  // dictionary payload bytes
     uint32_t page_begin = 0, page_end = 0;  // into pages (data pages only)
 };
 
@@ -161,7 +162,8 @@ struct PqColumn {
     int32_t ptype = -1;  // parquet physical type
     int32_t gtype = 0;   // gb_type (0 = unsupported)
     int32_t repetition = 0;
-    int32_t width = 0;   // bytes per PLAIN value
+    int32_t width = 0;   // bytes per PLAIN value (0: BYTE_ARRAY)
+    bool plain_strings = false;  // a BYTE_ARRAY column with PLAIN data pages
 };
 
 struct gb_pq_file {
@@ -237,6 +239,7 @@ static gb_status parse_footer(gb_pq_file *f) {
                     break;
                 case 2: c.gtype = GB_T_BIGINT; c.width = 8; break;
                 case 5: c.gtype = GB_T_DOUBLE; c.width = 8; break;
+                case 6: c.gtype = GB_T_VARCHAR; c.width = 0; break;  // BYTE_ARRAY (UTF8 or not)
                 default: c.gtype = 0; c.width = 0; break;
                 }
                 schema.push_back(c);
@@ -344,7 +347,11 @@ static gb_status parse_pages(gb_pq_file *f, uint32_t rg, uint32_t col) {
             if (dict_n < 0) return pq_corrupt("dictionary page header");
             ch.dict_off = (int64_t)payload;
             ch.dict_n = (uint32_t)dict_n;
+            ch.dict_bytes = (uint32_t)csize;
             if ((uint64_t)dict_n * f->cols[col].width > (uint64_t)csize) return pq_corrupt("dictionary size");
+            // BYTE_ARRAY: a 4-byte length before every value
+            if (f->cols[col].gtype == GB_T_VARCHAR && (uint64_t)dict_n * 4 > (uint64_t)csize)
+                return pq_corrupt("dictionary size");
         } else if (ptype == 0 || ptype == 3) {
             if (nvals < 0) return pq_corrupt("data page header");
             PqPage pg;
@@ -357,6 +364,7 @@ static gb_status parse_pages(gb_pq_file *f, uint32_t rg, uint32_t col) {
             if (enc == 0) {
                 pg.kind = 0;
                 if ((uint64_t)nvals * f->cols[col].width > (uint64_t)csize) return pq_corrupt("PLAIN page size");
+                if (f->cols[col].gtype == GB_T_VARCHAR) f->cols[col].plain_strings = true;
             } else if (enc == 2 || enc == 8) {
                 pg.kind = 1;
                 if (csize < 1) return pq_corrupt("dictionary-index page");
@@ -378,6 +386,7 @@ static gb_status parse_pages(gb_pq_file *f, uint32_t rg, uint32_t col) {
 struct DPage {
     uint64_t off;       // payload offset in the device file
     uint64_t dict_off;  // dictionary payload offset
+    uint64_t dict_ids;  // VARCHAR: device address of the dictionary's string ids (0: fixed-width values)
     uint32_t first_row, n_values, bytes, dict_n;
     uint32_t run_base, run_cap;  // run-table slice (dictionary pages)
     int32_t kind, width;
@@ -506,6 +515,86 @@ __global__ void k_pq_runs(const uint8_t *file, const DPage *pages, const uint32_
 }
 
 
+// ------------------------------------------------- VARCHAR dictionary pages
+// A BYTE_ARRAY dictionary page holds its values PLAIN: a 4-byte little-endian
+// length, then the bytes, per value (ReadDictionaryPage / the VARCHAR branch
+// of DecodeDataPageTyped, parquet.cpp:2340-2471, 2229-2331).  A batch's
+// dictionary strings are compacted into one offsets + bytes array and
+// encoded once into the handle's string dictionary; the data pages' indices
+// then gather string ids instead of values.
+struct DDict {
+    uint64_t off;           // payload offset in the device file
+    uint64_t entry_base;    // index of the page's first value in the batch's entries
+    uint64_t compact_base;  // its first byte in the compacted strings
+    uint32_t n, bytes;      // values, payload bytes
+};
+
+// One CTA per dictionary page: windows of the payload are staged in shared
+// memory and thread 0 walks the length prefixes, writing each value's source
+// address and compacted offset.  Every length is checked against the
+// payload, and the walk must end exactly at the payload's end; anything else
+// sets ERR_CORRUPT (and the host stops before using the entries).
+__global__ void k_pq_dict_walk(const uint8_t *file, const DDict *dicts, u64 *src, int64_t *offs, Ctl *ctl) {
+    __shared__ uint8_t win[PQ_WIN];
+    __shared__ u64 s_pos;
+    __shared__ uint32_t s_i;
+    __shared__ int s_state;  // 0 walking, 1 done, 2 corrupt
+    const DDict d = dicts[blockIdx.x];
+    if (threadIdx.x == 0) {
+        s_pos = 0;
+        s_i = 0;
+        s_state = d.n == 0 ? (d.bytes == 0 ? 1 : 2) : 0;
+    }
+    __syncthreads();
+    // each window moves the walk by at least one value: n + 1 windows suffice
+    for (u64 round = 0; round <= (u64)d.n && s_state == 0; round++) {
+        const u64 w0 = s_pos;
+        const u64 wn = min((u64)PQ_WIN, (u64)d.bytes - w0);
+        for (u64 k = threadIdx.x; k < wn; k += blockDim.x) win[k] = file[d.off + w0 + k];
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            u64 pos = w0;
+            uint32_t i = s_i;
+            int state = 0;
+            while (i < d.n) {
+                if (pos + 4 > w0 + wn) {
+                    if (pos + 4 > d.bytes) state = 2;  // no room for the length
+                    break;
+                }
+                const uint8_t *q = win + (pos - w0);
+                const uint32_t len = (uint32_t)q[0] | ((uint32_t)q[1] << 8) | ((uint32_t)q[2] << 16) |
+                                     ((uint32_t)q[3] << 24);
+                if ((u64)len > (u64)d.bytes - pos - 4) {
+                    state = 2;  // the value runs past the payload
+                    break;
+                }
+                src[d.entry_base + i] = d.off + pos + 4;
+                offs[d.entry_base + i] = (int64_t)(d.compact_base + pos - 4 * (u64)i);
+                pos += 4 + (u64)len;
+                i++;
+            }
+            if (state == 0 && i == d.n) state = pos == d.bytes ? 1 : 2;
+            if (state == 0 && pos == w0) state = 2;  // no progress (cannot happen with a valid window)
+            s_pos = pos;
+            s_i = i;
+            s_state = state;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && s_state != 1) atomicOr(&ctl->err, (u32)ERR_CORRUPT);
+}
+
+// Copy each dictionary value's bytes to its compacted offset (the walk has
+// checked every range against its page).
+__global__ void k_pq_dict_copy(const uint8_t *file, const u64 *src, const int64_t *offs, u64 n, uint8_t *out) {
+    for (u64 e = blockIdx.x * (u64)blockDim.x + threadIdx.x; e < n; e += (u64)gridDim.x * blockDim.x) {
+        const uint8_t *a = file + src[e];
+        uint8_t *b = out + offs[e];
+        const int64_t len = offs[e + 1] - offs[e];
+        for (int64_t k = 0; k < len; k++) b[k] = a[k];
+    }
+}
+
 // Locate the page of `col` holding row r of the chunk's row group:
 // pages [pb, pe) are sorted by first_row.
 __device__ __forceinline__ uint32_t find_page(const DPage *pages, uint32_t pb, uint32_t pe, uint32_t r) {
@@ -569,7 +658,8 @@ __device__ __forceinline__ u64 decode_at(const uint8_t *file, const DPage &pg, c
     } else {
         idx = load_bits(file + pg.off + rn.off, (u64)(i - rn.start) * bw, bw);
     }
-    if (idx >= pg.dict_n) return 0;  // the reference maps an out-of-range index to 0
+    if (idx >= pg.dict_n) return pg.dict_ids ? ~0ull : 0;  // out of range: the reference's 0 (VARCHAR: NULL id)
+    if (pg.dict_ids) return (u64)__ldg((const long long *)pg.dict_ids + idx);
     return load_plain(file + pg.dict_off + (u64)idx * pg.width, pg.width);
 }
 
@@ -640,7 +730,8 @@ __device__ __forceinline__ u64 dict_value(const uint8_t *file, const DPage &pg, 
     } else {
         idx = load_bits(file + pg.off + rn.off, (u64)(i - rn.start) * bw, bw);
     }
-    if (idx >= pg.dict_n) return 0;  // the reference maps an out-of-range index to 0
+    if (idx >= pg.dict_n) return pg.dict_ids ? ~0ull : 0;  // out of range: the reference's 0 (VARCHAR: NULL id)
+    if (pg.dict_ids) return (u64)__ldg((const long long *)pg.dict_ids + idx);
     return load_plain(file + pg.dict_off + (u64)idx * pg.width, pg.width);
 }
 
@@ -989,6 +1080,10 @@ struct PqScratch {
            ctl_cap = 0;
     void *out[GB_MAX_COLS] = {};
     size_t out_cap_rows = 0;
+    // VARCHAR dictionary pages of a batch: descriptors, value sources,
+    // compacted offsets and bytes
+    void *dicts = nullptr, *dsrc = nullptr, *doffs = nullptr, *dbytes = nullptr;
+    size_t dicts_cap = 0, dsrc_cap = 0, doffs_cap = 0, dbytes_cap = 0;
 };
 
 static gb_status grow(void *&p, size_t &cap, size_t need) {
@@ -1027,11 +1122,63 @@ void gb_pq_release_scratch(gb_agg *h) {
         s = it->second;
         g_pq_scratch.erase(it);
     }
-    for (void *p : {s->file_dev, s->pages, s->runs, s->page_runs, s->dict_pages, s->col_pages, s->chunks, s->ctl})
+    for (void *p : {s->file_dev, s->pages, s->runs, s->page_runs, s->dict_pages, s->col_pages, s->chunks, s->ctl,
+                    s->dicts, s->dsrc, s->doffs, s->dbytes})
         if (p) cudaFree(p);
     for (void *p : s->out)
         if (p) cudaFree(p);
     delete s;
+}
+
+// The batch's dictionary pages of VARCHAR file column `fcol`: walk, compact
+// and encode their values into the handle's string dictionary.  *ids gets
+// the ids of all values, page after page in row-group order (device).
+static gb_status pq_varchar_dict(gb_agg *h, const gb_pq_file *f, PqScratch *S, const uint8_t *dfile, uint64_t base,
+                                 uint32_t rg_begin, uint32_t rg_end, int fcol, Ctl *dctl, cudaStream_t st,
+                                 const int64_t **ids) {
+    std::vector<DDict> dd;
+    uint64_t D = 0, B = 0;
+    for (uint32_t g = rg_begin; g < rg_end; g++) {
+        const PqChunk &ch = f->chunks[g][fcol];
+        if (ch.dict_off < 0) {
+            if (ch.page_begin != ch.page_end) return pq_corrupt("VARCHAR column chunk without a dictionary page");
+            continue;
+        }
+        if ((uint64_t)ch.dict_n * 4 > ch.dict_bytes) return pq_corrupt("dictionary size");
+        DDict d{};
+        d.off = (uint64_t)ch.dict_off - base;
+        d.entry_base = D;
+        d.compact_base = B;
+        d.n = ch.dict_n;
+        d.bytes = ch.dict_bytes;
+        D += d.n;
+        B += (uint64_t)d.bytes - 4 * (uint64_t)d.n;
+        dd.push_back(d);
+    }
+    if (D == 0) {
+        set_error("VARCHAR column with an empty dictionary");
+        return GB_ERR_UNSUPPORTED;
+    }
+    gb_status s;
+    if ((s = grow(S->dicts, S->dicts_cap, dd.size() * sizeof(DDict) + 16)) ||
+        (s = grow(S->dsrc, S->dsrc_cap, D * 8 + 16)) || (s = grow(S->doffs, S->doffs_cap, (D + 1) * 8 + 16)) ||
+        (s = grow(S->dbytes, S->dbytes_cap, B + 16)))
+        return s;
+    const int64_t total = (int64_t)B;
+    GB_CUDA(cudaMemcpyAsync(S->dicts, dd.data(), dd.size() * sizeof(DDict), cudaMemcpyHostToDevice, st));
+    GB_CUDA(cudaMemcpyAsync((int64_t *)S->doffs + D, &total, 8, cudaMemcpyHostToDevice, st));
+    k_pq_dict_walk<<<(unsigned)dd.size(), 128, 0, st>>>(dfile, (const DDict *)S->dicts, (u64 *)S->dsrc,
+                                                        (int64_t *)S->doffs, dctl);
+    GB_CUDA(cudaGetLastError());
+    Ctl c;
+    GB_CUDA(cudaMemcpyAsync(&c, dctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if ((s = pq_fail_if_err(c))) return s;  // no value is copied from a page that failed its walk
+    k_pq_dict_copy<<<(unsigned)std::min<uint64_t>((D + 255) / 256, (uint64_t)sm_count() * 8), 256, 0, st>>>(
+        dfile, (const u64 *)S->dsrc, (const int64_t *)S->doffs, D, (uint8_t *)S->dbytes);
+    GB_CUDA(cudaGetLastError());
+    gb_agg_count_launch(h, 2);
+    return gb_agg_encode_strings(h, (const uint8_t *)S->dbytes, (const int64_t *)S->doffs, D, B, st, ids);
 }
 
 extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg_begin, uint32_t rg_end,
@@ -1074,6 +1221,21 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
             return GB_ERR_INVALID;
         }
     }
+    // a VARCHAR column is the group key, dictionary-encoded in the file
+    int vc = -1;
+    for (int c = 0; c < nc; c++) {
+        if (v.col_types[c] != GB_T_VARCHAR) continue;
+        if (c != v.str_col) {
+            set_error("VARCHAR column %d is not the group key", c);
+            return GB_ERR_UNSUPPORTED;
+        }
+        if (f->cols[col_map[c]].plain_strings) {
+            set_error("Parquet column '%s' has PLAIN BYTE_ARRAY pages; the GPU path decodes dictionary-encoded "
+                      "VARCHAR columns", f->cols[col_map[c]].name.c_str());
+            return GB_ERR_UNSUPPORTED;
+        }
+        vc = c;
+    }
     PqScratch *S = g_scratch_for(h);
     // device bytes: the uploaded file, or this batch's byte range copied now
     uint64_t lo = ~0ull, hi = 0;
@@ -1111,7 +1273,7 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
         return s;
     GB_CUDA(cudaMemsetAsync(S->ctl, 0, sizeof(Ctl), st));
     Ctl *dctl = (Ctl *)S->ctl;
-    if (mem == GB_MEM_DEVICE) {
+    if (mem == GB_MEM_DEVICE && vc < 0) {
         // the resident file's page index (built once), columns picked per call
         if ((s = pq_build_index(f, st))) return s;
         const int nfc = (int)f->cols.size();
@@ -1130,6 +1292,20 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
         uint32_t run_total = 0;
         if ((s = pq_page_table(f, rg_begin, rg_end, col_map, nc, base, pages, dict_pages, col_pages, run_total)))
             return s;
+        if (vc >= 0) {
+            // the VARCHAR key's data pages gather string ids: page after page,
+            // each row group's dictionary entries start at its running base
+            const int64_t *ids = nullptr;
+            if ((s = pq_varchar_dict(h, f, S, dfile, base, rg_begin, rg_end, col_map[vc], dctl, st, &ids))) return s;
+            uint64_t eb = 0;
+            for (uint32_t g = rg_begin; g < rg_end; g++) {
+                const PqChunk &ch = f->chunks[g][col_map[vc]];
+                const uint32_t k = (g - rg_begin) * (uint32_t)nc + (uint32_t)vc;
+                for (uint32_t p = col_pages[2 * k]; p < col_pages[2 * k + 1]; p++)
+                    if (pages[p].kind == 1) pages[p].dict_ids = (uint64_t)(uintptr_t)(ids + eb);
+                if (ch.dict_off >= 0) eb += ch.dict_n;
+            }
+        }
         if ((s = grow(S->pages, S->pages_cap, pages.size() * sizeof(DPage) + 16)) ||
             (s = grow(S->runs, S->runs_cap, (size_t)run_total * sizeof(DRun) + 16)) ||
             (s = grow(S->page_runs, S->page_runs_cap, pages.size() * 8 + 16)) ||
@@ -1175,7 +1351,7 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
     memset(&P, 0, sizeof P);
     P.n_cols = nc;
     for (int c = 0; c < nc; c++) {
-        P.out_type[c] = v.col_types[c];
+        P.out_type[c] = c == vc ? GB_T_BIGINT : v.col_types[c];  // VARCHAR: its string ids
         P.out[c] = S->out[c];
     }
     P.n_filters = v.n_filters;
@@ -1198,5 +1374,6 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
     // the survivors go through the ordinary ingest (filters already applied)
     gb_col cols[GB_MAX_COLS];
     for (int q = 0; q < nc; q++) cols[q] = {S->out[q], nullptr, nullptr};
+    if (vc >= 0) return gb_agg_ingest_prefiltered_ids(h, cols, c.out_count, (const int64_t *)S->out[vc], stream);
     return gb_agg_ingest_prefiltered(h, cols, c.out_count, stream);
 }

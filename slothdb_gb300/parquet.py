@@ -3,6 +3,8 @@
 Writes uncompressed files with DATA_PAGE (v1) pages, REQUIRED columns, and
 per column either PLAIN values or a PLAIN dictionary page plus
 RLE_DICTIONARY-encoded indices (RLE / bit-packed hybrid, fixed bit width).
+BYTE_ARRAY (VARCHAR) columns are written dictionary-encoded, each value of
+the dictionary page a 4-byte little-endian length followed by its bytes.
 The thrift compact protocol encoder is the project's own; the RLE/bit-packed
 hybrid encoder is ``pq_encode.c``.  Files written here are readable by any
 Parquet reader (checked against pyarrow in the CPU tests where available).
@@ -20,7 +22,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 _ENC_LIB = os.path.join(HERE, "_build", "libpqenc.so")
 
 # parquet.thrift enum values
-T_INT32, T_INT64, T_DOUBLE = 1, 2, 5
+T_INT32, T_INT64, T_DOUBLE, T_BYTE_ARRAY = 1, 2, 5, 6
 ENC_PLAIN, ENC_RLE, ENC_BIT_PACKED, ENC_RLE_DICTIONARY = 0, 3, 4, 8
 PAGE_DATA, PAGE_DICT = 0, 2
 REQUIRED = 0
@@ -170,9 +172,13 @@ def _page_header(ptype, size, num_values=None, encoding=None, dict_values=None):
 
 class Column:
     """One REQUIRED column.  values: numpy array of the physical type, or for
-    dictionary encoding `dictionary` (values) + `indices` (uint32)."""
+    dictionary encoding `dictionary` (values; a list of bytes for BYTE_ARRAY)
+    + `indices` (uint32).  shuffle_seed: each row group writes the dictionary
+    in its own order (a permutation drawn from the seed and the row-group
+    index) with the indices remapped, so the decoded values stay the same."""
 
-    def __init__(self, name, ptype, values=None, dictionary=None, indices=None, int16=False, page_rows=None):
+    def __init__(self, name, ptype, values=None, dictionary=None, indices=None, int16=False, page_rows=None,
+                 shuffle_seed=None):
         self.name = name
         self.page_rows = page_rows  # overrides the file-wide page size
         self.ptype = ptype
@@ -180,6 +186,7 @@ class Column:
         self.dictionary = dictionary
         self.indices = indices
         self.int16 = int16
+        self.shuffle_seed = shuffle_seed
 
     @property
     def dict_encoded(self):
@@ -191,6 +198,12 @@ class Column:
 
 def _np_dtype(ptype):
     return {T_INT32: "<i4", T_INT64: "<i8", T_DOUBLE: "<f8"}[ptype]
+
+
+def _dict_payload(ptype, dictionary):
+    if ptype == T_BYTE_ARRAY:
+        return b"".join(struct.pack("<I", len(x)) + bytes(x) for x in dictionary)
+    return np.ascontiguousarray(dictionary, dtype=_np_dtype(ptype)).tobytes()
 
 
 def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="slothdb_gb300 writer"):
@@ -208,9 +221,17 @@ def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="sloth
         for c in columns:
             start = pos
             dict_off = None
+            rg_dict, rg_idx = c.dictionary, c.indices
+            if c.dict_encoded and c.shuffle_seed is not None:
+                perm = np.random.default_rng([c.shuffle_seed, rg0]).permutation(len(c.dictionary))
+                inv = np.empty_like(perm)
+                inv[perm] = np.arange(len(perm))
+                rg_dict = [c.dictionary[i] for i in perm] if c.ptype == T_BYTE_ARRAY else np.asarray(c.dictionary)[perm]
+                rg_idx = np.zeros(len(c.indices), dtype=np.uint32)
+                rg_idx[rg0:rg1] = inv[c.indices[rg0:rg1]]
             if c.dict_encoded:
-                dvals = np.ascontiguousarray(c.dictionary, dtype=_np_dtype(c.ptype)).tobytes()
-                hdr = _page_header(PAGE_DICT, len(dvals), dict_values=len(c.dictionary))
+                dvals = _dict_payload(c.ptype, rg_dict)
+                hdr = _page_header(PAGE_DICT, len(dvals), dict_values=len(rg_dict))
                 dict_off = pos
                 parts += [hdr, dvals]
                 pos += len(hdr) + len(dvals)
@@ -220,7 +241,7 @@ def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="sloth
             for p0 in range(rg0, rg1, prows):
                 p1 = min(rg1, p0 + prows)
                 if c.dict_encoded:
-                    payload = bytes([bw]) + rle_hybrid(c.indices[p0:p1], bw)
+                    payload = bytes([bw]) + rle_hybrid(rg_idx[p0:p1], bw)
                     enc = ENC_RLE_DICTIONARY
                 else:
                     payload = np.ascontiguousarray(c.values[p0:p1], dtype=_np_dtype(c.ptype)).tobytes()
@@ -311,3 +332,36 @@ def filter_groupby_file(n_rows=200_000_000, seed=2, n_dict=65_536, row_group_row
             Column("v", T_INT64, values=v)]
     data = write(cols, row_group_rows=row_group_rows, page_rows=page_rows)
     return data, dictionary[idx], f, v
+
+
+def varchar_groupby_file(n_rows=200_000, seed=6, n_dict=3000, row_group_rows=50_000, page_rows=8192):
+    """A file whose group key is VARCHAR, dictionary-encoded: n_dict strings
+    of 8..32 characters over [a-z0-9] (each row group writes them in its own
+    order), indices in runs of geometric length (mean 4); f INT16 (stored
+    INT32) uniform [0, 1000) PLAIN; v INT64 uniform [-10^6, 10^6] PLAIN.
+    Returns (file bytes, dictionary (list of bytes), indices, f, v)."""
+    rng = np.random.default_rng(seed)
+    alphabet = np.frombuffer(b"abcdefghijklmnopqrstuvwxyz0123456789", dtype=np.uint8)
+    lens = rng.integers(8, 33, n_dict)
+    dictionary = [alphabet[rng.integers(0, 36, n)].tobytes() for n in lens]
+    runs = rng.geometric(0.25, n_rows // 4 + 64)
+    while runs.sum() < n_rows:
+        runs = np.concatenate([runs, rng.geometric(0.25, n_rows // 4 + 64)])
+    vals = rng.integers(0, n_dict, len(runs), dtype=np.int64)
+    idx = np.repeat(vals.astype(np.uint32), runs)[:n_rows]
+    f = rng.integers(0, 1000, n_rows, dtype=np.int32)
+    v = rng.integers(-10**6, 10**6 + 1, n_rows, dtype=np.int64)
+    cols = [Column("name", T_BYTE_ARRAY, dictionary=dictionary, indices=idx, shuffle_seed=seed),
+            Column("f", T_INT32, values=f, int16=True),
+            Column("v", T_INT64, values=v)]
+    data = write(cols, row_group_rows=row_group_rows, page_rows=page_rows)
+    return data, dictionary, idx, f, v
+
+
+def strings_of(dictionary, idx):
+    """VARCHAR column (offsets int64[n + 1], bytes uint8) of dictionary[idx]."""
+    lens = np.array([len(x) for x in dictionary], dtype=np.int64)
+    offs = np.zeros(len(idx) + 1, dtype=np.int64)
+    np.cumsum(lens[idx], out=offs[1:])
+    blob = b"".join(dictionary[i] for i in idx.tolist())
+    return offs, np.frombuffer(blob, dtype=np.uint8) if blob else np.zeros(1, np.uint8)

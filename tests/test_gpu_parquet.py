@@ -100,3 +100,20 @@ def test_plain_key_column_and_column_map():
     aggs = [("count_star", -1), ("sum", 1)]
     orc = oracle.run_query([BIGINT, INTEGER], [0], aggs, [b, a])
     compare(run_pq(data, [BIGINT, INTEGER], [1, 0], [0], aggs), orc)
+
+
+def test_varchar_dictionary_key():
+    """A dictionary-encoded BYTE_ARRAY key (each row group with its own
+    dictionary order): dictionary strings encoded once per batch into the
+    handle's string dictionary, data pages gathering string ids; host and
+    resident files, one or several batches, with a filter."""
+    data, d, idx, f, v = pq.varchar_groupby_file(n_rows=300_000, row_group_rows=60_000, page_rows=8192)
+    names = pq.strings_of(d, idx)
+    types = [capi.VARCHAR, SMALLINT, BIGINT]
+    aggs = [("count_star", -1), ("sum", 2), ("max", 1)]
+    for filters in ([], [(1, "<", 500)]):
+        orc = oracle.run_query(types, [0], aggs, [names, f.astype(np.int16), v], filters=filters)
+        for device, batches in [(False, 1), (True, 1), (False, 3), (True, 5)]:
+            gpu = run_pq(data, types, [0, 1, 2], [0], aggs, filters=filters, est_groups=3000, device=device,
+                         batches=batches)
+            compare(gpu, orc)

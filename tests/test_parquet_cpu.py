@@ -67,3 +67,20 @@ def test_malformed_files_are_rejected(damage):
     with pytest.raises(capi.GbError) as e:
         capi.ParquetFile(bytes(b))
     assert e.value.status in (6,)  # GB_ERR_CORRUPT
+
+
+def test_varchar_dictionary_file_writer_and_parser():
+    """BYTE_ARRAY dictionary-encoded key: pyarrow decodes the project writer's
+    file (each row group with its own dictionary order) to the same strings,
+    and the library's parser reports the column as VARCHAR."""
+    data, d, idx, f, v = pq.varchar_groupby_file(n_rows=30_000, row_group_rows=8_000, page_rows=2048)
+    pa = pytest.importorskip("pyarrow.parquet")
+    t = pa.read_table(io.BytesIO(data))
+    got = [x if isinstance(x, bytes) else x.encode() for x in t.column("name").to_pylist()]
+    assert got == [d[i] for i in idx.tolist()]
+    pf = capi.ParquetFile(data)
+    assert pf.num_row_groups == 4
+    assert pf.columns() == [("name", capi.VARCHAR), ("f", capi.SMALLINT), ("v", capi.BIGINT)]
+    pf.close()
+    offs, blob = pq.strings_of(d, idx[:5])
+    assert [bytes(blob[offs[i]:offs[i + 1]]) for i in range(5)] == [d[i] for i in idx[:5].tolist()]
