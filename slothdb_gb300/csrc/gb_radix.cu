@@ -17,15 +17,24 @@
 //               values) tuple to partition p = top hash bits through a
 //               per-CTA write-combining buffer of wcb tuples per partition,
 //               flushed in aligned groups (one global atomic per flush).
+//               The specialised instance (one non-NULL BIGINT key, one SUM,
+//               no predicates) keeps only the hot counts in registers and
+//               shared memory; every hot row's sum is a fire-and-forget L2
+//               reduction into the CTA's hot slice.
 //               Partition regions have per-partition capacities; a region
 //               that overflows is grown (and its tuples moved) by the host,
 //               and a re-execution keeps the grown capacities.
-//   P2 agg:     one CTA per partition: a shared open-addressing table, a warp
-//               pre-combine of equal keys (32-bit hash match checked on the
-//               full key), shared atomics; a table that overflows folds the
-//               rest into the HBM hash table.
-//   P3 hot:     per-CTA hot partials are reduced in a fixed order (hence a
-//               deterministic DOUBLE sum for hot keys) and emitted.
+//   P2 agg:     one CTA per partition: a shared open-addressing table (keys,
+//               32-bit counts) with either the state words beside it and a
+//               warp pre-combine of equal keys (32-bit hash match checked on
+//               the full key), or, when every op is a DOUBLE SUM, the words
+//               in the partition's L2 slice folded tuple by tuple as L2
+//               reductions; a table that overflows folds the rest into the
+//               HBM hash table.
+//   P3 hot:     per-CTA hot partials are reduced in a fixed order and
+//               emitted.  (DOUBLE sums are exact to rounding but, as with any
+//               atomic accumulation, their last bits depend on the order the
+//               rows arrive in.)
 //
 // A key is hot for the whole query or never, and lives in exactly one
 // partition, so every group is emitted exactly once.  Bounded probes fall
