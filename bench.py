@@ -197,12 +197,12 @@ def run_batch(args):
     queue + CUDA graph); plain = the same queries one after another, each
     through its own operator handle (ingest + finalize per query)."""
     ws, rank, local = dist_env()
+    if args.impl == "reference":  # host cores only; rank 0 alone under torchrun
+        return run_batch_reference(args) if rank == 0 else None
     import torch
     torch.cuda.set_device(local)
     from slothdb_gb300 import capi, datagen
     capi.load(build_if_missing=True)
-    if args.impl == "reference":
-        return run_batch_reference(args)
     t0 = time.time()
     shapes = datagen.batch_shapes(n_tables=args.tables, seed=3)
     tables = [datagen.batch_table_device(sh) for sh in shapes]
@@ -374,12 +374,12 @@ def run_serve(args):
     U[1%, 100%]; admission budget --budget-gb of estimated device bytes.
     Runs the same stream with continuous batching and one query at a time."""
     ws, rank, local = dist_env()
+    if args.impl == "reference":  # host cores only; rank 0 alone under torchrun
+        return run_serve_reference(args) if rank == 0 else None
     import torch
     torch.cuda.set_device(local)
     from slothdb_gb300 import capi, datagen
     capi.load(build_if_missing=True)
-    if args.impl == "reference":
-        return run_serve_reference(args)
     t0 = time.time()
     tabs, rows_of, res_bytes = [], {}, 0
     for i, t in enumerate(datagen.SERVE_TABLES):
@@ -557,10 +557,18 @@ def run_parquet(args):
     e2e = rows/s from the file in pinned host memory (row groups copied to
     HBM inside the call)."""
     ws, rank, local = dist_env()
+    from slothdb_gb300 import parquet as pq
+    if args.impl == "reference" and rank != 0:
+        return  # rank 0 alone runs the reference arm
+    rows = args.pq_rows
+    t0 = time.time()
+    data, key, f, v = pq.filter_groupby_file(n_rows=rows, row_group_rows=1_000_000)
+    gen_s = time.time() - t0
+    if args.impl == "reference":
+        return run_parquet_reference(args, key, f, v, rows)
     import torch
     torch.cuda.set_device(local)
     from slothdb_gb300 import capi
-    from slothdb_gb300 import parquet as pq
     capi.load(build_if_missing=True)
     peaks = {}
     try:
@@ -568,12 +576,6 @@ def run_parquet(args):
     except Exception:
         pass
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
-    rows = args.pq_rows
-    t0 = time.time()
-    data, key, f, v = pq.filter_groupby_file(n_rows=rows, row_group_rows=1_000_000)
-    gen_s = time.time() - t0
-    if args.impl == "reference":
-        return run_parquet_reference(args, key, f, v, rows)
     file_bytes = len(data)
     types = [capi.INTEGER, capi.SMALLINT, capi.BIGINT]
     aggs = [("sum", 2), ("count_star", -1)]
@@ -722,8 +724,8 @@ def run_distinct(args):
     gen_s = time.time() - t0
     types = [2, 2]
     aggs = [("count_distinct", 1), ("count_star", -1)]
-    if args.impl == "reference":
-        return run_distinct_reference(args, k, v, types, aggs)
+    if args.impl == "reference":  # host cores only; rank 0 alone under torchrun
+        return run_distinct_reference(args, k, v, types, aggs) if rank == 0 else None
     import torch
     torch.cuda.set_device(local)
     from slothdb_gb300 import capi
