@@ -46,6 +46,10 @@ def cases():
     (offs, data), s, m = datagen.varchar_table(40_000, 2000, seed=4)
     out["varchar_40k"] = ([VARCHAR, BIGINT, INTEGER], [0], [("count_star", -1), ("sum", 1), ("max", 2)], [],
                           [(offs, data), s, m])
+    a, b, s, m = datagen.composite(50_000, 400, seed=5)
+    out["distinct_50k"] = ([INTEGER, SMALLINT, BIGINT, INTEGER], [0, 1], [("count_distinct", 2), ("count_distinct", 3),
+                                                                          ("count_star", -1)], [(2, ">=", 500)],
+                           [a, b, s % 997, (m % 300).astype(np.int32)])
     return out
 
 
