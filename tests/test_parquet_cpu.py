@@ -84,3 +84,20 @@ def test_varchar_dictionary_file_writer_and_parser():
     pf.close()
     offs, blob = pq.strings_of(d, idx[:5])
     assert [bytes(blob[offs[i]:offs[i + 1]]) for i in range(5)] == [d[i] for i in idx[:5].tolist()]
+
+
+def test_varchar_dictionary_header_checked_on_open(monkeypatch):
+    """A BYTE_ARRAY dictionary page declaring more values than its payload
+    can hold (4 length bytes each) is rejected as corrupt by the parser."""
+    real = pq._page_header
+
+    def inflated(ptype, size, num_values=None, encoding=None, dict_values=None):
+        if ptype == pq.PAGE_DICT:
+            dict_values = size  # > size / 4
+        return real(ptype, size, num_values=num_values, encoding=encoding, dict_values=dict_values)
+
+    monkeypatch.setattr(pq, "_page_header", inflated)
+    data, _, _, _, _ = pq.varchar_groupby_file(n_rows=5_000, row_group_rows=5_000, page_rows=2048)
+    with pytest.raises(capi.GbError) as e:
+        capi.ParquetFile(data)
+    assert e.value.status == 6  # GB_ERR_CORRUPT
