@@ -25,8 +25,9 @@
  *    (RleDecoder::FetchRun / Next)
  *  - COUNT(DISTINCT col): each group keeps the set of the non-NULL int64
  *    values of col (src/execution/int_group_agg.cpp:89-92) and emits its
- *    size (the union of the per-thread sets, int_group_agg.cpp:154-270);
- *    here one set of (group, value) pairs per aggregate, single-threaded.
+ *    size; with several threads each keeps its own sets and the merge takes
+ *    their union per group (int_group_agg.cpp:154-270).  Here one set of
+ *    (group, value) pairs per aggregate and thread.
  *
  * Deliberate divergence: a NULL group key forms its own group (SQL
  * semantics).  The reference's in-memory chunk loop reads the key's raw
@@ -284,7 +285,7 @@ static inline void merge_states(or_state *dst, const or_state *src, const or_agg
     for (int a = 0; a < A->n_aggs; a++) {
         or_state *d = &dst[a];
         const or_state *s = &src[a];
-        d->count += s->count;
+        if (A->kind[a] != A_COUNT_DISTINCT) d->count += s->count;  /* distinct: the union, counted by the merge */
         double t = d->sum + s->sum;
         if (fabs(d->sum) >= fabs(s->sum)) d->comp += (d->sum - t) + s->sum;
         else d->comp += (s->sum - t) + d->sum;
@@ -417,18 +418,55 @@ static int run_range(or_table *t, int64_t r0, int64_t r1, const int64_t *keys, c
     return 0;
 }
 
+/* (thread-local group, value) pairs bound for one merge shard */
+typedef struct {
+    int64_t *g, *v;
+    uint64_t n, cap;
+} pvec;
+
+static int pvec_push(pvec *p, int64_t g, int64_t v) {
+    if (p->n == p->cap) {
+        uint64_t nc = p->cap ? p->cap * 2 : 256;
+        int64_t *ng = (int64_t *)realloc(p->g, nc * 8), *nv;
+        if (!ng) return -1;
+        p->g = ng;
+        nv = (int64_t *)realloc(p->v, nc * 8);
+        if (!nv) return -1;
+        p->v = nv;
+        p->cap = nc;
+    }
+    p->g[p->n] = g;
+    p->v[p->n] = v;
+    p->n++;
+    return 0;
+}
+
 typedef struct {
     or_table tab;
     int64_t r0, r1;
     const int64_t *keys;
     const uint8_t *key_null, *keep;
-    const or_aggs *A;
+    or_aggs A;  /* the query's aggregates with this thread's value sets */
+    int nshards;
+    pvec *bucket; /* [n_aggs][nshards]: this thread's pairs by merge shard */
     int rc;
 } or_job;
 
 static void *job_main(void *p) {
     or_job *j = (or_job *)p;
-    j->rc = run_range(&j->tab, j->r0, j->r1, j->keys, j->key_null, j->keep, j->A);
+    j->rc = run_range(&j->tab, j->r0, j->r1, j->keys, j->key_null, j->keep, &j->A);
+    /* hand each distinct pair to the shard that owns its group's key */
+    for (int a = 0; !j->rc && j->bucket && a < j->A.n_aggs; a++) {
+        if (j->A.kind[a] != A_COUNT_DISTINCT) continue;
+        const pset *ps = &j->A.dset[a];
+        for (uint64_t i = 0; i < ps->cap && !j->rc; i++) {
+            if (!ps->used[i]) continue;
+            const int64_t g = ps->g[i];
+            int is_null = j->tab.has_null && g == j->tab.null_g;
+            int owner = is_null ? 0 : (int)((or_mix(j->tab.gkey[g]) >> 40) % (uint64_t)j->nshards);
+            if (pvec_push(&j->bucket[a * j->nshards + owner], g, ps->v[i])) j->rc = -1;
+        }
+    }
     return NULL;
 }
 
@@ -437,6 +475,7 @@ typedef struct {
     int nt, shard, nshards;
     or_table out;
     const or_aggs *A;
+    pset *dset; /* the shard's value sets (COUNT(DISTINCT)), or NULL */
     int rc;
 } or_merge_job;
 
@@ -455,6 +494,22 @@ static void *merge_main(void *p) {
             int64_t d = tab_group(&m->out, A->n_aggs, key, is_null);
             if (d < 0) { m->rc = -1; return NULL; }
             merge_states(&m->out.st[(size_t)d * A->n_aggs], &src->st[(size_t)g * A->n_aggs], A);
+        }
+    }
+    /* COUNT(DISTINCT): the union of the threads' sets of each group */
+    for (int a = 0; m->dset && a < A->n_aggs; a++) {
+        if (A->kind[a] != A_COUNT_DISTINCT) continue;
+        for (int t = 0; t < m->nt; t++) {
+            const or_table *src = &m->jobs[t].tab;
+            const pvec *pv = &m->jobs[t].bucket[a * m->nshards + m->shard];
+            for (uint64_t i = 0; i < pv->n; i++) {
+                const int64_t g = pv->g[i];
+                int is_null = src->has_null && g == src->null_g;
+                int64_t d = tab_group(&m->out, A->n_aggs, src->gkey[g], is_null);
+                int isnew = d < 0 ? -1 : pset_insert(&m->dset[a], d, pv->v[i]);
+                if (isnew < 0) { m->rc = -1; return NULL; }
+                m->out.st[(size_t)d * A->n_aggs + a].count += isnew;
+            }
         }
     }
     return NULL;
@@ -476,7 +531,6 @@ int64_t or_groupby(int64_t n, const int64_t *keys, const uint8_t *key_null, cons
     if (nthreads > 256) nthreads = 256;
     int has_distinct = 0;
     for (int a = 0; a < n_aggs; a++) has_distinct |= agg_kind[a] == A_COUNT_DISTINCT;
-    if (has_distinct) nthreads = 1; /* the value sets are kept single-threaded */
     int64_t ng = 0;
     if (nthreads == 1) {
         or_table t;
@@ -505,31 +559,44 @@ int64_t or_groupby(int64_t n, const int64_t *keys, const uint8_t *key_null, cons
         jobs[i].keys = keys;
         jobs[i].key_null = key_null;
         jobs[i].keep = keep;
-        jobs[i].A = &A;
+        jobs[i].A = A;
+        jobs[i].nshards = nthreads;
+        if (has_distinct) {
+            jobs[i].A.dset = dsets_new(n_aggs, agg_kind);
+            jobs[i].bucket = (pvec *)calloc((size_t)n_aggs * nthreads, sizeof(pvec));
+        }
         tab_init(&jobs[i].tab, n_aggs, est_t);
+        if (has_distinct && (!jobs[i].A.dset || !jobs[i].bucket)) {
+            dsets_free(jobs[i].A.dset, n_aggs, agg_kind);
+            jobs[i].A.dset = NULL;
+            jobs[i].rc = -1;
+            continue;
+        }
         pthread_create(&th[i], NULL, job_main, &jobs[i]);
     }
     int rc = 0;
     for (int i = 0; i < nthreads; i++) {
-        pthread_join(th[i], NULL);
+        if (!has_distinct || jobs[i].A.dset) pthread_join(th[i], NULL);
         rc |= jobs[i].rc;
     }
     or_merge_job *mj = (or_merge_job *)calloc((size_t)nthreads, sizeof(or_merge_job));
+    int created = 0;
     for (int s = 0; s < nthreads && !rc; s++) {
         mj[s].jobs = jobs;
         mj[s].nt = nthreads;
         mj[s].shard = s;
         mj[s].nshards = nthreads;
         mj[s].A = &A;
+        mj[s].dset = has_distinct ? dsets_new(n_aggs, agg_kind) : NULL;
         tab_init(&mj[s].out, n_aggs, est_groups / nthreads + 16);
+        if (has_distinct && !mj[s].dset) { rc = -1; break; }
         pthread_create(&th[s], NULL, merge_main, &mj[s]);
+        created++;
     }
-    if (!rc) {
-        for (int s = 0; s < nthreads; s++) {
-            pthread_join(th[s], NULL);
-            rc |= mj[s].rc;
-            ng += mj[s].out.ng;
-        }
+    for (int s = 0; s < created; s++) {
+        pthread_join(th[s], NULL);
+        rc |= mj[s].rc;
+        ng += mj[s].out.ng;
     }
     if (!rc && ng <= cap) {
         int64_t o = 0;
@@ -544,6 +611,15 @@ int64_t or_groupby(int64_t n, const int64_t *keys, const uint8_t *key_null, cons
     }
     for (int s = 0; s < nthreads; s++) {
         if (mj[s].out.st) tab_free(&mj[s].out);
+        dsets_free(mj[s].dset, n_aggs, agg_kind);
+        dsets_free(jobs[s].A.dset, n_aggs, agg_kind);
+        if (jobs[s].bucket) {
+            for (int b = 0; b < n_aggs * nthreads; b++) {
+                free(jobs[s].bucket[b].g);
+                free(jobs[s].bucket[b].v);
+            }
+            free(jobs[s].bucket);
+        }
         tab_free(&jobs[s].tab);
     }
     free(mj);

@@ -134,8 +134,27 @@ def test_count_distinct_matches_numpy_sets():
     n = 50_000
     k = rng.integers(0, 300, n, dtype=np.int32)
     v = rng.integers(-40, 40, n, dtype=np.int64) * (10**15)
-    r = _q([2, 3], [0], [("count_distinct", 1)], [k, v], nthreads=4)  # the value sets keep it single-threaded
     pairs = np.unique(np.stack([k.astype(np.int64), v], axis=1), axis=0)
     keys, counts = np.unique(pairs[:, 0], return_counts=True)
-    got = dict(zip(r["keys"][0].tolist(), r["aggs"][0][0].tolist()))
-    assert got == dict(zip(keys.tolist(), counts.tolist()))
+    want = dict(zip(keys.tolist(), counts.tolist()))
+    for threads in (1, 4):  # per-thread value sets, their union in the sharded merge
+        r = _q([2, 3], [0], [("count_distinct", 1)], [k, v], nthreads=threads)
+        assert dict(zip(r["keys"][0].tolist(), r["aggs"][0][0].tolist())) == want
+
+
+def test_count_distinct_threads_agree_with_nulls():
+    rng = np.random.default_rng(22)
+    n = 200_000
+    k = rng.integers(0, 5_000, n, dtype=np.int32)
+    v = rng.integers(0, 300, n, dtype=np.int32)
+    kn = rng.random(n) < 0.02
+    vn = rng.random(n) < 0.1
+    aggs = [("count_distinct", 1), ("count_star", -1), ("sum", 1), ("count_distinct", 0)]
+    a = _q([2, 2], [0], aggs, [k, v], nulls=[kn, vn], nthreads=1)
+    b = _q([2, 2], [0], aggs, [k, v], nulls=[kn, vn], nthreads=8)
+    oa = np.lexsort((a["keys"][0], a["key_null"][0]))
+    ob = np.lexsort((b["keys"][0], b["key_null"][0]))
+    assert np.array_equal(a["keys"][0][oa], b["keys"][0][ob])
+    assert np.array_equal(a["key_null"][0][oa], b["key_null"][0][ob])
+    for x, y in zip(a["aggs"], b["aggs"]):
+        assert np.array_equal(x[0][oa], y[0][ob]) and np.array_equal(x[1][oa], y[1][ob])
