@@ -50,6 +50,8 @@ def load():
     lib.or_filter.argtypes = [C.c_int64, C.c_int32, P, P, C.c_int32, C.c_int64, C.c_double, P]
     lib.or_rle_decode.restype = C.c_int64
     lib.or_rle_decode.argtypes = [P, C.c_int64, C.c_int32, P, C.c_int64]
+    lib.or_snappy_decompress.restype = C.c_int64
+    lib.or_snappy_decompress.argtypes = [P, C.c_int64, P, C.c_int64]
     _lib = lib
     return lib
 
@@ -197,3 +199,23 @@ def rle_decode(buf: bytes, bit_width: int, n: int) -> np.ndarray:
     out = np.zeros(max(n, 1), dtype=np.uint32)
     got = lib.or_rle_decode(_p(a), len(a), bit_width, _p(out), n)
     return out[:got]
+
+
+def snappy_decompress(block: bytes, cap: int = 1 << 30) -> bytes:
+    """A raw Snappy block decompressed by the oracle's restatement of the
+    format (raises ValueError on a malformed block)."""
+    lib = load()
+    a = np.frombuffer(block, dtype=np.uint8) if block else np.zeros(1, np.uint8)
+    # the preamble bounds the output
+    want, sh, i = 0, 0, 0
+    while i < len(block) and sh <= 28:
+        want |= (block[i] & 0x7F) << sh
+        i += 1
+        if not block[i - 1] & 0x80:
+            break
+        sh += 7
+    out = np.zeros(max(1, min(want, cap)), dtype=np.uint8)
+    got = lib.or_snappy_decompress(_p(a), len(block), _p(out), min(want, cap))
+    if got < 0:
+        raise ValueError("malformed Snappy block")
+    return out[:got].tobytes()

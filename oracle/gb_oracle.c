@@ -789,4 +789,76 @@ int64_t or_rle_decode(const uint8_t *p, int64_t size, int32_t bw, uint32_t *out,
     return got;
 }
 
+/*
+ * Snappy raw-block decompression, restated from the published Snappy format
+ * (the reference decompresses Parquet pages with the vendored Google Snappy
+ * 1.2.1, third_party/snappy/, called from SnappyDecompress /
+ * SnappyDecompressRaw, src/storage/parquet.cpp:44-90):
+ *   preamble  the uncompressed length, a little-endian base-128 varint;
+ *   elements  a tag byte whose low 2 bits give the kind:
+ *     00 literal: length-1 in the upper 6 bits, or (60..63) in the next 1..4
+ *        little-endian bytes; the bytes follow;
+ *     01 copy: length 4 + bits 2..4, offset = bits 5..7 << 8 | next byte;
+ *     10 copy: length 1 + upper 6 bits, offset = next 2 bytes (LE);
+ *     11 copy: length 1 + upper 6 bits, offset = next 4 bytes (LE);
+ *   a copy repeats `length` bytes from `offset` bytes back (byte by byte, so
+ *   an offset below the length repeats a pattern); offset 0 or one reaching
+ *   before the start is invalid.
+ * Returns the decompressed length, or -1 (malformed, or more than cap).
+ */
+int64_t or_snappy_decompress(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap) {
+    int64_t pos = 0;
+    uint64_t want = 0;
+    for (int sh = 0;; sh += 7) {
+        if (pos >= n || sh > 28) return -1;
+        uint8_t b = src[pos++];
+        want |= (uint64_t)(b & 0x7f) << sh;
+        if (!(b & 0x80)) break;
+    }
+    if ((int64_t)want > cap) return -1;
+    int64_t out = 0;
+    while (pos < n) {
+        const uint8_t tag = src[pos++];
+        const int kind = tag & 3;
+        if (kind == 0) {
+            int64_t len = (tag >> 2) + 1;
+            if ((tag >> 2) >= 60) {
+                const int nb = (tag >> 2) - 59;
+                if (pos + nb > n) return -1;
+                uint64_t l = 0;
+                for (int i = 0; i < nb; i++) l |= (uint64_t)src[pos + i] << (8 * i);
+                pos += nb;
+                len = (int64_t)l + 1;
+            }
+            if (len > n - pos || len > (int64_t)want - out) return -1;
+            memcpy(dst + out, src + pos, (size_t)len);
+            pos += len;
+            out += len;
+            continue;
+        }
+        int64_t len, off;
+        if (kind == 1) {
+            if (pos + 1 > n) return -1;
+            len = 4 + ((tag >> 2) & 7);
+            off = ((int64_t)(tag >> 5) << 8) | src[pos];
+            pos += 1;
+        } else if (kind == 2) {
+            if (pos + 2 > n) return -1;
+            len = 1 + (tag >> 2);
+            off = (int64_t)src[pos] | ((int64_t)src[pos + 1] << 8);
+            pos += 2;
+        } else {
+            if (pos + 4 > n) return -1;
+            len = 1 + (tag >> 2);
+            off = (int64_t)((uint64_t)src[pos] | ((uint64_t)src[pos + 1] << 8) | ((uint64_t)src[pos + 2] << 16) |
+                            ((uint64_t)src[pos + 3] << 24));
+            pos += 4;
+        }
+        if (off == 0 || off > out || len > (int64_t)want - out) return -1;
+        for (int64_t i = 0; i < len; i++) dst[out + i] = dst[out - off + i];
+        out += len;
+    }
+    return out == (int64_t)want ? out : -1;
+}
+
 int32_t or_version(void) { return 1; }

@@ -48,8 +48,22 @@ def _encoder():
     lib = C.CDLL(_ENC_LIB)
     lib.pq_rle_encode.restype = C.c_int64
     lib.pq_rle_encode.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]
+    lib.pq_snappy_compress.restype = C.c_int64
+    lib.pq_snappy_compress.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]
     _enc = lib
     return lib
+
+
+def snappy_compress(data: bytes) -> bytes:
+    """One raw Snappy block of `data` (the writer's SNAPPY pages)."""
+    src = np.frombuffer(data, dtype=np.uint8) if data else np.zeros(1, np.uint8)
+    cap = len(data) + len(data) // 6 + 64
+    out = np.empty(cap, dtype=np.uint8)
+    table = np.empty(1 << 14, dtype=np.int32)
+    got = _encoder().pq_snappy_compress(src.ctypes.data, len(data), out.ctypes.data, cap, table.ctypes.data)
+    if got < 0:
+        raise RuntimeError("Snappy compress buffer overflow")
+    return out[:got].tobytes()
 
 
 def rle_hybrid(indices: np.ndarray, bit_width: int) -> bytes:
@@ -149,11 +163,14 @@ class TWriter:
         self.buf.append(0)
 
 
-def _page_header(ptype, size, num_values=None, encoding=None, dict_values=None):
+CODEC_UNCOMPRESSED, CODEC_SNAPPY = 0, 1
+
+
+def _page_header(ptype, size, num_values=None, encoding=None, dict_values=None, compressed_size=None):
     w = TWriter()
     w.i32(1, ptype)
     w.i32(2, size)
-    w.i32(3, size)
+    w.i32(3, size if compressed_size is None else compressed_size)
     if ptype == PAGE_DATA:
         w.begin_struct(5)
         w.i32(1, num_values)
@@ -206,8 +223,17 @@ def _dict_payload(ptype, dictionary):
     return np.ascontiguousarray(dictionary, dtype=_np_dtype(ptype)).tobytes()
 
 
-def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="slothdb_gb300 writer"):
-    """Return the bytes of a Parquet file holding `columns` (equal lengths)."""
+def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="slothdb_gb300 writer", codec=None):
+    """Return the bytes of a Parquet file holding `columns` (equal lengths);
+    codec "snappy" compresses every page (dictionary and data) as one raw
+    Snappy block."""
+    snappy = codec == "snappy"
+
+    def page(ptype, payload, **kw):
+        if not snappy:
+            return _page_header(ptype, len(payload), **kw), payload, len(payload)
+        body = snappy_compress(payload)
+        return _page_header(ptype, len(payload), compressed_size=len(body), **kw), body, len(payload)
     n = columns[0].n()
     for c in columns:
         assert c.n() == n
@@ -229,12 +255,13 @@ def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="sloth
                 rg_dict = [c.dictionary[i] for i in perm] if c.ptype == T_BYTE_ARRAY else np.asarray(c.dictionary)[perm]
                 rg_idx = np.zeros(len(c.indices), dtype=np.uint32)
                 rg_idx[rg0:rg1] = inv[c.indices[rg0:rg1]]
+            unc = 0
             if c.dict_encoded:
-                dvals = _dict_payload(c.ptype, rg_dict)
-                hdr = _page_header(PAGE_DICT, len(dvals), dict_values=len(rg_dict))
+                hdr, body, raw = page(PAGE_DICT, _dict_payload(c.ptype, rg_dict), dict_values=len(rg_dict))
                 dict_off = pos
-                parts += [hdr, dvals]
-                pos += len(hdr) + len(dvals)
+                parts += [hdr, body]
+                pos += len(hdr) + len(body)
+                unc += len(hdr) + raw
                 bw = max(1, int(len(c.dictionary) - 1).bit_length())
             data_off = pos
             prows = c.page_rows or page_rows
@@ -246,12 +273,13 @@ def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="sloth
                 else:
                     payload = np.ascontiguousarray(c.values[p0:p1], dtype=_np_dtype(c.ptype)).tobytes()
                     enc = ENC_PLAIN
-                hdr = _page_header(PAGE_DATA, len(payload), num_values=p1 - p0, encoding=enc)
-                parts += [hdr, payload]
-                pos += len(hdr) + len(payload)
+                hdr, body, raw = page(PAGE_DATA, payload, num_values=p1 - p0, encoding=enc)
+                parts += [hdr, body]
+                pos += len(hdr) + len(body)
+                unc += len(hdr) + raw
             size = pos - start
             rg_bytes += size
-            chunks.append((c, start, dict_off, data_off, size, rg1 - rg0))
+            chunks.append((c, start, dict_off, data_off, size, rg1 - rg0, unc))
         row_groups.append((chunks, rg_bytes, rg1 - rg0))
     # footer
     w = TWriter()
@@ -280,7 +308,7 @@ def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="sloth
     for chunks, rg_bytes, rg_rows in row_groups:
         w.list_struct_begin()
         w.begin_list(1, CT_STRUCT, len(chunks))
-        for c, start, dict_off, data_off, size, rows in chunks:
+        for c, start, dict_off, data_off, size, rows, unc in chunks:
             w.list_struct_begin()
             w.i64(2, start)
             w.begin_struct(3)
@@ -291,9 +319,9 @@ def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="sloth
                 w.list_i32(e)
             w.begin_list(3, CT_BINARY, 1)
             w.list_binary(c.name)
-            w.i32(4, 0)
+            w.i32(4, CODEC_SNAPPY if snappy else CODEC_UNCOMPRESSED)
             w.i64(5, rows)
-            w.i64(6, size)
+            w.i64(6, unc)
             w.i64(7, size)
             w.i64(9, data_off)
             if dict_off is not None:

@@ -82,3 +82,77 @@ int64_t pq_rle_encode(const uint32_t *x, int64_t n, int32_t bw, uint8_t *out, in
     }
     return pos;
 }
+
+/*
+ * Snappy raw-block compressor for the writer's SNAPPY column chunks (the
+ * published Snappy format: varint uncompressed length, then literal and copy
+ * elements).  Greedy: a 4-byte hash of each position finds an earlier match
+ * within 65535 bytes; matches become copies of at most 64 bytes (2-byte
+ * offsets, or 1-byte offsets for 4..11 bytes within 2047), everything else
+ * literals.  Returns the compressed size, or -1 if `cap` is too small
+ * (n + n / 6 + 32 always suffices).
+ */
+static int64_t put_literal(uint8_t *out, int64_t pos, int64_t cap, const uint8_t *p, int64_t len) {
+    while (len > 0) {
+        const int64_t l = len > 65536 ? 65536 : len;
+        const uint32_t m = (uint32_t)(l - 1);
+        if (pos + 3 + l > cap) return -1;
+        if (m < 60) {
+            out[pos++] = (uint8_t)(m << 2);
+        } else if (m < 256) {
+            out[pos++] = (uint8_t)(60 << 2);
+            out[pos++] = (uint8_t)m;
+        } else {
+            out[pos++] = (uint8_t)(61 << 2);
+            out[pos++] = (uint8_t)m;
+            out[pos++] = (uint8_t)(m >> 8);
+        }
+        memcpy(out + pos, p, (size_t)l);
+        pos += l;
+        p += l;
+        len -= l;
+    }
+    return pos;
+}
+
+static inline uint32_t load32(const uint8_t *p) {
+    uint32_t v;
+    memcpy(&v, p, 4);
+    return v;
+}
+
+int64_t pq_snappy_compress(const uint8_t *src, int64_t n, uint8_t *out, int64_t cap, int32_t *table) {
+    enum { HB = 14 };
+    int64_t pos = 0;
+    if (cap < 10) return -1;
+    pos = put_varint(out, pos, (uint64_t)n);
+    for (int i = 0; i < (1 << HB); i++) table[i] = -1;
+    int64_t i = 0, lit = 0;
+    while (i + 4 <= n) {
+        const uint32_t w = load32(src + i);
+        const uint32_t h = (w * 0x1e35a7bdu) >> (32 - HB);
+        const int64_t cand = table[h];
+        table[h] = (int32_t)i;
+        if (cand >= 0 && i - cand <= 65535 && load32(src + cand) == w) {
+            int64_t len = 4;
+            while (len < 64 && i + len < n && src[cand + len] == src[i + len]) len++;
+            if ((pos = put_literal(out, pos, cap, src + lit, i - lit)) < 0) return -1;
+            const int64_t off = i - cand;
+            if (pos + 3 > cap) return -1;
+            if (len <= 11 && off < 2048) {
+                out[pos++] = (uint8_t)(1 | ((len - 4) << 2) | ((off >> 8) << 5));
+                out[pos++] = (uint8_t)off;
+            } else {
+                out[pos++] = (uint8_t)(2 | ((len - 1) << 2));
+                out[pos++] = (uint8_t)off;
+                out[pos++] = (uint8_t)(off >> 8);
+            }
+            i += len;
+            lit = i;
+        } else {
+            i++;
+        }
+    }
+    if ((pos = put_literal(out, pos, cap, src + lit, n - lit)) < 0) return -1;
+    return pos;
+}

@@ -101,3 +101,41 @@ def test_varchar_dictionary_header_checked_on_open(monkeypatch):
     with pytest.raises(capi.GbError) as e:
         capi.ParquetFile(data)
     assert e.value.status == 6  # GB_ERR_CORRUPT
+
+
+def test_snappy_oracle_matches_pyarrow():
+    """The oracle's Snappy restatement decompresses blocks made by an
+    independent Snappy (pyarrow's) and by the project writer's compressor,
+    which pyarrow also decompresses; malformed blocks are refused."""
+    pa = pytest.importorskip("pyarrow")
+    rng = np.random.default_rng(7)
+    blocks = [b"", b"x", b"abcabcabcabc" * 500, rng.integers(0, 256, 70_000, dtype=np.uint8).tobytes(),
+              rng.integers(0, 3, 200_000, dtype=np.uint8).tobytes(),
+              np.repeat(rng.integers(0, 1 << 20, 5000), 7).astype(np.int64).tobytes()]
+    for data in blocks:
+        assert oracle.snappy_decompress(pa.compress(data, codec="snappy", asbytes=True)) == data
+        ours = pq.snappy_compress(data)
+        assert oracle.snappy_decompress(ours) == data
+        assert pa.decompress(ours, decompressed_size=len(data), codec="snappy", asbytes=True) == data
+    good = pq.snappy_compress(b"hello hello hello hello")
+    for bad in (good[:-1], good[:1] + b"\x0a\x00\x00", bytes([5, 0x06, 0xff, 0x00])):
+        with pytest.raises(ValueError):
+            oracle.snappy_decompress(bad)
+
+
+def test_snappy_file_read_by_pyarrow_and_refused_by_the_gpu_parser():
+    """SNAPPY column chunks from the writer are valid Parquet (pyarrow reads the
+    same values); the GPU path does not decompress pages yet and refuses the
+    file on open."""
+    pa = pytest.importorskip("pyarrow.parquet")
+    _, key, f, v = pq.filter_groupby_file(n_rows=30_000, row_group_rows=10_000, page_rows=4096, n_dict=512)
+    cols = [pq.Column("key", pq.T_INT32, values=key), pq.Column("f", pq.T_INT32, values=f, int16=True),
+            pq.Column("v", pq.T_INT64, values=v)]
+    data = pq.write(cols, row_group_rows=10_000, page_rows=4096, codec="snappy")
+    plain = pq.write(cols, row_group_rows=10_000, page_rows=4096)
+    assert len(data) < len(plain)
+    t = pa.read_table(io.BytesIO(data))
+    assert np.array_equal(t.column("key").to_numpy(), key) and np.array_equal(t.column("v").to_numpy(), v)
+    with pytest.raises(capi.GbError) as e:
+        capi.ParquetFile(data)
+    assert e.value.status == 3  # GB_ERR_UNSUPPORTED
