@@ -235,13 +235,23 @@ gb_status gb_engine_hash_aggregate(const int32_t *keys, const int32_t *values, u
  * 92-470 thrift + page headers, 1107-1366 metadata, 2475-2706 ReadColumnInto).
  * Supported: uncompressed column chunks, REQUIRED flat columns of INT32
  * (INT(16) annotation → SMALLINT), INT64 and DOUBLE, PLAIN or dictionary
- * (RLE / bit-packed hybrid) encoded, data page v1 and v2. */
+ * (RLE / bit-packed hybrid) encoded, data page v1 and v2, and a
+ * dictionary-encoded BYTE_ARRAY column as the VARCHAR group key. */
 typedef struct gb_pq_file gb_pq_file;
 gb_status gb_pq_open(const uint8_t *bytes, uint64_t size, gb_pq_file **out);
 uint32_t gb_pq_num_row_groups(const gb_pq_file *f);
 uint64_t gb_pq_num_rows(const gb_pq_file *f);
 uint32_t gb_pq_num_columns(const gb_pq_file *f);
 gb_status gb_pq_column_info(const gb_pq_file *f, uint32_t col, char *name, uint32_t name_cap, int32_t *type);
+/* Zone map: *might = 0 when row group `rg`'s column statistics (Statistics
+ * min_value / max_value, or the deprecated min / max) prove that no row passes
+ * every filter (filter columns are spec columns, mapped to file columns by
+ * col_map[0, n_cols)), else 1 — IsRowGroupPruned / RowGroupMightMatch
+ * (physical_planner.cpp:1142-1150, src/storage/parquet.cpp:3200-3240).
+ * INTEGER, BIGINT and DOUBLE statistics are read (the reference reads none
+ * for SMALLINT).  gb_agg_ingest_parquet skips the row groups this rules out. */
+gb_status gb_pq_row_group_might_match(const gb_pq_file *f, uint32_t rg, const int32_t *col_map, uint32_t n_cols,
+                                      const gb_filter *filters, uint32_t n_filters, int32_t *might);
 /* Copies the whole file into HBM once (a resident table). */
 gb_status gb_pq_upload(gb_pq_file *f, void *stream);
 void gb_pq_close(gb_pq_file *f);

@@ -125,6 +125,8 @@ _SIGS = {
     "gb_pq_num_rows": (C.c_uint64, [C.c_void_p]),
     "gb_pq_num_columns": (C.c_uint32, [C.c_void_p]),
     "gb_pq_column_info": (C.c_int, [C.c_void_p, C.c_uint32, C.c_char_p, C.c_uint32, C.POINTER(C.c_int32)]),
+    "gb_pq_row_group_might_match": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_int32), C.c_uint32,
+                                              C.c_void_p, C.c_uint32, C.POINTER(C.c_int32)]),
     "gb_pq_upload": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gb_pq_close": (None, [C.c_void_p]),
     "gb_agg_ingest_parquet": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_int32),
@@ -554,6 +556,24 @@ class ParquetFile:
     @property
     def num_rows(self):
         return int(self.lib.gb_pq_num_rows(self.h))
+
+    def row_group_might_match(self, rg, col_map, filters):
+        """Zone map of row group `rg`: False when its column statistics rule
+        out the (col, op, const) filters (col = spec column, read from file
+        column col_map[col])."""
+        types = [t for _, t in self.columns()]
+        fl = (Filter * max(1, len(filters)))()
+        for i, (col, op, const) in enumerate(filters):
+            opc = CMP_NAMES[op] if isinstance(op, str) else int(op)
+            if types[col_map[col]] == DOUBLE:
+                fl[i] = Filter(col, opc, 0, float(const))
+            else:
+                fl[i] = Filter(col, opc, int(const), 0.0)
+        cm = (C.c_int32 * len(col_map))(*col_map)
+        m = C.c_int32()
+        check(self.lib.gb_pq_row_group_might_match(self.h, int(rg), cm, len(col_map), C.cast(fl, C.c_void_p),
+                                                   len(filters), C.byref(m)))
+        return bool(m.value)
 
     def columns(self):
         out = []

@@ -154,6 +154,10 @@ struct PqChunk {
     int64_t dict_off = -1;  // dictionary payload offset (-1 = none)
     uint32_t dict_n = 0;
     uint32_t dict_bytes = 0;  // dictionary payload bytes
+    // column statistics (zone map): raw min / max bytes, Statistics fields
+    // 5/6 (min_value/max_value) over the deprecated 2/1 (min/max)
+    bool has_stats = false;
+    std::string stat_min, stat_max;
     uint32_t page_begin = 0, page_end = 0;  // into pages (data pages only)
 };
 
@@ -272,6 +276,18 @@ static gb_status parse_footer(gb_pq_file *f) {
                                         else if (f4 == 7 && t4 == 6) comp = r.zz();
                                         else if (f4 == 9 && t4 == 6) data_off = r.zz();
                                         else if (f4 == 11 && t4 == 6) dict_off = r.zz();
+                                        else if (f4 == 12 && t4 == 12) {  // Statistics
+                                            int f5, t5, l5 = 0;
+                                            while (r.field(f5, t5, l5)) {
+                                                if ((f5 == 1 || f5 == 5) && t5 == 8) {
+                                                    ch.stat_max = r.binary();
+                                                    ch.has_stats = true;
+                                                } else if ((f5 == 2 || f5 == 6) && t5 == 8) {
+                                                    ch.stat_min = r.binary();
+                                                    ch.has_stats = true;
+                                                } else r.skip(t5);
+                                            }
+                                        }
                                         else r.skip(t4);
                                     }
                                 } else r.skip(t3);
@@ -912,6 +928,59 @@ static gb_status pq_fail_if_err(Ctl &c) {
     return GB_OK;
 }
 
+// Zone map of one row group: false when file column `fcol`'s statistics prove
+// that no row passes `q` (IsRowGroupPruned / RowGroupMightMatch,
+// physical_planner.cpp:1142-1150, parquet.cpp:3200-3240).  Statistics are
+// read as INTEGER (4 bytes), BIGINT (8) or DOUBLE (8) like the reference's
+// decode_stat (parquet.cpp:1185-1230), which reads none for SMALLINT.
+static bool pq_rg_might_match(const gb_pq_file *f, uint32_t rg, int fcol, const Filter &q) {
+    const PqChunk &ch = f->chunks[rg][fcol];
+    if (!ch.has_stats) return true;
+    const int t = f->cols[fcol].gtype;
+    if (t == GB_T_INTEGER || t == GB_T_BIGINT) {
+        const size_t w = t == GB_T_INTEGER ? 4 : 8;
+        if (ch.stat_min.size() < w || ch.stat_max.size() < w) return true;
+        int64_t mn, mx;
+        if (w == 4) {
+            int32_t a, b;
+            memcpy(&a, ch.stat_min.data(), 4);
+            memcpy(&b, ch.stat_max.data(), 4);
+            mn = a;
+            mx = b;
+        } else {
+            memcpy(&mn, ch.stat_min.data(), 8);
+            memcpy(&mx, ch.stat_max.data(), 8);
+        }
+        const int64_t v = q.ic;
+        switch (q.op) {
+        case GB_CMP_EQ: return !(v < mn) && !(mx < v);
+        case GB_CMP_GT: return !(mx < v) && !(mx == v);
+        case GB_CMP_GE: return !(mx < v);
+        case GB_CMP_LT: return !(v < mn) && !(mn == v);
+        case GB_CMP_LE: return !(v < mn);
+        case GB_CMP_NE: return !(mn == v && mx == v);
+        default: return true;
+        }
+    }
+    if (t == GB_T_DOUBLE) {
+        if (ch.stat_min.size() < 8 || ch.stat_max.size() < 8) return true;
+        double mn, mx;
+        memcpy(&mn, ch.stat_min.data(), 8);
+        memcpy(&mx, ch.stat_max.data(), 8);
+        const double v = q.dc;
+        switch (q.op) {
+        case GB_CMP_EQ: return !(v < mn) && !(mx < v);
+        case GB_CMP_GT: return !(mx < v) && !(mx == v);
+        case GB_CMP_GE: return !(mx < v);
+        case GB_CMP_LT: return !(v < mn) && !(mn == v);
+        case GB_CMP_LE: return !(v < mn);
+        case GB_CMP_NE: return !(mn == v && mx == v);
+        default: return true;
+        }
+    }
+    return true;
+}
+
 // Page descriptors of row groups [rg_begin, rg_end) and the given file
 // columns (offsets relative to `base`), with run-table slots for the
 // dictionary pages; col_pages gets one {begin, end} pair per (rg, column).
@@ -1046,6 +1115,28 @@ gb_status gb_pq_column_info(const gb_pq_file *f, uint32_t col, char *name, uint3
         name[name_cap - 1] = 0;
     }
     if (type) *type = f->cols[col].gtype;
+    return GB_OK;
+}
+
+gb_status gb_pq_row_group_might_match(const gb_pq_file *f, uint32_t rg, const int32_t *col_map, uint32_t n_cols,
+                                      const gb_filter *filters, uint32_t n_filters, int32_t *might) {
+    if (!f || !might || rg >= f->rg_rows.size() || (n_filters && (!filters || !col_map))) {
+        set_error("invalid arguments to gb_pq_row_group_might_match");
+        return GB_ERR_INVALID;
+    }
+    *might = 1;
+    for (uint32_t i = 0; i < n_filters; i++) {
+        const gb_filter &g = filters[i];
+        if (g.col < 0 || (uint32_t)g.col >= n_cols || col_map[g.col] < 0 || col_map[g.col] >= (int)f->cols.size()) {
+            set_error("filter %u: column out of range", i);
+            return GB_ERR_INVALID;
+        }
+        Filter q{g.col, g.op, g.i_const, g.d_const};
+        if (!pq_rg_might_match(f, rg, col_map[g.col], q)) {
+            *might = 0;
+            break;
+        }
+    }
     return GB_OK;
 }
 
@@ -1236,6 +1327,18 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
         }
         vc = c;
     }
+    // zone maps: row groups whose statistics rule out a predicate are skipped
+    std::vector<char> live(rg_end - rg_begin, 1);
+    uint32_t n_live = 0;
+    for (uint32_t g = rg_begin; g < rg_end; g++) {
+        for (int q = 0; q < v.n_filters; q++)
+            if (!pq_rg_might_match(f, g, col_map[v.filters[q].col], v.filters[q])) {
+                live[g - rg_begin] = 0;
+                break;
+            }
+        n_live += live[g - rg_begin] ? 1u : 0u;
+    }
+    if (n_live == 0) return GB_OK;
     PqScratch *S = g_scratch_for(h);
     // device bytes: the uploaded file, or this batch's byte range copied now
     uint64_t lo = ~0ull, hi = 0;
@@ -1262,6 +1365,7 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
     std::vector<PqChunkArg> chunks;
     uint64_t rows = 0;
     for (uint32_t g = rg_begin; g < rg_end; g++) {
+        if (!live[g - rg_begin]) continue;
         for (uint64_t r0 = 0; r0 < f->rg_rows[g]; r0 += PQ_CHUNK)
             chunks.push_back({g - rg_begin, (uint32_t)r0, (uint32_t)std::min<uint64_t>(PQ_CHUNK, f->rg_rows[g] - r0)});
         rows += f->rg_rows[g];

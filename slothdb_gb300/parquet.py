@@ -223,10 +223,22 @@ def _dict_payload(ptype, dictionary):
     return np.ascontiguousarray(dictionary, dtype=_np_dtype(ptype)).tobytes()
 
 
-def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="slothdb_gb300 writer", codec=None):
+def _stat_bytes(c, lo, hi):
+    """min_value / max_value bytes of rows [lo, hi) of a numeric column (PLAIN
+    encoding of the value), or None."""
+    if c.ptype not in (T_INT32, T_INT64, T_DOUBLE) or hi <= lo:
+        return None
+    vals = np.asarray(c.dictionary)[c.indices[lo:hi]] if c.dict_encoded else np.asarray(c.values[lo:hi])
+    vals = vals.astype(_np_dtype(c.ptype))
+    return vals.min().tobytes(), vals.max().tobytes()
+
+
+def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="slothdb_gb300 writer", codec=None,
+          stats=False):
     """Return the bytes of a Parquet file holding `columns` (equal lengths);
     codec "snappy" compresses every page (dictionary and data) as one raw
-    Snappy block."""
+    Snappy block; stats writes each numeric column chunk's min / max
+    (Statistics min_value / max_value)."""
     snappy = codec == "snappy"
 
     def page(ptype, payload, **kw):
@@ -279,7 +291,8 @@ def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="sloth
                 unc += len(hdr) + raw
             size = pos - start
             rg_bytes += size
-            chunks.append((c, start, dict_off, data_off, size, rg1 - rg0, unc))
+            chunks.append((c, start, dict_off, data_off, size, rg1 - rg0, unc,
+                           _stat_bytes(c, rg0, rg1) if stats else None))
         row_groups.append((chunks, rg_bytes, rg1 - rg0))
     # footer
     w = TWriter()
@@ -308,7 +321,7 @@ def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="sloth
     for chunks, rg_bytes, rg_rows in row_groups:
         w.list_struct_begin()
         w.begin_list(1, CT_STRUCT, len(chunks))
-        for c, start, dict_off, data_off, size, rows, unc in chunks:
+        for c, start, dict_off, data_off, size, rows, unc, st in chunks:
             w.list_struct_begin()
             w.i64(2, start)
             w.begin_struct(3)
@@ -326,12 +339,26 @@ def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="sloth
             w.i64(9, data_off)
             if dict_off is not None:
                 w.i64(11, dict_off)
+            if st is not None:
+                w.begin_struct(12)  # Statistics
+                w.binary(5, st[1])  # max_value
+                w.binary(6, st[0])  # min_value
+                w.end_struct()
             w.end_struct()
             w.list_struct_end()
         w.i64(2, rg_bytes)
         w.i64(3, rg_rows)
         w.list_struct_end()
     w.binary(6, created_by)
+    if stats:
+        # column_orders: TYPE_ORDER for every column, which makes readers
+        # trust min_value / max_value
+        w.begin_list(7, CT_STRUCT, len(columns))
+        for _ in columns:
+            w.list_struct_begin()
+            w.begin_struct(1)
+            w.end_struct()
+            w.list_struct_end()
     w.stop()
     footer = bytes(w.buf)
     parts += [footer, struct.pack("<I", len(footer)), b"PAR1"]

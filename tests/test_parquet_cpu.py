@@ -139,3 +139,77 @@ def test_snappy_file_read_by_pyarrow_and_refused_by_the_gpu_parser():
     with pytest.raises(capi.GbError) as e:
         capi.ParquetFile(data)
     assert e.value.status == 3  # GB_ERR_UNSUPPORTED
+
+
+def _zone_expect(op, v, mn, mx):
+    """The reference's RowGroupMightMatch rules (parquet.cpp:3200-3240)."""
+    return {"==": not (v < mn) and not (mx < v), ">": not (mx < v) and not (mx == v), ">=": not (mx < v),
+            "<": not (v < mn) and not (mn == v), "<=": not (v < mn), "!=": not (mn == v and mx == v)}[op]
+
+
+OPS = ["==", "!=", "<", "<=", ">", ">="]
+
+
+def test_zone_maps_follow_the_reference_rules():
+    """Row-group statistics written by the project writer (read back by
+    pyarrow as the same min/max) rule row groups out exactly as the
+    reference's zone-map check does, never ruling out one that has a passing
+    row; SMALLINT columns carry none (as in the reference) and files without
+    statistics rule nothing out."""
+    pa = pytest.importorskip("pyarrow.parquet")
+    n, rg = 40_000, 10_000
+    rng = np.random.default_rng(11)
+    k = np.sort(rng.integers(-1000, 1000, n)).astype(np.int32)
+    x = np.sort(rng.normal(0, 3, n))
+    v = np.arange(n, dtype=np.int64) * 3
+    s16 = np.sort(rng.integers(0, 1000, n)).astype(np.int32)
+    cols = [pq.Column("k", pq.T_INT32, values=k), pq.Column("x", pq.T_DOUBLE, values=x),
+            pq.Column("v", pq.T_INT64, values=v), pq.Column("s", pq.T_INT32, values=s16, int16=True)]
+    data = pq.write(cols, row_group_rows=rg, page_rows=4096, stats=True)
+    md = pa.ParquetFile(io.BytesIO(data)).metadata
+    pf = capi.ParquetFile(data)
+    cm = [0, 1, 2, 3]
+    consts = {0: [-1000, -509, -508, 0, 500, 999, 1000], 1: [-20.0, float(x[9_999]), 0.0, float(x[20_000]), 20.0],
+              2: [0, 3 * 9_999, 3 * 10_000, 3 * 39_999, 10**9]}
+    for g in range(4):
+        lo, hi = g * rg, (g + 1) * rg
+        for c, arr in ((0, k), (1, x), (2, v)):
+            st = md.row_group(g).column(c).statistics
+            assert st.min == arr[lo:hi].min() and st.max == arr[lo:hi].max()
+            for const in consts[c]:
+                for op in OPS:
+                    got = pf.row_group_might_match(g, cm, [(c, op, const)])
+                    assert got == _zone_expect(op, const, arr[lo:hi].min(), arr[lo:hi].max()), (g, c, op, const)
+                    passing = {"==": arr[lo:hi] == const, "!=": arr[lo:hi] != const, "<": arr[lo:hi] < const,
+                               "<=": arr[lo:hi] <= const, ">": arr[lo:hi] > const, ">=": arr[lo:hi] >= const}[op]
+                    assert got or not passing.any()
+        assert pf.row_group_might_match(g, cm, [(3, "<", -1)])       # SMALLINT: no statistics read
+        assert pf.row_group_might_match(g, cm, [])
+    # a conjunction is ruled out when any one filter is
+    assert not pf.row_group_might_match(3, cm, [(1, ">", -100.0), (0, "<", 0)])
+    pf.close()
+    plain = capi.ParquetFile(pq.write(cols, row_group_rows=rg, page_rows=4096))
+    assert all(plain.row_group_might_match(g, cm, [(0, "<", -5000)]) for g in range(4))
+    plain.close()
+
+
+def test_zone_maps_from_pyarrow_statistics():
+    """Statistics written by pyarrow (an independent writer) drive the same
+    decisions."""
+    pa = pytest.importorskip("pyarrow")
+    pq_ = pytest.importorskip("pyarrow.parquet")
+    n = 30_000
+    k = np.sort(np.random.default_rng(12).integers(-10**9, 10**9, n))
+    t = pa.table({"k": pa.array(k, type=pa.int64()), "w": pa.array(np.arange(n, dtype=np.int32))})
+    buf = io.BytesIO()
+    pq_.write_table(t, buf, row_group_size=7_500, compression="none", use_dictionary=False,
+                    write_statistics=True, data_page_version="1.0")
+    data = buf.getvalue()
+    pf = capi.ParquetFile(data)
+    for g in range(4):
+        lo, hi = g * 7_500, (g + 1) * 7_500
+        for const in (int(k[0]) - 1, int(k[lo]), int(k[hi - 1]), 0, int(k[-1]) + 1):
+            for op in OPS:
+                assert pf.row_group_might_match(g, [0, 1], [(0, op, const)]) == \
+                    _zone_expect(op, const, int(k[lo:hi].min()), int(k[lo:hi].max())), (g, op, const)
+    pf.close()
