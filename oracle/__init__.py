@@ -89,11 +89,13 @@ def filter_mask(n, col_types, cols, filters, nulls=None):
 
 
 def run_query(col_types, group_cols, aggs, cols, filters=(), nulls=None, nthreads=1, est_groups=0,
-              str_cols=None):
+              str_cols=None, max_groups=None):
     """Evaluate SELECT keys, aggs FROM cols [WHERE filters] GROUP BY keys.
 
     cols: list of numpy arrays (VARCHAR columns: (offsets int64[n+1], bytes uint8)).
     nulls: optional list (per column) of bool arrays, True = NULL.
+    max_groups: output capacity in groups (default: one per row); a result
+    with more groups is recomputed with the capacity it needs.
     Returns dict(keys=[ndarray...], key_null=[bool ndarray...],
                  aggs=[(values, null bool, comp float64)...], out_types=[...]).
     """
@@ -116,7 +118,7 @@ def run_query(col_types, group_cols, aggs, cols, filters=(), nulls=None, nthread
                 m = np.ascontiguousarray(nulls[c], dtype=np.uint8)
                 held.append(m)
                 null_ptrs[i] = m.ctypes.data
-    cap = n + 2
+    cap = (min(n, int(max_groups)) if max_groups else n) + 2
     out_i = np.zeros(na * cap, dtype=np.int64)
     out_d = np.zeros(na * cap, dtype=np.float64)
     out_null = np.zeros(na * cap, dtype=np.uint8)
@@ -135,6 +137,9 @@ def run_query(col_types, group_cols, aggs, cols, filters=(), nulls=None, nthread
         ng = lib.or_groupby_str(n, _p(offs), _p(data), _p(kn), _p(keep), na, _p(kinds), _p(in_types), data_ptrs,
                                 null_ptrs, cap, _p(out_rep), _p(out_key_null), _p(out_i), _p(out_d),
                                 _p(out_null), _p(out_comp))
+        if ng < -1:
+            return run_query(col_types, group_cols, aggs, cols, filters, nulls, nthreads, est_groups, str_cols,
+                             max_groups=-ng - 2)
         if ng < 0:
             raise RuntimeError("oracle failed (%d)" % ng)
         reps = out_rep[:ng]
@@ -170,6 +175,9 @@ def run_query(col_types, group_cols, aggs, cols, filters=(), nulls=None, nthread
         ng = lib.or_groupby(n, _p(packed), _p(knull), _p(keep), na, _p(kinds), _p(in_types), data_ptrs, null_ptrs,
                             int(nthreads), int(est_groups), cap, _p(out_keys), _p(out_key_null), _p(out_i),
                             _p(out_d), _p(out_null), _p(out_comp))
+        if ng < -1:
+            return run_query(col_types, group_cols, aggs, cols, filters, nulls, nthreads, est_groups, str_cols,
+                             max_groups=-ng - 2)
         if ng < 0:
             raise RuntimeError("oracle failed (%d)" % ng)
         if len(group_cols) == 1:
