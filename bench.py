@@ -13,9 +13,14 @@ LIMIT 10 TopN on it.
            of the columns, the GROUP BY, and the device→host copy of the
            full result, every step.
 
+  parity — the full GROUP BY result and the TopN checked against the
+           oracle over the same 100M rows (outside the timed region): keys
+           and COUNT equal, SUM/AVG max relative error vs the compensated
+           FP64 sum (bar 1e-12), reported per query.
+
 Inputs (1.6 GB) are larger than L2 (129 MB), so no L2 flush is needed.
 ``--impl reference`` times the CPU restatement of the reference's GROUP BY
-(per-thread maps + shard merge, all host cores) on a bounded sample.
+(per-thread maps + shard merge, all host cores) over the same 100M rows.
 Multi-GPU: the path runs as independent replicas (one full workload per
 rank, no collective); value = rows of all ranks / max-over-ranks time.
 """
@@ -143,48 +148,86 @@ def gen_data(rows):
     return k, x, time.time() - t
 
 
-def cpu_baseline(k, x, sample_rows, threads=None):
-    """Time the oracle's CPU restatement of the reference GROUP BY on the
-    first `sample_rows` rows with all host threads."""
+def oracle_zipf(k, x, threads):
+    """The oracle's CPU restatement of the reference GROUP BY (per-thread
+    maps + sharded merge) over every row given; returns (result, seconds)."""
     import oracle
-    threads = threads or os.cpu_count() or 1
-    n = min(sample_rows, len(k))
-    ks, xs = k[:n], x[:n]
-    oracle.run_query([3, 4], [0], [("count_star", -1), ("sum", 1), ("avg", 1)], [ks[:100_000], xs[:100_000]],
-                     nthreads=threads)
+    aggs = [("count_star", -1), ("sum", 1), ("avg", 1)]
     t = time.perf_counter()
-    oracle.run_query([3, 4], [0], [("count_star", -1), ("sum", 1), ("avg", 1)], [ks, xs], nthreads=threads,
-                     est_groups=N_VALUES // 4)
-    dt = time.perf_counter() - t
-    return {"value": n / dt, "unit": "rows/s", "cores": threads, "kind": "port",
-            "sample": "first %d rows of the 100M-row workload, one pass, %d threads (%.2f s)" % (n, threads, dt)}
+    orc = oracle.run_query([3, 4], [0], aggs, [k, x], nthreads=threads, est_groups=N_VALUES // 4,
+                           max_groups=N_VALUES)
+    return orc, time.perf_counter() - t
+
+
+REL_TOL_F64 = 1e-12  # DOUBLE SUM/AVG: relative error against the FP64 compensated sum, per query
+
+
+def parity_zipf(k, x, full, top, threads=None):
+    """Full-size parity of the 100M-row GROUP BY: the oracle runs the same
+    query over the same rows (every host thread, outside the timed region)
+    and the GPU's full result and TopN are compared with it.  Group keys,
+    COUNT and the TopN keys/counts must be equal; SUM(x) and AVG(x) are
+    reported as the max relative error against the oracle's compensated FP64
+    sums (bar: 1e-12).  Returns the JSON fields and the oracle's timing."""
+    threads = threads or os.cpu_count() or 1
+    orc, orc_s = oracle_zipf(k, x, threads)
+    ok = orc["keys"][0].astype(np.int64)
+    oc = orc["aggs"][0][0].astype(np.int64)
+    os_ = orc["aggs"][1][2]
+    oa = orc["aggs"][2][2]
+    gk = full[0][0].astype(np.int64)
+    go_, oo = np.argsort(gk, kind="stable"), np.argsort(ok, kind="stable")
+    out = {"n_groups_gpu": int(len(gk)), "n_groups_oracle": int(len(ok)), "groups_equal": False,
+           "int_mismatches": None, "max_rel_err_f64": None, "tol_f64": REL_TOL_F64}
+    if len(gk) == len(ok) and np.array_equal(gk[go_], ok[oo]):
+        out["groups_equal"] = True
+        gc = full[1][0].astype(np.int64)[go_]
+        out["int_mismatches"] = int(np.count_nonzero(gc != oc[oo]))
+        errs = {}
+        for name, col, ref in (("sum", 2, os_), ("avg", 3, oa)):
+            r = ref[oo]
+            e = np.abs(full[col][0][go_] - r) / np.maximum(np.abs(r), np.finfo(np.float64).tiny)
+            errs[name] = float(e.max()) if e.size else 0.0
+        out["max_rel_err_f64"] = errs
+        out["within_tol"] = max(errs.values()) <= REL_TOL_F64
+    # TopN 10 by COUNT(*) DESC, ties by key ASC
+    order = np.lexsort((ok, -oc))[:10]
+    tk, tc = top[0][0].astype(np.int64), top[1][0].astype(np.int64)
+    out["topn_equal"] = bool(np.array_equal(tk, ok[order]) and np.array_equal(tc, oc[order]))
+    out["top_group_rows"] = int(oc[order[0]]) if len(order) else 0
+    out["topn_boundary_tie"] = bool(len(oc) > 10 and np.sort(oc)[::-1][9] == np.sort(oc)[::-1][10])
+    if len(order):
+        ti = order[0]
+        out["top_group_sum_rel_err"] = float(abs(full[2][0][go_][np.searchsorted(gk[go_], ok[ti])] - os_[ti])
+                                             / abs(os_[ti])) if out["groups_equal"] else None
+    out["oracle"] = {"threads": threads, "seconds": round(orc_s, 2), "rows": int(len(k))}
+    return out, orc_s
 
 
 def run_reference(args):
+    """The CPU arm: the oracle's restatement of the reference GROUP BY over
+    the whole 100M-row workload per step, every host thread (rank 0 only)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    sample = min(args.cpu_sample // 2, args.rows)
-    k, x, _ = gen_data(max(sample, 1))
-    import oracle
-    aggs = [("count_star", -1), ("sum", 1), ("avg", 1)]
+    k, x, _ = gen_data(args.rows)
+    oracle_zipf(k[:100_000], x[:100_000], threads)
     times = []
     for i in range(args.warmup + args.steps):
-        t = time.perf_counter()
-        oracle.run_query([3, 4], [0], aggs, [k, x], nthreads=threads, est_groups=N_VALUES // 4)
-        dt = time.perf_counter() - t
+        _, dt = oracle_zipf(k, x, threads)
         if i >= args.warmup:
             times.append(dt)
     per = statistics.mean(times)
-    val = sample / per
+    val = args.rows / per
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "rows/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic",
-            "config": {"workload": "zipf-groupby-100M (bounded sample of %d rows per step)" % sample,
-                       "rows": sample, "distinct_values": N_VALUES, "aggs": "COUNT(*),SUM(x),AVG(x)"},
+            "config": {"workload": "zipf-groupby-100M", "rows": args.rows, "distinct_values": N_VALUES,
+                       "aggs": "COUNT(*),SUM(x),AVG(x)"},
             "cpu_baseline": {"value": val, "unit": "rows/s", "cores": threads, "kind": "port",
-                             "sample": "first %d rows of the 100M-row workload per step" % sample},
+                             "sample": "all %d rows of the workload per step (oracle restatement of the "
+                                       "reference's per-thread maps + sharded merge)" % args.rows},
             "e2e": {"value": val, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -944,11 +987,10 @@ def main():
     g2 = capi.GroupBy([capi.BIGINT, capi.DOUBLE], [0], aggs, est_groups=EST_GROUPS)
     g2.ingest([dk, dx], nrows=rows, device=True, stream=sp)
     g2.finalize(stream=sp)
-    import ctypes as C
-    rr = capi.Result()
-    capi.check(g2.lib.gb_agg_result_device(g2.h, C.byref(rr)))
-    n_groups = int(rr.n_rows)
+    full = g2.result()  # the full GROUP BY result in host memory (parity leg below)
+    n_groups = len(full[0][0])
     g2.close()
+    top = g.result()  # the TopN of the last timed step
 
     in_bytes = rows * 16
     out_bytes = n_groups * 32
@@ -1004,8 +1046,14 @@ def main():
         px.close()
 
     cpu = None
+    parity = None
     if rank == 0:
-        cpu = cpu_baseline(k, x, args.cpu_sample)
+        # full-size parity (oracle over the same 100M rows, outside the timed
+        # region); the same oracle pass is the timed CPU baseline
+        parity, orc_s = parity_zipf(k, x, full, top)
+        thr = parity["oracle"]["threads"]
+        cpu = {"value": rows / orc_s, "unit": "rows/s", "cores": thr, "kind": "port",
+               "sample": "all %d rows of the workload, one pass, %d threads (%.2f s)" % (rows, thr, orc_s)}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": ws, "steps": args.steps,
@@ -1018,7 +1066,7 @@ def main():
                            "parallelism": "replicas" if ws > 1 else "single",
                            "est_groups_hint": EST_GROUPS, "datagen_s": round(gen_s, 1)},
                 "algorithmic_bytes_per_step": alg_bytes,
-                "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clk,
+                "roofline": roofline, "cpu_baseline": cpu, "parity": parity, "e2e": e2e, "clocks": clk,
                 "gpu_launches": launches}
         print(json.dumps(line), flush=True)
     g.close()

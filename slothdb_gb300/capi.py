@@ -13,6 +13,8 @@ import numpy as np
 from . import build as _build
 
 GB_OK = 0
+GB_ERR_INVALID = 1
+GB_ERR_UNSUPPORTED = 3
 GB_ERR_TIMEOUT = 4
 GB_ERR_BUDGET = 8
 STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "OOM", 3: "UNSUPPORTED", 4: "TIMEOUT", 5: "CUDA", 6: "CORRUPT",

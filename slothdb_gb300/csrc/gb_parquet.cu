@@ -211,6 +211,7 @@ static gb_status parse_footer(gb_pq_file *f) {
             for (uint64_t i = 0; i < sz && !r.bad; i++) {
                 PqColumn c;
                 int nchild = 0, conv = -1, int_bits = 0;
+                bool int_signed = true;
                 int f2, t2, l2 = 0;
                 while (r.field(f2, t2, l2)) {
                     if (f2 == 1 && t2 == 5) c.ptype = (int)r.zz();
@@ -225,6 +226,7 @@ static gb_status parse_footer(gb_pq_file *f) {
                                 int f4, t4, l4 = 0;
                                 while (r.field(f4, t4, l4)) {
                                     if (f4 == 1 && t4 == 3) int_bits = (int8_t)r.byte();
+                                    else if (f4 == 2 && (t4 == 1 || t4 == 2)) int_signed = t4 == 1;  // isSigned
                                     else r.skip(t4);
                                 }
                             } else r.skip(t3);
@@ -236,12 +238,20 @@ static gb_status parse_footer(gb_pq_file *f) {
                     set_error("nested Parquet schemas are not supported on the GPU path");
                     return GB_ERR_UNSUPPORTED;
                 }
+                // unsigned integers (converted types UINT_8..UINT_64, or a
+                // LogicalType INTEGER with isSigned = false): 8- and 16-bit
+                // values fit an INTEGER; 32- and 64-bit values (and their
+                // statistics, which Parquet orders unsigned) do not fit the
+                // signed types, so those columns are refused
+                const bool uns = (conv >= 11 && conv <= 14) || (int_bits != 0 && !int_signed);
+                const int ubits = conv == 11 ? 8 : conv == 12 ? 16 : conv == 13 ? 32 : conv == 14 ? 64 : int_bits;
                 switch (c.ptype) {
                 case 1:
-                    c.gtype = (conv == 16 || int_bits == 16) ? GB_T_SMALLINT : GB_T_INTEGER;
+                    if (uns) c.gtype = ubits <= 16 ? GB_T_INTEGER : 0;
+                    else c.gtype = (conv == 16 || int_bits == 16) ? GB_T_SMALLINT : GB_T_INTEGER;
                     c.width = 4;
                     break;
-                case 2: c.gtype = GB_T_BIGINT; c.width = 8; break;
+                case 2: c.gtype = uns ? 0 : GB_T_BIGINT; c.width = 8; break;
                 case 5: c.gtype = GB_T_DOUBLE; c.width = 8; break;
                 case 6: c.gtype = GB_T_VARCHAR; c.width = 0; break;  // BYTE_ARRAY (UTF8 or not)
                 default: c.gtype = 0; c.width = 0; break;
@@ -1331,11 +1341,16 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
     std::vector<char> live(rg_end - rg_begin, 1);
     uint32_t n_live = 0;
     for (uint32_t g = rg_begin; g < rg_end; g++) {
-        for (int q = 0; q < v.n_filters; q++)
-            if (!pq_rg_might_match(f, g, col_map[v.filters[q].col], v.filters[q])) {
+        for (int q = 0; q < v.n_filters; q++) {
+            // a SMALLINT spec over an INT32 file column compares narrowed
+            // values: the file's int32 statistics do not bound them
+            const int fc = col_map[v.filters[q].col];
+            if (v.col_types[v.filters[q].col] == GB_T_SMALLINT && f->cols[fc].gtype == GB_T_INTEGER) continue;
+            if (!pq_rg_might_match(f, g, fc, v.filters[q])) {
                 live[g - rg_begin] = 0;
                 break;
             }
+        }
         n_live += live[g - rg_begin] ? 1u : 0u;
     }
     if (n_live == 0) return GB_OK;

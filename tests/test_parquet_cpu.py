@@ -213,3 +213,24 @@ def test_zone_maps_from_pyarrow_statistics():
                 assert pf.row_group_might_match(g, [0, 1], [(0, op, const)]) == \
                     _zone_expect(op, const, int(k[lo:hi].min()), int(k[lo:hi].max())), (g, op, const)
     pf.close()
+
+
+def test_unsigned_columns():
+    """Unsigned integers: uint8/uint16 columns (stored INT32) read as INTEGER;
+    uint32/uint64 columns, whose values and statistics are ordered unsigned
+    (values >= 2^31 would read negative), are refused by the GPU path, so a
+    zone map can never rule out a row group on statistics read with the wrong
+    sign."""
+    pa = pytest.importorskip("pyarrow")
+    pq_ = pytest.importorskip("pyarrow.parquet")
+    n = 1000
+    u32 = np.array([1, 0xFFFFFFFF] * (n // 2), dtype=np.uint32)
+    t = pa.table({"a": pa.array(np.arange(n) % 200, type=pa.uint8()),
+                  "b": pa.array(np.arange(n) * 60, type=pa.uint16()),
+                  "c": pa.array(u32, type=pa.uint32()),
+                  "d": pa.array(np.arange(n, dtype=np.uint64) << np.uint64(40), type=pa.uint64())})
+    buf = io.BytesIO()
+    pq_.write_table(t, buf, row_group_size=500, compression="none", write_statistics=True)
+    pf = capi.ParquetFile(buf.getvalue())
+    assert pf.columns() == [("a", capi.INTEGER), ("b", capi.INTEGER), ("c", 0), ("d", 0)]
+    pf.close()
