@@ -479,7 +479,7 @@ struct gb_agg {
     bool r_ready = false;
     DevBuf r_skeys, r_scnt, r_hist, r_hot_keys, r_hot_part, r_cursor, r_part, r_part2, r_ovf;
     DevBuf r_off, r_cap, r_off2, r_cap2;    // per-partition region start / capacity (device)
-    DevBuf r_hot_idx, r_hot_list, r_hstate;
+    DevBuf r_hot_idx, r_hot_list, r_hstate, r_cand;
     DevBuf r_p2w;                           // P2 state words folded in L2 (plans whose ops are all DOUBLE SUM)
     std::vector<u64> h_off;                 // host copies
     std::vector<u32> h_capv;
@@ -856,7 +856,7 @@ static RadixRef radix_ref(gb_agg *h) {
     X.ovf = (u64 *)h->r_ovf.p;
     X.ovf_cap = h->r_ovf_cap;
     // tiles still in flight after the threshold trips add at most grid * tile rows
-    const u64 inflight = (u64)h->r_grid * radix_tile_rows(h->rplan) + 4096;
+    const u64 inflight = radix_inflight_rows(h->rplan, h->r_grid) + 4096;
     X.ovf_threshold = h->r_ovf_cap > inflight ? (u32)(h->r_ovf_cap - inflight) : 0u;
     X.hot_keys = (const u64 *)h->r_hot_keys.p;
     X.hot_idx = (const uint16_t *)h->r_hot_idx.p;
@@ -879,7 +879,7 @@ static gb_status radix_begin(gb_agg *h, u64 n, cudaStream_t st) {
     if ((s = h->r_skeys.ensure(scap * 8)) || (s = h->r_scnt.ensure(scap * 4)) ||
         (s = h->r_hist.ensure(HIST_BINS * 4)) || (s = h->r_hstate.ensure(16)) ||
         (s = h->r_hot_keys.ensure((size_t)R.HS * 8)) || (s = h->r_hot_idx.ensure((size_t)R.HS * 2)) ||
-        (s = h->r_hot_list.ensure((size_t)R.nh * 8)))
+        (s = h->r_hot_list.ensure((size_t)R.nh * 8)) || (s = h->r_cand.ensure((size_t)R.nh * 12)))
         return s;
     if ((s = radix_fill_u64((u64 *)h->r_skeys.p, scap, EMPTY_KEY, st))) return s;
     GB_CUDA(cudaMemsetAsync(h->r_scnt.p, 0, scap * 4, st));
@@ -891,7 +891,8 @@ static gb_status radix_begin(gb_agg *h, u64 n, cudaStream_t st) {
     {
         ProfScope ps(h, "k_sample", st);
         if ((s = radix_launch_sample(h->plan, R, n, (u64 *)h->r_skeys.p, (u32 *)h->r_scnt.p, scap,
-                                     (u32 *)h->r_hist.p, (u32 *)h->r_hstate.p, (u64 *)h->r_hot_keys.p,
+                                     (u32 *)h->r_hist.p, (u32 *)h->r_hstate.p, (u64 *)h->r_cand.p,
+                                     (u32 *)((u64 *)h->r_cand.p + R.nh), (u64 *)h->r_hot_keys.p,
                                      (uint16_t *)h->r_hot_idx.p, (u64 *)h->r_hot_list.p, st, &h->launches)))
             return s;
     }
@@ -924,7 +925,7 @@ static gb_status radix_begin(gb_agg *h, u64 n, cudaStream_t st) {
     if ((s = h->r_hot_part.ensure((size_t)h->r_grid * R.nh * W * 8))) return s;
     if ((s = radix_fill_identity((u64 *)h->r_hot_part.p, (u64)h->r_grid * R.nh * W, W, h->plan, st))) return s;
     h->launches++;
-    u32 ovf_cap = (1u << 21) + (u32)(h->r_grid * radix_tile_rows(R)) + 4096;
+    u32 ovf_cap = (1u << 21) + (u32)radix_inflight_rows(R, h->r_grid) + 4096;
     if (h->r_ovf_cap < ovf_cap) {
         if ((s = h->r_ovf.ensure((size_t)ovf_cap * (TV + 1) * 8))) return s;
         h->r_ovf_cap = ovf_cap;
@@ -1937,7 +1938,7 @@ void gb_agg_destroy(gb_agg *h) {
     h->host_str_bytes.release();
     for (DevBuf *b : {&h->r_skeys, &h->r_scnt, &h->r_hist, &h->r_hot_keys, &h->r_hot_part, &h->r_cursor, &h->r_part,
                       &h->r_part2, &h->r_ovf, &h->r_off, &h->r_cap, &h->r_off2, &h->r_cap2, &h->r_hot_idx,
-                      &h->r_hot_list, &h->r_hstate, &h->r_p2w, &h->dsets, &h->dsets_old, &h->null_sets,
+                      &h->r_hot_list, &h->r_hstate, &h->r_cand, &h->r_p2w, &h->dsets, &h->dsets_old, &h->null_sets,
                       &h->null_sets_old, &h->dmeta})
         b->release();
     h->topn_ids_a.release();

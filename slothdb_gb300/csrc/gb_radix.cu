@@ -49,8 +49,12 @@
 
 namespace gb {
 
+// P1 hash of a group key: the high half folded into the low half, then one
+// multiplicative (Fibonacci) step.  Its top bits pick the partition, bits
+// 32.. the hot bucket.  (P2 hashes the keys of a partition with mix64.)
+__device__ __forceinline__ u64 p1_hash(u64 k) { return (k ^ (k >> 32)) * 0x9E3779B97F4A7C15ull; }
 __device__ __forceinline__ u32 part_of(u64 h, int pbits) { return pbits ? (u32)(h >> (64 - pbits)) : 0u; }
-__device__ __forceinline__ u32 hot_slot(u64 h, int HS) { return (u32)h & (u32)(HS - 1); }
+__device__ __forceinline__ u32 hot_bucket(u64 h, int HB) { return (u32)(h >> 32) & (u32)(HB - 1); }
 __device__ __forceinline__ u32 agg_slot(u64 h, int SP) { return (u32)(h >> 20) & (u32)(SP - 1); }
 
 // ------------------------------------------------------------- sampling
@@ -101,42 +105,99 @@ __device__ __forceinline__ u32 count_threshold(const u32 *hist, u32 cap, u32 flo
     return t;
 }
 
-// Build the hot table (HS slots: key, dense hot index) and the hot list.
-// hstate[0] = super-hot keys assigned, hstate[1] = warm keys assigned,
-// hstate[2] = sampled rows covered by hot keys.
-__global__ void k_hot_build(const u64 *skeys, const u32 *scnt, u64 scap, const u32 *hist, u32 *hstate, int NSUP,
-                            int NH, u64 *hot_keys, uint16_t *hot_idx, u64 *hot_list, int HS) {
-    __shared__ u32 s_t, s_ts;
-    if (threadIdx.x == 0) {
-        s_t = count_threshold(hist, (u32)NH, 2);
-        s_ts = count_threshold(hist, (u32)NSUP, max(2u, s_t));
-    }
+// Hot-set candidates: every sampled key whose count reaches the threshold
+// that admits at most NH keys (hstate[3] = candidates found).
+__global__ void k_hot_collect(const u64 *skeys, const u32 *scnt, u64 scap, const u32 *hist, u32 *hstate, int NH,
+                              u64 *cand_key, u32 *cand_cnt) {
+    __shared__ u32 s_t;
+    if (threadIdx.x == 0) s_t = count_threshold(hist, (u32)NH, 2);
     __syncthreads();
-    const u32 t = s_t, ts = s_ts;
+    const u32 t = s_t;
     if (t >= HIST_BINS) return;
     for (u64 s = blockIdx.x * (u64)blockDim.x + threadIdx.x; s < scap; s += (u64)gridDim.x * blockDim.x) {
         const u64 k = skeys[s];
         if (k == EMPTY_KEY) continue;
         const u32 c = min(scnt[s], (u32)(HIST_BINS - 1));
         if (c < t) continue;
-        u32 idx;
-        if (c >= ts && ts < HIST_BINS) {
-            idx = atomicAdd(&hstate[0], 1u);
-            if (idx >= (u32)NSUP) continue;  // cannot happen: the threshold admits <= NSUP
-        } else {
-            idx = atomicAdd(&hstate[1], 1u) + (u32)NSUP;
-            if (idx >= (u32)NH) continue;
+        const u32 i = atomicAdd(&hstate[3], 1u);
+        if (i < (u32)NH) {
+            cand_key[i] = k;
+            cand_cnt[i] = scnt[s];
         }
-        atomicAdd(&hstate[2], scnt[s]);
-        hot_list[idx] = k;
-        u32 h = hot_slot(mix64(k), HS);
-        for (int p = 0; p < HS; p++) {
-            const u64 old = atomicCAS(&hot_keys[h], EMPTY_KEY, k);
-            if (old == EMPTY_KEY) {
-                hot_idx[h] = (uint16_t)idx;
-                break;
+    }
+}
+
+// Rank the candidates (sampled count descending, key ascending: rank 0 is
+// the hottest key) and place them, in rank order, into the 2-way bucket
+// table: slot 2b + w of bucket b = hot_bucket(key).  A key whose bucket is
+// already full is not hot (its rows take the partitioned path), so the
+// hottest keys always get a slot and a lookup is one 16-byte shared load.
+// hot_list[rank] = key for every candidate; hstate[0] = candidates among the
+// NSUP hottest, hstate[1] = the others, hstate[2] = sampled rows of the
+// placed keys.  One block of 1024 threads, HOT_RANK_SMEM bytes of dynamic
+// shared memory; NH <= 4096, HB <= 4096.
+#define HOT_RANK_SMEM (4096 * 8 + 4096 * 4 + 4096)
+__global__ void __launch_bounds__(1024) k_hot_rank(const u64 *cand_key, const u32 *cand_cnt, u32 *hstate, int NSUP,
+                                                   int NH, int HB, u64 *hot_keys, uint16_t *hot_rank,
+                                                   u64 *hot_list) {
+    extern __shared__ u64 hrsm[];
+    u64 *sk = hrsm;                          // [4096]
+    u32 *scn = (u32 *)(sk + 4096);           // [4096]
+    uint8_t *fill = (uint8_t *)(scn + 4096); // [4096]
+    const u32 n = min(hstate[3], (u32)min(NH, 4096));
+    u32 n2 = 1;
+    while (n2 < n) n2 <<= 1;
+    for (u32 i = threadIdx.x; i < n2; i += blockDim.x) {
+        sk[i] = i < n ? cand_key[i] : ~0ull;
+        scn[i] = i < n ? cand_cnt[i] : 0u;
+    }
+    for (int i = threadIdx.x; i < HB; i += blockDim.x) fill[i] = 0;
+    __syncthreads();
+    // bitonic sort of n2 entries: "before" = larger count, then smaller key
+    for (u32 size = 2; size <= n2; size <<= 1) {
+        for (u32 stride = size >> 1; stride > 0; stride >>= 1) {
+            for (u32 i = threadIdx.x; i < n2 / 2; i += blockDim.x) {
+                const u32 lo = 2 * i - (i & (stride - 1));
+                const u32 hi = lo + stride;
+                const bool up = (lo & size) == 0;
+                const u32 ca = scn[lo], cb = scn[hi];
+                const u64 ka = sk[lo], kb = sk[hi];
+                const bool b_first = cb > ca || (cb == ca && kb < ka);
+                if (b_first == up) {
+                    scn[lo] = cb;
+                    scn[hi] = ca;
+                    sk[lo] = kb;
+                    sk[hi] = ka;
+                }
             }
-            h = (h + 1) & (u32)(HS - 1);
+            __syncthreads();
+        }
+    }
+    for (u32 i = threadIdx.x; i < n; i += blockDim.x) hot_list[i] = sk[i];
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        u32 placed_rows = 0;
+        for (u32 c0 = 0; c0 < n; c0 += 32) {
+            const u32 r = c0 + lane;
+            const u64 k = r < n ? sk[r] : 0ull;
+            const u32 b = r < n ? hot_bucket(p1_hash(k), HB) : 0xffffffffu;
+            const unsigned peers = __match_any_sync(FULL, b);
+            const u32 f = r < n ? fill[b] : 2u;
+            const u32 pos = __popc(peers & ((1u << lane) - 1u));
+            if (r < n && f + pos < 2) {
+                hot_keys[2 * b + f + pos] = k;
+                hot_rank[2 * b + f + pos] = (uint16_t)r;
+                placed_rows += scn[r];
+            }
+            __syncwarp();
+            if (r < n && lane == 31 - __clz(peers)) fill[b] = (uint8_t)min(2u, f + (u32)__popc(peers));
+            __syncwarp();
+        }
+        placed_rows = __reduce_add_sync(FULL, placed_rows);
+        if (lane == 0) {
+            hstate[0] = min(n, (u32)NSUP);
+            hstate[1] = n - min(n, (u32)NSUP);
+            hstate[2] = placed_rows;
         }
     }
 }
@@ -249,14 +310,12 @@ __device__ __forceinline__ void store_at(const RadixRef &X, const TableRef &T, u
 }
 
 // ------------------------------------------------------------- P1 scatter
-// Block: P1_WARPS warps, ROWS rows per thread per tile.  The REG_HOT hottest
-// keys accumulate in per-lane registers; the next NPRIV - REG_HOT have a
-// private state per warp (u32 count + W-1 words; only this warp's lanes
-// contend on its atomics); the other hot keys share one state per CTA.
-// SPEC != 0: the plan is one non-NULL BIGINT key, one non-NULL value column,
-// one op (SPEC = OP_ADD_F or OP_ADD_I) and no predicates — every per-row plan
-// interpretation (key packing, type and op switches) is compiled away.
-template <int ROWS, int VV, int NOPS, int SPEC = 0>
+// Generic plans.  Block: P1_WARPS warps, ROWS rows per thread per tile.  The
+// REG_HOT hottest keys accumulate in per-lane registers; the next NPRIV -
+// REG_HOT have a private state per warp (u32 count + W-1 words; only this
+// warp's lanes contend on its atomics); the other hot keys share one state
+// per CTA.  Cold tuples go through per-CTA write-combining buffers.
+template <int ROWS, int VV, int NOPS>
 __global__ void __launch_bounds__(P1_WARPS * 32, 1)
     k_partition(const __grid_constant__ Plan P, const __grid_constant__ RadixPlan R, const RadixRef X,
                 const TableRef T, const RadixTile A) {
@@ -276,7 +335,8 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
     u32 *bcnt = sc + NWARM;                               // [NP] buffered tuples
     u32 *sbase = bcnt + NP;                               // [NP] flush base this tile
     u32 *snf = sbase + NP;                                // [NP] tuples flushed this tile
-    uint16_t *hix = (uint16_t *)(snf + NP);               // [HS] hot index
+    uint16_t *hix = (uint16_t *)(snf + NP);               // [HS] hot rank of each bucket slot
+    const int HB = HS >> 1;
     __shared__ u32 s_tile;
     for (int i = threadIdx.x; i < HS; i += NT) {
         hk[i] = X.hot_keys[i];
@@ -339,14 +399,8 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
             kinds[j] = 0;
             pk[j] = 0;
             if (acts[j]) {
-                if (SPEC) {
-                    pk[j] = (u64)__ldg((const long long *)P.cols[P.key_col[0]].data + r);
-                    kinds[j] = pk[j] == EMPTY_KEY ? 1 : 0;
-                    tv[j][0] = (u64)__ldg((const long long *)P.cols[R.vcol[0]].data + r);
-                } else {
-                    kinds[j] = make_key(P, r, pk[j]);
-                    tuple_vals<VV>(P, R, r, tv[j]);
-                }
+                kinds[j] = make_key(P, r, pk[j]);
+                tuple_vals<VV>(P, R, r, tv[j]);
             }
         }
 #pragma unroll
@@ -355,15 +409,14 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
             pend[j] = 0;
             pslot[j] = 0;
             bool act = acts[j];
-            if (!SPEC && act && P.n_filters) act = pass_filters(P, r);
+            if (act && P.n_filters) act = pass_filters(P, r);
             u32 hidx = 0;
             u64 v[NOPS > 0 ? NOPS : 1];
 #pragma unroll
             for (int q = 0; q < (NOPS > 0 ? NOPS : 1); q++) v[q] = 0;
             if (act) {
                 const int kind = kinds[j];
-                if (SPEC) v[0] = tv[j][0];
-                else tuple_contrib<VV, NOPS>(P, R, tv[j], v);
+                tuple_contrib<VV, NOPS>(P, R, tv[j], v);
                 if (kind != 0) {
                     if (kind == 3) {
                         atomicOr(&T.ctl->err, (u32)ERR_NULL_IN_WIDE_KEY);
@@ -372,39 +425,22 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
                         fold_atomic<NOPS>(P, w, 1, v);
                     }
                 } else {
-                    const u64 h = mix64(pk[j]);
+                    const u64 h = p1_hash(pk[j]);
                     bool hot = false;
                     if (HS) {
-                        u32 s = hot_slot(h, HS);
-                        for (int q = 0; q < R.hot_probe; q++) {
-                            const u64 k = hk[s];
-                            if (k == pk[j]) {
-                                hidx = hix[s];
-                                hot = true;
-                                break;
-                            }
-                            if (k == EMPTY_KEY) break;
-                            s = (s + 1) & (u32)(HS - 1);
+                        // the key's 2-way bucket: one 16-byte shared load
+                        const u32 b = hot_bucket(h, HB);
+                        const ulonglong2 kk = *(const ulonglong2 *)(hk + 2 * b);
+                        if (kk.x == pk[j]) {
+                            hidx = hix[2 * b];
+                            hot = true;
+                        } else if (kk.y == pk[j]) {
+                            hidx = hix[2 * b + 1];
+                            hot = true;
                         }
                     }
                     if (hot) {
-                        if (SPEC) {
-                            // one path for every hot tier (lanes of a warp hit
-                            // different tiers; separate paths would run one after
-                            // another): branch-free register counts for the
-                            // REG_HOT hottest keys, one native 32-bit shared
-                            // atomic for the other counts, and the sum as one
-                            // fire-and-forget reduction into this CTA's hot slice
-                            // in L2 (no FP64 arithmetic on the SM, no shared
-                            // 64-bit compare-and-swap loop)
-#pragma unroll
-                            for (int k = 0; k < REG_HOT; k++) rc[k] += hidx == (u32)k ? 1u : 0u;
-                            if (hidx >= (u32)REG_HOT)
-                                atomicAdd((int)hidx < NPRIV ? mypc + hidx : sc + (hidx - NPRIV), 1u);
-                            u64 *hw = hpart + (size_t)hidx * W + P.ops[0].word;
-                            if (SPEC == OP_ADD_F) atomicAdd((double *)hw, __longlong_as_double((i64)v[0]));
-                            else atomicAdd((unsigned long long *)hw, (unsigned long long)v[0]);
-                        } else if (hidx < (u32)REG_HOT) {
+                        if (hidx < (u32)REG_HOT) {
 #pragma unroll
                             for (int k = 0; k < REG_HOT; k++) {
                                 if (hidx == (u32)k) {
@@ -506,12 +542,7 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
         }
     }
     __syncthreads();
-    // fold private and shared hot states into this CTA's slice (after the
-    // slice's L2 reductions of the specialised kernel are visible)
-    if (SPEC) {
-        __threadfence();
-        __syncthreads();
-    }
+    // fold private and shared hot states into this CTA's slice
     u64 *hp = hpart;
     for (int i = threadIdx.x; i < NH; i += NT) {
         u64 acc[GB_MAX_WORDS];
@@ -529,6 +560,154 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
         }
         for (int w = 0; w < W; w++) hp[(size_t)i * W + w] = acc[w];
     }
+}
+
+// ------------------------------------------------------------- P1, one key + one SUM
+// The specialised P1 for the plan "one non-NULL BIGINT key, one non-NULL
+// value column, one SUM (DOUBLE: OPK = OP_ADD_F, BIGINT: OP_ADD_I), no
+// predicates".  Nothing in its row loop waits on other warps: each warp
+// claims P1D_CLAIM steps of P1D_RUN rows at a time and streams them with
+// 128-bit loads (4 rows per lane).  A hot row (its key in the 2-way bucket
+// table) counts in registers (the REG_HOT hottest keys) or in a shared u32
+// counter, and adds its value to this CTA's hot slice with one
+// fire-and-forget L2 reduction (no FP64 arithmetic on the SM).  A cold row
+// reserves its slot with one atomic on its partition's cursor and writes its
+// 16-byte tuple straight to the partition region: the regions' write
+// frontiers stay in L2, so every 32-byte sector is complete before it is
+// written back.  A tuple beyond its region's capacity goes to the overflow
+// list (the host grows the region and re-runs the rest).
+#define P1D_RUN 128   // rows per warp step: lane l owns rows 64j + 2l, 64j + 2l + 1 (j = 0, 1)
+#define P1D_CLAIM 8   // steps per claim (1024 rows)
+
+size_t radix_p1d_smem(const RadixPlan &R) {
+    const size_t HB = (size_t)R.HS / 2, NP = (size_t)1 << R.pbits;
+    return HB * 16 + NP * 8 + HB * 4 + NP * 4 + (size_t)R.nh * 4;
+}
+
+template <int OPK>
+__global__ void __launch_bounds__(P1_WARPS * 32, 1)
+    k_partition_direct(const __grid_constant__ Plan P, const __grid_constant__ RadixPlan R, const RadixRef X,
+                       const TableRef T, const RadixTile A) {
+    extern __shared__ u64 rsm[];
+    const int HB = R.HS >> 1, NH = R.nh, NP = 1 << R.pbits, W = P.words;
+    const int lane = threadIdx.x & 31;
+    ulonglong2 *hb = (ulonglong2 *)rsm;  // [HB] bucket keys (way 0, way 1)
+    u64 *pbase = (u64 *)(hb + HB);       // [NP] first tuple of each partition region
+    u32 *hr = (u32 *)(pbase + NP);       // [HB] bucket ranks: way 0 in the low half, way 1 in the high half
+    u32 *pcap = hr + HB;                 // [NP] tuples each region holds
+    u32 *sc = pcap + NP;                 // [NH] hot counts (ranks >= REG_HOT)
+    for (int i = threadIdx.x; i < HB; i += blockDim.x) {
+        hb[i] = ((const ulonglong2 *)X.hot_keys)[i];
+        hr[i] = ((const u32 *)X.hot_idx)[i];
+    }
+    for (int p = threadIdx.x; p < NP; p += blockDim.x) {
+        pbase[p] = X.part_off[p];
+        pcap[p] = X.part_cap[p];
+    }
+    for (int i = threadIdx.x; i < NH; i += blockDim.x) sc[i] = 0;
+    __syncthreads();
+    const u64 *kcol = (const u64 *)P.cols[P.key_col[0]].data;
+    const u64 *vcol = (const u64 *)P.cols[R.vcol[0]].data;
+    const bool vec = ((((u64)kcol) | ((u64)vcol)) & 15) == 0;
+    u64 *hsum = X.hot_part + (u64)blockIdx.x * NH * W + P.ops[0].word;  // this CTA's hot slice, SUM word
+    u64 *oob = T.slots + T.cap * (u64)T.stride + 1;  // state words of the key equal to EMPTY_KEY
+    const u64 n = A.n_rows;
+    u32 rc[REG_HOT];
+#pragma unroll
+    for (int q = 0; q < REG_HOT; q++) rc[q] = 0;
+    for (;;) {
+        u32 c = ~0u;
+        if (lane == 0 && *(volatile u32 *)&T.ctl->stop == 0) {
+            const u32 t = atomicAdd(&T.ctl->tile_counter, 1u);
+            if (t < A.n_tiles) c = t;
+        }
+        c = __shfl_sync(FULL, c, 0);
+        if (c == ~0u) break;
+        const u64 c0 = ((u64)A.first_tile + c) * (u64)(P1D_RUN * P1D_CLAIM);
+        for (int stp = 0; stp < P1D_CLAIM; stp++) {
+            const u64 r0 = c0 + (u64)stp * P1D_RUN;
+            if (r0 >= n) break;
+            u64 k[4], v[4];
+            u32 live = 0xfu;
+            if (vec && r0 + P1D_RUN <= n) {
+#pragma unroll
+                for (int j = 0; j < 2; j++) {
+                    const ulonglong2 a = __ldcs((const ulonglong2 *)(kcol + r0 + 64 * j + 2 * lane));
+                    const ulonglong2 b = __ldcs((const ulonglong2 *)(vcol + r0 + 64 * j + 2 * lane));
+                    k[2 * j] = a.x;
+                    k[2 * j + 1] = a.y;
+                    v[2 * j] = b.x;
+                    v[2 * j + 1] = b.y;
+                }
+            } else {
+                live = 0;
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const u64 r = r0 + 64 * (j >> 1) + 2 * lane + (j & 1);
+                    k[j] = 0;
+                    v[j] = 0;
+                    if (r < n) {
+                        k[j] = kcol[r];
+                        v[j] = vcol[r];
+                        live |= 1u << j;
+                    }
+                }
+            }
+            u32 cp[4];  // partition + 1 of a cold row, 0 otherwise
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                cp[j] = 0;
+                if (!((live >> j) & 1u)) continue;
+                const u64 key = k[j];
+                if (key == EMPTY_KEY) {  // out-of-band slot of the HBM table
+                    fold_atomic<1>(P, oob, 1, &v[j]);
+                    continue;
+                }
+                const u64 h = p1_hash(key);
+                const u32 b = hot_bucket(h, HB);
+                const ulonglong2 kk = hb[b];
+                const u32 rr = hr[b];
+                const int rank = kk.x == key ? (int)(rr & 0xffffu) : (kk.y == key ? (int)(rr >> 16) : -1);
+                if (rank >= 0) {
+#pragma unroll
+                    for (int q = 0; q < REG_HOT; q++) rc[q] += rank == q ? 1u : 0u;
+                    if (rank >= REG_HOT) atomicAdd(&sc[rank], 1u);
+                    u64 *w = hsum + (size_t)rank * W;
+                    if (OPK == OP_ADD_F) atomicAdd((double *)w, __longlong_as_double((i64)v[j]));
+                    else atomicAdd((unsigned long long *)w, (unsigned long long)v[j]);
+                } else {
+                    cp[j] = part_of(h, R.pbits) + 1;
+                }
+            }
+            // every reservation of the step is issued before its stores
+            u32 pos[4];
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                pos[j] = cp[j] ? atomicAdd(&X.cursor[(u64)(cp[j] - 1) * CURSOR_PAD], 1u) : 0u;
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                if (!cp[j]) continue;
+                const u32 p = cp[j] - 1;
+                if (pos[j] < pcap[p]) {
+                    *(ulonglong2 *)(X.part + (pbase[p] + pos[j]) * 2) = make_ulonglong2(k[j], v[j]);
+                } else {
+                    put_overflow<1>(X, T, p, k[j], &v[j]);
+                    if (*(volatile u32 *)&T.ctl->aux0 > X.ovf_threshold) atomicExch(&T.ctl->stop, 1u);
+                }
+            }
+        }
+    }
+    // register counts (summed over the warp) join the shared counts
+#pragma unroll
+    for (int q = 0; q < REG_HOT; q++) {
+        const u32 t = __reduce_add_sync(FULL, rc[q]);
+        if (lane == 0 && t && q < NH) atomicAdd(&sc[q], t);
+    }
+    __syncthreads();
+    // counts into word 0 of this CTA's hot slice (only this CTA writes it)
+    u64 *hcnt = X.hot_part + (u64)blockIdx.x * NH * W;
+    for (int i = threadIdx.x; i < NH; i += blockDim.x)
+        if (sc[i]) hcnt[(size_t)i * W] += sc[i];
 }
 
 // Append overflow tuples to their (grown) partitions.
@@ -780,7 +959,29 @@ bool radix_p2_global_words(const Plan &P, const RadixPlan &R) {
     return true;
 }
 
-u32 radix_tile_rows(const RadixPlan &R) { return (u32)((R.V == 3 ? RADIX_ROWS / 2 : RADIX_ROWS) * P1_WARPS * 32); }
+// Rows of one claim of the P1 kernel that runs (a CTA tile of the generic
+// kernel, a warp claim of the specialised one) and the rows that can still be
+// in flight when the kernel is told to stop (every claim is finished).
+u32 radix_tile_rows(const RadixPlan &R) {
+    if (R.spec) return (u32)(P1D_RUN * P1D_CLAIM);
+    return (u32)((R.V == 3 ? RADIX_ROWS / 2 : RADIX_ROWS) * P1_WARPS * 32);
+}
+u64 radix_inflight_rows(const RadixPlan &R, int grid) {
+    return (u64)grid * radix_tile_rows(R) * (R.spec ? P1_WARPS : 1);
+}
+
+// The specialised P1 applies (decided when the plan is made: the columns'
+// NOT NULL declarations hold for every ingest): one non-NULL BIGINT key, one
+// non-NULL value column, one ADD op, no predicates.
+static int p1_spec(const Plan &P, const RadixPlan &R, u64 nullable_mask) {
+    if (P.key_mode != KEY_SINGLE || P.cols[P.key_col[0]].type != GB_T_BIGINT) return 0;
+    if ((nullable_mask >> P.key_col[0]) & 1ull) return 0;
+    if (R.V != 1 || P.n_ops != 1 || P.n_filters || ((nullable_mask >> R.vcol[0]) & 1ull)) return 0;
+    const int t = P.cols[R.vcol[0]].type;
+    if (P.ops[0].kind == OP_ADD_F && t == GB_T_DOUBLE) return OP_ADD_F;
+    if (P.ops[0].kind == OP_ADD_I && t == GB_T_BIGINT) return OP_ADD_I;
+    return 0;
+}
 
 static const size_t kSmemBudget = 224 * 1024;  // <= the 227 KiB opt-in minus static shared memory
 
@@ -805,10 +1006,16 @@ gb_status radix_prepare(const Plan &P, RadixPlan &R, u64 est_groups, u64 nullabl
         R.V = 1;
     }
     if (P.words > GB_MAX_WORDS) return GB_ERR_UNSUPPORTED;
-    // P2: one shared table of `sub` slots per partition
+    R.spec = p1_spec(P, R, nullable_mask);
+    // P2: one shared table of `sub` slots per partition (keys + counts only,
+    // 12 bytes a slot, when the state words fold in L2)
     int sp = 8192;
     R.sub = sp;
-    while (sp > 512 && radix_p2_smem(P, R) > kSmemBudget) {
+    if (radix_p2_global_words(P, R) && (size_t)16384 * 12 <= kSmemBudget) {
+        sp = 16384;
+        R.sub = sp;
+    }
+    while (sp > 512 && !radix_p2_global_words(P, R) && radix_p2_smem(P, R) > kSmemBudget) {
         sp /= 2;
         R.sub = sp;
     }
@@ -828,6 +1035,7 @@ gb_status radix_prepare(const Plan &P, RadixPlan &R, u64 est_groups, u64 nullabl
     R.nh = 4096;
     R.nsup = 64;
     R.hot_probe = 8;
+    if (R.spec) return radix_p1d_smem(R) <= kSmemBudget ? GB_OK : GB_ERR_UNSUPPORTED;
     while (radix_p1_smem(P, R) > kSmemBudget) {
         // keep the hot set large (a key left out of it lands in P2, where its
         // repeats contend): shrink the warp-private tier first
@@ -852,22 +1060,31 @@ gb_status radix_set_bits(const Plan &P, RadixPlan &R, int bits) {
     if (bits < 6 || bits > 12) return GB_ERR_INVALID;
     RadixPlan t = R;
     t.pbits = bits;
-    if (radix_p1_smem(P, t) > kSmemBudget) return GB_ERR_UNSUPPORTED;
+    if ((t.spec ? radix_p1d_smem(t) : radix_p1_smem(P, t)) > kSmemBudget) return GB_ERR_UNSUPPORTED;
     R = t;
     return GB_OK;
 }
 
+static gb_status radix_set_attributes();
+
 gb_status radix_launch_sample(const Plan &P, const RadixPlan &R, u64 n, u64 *skeys, u32 *scnt, u64 scap,
-                              u32 *hist, u32 *hstate, u64 *hot_keys, uint16_t *hot_idx, u64 *hot_list,
-                              cudaStream_t st, u64 *launches) {
+                              u32 *hist, u32 *hstate, u64 *cand_key, u32 *cand_cnt, u64 *hot_keys,
+                              uint16_t *hot_idx, u64 *hot_list, cudaStream_t st, u64 *launches) {
+    if (R.nh > 4096 || R.HS != 2 * R.nh) {
+        set_error("radix plan: the hot set holds at most 4096 keys in twice as many bucket slots");
+        return GB_ERR_INVALID;
+    }
+    if (gb_status s = radix_set_attributes()) return s;
     const u64 m = std::min<u64>(n, scap / 2);
     const u64 step = std::max<u64>(1, n / std::max<u64>(m, 1));
     const int sms = sm_count();
     k_sample_count<<<grid_of(m, 256, sms * 4), 256, 0, st>>>(P, n, step, m, skeys, scnt, scap);
     k_sample_hist<<<grid_of(scap, 256, sms * 2), 256, 0, st>>>(skeys, scnt, scap, hist);
-    k_hot_build<<<grid_of(scap, 256, sms * 2), 256, 0, st>>>(skeys, scnt, scap, hist, hstate, R.nsup, R.nh,
-                                                            hot_keys, hot_idx, hot_list, R.HS);
-    *launches += 3;
+    k_hot_collect<<<grid_of(scap, 256, sms * 2), 256, 0, st>>>(skeys, scnt, scap, hist, hstate, R.nh, cand_key,
+                                                              cand_cnt);
+    k_hot_rank<<<1, 1024, HOT_RANK_SMEM, st>>>(cand_key, cand_cnt, hstate, R.nsup, R.nh, R.HS / 2, hot_keys, hot_idx,
+                                               hot_list);
+    *launches += 4;
     GB_CUDA(cudaGetLastError());
     return GB_OK;
 }
@@ -908,29 +1125,19 @@ static P2Fn g_p2[4 * (RADIX_MAX_OPS + 1)];
 static P1Fn g_p1_spec_f, g_p1_spec_i;  // specialised P1: BIGINT key, one SUM (DOUBLE / integer)
 static P2Fn g_p2_gw[RADIX_MAX_OPS + 1];  // P2 with the state words in L2 (ops all DOUBLE SUM), one value column
 
-// The specialised P1 applies: one non-NULL BIGINT key, one non-NULL value
-// column, one ADD op, no predicates.
-static int p1_spec(const Plan &P, const RadixPlan &R) {
-    if (P.key_mode != KEY_SINGLE || P.cols[P.key_col[0]].type != GB_T_BIGINT || P.cols[P.key_col[0]].valid) return 0;
-    if (R.V != 1 || P.n_ops != 1 || P.n_filters || P.cols[R.vcol[0]].valid) return 0;
-    const int t = P.cols[R.vcol[0]].type;
-    if (P.ops[0].kind == OP_ADD_F && t == GB_T_DOUBLE) return OP_ADD_F;
-    if (P.ops[0].kind == OP_ADD_I && t == GB_T_BIGINT) return OP_ADD_I;
-    return 0;
-}
-
 static gb_status radix_set_attributes() {
     static bool done = false;
     if (done) return GB_OK;
     fill_tables<1>(g_p1, g_p2);
     fill_tables<2>(g_p1, g_p2);
     fill_tables<3>(g_p1, g_p2);
-    g_p1_spec_f = (P1Fn)k_partition<RADIX_ROWS, 1, 1, OP_ADD_F>;
-    g_p1_spec_i = (P1Fn)k_partition<RADIX_ROWS, 1, 1, OP_ADD_I>;
+    g_p1_spec_f = (P1Fn)k_partition_direct<OP_ADD_F>;
+    g_p1_spec_i = (P1Fn)k_partition_direct<OP_ADD_I>;
     g_p2_gw[1] = (P2Fn)k_part_agg<1, 1, true>;
     g_p2_gw[2] = (P2Fn)k_part_agg<1, 2, true>;
     for (P1Fn f : {g_p1_spec_f, g_p1_spec_i})
         if (gb_status s = allow_max_smem(f)) return s;
+    if (gb_status s = allow_max_smem(k_hot_rank)) return s;
     for (int o = 1; o <= 2; o++)
         if (gb_status s = allow_max_smem(g_p2_gw[o])) return s;
     for (int v = 1; v <= 3; v++)
@@ -947,11 +1154,17 @@ gb_status radix_launch_p1(const Plan &P, const RadixPlan &R, const RadixRef &X, 
                           const RadixTile &A, int grid, cudaStream_t st) {
     gb_status s = radix_set_attributes();
     if (s) return s;
-    const size_t smem = radix_p1_smem(P, R);
+    size_t smem = radix_p1_smem(P, R);
     P1Fn f = g_p1[R.V * (RADIX_MAX_OPS + 1) + P.n_ops];
-    const int spec = p1_spec(P, R);
-    if (spec == OP_ADD_F) f = g_p1_spec_f;
-    else if (spec == OP_ADD_I) f = g_p1_spec_i;
+    if (R.spec) {
+        // the plan's NOT NULL declarations were checked against every column
+        if (P.cols[P.key_col[0]].valid || P.cols[R.vcol[0]].valid) {
+            set_error("radix plan: a NOT NULL column carries a validity mask");
+            return GB_ERR_INVALID;
+        }
+        f = R.spec == OP_ADD_F ? g_p1_spec_f : g_p1_spec_i;
+        smem = radix_p1d_smem(R);
+    }
     f<<<grid, P1_WARPS * 32, smem, st>>>(P, R, X, T, A);
     GB_CUDA(cudaGetLastError());
     return GB_OK;

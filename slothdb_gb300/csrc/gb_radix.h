@@ -29,6 +29,7 @@ struct RadixPlan {
     int32_t hot_probe;
     int32_t agg_probe;
     int32_t p2_pre;                     // P2: warps pre-combine equal keys (1) or fold each tuple (0)
+    int32_t spec;                       // specialised P1 (OP_ADD_F / OP_ADD_I) or 0
 };
 
 struct RadixRef {
@@ -39,8 +40,8 @@ struct RadixRef {
     u64 *ovf;                 // overflow tuples (partition, key, values...)
     u32 ovf_cap;
     u32 ovf_threshold;
-    const u64 *hot_keys;      // HS keys (EMPTY_KEY = unused)
-    const uint16_t *hot_idx;  // HS dense hot index
+    const u64 *hot_keys;      // HS/2 buckets of 2 keys (EMPTY_KEY = unused)
+    const uint16_t *hot_idx;  // hot rank of each bucket slot
     const u64 *hot_list;      // nh keys by hot index
     u64 *hot_part;            // [grid][nh][words] per-CTA hot partials
     u64 *p2_words;            // [np][sub][words - 1] P2 state words when they fold in L2 (or null)
@@ -58,9 +59,11 @@ gb_status radix_set_bits(const Plan &P, RadixPlan &R, int bits);
 size_t radix_p2_smem(const Plan &P, const RadixPlan &R);
 bool radix_p2_global_words(const Plan &P, const RadixPlan &R);
 u32 radix_tile_rows(const RadixPlan &R);
+u64 radix_inflight_rows(const RadixPlan &R, int grid);
+size_t radix_p1d_smem(const RadixPlan &R);
 gb_status radix_launch_sample(const Plan &P, const RadixPlan &R, u64 n, u64 *skeys, u32 *scnt, u64 scap, u32 *hist,
-                              u32 *hstate, u64 *hot_keys, uint16_t *hot_idx, u64 *hot_list, cudaStream_t st,
-                              u64 *launches);
+                              u32 *hstate, u64 *cand_key, u32 *cand_cnt, u64 *hot_keys, uint16_t *hot_idx,
+                              u64 *hot_list, cudaStream_t st, u64 *launches);
 gb_status radix_launch_p1(const Plan &P, const RadixPlan &R, const RadixRef &X, const TableRef &T,
                           const RadixTile &A, int grid, cudaStream_t st);
 gb_status radix_launch_drain(const RadixRef &X, int V, u32 n, cudaStream_t st);
