@@ -290,44 +290,63 @@ __global__ void __launch_bounds__(512) k_topn(const __grid_constant__ TopnArgs A
     __shared__ int s_nbest, s_ncand;
     __shared__ u64 s_thr_p, s_thr_s;
     const int K = A.K;
+    const int CAPC = sortn - K;  // candidates collected before a sort
     if (threadIdx.x == 0) { s_nbest = 0; s_ncand = 0; s_thr_p = ~0ull; s_thr_s = ~0ull; }
-    // entries [0, K) = best (sorted), [K, 2K) = candidates, rest padding
+    // entries [0, K) = best (sorted), [K, sortn) = candidates
     for (int i = threadIdx.x; i < sortn; i += blockDim.x) { Pp[i] = ~0ull; Ss[i] = ~0ull; Ii[i] = ~0u; }
     __syncthreads();
     const u64 per = (n + gridDim.x - 1) / gridDim.x;
     const u64 lo = blockIdx.x * per, hi = min(n, lo + per);
-    for (u64 base = lo; base < hi; base += blockDim.x) {
-        const u64 it = base + threadIdx.x;
-        u64 cp = ~0ull, cs = ~0ull;
-        u32 row = ~0u;
-        bool want = false;
-        if (it < hi) {
-            row = ids ? ids[it] : (u32)it;
-            if (row != ~0u) {
-                topn_code(A, row, cp, cs);
-                want = s_nbest < K || code_less(cp, cs, s_thr_p, s_thr_s);
+    constexpr int TR = 8;  // rows per thread per pass: their loads are issued together
+    for (u64 base = lo; base < hi; base += (u64)blockDim.x * TR) {
+        u64 cpv[TR], csv[TR];
+        u32 rowv[TR];
+        bool wantv[TR];
+        bool any = false;
+#pragma unroll
+        for (int j = 0; j < TR; j++) {
+            const u64 it = base + (u64)j * blockDim.x + threadIdx.x;
+            cpv[j] = ~0ull;
+            csv[j] = ~0ull;
+            rowv[j] = ~0u;
+            wantv[j] = false;
+            if (it < hi) {
+                rowv[j] = ids ? ids[it] : (u32)it;
+                if (rowv[j] != ~0u) {
+                    topn_code(A, rowv[j], cpv[j], csv[j]);
+                    wantv[j] = s_nbest < K || code_less(cpv[j], csv[j], s_thr_p, s_thr_s);
+                }
             }
+            any |= wantv[j];
         }
-        while (__syncthreads_or(want)) {
-            if (want) {
-                int pos = atomicAdd(&s_ncand, 1);
-                if (pos < K) {
-                    Pp[K + pos] = cp; Ss[K + pos] = cs; Ii[K + pos] = row;
-                    want = false;
+        // once the threshold has settled, no row of a pass usually beats it:
+        // one barrier for TR * blockDim rows
+        if (!__syncthreads_or(any)) continue;
+        for (int j = 0; j < TR; j++) {
+            const u64 cp = cpv[j], cs = csv[j];
+            const u32 row = rowv[j];
+            bool want = wantv[j] && (s_nbest < K || code_less(cp, cs, s_thr_p, s_thr_s));
+            while (__syncthreads_or(want)) {
+                if (want) {
+                    int pos = atomicAdd(&s_ncand, 1);
+                    if (pos < CAPC) {
+                        Pp[K + pos] = cp; Ss[K + pos] = cs; Ii[K + pos] = row;
+                        want = false;
+                    }
                 }
-            }
-            __syncthreads();
-            if (s_ncand >= K) {
-                smem_bitonic(Pp, Ss, Ii, sortn);
-                if (threadIdx.x == 0) {
-                    s_nbest = min(s_nbest + K, K);
-                    s_ncand = 0;
-                    s_thr_p = Pp[K - 1];
-                    s_thr_s = Ss[K - 1];
-                }
-                for (int i = K + threadIdx.x; i < sortn; i += blockDim.x) { Pp[i] = ~0ull; Ss[i] = ~0ull; Ii[i] = ~0u; }
                 __syncthreads();
-                if (want) want = code_less(cp, cs, s_thr_p, s_thr_s);
+                if (s_ncand >= CAPC) {
+                    smem_bitonic(Pp, Ss, Ii, sortn);
+                    if (threadIdx.x == 0) {
+                        s_nbest = min(s_nbest + CAPC, K);
+                        s_ncand = 0;
+                        s_thr_p = Pp[K - 1];
+                        s_thr_s = Ss[K - 1];
+                    }
+                    for (int i = K + threadIdx.x; i < sortn; i += blockDim.x) { Pp[i] = ~0ull; Ss[i] = ~0ull; Ii[i] = ~0u; }
+                    __syncthreads();
+                    if (want) want = code_less(cp, cs, s_thr_p, s_thr_s);
+                }
             }
         }
     }
@@ -1468,8 +1487,10 @@ static gb_status run_topn(gb_agg *h, cudaStream_t st) {
         A.key_type1 = h->out_types[1];
     }
     A.K = K;
+    // the best K plus up to sortn - K candidates between sorts: a wide
+    // candidate buffer lets the threshold rise after few sorts
     int sortn = (int)next_pow2((u64)2 * K);
-    if (sortn < 64) sortn = 64;
+    if (sortn < 1024) sortn = 1024;
     size_t smem = (size_t)sortn * (8 + 8 + 4);
     static bool attr = false;
     if (!attr) {

@@ -94,25 +94,47 @@ __global__ void k_sample_hist(const u64 *skeys, const u32 *scnt, u64 scap, u32 *
 }
 
 // The smallest t >= floor_t admitting at most `cap` keys with sample count
-// >= t (HIST_BINS = none).
-__device__ __forceinline__ u32 count_threshold(const u32 *hist, u32 cap, u32 floor_t) {
-    u32 cum = 0, t = HIST_BINS;
-    for (int c = HIST_BINS - 1; c >= (int)floor_t; c--) {
-        if (cum + hist[c] > cap) break;
-        cum += hist[c];
-        t = c;
+// >= t (HIST_BINS = none), computed by a whole block: the histogram is
+// loaded into shared memory and suffix-summed by one warp's scan (one thread
+// walking 1024 bins in global memory took tens of microseconds).  `hs` holds
+// HIST_BINS u32; every thread gets the result.
+__device__ u32 block_count_threshold(const u32 *hist, u32 cap, u32 floor_t, u32 *hs) {
+    __shared__ u32 s_t;
+    const int lane = threadIdx.x & 31;
+    for (int c = threadIdx.x; c < HIST_BINS; c += blockDim.x) hs[c] = hist[c];
+    if (threadIdx.x == 0) s_t = HIST_BINS;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        // lane L sums the chunk [c1 - per, c1) of bins, chunks from the top
+        const int per = HIST_BINS / 32;
+        const int c1 = HIST_BINS - lane * per;
+        u32 sum = 0;
+        for (int c = c1 - 1; c >= c1 - per; c--) sum += hs[c];
+        u32 incl = sum;
+        for (int o = 1; o < 32; o <<= 1) {
+            const u32 y = __shfl_up_sync(FULL, incl, o);
+            if (lane >= o) incl += y;
+        }
+        u32 run = incl - sum;  // keys with count >= c1
+        for (int c = c1 - 1; c >= c1 - per; c--) {
+            run += hs[c];
+            hs[c] = run;  // keys with count >= c
+        }
     }
-    return t;
+    __syncthreads();
+    // hs is non-increasing: t = max(floor_t, the first c with hs[c] <= cap)
+    for (int c = threadIdx.x; c < HIST_BINS; c += blockDim.x)
+        if (c >= (int)floor_t && hs[c] <= cap && (c == (int)floor_t || hs[c - 1] > cap)) atomicMin(&s_t, (u32)c);
+    __syncthreads();
+    return s_t;
 }
 
 // Hot-set candidates: every sampled key whose count reaches the threshold
 // that admits at most NH keys (hstate[3] = candidates found).
 __global__ void k_hot_collect(const u64 *skeys, const u32 *scnt, u64 scap, const u32 *hist, u32 *hstate, int NH,
                               u64 *cand_key, u32 *cand_cnt) {
-    __shared__ u32 s_t;
-    if (threadIdx.x == 0) s_t = count_threshold(hist, (u32)NH, 2);
-    __syncthreads();
-    const u32 t = s_t;
+    __shared__ u32 hs[HIST_BINS];
+    const u32 t = block_count_threshold(hist, (u32)NH, 2, hs);
     if (t >= HIST_BINS) return;
     for (u64 s = blockIdx.x * (u64)blockDim.x + threadIdx.x; s < scap; s += (u64)gridDim.x * blockDim.x) {
         const u64 k = skeys[s];
@@ -127,78 +149,78 @@ __global__ void k_hot_collect(const u64 *skeys, const u32 *scnt, u64 scap, const
     }
 }
 
-// Rank the candidates (sampled count descending, key ascending: rank 0 is
-// the hottest key) and place them, in rank order, into the 2-way bucket
-// table: slot 2b + w of bucket b = hot_bucket(key).  A key whose bucket is
-// already full is not hot (its rows take the partitioned path), so the
-// hottest keys always get a slot and a lookup is one 16-byte shared load.
-// hot_list[rank] = key for every candidate; hstate[0] = candidates among the
-// NSUP hottest, hstate[1] = the others, hstate[2] = sampled rows of the
-// placed keys.  One block of 1024 threads, HOT_RANK_SMEM bytes of dynamic
-// shared memory; NH <= 4096, HB <= 4096.
-#define HOT_RANK_SMEM (4096 * 8 + 4096 * 4 + 4096)
+// Rank the candidates (sampled count descending, equal counts by candidate
+// slot: rank 0 is the hottest key) and place them into the 2-way bucket
+// table: each bucket b = hot_bucket(key) takes its two best-ranked keys
+// (slots 2b, 2b + 1), so the hottest keys always get a slot and a lookup is
+// one 16-byte shared load.  A key whose bucket holds two better-ranked keys
+// is not hot (its rows take the partitioned path).  hot_list[rank] = key for
+// every candidate; hstate[0] = candidates among the NSUP hottest, hstate[1]
+// = the others, hstate[2] = sampled rows of the placed keys.  One block of
+// 1024 threads, HOT_RANK_SMEM bytes of dynamic shared memory; NH <= 4096,
+// HB <= 4096.
+#define HOT_RANK_SMEM (4096 * 8 + 4096 * 4 * 2)
 __global__ void __launch_bounds__(1024) k_hot_rank(const u64 *cand_key, const u32 *cand_cnt, u32 *hstate, int NSUP,
                                                    int NH, int HB, u64 *hot_keys, uint16_t *hot_rank,
                                                    u64 *hot_list) {
     extern __shared__ u64 hrsm[];
-    u64 *sk = hrsm;                          // [4096]
-    u32 *scn = (u32 *)(sk + 4096);           // [4096]
-    uint8_t *fill = (uint8_t *)(scn + 4096); // [4096]
+    u64 *sv = hrsm;                // [4096] sort values: (~count << 32) | candidate slot
+    u32 *b1 = (u32 *)(sv + 4096);  // [4096] best rank of each bucket
+    u32 *b2 = b1 + 4096;           // [4096] second-best rank
+    __shared__ u32 s_rows;
     const u32 n = min(hstate[3], (u32)min(NH, 4096));
     u32 n2 = 1;
     while (n2 < n) n2 <<= 1;
-    for (u32 i = threadIdx.x; i < n2; i += blockDim.x) {
-        sk[i] = i < n ? cand_key[i] : ~0ull;
-        scn[i] = i < n ? cand_cnt[i] : 0u;
+    for (u32 i = threadIdx.x; i < n2; i += blockDim.x) sv[i] = i < n ? ((u64)(~cand_cnt[i]) << 32) | i : ~0ull;
+    for (int i = threadIdx.x; i < HB; i += blockDim.x) {
+        b1[i] = ~0u;
+        b2[i] = ~0u;
     }
-    for (int i = threadIdx.x; i < HB; i += blockDim.x) fill[i] = 0;
+    if (threadIdx.x == 0) s_rows = 0;
     __syncthreads();
-    // bitonic sort of n2 entries: "before" = larger count, then smaller key
+    // bitonic sort, ascending: larger count first, then the lower candidate slot
     for (u32 size = 2; size <= n2; size <<= 1) {
         for (u32 stride = size >> 1; stride > 0; stride >>= 1) {
             for (u32 i = threadIdx.x; i < n2 / 2; i += blockDim.x) {
                 const u32 lo = 2 * i - (i & (stride - 1));
                 const u32 hi = lo + stride;
-                const bool up = (lo & size) == 0;
-                const u32 ca = scn[lo], cb = scn[hi];
-                const u64 ka = sk[lo], kb = sk[hi];
-                const bool b_first = cb > ca || (cb == ca && kb < ka);
-                if (b_first == up) {
-                    scn[lo] = cb;
-                    scn[hi] = ca;
-                    sk[lo] = kb;
-                    sk[hi] = ka;
+                const u64 a = sv[lo], b = sv[hi];
+                if ((b < a) == ((lo & size) == 0)) {
+                    sv[lo] = b;
+                    sv[hi] = a;
                 }
             }
             __syncthreads();
         }
     }
-    for (u32 i = threadIdx.x; i < n; i += blockDim.x) hot_list[i] = sk[i];
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-        u32 placed_rows = 0;
-        for (u32 c0 = 0; c0 < n; c0 += 32) {
-            const u32 r = c0 + lane;
-            const u64 k = r < n ? sk[r] : 0ull;
-            const u32 b = r < n ? hot_bucket(p1_hash(k), HB) : 0xffffffffu;
-            const unsigned peers = __match_any_sync(FULL, b);
-            const u32 f = r < n ? fill[b] : 2u;
-            const u32 pos = __popc(peers & ((1u << lane) - 1u));
-            if (r < n && f + pos < 2) {
-                hot_keys[2 * b + f + pos] = k;
-                hot_rank[2 * b + f + pos] = (uint16_t)r;
-                placed_rows += scn[r];
-            }
-            __syncwarp();
-            if (r < n && lane == 31 - __clz(peers)) fill[b] = (uint8_t)min(2u, f + (u32)__popc(peers));
-            __syncwarp();
+    // each bucket keeps its two best ranks
+    for (u32 r = threadIdx.x; r < n; r += blockDim.x) {
+        const u64 k = cand_key[(u32)sv[r]];
+        hot_list[r] = k;
+        atomicMin(&b1[hot_bucket(p1_hash(k), HB)], r);
+    }
+    __syncthreads();
+    for (u32 r = threadIdx.x; r < n; r += blockDim.x) {
+        const u32 b = hot_bucket(p1_hash(hot_list[r]), HB);
+        if (b1[b] != r) atomicMin(&b2[b], r);
+    }
+    __syncthreads();
+    for (u32 r = threadIdx.x; r < n; r += blockDim.x) {
+        const u32 ci = (u32)sv[r];
+        const u64 k = cand_key[ci];
+        const u32 b = hot_bucket(p1_hash(k), HB);
+        const int way = b1[b] == r ? 0 : (b2[b] == r ? 1 : -1);
+        if (way >= 0) {
+            hot_keys[2 * b + way] = k;
+            hot_rank[2 * b + way] = (uint16_t)r;
+            atomicAdd(&s_rows, cand_cnt[ci]);
         }
-        placed_rows = __reduce_add_sync(FULL, placed_rows);
-        if (lane == 0) {
-            hstate[0] = min(n, (u32)NSUP);
-            hstate[1] = n - min(n, (u32)NSUP);
-            hstate[2] = placed_rows;
-        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        hstate[0] = min(n, (u32)NSUP);
+        hstate[1] = n - min(n, (u32)NSUP);
+        hstate[2] = s_rows;
     }
 }
 
@@ -325,7 +347,7 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
     const int HS = R.HS, W = P.words, NP = 1 << R.pbits, NH = R.nh, NPRIV = R.nsup, NWARM = R.nh - R.nsup;
     const int B = R.wcb;
     const int WM = W - 1;  // state words besides the count
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int warp = threadIdx.x >> 5;
     u64 *hk = rsm;                                        // [HS] hot keys
     u64 *pw = hk + HS;                                    // [P1_WARPS][NPRIV][WM] private words
     u64 *sw = pw + (size_t)P1_WARPS * NPRIV * WM;         // [NWARM][WM] shared words
@@ -740,10 +762,9 @@ __global__ void k_fill_u64(u64 *dst, u64 n, u64 value) {
 // One CTA per partition: a shared open-addressing table (u64 keys, u32
 // counts, W-1 state words).  Warps pre-combine duplicate keys, then fold with
 // native u32 count atomics and (rarely contended) word atomics; no barriers
-// in the main loop.  GW: every op is a DOUBLE SUM, whose shared-memory atomic
-// is a compare-and-swap loop; the state words then live in the partition's
-// slice of X.p2_words (L2-resident) and fold as fire-and-forget L2 reductions.
-template <int VV, int NOPS, bool GW>
+// in the main loop.  (Plans whose ops are all DOUBLE SUMs take
+// k_part_agg_sum, whose words fold in L2.)
+template <int VV, int NOPS>
 __global__ void __launch_bounds__(RADIX_BLOCK, 1)
     k_part_agg(const __grid_constant__ Plan P, const __grid_constant__ RadixPlan R, const RadixRef X,
                const TableRef T, const __grid_constant__ EmitArgs E, int SP) {
@@ -753,8 +774,8 @@ __global__ void __launch_bounds__(RADIX_BLOCK, 1)
     const int W = P.words, WM = W - 1;
     const int lane = threadIdx.x & 31;
     u64 *keys = rsm;  // [SP]
-    u64 *wd = GW ? X.p2_words + (size_t)blockIdx.x * SP * WM : keys + SP;  // [SP][WM]
-    u32 *cn = GW ? (u32 *)(keys + SP) : (u32 *)(wd + (size_t)SP * WM);   // [SP]
+    u64 *wd = keys + SP;                        // [SP][WM]
+    u32 *cn = (u32 *)(wd + (size_t)SP * WM);    // [SP]
     __shared__ u32 s_new;
     for (int i = threadIdx.x; i < SP; i += blockDim.x) {
         keys[i] = EMPTY_KEY;
@@ -865,7 +886,6 @@ __global__ void __launch_bounds__(RADIX_BLOCK, 1)
         }
         if (!done) global_fold_n<NOPS>(P, T, pk, cnt, v, &s_new);
     }
-    if (GW) __threadfence();  // the reductions reach L2 before the emit reads them
     __syncthreads();
     // emit: one output reservation per CTA
     u32 mine = 0;
@@ -879,7 +899,95 @@ __global__ void __launch_bounds__(RADIX_BLOCK, 1)
         }
         u64 w[GB_MAX_WORDS];
         w[0] = cn[s];
-        for (int q = 0; q < WM; q++) w[1 + q] = GW ? __ldcg(wd + (size_t)s * WM + q) : wd[(size_t)s * WM + q];
+        for (int q = 0; q < WM; q++) w[1 + q] = wd[(size_t)s * WM + q];
+        emit_group(P, E, o, keys[s], false, w);
+        o++;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_new) atomicAdd(&T.ctl->n_groups, s_new);
+}
+
+// P2 for plans whose ops are all DOUBLE SUMs of the one value column (the
+// COUNT / SUM / AVG(DOUBLE) shape): shared memory holds only keys and u32
+// counts; the sum words of this partition live in its slice of p2_words and
+// fold as fire-and-forget L2 reductions.  The CTA zeroes its slice first:
+// full-line stores allocate the lines in L2 without a DRAM read, so the
+// reductions that follow hit L2 (a slice left zero between runs instead made
+// every first reduction of a line miss).  One 128-bit load per tuple, no
+// per-op switch; the slot comes from bits 20.. of the P1 hash (the partition
+// took its top bits).
+template <int NOPS>
+__global__ void __launch_bounds__(RADIX_BLOCK, 1)
+    k_part_agg_sum(const __grid_constant__ Plan P, const __grid_constant__ RadixPlan R, const RadixRef X,
+                   const TableRef T, const __grid_constant__ EmitArgs E, int SP) {
+    extern __shared__ u64 rsm[];
+    const int WM = P.words - 1;
+    u64 *keys = rsm;               // [SP]
+    u32 *cn = (u32 *)(keys + SP);  // [SP]
+    u64 *wd = X.p2_words + (size_t)blockIdx.x * SP * WM;  // [SP][WM]
+    __shared__ u32 s_new;
+    for (int i = threadIdx.x; i < SP; i += blockDim.x) {
+        keys[i] = EMPTY_KEY;
+        cn[i] = 0;
+    }
+    for (int i = threadIdx.x; i < SP * WM; i += blockDim.x) wd[i] = 0ull;  // DOUBLE SUM identity
+    if (threadIdx.x == 0) s_new = 0;
+    const u32 p = blockIdx.x;
+    const u64 n = min((u64)X.cursor[(u64)p * CURSOR_PAD], (u64)X.part_cap[p]);
+    const ulonglong2 *base = (const ulonglong2 *)(X.part + X.part_off[p] * 2);
+    if (threadIdx.x < 32) {
+        const u64 bytes = n * 16, piece = 32768;
+        for (u64 o = (u64)threadIdx.x * piece; o < bytes; o += 32 * piece)
+            l2_prefetch((const char *)base + o, min(piece, bytes - o));
+    }
+    int wo[NOPS];
+#pragma unroll
+    for (int o = 0; o < NOPS; o++) wo[o] = P.ops[o].word - 1;
+    __syncthreads();
+    volatile u64 *vk = keys;
+    for (u64 i = threadIdx.x; i < n; i += blockDim.x) {
+        const ulonglong2 t = __ldcs(base + i);
+        const u64 pk = t.x;
+        if (pk == EMPTY_KEY) continue;  // a padding hole of the write-combining P1
+        u32 s = agg_slot(p1_hash(pk), SP);
+        bool done = false;
+        for (int q = 0; q < R.agg_probe; q++) {
+            u64 k = vk[s];
+            if (k == EMPTY_KEY) {
+                const u64 old = atomicCAS(&keys[s], EMPTY_KEY, pk);
+                k = (old == EMPTY_KEY) ? pk : old;
+            }
+            if (k == pk) {
+                atomicAdd(&cn[s], 1u);
+#pragma unroll
+                for (int o = 0; o < NOPS; o++)
+                    atomicAdd((double *)(wd + (size_t)s * WM + wo[o]), __longlong_as_double((i64)t.y));
+                done = true;
+                break;
+            }
+            s = (s + 1) & (u32)(SP - 1);
+        }
+        if (!done) {
+            u64 v[NOPS];
+#pragma unroll
+            for (int o = 0; o < NOPS; o++) v[o] = t.y;
+            global_fold_n<NOPS>(P, T, pk, 1, v, &s_new);
+        }
+    }
+    __threadfence();  // the reductions reach L2 before the emit reads them
+    __syncthreads();
+    u32 mine = 0;
+    for (int s = threadIdx.x; s < SP; s += blockDim.x) mine += keys[s] != EMPTY_KEY;
+    u64 o = block_out_base(T.ctl, mine);
+    for (int s = threadIdx.x; s < SP; s += blockDim.x) {
+        if (keys[s] == EMPTY_KEY) continue;
+        if (o >= E.out_cap) {
+            atomicOr(&T.ctl->err, (u32)ERR_OUT_OVERFLOW);
+            continue;
+        }
+        u64 w[GB_MAX_WORDS];
+        w[0] = cn[s];
+        for (int q = 0; q < WM; q++) w[1 + q] = __ldcg(wd + (size_t)s * WM + q);
         emit_group(P, E, o, keys[s], false, w);
         o++;
     }
@@ -1111,7 +1219,7 @@ static void p1_table(P1Fn *t) {
 }
 template <int VV, int NOPS>
 static void p2_table(P2Fn *t) {
-    t[VV * (RADIX_MAX_OPS + 1) + NOPS] = (P2Fn)k_part_agg<VV, NOPS, false>;
+    t[VV * (RADIX_MAX_OPS + 1) + NOPS] = (P2Fn)k_part_agg<VV, NOPS>;
 }
 
 template <int VV>
@@ -1133,8 +1241,8 @@ static gb_status radix_set_attributes() {
     fill_tables<3>(g_p1, g_p2);
     g_p1_spec_f = (P1Fn)k_partition_direct<OP_ADD_F>;
     g_p1_spec_i = (P1Fn)k_partition_direct<OP_ADD_I>;
-    g_p2_gw[1] = (P2Fn)k_part_agg<1, 1, true>;
-    g_p2_gw[2] = (P2Fn)k_part_agg<1, 2, true>;
+    g_p2_gw[1] = (P2Fn)k_part_agg_sum<1>;
+    g_p2_gw[2] = (P2Fn)k_part_agg_sum<2>;
     for (P1Fn f : {g_p1_spec_f, g_p1_spec_i})
         if (gb_status s = allow_max_smem(f)) return s;
     if (gb_status s = allow_max_smem(k_hot_rank)) return s;

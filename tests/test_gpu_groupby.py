@@ -163,6 +163,23 @@ def test_radix_partition_pass_with_and_without_precombine(vtype, pre):
     assert err <= REL_TOL
 
 
+@pytest.mark.parametrize("vtype", [DOUBLE, BIGINT])
+def test_radix_hot_table_full_key_range(vtype):
+    """The specialised partition pass on Zipf ranks mapped to keys across the
+    whole int64 range: INT64_MIN (also the hot table's empty marker) and
+    INT64_MAX among the hottest keys."""
+    rng = np.random.default_rng(21)
+    n = 1_500_000
+    ranks = np.minimum(rng.zipf(1.2, n), 300_000) - 1
+    vals = rng.integers(np.iinfo(np.int64).min, np.iinfo(np.int64).max, 300_000, dtype=np.int64)
+    vals[:4] = [np.iinfo(np.int64).min, np.iinfo(np.int64).max, -1, 0]
+    k = vals[ranks]
+    x = rng.normal(50, 10, n) if vtype == DOUBLE else rng.integers(-10**6, 10**6, n, dtype=np.int64)
+    aggs = [("count_star", -1), ("sum", 1)]
+    err, _, _ = check([BIGINT, vtype], [0], aggs, [k, x], est_groups=300_000, mode=RADIX, device=True)
+    assert err <= REL_TOL
+
+
 @pytest.mark.parametrize("mode", [HASH, RADIX])
 def test_zipf_topn_count_desc(mode):
     k, x = datagen.zipf(2_000_000, seed=1, n_values=400_000)
