@@ -298,6 +298,17 @@ __global__ void __launch_bounds__(512) k_topn(const __grid_constant__ TopnArgs A
     const u64 per = (n + gridDim.x - 1) / gridDim.x;
     const u64 lo = blockIdx.x * per, hi = min(n, lo + per);
     constexpr int TR = 8;  // rows per thread per pass: their loads are issued together
+    // Until K rows are held, rows no better than `bound` are skipped: bound
+    // is the K-th best of the warps' best rows of the first pass (K distinct
+    // rows are at least that good, so every row of the final top K is too).
+    __shared__ u64 s_bp, s_bs;
+    __shared__ u64 s_wp[32], s_ws[32];
+    if (threadIdx.x == 0) {
+        s_bp = ~0ull;
+        s_bs = ~0ull;
+    }
+    __syncthreads();
+    bool first = true;
     for (u64 base = lo; base < hi; base += (u64)blockDim.x * TR) {
         u64 cpv[TR], csv[TR];
         u32 rowv[TR];
@@ -314,18 +325,65 @@ __global__ void __launch_bounds__(512) k_topn(const __grid_constant__ TopnArgs A
                 rowv[j] = ids ? ids[it] : (u32)it;
                 if (rowv[j] != ~0u) {
                     topn_code(A, rowv[j], cpv[j], csv[j]);
-                    wantv[j] = s_nbest < K || code_less(cpv[j], csv[j], s_thr_p, s_thr_s);
+                    wantv[j] = s_nbest < K ? !code_less(s_bp, s_bs, cpv[j], csv[j])
+                                           : code_less(cpv[j], csv[j], s_thr_p, s_thr_s);
                 }
             }
             any |= wantv[j];
         }
+        const int nwarps = blockDim.x >> 5;
+        if (first && K <= nwarps) {
+            first = false;
+            u64 bp = ~0ull, bs = ~0ull;
+#pragma unroll
+            for (int j = 0; j < TR; j++)
+                if (code_less(cpv[j], csv[j], bp, bs)) {
+                    bp = cpv[j];
+                    bs = csv[j];
+                }
+            for (int o = 16; o > 0; o >>= 1) {
+                const u64 op = __shfl_xor_sync(0xffffffffu, bp, o), os = __shfl_xor_sync(0xffffffffu, bs, o);
+                if (code_less(op, os, bp, bs)) {
+                    bp = op;
+                    bs = os;
+                }
+            }
+            if ((threadIdx.x & 31) == 0) {
+                s_wp[threadIdx.x >> 5] = bp;
+                s_ws[threadIdx.x >> 5] = bs;
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                // insertion sort of the warps' best rows; the K-th is the bound
+                for (int a = 1; a < nwarps; a++)
+                    for (int b = a; b > 0 && code_less(s_wp[b], s_ws[b], s_wp[b - 1], s_ws[b - 1]); b--) {
+                        const u64 tp = s_wp[b], ts = s_ws[b];
+                        s_wp[b] = s_wp[b - 1];
+                        s_ws[b] = s_ws[b - 1];
+                        s_wp[b - 1] = tp;
+                        s_ws[b - 1] = ts;
+                    }
+                s_bp = s_wp[K - 1];
+                s_bs = s_ws[K - 1];
+            }
+            __syncthreads();
+            const u64 qp = s_bp, qs = s_bs;
+            any = false;
+#pragma unroll
+            for (int j = 0; j < TR; j++) {
+                wantv[j] = wantv[j] && (s_nbest >= K || !code_less(qp, qs, cpv[j], csv[j]));
+                any |= wantv[j];
+            }
+        }
+        first = false;
         // once the threshold has settled, no row of a pass usually beats it:
         // one barrier for TR * blockDim rows
         if (!__syncthreads_or(any)) continue;
         for (int j = 0; j < TR; j++) {
             const u64 cp = cpv[j], cs = csv[j];
             const u32 row = rowv[j];
-            bool want = wantv[j] && (s_nbest < K || code_less(cp, cs, s_thr_p, s_thr_s));
+            bool want = wantv[j] && (s_nbest < K ? !code_less(s_bp, s_bs, cp, cs)
+                                                 : code_less(cp, cs, s_thr_p, s_thr_s));
             while (__syncthreads_or(want)) {
                 if (want) {
                     int pos = atomicAdd(&s_ncand, 1);
@@ -496,6 +554,7 @@ struct gb_agg {
     int mode_option = 0;   // 0 = auto, 1 = force hash, 2 = force radix
     RadixPlan rplan{};
     bool r_ready = false;
+    bool pending_reset = false;  // gb_agg_reset's device work waits for the next ingest / finalize
     DevBuf r_skeys, r_scnt, r_hist, r_hot_keys, r_hot_part, r_cursor, r_part, r_part2, r_ovf;
     DevBuf r_off, r_cap, r_off2, r_cap2;    // per-partition region start / capacity (device)
     DevBuf r_hot_idx, r_hot_list, r_hstate, r_cand;
@@ -626,6 +685,19 @@ static gb_status init_table(gb_agg *h, DevBuf &buf, u64 cap, cudaStream_t st) {
     }
     h->launches++;
     GB_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+static gb_status dist_clear(gb_agg *h, cudaStream_t st);
+
+// The device part of gb_agg_reset, on the stream of the call that follows it.
+static gb_status apply_reset(gb_agg *h, cudaStream_t st) {
+    if (!h->pending_reset) return GB_OK;
+    gb_status s = init_table(h, h->table, h->cap, st);
+    if (s) return s;
+    if ((s = dist_clear(h, st))) return s;
+    GB_CUDA(cudaMemsetAsync(h->ctl_buf.p, 0, sizeof(Ctl), st));
+    h->pending_reset = false;
     return GB_OK;
 }
 
@@ -885,6 +957,26 @@ static RadixRef radix_ref(gb_agg *h) {
     return X;
 }
 
+// The per-CTA hot slices (identity-initialised) and the overflow list of a
+// run whose partition layout is in place.
+static gb_status radix_begin_slices(gb_agg *h, cudaStream_t st) {
+    const RadixPlan &R = h->rplan;
+    const int W = h->plan.words;
+    const int TV = 1 + R.V;
+    gb_status s;
+    h->r_grid = sm_count();
+    if ((s = h->r_hot_part.ensure((size_t)h->r_grid * R.nh * W * 8))) return s;
+    if ((s = radix_fill_identity((u64 *)h->r_hot_part.p, (u64)h->r_grid * R.nh * W, W, h->plan, st))) return s;
+    h->launches++;
+    u32 ovf_cap = (1u << 21) + (u32)radix_inflight_rows(R, h->r_grid) + 4096;
+    if (h->r_ovf_cap < ovf_cap) {
+        if ((s = h->r_ovf.ensure((size_t)ovf_cap * (TV + 1) * 8))) return s;
+        h->r_ovf_cap = ovf_cap;
+    }
+    h->r_ready = true;
+    return GB_OK;
+}
+
 static gb_status radix_begin(gb_agg *h, u64 n, cudaStream_t st) {
     const RadixPlan &R = h->rplan;
     const u64 np = 1ull << R.pbits;
@@ -915,6 +1007,13 @@ static gb_status radix_begin(gb_agg *h, u64 n, cudaStream_t st) {
                                      (uint16_t *)h->r_hot_idx.p, (u64 *)h->r_hot_list.p, st, &h->launches)))
             return s;
     }
+    if (h->h_capv.size() == np && h->h_off.size() == np + 1) {
+        // a re-execution keeps the partition layout of the earlier runs (the
+        // regions they grew to stay large; a region that overflows grows
+        // again), so the sample's hot fraction need not come back to the host
+        GB_CUDA(cudaMemsetAsync(h->r_cursor.p, 0, (size_t)np * CURSOR_PAD * 4, st));
+        return radix_begin_slices(h, st);
+    }
     u32 hst[4] = {0, 0, 0, 0};
     GB_CUDA(cudaMemcpyAsync(hst, h->r_hstate.p, 16, cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
@@ -925,13 +1024,7 @@ static gb_status radix_begin(gb_agg *h, u64 n, cudaStream_t st) {
     u64 cap_p = (u64)(tail / (double)np * 1.5) + 2048;
     cap_p = (cap_p + 31) / 32 * 32;
     h->r_cap_p = cap_p;
-    // a re-execution of the handle keeps the per-partition capacities its
-    // earlier runs grew to (skewed partitions stay large), so the regions
-    // are not regrown and moved on every run
-    std::vector<u32> prev;
-    if (h->h_capv.size() == np) prev.swap(h->h_capv);
     h->h_capv.assign(np, (u32)cap_p);
-    for (u64 p = 0; p < prev.size(); p++) h->h_capv[p] = std::max<u32>(h->h_capv[p], prev[p]);
     h->h_off.assign(np + 1, 0);
     for (u64 p = 0; p < np; p++) h->h_off[p + 1] = h->h_off[p] + h->h_capv[p];
     if ((s = h->r_part.ensure((size_t)h->h_off[np] * TV * 8))) return s;
@@ -940,17 +1033,7 @@ static gb_status radix_begin(gb_agg *h, u64 n, cudaStream_t st) {
     GB_CUDA(cudaMemcpyAsync(h->r_cap.p, h->h_capv.data(), np * 4, cudaMemcpyHostToDevice, st));
     if ((s = h->r_cursor.ensure((size_t)np * CURSOR_PAD * 4))) return s;
     GB_CUDA(cudaMemsetAsync(h->r_cursor.p, 0, (size_t)np * CURSOR_PAD * 4, st));
-    h->r_grid = sm_count();
-    if ((s = h->r_hot_part.ensure((size_t)h->r_grid * R.nh * W * 8))) return s;
-    if ((s = radix_fill_identity((u64 *)h->r_hot_part.p, (u64)h->r_grid * R.nh * W, W, h->plan, st))) return s;
-    h->launches++;
-    u32 ovf_cap = (1u << 21) + (u32)radix_inflight_rows(R, h->r_grid) + 4096;
-    if (h->r_ovf_cap < ovf_cap) {
-        if ((s = h->r_ovf.ensure((size_t)ovf_cap * (TV + 1) * 8))) return s;
-        h->r_ovf_cap = ovf_cap;
-    }
-    h->r_ready = true;
-    return GB_OK;
+    return radix_begin_slices(h, st);
 }
 
 // Grow the regions of the partitions that overflowed (each to what it
@@ -1671,6 +1754,7 @@ gb_status gb_agg_ingest(gb_agg *h, const gb_col *cols, uint64_t nrows, int32_t m
     }
     if (nrows == 0) return GB_OK;
     cudaStream_t st = (cudaStream_t)stream;
+    if (gb_status s0 = apply_reset(h, st)) return s0;
     const int nc = (int)h->col_types.size();  // spec columns (the plan may add a hidden id column)
     for (int c = 0; c < nc; c++) {
         if (!cols[c].data && !(h->col_types[c] == GB_T_VARCHAR && cols[c].offsets)) {
@@ -1804,6 +1888,7 @@ gb_status gb_agg_finalize(gb_agg *h, void *stream) {
     if (h->finalized) return GB_OK;
     cudaStream_t st = (cudaStream_t)stream;
     gb_status s;
+    if ((s = apply_reset(h, st))) return s;
     Ctl *dctl = (Ctl *)h->ctl_buf.p;
     if (h->mode == 1) {
         if ((s = radix_emit(h, st))) return s;
@@ -1922,11 +2007,10 @@ gb_status gb_agg_result_device(gb_agg *h, gb_result *out) {
 
 gb_status gb_agg_reset(gb_agg *h) {
     if (!h) return GB_ERR_INVALID;
-    gb_status s = init_table(h, h->table, h->cap, 0);
-    if (s) return s;
-    if ((s = dist_clear(h, 0))) return s;
-    GB_CUDA(cudaMemset(h->ctl_buf.p, 0, sizeof(Ctl)));
-    GB_CUDA(cudaStreamSynchronize(0));  // before ingests on streams that do not synchronise with it
+    // the device work of the rewind (table, COUNT(DISTINCT) sets, control
+    // words) runs on the stream of the handle's next ingest or finalize, so
+    // a reset neither blocks the host nor races work on another stream
+    h->pending_reset = true;
     h->n_groups = 0;
     h->sd_cap = 0;  // the string dictionary is rebuilt by the next ingest
     h->r_ready = false;
@@ -2169,6 +2253,7 @@ gb_status gb_agg_ingest_prefiltered_ids(gb_agg *h, const gb_col *cols, uint64_t 
     }
     if (nrows == 0) return GB_OK;
     cudaStream_t st = (cudaStream_t)stream;
+    if (gb_status s0 = apply_reset(h, st)) return s0;
     const int nc = (int)h->col_types.size();
     for (int c = 0; c < nc; c++) {
         h->plan.cols[c].data = cols[c].data;
