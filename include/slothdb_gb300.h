@@ -70,11 +70,23 @@ typedef enum gb_agg_kind {
 
 #define GB_MAX_DISTINCT 2
 
-/* Comparison of a SimplePredicate (src/execution/physical_planner.cpp:110-135). */
+/* Comparison of a SimplePredicate (src/execution/physical_planner.cpp:110-135):
+ * the six numeric compares; INTEGER/BIGINT/SMALLINT `col IN (set)`
+ * (int_in_form); VARCHAR `col = 'lit'` / `col <> 'lit'` (str_form); VARCHAR
+ * `col LIKE '%needle%'` / `NOT LIKE` (like_contains / like_negated:
+ * case-sensitive byte substring, an empty needle matches every non-NULL
+ * value).  A NULL row never passes. */
 typedef enum gb_cmp {
     GB_CMP_EQ = 0, GB_CMP_NE = 1, GB_CMP_LT = 2,
-    GB_CMP_LE = 3, GB_CMP_GT = 4, GB_CMP_GE = 5
+    GB_CMP_LE = 3, GB_CMP_GT = 4, GB_CMP_GE = 5,
+    GB_CMP_IN = 6,         /* data: int64_t[n] set members (any order, duplicates allowed) */
+    GB_CMP_STR_EQ = 7,     /* data: n literal bytes */
+    GB_CMP_STR_NE = 8,
+    GB_CMP_LIKE = 9,       /* data: n needle bytes of LIKE '%needle%' */
+    GB_CMP_NOT_LIKE = 10
 } gb_cmp;
+#define GB_MAX_IN_SET 65536       /* members of one IN set */
+#define GB_MAX_STR_LITERAL 4096   /* bytes of one string literal */
 
 typedef struct gb_agg_desc {
     int32_t kind;   /* gb_agg_kind */
@@ -83,12 +95,17 @@ typedef struct gb_agg_desc {
 
 /* col OP constant.  Integer columns compare in int64 (the reference widens
  * to int64 before comparing, physical_planner.cpp:466-479, 693-716); DOUBLE
- * columns compare against d_const. */
+ * columns compare against d_const.  IN and the VARCHAR forms read their
+ * literal from `data` (host memory, n elements / bytes): the library keeps
+ * its own copy, so the caller's buffer is needed only during the call that
+ * takes the filter. */
 typedef struct gb_filter {
     int32_t col;
     int32_t op;      /* gb_cmp */
     int64_t i_const;
     double d_const;
+    const void *data;  /* GB_CMP_IN / STR / LIKE literal, else NULL */
+    uint64_t n;
 } gb_filter;
 
 #define GB_SPEC_COL_NULLABLE_BITS 0  /* see gb_agg_spec.nullable_mask */

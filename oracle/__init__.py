@@ -25,7 +25,8 @@ COUNT_STAR, COUNT, SUM, AVG, MIN, MAX, COUNT_DISTINCT = 0, 1, 2, 3, 4, 5, 6
 NP_TYPES = {SMALLINT: np.int16, INTEGER: np.int32, BIGINT: np.int64, DOUBLE: np.float64}
 AGG_NAMES = {"count_star": COUNT_STAR, "count": COUNT, "sum": SUM, "avg": AVG, "min": MIN, "max": MAX,
              "count_distinct": COUNT_DISTINCT}
-CMP_NAMES = {"==": 0, "=": 0, "!=": 1, "<>": 1, "<": 2, "<=": 3, ">": 4, ">=": 5}
+CMP_NAMES = {"==": 0, "=": 0, "!=": 1, "<>": 1, "<": 2, "<=": 3, ">": 4, ">=": 5, "in": 6, "like": 9,
+             "not like": 10}
 
 _lib = None
 
@@ -50,6 +51,10 @@ def load():
     lib.or_filter.argtypes = [C.c_int64, C.c_int32, P, P, C.c_int32, C.c_int64, C.c_double, P]
     lib.or_rle_decode.restype = C.c_int64
     lib.or_rle_decode.argtypes = [P, C.c_int64, C.c_int32, P, C.c_int64]
+    lib.or_filter_in.restype = None
+    lib.or_filter_in.argtypes = [C.c_int64, C.c_int32, P, P, P, C.c_int64, P]
+    lib.or_filter_str.restype = None
+    lib.or_filter_str.argtypes = [C.c_int64, P, P, P, C.c_int32, P, C.c_int64, P]
     lib.or_snappy_decompress.restype = C.c_int64
     lib.or_snappy_decompress.argtypes = [P, C.c_int64, P, C.c_int64]
     _lib = lib
@@ -77,10 +82,24 @@ def filter_mask(n, col_types, cols, filters, nulls=None):
     for col, op, const in filters:
         opc = CMP_NAMES[op] if isinstance(op, str) else int(op)
         t = col_types[col]
-        a = np.ascontiguousarray(cols[col], dtype=NP_TYPES[t])
         nul = None
         if nulls is not None and nulls[col] is not None:
             nul = np.ascontiguousarray(nulls[col], dtype=np.uint8)
+        if t == VARCHAR:
+            # = / <> / LIKE '%x%' / NOT LIKE on the bytes (const: bytes)
+            if opc in (0, 1):
+                opc += 7
+            offs = np.ascontiguousarray(cols[col][0], dtype=np.int64)
+            data = np.ascontiguousarray(cols[col][1], dtype=np.uint8)
+            lit = np.frombuffer(bytes(const), dtype=np.uint8) if len(const) else np.zeros(1, np.uint8)
+            lib.or_filter_str(n, _p(offs), _p(data), _p(nul), opc, _p(lit), len(const), _p(keep))
+            continue
+        a = np.ascontiguousarray(cols[col], dtype=NP_TYPES[t])
+        if opc == 6:
+            members = np.ascontiguousarray(np.asarray(list(const), dtype=np.int64)) if len(const) else np.zeros(1,
+                                                                                                          np.int64)
+            lib.or_filter_in(n, t, _p(a), _p(nul), _p(members), len(const), _p(keep))
+            continue
         if t == DOUBLE:
             lib.or_filter(n, t, _p(a), _p(nul), opc, 0, float(const), _p(keep))
         else:

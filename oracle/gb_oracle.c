@@ -861,4 +861,50 @@ int64_t or_snappy_decompress(const uint8_t *src, int64_t n, uint8_t *dst, int64_
     return out == (int64_t)want ? out : -1;
 }
 
-int32_t or_version(void) { return 1; }
+/* INTEGER/BIGINT/SMALLINT `col IN (set)`: keep[r] &= the row is not NULL and
+ * its int64 value is a member (SimplePredicate::int_in_form,
+ * physical_planner.cpp:126-133, 409-418: sorted set, binary search). */
+static int or_cmp_i64(const void *a, const void *b) {
+    int64_t x = *(const int64_t *)a, y = *(const int64_t *)b;
+    return x < y ? -1 : (x > y);
+}
+
+void or_filter_in(int64_t n, int32_t type, const void *data, const uint8_t *nul, const int64_t *set, int64_t nset,
+                  uint8_t *keep) {
+    int64_t *s = (int64_t *)malloc((size_t)(nset > 0 ? nset : 1) * 8);
+    if (nset > 0) memcpy(s, set, (size_t)nset * 8);
+    qsort(s, (size_t)nset, 8, or_cmp_i64);
+    for (int64_t r = 0; r < n; r++) {
+        if (!keep[r]) continue;
+        if (nul && nul[r]) { keep[r] = 0; continue; }
+        int64_t v = read_int(type, data, r);
+        keep[r] = nset > 0 && bsearch(&v, s, (size_t)nset, 8, or_cmp_i64) != NULL;
+    }
+    free(s);
+}
+
+/* VARCHAR predicates (SimplePredicate::str_form / like_contains,
+ * physical_planner.cpp:419-462): op 7 `= lit`, 8 `<> lit` (length and bytes
+ * equal), 9 `LIKE '%lit%'`, 10 `NOT LIKE '%lit%'` (byte substring, an empty
+ * needle matches).  A NULL row never passes. */
+void or_filter_str(int64_t n, const int64_t *offs, const uint8_t *bytes, const uint8_t *nul, int32_t op,
+                   const uint8_t *lit, int64_t len, uint8_t *keep) {
+    for (int64_t r = 0; r < n; r++) {
+        if (!keep[r]) continue;
+        if (nul && nul[r]) { keep[r] = 0; continue; }
+        const uint8_t *p = bytes + offs[r];
+        const int64_t sl = offs[r + 1] - offs[r];
+        int match;
+        if (op == 7 || op == 8) {
+            int eq = sl == len && (len == 0 || memcmp(p, lit, (size_t)len) == 0);
+            match = op == 7 ? eq : !eq;
+        } else {
+            int found = len == 0;
+            for (int64_t i = 0; !found && i + len <= sl; i++) found = memcmp(p + i, lit, (size_t)len) == 0;
+            match = op == 9 ? found : !found;
+        }
+        keep[r] = (uint8_t)match;
+    }
+}
+
+int32_t or_version(void) { return 2; }

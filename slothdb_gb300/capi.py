@@ -23,12 +23,14 @@ STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "OOM", 3: "UNSUPPORTED", 4: "TIMEOUT",
 SMALLINT, INTEGER, BIGINT, DOUBLE, VARCHAR = 1, 2, 3, 4, 5
 COUNT_STAR, COUNT, SUM, AVG, MIN, MAX, COUNT_DISTINCT = 0, 1, 2, 3, 4, 5, 6
 EQ, NE, LT, LE, GT, GE = 0, 1, 2, 3, 4, 5
+IN, STR_EQ, STR_NE, LIKE, NOT_LIKE = 6, 7, 8, 9, 10
 MEM_HOST, MEM_DEVICE = 0, 1
 
 NP_TYPES = {SMALLINT: np.int16, INTEGER: np.int32, BIGINT: np.int64, DOUBLE: np.float64}
 AGG_NAMES = {"count_star": COUNT_STAR, "count": COUNT, "sum": SUM, "avg": AVG, "min": MIN, "max": MAX,
              "count_distinct": COUNT_DISTINCT}
-CMP_NAMES = {"==": EQ, "=": EQ, "!=": NE, "<>": NE, "<": LT, "<=": LE, ">": GT, ">=": GE}
+CMP_NAMES = {"==": EQ, "=": EQ, "!=": NE, "<>": NE, "<": LT, "<=": LE, ">": GT, ">=": GE, "in": IN, "like": LIKE,
+             "not like": NOT_LIKE}
 
 
 class GbError(RuntimeError):
@@ -42,7 +44,34 @@ class AggDesc(C.Structure):
 
 
 class Filter(C.Structure):
-    _fields_ = [("col", C.c_int32), ("op", C.c_int32), ("i_const", C.c_int64), ("d_const", C.c_double)]
+    _fields_ = [("col", C.c_int32), ("op", C.c_int32), ("i_const", C.c_int64), ("d_const", C.c_double),
+                ("data", C.c_void_p), ("n", C.c_uint64)]
+
+
+def _filters(filters, types):
+    """gb_filter array for (col, op, const) triples; returns (array, buffers
+    it points into).  op: '=', '!=', '<', '<=', '>', '>=' (a VARCHAR column
+    compares its bytes with const for '=' / '!='), 'in' (const: integers),
+    'like' / 'not like' (const: the needle of LIKE '%needle%')."""
+    fl = (Filter * max(1, len(filters)))()
+    keep = []
+    for i, (col, op, const) in enumerate(filters):
+        opc = CMP_NAMES[op] if isinstance(op, str) else int(op)
+        if opc == IN:
+            a = np.ascontiguousarray(np.asarray(list(const), dtype=np.int64))
+            keep.append(a)
+            fl[i] = Filter(col, opc, 0, 0.0, a.ctypes.data if len(a) else None, len(a))
+        elif types[col] == VARCHAR:
+            if opc in (EQ, NE):
+                opc += STR_EQ - EQ
+            b = (C.c_char * max(1, len(const))).from_buffer_copy(bytes(const) or b"\0")
+            keep.append(b)
+            fl[i] = Filter(col, opc, 0, 0.0, C.addressof(b), len(const))
+        elif types[col] == DOUBLE:
+            fl[i] = Filter(col, opc, 0, float(const))
+        else:
+            fl[i] = Filter(col, opc, int(const), 0.0)
+    return fl, keep
 
 
 class AggSpec(C.Structure):
@@ -195,19 +224,13 @@ def _make_spec(col_types, group_cols, aggs, filters=(), nullable=(), est_groups=
     ct = (C.c_int32 * len(col_types))(*col_types)
     gc = (C.c_int32 * len(group_cols))(*group_cols)
     ag = (AggDesc * len(aggs))(*[AggDesc(k, c) for k, c in aggs])
-    fl = (Filter * max(1, len(filters)))()
-    for i, (col, op, const) in enumerate(filters):
-        opc = CMP_NAMES[op] if isinstance(op, str) else int(op)
-        if col_types[col] == DOUBLE:
-            fl[i] = Filter(col, opc, 0, float(const))
-        else:
-            fl[i] = Filter(col, opc, int(const), 0.0)
+    fl, fkeep = _filters(filters, col_types)
     mask = 0
     for c in nullable:
         mask |= 1 << int(c)
     spec = AggSpec(len(col_types), ct, len(group_cols), gc, len(aggs), ag,
                    len(filters), fl if filters else None, mask, int(est_groups))
-    return spec, (ct, gc, ag, fl)
+    return spec, (ct, gc, ag, fl, fkeep)
 
 
 def _read_result(r):
@@ -333,13 +356,7 @@ class GroupBy:
 
     def set_filters(self, filters):
         """Replace the WHERE predicates (after create or reset)."""
-        fl = (Filter * max(1, len(filters)))()
-        for i, (col, op, const) in enumerate(filters):
-            opc = CMP_NAMES[op] if isinstance(op, str) else int(op)
-            if self.col_types[col] == DOUBLE:
-                fl[i] = Filter(col, opc, 0, float(const))
-            else:
-                fl[i] = Filter(col, opc, int(const), 0.0)
+        fl, _keep = _filters(filters, self.col_types)
         check(self.lib.gb_agg_set_filters(self.h, fl, len(filters)))
 
     def mode(self):
@@ -564,13 +581,7 @@ class ParquetFile:
         out the (col, op, const) filters (col = spec column, read from file
         column col_map[col])."""
         types = [t for _, t in self.columns()]
-        fl = (Filter * max(1, len(filters)))()
-        for i, (col, op, const) in enumerate(filters):
-            opc = CMP_NAMES[op] if isinstance(op, str) else int(op)
-            if types[col_map[col]] == DOUBLE:
-                fl[i] = Filter(col, opc, 0, float(const))
-            else:
-                fl[i] = Filter(col, opc, int(const), 0.0)
+        fl, _keep = _filters(filters, [types[c] for c in col_map])
         cm = (C.c_int32 * len(col_map))(*col_map)
         m = C.c_int32()
         check(self.lib.gb_pq_row_group_might_match(self.h, int(rg), cm, len(col_map), C.cast(fl, C.c_void_p),

@@ -514,6 +514,8 @@ struct gb_agg {
     std::vector<int32_t> group_cols;
     std::vector<gb_agg_desc> aggs;
     std::vector<gb_filter> filters;
+    std::vector<uint8_t> filt_host;  // the filters' literals (host copy they point at)
+    DevBuf filt_dev;                 // ... and their device copy
     uint64_t nullable_mask = 0;
     uint64_t est_groups = 0;
 
@@ -1325,20 +1327,68 @@ static gb_status strdict_emit(gb_agg *h, const long long *ids, u64 n, cudaStream
 static gb_status compile_filters(gb_agg *h) {
     Plan &P = h->plan;
     const int nc = (int)h->col_types.size();
+    // literals (IN sets sorted and deduplicated, string bytes) are copied into
+    // the handle: a host copy the filters point at, and one device buffer
+    std::vector<uint8_t> lit;
+    std::vector<size_t> at(h->filters.size(), 0);
+    std::vector<u64> cnt(h->filters.size(), 0);
     for (size_t i = 0; i < h->filters.size(); i++) {
         const gb_filter &f = h->filters[i];
-        if (f.col < 0 || f.col >= nc || f.op < 0 || f.op > 5 || h->col_types[f.col] == GB_T_VARCHAR) {
-            set_error("filter %zu invalid (column, operator or VARCHAR predicate)", i);
-            return GB_ERR_INVALID;
-        }
         if (i >= GB_MAX_FILTERS) {
             set_error("too many filters (max %d)", GB_MAX_FILTERS);
             return GB_ERR_UNSUPPORTED;
+        }
+        const int t = (f.col >= 0 && f.col < nc) ? h->col_types[f.col] : -1;
+        const bool is_int = t == GB_T_SMALLINT || t == GB_T_INTEGER || t == GB_T_BIGINT;
+        const bool num_op = f.op >= GB_CMP_EQ && f.op <= GB_CMP_GE;
+        const bool str_op = f.op >= GB_CMP_STR_EQ && f.op <= GB_CMP_NOT_LIKE;
+        if (t < 0 || (num_op && t == GB_T_VARCHAR) || (f.op == GB_CMP_IN && !is_int) || (str_op && t != GB_T_VARCHAR) ||
+            (!num_op && !str_op && f.op != GB_CMP_IN)) {
+            set_error("filter %zu invalid (column %d, operator %d)", i, f.col, f.op);
+            return GB_ERR_INVALID;
+        }
+        if (num_op) continue;
+        const u64 lim = f.op == GB_CMP_IN ? GB_MAX_IN_SET : GB_MAX_STR_LITERAL;
+        if (f.n > lim || (f.n && !f.data)) {
+            set_error("filter %zu: literal of %llu elements (max %llu) or without data", i, (unsigned long long)f.n,
+                      (unsigned long long)lim);
+            return f.n > lim ? GB_ERR_UNSUPPORTED : GB_ERR_INVALID;
+        }
+        while (lit.size() % 8) lit.push_back(0);
+        at[i] = lit.size();
+        if (f.op == GB_CMP_IN) {
+            std::vector<int64_t> v((const int64_t *)f.data, (const int64_t *)f.data + f.n);
+            std::sort(v.begin(), v.end());
+            v.erase(std::unique(v.begin(), v.end()), v.end());
+            cnt[i] = v.size();
+            lit.insert(lit.end(), (const uint8_t *)v.data(), (const uint8_t *)(v.data() + v.size()));
+        } else {
+            cnt[i] = f.n;
+            lit.insert(lit.end(), (const uint8_t *)f.data, (const uint8_t *)f.data + f.n);
+        }
+    }
+    lit.resize(lit.size() + 8, 0);
+    if (lit.size() > 8) {
+        if (gb_status s = h->filt_dev.ensure(lit.size())) return s;
+        GB_CUDA(cudaMemcpy(h->filt_dev.p, lit.data(), lit.size(), cudaMemcpyHostToDevice));
+    }
+    h->filt_host.swap(lit);
+    for (size_t i = 0; i < h->filters.size(); i++) {
+        gb_filter &f = h->filters[i];
+        const bool has_lit = f.op >= GB_CMP_IN;
+        if (has_lit) {  // the handle's own copy from now on
+            f.data = h->filt_host.data() + at[i];
+            f.n = cnt[i];
+        } else {
+            f.data = nullptr;
+            f.n = 0;
         }
         P.filters[i].col = f.col;
         P.filters[i].op = f.op;
         P.filters[i].ic = f.i_const;
         P.filters[i].dc = f.d_const;
+        P.filters[i].ptr = has_lit ? (const uint8_t *)h->filt_dev.p + at[i] : nullptr;
+        P.filters[i].n = has_lit ? cnt[i] : 0;
     }
     P.n_filters = (int)h->filters.size();
     return GB_OK;
@@ -1863,6 +1913,12 @@ gb_status gb_agg_ingest(gb_agg *h, const gb_col *cols, uint64_t nrows, int32_t m
             h->plan.cols[c].data = h->stage[b][c].p;
             h->plan.cols[c].valid = cols[c].validity ? (const uint64_t *)h->stage[b][nc + c].p : nullptr;
             h->plan.cols[c].offsets = nullptr;
+            if (h->col_types[c] == GB_T_VARCHAR) {
+                // the staged offsets are the caller's (absolute): the bytes
+                // pointer is shifted so that data + offsets[r] is row r's string
+                h->plan.cols[c].offsets = (const int64_t *)h->stage[b][2 * nc + c].p;
+                h->plan.cols[c].data = (const uint8_t *)h->stage[b][c].p - cols[c].offsets[r0];
+            }
         }
         if (h->str_col >= 0) {
             const int c = h->str_col;
@@ -2043,7 +2099,8 @@ void gb_agg_destroy(gb_agg *h) {
     h->host_str_bytes.release();
     for (DevBuf *b : {&h->r_skeys, &h->r_scnt, &h->r_hist, &h->r_hot_keys, &h->r_hot_part, &h->r_cursor, &h->r_part,
                       &h->r_part2, &h->r_ovf, &h->r_off, &h->r_cap, &h->r_off2, &h->r_cap2, &h->r_hot_idx,
-                      &h->r_hot_list, &h->r_hstate, &h->r_cand, &h->r_p2w, &h->dsets, &h->dsets_old, &h->null_sets,
+                      &h->r_hot_list, &h->r_hstate, &h->r_cand, &h->r_p2w, &h->filt_dev, &h->dsets, &h->dsets_old,
+                      &h->null_sets,
                       &h->null_sets_old, &h->dmeta})
         b->release();
     h->topn_ids_a.release();
@@ -2230,6 +2287,7 @@ gb_status gb_agg_view(gb_agg *h, AggView *v) {
     v->col_types = h->col_types.data();
     v->n_filters = h->plan.n_filters;
     for (int i = 0; i < h->plan.n_filters; i++) v->filters[i] = h->plan.filters[i];
+    v->nullable_mask = h->nullable_mask;
     return GB_OK;
 }
 
@@ -2256,8 +2314,12 @@ gb_status gb_agg_ingest_prefiltered_ids(gb_agg *h, const gb_col *cols, uint64_t 
     if (gb_status s0 = apply_reset(h, st)) return s0;
     const int nc = (int)h->col_types.size();
     for (int c = 0; c < nc; c++) {
+        if (cols[c].validity && !((h->nullable_mask >> c) & 1ull)) {
+            set_error("column %d carries a validity mask but the spec declares it NOT NULL", c);
+            return GB_ERR_INVALID;
+        }
         h->plan.cols[c].data = cols[c].data;
-        h->plan.cols[c].valid = nullptr;
+        h->plan.cols[c].valid = c == h->str_col ? nullptr : cols[c].validity;  // a NULL key arrives as id -1
         h->plan.cols[c].offsets = cols[c].offsets;
     }
     h->plan.cols[nc].data = ids;

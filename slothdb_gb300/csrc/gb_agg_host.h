@@ -15,6 +15,7 @@ struct AggView {
     const int32_t *col_types;
     int n_filters;
     gb::Filter filters[GB_MAX_FILTERS];
+    uint64_t nullable_mask;  // spec columns declared nullable (bit c)
 };
 gb_status gb_agg_view(gb_agg *h, AggView *v);
 void gb_agg_count_launch(gb_agg *h, int n);

@@ -661,7 +661,7 @@ static FastPlan make_fast_plan(const Plan &P, FastFilters &FF) {
     for (int j = 0; j < P.n_filters; j++) {
         const Filter &f = P.filters[j];
         const int t = P.cols[f.col].type;
-        if (!is_int(t) && t != GB_T_DOUBLE) return F;
+        if ((!is_int(t) && t != GB_T_DOUBLE) || f.op > GB_CMP_GE) return F;  // IN / VARCHAR forms: generic path
         FF.fp[j] = P.cols[f.col].data;
         FF.fv[j] = P.cols[f.col].valid;
         if (t == GB_T_DOUBLE) memcpy(&FF.fk[j], &f.dc, 8);

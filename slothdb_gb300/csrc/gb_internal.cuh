@@ -82,6 +82,8 @@ struct Filter {
     int32_t op;
     int64_t ic;
     double dc;
+    const void *ptr;  // device copy of an IN set (sorted int64) or a string literal
+    u64 n;            // its members / bytes
 };
 
 struct Plan {
@@ -189,6 +191,36 @@ __device__ __forceinline__ bool cmp_f(int op, double a, double b) {
     case GB_CMP_GT: return a > b;
     default: return a >= b;
     }
+}
+
+// Membership of x in a sorted int64 set of n members (IN).
+__device__ __forceinline__ bool in_set(const void *set, u64 n, i64 x) {
+    const long long *a = (const long long *)set;
+    u64 lo = 0, hi = n;  // first member >= x
+    while (lo < hi) {
+        const u64 mid = (lo + hi) >> 1;
+        if (__ldg(a + mid) < x) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo < n && __ldg(a + lo) == x;
+}
+
+// A VARCHAR predicate on the bytes s[0, len): = / <> the literal, or LIKE /
+// NOT LIKE '%needle%' (byte substring; an empty needle is in every string).
+__device__ __forceinline__ bool str_pred(int op, const uint8_t *s, u64 len, const void *lit_, u64 n) {
+    const uint8_t *lit = (const uint8_t *)lit_;
+    if (op == GB_CMP_STR_EQ || op == GB_CMP_STR_NE) {
+        bool eq = len == n;
+        for (u64 i = 0; eq && i < n; i++) eq = s[i] == __ldg(lit + i);
+        return (op == GB_CMP_STR_EQ) == eq;
+    }
+    bool found = n == 0;
+    for (u64 i = 0; !found && i + n <= len; i++) {
+        bool m = true;
+        for (u64 k = 0; m && k < n; k++) m = s[i + k] == __ldg(lit + k);
+        found = m;
+    }
+    return (op == GB_CMP_LIKE) == found;
 }
 
 // Combine two partial values of one op (registers, no atomics).

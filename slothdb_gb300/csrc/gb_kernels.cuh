@@ -77,7 +77,12 @@ __device__ __forceinline__ bool pass_filters(const Plan &P, u64 r) {
         const Filter &f = P.filters[i];
         const DevCol &c = P.cols[f.col];
         if (!row_valid(c.valid, r)) return false;
-        if (c.type == GB_T_DOUBLE) {
+        if (c.type == GB_T_VARCHAR) {
+            const i64 b = c.offsets[r], e = c.offsets[r + 1];
+            if (!str_pred(f.op, (const uint8_t *)c.data + b, (u64)(e - b), f.ptr, f.n)) return false;
+        } else if (f.op == GB_CMP_IN) {
+            if (!in_set(f.ptr, f.n, load_int(c, r))) return false;
+        } else if (c.type == GB_T_DOUBLE) {
             if (!cmp_f(f.op, load_f64(c, r), f.dc)) return false;
         } else {
             if (!cmp_i(f.op, load_int(c, r), f.ic)) return false;

@@ -142,9 +142,11 @@ struct PqPage {
     int32_t col;         // file column
     uint32_t rg;
     uint32_t first_row;  // within the row group
-    uint32_t n_values;
-    uint32_t bytes;      // payload bytes
-    uint64_t off;        // payload offset in the file
+    uint32_t n_values;   // entries, NULLs included (rows of a flat column)
+    uint32_t bytes;      // bytes of the encoded values
+    uint64_t off;        // offset of the encoded values in the file
+    uint64_t def_off = 0;    // OPTIONAL column: its definition levels (RLE/bit-packed, bit width 1)
+    uint32_t def_bytes = 0;  // 0: REQUIRED column (no levels)
 };
 
 struct PqChunk {
@@ -336,17 +338,22 @@ static gb_status parse_pages(gb_pq_file *f, uint32_t rg, uint32_t col) {
     uint64_t pos = ch.start, end = ch.start + ch.size;
     uint32_t row = 0;
     ch.page_begin = (uint32_t)f->pages.size();
+    // a flat OPTIONAL column (maximum definition level 1) prefixes every data
+    // page's values with its definition levels (ReadDefLevels,
+    // parquet.cpp:1879-1981): page v1 as a 4-byte length + RLE/bit-packed
+    // hybrid, page v2 as the hybrid alone, its length in the page header
+    const bool opt = f->cols[col].repetition == 1;
     while (pos < end) {
         TReader r(f->host, end, pos);
         int fid, type, last = 0;
-        int ptype = -1, enc = -1;
-        int64_t csize = -1, nvals = -1, dict_n = -1;
+        int ptype = -1, enc = -1, version = 0;
+        int64_t csize = -1, nvals = -1, dict_n = -1, def_len = 0, rep_len = 0;
         while (r.field(fid, type, last)) {
             if (fid == 1 && type == 5) ptype = (int)r.zz();
             else if (fid == 3 && type == 5) csize = r.zz();
             else if ((fid == 5 || fid == 8) && type == 12) {  // data page v1 / v2
+                version = fid == 5 ? 1 : 2;
                 int f2, t2, l2 = 0;
-                int64_t def_len = 0, rep_len = 0;
                 while (r.field(f2, t2, l2)) {
                     if (f2 == 1 && t2 == 5) nvals = r.zz();
                     else if (fid == 5 && f2 == 2 && t2 == 5) enc = (int)r.zz();
@@ -355,8 +362,8 @@ static gb_status parse_pages(gb_pq_file *f, uint32_t rg, uint32_t col) {
                     else if (fid == 8 && f2 == 6 && t2 == 5) rep_len = r.zz();
                     else r.skip(t2);
                 }
-                if (def_len || rep_len) {
-                    set_error("Parquet data page v2 with repetition/definition levels is not supported");
+                if (rep_len || (def_len && !opt)) {
+                    set_error("Parquet levels on a non-OPTIONAL or repeated column are not supported");
                     return GB_ERR_UNSUPPORTED;
                 }
             } else if (fid == 7 && type == 12) {
@@ -387,13 +394,34 @@ static gb_status parse_pages(gb_pq_file *f, uint32_t rg, uint32_t col) {
             pg.n_values = (uint32_t)nvals;
             pg.bytes = (uint32_t)csize;
             pg.off = payload;
+            if (opt) {
+                uint64_t lv;
+                if (version == 1) {
+                    if (csize < 4) return pq_corrupt("definition levels");
+                    uint32_t l4;
+                    memcpy(&l4, f->host + payload, 4);
+                    pg.def_off = payload + 4;
+                    lv = 4 + (uint64_t)l4;
+                    pg.def_bytes = l4;
+                } else {
+                    if (def_len < 0) return pq_corrupt("definition levels");
+                    pg.def_off = payload;
+                    lv = (uint64_t)def_len;
+                    pg.def_bytes = (uint32_t)def_len;
+                }
+                if (lv > (uint64_t)csize || (pg.def_bytes == 0 && nvals > 0)) return pq_corrupt("definition levels");
+                pg.off = payload + lv;
+                pg.bytes = (uint32_t)((uint64_t)csize - lv);
+            }
             if (enc == 0) {
                 pg.kind = 0;
-                if ((uint64_t)nvals * f->cols[col].width > (uint64_t)csize) return pq_corrupt("PLAIN page size");
+                // with NULLs only the defined values are stored: their count
+                // is checked on the GPU once the levels are decoded
+                if (!opt && (uint64_t)nvals * f->cols[col].width > (uint64_t)csize) return pq_corrupt("PLAIN page size");
                 if (f->cols[col].gtype == GB_T_VARCHAR) f->cols[col].plain_strings = true;
             } else if (enc == 2 || enc == 8) {
                 pg.kind = 1;
-                if (csize < 1) return pq_corrupt("dictionary-index page");
+                if (pg.bytes < 1 && !(opt && nvals > 0)) return pq_corrupt("dictionary-index page");
             } else {
                 set_error("Parquet encoding %d is not supported on the GPU path", enc);
                 return GB_ERR_UNSUPPORTED;
@@ -410,69 +438,101 @@ static gb_status parse_pages(gb_pq_file *f, uint32_t rg, uint32_t col) {
 
 // ================================================================= kernels
 struct DPage {
-    uint64_t off;       // payload offset in the device file
+    uint64_t off;       // offset of the encoded values in the device file
     uint64_t dict_off;  // dictionary payload offset
     uint64_t dict_ids;  // VARCHAR: device address of the dictionary's string ids (0: fixed-width values)
-    uint32_t first_row, n_values, bytes, dict_n;
-    uint32_t run_base, run_cap;  // run-table slice (dictionary pages)
+    uint64_t dict_match;  // VARCHAR: per dictionary entry, 1 = passes the string predicates (0: none)
+    uint64_t def_off;   // definition levels (OPTIONAL column; def_bytes = 0: REQUIRED)
+    uint32_t first_row, n_values, bytes, dict_n;  // n_values: entries, NULLs included
+    uint32_t run_base, run_cap;          // run-table slice of the dictionary indices
+    uint32_t def_run_base, def_run_cap;  // run-table slice of the definition levels
+    uint32_t def_bytes;
     int32_t kind, width;
+    uint32_t pad;
 };
 
 struct DRun {
-    uint32_t start;  // first value index of the run within the page
+    uint32_t start;  // first entry of the run within its stream
     uint32_t off;    // payload byte of the packed values (0xffffffff = RLE)
     uint32_t cnt;
     uint32_t val;    // RLE value
+    uint32_t nn;     // definition levels: defined entries before the run
+};
+
+// One RLE/bit-packed hybrid stream for the run walk: the dictionary indices
+// of a data page (bit width in its first byte) or the definition levels of
+// an OPTIONAL column's data page (bit width 1).  Per page, page_runs holds
+// PQ_PR words: {index runs, index bit width, level runs, defined entries}.
+#define PQ_PR 4
+struct RunJob {
+    uint64_t off;       // stream offset in the device file
+    uint32_t bytes;     // stream bytes
+    uint32_t n_values;  // entries to decode (an upper bound for indices)
+    uint32_t run_base, run_cap;
+    uint32_t page;      // index into pages / page_runs
+    uint32_t levels;    // 1: definition levels
 };
 
 #define PQ_WIN 16384
+#define PQ_LEVEL_RUN 512  // bit-packed level runs are split at this many entries (bounds the popcount)
 
-// One CTA per dictionary-index page: stage windows of the payload in shared
-// memory; thread 0 walks the run headers.  Run counts/bit width per page go
-// to page_runs[p] = {n_runs, bit_width}.
-__global__ void k_pq_runs(const uint8_t *file, const DPage *pages, const uint32_t *dict_pages, DRun *runs,
+// One CTA per stream: windows of the payload are staged in shared memory and
+// thread 0 walks the run headers (RleDecoder::FetchRun, parquet.cpp:476-540).
+// A level stream's runs also carry the defined entries before them, and its
+// bit-packed runs are split every PQ_LEVEL_RUN entries so that a row's
+// position among the defined values needs at most PQ_LEVEL_RUN / 64 words of
+// popcount.  For a level stream, the page's defined entries must fit its
+// values (PLAIN: width bytes each); anything else sets ERR_CORRUPT.
+__global__ void k_pq_runs(const uint8_t *file, const DPage *pages, const RunJob *jobs, DRun *runs,
                           uint32_t *page_runs, Ctl *ctl) {
     __shared__ uint8_t win[PQ_WIN + 16];
-    __shared__ uint64_t s_pos;   // absolute payload position of the walk
-    __shared__ uint32_t s_vals, s_runs, s_done, s_bw;
-    const uint32_t pidx = dict_pages[blockIdx.x];
-    const DPage pg = pages[pidx];
+    __shared__ uint64_t s_pos;   // stream position of the walk
+    __shared__ uint32_t s_vals, s_runs, s_done, s_bw, s_nn;
+    const RunJob J = jobs[blockIdx.x];
     if (threadIdx.x == 0) {
-        s_pos = 0;
         s_vals = 0;
         s_runs = 0;
+        s_nn = 0;
         s_done = 0;
-        s_bw = file[pg.off];
-        if (s_bw > 32) {
-            atomicOr(&ctl->err, (u32)ERR_CORRUPT);
+        s_pos = 0;
+        if (J.levels) {
+            s_bw = 1;
+        } else if (J.bytes == 0) {  // no encoded values (a page of NULLs only)
+            s_bw = 0;
             s_done = 1;
+        } else {
+            s_bw = file[J.off];
+            s_pos = 1;
+            if (s_bw > 32) {
+                atomicOr(&ctl->err, (u32)ERR_CORRUPT);
+                s_done = 1;
+            }
         }
-        s_pos = 1;
     }
     __syncthreads();
     while (!s_done) {
         const uint64_t w0 = s_pos;
-        const uint64_t wn = min((uint64_t)PQ_WIN, (uint64_t)pg.bytes - w0);
-        for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) win[i] = file[pg.off + w0 + i];
+        const uint64_t wn = min((uint64_t)PQ_WIN, (uint64_t)J.bytes - w0);
+        for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) win[i] = file[J.off + w0 + i];
         __syncthreads();
         if (threadIdx.x == 0) {
             const uint32_t bw = s_bw;
             const uint32_t vb = (bw + 7) / 8;
             uint64_t pos = w0;
-            uint32_t vals = s_vals, nr = s_runs;
+            uint32_t vals = s_vals, nr = s_runs, nn = s_nn;
             bool done = false, err = false;
             while (!done) {
-                if (vals >= pg.n_values || pos >= pg.bytes) {
+                if (vals >= J.n_values || pos >= J.bytes) {
                     done = true;
                     break;
                 }
                 // a header (<= 10 bytes) plus an RLE value must lie inside the window
-                if (pos + 16 > w0 + wn && w0 + wn < pg.bytes) break;
+                if (pos + 16 > w0 + wn && w0 + wn < J.bytes) break;
                 uint64_t hdr = 0;
                 int sh = 0;
                 uint64_t q = pos;
                 for (;;) {
-                    if (q >= pg.bytes || sh > 35) {
+                    if (q >= J.bytes || sh > 35) {
                         err = true;
                         break;
                     }
@@ -483,43 +543,79 @@ __global__ void k_pq_runs(const uint8_t *file, const DPage *pages, const uint32_
                     sh += 7;
                 }
                 if (err) break;
-                DRun rn;
-                rn.start = vals;
                 if (hdr & 1) {
-                    const uint64_t cnt = (hdr >> 1) * 8;
+                    const uint64_t cnt = min((hdr >> 1) * 8, (uint64_t)(J.n_values - vals));
                     const uint64_t plen = (hdr >> 1) * (uint64_t)bw;
-                    rn.off = (uint32_t)q;
-                    rn.cnt = (uint32_t)min(cnt, (uint64_t)(pg.n_values - vals));
-                    rn.val = 0;
-                    q += plen;
-                    if (q > pg.bytes) {
+                    uint64_t have = cnt;
+                    bool trunc = false;
+                    if (q + plen > J.bytes) {
                         // truncated packed run: the reference decodes what is there
                         // and leaves the rest unset (RleDecoder::NextBatch refill)
-                        const uint64_t have = ((uint64_t)pg.bytes - rn.off) * 8 / (bw ? bw : 1);
-                        rn.cnt = (uint32_t)min((uint64_t)rn.cnt, have);
-                        done = true;
+                        have = min(cnt, ((uint64_t)J.bytes - q) * 8 / (bw ? bw : 1));
+                        trunc = true;
                     }
+                    // level runs split every PQ_LEVEL_RUN entries (byte aligned: 512 bits)
+                    for (uint64_t e0 = 0; e0 < have && !err; e0 += (J.levels ? PQ_LEVEL_RUN : have)) {
+                        DRun rn;
+                        rn.start = vals + (uint32_t)e0;
+                        rn.off = (uint32_t)(q + (J.levels ? e0 / 8 : 0));
+                        rn.cnt = (uint32_t)min(have - e0, (uint64_t)(J.levels ? PQ_LEVEL_RUN : have));
+                        rn.val = 0;
+                        rn.nn = nn;
+                        if (J.levels) {
+                            // defined entries of this piece: popcount of its bits
+                            // (read from the file: a run may extend past the window)
+                            uint32_t c = 0;
+                            for (uint32_t b = 0; b < rn.cnt; b += 8) {
+                                uint32_t byte = __ldg(file + J.off + rn.off + b / 8);
+                                if (rn.cnt - b < 8) byte &= (1u << (rn.cnt - b)) - 1u;
+                                c += __popc(byte);
+                            }
+                            nn += c;
+                        }
+                        if (rn.cnt) {
+                            if (nr >= J.run_cap) {
+                                err = true;
+                                break;
+                            }
+                            runs[J.run_base + nr] = rn;
+                            nr++;
+                        }
+                    }
+                    vals += (uint32_t)have;
+                    q += plen;
+                    if (trunc) done = true;
                 } else {
                     const uint64_t cnt = hdr >> 1;
-                    if (q + vb > pg.bytes) {
+                    if (q + vb > J.bytes) {
                         done = true;
                         break;
                     }
                     uint32_t v = 0;
                     for (uint32_t b = 0; b < vb; b++) v |= (uint32_t)win[q - w0 + b] << (8 * b);
                     q += vb;
+                    DRun rn;
+                    rn.start = vals;
                     rn.off = 0xffffffffu;
-                    rn.cnt = (uint32_t)min(cnt, (uint64_t)(pg.n_values - vals));
+                    rn.cnt = (uint32_t)min(cnt, (uint64_t)(J.n_values - vals));
                     rn.val = v;
-                }
-                if (rn.cnt) {
-                    if (nr >= pg.run_cap) {
-                        err = true;
-                        break;
+                    rn.nn = nn;
+                    if (J.levels) {
+                        if (v > 1) {  // a flat OPTIONAL column has levels 0 and 1
+                            err = true;
+                            break;
+                        }
+                        nn += v ? rn.cnt : 0u;
                     }
-                    runs[pg.run_base + nr] = rn;
-                    nr++;
-                    vals += rn.cnt;
+                    if (rn.cnt) {
+                        if (nr >= J.run_cap) {
+                            err = true;
+                            break;
+                        }
+                        runs[J.run_base + nr] = rn;
+                        nr++;
+                        vals += rn.cnt;
+                    }
                 }
                 pos = q;
             }
@@ -530,13 +626,24 @@ __global__ void k_pq_runs(const uint8_t *file, const DPage *pages, const uint32_
             s_pos = pos;
             s_vals = vals;
             s_runs = nr;
+            s_nn = nn;
             s_done = done;
         }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        page_runs[2 * pidx] = s_runs;
-        page_runs[2 * pidx + 1] = s_bw;
+        uint32_t *pr = page_runs + (u64)PQ_PR * J.page;
+        if (J.levels) {
+            const DPage &pg = pages[J.page];
+            pr[2] = s_runs;
+            pr[3] = s_nn;
+            // the defined entries are the stored values: they must fit
+            if (s_vals < pg.n_values || (pg.kind == 0 && (u64)s_nn * (u64)pg.width > pg.bytes))
+                atomicOr(&ctl->err, (u32)ERR_CORRUPT);
+        } else {
+            pr[0] = s_runs;
+            pr[1] = s_bw;
+        }
     }
 }
 
@@ -663,10 +770,56 @@ __device__ __forceinline__ u64 load_plain(const uint8_t *p, int width) {
     return sh ? ((lo >> sh) | (__ldg(w + 1) << (64 - sh))) : lo;
 }
 
+// 64 bits starting at bit `bit` of p (LSB first): the aligned words that hold
+// them, joined by a funnel shift.
+__device__ __forceinline__ u64 load64_bits(const uint8_t *p, u64 bit) {
+    const uintptr_t a = (uintptr_t)p + (uintptr_t)(bit >> 3);
+    const u64 *w = (const u64 *)(a & ~(uintptr_t)7);
+    const uint32_t sh = (uint32_t)(a & 7) * 8 + (uint32_t)(bit & 7);  // < 64
+    const u64 lo = __ldg(w);
+    return sh ? ((lo >> sh) | (__ldg(w + 1) << (64 - sh))) : lo;
+}
+
+// Entry i of a page: is it defined (not NULL), and if so its index j among
+// the page's stored values (the defined entries before it).  A REQUIRED
+// column's entries are all defined (j = i).
+__device__ __forceinline__ bool level_at(const uint8_t *file, const DPage &pg, const DRun *runs,
+                                         const uint32_t *page_runs, uint32_t pidx, uint32_t i, uint32_t &j) {
+    j = i;
+    if (pg.def_bytes == 0) return true;
+    const uint32_t nr = page_runs[PQ_PR * pidx + 2];
+    const DRun *rr = runs + pg.def_run_base;
+    if (nr == 0) return false;
+    uint32_t lo = 0, hi = nr;  // last run with start <= i
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (rr[mid].start <= i) lo = mid;
+        else hi = mid;
+    }
+    const DRun rn = rr[lo];
+    if (i < rn.start || i >= rn.start + rn.cnt) return false;  // past the decoded levels (corrupt page)
+    const uint32_t d = i - rn.start;
+    if (rn.off == 0xffffffffu) {
+        j = rn.nn + (rn.val ? d : 0u);
+        return rn.val != 0;
+    }
+    // a bit-packed piece (<= PQ_LEVEL_RUN entries): popcount of the bits before d
+    const uint8_t *bp = file + pg.def_off + rn.off;
+    uint32_t c = 0;
+    for (uint32_t w = 0; w + 64 <= d; w += 64) c += __popcll(load64_bits(bp, w));
+    const u64 tail = load64_bits(bp, d & ~63u);
+    const uint32_t r = d & 63u;
+    if (r) c += __popcll(tail & ((1ull << r) - 1ull));
+    j = rn.nn + c;
+    return (tail >> r) & 1ull;
+}
+
+// Value i of page pg; for a VARCHAR page `match` asks for its entry's
+// string-predicate flag instead of its string id.
 __device__ __forceinline__ u64 decode_at(const uint8_t *file, const DPage &pg, const DRun *runs,
-                                         const uint32_t *page_runs, uint32_t pidx, uint32_t i) {
+                                         const uint32_t *page_runs, uint32_t pidx, uint32_t i, bool match = false) {
     if (pg.kind == 0) return load_plain(file + pg.off + (u64)i * pg.width, pg.width);
-    const uint32_t nr = page_runs[2 * pidx], bw = page_runs[2 * pidx + 1];
+    const uint32_t nr = page_runs[PQ_PR * pidx], bw = page_runs[PQ_PR * pidx + 1];
     const DRun *rr = runs + pg.run_base;
     uint32_t lo = 0, hi = nr;  // last run with start <= i
     if (nr == 0) return 0;
@@ -684,8 +837,11 @@ __device__ __forceinline__ u64 decode_at(const uint8_t *file, const DPage &pg, c
     } else {
         idx = load_bits(file + pg.off + rn.off, (u64)(i - rn.start) * bw, bw);
     }
-    if (idx >= pg.dict_n) return pg.dict_ids ? ~0ull : 0;  // out of range: the reference's 0 (VARCHAR: NULL id)
-    if (pg.dict_ids) return (u64)__ldg((const long long *)pg.dict_ids + idx);
+    if (idx >= pg.dict_n) return pg.dict_ids ? (match ? 0ull : ~0ull) : 0;  // out of range: the reference's 0 (VARCHAR: NULL id)
+    if (pg.dict_ids) {
+        if (match) return pg.dict_match ? (u64)__ldg((const uint8_t *)pg.dict_match + idx) : 1ull;
+        return (u64)__ldg((const long long *)pg.dict_ids + idx);
+    }
     return load_plain(file + pg.dict_off + (u64)idx * pg.width, pg.width);
 }
 
@@ -698,8 +854,11 @@ struct PqScan {
     int32_t n_cols;
     int32_t out_type[GB_MAX_COLS];   // gb_type of each compacted output column
     int32_t n_filters;
+    int32_t id_col;                  // the VARCHAR key's string-id column (-1: none); a NULL key is id -1
+    int32_t str_match;               // 1: the VARCHAR key has string predicates (pages' dict_match)
     Filter filters[GB_MAX_FILTERS];
     void *out[GB_MAX_COLS];
+    uint64_t *out_valid[GB_MAX_COLS];  // validity words of an OPTIONAL column's output (all ones on entry)
     u64 out_cap;
 };
 
@@ -710,11 +869,13 @@ struct PqScan {
 #define PQ_CHUNK 4096
 __device__ __forceinline__ u64 decode_col(const uint8_t *file, const DPage *pages, const DRun *runs,
                                           const uint32_t *page_runs, const uint32_t *col_pages, int n_cols,
-                                          uint32_t rg, int c, uint32_t r) {
+                                          uint32_t rg, int c, uint32_t r, bool &valid, bool match = false) {
     const uint32_t pb = col_pages[2 * (rg * n_cols + c)], pe = col_pages[2 * (rg * n_cols + c) + 1];
     const uint32_t pi = find_page(pages, pb, pe, r);
     const DPage &pg = pages[pi];
-    return decode_at(file, pg, runs, page_runs, pi, r - pg.first_row);
+    uint32_t j;
+    valid = level_at(file, pg, runs, page_runs, pi, r - pg.first_row, j);
+    return valid ? decode_at(file, pg, runs, page_runs, pi, j, match) : 0;
 }
 
 // Per chunk, shared memory holds each column's pages that overlap the chunk
@@ -745,7 +906,7 @@ __device__ __forceinline__ uint32_t run_search(const DRun *rr, uint32_t lo, uint
 
 // Value i of dictionary page pg, its run found in `rr[lo, hi)`.
 __device__ __forceinline__ u64 dict_value(const uint8_t *file, const DPage &pg, const DRun *rr, uint32_t lo,
-                                          uint32_t hi, uint32_t bw, uint32_t i) {
+                                          uint32_t hi, uint32_t bw, uint32_t i, bool match = false) {
     if (hi <= lo) return 0;
     const DRun rn = rr[run_search(rr, lo, hi, i)];
     uint32_t idx;
@@ -756,26 +917,32 @@ __device__ __forceinline__ u64 dict_value(const uint8_t *file, const DPage &pg, 
     } else {
         idx = load_bits(file + pg.off + rn.off, (u64)(i - rn.start) * bw, bw);
     }
-    if (idx >= pg.dict_n) return pg.dict_ids ? ~0ull : 0;  // out of range: the reference's 0 (VARCHAR: NULL id)
-    if (pg.dict_ids) return (u64)__ldg((const long long *)pg.dict_ids + idx);
+    if (idx >= pg.dict_n) return pg.dict_ids ? (match ? 0ull : ~0ull) : 0;  // out of range: the reference's 0 (VARCHAR: NULL id)
+    if (pg.dict_ids) {
+        if (match) return pg.dict_match ? (u64)__ldg((const uint8_t *)pg.dict_match + idx) : 1ull;
+        return (u64)__ldg((const long long *)pg.dict_ids + idx);
+    }
     return load_plain(file + pg.dict_off + (u64)idx * pg.width, pg.width);
 }
 
-// Row r (row-group relative) of column c through the chunk's staged view.
+// Row r (row-group relative) of column c through the chunk's staged view;
+// valid = false for a NULL entry of an OPTIONAL column.
 __device__ __forceinline__ u64 decode_staged(const uint8_t *file, const DPage *pages, const DRun *runs,
                                              const uint32_t *page_runs, const uint32_t *col_pages, int n_cols,
                                              uint32_t rg, int c, uint32_t r, const PqChunkView &V,
-                                             const DRun *srun) {
+                                             const DRun *srun, bool &valid, bool match = false) {
     const uint32_t np = V.np[c];
-    if (np == 0) return decode_col(file, pages, runs, page_runs, col_pages, n_cols, rg, c, r);
+    if (np == 0) return decode_col(file, pages, runs, page_runs, col_pages, n_cols, rg, c, r, valid, match);
     uint32_t k = 0;
     while (k + 1 < np && V.pfirst[c][k + 1] <= r) k++;
     const uint32_t pi = V.pidx[c][k];
     const DPage &pg = pages[pi];
-    const uint32_t i = r - pg.first_row;
-    if (pg.kind != 0 && c == V.dcol)
-        return dict_value(file, pg, srun + V.rbeg[k], 0, V.rcnt[k], page_runs[2 * pi + 1], i);
-    return decode_at(file, pg, runs, page_runs, pi, i);
+    uint32_t j;
+    valid = level_at(file, pg, runs, page_runs, pi, r - pg.first_row, j);
+    if (!valid) return 0;
+    if (pg.kind != 0 && c == V.dcol)  // (staged runs: REQUIRED columns only, j = i)
+        return dict_value(file, pg, srun + V.rbeg[k], 0, V.rcnt[k], page_runs[PQ_PR * pi + 1], j, match);
+    return decode_at(file, pg, runs, page_runs, pi, j, match);
 }
 
 __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPage *pages, const DRun *runs,
@@ -815,7 +982,7 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
         if (threadIdx.x == 0) {
             int dc = -1;
             for (int c = 0; c < S.n_cols && dc < 0; c++)
-                if (V.np[c] && pages[V.pidx[c][0]].kind != 0) dc = c;
+                if (V.np[c] && pages[V.pidx[c][0]].kind != 0 && pages[V.pidx[c][0]].def_bytes == 0) dc = c;
             uint32_t tot = 0;
             if (dc >= 0) {
                 for (uint32_t k = 0; k < V.np[dc]; k++) {
@@ -827,7 +994,7 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
                         V.rcnt[k] = 0;
                         continue;
                     }
-                    const uint32_t nr = page_runs[2 * pi];
+                    const uint32_t nr = page_runs[PQ_PR * pi];
                     const DRun *rr = runs + pg.run_base;
                     const uint32_t i0 = ch.row0 > pg.first_row ? ch.row0 - pg.first_row : 0;
                     const uint32_t i1 = rlast - pg.first_row;  // inclusive (clipped by the run search)
@@ -852,8 +1019,8 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
         u32 mine = 0;
         // one predicate on a PLAIN column inside one page (the common case):
         // every load of the chunk is issued before any compare
-        const int fc = S.n_filters == 1 ? S.filters[0].col : -1;
-        if (fc >= 0 && V.np[fc] == 1 && pages[V.pidx[fc][0]].kind == 0) {
+        const int fc = (S.n_filters == 1 && S.filters[0].op <= GB_CMP_GE) ? S.filters[0].col : -1;
+        if (fc >= 0 && V.np[fc] == 1 && pages[V.pidx[fc][0]].kind == 0 && pages[V.pidx[fc][0]].def_bytes == 0) {
             const DPage pg = pages[V.pidx[fc][0]];
             const Filter f = S.filters[0];
             const uint8_t *base = file + pg.off;  // page payloads start at any byte
@@ -882,10 +1049,21 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
             keep[j] = rr < ch.nrows;
             if (!keep[j]) continue;
             const uint32_t r = ch.row0 + rr;
+            if (S.str_match) {  // the VARCHAR key's string predicates, per dictionary entry
+                bool valid;
+                const u64 m = decode_staged(file, pages, runs, page_runs, col_pages, S.n_cols, ch.rg, S.id_col, r, V,
+                                            srun, valid, true);
+                keep[j] = valid && m != 0;
+            }
             for (int q = 0; q < S.n_filters && keep[j]; q++) {
                 const Filter &f = S.filters[q];
-                const u64 x = decode_staged(file, pages, runs, page_runs, col_pages, S.n_cols, ch.rg, f.col, r, V, srun);
-                if (S.out_type[f.col] == GB_T_DOUBLE) keep[j] = cmp_f(f.op, __longlong_as_double((i64)x), f.dc);
+                if (f.op >= GB_CMP_STR_EQ) continue;  // folded into the dictionary match above
+                bool valid;
+                const u64 x = decode_staged(file, pages, runs, page_runs, col_pages, S.n_cols, ch.rg, f.col, r, V, srun,
+                                            valid);
+                if (!valid) keep[j] = false;  // a comparison with NULL keeps no row
+                else if (f.op == GB_CMP_IN) keep[j] = in_set(f.ptr, f.n, (i64)x);
+                else if (S.out_type[f.col] == GB_T_DOUBLE) keep[j] = cmp_f(f.op, __longlong_as_double((i64)x), f.dc);
                 else keep[j] = cmp_i(f.op, (i64)x, f.ic);
             }
             mine += keep[j];
@@ -913,7 +1091,12 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
             }
             const uint32_t r = s_surv[wid][e];
             for (int c = 0; c < S.n_cols; c++) {
-                const u64 x = decode_staged(file, pages, runs, page_runs, col_pages, S.n_cols, ch.rg, c, r, V, srun);
+                bool valid;
+                u64 x = decode_staged(file, pages, runs, page_runs, col_pages, S.n_cols, ch.rg, c, r, V, srun, valid);
+                if (!valid) {
+                    if (c == S.id_col) x = ~0ull;  // the NULL string id
+                    else if (S.out_valid[c]) atomicAnd((unsigned long long *)&S.out_valid[c][oe >> 6], ~(1ull << (oe & 63)));
+                }
                 switch (S.out_type[c]) {
                 case GB_T_SMALLINT: ((int16_t *)S.out[c])[oe] = (int16_t)(i64)x; break;
                 case GB_T_INTEGER: ((int32_t *)S.out[c])[oe] = (int32_t)(i64)x; break;
@@ -995,7 +1178,7 @@ static bool pq_rg_might_match(const gb_pq_file *f, uint32_t rg, int fcol, const 
 // columns (offsets relative to `base`), with run-table slots for the
 // dictionary pages; col_pages gets one {begin, end} pair per (rg, column).
 static gb_status pq_page_table(const gb_pq_file *f, uint32_t rg_begin, uint32_t rg_end, const int32_t *cols, int nc,
-                               uint64_t base, std::vector<DPage> &pages, std::vector<uint32_t> &dict_pages,
+                               uint64_t base, std::vector<DPage> &pages, std::vector<RunJob> &jobs,
                                std::vector<uint32_t> &col_pages, uint32_t &run_total) {
     for (uint32_t g = rg_begin; g < rg_end; g++) {
         for (int c = 0; c < nc; c++) {
@@ -1011,6 +1194,7 @@ static gb_status pq_page_table(const gb_pq_file *f, uint32_t rg_begin, uint32_t 
                 d.bytes = pp.bytes;
                 d.kind = pp.kind;
                 d.width = pc.width;
+                const uint32_t pidx = (uint32_t)pages.size();
                 if (pp.kind == 1) {
                     if (ch.dict_off < 0) {
                         set_error("dictionary-encoded page without a dictionary page");
@@ -1021,7 +1205,17 @@ static gb_status pq_page_table(const gb_pq_file *f, uint32_t rg_begin, uint32_t 
                     d.run_base = run_total;
                     d.run_cap = std::min<uint32_t>(pp.n_values, pp.bytes) + 1;
                     run_total += d.run_cap;
-                    dict_pages.push_back((uint32_t)pages.size());
+                    jobs.push_back({d.off, d.bytes, d.n_values, d.run_base, d.run_cap, pidx, 0u});
+                }
+                if (pp.def_bytes) {
+                    // every header byte opens at most one run; bit-packed runs
+                    // split every PQ_LEVEL_RUN entries
+                    d.def_off = pp.def_off - base;
+                    d.def_bytes = pp.def_bytes;
+                    d.def_run_base = run_total;
+                    d.def_run_cap = pp.def_bytes + pp.n_values / PQ_LEVEL_RUN + 2;
+                    run_total += d.def_run_cap;
+                    jobs.push_back({d.def_off, d.def_bytes, d.n_values, d.def_run_base, d.def_run_cap, pidx, 1u});
                 }
                 pages.push_back(d);
             }
@@ -1040,9 +1234,10 @@ static gb_status pq_build_index(gb_pq_file *f, cudaStream_t st) {
     std::vector<int32_t> all(nfc);
     for (int c = 0; c < nfc; c++) all[c] = c;
     std::vector<DPage> pages;
-    std::vector<uint32_t> dict_pages, col_pages;
+    std::vector<RunJob> jobs;
+    std::vector<uint32_t> col_pages;
     uint32_t run_total = 0;
-    gb_status s = pq_page_table(f, 0, (uint32_t)f->rg_rows.size(), all.data(), nfc, 0, pages, dict_pages, col_pages,
+    gb_status s = pq_page_table(f, 0, (uint32_t)f->rg_rows.size(), all.data(), nfc, 0, pages, jobs, col_pages,
                                 run_total);
     if (s) return s;
     void *dp = nullptr, *ctl = nullptr;
@@ -1056,17 +1251,18 @@ static gb_status pq_build_index(gb_pq_file *f, cudaStream_t st) {
     cudaError_t e;
     if ((e = cudaMalloc(&f->idx_pages, std::max<size_t>(pages.size() * sizeof(DPage), 16))) ||
         (e = cudaMalloc(&f->idx_runs, (size_t)run_total * sizeof(DRun) + 16)) ||
-        (e = cudaMalloc(&f->idx_page_runs, pages.size() * 8 + 16)) ||
-        (e = cudaMalloc(&dp, dict_pages.size() * 4 + 16)) || (e = cudaMalloc(&ctl, sizeof(Ctl))))
+        (e = cudaMalloc(&f->idx_page_runs, pages.size() * PQ_PR * 4 + 16)) ||
+        (e = cudaMalloc(&dp, jobs.size() * sizeof(RunJob) + 16)) || (e = cudaMalloc(&ctl, sizeof(Ctl))))
         return fail(e, "cudaMalloc (Parquet page index)");
     if ((e = cudaMemcpyAsync(f->idx_pages, pages.data(), pages.size() * sizeof(DPage), cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(dp, dict_pages.data(), dict_pages.size() * 4, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(dp, jobs.data(), jobs.size() * sizeof(RunJob), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemsetAsync(f->idx_page_runs, 0, pages.size() * PQ_PR * 4 + 16, st)) ||
         (e = cudaMemsetAsync(ctl, 0, sizeof(Ctl), st)))
         return fail(e, "cudaMemcpy (Parquet page index)");
-    if (!dict_pages.empty()) {
-        k_pq_runs<<<(unsigned)dict_pages.size(), 128, 0, st>>>((const uint8_t *)f->dev, (const DPage *)f->idx_pages,
-                                                               (const uint32_t *)dp, (DRun *)f->idx_runs,
-                                                               (uint32_t *)f->idx_page_runs, (Ctl *)ctl);
+    if (!jobs.empty()) {
+        k_pq_runs<<<(unsigned)jobs.size(), 128, 0, st>>>((const uint8_t *)f->dev, (const DPage *)f->idx_pages,
+                                                         (const RunJob *)dp, (DRun *)f->idx_runs,
+                                                         (uint32_t *)f->idx_page_runs, (Ctl *)ctl);
         if ((e = cudaGetLastError())) return fail(e, "k_pq_runs");
     }
     Ctl c;
@@ -1153,7 +1349,9 @@ gb_status gb_pq_row_group_might_match(const gb_pq_file *f, uint32_t rg, const in
 gb_status gb_pq_upload(gb_pq_file *f, void *stream) {
     if (!f) return GB_ERR_INVALID;
     if (f->dev) return GB_OK;
-    GB_CUDA(cudaMalloc(&f->dev, f->size));
+    // 64 bytes of slack: the word loads of a level or index stream that ends
+    // the file may touch up to 15 bytes past its last byte
+    GB_CUDA(cudaMalloc(&f->dev, f->size + 64));
     GB_CUDA(cudaMemcpyAsync(f->dev, f->host, f->size, cudaMemcpyHostToDevice, (cudaStream_t)stream));
     GB_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
     return GB_OK;
@@ -1181,10 +1379,12 @@ struct PqScratch {
            ctl_cap = 0;
     void *out[GB_MAX_COLS] = {};
     size_t out_cap_rows = 0;
+    void *out_valid[GB_MAX_COLS] = {};  // validity words of OPTIONAL columns' output
+    size_t out_valid_cap[GB_MAX_COLS] = {};
     // VARCHAR dictionary pages of a batch: descriptors, value sources,
     // compacted offsets and bytes
-    void *dicts = nullptr, *dsrc = nullptr, *doffs = nullptr, *dbytes = nullptr;
-    size_t dicts_cap = 0, dsrc_cap = 0, doffs_cap = 0, dbytes_cap = 0;
+    void *dicts = nullptr, *dsrc = nullptr, *doffs = nullptr, *dbytes = nullptr, *dmatch = nullptr;
+    size_t dicts_cap = 0, dsrc_cap = 0, doffs_cap = 0, dbytes_cap = 0, dmatch_cap = 0;
 };
 
 static gb_status grow(void *&p, size_t &cap, size_t need) {
@@ -1224,9 +1424,11 @@ void gb_pq_release_scratch(gb_agg *h) {
         g_pq_scratch.erase(it);
     }
     for (void *p : {s->file_dev, s->pages, s->runs, s->page_runs, s->dict_pages, s->col_pages, s->chunks, s->ctl,
-                    s->dicts, s->dsrc, s->doffs, s->dbytes})
+                    s->dicts, s->dsrc, s->doffs, s->dbytes, s->dmatch})
         if (p) cudaFree(p);
     for (void *p : s->out)
+        if (p) cudaFree(p);
+    for (void *p : s->out_valid)
         if (p) cudaFree(p);
     delete s;
 }
@@ -1234,9 +1436,30 @@ void gb_pq_release_scratch(gb_agg *h) {
 // The batch's dictionary pages of VARCHAR file column `fcol`: walk, compact
 // and encode their values into the handle's string dictionary.  *ids gets
 // the ids of all values, page after page in row-group order (device).
+// The string predicates on a batch's VARCHAR key.
+struct PqStrFilters {
+    int32_t n;
+    int32_t op[GB_MAX_FILTERS];
+    const void *ptr[GB_MAX_FILTERS];
+    u64 len[GB_MAX_FILTERS];
+};
+
+// Per dictionary entry of a batch: 1 when its string passes every string
+// predicate on the key (the dictionary match table of BuildTypedKeepMask,
+// physical_planner.cpp:505-720: each entry is tested once, rows look it up).
+__global__ void k_pq_dict_match(const uint8_t *bytes, const int64_t *offs, u64 n, const __grid_constant__ PqStrFilters F,
+                                uint8_t *match) {
+    for (u64 e = blockIdx.x * (u64)blockDim.x + threadIdx.x; e < n; e += (u64)gridDim.x * blockDim.x) {
+        const int64_t b = offs[e], len = offs[e + 1] - b;
+        bool m = true;
+        for (int q = 0; q < F.n && m; q++) m = str_pred(F.op[q], bytes + b, (u64)len, F.ptr[q], F.len[q]);
+        match[e] = m ? 1 : 0;
+    }
+}
+
 static gb_status pq_varchar_dict(gb_agg *h, const gb_pq_file *f, PqScratch *S, const uint8_t *dfile, uint64_t base,
                                  uint32_t rg_begin, uint32_t rg_end, int fcol, Ctl *dctl, cudaStream_t st,
-                                 const int64_t **ids) {
+                                 const int64_t **ids, const PqStrFilters &SF, const uint8_t **match) {
     std::vector<DDict> dd;
     uint64_t D = 0, B = 0;
     for (uint32_t g = rg_begin; g < rg_end; g++) {
@@ -1279,6 +1502,15 @@ static gb_status pq_varchar_dict(gb_agg *h, const gb_pq_file *f, PqScratch *S, c
         dfile, (const u64 *)S->dsrc, (const int64_t *)S->doffs, D, (uint8_t *)S->dbytes);
     GB_CUDA(cudaGetLastError());
     gb_agg_count_launch(h, 2);
+    *match = nullptr;
+    if (SF.n) {
+        if ((s = grow(S->dmatch, S->dmatch_cap, D + 16))) return s;
+        k_pq_dict_match<<<(unsigned)std::min<uint64_t>((D + 255) / 256, (uint64_t)sm_count() * 8), 256, 0, st>>>(
+            (const uint8_t *)S->dbytes, (const int64_t *)S->doffs, D, SF, (uint8_t *)S->dmatch);
+        GB_CUDA(cudaGetLastError());
+        gb_agg_count_launch(h, 1);
+        *match = (const uint8_t *)S->dmatch;
+    }
     return gb_agg_encode_strings(h, (const uint8_t *)S->dbytes, (const int64_t *)S->doffs, D, B, st, ids);
 }
 
@@ -1309,9 +1541,13 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
             set_error("Parquet column '%s' has a physical type the GPU path does not decode", pc.name.c_str());
             return GB_ERR_UNSUPPORTED;
         }
-        if (pc.repetition != 0) {
-            set_error("Parquet column '%s' is OPTIONAL/REPEATED; the GPU path reads REQUIRED columns", pc.name.c_str());
+        if (pc.repetition == 2) {
+            set_error("Parquet column '%s' is REPEATED; the GPU path reads flat columns", pc.name.c_str());
             return GB_ERR_UNSUPPORTED;
+        }
+        if (pc.repetition == 1 && !((v.nullable_mask >> c) & 1ull)) {
+            set_error("Parquet column '%s' is OPTIONAL: declare spec column %d nullable", pc.name.c_str(), c);
+            return GB_ERR_INVALID;
         }
         const int want = v.col_types[c];
         const bool ok = want == pc.gtype || (want == GB_T_INTEGER && pc.gtype == GB_T_SMALLINT) ||
@@ -1336,6 +1572,21 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
             return GB_ERR_UNSUPPORTED;
         }
         vc = c;
+    }
+    // string predicates must be on the VARCHAR key (tested per dictionary entry)
+    PqStrFilters SF;
+    memset(&SF, 0, sizeof SF);
+    for (int q = 0; q < v.n_filters; q++) {
+        const Filter &fl = v.filters[q];
+        if (fl.op < GB_CMP_STR_EQ) continue;
+        if (fl.col != vc) {
+            set_error("filter %d: string predicates apply to the dictionary-encoded VARCHAR key on the Parquet path", q);
+            return GB_ERR_UNSUPPORTED;
+        }
+        SF.op[SF.n] = fl.op;
+        SF.ptr[SF.n] = fl.ptr;
+        SF.len[SF.n] = fl.n;
+        SF.n++;
     }
     // zone maps: row groups whose statistics rule out a predicate are skipped
     std::vector<char> live(rg_end - rg_begin, 1);
@@ -1372,7 +1623,7 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
         }
         dfile = (const uint8_t *)f->dev;
     } else {
-        if ((s = grow(S->file_dev, S->file_cap, hi - lo))) return s;
+        if ((s = grow(S->file_dev, S->file_cap, hi - lo + 64))) return s;  // slack for word loads past a stream's end
         GB_CUDA(cudaMemcpyAsync(S->file_dev, f->host + lo, hi - lo, cudaMemcpyHostToDevice, st));
         dfile = (const uint8_t *)S->file_dev;
         base = lo;
@@ -1407,37 +1658,43 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
     } else {
         // this batch's page table (offsets relative to its byte range) and runs
         std::vector<DPage> pages;
-        std::vector<uint32_t> dict_pages;
+        std::vector<RunJob> jobs;
         uint32_t run_total = 0;
-        if ((s = pq_page_table(f, rg_begin, rg_end, col_map, nc, base, pages, dict_pages, col_pages, run_total)))
+        if ((s = pq_page_table(f, rg_begin, rg_end, col_map, nc, base, pages, jobs, col_pages, run_total)))
             return s;
         if (vc >= 0) {
             // the VARCHAR key's data pages gather string ids: page after page,
             // each row group's dictionary entries start at its running base
             const int64_t *ids = nullptr;
-            if ((s = pq_varchar_dict(h, f, S, dfile, base, rg_begin, rg_end, col_map[vc], dctl, st, &ids))) return s;
+            const uint8_t *match = nullptr;
+            if ((s = pq_varchar_dict(h, f, S, dfile, base, rg_begin, rg_end, col_map[vc], dctl, st, &ids, SF, &match)))
+                return s;
             uint64_t eb = 0;
             for (uint32_t g = rg_begin; g < rg_end; g++) {
                 const PqChunk &ch = f->chunks[g][col_map[vc]];
                 const uint32_t k = (g - rg_begin) * (uint32_t)nc + (uint32_t)vc;
                 for (uint32_t p = col_pages[2 * k]; p < col_pages[2 * k + 1]; p++)
-                    if (pages[p].kind == 1) pages[p].dict_ids = (uint64_t)(uintptr_t)(ids + eb);
+                    if (pages[p].kind == 1) {
+                        pages[p].dict_ids = (uint64_t)(uintptr_t)(ids + eb);
+                        pages[p].dict_match = match ? (uint64_t)(uintptr_t)(match + eb) : 0;
+                    }
                 if (ch.dict_off >= 0) eb += ch.dict_n;
             }
         }
         if ((s = grow(S->pages, S->pages_cap, pages.size() * sizeof(DPage) + 16)) ||
             (s = grow(S->runs, S->runs_cap, (size_t)run_total * sizeof(DRun) + 16)) ||
-            (s = grow(S->page_runs, S->page_runs_cap, pages.size() * 8 + 16)) ||
-            (s = grow(S->dict_pages, S->dict_pages_cap, dict_pages.size() * 4 + 16)))
+            (s = grow(S->page_runs, S->page_runs_cap, pages.size() * PQ_PR * 4 + 16)) ||
+            (s = grow(S->dict_pages, S->dict_pages_cap, jobs.size() * sizeof(RunJob) + 16)))
             return s;
         GB_CUDA(cudaMemcpyAsync(S->pages, pages.data(), pages.size() * sizeof(DPage), cudaMemcpyHostToDevice, st));
-        if (!dict_pages.empty()) {
-            GB_CUDA(cudaMemcpyAsync(S->dict_pages, dict_pages.data(), dict_pages.size() * 4, cudaMemcpyHostToDevice,
+        GB_CUDA(cudaMemsetAsync(S->page_runs, 0, pages.size() * PQ_PR * 4 + 16, st));
+        if (!jobs.empty()) {
+            GB_CUDA(cudaMemcpyAsync(S->dict_pages, jobs.data(), jobs.size() * sizeof(RunJob), cudaMemcpyHostToDevice,
                                     st));
             gb_prof_mark *pm = gb_agg_prof_begin(h, "k_pq_runs", st);
-            k_pq_runs<<<(unsigned)dict_pages.size(), 128, 0, st>>>(dfile, (const DPage *)S->pages,
-                                                                   (const uint32_t *)S->dict_pages, (DRun *)S->runs,
-                                                                   (uint32_t *)S->page_runs, dctl);
+            k_pq_runs<<<(unsigned)jobs.size(), 128, 0, st>>>(dfile, (const DPage *)S->pages,
+                                                             (const RunJob *)S->dict_pages, (DRun *)S->runs,
+                                                             (uint32_t *)S->page_runs, dctl);
             gb_agg_prof_end(h, pm, st);
             GB_CUDA(cudaGetLastError());
             gb_agg_count_launch(h, 1);
@@ -1466,12 +1723,22 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
         }
         S->out_cap_rows = rows;
     }
+    // validity of the OPTIONAL columns' output (all ones; the scan clears NULLs)
+    const size_t vwords = (size_t)(rows + 63) / 64 + 1;
+    for (int c = 0; c < nc; c++) {
+        if (c == vc || f->cols[col_map[c]].repetition != 1) continue;
+        if ((s = grow(S->out_valid[c], S->out_valid_cap[c], vwords * 8))) return s;
+        GB_CUDA(cudaMemsetAsync(S->out_valid[c], 0xff, vwords * 8, st));
+    }
     PqScan P;
     memset(&P, 0, sizeof P);
     P.n_cols = nc;
+    P.id_col = vc;
+    P.str_match = SF.n ? 1 : 0;
     for (int c = 0; c < nc; c++) {
         P.out_type[c] = c == vc ? GB_T_BIGINT : v.col_types[c];  // VARCHAR: its string ids
         P.out[c] = S->out[c];
+        P.out_valid[c] = (c != vc && f->cols[col_map[c]].repetition == 1) ? (uint64_t *)S->out_valid[c] : nullptr;
     }
     P.n_filters = v.n_filters;
     for (int q = 0; q < v.n_filters; q++) P.filters[q] = v.filters[q];
@@ -1492,7 +1759,7 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
     if ((s = pq_fail_if_err(c))) return s;
     // the survivors go through the ordinary ingest (filters already applied)
     gb_col cols[GB_MAX_COLS];
-    for (int q = 0; q < nc; q++) cols[q] = {S->out[q], nullptr, nullptr};
+    for (int q = 0; q < nc; q++) cols[q] = {S->out[q], (const uint64_t *)P.out_valid[q], nullptr};
     if (vc >= 0) return gb_agg_ingest_prefiltered_ids(h, cols, c.out_count, (const int64_t *)S->out[vc], stream);
     return gb_agg_ingest_prefiltered(h, cols, c.out_count, stream);
 }

@@ -140,6 +140,7 @@ struct Query {
     std::vector<int32_t> col_types, group_cols;
     std::vector<gb_agg_desc> aggs;
     std::vector<gb_filter> filters;
+    std::vector<std::vector<uint8_t>> literals;  // the filters' IN sets / strings (the caller's may be gone)
     u64 nullable_mask = 0, est_groups = 0;
     u64 est_bytes = 0;
     bool done = false;
@@ -525,6 +526,14 @@ gb_status gb_server_submit(gb_server *s, uint32_t table_id, uint64_t row_begin, 
     q->group_cols.assign(spec->group_cols, spec->group_cols + spec->n_groups);
     q->aggs.assign(spec->aggs, spec->aggs + spec->n_aggs);
     if (spec->n_filters) q->filters.assign(spec->filters, spec->filters + spec->n_filters);
+    q->literals.resize(q->filters.size());
+    for (size_t i = 0; i < q->filters.size(); i++) {
+        gb_filter &f = q->filters[i];
+        if (f.op < GB_CMP_IN || !f.data) continue;
+        const size_t bytes = f.op == GB_CMP_IN ? f.n * sizeof(int64_t) : f.n;
+        q->literals[i].assign((const uint8_t *)f.data, (const uint8_t *)f.data + bytes);
+        f.data = q->literals[i].data();
+    }
     q->nullable_mask = spec->nullable_mask;
     q->est_groups = spec->est_groups;
     const gb_agg_spec sp = q->spec();

@@ -344,3 +344,35 @@ def test_varchar_dictionary_growth():
     """100K distinct strings into a dictionary sized for 16: retries + rehash."""
     (offs, data), s, m = datagen.varchar_table(400_000, 100_000, seed=33)
     check([VARCHAR, BIGINT, INTEGER], [0], [("count_star", -1), ("sum", 1)], [(offs, data), s, m], est_groups=16)
+
+
+@pytest.mark.parametrize("form", ["in", "str_eq", "str_ne", "like", "not_like", "like_empty", "in_and_like"])
+@pytest.mark.parametrize("device", [False, True])
+def test_in_list_and_varchar_predicates(form, device):
+    """The IN-list and VARCHAR predicate forms of the scan filter (=, <>,
+    LIKE '%x%', NOT LIKE) on a non-key VARCHAR column, and on a VARCHAR key."""
+    (offs, data), s, m = datagen.varchar_table(120_000, 4000, seed=9)
+    rng = np.random.default_rng(9)
+    k = rng.integers(0, 300, len(s)).astype(np.int32)
+    lit = bytes(data[offs[17]:offs[18]])
+    filters = {"in": [(0, "in", [3, 7, 11, 299, 1000, 7, -4])], "str_eq": [(1, "=", lit)],
+               "str_ne": [(1, "!=", lit)], "like": [(1, "like", b"ab")], "not_like": [(1, "not like", b"a")],
+               "like_empty": [(1, "like", b"")], "in_and_like": [(0, "in", [5, 6]), (1, "like", b"z")]}[form]
+    types = [INTEGER, capi.VARCHAR, BIGINT, INTEGER]
+    aggs = [("count_star", -1), ("sum", 2), ("max", 3)]
+    check(types, [0], aggs, [k, (offs, data), s, m], filters=filters, device=device)
+    # the same predicates with the VARCHAR column as the group key
+    check(types, [1], aggs, [k, (offs, data), s, m], filters=filters, device=device)
+
+
+def test_in_list_radix_and_nulls():
+    """IN on the radix path (generic partition pass) and NULLs in the IN
+    column (a NULL row never passes)."""
+    k, x = datagen.zipf(1_000_000, seed=5, n_values=300_000)
+    rng = np.random.default_rng(10)
+    tag = rng.integers(0, 50, len(k)).astype(np.int16)
+    tn = rng.random(len(k)) < 0.05
+    aggs = [("count_star", -1), ("sum", 1)]
+    check([BIGINT, DOUBLE, SMALLINT], [0], aggs, [k, x, tag], filters=[(2, "in", [1, 2, 3, 40])],
+          est_groups=300_000, mode=RADIX, nulls=[None, None, tn])
+    check([BIGINT, DOUBLE, SMALLINT], [0], aggs, [k, x, tag], filters=[(2, "in", [])], mode=HASH)

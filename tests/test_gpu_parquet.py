@@ -14,12 +14,12 @@ pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("oracle_lib", "gblib")]
 
 
 def run_pq(data, col_types, col_map, group_cols, aggs, filters=(), est_groups=0, device=False, batches=1,
-           mode=0):
+           mode=0, nullable=()):
     pf = capi.ParquetFile(data)
     if device:
         pf.upload()
     g = capi.GroupBy(col_types, group_cols, aggs, filters=filters, est_groups=est_groups,
-                     options={"mode": mode} if mode else None)
+                     options={"mode": mode} if mode else None, nullable=nullable)
     try:
         nrg = pf.num_row_groups
         step = max(1, (nrg + batches - 1) // batches)
@@ -117,3 +117,85 @@ def test_varchar_dictionary_key():
             gpu = run_pq(data, types, [0, 1, 2], [0], aggs, filters=filters, est_groups=3000, device=device,
                          batches=batches)
             compare(gpu, orc)
+
+
+import os  # noqa: E402
+import sys  # noqa: E402
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+import make_pyarrow_files as paf  # noqa: E402
+
+
+@pytest.mark.parametrize("name", sorted(paf.CASES))
+def test_pyarrow_files_with_nulls(name):
+    """Files written by pyarrow (an independent writer: OPTIONAL columns with
+    definition levels, data page v1 and v2, its own page splits, dictionary
+    fallback to PLAIN pages; committed under tests/golden/) through the GPU
+    decoder: NULLs in the key, the filter column and the value columns,
+    against the oracle on the same logical columns."""
+    data = paf.load(name)
+    (key, f, v, x), nulls = paf.columns()
+    types = [INTEGER, SMALLINT, BIGINT, DOUBLE]
+    aggs = [("count_star", -1), ("count", 2), ("sum", 2), ("min", 2), ("max", 3), ("sum", 3), ("avg", 3)]
+    for filters in ([], [(1, "<", 500)], [(1, "in", [3, 5, 800])]):
+        orc = oracle.run_query(types, [0], aggs, [key, f, v, x], filters=filters, nulls=nulls)
+        for device in (False, True):
+            gpu = run_pq(data, types, [0, 1, 2, 3], [0], aggs, filters=filters, est_groups=2000, device=device,
+                         nullable=[0, 1, 2, 3])
+            compare(gpu, orc)
+
+
+def test_pyarrow_varchar_key_with_nulls():
+    """A pyarrow-written dictionary-encoded VARCHAR key with NULL keys (one
+    NULL group) and a nullable value column; a LIKE on the key."""
+    data = paf.load("pa_varchar_nulls")
+    _, names, v, kn, vn = paf.varchar_columns()
+    types = [capi.VARCHAR, BIGINT]
+    aggs = [("count_star", -1), ("count", 1), ("sum", 1)]
+    for filters in ([], [(0, "like", b"k001")]):
+        orc = oracle.run_query(types, [0], aggs, [names, v], filters=filters, nulls=[kn, vn])
+        for device in (False, True):
+            gpu = run_pq(data, types, [0, 1], [0], aggs, filters=filters, est_groups=1500, device=device,
+                         nullable=[0, 1])
+            compare(gpu, orc)
+
+
+def test_optional_column_must_be_declared_nullable():
+    pf = capi.ParquetFile(paf.load("pa_optional_nonnull"))
+    g = capi.GroupBy([INTEGER, BIGINT], [0], [("sum", 1)])
+    try:
+        with pytest.raises(capi.GbError) as e:
+            capi.ingest_parquet(g, pf, [0, 1])
+        assert "nullable" in str(e.value)
+    finally:
+        g.close()
+        pf.close()
+    # declared nullable, the same file aggregates (no NULLs in it)
+    k = np.arange(1000, dtype=np.int32) % 7
+    v = np.arange(1000, dtype=np.int64)
+    orc = oracle.run_query([INTEGER, BIGINT], [0], [("sum", 1)], [k, v])
+    compare(run_pq(paf.load("pa_optional_nonnull"), [INTEGER, BIGINT], [0, 1], [0], [("sum", 1)], nullable=[0, 1]),
+            orc)
+
+
+def test_parquet_in_list_and_key_string_predicates():
+    """IN on integer Parquet columns in the fused scan, and string
+    predicates on a dictionary-encoded VARCHAR key, tested once per
+    dictionary entry (a dictionary match table)."""
+    data, key, f, v = pq.filter_groupby_file(n_rows=400_000, row_group_rows=100_000, page_rows=16_384, n_dict=2048)
+    types = [INTEGER, SMALLINT, BIGINT]
+    aggs = [("sum", 2), ("count_star", -1)]
+    members = [int(x) for x in np.unique(key)[:40]] + [5, 6]
+    for filters in ([(1, "in", [1, 2, 3, 500, 999])], [(0, "in", members), (1, "<", 700)]):
+        orc = oracle.run_query(types, [0], aggs, [key, f.astype(np.int16), v], filters=filters)
+        for device in (False, True):
+            compare(run_pq(data, types, [0, 1, 2], [0], aggs, filters=filters, est_groups=2048, device=device), orc)
+    data, d, idx, f, v = pq.varchar_groupby_file(n_rows=200_000, row_group_rows=50_000, page_rows=8192)
+    names = pq.strings_of(d, idx)
+    types = [capi.VARCHAR, SMALLINT, BIGINT]
+    aggs = [("count_star", -1), ("sum", 2)]
+    for filters in ([(0, "like", b"ab")], [(0, "not like", b"a"), (1, "<", 500)], [(0, "=", d[3])],
+                    [(0, "!=", d[3]), (0, "like", b"")]):
+        orc = oracle.run_query(types, [0], aggs, [names, f.astype(np.int16), v], filters=filters)
+        for device in (False, True):
+            compare(run_pq(data, types, [0, 1, 2], [0], aggs, filters=filters, est_groups=3000, device=device), orc)

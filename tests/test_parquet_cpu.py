@@ -234,3 +234,62 @@ def test_unsigned_columns():
     pf = capi.ParquetFile(buf.getvalue())
     assert pf.columns() == [("a", capi.INTEGER), ("b", capi.INTEGER), ("c", 0), ("d", 0)]
     pf.close()
+
+
+def test_optional_columns_parse():
+    """pyarrow writes OPTIONAL columns (definition levels before the values,
+    page v1 and v2): the footer and page parser accepts them; a page whose
+    level length overruns the page is rejected."""
+    pa = pytest.importorskip("pyarrow")
+    pq_ = pytest.importorskip("pyarrow.parquet")
+    n = 5000
+    rng = np.random.default_rng(3)
+    v = pa.array(rng.integers(0, 100, n), type=pa.int64(), mask=rng.random(n) < 0.2)
+    for version in ("1.0", "2.0"):
+        buf = io.BytesIO()
+        pq_.write_table(pa.table({"k": pa.array(np.arange(n, dtype=np.int32) % 9), "v": v}), buf,
+                        compression="none", data_page_version=version, row_group_size=2000)
+        pf = capi.ParquetFile(buf.getvalue())
+        assert pf.columns() == [("k", capi.INTEGER), ("v", capi.BIGINT)]
+        assert pf.num_rows == n and pf.num_row_groups == 3
+        pf.close()
+    # page v1 of column v: overrun the 4-byte level length
+    buf = io.BytesIO()
+    pq_.write_table(pa.table({"v": v}), buf, compression="none", data_page_version="1.0", use_dictionary=False,
+                    write_statistics=False)
+    b = bytearray(buf.getvalue())
+    md = pq_.ParquetFile(io.BytesIO(bytes(b))).metadata.row_group(0).column(0)
+    start = md.data_page_offset
+    # the page header is followed by the 4-byte level length (5000 levels at
+    # bit width 1 take a little over 625 bytes)
+    found = False
+    for off in range(start + 4, start + 64):
+        ln = int.from_bytes(b[off:off + 4], "little")
+        if 625 <= ln <= 800:
+            b[off:off + 4] = (1 << 30).to_bytes(4, "little")
+            found = True
+            break
+    assert found
+    with pytest.raises(capi.GbError):
+        capi.ParquetFile(bytes(b))
+
+
+def test_pyarrow_fixtures_match_their_columns():
+    """The committed pyarrow files (tests/golden/*.parquet.gz) hold exactly
+    the columns and NULLs that make_pyarrow_files.columns() regenerates."""
+    pq_ = pytest.importorskip("pyarrow.parquet")
+    import os
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_pyarrow_files as paf
+    cols, nulls = paf.columns()
+    for name in paf.CASES:
+        t = pq_.read_table(io.BytesIO(paf.load(name)))
+        for i, c in enumerate(["key", "f", "v", "x"]):
+            col = t.column(c)
+            assert np.array_equal(col.is_null().to_numpy(zero_copy_only=False), nulls[i])
+            ok = ~nulls[i]
+            assert np.array_equal(col.to_numpy(zero_copy_only=False)[ok].astype(cols[i].dtype), cols[i][ok])
+        pf = capi.ParquetFile(paf.load(name))
+        assert pf.columns() == [("key", capi.INTEGER), ("f", capi.SMALLINT), ("v", capi.BIGINT), ("x", capi.DOUBLE)]
+        pf.close()

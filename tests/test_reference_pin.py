@@ -125,6 +125,31 @@ def test_parquet_filter_groupby_project_writer_file():
               filters=[(1, "<", 100)], ref_file=path)
 
 
+def test_parquet_optional_columns_with_nulls():
+    """pyarrow OPTIONAL columns with NULL values (definition levels), read by
+    the reference's own Parquet reader, against the oracle with the same
+    NULLs: COUNT(col) skips them, SUM/MIN/MAX of an all-NULL group are NULL."""
+    pa = pytest.importorskip("pyarrow")
+    pq = pytest.importorskip("pyarrow.parquet")
+    rng = np.random.default_rng(33)
+    n = 300_000
+    key = rng.integers(0, 3000, n).astype(np.int32)
+    v = rng.integers(-10**6, 10**6, n, dtype=np.int64)
+    x = rng.normal(20, 4, n)
+    vn = rng.random(n) < 0.15
+    vn[key == 11] = True
+    xn = rng.random(n) < 0.05
+    tbl = pa.table({"key": pa.array(key, pa.int32()), "v": pa.array(v, pa.int64(), mask=vn),
+                    "x": pa.array(x, pa.float64(), mask=xn)})
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "t.parquet")
+        pq.write_table(tbl, path, row_group_size=100_000, compression="NONE", data_page_size=64 * 1024)
+        check("SELECT \"key\", COUNT(*), COUNT(v), SUM(v), MIN(v), MAX(v), SUM(x), AVG(x) FROM '{file}' GROUP BY \"key\"",
+              [INTEGER, BIGINT, DOUBLE], [0],
+              [("count_star", -1), ("count", 1), ("sum", 1), ("min", 1), ("max", 1), ("sum", 2), ("avg", 2)],
+              [key, v, x], nulls=[None, vn, xn], ref_file=path)
+
+
 def test_composite_key_500k_rows():
     """(INT32, SMALLINT) key, COUNT/SUM(INT64)/MAX(INT32) — the batched
     workload's composite shape."""
@@ -155,6 +180,31 @@ def test_scan_filter_ops(op):
     sql = "SELECT c0, COUNT(*), SUM(c2), MIN(c1) FROM t WHERE c1 %s 37 AND c2 %s 5.25 GROUP BY c0" % (op, op)
     check(sql, [INTEGER, INTEGER, DOUBLE], [0], [("count_star", -1), ("sum", 2), ("min", 1)], [k, f, x],
           filters=[(1, op, 37), (2, op, 5.25)])
+
+
+@pytest.mark.parametrize("form", ["in", "str_eq", "str_ne", "like", "not_like", "like_empty", "in_empty_str"])
+def test_scan_filter_in_and_varchar_forms(form):
+    """The other SimplePredicate forms (physical_planner.cpp:110-135,
+    396-496): an integer IN list, VARCHAR = / <> a literal, LIKE '%x%' and
+    NOT LIKE '%x%' (LIKE '%%' matches every string)."""
+    (offs, data), s_, m = datagen.varchar_table(60_000, 3000, seed=8)
+    rng = np.random.default_rng(8)
+    k = rng.integers(0, 300, len(s_)).astype(np.int32)
+    strs = [bytes(data[offs[i]:offs[i + 1]]) for i in range(len(s_))]
+    lit = strs[17]
+    cases = {
+        "in": ("c0 IN (3, 7, 11, 299, 1000, 7)", [(0, "in", [3, 7, 11, 299, 1000, 7])]),
+        "str_eq": ("c1 = '%s'" % lit.decode(), [(1, "=", lit)]),
+        "str_ne": ("c1 <> '%s'" % lit.decode(), [(1, "!=", lit)]),
+        "like": ("c1 LIKE '%ab%'", [(1, "like", b"ab")]),
+        "not_like": ("c1 NOT LIKE '%a%'", [(1, "not like", b"a")]),
+        "like_empty": ("c1 LIKE '%%'", [(1, "like", b"")]),
+        "in_empty_str": ("c0 IN (5) AND c1 LIKE '%z%'", [(0, "in", [5]), (1, "like", b"z")]),
+    }
+    where, filters = cases[form]
+    check("SELECT c0, COUNT(*), SUM(c2), MAX(c3) FROM t WHERE %s GROUP BY c0" % where,
+          [INTEGER, VARCHAR, BIGINT, INTEGER], [0], [("count_star", -1), ("sum", 2), ("max", 3)],
+          [k, (offs, data), s_, m], filters=filters)
 
 
 def test_nullable_values_and_empty_sums():
