@@ -182,10 +182,27 @@ def run_query(col_types, group_cols, aggs, cols, filters=(), nulls=None, nthread
             knull = kn.astype(np.uint8)
             inv = None
         else:
+            # a VARCHAR column of a pair key groups by its bytes: dense codes
+            # per distinct string (the reference's concatenated group key,
+            # physical_planner.cpp:6185-6206, compares the bytes)
+            pair = []
+            strings = {}
+            for j, g in enumerate(group_cols):
+                if col_types[g] == VARCHAR:
+                    offs, data = cols[g]
+                    code_of = {}
+                    codes = np.empty(n, dtype=np.int64)
+                    for r in range(n):
+                        s_ = bytes(data[offs[r]:offs[r + 1]])
+                        codes[r] = code_of.setdefault(s_, len(code_of))
+                    strings[j] = np.array(list(code_of.keys()) + [b""], dtype=object)
+                    pair.append(codes)
+                else:
+                    pair.append(cols[g])
             rec = np.empty(n, dtype=[("a", np.int64), ("na", np.bool_), ("b", np.int64), ("nb", np.bool_)])
-            rec["a"] = np.where(kn_list[0], 0, cols[group_cols[0]])
+            rec["a"] = np.where(kn_list[0], 0, pair[0])
             rec["na"] = kn_list[0]
-            rec["b"] = np.where(kn_list[1], 0, cols[group_cols[1]])
+            rec["b"] = np.where(kn_list[1], 0, pair[1])
             rec["nb"] = kn_list[1]
             uniq, inv = np.unique(rec, return_inverse=True)
             packed = inv.astype(np.int64).reshape(-1)
@@ -204,7 +221,12 @@ def run_query(col_types, group_cols, aggs, cols, filters=(), nulls=None, nthread
             key_null = [out_key_null[:ng].astype(bool)]
         else:
             u = uniq[out_keys[:ng]]
-            keys = [u["a"].astype(NP_TYPES[key_types[0]]), u["b"].astype(NP_TYPES[key_types[1]])]
+            keys = []
+            for j, f in enumerate(("a", "b")):
+                if j in strings:
+                    keys.append(strings[j][np.where(u["n" + f], len(strings[j]) - 1, u[f])])
+                else:
+                    keys.append(u[f].astype(NP_TYPES[key_types[j]]))
             key_null = [u["na"].astype(bool), u["nb"].astype(bool)]
     out_aggs = []
     out_types = list(key_types)

@@ -1303,14 +1303,20 @@ static gb_status strdict_encode(gb_agg *h, const uint8_t *bytes, const int64_t *
     return GB_ERR_OOM;
 }
 
-// Turn the emitted ids of a VARCHAR key column into offsets + bytes.
+// The output column of the VARCHAR key.
+static int str_out_col(const gb_agg *h) { return h->plan.key_mode == KEY_STRING ? 0 : std::max(0, h->plan.str_key); }
+
+// Turn the emitted ids of a VARCHAR key column into offsets + bytes (a
+// negative id, the NULL string of a pair key, becomes NULL).
 static gb_status strdict_emit(gb_agg *h, const long long *ids, u64 n, cudaStream_t st) {
     gb_status s;
     if ((s = h->str_lens.ensure(n * 8 + 8)) || (s = h->out_str_offs.ensure(n * 8 + 16)) ||
         (s = h->scan_tmp.ensure(((n + 1023) / 1024 + 1) * 8)))
         return s;
     StrDictRef D = strdict_ref(h);
-    if ((s = strdict_launch_lengths(D, ids, n, (int64_t *)h->str_lens.p, st))) return s;
+    if ((s = strdict_launch_lengths(D, ids, n, (int64_t *)h->str_lens.p, st,
+                                    (uint64_t *)h->out_valid[str_out_col(h)].p)))
+        return s;
     int64_t total = 0;
     if ((s = device_exclusive_scan((const int64_t *)h->str_lens.p, (int64_t *)h->out_str_offs.p, n,
                                    (int64_t *)h->scan_tmp.p, st, &total)))
@@ -1445,9 +1451,32 @@ static gb_status compile_plan(gb_agg *h) {
             P.key_type[0] = GB_T_BIGINT;
         }
     } else {
-        if (P.key_type[0] == GB_T_VARCHAR || P.key_type[1] == GB_T_VARCHAR) {
-            set_error("VARCHAR in a two-column key is not supported on the GPU path");
+        P.str_key = -1;
+        const bool s0 = P.key_type[0] == GB_T_VARCHAR, s1 = P.key_type[1] == GB_T_VARCHAR;
+        if (s0 && s1) {
+            set_error("two VARCHAR columns in one key are not supported on the GPU path");
             return GB_ERR_UNSUPPORTED;
+        }
+        if (s0 || s1) {
+            // (int, varchar): the string column becomes 32-bit dense ids on a
+            // hidden BIGINT column, packed beside the integer key
+            // (RadixCount2ColIntStr, radix_count_agg.cpp:767-1358, keys the
+            // pair by its string's hash; here by its dictionary id)
+            const int pos = s0 ? 0 : 1;
+            const int other = P.key_type[1 - pos];
+            if (other != GB_T_SMALLINT && other != GB_T_INTEGER) {
+                set_error("a VARCHAR pair key needs a SMALLINT or INTEGER partner on the GPU path");
+                return GB_ERR_UNSUPPORTED;
+            }
+            if (nc + 1 > GB_MAX_COLS) {
+                set_error("too many columns for a VARCHAR key (max %d)", GB_MAX_COLS - 1);
+                return GB_ERR_UNSUPPORTED;
+            }
+            h->str_col = P.key_col[pos];
+            P.cols[nc].type = GB_T_BIGINT;
+            P.key_col[pos] = nc;
+            P.key_type[pos] = GB_T_INTEGER;
+            P.str_key = pos;
         }
         int ba = type_bits(P.key_type[0]), bb = type_bits(P.key_type[1]);
         if (ba + bb + 2 <= 64) {
@@ -1482,7 +1511,8 @@ static gb_status compile_plan(gb_agg *h) {
     };
     h->emit.clear();
     h->out_types.clear();
-    for (int i = 0; i < ng; i++) h->out_types.push_back(P.key_mode == KEY_STRING ? GB_T_VARCHAR : P.key_type[i]);
+    for (int i = 0; i < ng; i++)
+        h->out_types.push_back((P.key_mode == KEY_STRING || (ng == 2 && P.str_key == i)) ? GB_T_VARCHAR : P.key_type[i]);
     if (h->aggs.empty() || h->aggs.size() > GB_MAX_AGGS) {
         set_error("need 1..%d aggregates", GB_MAX_AGGS);
         return GB_ERR_INVALID;
@@ -1563,7 +1593,7 @@ static gb_status compile_plan(gb_agg *h) {
     // the NULL-key group of a nullable BIGINT key has no spare key value
     h->dist_null_sets = P.n_dist && P.key_mode == KEY_SINGLE && P.key_type[0] == GB_T_BIGINT &&
                         ((h->nullable_mask >> P.key_col[0]) & 1ull);
-    if (P.key_mode == KEY_STRING) P.n_cols = nc + 1;
+    if (h->str_col >= 0) P.n_cols = nc + 1;
     {
         int need = words + 1;
         int stride = need <= 4 ? (int)next_pow2(need) : ((need + 3) / 4) * 4;
@@ -1971,7 +2001,7 @@ gb_status gb_agg_finalize(gb_agg *h, void *stream) {
     if (h->str_col >= 0) {
         // VARCHAR keys: the TopN hint is not applied (the ORDER BY above sorts
         // the full result); ids become offsets + bytes
-        if ((s = strdict_emit(h, (const long long *)h->out_cols[0].p, h->n_rows_out, st))) return s;
+        if ((s = strdict_emit(h, (const long long *)h->out_cols[str_out_col(h)].p, h->n_rows_out, st))) return s;
     } else if (h->topn && h->topn_limit > 0 && h->topn_limit <= 1024 && h->n_rows_out > 0) {
         if ((s = run_topn(h, st))) return s;
     }

@@ -983,6 +983,13 @@ gb_status gb_batch_add(gb_batch *b, const gb_agg_spec *spec, const gb_col *cols,
             set_error("COUNT(DISTINCT) runs on its own handle (gb_agg_*), not in a batch");
             return GB_ERR_UNSUPPORTED;
         }
+    if (spec->n_groups == 2 && spec->group_cols && spec->col_types)
+        for (uint32_t g = 0; g < 2; g++)
+            if (spec->group_cols[g] >= 0 && (uint32_t)spec->group_cols[g] < spec->n_cols &&
+                spec->col_types[spec->group_cols[g]] == GB_T_VARCHAR) {
+                set_error("a VARCHAR in a pair key runs on its own handle (gb_agg_*), not in a batch");
+                return GB_ERR_UNSUPPORTED;
+            }
     // a table never has more groups than rows: size it for min(estimate, rows)
     gb_agg_spec sp = *spec;
     const u64 est = sp.est_groups ? sp.est_groups : (1u << 15);

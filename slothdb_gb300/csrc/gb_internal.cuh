@@ -100,6 +100,7 @@ struct Plan {
     int32_t words;        // state words (word 0 = row count)
     int32_t stride;       // words per table slot incl. key, power of two
     int32_t n_dist;       // OP_DIST ops (COUNT(DISTINCT) columns)
+    int32_t str_key;      // a pair key's VARCHAR position (its 32-bit string ids are packed), -1: none
     uint64_t word_init[GB_MAX_WORDS];
     // COUNT(DISTINCT): per OP_DIST op a set of (group key, value) pairs,
     // 16-byte slots of which dmask + 1 per set; the NULL-key group of a

@@ -401,13 +401,14 @@ __device__ __forceinline__ void emit_group(const Plan &P, const EmitArgs &E, u64
         const int bb = P.key_bits_b, ba = P.key_bits_a;
         i64 a = sext(pk >> bb, ba), b = sext(pk, bb);
         bool na = (pk >> (ba + bb)) & 1ull, nb = (pk >> (ba + bb + 1)) & 1ull;
-        store_int(E.out[0], P.key_type[0], o, a);
-        store_int(E.out[1], P.key_type[1], o, b);
+        // a VARCHAR position holds its string id, emitted as BIGINT
+        store_int(E.out[0], P.str_key == 0 ? GB_T_BIGINT : P.key_type[0], o, a);
+        store_int(E.out[1], P.str_key == 1 ? GB_T_BIGINT : P.key_type[1], o, b);
         if (na) clear_valid(E.valid[0], o);
         if (nb) clear_valid(E.valid[1], o);
     } else {
-        store_int(E.out[0], P.key_type[0], o, (i64)(int32_t)(uint32_t)(pk >> 32));
-        store_int(E.out[1], P.key_type[1], o, (i64)(int32_t)(uint32_t)pk);
+        store_int(E.out[0], P.str_key == 0 ? GB_T_BIGINT : P.key_type[0], o, (i64)(int32_t)(uint32_t)(pk >> 32));
+        store_int(E.out[1], P.str_key == 1 ? GB_T_BIGINT : P.key_type[1], o, (i64)(int32_t)(uint32_t)pk);
     }
     for (int a = 0; a < E.n_aggs; a++) {
         const EmitAgg &g = E.aggs[a];

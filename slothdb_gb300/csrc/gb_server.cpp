@@ -150,9 +150,14 @@ struct Query {
     u64 t_submit = 0, t_start = 0, t_done = 0;
     uint32_t batch_size = 0;
 
+    // queries the batch kernels do not take (COUNT(DISTINCT), a VARCHAR in a
+    // pair key) run alone on their own handle
     bool distinct() const {
         for (const gb_agg_desc &a : aggs)
             if (a.kind == GB_AGG_COUNT_DISTINCT) return true;
+        if (group_cols.size() == 2)
+            for (int32_t g : group_cols)
+                if (col_types[g] == GB_T_VARCHAR) return true;
         return false;
     }
 

@@ -81,10 +81,11 @@ __global__ void k_strdict_rehash(const u64 *old_hash, const u64 *old_ref, const 
 }
 
 // Output strings of ids[0, n): lengths first (for the offsets scan), then bytes.
-__global__ void k_strdict_lengths(const StrDictRef D, const long long *ids, u64 n, int64_t *lens) {
+__global__ void k_strdict_lengths(const StrDictRef D, const long long *ids, u64 n, int64_t *lens, uint64_t *valid) {
     for (u64 i = blockIdx.x * (u64)blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x) {
         const long long id = ids[i];
         lens[i] = id < 0 ? 0 : (int64_t)(D.ref_by_id[id] & 0xffffffu);
+        if (id < 0 && valid) atomicAnd((unsigned long long *)&valid[i >> 6], ~(1ull << (i & 63)));  // NULL string
     }
 }
 
@@ -189,9 +190,10 @@ gb_status device_exclusive_scan(const int64_t *lens, int64_t *offs, u64 n, int64
     return GB_OK;
 }
 
-gb_status strdict_launch_lengths(const StrDictRef &D, const long long *ids, u64 n, int64_t *lens, cudaStream_t st) {
+gb_status strdict_launch_lengths(const StrDictRef &D, const long long *ids, u64 n, int64_t *lens, cudaStream_t st,
+                                 uint64_t *valid) {
     if (!n) return GB_OK;
-    k_strdict_lengths<<<grid_n(n, 256, sm_count() * 8), 256, 0, st>>>(D, ids, n, lens);
+    k_strdict_lengths<<<grid_n(n, 256, sm_count() * 8), 256, 0, st>>>(D, ids, n, lens, valid);
     GB_CUDA(cudaGetLastError());
     return GB_OK;
 }

@@ -312,7 +312,8 @@ gb_status strdict_launch_encode(const StrDictRef &D, const uint8_t *bytes, const
 gb_status strdict_launch_rehash(const u64 *old_hash, const u64 *old_ref, const u64 *old_id, u64 old_cap,
                                 const StrDictRef &D, cudaStream_t st);
 gb_status strdict_fill(u64 *p, u64 n, u64 v, cudaStream_t st);
-gb_status strdict_launch_lengths(const StrDictRef &D, const long long *ids, u64 n, int64_t *lens, cudaStream_t st);
+gb_status strdict_launch_lengths(const StrDictRef &D, const long long *ids, u64 n, int64_t *lens, cudaStream_t st,
+                                 uint64_t *valid = nullptr);
 gb_status strdict_launch_gather(const StrDictRef &D, const long long *ids, u64 n, const int64_t *offs, uint8_t *out,
                                 cudaStream_t st);
 gb_status device_exclusive_scan(const int64_t *lens, int64_t *offs, u64 n, int64_t *tmp, cudaStream_t st,

@@ -376,3 +376,29 @@ def test_in_list_radix_and_nulls():
     check([BIGINT, DOUBLE, SMALLINT], [0], aggs, [k, x, tag], filters=[(2, "in", [1, 2, 3, 40])],
           est_groups=300_000, mode=RADIX, nulls=[None, None, tn])
     check([BIGINT, DOUBLE, SMALLINT], [0], aggs, [k, x, tag], filters=[(2, "in", [])], mode=HASH)
+
+
+@pytest.mark.parametrize("other", [INTEGER, SMALLINT])
+@pytest.mark.parametrize("order", ["int_str", "str_int"])
+@pytest.mark.parametrize("device", [False, True])
+def test_int_varchar_pair_key(other, order, device):
+    """(INTEGER or SMALLINT, VARCHAR) pair keys: the string becomes a 32-bit
+    dictionary id packed beside the integer; NULL strings form their own
+    groups, and with a SMALLINT partner NULL integers too."""
+    (offs, data), s, m = datagen.varchar_table(150_000, 2000, seed=13)
+    rng = np.random.default_rng(13)
+    k = rng.integers(-60, 60, len(s)).astype(np.int32 if other == INTEGER else np.int16)
+    sn = rng.random(len(s)) < 0.02
+    kn = (rng.random(len(s)) < 0.03) if other == SMALLINT else None
+    groups = [0, 1] if order == "int_str" else [1, 0]
+    types = [other, capi.VARCHAR, BIGINT, INTEGER]
+    aggs = [("count_star", -1), ("sum", 2), ("max", 3)]
+    check(types, groups, aggs, [k, (offs, data), s, m], nulls=[kn, sn, None, None], device=device,
+          filters=[(1, "not like", b"q")])
+
+
+def test_int_varchar_pair_key_radix():
+    (offs, data), s, m = datagen.varchar_table(400_000, 150_000, seed=14)
+    k = np.random.default_rng(14).integers(0, 8, len(s)).astype(np.int16)
+    check([SMALLINT, capi.VARCHAR, BIGINT, INTEGER], [0, 1], [("count_star", -1), ("sum", 2)],
+          [k, (offs, data), s, m], est_groups=1_200_000, mode=RADIX)

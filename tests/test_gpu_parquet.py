@@ -199,3 +199,16 @@ def test_parquet_in_list_and_key_string_predicates():
         orc = oracle.run_query(types, [0], aggs, [names, f.astype(np.int16), v], filters=filters)
         for device in (False, True):
             compare(run_pq(data, types, [0, 1, 2], [0], aggs, filters=filters, est_groups=3000, device=device), orc)
+
+
+def test_parquet_int_varchar_pair_key():
+    """(SMALLINT, VARCHAR) pair key from a Parquet file: the dictionary
+    strings become ids once per batch, packed beside the integer key."""
+    data, d, idx, f, v = pq.varchar_groupby_file(n_rows=150_000, row_group_rows=50_000, page_rows=8192, n_dict=300)
+    names = pq.strings_of(d, idx)
+    types = [capi.VARCHAR, SMALLINT, BIGINT]
+    aggs = [("count_star", -1), ("sum", 2)]
+    orc = oracle.run_query(types, [1, 0], aggs, [names, f.astype(np.int16), v], filters=[(1, "<", 20)])
+    for device in (False, True):
+        compare(run_pq(data, types, [0, 1, 2], [1, 0], aggs, filters=[(1, "<", 20)], est_groups=6000, device=device),
+                orc)

@@ -207,6 +207,21 @@ def test_scan_filter_in_and_varchar_forms(form):
           [k, (offs, data), s_, m], filters=filters)
 
 
+@pytest.mark.parametrize("order", ["int_str", "str_int"])
+def test_int_varchar_pair_key(order):
+    """An (INTEGER, VARCHAR) pair key — the shape of RadixCount2ColIntStr
+    (radix_count_agg.cpp:767-1358) — in both column orders."""
+    (offs, data), s_, m = datagen.varchar_table(80_000, 600, seed=12)
+    rng = np.random.default_rng(12)
+    k = rng.integers(0, 40, len(s_)).astype(np.int32)
+    if order == "int_str":
+        sql, groups = "SELECT c0, c1, COUNT(*), SUM(c2), MAX(c3) FROM t GROUP BY c0, c1", [0, 1]
+    else:
+        sql, groups = "SELECT c1, c0, COUNT(*), SUM(c2), MAX(c3) FROM t GROUP BY c1, c0", [1, 0]
+    check(sql, [INTEGER, VARCHAR, BIGINT, INTEGER], groups, [("count_star", -1), ("sum", 2), ("max", 3)],
+          [k, (offs, data), s_, m])
+
+
 def test_nullable_values_and_empty_sums():
     """NULLs in the value columns: COUNT(col) skips them, SUM/AVG/MIN/MAX of
     a group whose values are all NULL are NULL (agg_emit_helpers.cpp).
