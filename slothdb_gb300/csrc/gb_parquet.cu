@@ -147,6 +147,15 @@ struct PqPage {
     uint64_t off;        // offset of the encoded values in the file
     uint64_t def_off = 0;    // OPTIONAL column: its definition levels (RLE/bit-packed, bit width 1)
     uint32_t def_bytes = 0;  // 0: REQUIRED column (no levels)
+    // a page of a compressed (SNAPPY) column chunk: where its bytes are in the
+    // file; off / def_off above are then offsets in the batch's decompressed
+    // image (set per batch)
+    uint64_t src_off = 0;    // compressed values (page v1: the whole payload)
+    uint32_t src_bytes = 0;
+    uint32_t raw_bytes = 0;  // their uncompressed size
+    uint32_t lvl_copy = 0;   // page v2: level bytes stored uncompressed before them
+    uint8_t lvl_pending = 0; // page v1 of an OPTIONAL column: the level length is inside the compressed bytes
+    uint8_t stored = 0;      // page v2 with is_compressed = false: values copied, not inflated
 };
 
 struct PqChunk {
@@ -155,7 +164,9 @@ struct PqChunk {
     int32_t codec = 0;
     int64_t dict_off = -1;  // dictionary payload offset (-1 = none)
     uint32_t dict_n = 0;
-    uint32_t dict_bytes = 0;  // dictionary payload bytes
+    uint32_t dict_bytes = 0;  // dictionary payload bytes (uncompressed)
+    uint64_t dict_src = 0;    // compressed chunk: the dictionary page's compressed bytes in the file
+    uint32_t dict_src_bytes = 0;
     // column statistics (zone map): raw min / max bytes, Statistics fields
     // 5/6 (min_value/max_value) over the deprecated 2/1 (min/max)
     bool has_stats = false;
@@ -180,6 +191,7 @@ struct gb_pq_file {
     std::vector<std::vector<PqChunk>> chunks;  // [rg][col]
     std::vector<PqPage> pages;
     uint64_t num_rows = 0;
+    bool compressed = false;  // some column chunk is SNAPPY-compressed
     void *dev = nullptr;  // device copy of the file (gb_pq_upload)
     // page index of the uploaded file, built on the GPU by the first
     // device-resident scan and kept with the file (like Parquet's offset
@@ -347,9 +359,11 @@ static gb_status parse_pages(gb_pq_file *f, uint32_t rg, uint32_t col) {
         TReader r(f->host, end, pos);
         int fid, type, last = 0;
         int ptype = -1, enc = -1, version = 0;
-        int64_t csize = -1, nvals = -1, dict_n = -1, def_len = 0, rep_len = 0;
+        int64_t csize = -1, usize = -1, nvals = -1, dict_n = -1, def_len = 0, rep_len = 0;
+        bool v2_compressed = true;
         while (r.field(fid, type, last)) {
             if (fid == 1 && type == 5) ptype = (int)r.zz();
+            else if (fid == 2 && type == 5) usize = r.zz();
             else if (fid == 3 && type == 5) csize = r.zz();
             else if ((fid == 5 || fid == 8) && type == 12) {  // data page v1 / v2
                 version = fid == 5 ? 1 : 2;
@@ -360,6 +374,7 @@ static gb_status parse_pages(gb_pq_file *f, uint32_t rg, uint32_t col) {
                     else if (fid == 8 && f2 == 4 && t2 == 5) enc = (int)r.zz();
                     else if (fid == 8 && f2 == 5 && t2 == 5) def_len = r.zz();
                     else if (fid == 8 && f2 == 6 && t2 == 5) rep_len = r.zz();
+                    else if (fid == 8 && f2 == 7 && (t2 == 1 || t2 == 2)) v2_compressed = t2 == 1;  // is_compressed
                     else r.skip(t2);
                 }
                 if (rep_len || (def_len && !opt)) {
@@ -376,11 +391,20 @@ static gb_status parse_pages(gb_pq_file *f, uint32_t rg, uint32_t col) {
         }
         if (r.bad || csize < 0 || r.pos + (uint64_t)csize > end) return pq_corrupt("page header");
         const uint64_t payload = r.pos;
+        const uint64_t next_page = payload + (uint64_t)csize;
+        const bool comp = ch.codec != 0;
+        if (comp && (usize < 0 || usize > (int64_t)0x7fffffff)) return pq_corrupt("uncompressed page size");
         if (ptype == 2) {
             if (dict_n < 0) return pq_corrupt("dictionary page header");
             ch.dict_off = (int64_t)payload;
             ch.dict_n = (uint32_t)dict_n;
             ch.dict_bytes = (uint32_t)csize;
+            if (comp) {  // decompressed into the batch's image; its offset is set there
+                ch.dict_src = payload;
+                ch.dict_src_bytes = (uint32_t)csize;
+                ch.dict_bytes = (uint32_t)usize;
+                csize = usize;  // the checks below bound the uncompressed values
+            }
             if ((uint64_t)dict_n * f->cols[col].width > (uint64_t)csize) return pq_corrupt("dictionary size");
             // BYTE_ARRAY: a 4-byte length before every value
             if (f->cols[col].gtype == GB_T_VARCHAR && (uint64_t)dict_n * 4 > (uint64_t)csize)
@@ -394,7 +418,23 @@ static gb_status parse_pages(gb_pq_file *f, uint32_t rg, uint32_t col) {
             pg.n_values = (uint32_t)nvals;
             pg.bytes = (uint32_t)csize;
             pg.off = payload;
-            if (opt) {
+            if (comp) {
+                // page v1: levels and values are compressed together; page v2:
+                // its levels are stored as is, then the (compressed) values
+                const uint64_t lv = version == 2 ? (uint64_t)def_len : 0;
+                if (lv > (uint64_t)csize || (version == 2 && (uint64_t)usize < lv)) return pq_corrupt("page sizes");
+                pg.lvl_copy = (uint32_t)lv;
+                pg.src_off = payload + lv;
+                pg.src_bytes = (uint32_t)((uint64_t)csize - lv);
+                pg.raw_bytes = (uint32_t)((uint64_t)usize - lv);
+                pg.stored = version == 2 && !v2_compressed;
+                if (pg.stored && pg.src_bytes != pg.raw_bytes) return pq_corrupt("page sizes");
+                pg.lvl_pending = opt && version == 1;
+                pg.def_bytes = (uint32_t)lv;  // v1 OPTIONAL: known once inflated
+                if (opt && version == 2 && lv == 0 && nvals > 0) return pq_corrupt("definition levels");
+                pg.bytes = pg.raw_bytes;  // values bytes (v1 OPTIONAL: less its levels, set per batch)
+                csize = usize;
+            } else if (opt) {
                 uint64_t lv;
                 if (version == 1) {
                     if (csize < 4) return pq_corrupt("definition levels");
@@ -429,7 +469,7 @@ static gb_status parse_pages(gb_pq_file *f, uint32_t rg, uint32_t col) {
             f->pages.push_back(pg);
             row += (uint32_t)nvals;
         }
-        pos = payload + (uint64_t)csize;
+        pos = next_page;
     }
     ch.page_end = (uint32_t)f->pages.size();
     if (row != f->rg_rows[rg]) return pq_corrupt("page values do not add up to the row group");
@@ -1177,16 +1217,27 @@ static bool pq_rg_might_match(const gb_pq_file *f, uint32_t rg, int fcol, const 
 // Page descriptors of row groups [rg_begin, rg_end) and the given file
 // columns (offsets relative to `base`), with run-table slots for the
 // dictionary pages; col_pages gets one {begin, end} pair per (rg, column).
-static gb_status pq_page_table(const gb_pq_file *f, uint32_t rg_begin, uint32_t rg_end, const int32_t *cols, int nc,
-                               uint64_t base, std::vector<DPage> &pages, std::vector<RunJob> &jobs,
+// The page metadata a batch decodes from: the file's own, or a copy whose
+// offsets point into the batch's decompressed image.
+struct PqView {
+    const std::vector<std::vector<PqChunk>> *chunks;
+    const std::vector<PqPage> *pages;
+};
+
+// Row groups a batch skips (zone maps) get empty page ranges: none of their
+// bytes is read.
+static gb_status pq_page_table(const gb_pq_file *f, const PqView &V, uint32_t rg_begin, uint32_t rg_end,
+                               const int32_t *cols, int nc, uint64_t base, const std::vector<char> *live,
+                               std::vector<DPage> &pages, std::vector<RunJob> &jobs,
                                std::vector<uint32_t> &col_pages, uint32_t &run_total) {
     for (uint32_t g = rg_begin; g < rg_end; g++) {
+        const bool skip = live && !(*live)[g - rg_begin];
         for (int c = 0; c < nc; c++) {
-            const PqChunk &ch = f->chunks[g][cols[c]];
+            const PqChunk &ch = (*V.chunks)[g][cols[c]];
             const PqColumn &pc = f->cols[cols[c]];
             col_pages.push_back((uint32_t)pages.size());
-            for (uint32_t p = ch.page_begin; p < ch.page_end; p++) {
-                const PqPage &pp = f->pages[p];
+            for (uint32_t p = ch.page_begin; p < ch.page_end && !skip; p++) {
+                const PqPage &pp = (*V.pages)[p];
                 DPage d{};
                 d.off = pp.off - base;
                 d.first_row = pp.first_row;
@@ -1237,8 +1288,8 @@ static gb_status pq_build_index(gb_pq_file *f, cudaStream_t st) {
     std::vector<RunJob> jobs;
     std::vector<uint32_t> col_pages;
     uint32_t run_total = 0;
-    gb_status s = pq_page_table(f, 0, (uint32_t)f->rg_rows.size(), all.data(), nfc, 0, pages, jobs, col_pages,
-                                run_total);
+    gb_status s = pq_page_table(f, PqView{&f->chunks, &f->pages}, 0, (uint32_t)f->rg_rows.size(), all.data(), nfc, 0,
+                                nullptr, pages, jobs, col_pages, run_total);
     if (s) return s;
     void *dp = nullptr, *ctl = nullptr;
     auto fail = [&](cudaError_t e, const char *what) {
@@ -1294,12 +1345,13 @@ gb_status gb_pq_open(const uint8_t *bytes, uint64_t size, gb_pq_file **out) {
     gb_status s = parse_footer(f);
     for (uint32_t g = 0; !s && g < f->chunks.size(); g++)
         for (uint32_t c = 0; !s && c < f->cols.size(); c++) {
-            if (f->chunks[g][c].codec != 0) {
-                set_error("compressed Parquet column chunks (codec %d) are not supported on the GPU path",
-                          f->chunks[g][c].codec);
+            if (f->chunks[g][c].codec != 0 && f->chunks[g][c].codec != 1) {
+                set_error("Parquet column chunks compressed with codec %d are not supported on the GPU path "
+                          "(uncompressed and SNAPPY are)", f->chunks[g][c].codec);
                 s = GB_ERR_UNSUPPORTED;
                 break;
             }
+            f->compressed = f->compressed || f->chunks[g][c].codec != 0;
             s = parse_pages(f, g, c);
         }
     if (s) {
@@ -1385,6 +1437,9 @@ struct PqScratch {
     // compacted offsets and bytes
     void *dicts = nullptr, *dsrc = nullptr, *doffs = nullptr, *dbytes = nullptr, *dmatch = nullptr;
     size_t dicts_cap = 0, dsrc_cap = 0, doffs_cap = 0, dbytes_cap = 0, dmatch_cap = 0;
+    // compressed batches: the decompressed image, its jobs, the level lengths found inside
+    void *img = nullptr, *ijobs = nullptr, *ilvl = nullptr;
+    size_t img_cap = 0, ijobs_cap = 0, ilvl_cap = 0;
 };
 
 static gb_status grow(void *&p, size_t &cap, size_t need) {
@@ -1424,7 +1479,7 @@ void gb_pq_release_scratch(gb_agg *h) {
         g_pq_scratch.erase(it);
     }
     for (void *p : {s->file_dev, s->pages, s->runs, s->page_runs, s->dict_pages, s->col_pages, s->chunks, s->ctl,
-                    s->dicts, s->dsrc, s->doffs, s->dbytes, s->dmatch})
+                    s->dicts, s->dsrc, s->doffs, s->dbytes, s->dmatch, s->img, s->ijobs, s->ilvl})
         if (p) cudaFree(p);
     for (void *p : s->out)
         if (p) cudaFree(p);
@@ -1457,13 +1512,15 @@ __global__ void k_pq_dict_match(const uint8_t *bytes, const int64_t *offs, u64 n
     }
 }
 
-static gb_status pq_varchar_dict(gb_agg *h, const gb_pq_file *f, PqScratch *S, const uint8_t *dfile, uint64_t base,
-                                 uint32_t rg_begin, uint32_t rg_end, int fcol, Ctl *dctl, cudaStream_t st,
-                                 const int64_t **ids, const PqStrFilters &SF, const uint8_t **match) {
+static gb_status pq_varchar_dict(gb_agg *h, const PqView &V, PqScratch *S, const uint8_t *dfile, uint64_t base,
+                                 uint32_t rg_begin, uint32_t rg_end, const std::vector<char> &live, int fcol,
+                                 Ctl *dctl, cudaStream_t st, const int64_t **ids, const PqStrFilters &SF,
+                                 const uint8_t **match) {
     std::vector<DDict> dd;
     uint64_t D = 0, B = 0;
     for (uint32_t g = rg_begin; g < rg_end; g++) {
-        const PqChunk &ch = f->chunks[g][fcol];
+        if (!live[g - rg_begin]) continue;
+        const PqChunk &ch = (*V.chunks)[g][fcol];
         if (ch.dict_off < 0) {
             if (ch.page_begin != ch.page_end) return pq_corrupt("VARCHAR column chunk without a dictionary page");
             continue;
@@ -1512,6 +1569,219 @@ static gb_status pq_varchar_dict(gb_agg *h, const gb_pq_file *f, PqScratch *S, c
         *match = (const uint8_t *)S->dmatch;
     }
     return gb_agg_encode_strings(h, (const uint8_t *)S->dbytes, (const int64_t *)S->doffs, D, B, st, ids);
+}
+
+// ------------------------------------------------ compressed column chunks
+// One piece of a batch's decompressed image: `src_len` bytes at file offset
+// `src` copied (mode 0) or inflated from a raw Snappy block (mode 1, the
+// codec of parquet.cpp:44-90, the vendored snappy 1.2.1) into `dst_len`
+// bytes at image offset `dst`.  lvl_slot != ~0: the piece is a page v1 of an
+// OPTIONAL column, whose first 4 bytes (the level length) go to lvl[slot].
+struct InflateJob {
+    uint64_t src, dst;
+    uint32_t src_len, dst_len;
+    uint32_t mode, lvl_slot;
+};
+
+// One warp per piece.  Snappy (the published format): a varint with the
+// uncompressed length, then elements whose tag's low 2 bits say literal (00:
+// length in the tag or in 1-4 following bytes), or copy with a 1-, 2- or
+// 4-byte offset (01/10/11) of an earlier output position, possibly
+// overlapping the bytes it writes.  Lane 0 parses the tags; the warp moves
+// the bytes (an overlapping copy in rounds of at most `offset` bytes).  Every
+// length and offset is checked against the piece's bounds; a malformed block
+// sets ERR_CORRUPT and stops.
+__global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *file, const InflateJob *jobs, uint32_t n,
+                                                    uint8_t *img, uint32_t *lvl, Ctl *ctl) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (j >= n) return;  // the whole warp
+    const InflateJob J = jobs[j];
+    const uint8_t *src = file + J.src;
+    uint8_t *dst = img + J.dst;
+    bool bad = false;
+    if (J.mode == 0) {
+        for (uint32_t i = lane; i < J.src_len; i += 32) dst[i] = src[i];
+    } else {
+        uint32_t ip = 0, op = 0;
+        if (lane == 0) {
+            uint64_t ulen = 0;
+            int sh = 0;
+            for (;;) {
+                if (ip >= J.src_len || sh > 28) {
+                    bad = true;
+                    break;
+                }
+                const uint8_t b = src[ip++];
+                ulen |= (uint64_t)(b & 0x7f) << sh;
+                if (!(b & 0x80)) break;
+                sh += 7;
+            }
+            if (ulen != J.dst_len) bad = true;
+        }
+        bad = __shfl_sync(FULL, (int)bad, 0) != 0;
+        ip = __shfl_sync(FULL, ip, 0);
+        while (!bad && op < J.dst_len) {
+            uint32_t kind = 0, len = 0, from = 0;  // kind 0: literal at src[from]; 1: copy of dst[from]
+            if (lane == 0) {
+                if (ip >= J.src_len) {
+                    bad = true;
+                } else {
+                    const uint32_t tag = src[ip++];
+                    const uint32_t t = tag & 3u;
+                    uint32_t off = 0;
+                    if (t == 0) {
+                        uint32_t l = tag >> 2;
+                        if (l >= 60) {
+                            const uint32_t nb = l - 59;
+                            if (ip + nb > J.src_len) bad = true;
+                            l = 0;
+                            for (uint32_t b = 0; b < nb && !bad; b++) l |= (uint32_t)src[ip + b] << (8 * b);
+                            ip += nb;
+                        }
+                        len = l + 1;
+                        if (!bad && (len > J.src_len - ip || len == 0)) bad = true;
+                        from = ip;
+                        ip += len;
+                    } else {
+                        kind = 1;
+                        const uint32_t nb = t == 1 ? 1 : (t == 2 ? 2 : 4);
+                        len = t == 1 ? 4 + ((tag >> 2) & 7u) : (tag >> 2) + 1;
+                        if (ip + nb > J.src_len) {
+                            bad = true;
+                        } else {
+                            for (uint32_t b = 0; b < nb; b++) off |= (uint32_t)src[ip + b] << (8 * b);
+                            if (t == 1) off = ((tag >> 5) << 8) | (off & 0xffu);
+                            ip += nb;
+                        }
+                        if (!bad && (off == 0 || off > op)) bad = true;
+                        from = op - off;
+                    }
+                    if (!bad && len > J.dst_len - op) bad = true;
+                }
+            }
+            bad = __shfl_sync(FULL, (int)bad, 0) != 0;
+            if (bad) break;
+            kind = __shfl_sync(FULL, kind, 0);
+            len = __shfl_sync(FULL, len, 0);
+            from = __shfl_sync(FULL, from, 0);
+            ip = __shfl_sync(FULL, ip, 0);
+            if (kind == 0) {
+                for (uint32_t i = lane; i < len; i += 32) dst[op + i] = src[from + i];
+            } else {
+                const uint32_t step = min(op - from, 32u);  // bytes of one round: all written before it
+                for (uint32_t b0 = 0; b0 < len; b0 += step) {
+                    const uint32_t i = b0 + (uint32_t)lane;
+                    if ((uint32_t)lane < step && i < len) dst[op + i] = dst[from + i];
+                    __syncwarp();
+                }
+            }
+            op += len;
+            __syncwarp();
+        }
+    }
+    if (bad && lane == 0) atomicOr(&ctl->err, (u32)ERR_CORRUPT);
+    __syncwarp();
+    if (lane == 0 && J.lvl_slot != ~0u) {
+        uint32_t l4 = ~0u;  // too short to hold a level length: corrupt
+        if (!bad && J.dst_len >= 4)
+            l4 = (uint32_t)dst[0] | ((uint32_t)dst[1] << 8) | ((uint32_t)dst[2] << 16) | ((uint32_t)dst[3] << 24);
+        lvl[J.lvl_slot] = l4;
+    }
+}
+
+// Build a batch's decompressed image: per live row group and mapped file
+// column, an uncompressed chunk is copied whole, a SNAPPY chunk's
+// dictionary page and data pages are inflated (page v2 levels copied as
+// stored); ic / ip get the batch's page metadata with image offsets.  A page
+// v1 of an OPTIONAL column learns its level length from the inflated bytes
+// (one device round trip).
+static gb_status pq_inflate_batch(gb_agg *h, const gb_pq_file *f, PqScratch *S, const uint8_t *dfile, uint64_t base,
+                                  uint32_t rg_begin, uint32_t rg_end, const std::vector<char> &live,
+                                  const int32_t *col_map, int nc, Ctl *dctl, cudaStream_t st,
+                                  std::vector<std::vector<PqChunk>> &ic, std::vector<PqPage> &ip) {
+    ic = f->chunks;
+    ip = f->pages;
+    std::vector<int32_t> fcols(col_map, col_map + nc);
+    std::sort(fcols.begin(), fcols.end());
+    fcols.erase(std::unique(fcols.begin(), fcols.end()), fcols.end());
+    std::vector<InflateJob> jobs;
+    std::vector<uint32_t> pending;
+    uint64_t pos = 0;
+    auto place = [&](uint64_t n) {
+        const uint64_t at = pos;
+        pos += (n + 15) & ~15ull;
+        return at;
+    };
+    for (uint32_t g = rg_begin; g < rg_end; g++) {
+        if (!live[g - rg_begin]) continue;
+        for (int32_t fc : fcols) {
+            PqChunk &ch = ic[g][fc];
+            if (ch.codec == 0) {
+                if (ch.size > 0xffffffffull) return pq_corrupt("column chunk size");
+                const uint64_t at = place(ch.size);
+                jobs.push_back({ch.start - base, at, (uint32_t)ch.size, (uint32_t)ch.size, 0u, ~0u});
+                const int64_t d = (int64_t)at - (int64_t)ch.start;
+                if (ch.dict_off >= 0) ch.dict_off += d;
+                for (uint32_t p = ch.page_begin; p < ch.page_end; p++) {
+                    ip[p].off = (uint64_t)((int64_t)ip[p].off + d);
+                    if (ip[p].def_bytes) ip[p].def_off = (uint64_t)((int64_t)ip[p].def_off + d);
+                }
+                continue;
+            }
+            if (ch.dict_off >= 0) {
+                const uint64_t at = place(ch.dict_bytes);
+                jobs.push_back({ch.dict_src - base, at, ch.dict_src_bytes, ch.dict_bytes, 1u, ~0u});
+                ch.dict_off = (int64_t)at;
+            }
+            for (uint32_t p = ch.page_begin; p < ch.page_end; p++) {
+                PqPage &pg = ip[p];
+                const uint64_t at = place((uint64_t)pg.lvl_copy + pg.raw_bytes);
+                if (pg.lvl_copy) {
+                    jobs.push_back({pg.src_off - pg.lvl_copy - base, at, pg.lvl_copy, pg.lvl_copy, 0u, ~0u});
+                    pg.def_off = at;
+                    pg.def_bytes = pg.lvl_copy;
+                }
+                jobs.push_back({pg.src_off - base, at + pg.lvl_copy, pg.src_bytes, pg.raw_bytes, pg.stored ? 0u : 1u,
+                                pg.lvl_pending ? (uint32_t)pending.size() : ~0u});
+                if (pg.lvl_pending) pending.push_back(p);
+                pg.off = at + pg.lvl_copy;
+                pg.bytes = pg.raw_bytes;
+            }
+        }
+    }
+    gb_status s;
+    if ((s = grow(S->img, S->img_cap, pos + 64)) || (s = grow(S->ijobs, S->ijobs_cap, jobs.size() * sizeof(InflateJob) + 16)) ||
+        (s = grow(S->ilvl, S->ilvl_cap, pending.size() * 4 + 16)))
+        return s;
+    if (!jobs.empty()) {
+        GB_CUDA(cudaMemcpyAsync(S->ijobs, jobs.data(), jobs.size() * sizeof(InflateJob), cudaMemcpyHostToDevice, st));
+        gb_prof_mark *pm = gb_agg_prof_begin(h, "k_pq_inflate", st);
+        k_pq_inflate<<<(unsigned)((jobs.size() + 3) / 4), 128, 0, st>>>(dfile, (const InflateJob *)S->ijobs,
+                                                                       (uint32_t)jobs.size(), (uint8_t *)S->img,
+                                                                       (uint32_t *)S->ilvl, dctl);
+        gb_agg_prof_end(h, pm, st);
+        GB_CUDA(cudaGetLastError());
+        gb_agg_count_launch(h, 1);
+    }
+    std::vector<uint32_t> lvl(pending.size());
+    if (!pending.empty())
+        GB_CUDA(cudaMemcpyAsync(lvl.data(), S->ilvl, pending.size() * 4, cudaMemcpyDeviceToHost, st));
+    Ctl c;
+    GB_CUDA(cudaMemcpyAsync(&c, dctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+    GB_CUDA(cudaStreamSynchronize(st));
+    if ((s = pq_fail_if_err(c))) return s;  // nothing is decoded from a malformed block
+    for (size_t k = 0; k < pending.size(); k++) {
+        PqPage &pg = ip[pending[k]];
+        const uint32_t l4 = lvl[k];
+        if (l4 == ~0u || 4 + (uint64_t)l4 > pg.raw_bytes || (l4 == 0 && pg.n_values > 0))
+            return pq_corrupt("definition levels");
+        pg.def_off = pg.off + 4;
+        pg.def_bytes = l4;
+        pg.off += 4 + (uint64_t)l4;
+        pg.bytes = pg.raw_bytes - 4 - l4;
+    }
+    return GB_OK;
 }
 
 extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg_begin, uint32_t rg_end,
@@ -1608,12 +1878,14 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
     PqScratch *S = g_scratch_for(h);
     // device bytes: the uploaded file, or this batch's byte range copied now
     uint64_t lo = ~0ull, hi = 0;
-    for (uint32_t g = rg_begin; g < rg_end; g++)
+    for (uint32_t g = rg_begin; g < rg_end; g++) {
+        if (!live[g - rg_begin]) continue;  // skipped row groups are not copied
         for (int c = 0; c < nc; c++) {
             const PqChunk &ch = f->chunks[g][col_map[c]];
             lo = std::min(lo, ch.start);
             hi = std::max(hi, ch.start + ch.size);
         }
+    }
     const uint8_t *dfile;
     uint64_t base = 0;
     if (mem == GB_MEM_DEVICE) {
@@ -1627,6 +1899,22 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
         GB_CUDA(cudaMemcpyAsync(S->file_dev, f->host + lo, hi - lo, cudaMemcpyHostToDevice, st));
         dfile = (const uint8_t *)S->file_dev;
         base = lo;
+    }
+    // compressed column chunks: every page of the batch is inflated (or
+    // copied) into one device image, and the batch decodes from that image
+    // through a copy of the page metadata whose offsets point into it
+    std::vector<std::vector<PqChunk>> img_chunks;
+    std::vector<PqPage> img_pages;
+    PqView V{&f->chunks, &f->pages};
+    if (f->compressed) {
+        if ((s = grow(S->ctl, S->ctl_cap, sizeof(Ctl)))) return s;
+        GB_CUDA(cudaMemsetAsync(S->ctl, 0, sizeof(Ctl), st));
+        if ((s = pq_inflate_batch(h, f, S, dfile, base, rg_begin, rg_end, live, col_map, nc, (Ctl *)S->ctl, st,
+                                  img_chunks, img_pages)))
+            return s;
+        dfile = (const uint8_t *)S->img;
+        base = 0;
+        V = PqView{&img_chunks, &img_pages};
     }
     std::vector<PqChunkArg> chunks;
     uint64_t rows = 0;
@@ -1643,7 +1931,7 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
         return s;
     GB_CUDA(cudaMemsetAsync(S->ctl, 0, sizeof(Ctl), st));
     Ctl *dctl = (Ctl *)S->ctl;
-    if (mem == GB_MEM_DEVICE && vc < 0) {
+    if (mem == GB_MEM_DEVICE && vc < 0 && !f->compressed) {
         // the resident file's page index (built once), columns picked per call
         if ((s = pq_build_index(f, st))) return s;
         const int nfc = (int)f->cols.size();
@@ -1660,18 +1948,20 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
         std::vector<DPage> pages;
         std::vector<RunJob> jobs;
         uint32_t run_total = 0;
-        if ((s = pq_page_table(f, rg_begin, rg_end, col_map, nc, base, pages, jobs, col_pages, run_total)))
+        if ((s = pq_page_table(f, V, rg_begin, rg_end, col_map, nc, base, &live, pages, jobs, col_pages, run_total)))
             return s;
         if (vc >= 0) {
             // the VARCHAR key's data pages gather string ids: page after page,
             // each row group's dictionary entries start at its running base
             const int64_t *ids = nullptr;
             const uint8_t *match = nullptr;
-            if ((s = pq_varchar_dict(h, f, S, dfile, base, rg_begin, rg_end, col_map[vc], dctl, st, &ids, SF, &match)))
+            if ((s = pq_varchar_dict(h, V, S, dfile, base, rg_begin, rg_end, live, col_map[vc], dctl, st, &ids, SF,
+                                     &match)))
                 return s;
             uint64_t eb = 0;
             for (uint32_t g = rg_begin; g < rg_end; g++) {
-                const PqChunk &ch = f->chunks[g][col_map[vc]];
+                if (!live[g - rg_begin]) continue;
+                const PqChunk &ch = (*V.chunks)[g][col_map[vc]];
                 const uint32_t k = (g - rg_begin) * (uint32_t)nc + (uint32_t)vc;
                 for (uint32_t p = col_pages[2 * k]; p < col_pages[2 * k + 1]; p++)
                     if (pages[p].kind == 1) {

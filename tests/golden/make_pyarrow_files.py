@@ -9,8 +9,9 @@ under tests/golden/; their logical columns are regenerated from the seeds by
 Cases: OPTIONAL columns with NULLs in the key, the filter column and the
 value columns, written as data page v1 and v2, with dictionary encoding on
 every column (values falling back to PLAIN pages once the dictionary page
-limit is reached), on no column, or on the key only; a dictionary-encoded
-VARCHAR key with NULL keys; OPTIONAL columns without NULLs.
+limit is reached), on no column, or on the key only, uncompressed or with
+pyarrow's default SNAPPY codec; a dictionary-encoded VARCHAR key with NULL
+keys (uncompressed and SNAPPY); OPTIONAL columns without NULLs.
 """
 from __future__ import annotations
 
@@ -28,6 +29,9 @@ CASES = {
     "pa_nulls_v2_dict": dict(version="2.0", dictionary=True),
     "pa_nulls_v1_plain": dict(version="1.0", dictionary=False),
     "pa_nulls_v2_keydict": dict(version="2.0", dictionary=["key"]),
+    # pyarrow's default codec: SNAPPY pages (inflated on the GPU)
+    "pa_nulls_v1_snappy": dict(version="1.0", dictionary=True, compression="snappy"),
+    "pa_nulls_v2_snappy": dict(version="2.0", dictionary=["key"], compression="snappy"),
 }
 
 
@@ -64,10 +68,10 @@ def load(name):
         return fh.read()
 
 
-def _write(name, table, **kw):
+def _write(name, table, compression="none", **kw):
     import pyarrow.parquet as pq
     buf = io.BytesIO()
-    pq.write_table(table, buf, compression="none", **kw)
+    pq.write_table(table, buf, compression=compression, **kw)
     with gzip.open(os.path.join(OUT, name + ".parquet.gz"), "wb", compresslevel=9) as fh:
         fh.write(buf.getvalue())
     print(name, len(buf.getvalue()), "bytes")
@@ -83,11 +87,12 @@ def main():
                   use_dictionary=c["dictionary"])
         if c["dictionary"] is True:
             kw["dictionary_pagesize_limit"] = 16 * 1024  # v and x fall back to PLAIN pages
-        _write(name, tbl, **kw)
+        _write(name, tbl, compression=c.get("compression", "none"), **kw)
     strs, _, v2, kn2, vn2 = varchar_columns()
     t2 = pa.table({"name": pa.array([s.decode() for s in strs], pa.string(), mask=kn2),
                    "v": pa.array(v2, pa.int64(), mask=vn2)})
     _write("pa_varchar_nulls", t2, row_group_size=8_000, data_page_size=4 * 1024)
+    _write("pa_varchar_nulls_snappy", t2, compression="snappy", row_group_size=8_000, data_page_size=4 * 1024)
     t3 = pa.table({"k": pa.array(np.arange(1000, dtype=np.int32) % 7), "v": pa.array(np.arange(1000, dtype=np.int64))})
     _write("pa_optional_nonnull", t3)
 

@@ -145,10 +145,12 @@ def test_pyarrow_files_with_nulls(name):
             compare(gpu, orc)
 
 
-def test_pyarrow_varchar_key_with_nulls():
+@pytest.mark.parametrize("name", ["pa_varchar_nulls", "pa_varchar_nulls_snappy"])
+def test_pyarrow_varchar_key_with_nulls(name):
     """A pyarrow-written dictionary-encoded VARCHAR key with NULL keys (one
-    NULL group) and a nullable value column; a LIKE on the key."""
-    data = paf.load("pa_varchar_nulls")
+    NULL group) and a nullable value column; a LIKE on the key; uncompressed
+    and SNAPPY pages."""
+    data = paf.load(name)
     _, names, v, kn, vn = paf.varchar_columns()
     types = [capi.VARCHAR, BIGINT]
     aggs = [("count_star", -1), ("count", 1), ("sum", 1)]
@@ -212,3 +214,49 @@ def test_parquet_int_varchar_pair_key():
     for device in (False, True):
         compare(run_pq(data, types, [0, 1, 2], [1, 0], aggs, filters=[(1, "<", 20)], est_groups=6000, device=device),
                 orc)
+
+
+@pytest.mark.parametrize("device", [False, True])
+def test_snappy_pages_from_the_project_writer(device):
+    """SNAPPY column chunks (dictionary and data pages) inflated on the GPU
+    per batch and decoded from the image, against the oracle; several
+    batches, with a filter that the zone maps do not prune."""
+    _, key, f, v = pq.filter_groupby_file(n_rows=300_000, row_group_rows=50_000, page_rows=8192, n_dict=4096)
+    cols = [pq.Column("key", pq.T_INT32, values=key), pq.Column("f", pq.T_INT32, values=f, int16=True),
+            pq.Column("v", pq.T_INT64, values=v)]
+    data = pq.write(cols, row_group_rows=50_000, page_rows=8192, codec="snappy")
+    types = [INTEGER, SMALLINT, BIGINT]
+    aggs = [("sum", 2), ("count_star", -1), ("max", 2)]
+    for filters, batches in (([], 1), ([(1, "<", 300)], 3)):
+        orc = oracle.run_query(types, [0], aggs, [key, f.astype(np.int16), v], filters=filters)
+        compare(run_pq(data, types, [0, 1, 2], [0], aggs, filters=filters, est_groups=4096, device=device,
+                       batches=batches), orc)
+
+
+def test_corrupt_snappy_block_is_reported():
+    """A page whose Snappy block is damaged (a copy reaching before the
+    start of the output) is reported as a corrupt file, not decoded."""
+    zeros = np.zeros(20_000, dtype=np.int64)
+    data = bytearray(pq.write([pq.Column("v", pq.T_INT64, values=zeros)], row_group_rows=20_000, page_rows=20_000,
+                              codec="snappy"))
+    # the page's block: a varint length, a literal, then copies with a 2-byte
+    # offset (tag ..10); its first copy's offset is raised past its position
+    blk = pq.snappy_compress(zeros.tobytes())
+    at = bytes(data).index(blk)
+    j = 0
+    while blk[j] & 0x80:
+        j += 1
+    j += 1  # past the length varint
+    assert blk[j] & 3 == 0  # the literal
+    j += 1 + (blk[j] >> 2) + 1
+    assert blk[j] & 3 == 2  # the first copy
+    data[at + j + 1], data[at + j + 2] = 0xff, 0x7f
+    pf = capi.ParquetFile(bytes(data))
+    g = capi.GroupBy([BIGINT], [0], [("count_star", -1)])
+    try:
+        with pytest.raises(capi.GbError) as e:
+            capi.ingest_parquet(g, pf, [0])
+        assert e.value.status == 6  # GB_ERR_CORRUPT
+    finally:
+        g.close()
+        pf.close()

@@ -123,10 +123,10 @@ def test_snappy_oracle_matches_pyarrow():
             oracle.snappy_decompress(bad)
 
 
-def test_snappy_file_read_by_pyarrow_and_refused_by_the_gpu_parser():
+def test_snappy_file_read_by_pyarrow_and_opened_by_the_gpu_parser():
     """SNAPPY column chunks from the writer are valid Parquet (pyarrow reads the
-    same values); the GPU path does not decompress pages yet and refuses the
-    file on open."""
+    same values) and the library's parser takes them (the pages are inflated
+    on the GPU per batch); a GZIP file is refused on open."""
     pa = pytest.importorskip("pyarrow.parquet")
     _, key, f, v = pq.filter_groupby_file(n_rows=30_000, row_group_rows=10_000, page_rows=4096, n_dict=512)
     cols = [pq.Column("key", pq.T_INT32, values=key), pq.Column("f", pq.T_INT32, values=f, int16=True),
@@ -136,8 +136,14 @@ def test_snappy_file_read_by_pyarrow_and_refused_by_the_gpu_parser():
     assert len(data) < len(plain)
     t = pa.read_table(io.BytesIO(data))
     assert np.array_equal(t.column("key").to_numpy(), key) and np.array_equal(t.column("v").to_numpy(), v)
+    pf = capi.ParquetFile(data)
+    assert pf.num_rows == 30_000 and pf.columns() == [("key", capi.INTEGER), ("f", capi.SMALLINT), ("v", capi.BIGINT)]
+    pf.close()
+    import pyarrow as pa_
+    buf = io.BytesIO()
+    pa.write_table(pa_.table({"v": pa_.array(v)}), buf, compression="gzip")
     with pytest.raises(capi.GbError) as e:
-        capi.ParquetFile(data)
+        capi.ParquetFile(buf.getvalue())
     assert e.value.status == 3  # GB_ERR_UNSUPPORTED
 
 
