@@ -372,8 +372,10 @@ void gb_server_destroy(gb_server *s);
  * values) on DEVICE buffers, with all scratch in fixed-size device arrays
  * inside the library (about 8.1 MiB, held by every GPU that loads the
  * library until the process exits).  Limits: out_cap <= GB_NOALLOC_MAX_GROUPS
- * and at most that many distinct keys, n <= 2^31 rows; beyond them the call
- * fails with a message and writes no result count.  The first call on a
+ * and at most that many distinct keys (the key INT64_MIN included), n <=
+ * 2^31 rows; beyond them the call fails with a message and writes no result
+ * count.  Keys whose hashes cluster are still exact: records of probe runs
+ * past the table's bound fold back in a second pass.  The first call on a
  * device resolves the scratch addresses (cudaGetSymbolAddress), so make it
  * before any stream capture.  All calls share the scratch, which each call
  * clears first: calls that overlap on the GPU race and must be serialised.

@@ -106,6 +106,32 @@ __global__ void __launch_bounds__(512) k_ingest_noalloc(const __grid_constant__ 
     if (threadIdx.x == 0 && s_new) atomicAdd(&T.ctl->n_groups, s_new);
 }
 
+// Records the ingest spilled (a probe run longer than the bound: keys whose
+// hashes cluster) fold into the table with an unbounded probe: at most
+// kMaxGroups keys fill at most half of its kCap slots, so a free slot is
+// always found.  Records beyond the spill area were lost and the call is
+// refused (ERR_SPILL_OVERFLOW).
+__global__ void k_merge_noalloc(const __grid_constant__ Plan P, const TableRef T) {
+    __shared__ u32 s_new;  // new groups of this block (g_slot counts with a shared-memory atomic)
+    if (threadIdx.x == 0) s_new = 0;
+    __syncthreads();
+    const u32 n = min(*(volatile u32 *)&T.ctl->spill_count, T.spill_cap);
+    TableRef U = T;
+    U.gmax_probe = (int32_t)kCap;
+    for (u32 i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const u64 *rec = T.spill + (u64)i * (1 + kWords);
+        const long long s = g_slot(U, rec[0], mix64(rec[0]), &s_new);
+        if (s < 0) {  // cannot happen below the limit (a free slot exists)
+            atomicOr(&T.ctl->err, (u32)ERR_SPILL_OVERFLOW);
+            continue;
+        }
+        u64 v[GB_MAX_OPS] = {rec[2]};
+        apply_state(P, T.slots + (u64)s * (u64)T.stride + 1, rec[1], v);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0 && s_new) atomicAdd(&T.ctl->n_groups, s_new);
+}
+
 __global__ void k_emit_noalloc(const u64 *table, Ctl *ctl, int64_t *out_keys, int64_t *out_sums,
                                int64_t *out_counts, u64 out_cap) {
     const int lane = threadIdx.x & 31;
@@ -200,13 +226,15 @@ extern "C" gb_status gb_hash_aggregate_noalloc(const int64_t *keys, const int64_
         int grid = (int)std::min<u64>((u64)sms * 2, std::max<u64>(1, want));
         k_ingest_noalloc<<<grid, 512, smem, st>>>(P, T, n, smem_slots);
         GB_CUDA(cudaGetLastError());
+        k_merge_noalloc<<<(kSpillCap + 255) / 256, 256, 0, st>>>(P, T);
+        GB_CUDA(cudaGetLastError());
     }
     k_emit_noalloc<<<sms * 4, 256, 0, st>>>(S.table, S.ctl, out_keys, out_sums, out_counts, out_cap);
     GB_CUDA(cudaGetLastError());
     Ctl c;
     GB_CUDA(cudaMemcpyAsync(&c, S.ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
     GB_CUDA(cudaStreamSynchronize(st));
-    if (c.spill_count > 0 || (c.err & ERR_SPILL_OVERFLOW)) {
+    if (c.err & ERR_SPILL_OVERFLOW) {
         set_error("more than %llu distinct keys: beyond the allocation-free table",
                   (unsigned long long)kMaxGroups);
         return GB_ERR_UNSUPPORTED;
@@ -216,6 +244,8 @@ extern "C" gb_status gb_hash_aggregate_noalloc(const int64_t *keys, const int64_
                   (unsigned long long)kMaxGroups);
         return GB_ERR_UNSUPPORTED;
     }
+    // (the key INT64_MIN, the table's empty marker, has its own slot and is
+    // emitted like any other group)
     if (c.err & ERR_OUT_OVERFLOW) {
         set_error("%u groups do not fit the output capacity %llu", c.out_count, (unsigned long long)out_cap);
         return GB_ERR_INVALID;

@@ -73,3 +73,50 @@ def test_noalloc_rejects_sizes_beyond_limit(gblib):
                                          C.c_void_p(8), 131073, C.byref(n), None)
     assert st == 1
     assert b"131072" in gblib.gb_last_error()
+
+
+def _fmix64_inverse(h):
+    """Keys whose murmur3 fmix64 hash is h (the hash is a bijection)."""
+    m = np.uint64(0xFFFFFFFFFFFFFFFF)
+    c1_inv = np.uint64(pow(0xff51afd7ed558ccd, -1, 1 << 64))
+    c2_inv = np.uint64(pow(0xc4ceb9fe1a85ec53, -1, 1 << 64))
+    k = h.astype(np.uint64)
+    with np.errstate(over="ignore"):
+        k ^= k >> np.uint64(33)
+        k = (k * c2_inv) & m
+        k ^= k >> np.uint64(33)
+        k = (k * c1_inv) & m
+        k ^= k >> np.uint64(33)
+    return k.view(np.int64)
+
+
+def test_noalloc_edges(gblib):
+    """INT64_MIN (the table's empty marker) and INT64_MAX as keys; exactly
+    GB_NOALLOC_MAX_GROUPS groups; one group more is refused; keys whose
+    hashes all land on one slot (probe runs past the bound spill, and the
+    spilled records fold back into the table)."""
+    rng = np.random.default_rng(22)
+    lo, hi = np.iinfo(np.int64).min, np.iinfo(np.int64).max
+    k = np.concatenate([np.array([lo, hi, lo, 0, -1], dtype=np.int64), rng.integers(0, 50, 10_000)])
+    v = rng.integers(-10**6, 10**6, len(k), dtype=np.int64)
+    _same(_noalloc(gblib, k, v, 1000), _allocating(k, v))
+    k = rng.permutation(np.arange(131_072, dtype=np.int64) * 7919 - 2**50)
+    k = np.concatenate([k, k[:50_000]])
+    v = rng.integers(0, 1000, len(k), dtype=np.int64)
+    r = _noalloc(gblib, k, v, 131_072)
+    assert len(r[0]) == 131_072
+    _same(r, _allocating(k, v))
+    k2 = np.concatenate([k, np.array([2**51 + 3], dtype=np.int64)])
+    with pytest.raises(capi.GbError) as e:
+        _noalloc(gblib, k2, np.ones(len(k2), dtype=np.int64), 131_072)
+    assert e.value.status == capi.GB_ERR_UNSUPPORTED
+    # 6000 keys on one slot of the 2^18-slot table (low 18 hash bits equal)
+    h = (np.arange(6000, dtype=np.uint64) << np.uint64(18)) | np.uint64(777)
+    k = _fmix64_inverse(h)
+    k = np.repeat(k, 3)
+    v = rng.integers(-10**6, 10**6, len(k), dtype=np.int64)
+    r = _noalloc(gblib, k, v, 10_000)
+    assert len(r[0]) == 6000
+    _same(r, _allocating(k, v))
+    # the next call starts from a clear table
+    _same(_noalloc(gblib, k[:30], v[:30], 100), _allocating(k[:30], v[:30]))
