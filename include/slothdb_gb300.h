@@ -349,6 +349,7 @@ typedef struct gb_server_stat {
     uint64_t peak_admitted_bytes;
     double busy_ms;
     uint64_t kernel_launches;
+    uint64_t result_bytes; /* device→host bytes of the results copied so far */
 } gb_server_stat;
 gb_status gb_server_create(uint64_t budget_bytes, uint32_t max_batch, int32_t mode, gb_server **out);
 gb_status gb_server_add_table(gb_server *s, const int32_t *col_types, uint32_t n_cols, const gb_col *cols,

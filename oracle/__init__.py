@@ -165,6 +165,23 @@ def run_query(col_types, group_cols, aggs, cols, filters=(), nulls=None, nthread
         strs = np.array([bytes(data[offs[r]:offs[r + 1]]) for r in reps], dtype=object)
         keys = [strs]
         key_null = [out_key_null[:ng].astype(bool)]
+    elif (len(group_cols) == 2 and all(t in (SMALLINT, INTEGER) for t in key_types)
+          and (nulls is None or all(nulls[g] is None for g in group_cols))):
+        # two non-NULL 16/32-bit keys: one int64 key (a << 32 | b as 32 bits),
+        # the same groups, through the multithreaded single-key loop
+        a = np.asarray(cols[group_cols[0]]).astype(np.int64)
+        b = np.asarray(cols[group_cols[1]]).astype(np.int64)
+        packed = (a << 32) | (b & 0xFFFFFFFF)
+        sub_types = list(col_types) + [BIGINT]
+        sub = run_query(sub_types, [len(col_types)], [(k, c) for k, c in aggs], list(cols) + [packed],
+                        filters=filters, nulls=(list(nulls) + [None]) if nulls is not None else None,
+                        nthreads=nthreads, est_groups=est_groups, max_groups=max_groups)
+        pk = sub["keys"][0]
+        sub["keys"] = [(pk >> 32).astype(NP_TYPES[key_types[0]]),
+                       (pk & 0xFFFFFFFF).astype(np.uint32).astype(np.int32).astype(NP_TYPES[key_types[1]])]
+        sub["key_null"] = [np.zeros(len(pk), bool), np.zeros(len(pk), bool)]
+        sub["out_types"] = list(key_types) + sub["out_types"][1:]
+        return sub
     else:
         # group ids: single int key directly; composite keys via a dense id
         # over the (value, null) tuples (equality of the reference's

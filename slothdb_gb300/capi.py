@@ -99,7 +99,7 @@ class Result(C.Structure):
 class ServerStat(C.Structure):
     _fields_ = [("batches", C.c_uint64), ("completed", C.c_uint64), ("rejected", C.c_uint64),
                 ("failed", C.c_uint64), ("queued", C.c_uint64), ("peak_admitted_bytes", C.c_uint64),
-                ("busy_ms", C.c_double), ("kernel_launches", C.c_uint64)]
+                ("busy_ms", C.c_double), ("kernel_launches", C.c_uint64), ("result_bytes", C.c_uint64)]
 
 
 # every exported symbol of include/slothdb_gb300.h (checked by tests)
@@ -233,6 +233,22 @@ def _make_spec(col_types, group_cols, aggs, filters=(), nullable=(), est_groups=
     return spec, (ct, gc, ag, fl, fkeep)
 
 
+def _result_bytes(r):
+    """(rows, bytes) of a host result: validity words, fixed-width values,
+    VARCHAR offsets and string bytes."""
+    n = int(r.n_rows)
+    nbytes = 0
+    for c in range(r.n_cols):
+        t = r.types[c]
+        nbytes += (n + 63) // 64 * 8
+        if t == VARCHAR:
+            offs = np.frombuffer((C.c_char * ((n + 1) * 8)).from_address(r.offsets[c]), dtype=np.int64)
+            nbytes += (n + 1) * 8 + int(offs[-1]) if n else 0
+        else:
+            nbytes += n * np.dtype(NP_TYPES[t]).itemsize
+    return n, nbytes
+
+
 def _read_result(r):
     """Host gb_result -> list of (values ndarray, valid bool ndarray)."""
     out = []
@@ -339,17 +355,7 @@ class GroupBy:
         pinned buffers, no Python conversion); returns (rows, bytes copied)."""
         r = Result()
         check(self.lib.gb_agg_result(self.h, C.byref(r)))
-        n = int(r.n_rows)
-        nbytes = 0
-        for c in range(r.n_cols):
-            t = r.types[c]
-            nbytes += (n + 63) // 64 * 8
-            if t == VARCHAR:
-                offs = np.frombuffer((C.c_char * ((n + 1) * 8)).from_address(r.offsets[c]), dtype=np.int64)
-                nbytes += (n + 1) * 8 + int(offs[-1]) if n else 0
-            else:
-                nbytes += n * np.dtype(NP_TYPES[t]).itemsize
-        return n, nbytes
+        return _result_bytes(r)
 
     def set_option(self, name, value):
         check(self.lib.gb_agg_set_option(self.h, name.encode(), int(value)))
@@ -441,6 +447,13 @@ class Batch:
         r = Result()
         check(self.lib.gb_batch_result(self.h, int(q), C.byref(r)))
         return _read_result(r)
+
+    def result_host_bytes(self, q):
+        """gb_batch_result only (device→host copy of query q's result into
+        the library's pinned buffers); returns (rows, bytes copied)."""
+        r = Result()
+        check(self.lib.gb_batch_result(self.h, int(q), C.byref(r)))
+        return _result_bytes(r)
 
     def slow_queries(self):
         return int(self.lib.gb_batch_slow_queries(self.h))

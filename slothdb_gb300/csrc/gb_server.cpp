@@ -126,6 +126,7 @@ private:
 // A host copy of one result, in pinned blocks of the pool.
 struct HostResult {
     u64 n_rows = 0;
+    u64 bytes = 0;  // device→host bytes copied
     std::vector<int32_t> types;
     std::vector<PinnedPool::Block> blocks;
     std::vector<const void *> data_p;
@@ -200,7 +201,9 @@ struct gb_server {
     std::unordered_multimap<std::string, gb_agg *> alone;   // idle handles of queries run alone, by plan shape
     std::deque<std::string> alone_order;
     // statistics
-    u64 n_batches = 0, n_done = 0, n_rejected = 0, n_failed = 0, peak_admitted = 0, busy_ns = 0, launches = 0;
+    u64 n_batches = 0, n_done = 0, n_rejected = 0, n_failed = 0, peak_admitted = 0, busy_ns = 0;
+    // written by the dispatcher outside the lock, read by gb_server_stats
+    std::atomic<u64> launches{0}, result_bytes{0};
 };
 
 namespace {
@@ -215,6 +218,7 @@ gb_status copy_result_device(const gb_result &r, HostResult &out, PinnedPool &po
     out.offs_p.assign(r.n_cols, nullptr);
     out.valid_p.assign(r.n_cols, nullptr);
     const u64 vw = (n + 63) / 64;
+    out.bytes = 0;
     auto take = [&](size_t bytes) -> void * {
         PinnedPool::Block b = pool.get(std::max<size_t>(bytes, 8));
         if (b.p) out.blocks.push_back(b);
@@ -226,6 +230,7 @@ gb_status copy_result_device(const gb_result &r, HostResult &out, PinnedPool &po
         if (r.validity && r.validity[c]) {
             if (vw && cudaMemcpyAsync(v, r.validity[c], vw * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess)
                 return GB_ERR_CUDA;
+            out.bytes += vw * 8;
         } else {
             for (u64 i = 0; i < vw; i++) v[i] = ~0ull;
         }
@@ -235,6 +240,7 @@ gb_status copy_result_device(const gb_result &r, HostResult &out, PinnedPool &po
             if (!o) return GB_ERR_OOM;
             if (cudaMemcpyAsync(o, r.offsets[c], (n + 1) * 8, cudaMemcpyDeviceToHost, st) != cudaSuccess)
                 return GB_ERR_CUDA;
+            out.bytes += (n + 1) * 8;
             out.offs_p[c] = o;
         } else if (n) {
             void *d = take(n * (u64)type_bytes(r.types[c]));
@@ -242,6 +248,7 @@ gb_status copy_result_device(const gb_result &r, HostResult &out, PinnedPool &po
             if (cudaMemcpyAsync(d, r.data[c], n * (u64)type_bytes(r.types[c]), cudaMemcpyDeviceToHost, st) !=
                 cudaSuccess)
                 return GB_ERR_CUDA;
+            out.bytes += n * (u64)type_bytes(r.types[c]);
             out.data_p[c] = d;
         }
     }
@@ -254,6 +261,7 @@ gb_status copy_result_device(const gb_result &r, HostResult &out, PinnedPool &po
         if (!d) return GB_ERR_OOM;
         if (nb && cudaMemcpyAsync(d, (const uint8_t *)r.data[c] + o[0], nb, cudaMemcpyDeviceToHost, st) != cudaSuccess)
             return GB_ERR_CUDA;
+        out.bytes += nb;
         out.data_p[c] = d;
         if (o[0]) {  // offsets relative to the copied bytes
             int64_t *w = const_cast<int64_t *>(o);
@@ -340,6 +348,7 @@ void run_alone(gb_server *s, Query *q) {
         gb_result r{};
         if (st == GB_OK) st = gb_agg_result_device(h, &r);
         if (st == GB_OK) st = copy_result_device(r, q->res, s->pinned, s->stream);
+        if (st == GB_OK) s->result_bytes += q->res.bytes;
         s->launches += gb_agg_kernel_launches(h);
     }
     finish(q, st, st ? gb_last_error() : nullptr);
@@ -389,6 +398,7 @@ void run_batch(gb_server *s, std::vector<Query *> &qs) {
             gb_result r{};
             gb_status rs = st ? st : gb_batch_result_device(b, (uint32_t)i, &r);
             if (rs == GB_OK) rs = copy_result_device(r, in[i]->res, s->pinned, s->stream);
+            if (rs == GB_OK) s->result_bytes += in[i]->res.bytes;
             finish(in[i], rs, rs ? gb_last_error() : nullptr);
         }
         s->launches += gb_batch_kernel_launches(b) - l0;
@@ -630,7 +640,8 @@ gb_status gb_server_stats(gb_server *s, gb_server_stat *out) {
     out->queued = s->queue.size();
     out->peak_admitted_bytes = s->peak_admitted;
     out->busy_ms = (double)s->busy_ns / 1e6;
-    out->kernel_launches = s->launches;
+    out->kernel_launches = s->launches.load();
+    out->result_bytes = s->result_bytes.load();
     return GB_OK;
 }
 
