@@ -93,19 +93,63 @@ def dist_env():
 
 
 class Clocks:
-    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    """SM clocks and throttle reasons sampled during a timed region: NVML
+    (libnvidia-ml through ctypes, read-only queries) every 10 ms from a
+    thread, so even a region of a few tens of milliseconds gets samples;
+    nvidia-smi at 200 ms where NVML cannot be loaded."""
 
+    # nvmlClocksEventReasons bits (nvml.h)
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index=0):
-        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
-        self.p = None
+    def __init__(self, gpu_index=0, period_s=0.01):
         self.idx = gpu_index
+        self.period = period_s
+        self.sm, self.smax, self.reasons = [], [], set()
+        self.nvml = self.dev = None
+        self.th = self.p = self.f = None
+        try:
+            import ctypes
+            lib = ctypes.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() == 0:
+                dev = ctypes.c_void_p()
+                if lib.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(gpu_index), ctypes.byref(dev)) == 0:
+                    self.nvml, self.dev = lib, dev
+                    self.fn_reasons = (getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+                                       or getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons", None))
+        except Exception:
+            self.nvml = None
+
+    def _sample_nvml(self):
+        import ctypes
+        clk, mx, rs = ctypes.c_uint(), ctypes.c_uint(), ctypes.c_ulonglong()
+        while not self.stop_flag:
+            try:
+                if self.nvml.nvmlDeviceGetClockInfo(self.dev, 1, ctypes.byref(clk)) == 0:  # NVML_CLOCK_SM
+                    self.sm.append(float(clk.value))
+                if self.nvml.nvmlDeviceGetMaxClockInfo(self.dev, 1, ctypes.byref(mx)) == 0:
+                    self.smax.append(float(mx.value))
+                if self.fn_reasons is not None and self.fn_reasons(self.dev, ctypes.byref(rs)) == 0:
+                    for bit, nm in self.REASONS.items():
+                        if rs.value & bit:
+                            self.reasons.add(nm)
+            except Exception:
+                self.reasons.add("sampling error")
+                return
+            time.sleep(self.period)
 
     def start(self):
+        self.stop_flag = False
+        if self.nvml is not None:
+            import threading
+            self.th = threading.Thread(target=self._sample_nvml, daemon=True)
+            self.th.start()
+            return
         try:
+            self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.Q,
                                        "--format=csv,noheader,nounits", "-lms", "200"],
                                       stdout=self.f, stderr=subprocess.DEVNULL)
@@ -113,32 +157,38 @@ class Clocks:
             self.p = None
 
     def stop(self):
-        if self.p is None:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        self.p.terminate()
-        try:
-            self.p.wait(timeout=5)
-        except Exception:
-            self.p.kill()
-        self.f.flush()
-        self.f.seek(0)
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.f.read().splitlines():
-            parts = [x.strip() for x in ln.split(",")]
-            if len(parts) < 9:
-                continue
+        self.stop_flag = True
+        if self.th is not None:
+            self.th.join()
+            src = "nvml"
+        elif self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["clock sampling unavailable"]}
+        else:
+            src = "nvidia-smi"
+            self.p.terminate()
             try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
-            except ValueError:
-                continue
-            for nm, val in zip(names, parts[5:9]):
-                if val.lower().startswith("active"):
-                    reasons.add(nm)
-        os.unlink(self.f.name)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+            self.f.flush()
+            self.f.seek(0)
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for ln in self.f.read().splitlines():
+                parts = [x.strip() for x in ln.split(",")]
+                if len(parts) < 9:
+                    continue
+                try:
+                    self.sm.append(float(parts[1]))
+                    self.smax.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, val in zip(names, parts[5:9]):
+                    if val.lower().startswith("active"):
+                        self.reasons.add(nm)
+            os.unlink(self.f.name)
+        return {"sm_mhz": statistics.median(self.sm) if self.sm else None,
+                "sm_max_mhz": max(self.smax) if self.smax else None,
+                "reasons": sorted(self.reasons), "samples": len(self.sm), "source": src}
 
 
 def gen_data(rows):
@@ -160,6 +210,15 @@ def oracle_zipf(k, x, threads):
 
 
 REL_TOL_F64 = 1e-12  # DOUBLE SUM/AVG: relative error against the FP64 compensated sum, per query
+
+
+def ref_threads(path):
+    """Host threads the reference itself uses on a path, which its CPU
+    baseline (the oracle port) is timed with: the in-memory chunk loop of
+    PhysicalHashAggregate runs on one thread (physical_planner.cpp:7933-8021);
+    the fused Parquet path (TLSingle, physical_planner.cpp:7613-7931) runs
+    its row groups on up to 8 worker threads."""
+    return min(8, os.cpu_count() or 1) if path == "parquet" else 1
 
 
 def hbm_peak_gbs():
@@ -255,30 +314,46 @@ def parity_zipf(k, x, full, top, threads=None):
     return out, orc_s
 
 
+def zipf_cpu_sample(args, k, x):
+    """The CPU baseline's sample of the 100M-row workload: its first
+    --cpu-sample rows through the oracle port on the reference's thread
+    count; returns (rows/s, cpu_baseline dict)."""
+    n = min(args.cpu_sample, len(k))
+    thr = ref_threads("memory")
+    _, dt = oracle_zipf(k[:n], x[:n], thr)
+    return n / dt, {"value": n / dt, "unit": "rows/s", "cores": thr, "kind": "port",
+                    "sample": "first %d rows of the workload, oracle port on %d thread (the reference's in-memory "
+                              "chunk loop is single-threaded)" % (n, thr)}
+
+
 def run_reference(args):
-    """The CPU arm: the oracle's restatement of the reference GROUP BY over
-    the whole 100M-row workload per step, every host thread (rank 0 only)."""
+    """The CPU arm: the oracle's restatement of the reference GROUP BY on the
+    reference's own thread count, a bounded sample of the 100M-row workload
+    per step (rank 0 only)."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    threads = os.cpu_count() or 1
     k, x, _ = gen_data(args.rows)
-    oracle_zipf(k[:100_000], x[:100_000], threads)
-    times = []
+    oracle_zipf(k[:100_000], x[:100_000], 1)
+    times, cpu = [], None
     for i in range(args.warmup + args.steps):
-        _, dt = oracle_zipf(k, x, threads)
-        if i >= args.warmup:
-            times.append(dt)
+        if i < args.warmup:  # untimed: a short prefix warms the code and allocator
+            oracle_zipf(k[:1_000_000], x[:1_000_000], 1)
+            continue
+        val, cpu = zipf_cpu_sample(args, k, x)
+        times.append(min(args.cpu_sample, len(k)) / val)
     per = statistics.mean(times)
-    val = args.rows / per
+    n = min(args.cpu_sample, len(k))
+    val = n / per
+    threads = cpu["cores"]
     line = {"impl": "reference", "metric": METRIC, "value": val, "unit": "rows/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic",
             "config": {"workload": "zipf-groupby-100M", "rows": args.rows, "distinct_values": N_VALUES,
-                       "aggs": "COUNT(*),SUM(x),AVG(x)"},
+                       "aggs": "COUNT(*),SUM(x),AVG(x)", "sample_rows": n},
             "cpu_baseline": {"value": val, "unit": "rows/s", "cores": threads, "kind": "port",
-                             "sample": "all %d rows of the workload per step (oracle restatement of the "
-                                       "reference's per-thread maps + sharded merge)" % args.rows},
+                             "sample": "first %d rows of the workload per step, %d thread (the reference's "
+                                       "in-memory chunk loop is single-threaded)" % (n, threads)},
             "e2e": {"value": val, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -385,13 +460,15 @@ def run_plain(args):
         orc = oracle.run_query(types, [0], PLAIN_AGGS, [k, v], nthreads=thr)
         diff = oracle_mismatch(res, orc, 1)
         parity = {"bit_exact": diff is None, "groups": int(orc["n_groups"]), "first_difference": diff}
+        rt = ref_threads("memory")
         reps, tc = 0, time.perf_counter()
         while time.perf_counter() - tc < 5.0:
-            oracle.run_query(types, [0], PLAIN_AGGS, [k, v], nthreads=thr)
+            oracle.run_query(types, [0], PLAIN_AGGS, [k, v], nthreads=rt)
             reps += 1
         per = (time.perf_counter() - tc) / reps
-        cpu = {"value": rows / per, "unit": "rows/s", "cores": thr, "kind": "port",
-               "sample": "the full 1M-row query, %d repetitions, %d threads" % (reps, thr)}
+        cpu = {"value": rows / per, "unit": "rows/s", "cores": rt, "kind": "port",
+               "sample": "the full 1M-row query, %d repetitions, %d thread (the reference's in-memory chunk loop)"
+                         % (reps, rt)}
         line = {"metric": "plain GROUP BY rows/s (1M rows, 1,024 groups)", "value": whole_job_rate(rows, ws, ms),
                 "unit": "rows/s", "n_gpus": ws, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
@@ -411,9 +488,10 @@ def run_plain(args):
 
 
 def run_plain_reference(args, k, v):
-    """The oracle over the same 1M rows, all host threads, one query per step."""
+    """The oracle over the same 1M rows on the reference's thread count, one
+    query per step."""
     import oracle
-    thr = os.cpu_count() or 1
+    thr = ref_threads("memory")
     times = []
     for i in range(args.warmup + args.steps):
         t = time.perf_counter()
@@ -427,7 +505,7 @@ def run_plain_reference(args, k, v):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
             "config": {"workload": "plain-groupby-1M", "rows": len(k), "groups": 1024},
             "cpu_baseline": {"value": val, "unit": "rows/s", "cores": thr, "kind": "port",
-                             "sample": "the full 1M-row query per step, %d threads" % thr},
+                             "sample": "the full 1M-row query per step, %d thread" % thr},
             "e2e": {"value": val, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -604,9 +682,11 @@ def run_batch(args):
         if d:
             diffs.append("q%d (%s, %d rows): %s" % (i, shapes[i]["kind"], shapes[i]["rows"], d))
     del host_tabs, orcs
-    cpu = {"value": nq / orc_s, "unit": "queries/s", "cores": thr, "kind": "port",
-           "sample": "all %d queries over the same tables (%d rows), one query per thread, %d threads (%.1f s)"
-                     % (nq, total_rows, thr, orc_s)}
+    smp = BatchCpuSample(args)
+    cpu = smp.baseline(smp.seconds(), nq)
+    cpu["all_queries_parallel"] = {"value": nq / orc_s, "threads": thr,
+                                   "sample": "all %d queries (%d rows), one query per thread (the parity pass)"
+                                             % (nq, total_rows)}
     line = {"metric": "batched GROUP BY queries/s (256 uneven tables) vs sequential plain launches",
             "value": value, "unit": "queries/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms_batch, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -631,28 +711,47 @@ def run_batch(args):
         g.close()
 
 
+class BatchCpuSample:
+    """The batch workload's CPU baseline: the reference's generic chunk loop
+    restated in the oracle, queries one after another on one thread each,
+    over a bounded sample (the first tables, in generation order, up to
+    about 20M rows, host-generated with the same shapes)."""
+
+    def __init__(self, args):
+        from slothdb_gb300 import datagen
+        shapes = datagen.batch_shapes(n_tables=args.tables, seed=3)
+        self.picked, self.rows = [], 0
+        for sh in shapes:
+            if self.rows + sh["rows"] > 20_000_000 and self.picked:
+                continue
+            self.picked.append(sh)
+            self.rows += sh["rows"]
+        self.tabs = [datagen.batch_table_host(sh) for sh in self.picked]
+
+    def seconds(self):
+        import oracle
+        from slothdb_gb300 import datagen
+        t = time.perf_counter()
+        for sh, cols in zip(self.picked, self.tabs):
+            q = datagen.BATCH_COMPOSITE if sh["kind"] == "composite" else datagen.BATCH_VARCHAR
+            oracle.run_query(q["col_types"], q["group_cols"], q["aggs"], cols, nthreads=ref_threads("memory"))
+        return time.perf_counter() - t
+
+    def baseline(self, per, n_tables):
+        return {"value": len(self.picked) / per, "unit": "queries/s", "cores": ref_threads("memory"),
+                "kind": "port", "sample": "%d of the %d tables (%d rows), sequential, 1 thread" % (
+                    len(self.picked), n_tables, self.rows)}
+
+
 def run_batch_reference(args):
-    """The reference's generic chunk loop restated in the oracle, queries run
-    one after another with one thread each, on a bounded sample: the first
-    tables (by generation order) up to about 20M rows, host-generated."""
-    import oracle
-    from slothdb_gb300 import datagen
-    shapes = datagen.batch_shapes(n_tables=args.tables, seed=3)
-    picked, rows = [], 0
-    for sh in shapes:
-        if rows + sh["rows"] > 20_000_000 and picked:
-            continue
-        picked.append(sh)
-        rows += sh["rows"]
-    tabs = [datagen.batch_table_host(sh) for sh in picked]
+    """The batch CPU baseline (BatchCpuSample) timed per step."""
+    smp = BatchCpuSample(args)
+    picked, rows = smp.picked, smp.rows
     times = []
     for i in range(args.warmup + args.steps):
-        t = time.perf_counter()
-        for sh, cols in zip(picked, tabs):
-            q = datagen.BATCH_COMPOSITE if sh["kind"] == "composite" else datagen.BATCH_VARCHAR
-            oracle.run_query(q["col_types"], q["group_cols"], q["aggs"], cols, nthreads=1)
+        dt = smp.seconds()
         if i >= args.warmup:
-            times.append(time.perf_counter() - t)
+            times.append(dt)
     per = statistics.mean(times)
     val = len(picked) / per
     line = {"impl": "reference", "metric": "batched GROUP BY queries/s (256 uneven tables) vs sequential plain launches",
@@ -661,9 +760,7 @@ def run_batch_reference(args):
             "dtype": "int64", "data": "synthetic",
             "config": {"workload": "batch-%d-tables (bounded sample: %d tables, %d rows)" % (
                 args.tables, len(picked), rows)},
-            "cpu_baseline": {"value": val, "unit": "queries/s", "cores": 1, "kind": "port",
-                             "sample": "%d of the %d tables (%d rows), sequential, 1 thread" % (
-                                 len(picked), args.tables, rows)},
+            "cpu_baseline": smp.baseline(per, args.tables),
             "e2e": {"value": val, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -827,9 +924,11 @@ def run_serve(args):
         d = oracle_mismatch(results[i][0], orc, len(q["group_cols"]))
         if d:
             orc_diffs.append("q%d shape %d: %s" % (i, q["shape"], d))
-    cpu = {"value": len(results) / orc_s, "unit": "queries/s", "cores": thr, "kind": "port",
-           "sample": "the %d sampled queries of the stream (%d rows), one after another, %d threads each"
-                     % (len(results), orc_rows, thr)}
+    smp = ServeCpuSample(args)
+    cpu = smp.baseline(smp.seconds())
+    cpu["sampled_all_threads"] = {"value": len(results) / orc_s, "threads": thr,
+                                  "sample": "the %d parity-sampled queries (%d rows), %d threads each"
+                                            % (len(results), orc_rows, thr)}
     hbm_peak, peak_src = hbm_peak_gbs()
     b = out["batched"]
     busy_s = max(1e-9, b["busy_ms"] / 1e3)
@@ -863,46 +962,66 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+class ServeCpuSample:
+    """The served stream's CPU baseline: the oracle (restatement of the
+    reference's GROUP BY) on a sample of the query mix, the first queries of
+    the stream whose row ranges sum to about 30M rows, over host-generated
+    columns of the same families, one query after another on one thread
+    (the full stream is infeasible on the CPU)."""
+
+    def __init__(self, args):
+        from slothdb_gb300 import datagen
+        rows_of = {i: int(t["rows"] * args.scale) for i, t in enumerate(datagen.SERVE_TABLES)}
+        queries = datagen.serve_queries(args.duration, args.rate, rows_of, seed=4)
+        self.picked, self.rows = [], 0
+        for q in queries:
+            n = q["r1"] - q["r0"]
+            if self.rows + n > 30_000_000:
+                continue
+            self.picked.append(q)
+            self.rows += n
+        rng = np.random.default_rng(5)
+
+        def host_cols(q):
+            n = q["r1"] - q["r0"]
+            fam = datagen.SERVE_TABLES[q["table"]]["family"]
+            g = datagen.SERVE_TABLES[q["table"]]["groups"]
+            if fam == "plain":
+                return [rng.integers(0, g, n, dtype=np.int32), rng.integers(0, 10**6, n, dtype=np.int64)]
+            if fam == "zipf":
+                return [rng.integers(0, 2**40, n, dtype=np.int64), rng.normal(100, 25, n)]
+            if fam == "filter":
+                return [rng.integers(0, g, n, dtype=np.int32), rng.integers(0, 1000, n, dtype=np.int16),
+                        rng.integers(-10**9, 10**9, n, dtype=np.int64)]
+            return datagen.batch_table_host(dict(kind=fam, rows=n, groups=g, seed=int(rng.integers(1 << 30))))
+
+        self.data = [host_cols(q) for q in self.picked]
+
+    def seconds(self):
+        import oracle
+        from slothdb_gb300 import datagen
+        t = time.perf_counter()
+        for q, cols in zip(self.picked, self.data):
+            types = datagen.SERVE_TYPES[datagen.SERVE_TABLES[q["table"]]["family"]]
+            oracle.run_query(types, q["group_cols"], q["aggs"], cols, filters=q["filters"],
+                             nthreads=ref_threads("memory"))
+        return time.perf_counter() - t
+
+    def baseline(self, per):
+        return {"value": len(self.picked) / per, "unit": "queries/s", "cores": ref_threads("memory"),
+                "kind": "port", "sample": "first %d queries of the stream (%d rows), sequential, 1 thread" % (
+                    len(self.picked), self.rows)}
+
+
 def run_serve_reference(args):
-    """The oracle (restatement of the reference's GROUP BY) on a sample of
-    the query mix: the first queries of the stream whose row ranges sum to
-    about 30M rows, host-generated columns of the same families, 1 thread
-    per query (the full stream is infeasible on the CPU)."""
-    import oracle
-    from slothdb_gb300 import datagen
-    rows_of = {i: int(t["rows"] * args.scale) for i, t in enumerate(datagen.SERVE_TABLES)}
-    queries = datagen.serve_queries(args.duration, args.rate, rows_of, seed=4)
-    picked, tot = [], 0
-    for q in queries:
-        n = q["r1"] - q["r0"]
-        if tot + n > 30_000_000:
-            continue
-        picked.append(q)
-        tot += n
-    rng = np.random.default_rng(5)
-
-    def host_cols(q):
-        n = q["r1"] - q["r0"]
-        fam = datagen.SERVE_TABLES[q["table"]]["family"]
-        g = datagen.SERVE_TABLES[q["table"]]["groups"]
-        if fam == "plain":
-            return [rng.integers(0, g, n, dtype=np.int32), rng.integers(0, 10**6, n, dtype=np.int64)]
-        if fam == "zipf":
-            return [rng.integers(0, 2**40, n, dtype=np.int64), rng.normal(100, 25, n)]
-        if fam == "filter":
-            return [rng.integers(0, g, n, dtype=np.int32), rng.integers(0, 1000, n, dtype=np.int16),
-                    rng.integers(-10**9, 10**9, n, dtype=np.int64)]
-        return datagen.batch_table_host(dict(kind=fam, rows=n, groups=g, seed=int(rng.integers(1 << 30))))
-
-    data = [host_cols(q) for q in picked]
+    """The served stream's CPU baseline (ServeCpuSample) timed per step."""
+    smp = ServeCpuSample(args)
+    picked, tot = smp.picked, smp.rows
     times = []
     for i in range(args.warmup + max(1, args.steps)):
-        t = time.perf_counter()
-        for q, cols in zip(picked, data):
-            types = datagen.SERVE_TYPES[datagen.SERVE_TABLES[q["table"]]["family"]]
-            oracle.run_query(types, q["group_cols"], q["aggs"], cols, filters=q["filters"], nthreads=1)
+        dt = smp.seconds()
         if i >= args.warmup:
-            times.append(time.perf_counter() - t)
+            times.append(dt)
     per = statistics.mean(times)
     val = len(picked) / per
     line = {"impl": "reference", "metric": "served GROUP BY queries/s and latency percentiles (Poisson stream, "
@@ -910,9 +1029,7 @@ def run_serve_reference(args):
             "warmup": args.warmup, "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic",
             "config": {"workload": "serve-10-tables (bounded sample: %d queries, %d rows)" % (len(picked), tot)},
-            "cpu_baseline": {"value": val, "unit": "queries/s", "cores": 1, "kind": "port",
-                             "sample": "first %d queries of the stream (%d rows), sequential, 1 thread" % (
-                                 len(picked), tot)},
+            "cpu_baseline": smp.baseline(per),
             "e2e": {"value": val, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -1018,7 +1135,7 @@ def run_parquet(args):
     cpu = None
     if rank == 0:
         n = min(args.cpu_sample, rows)
-        thr = os.cpu_count() or 1
+        thr = ref_threads("parquet")
         tc = time.perf_counter()
         oracle.run_query(types, [0], aggs, [key[:n], f[:n].astype(np.int16), v[:n]], filters=filters, nthreads=thr)
         dt = time.perf_counter() - tc
@@ -1044,10 +1161,11 @@ def run_parquet(args):
 
 def run_parquet_reference(args, key, f, v, rows):
     """The oracle's filter + GROUP BY over the decoded columns of a bounded
-    sample (page decode not included), all host threads."""
+    sample (page decode not included), on the reference's Parquet thread
+    count."""
     import oracle
     n = min(args.cpu_sample, rows)
-    thr = os.cpu_count() or 1
+    thr = ref_threads("parquet")
     types = [2, 1, 3]
     times = []
     for i in range(args.warmup + args.steps):
@@ -1187,12 +1305,12 @@ def run_distinct(args):
     if rank == 0:
         import oracle
         n = min(args.cpu_sample, rows)
-        thr = os.cpu_count() or 1
+        thr = ref_threads("memory")
         tc = time.perf_counter()
         oracle.run_query(types, [0], aggs, [k[:n], v[:n]], nthreads=thr)
         dt = time.perf_counter() - tc
         cpu = {"value": n / dt, "unit": "rows/s", "cores": thr, "kind": "port",
-               "sample": "first %d rows, per-thread value sets + sharded union, %d threads (%.2f s)" % (n, thr, dt)}
+               "sample": "first %d rows, %d thread (%.2f s)" % (n, thr, dt)}
     line = {"metric": "COUNT(DISTINCT) GROUP BY rows/s (100M rows, 100K groups)", "value": rows / (ms / 1e3),
             "unit": "rows/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32", "data": "synthetic",
@@ -1208,11 +1326,11 @@ def run_distinct(args):
 
 
 def run_distinct_reference(args, k, v, types, aggs):
-    """The oracle's per-group value sets over a bounded sample, every host
-    thread (per-thread sets, their union in a sharded merge)."""
+    """The oracle's per-group value sets over a bounded sample, on the
+    reference's in-memory thread count."""
     import oracle
     n = min(args.cpu_sample, len(k))
-    thr = os.cpu_count() or 1
+    thr = ref_threads("memory")
     times = []
     for i in range(args.warmup + args.steps):
         t = time.perf_counter()
@@ -1380,9 +1498,9 @@ def main():
         # full-size parity (oracle over the same 100M rows, outside the timed
         # region); the same oracle pass is the timed CPU baseline
         parity, orc_s = parity_zipf(k, x, full, top)
-        thr = parity["oracle"]["threads"]
-        cpu = {"value": rows / orc_s, "unit": "rows/s", "cores": thr, "kind": "port",
-               "sample": "all %d rows of the workload, one pass, %d threads (%.2f s)" % (rows, thr, orc_s)}
+        _, cpu = zipf_cpu_sample(args, k, x)
+        cpu["all_threads"] = {"value": rows / orc_s, "threads": parity["oracle"]["threads"],
+                              "sample": "all %d rows (the parity pass)" % rows}
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "rows/s", "n_gpus": ws, "steps": args.steps,
