@@ -207,6 +207,12 @@ void gb_agg_destroy(gb_agg *h);
  * accounting). */
 uint64_t gb_agg_kernel_launches(const gb_agg *h);
 
+/* Parquet row groups that this handle's gb_agg_ingest_parquet calls skipped
+ * since create/reset because their statistics rule out a predicate (the
+ * reference marks the same row groups RGWork::pruned,
+ * physical_planner.cpp:1020, 1142-1182). */
+uint64_t gb_agg_row_groups_pruned(const gb_agg *h);
+
 /* Execution options of a handle, set before its first ingest (the
  * autotuner's knobs; no reference counterpart beyond the hard-coded thread
  * counts of physical_planner.cpp:7320-7641):

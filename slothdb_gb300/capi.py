@@ -116,6 +116,7 @@ _SIGS = {
     "gb_agg_reset": (C.c_int, [C.c_void_p]),
     "gb_agg_destroy": (None, [C.c_void_p]),
     "gb_agg_kernel_launches": (C.c_uint64, [C.c_void_p]),
+    "gb_agg_row_groups_pruned": (C.c_uint64, [C.c_void_p]),
     "gb_agg_set_option": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int64]),
     "gb_agg_get_mode": (C.c_int32, [C.c_void_p]),
     "gb_agg_set_profiling": (C.c_int, [C.c_void_p, C.c_int32]),
@@ -379,6 +380,9 @@ class GroupBy:
 
     def launches(self):
         return int(self.lib.gb_agg_kernel_launches(self.h))
+
+    def row_groups_pruned(self):
+        return int(self.lib.gb_agg_row_groups_pruned(self.h))
 
     def reset(self):
         check(self.lib.gb_agg_reset(self.h))

@@ -596,6 +596,7 @@ struct gb_agg {
     std::vector<gb_kernel_stat> stats;
     // accounting / state
     u64 launches = 0;
+    u64 rg_pruned = 0;  // Parquet row groups skipped by zone maps
     bool finalized = false;
     bool has_result = false;
     Ctl ctl_host{};
@@ -2106,6 +2107,7 @@ gb_status gb_agg_reset(gb_agg *h) {
     h->topn_applied = false;
     h->n_rows_out = 0;
     h->launches = 0;
+    h->rg_pruned = 0;
     return GB_OK;
 }
 
@@ -2154,6 +2156,8 @@ void gb_agg_destroy(gb_agg *h) {
 }
 
 uint64_t gb_agg_kernel_launches(const gb_agg *h) { return h ? h->launches : 0; }
+
+uint64_t gb_agg_row_groups_pruned(const gb_agg *h) { return h ? h->rg_pruned : 0; }
 
 gb_status gb_agg_set_option(gb_agg *h, const char *name, int64_t value) {
     if (!h || !name) return GB_ERR_INVALID;
@@ -2322,6 +2326,8 @@ gb_status gb_agg_view(gb_agg *h, AggView *v) {
 }
 
 void gb_agg_count_launch(gb_agg *h, int n) { h->launches += (u64)n; }
+
+void gb_agg_count_pruned(gb_agg *h, uint64_t n) { h->rg_pruned += n; }
 
 gb_status gb_agg_ingest_prefiltered(gb_agg *h, const gb_col *cols, uint64_t nrows, void *stream) {
     const int nf = h->plan.n_filters;

@@ -19,6 +19,7 @@ struct AggView {
 };
 gb_status gb_agg_view(gb_agg *h, AggView *v);
 void gb_agg_count_launch(gb_agg *h, int n);
+void gb_agg_count_pruned(gb_agg *h, uint64_t n);
 // Device-resident columns whose rows already passed the spec's filters.
 gb_status gb_agg_ingest_prefiltered(gb_agg *h, const gb_col *cols, uint64_t nrows, void *stream);
 // As above for a VARCHAR group key whose rows arrive as this handle's string

@@ -1874,6 +1874,7 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
         }
         n_live += live[g - rg_begin] ? 1u : 0u;
     }
+    gb_agg_count_pruned(h, (rg_end - rg_begin) - n_live);
     if (n_live == 0) return GB_OK;
     PqScratch *S = g_scratch_for(h);
     // device bytes: the uploaded file, or this batch's byte range copied now

@@ -180,6 +180,27 @@ def test_radix_hot_table_full_key_range(vtype):
     assert err <= REL_TOL
 
 
+@pytest.mark.parametrize("n_keys", [1, 700])
+def test_radix_specialised_pass_all_keys_hot(n_keys):
+    """The specialised partition pass (one BIGINT key, one DOUBLE SUM) when
+    every key lands in the hot table: no row is partitioned, so the
+    per-partition pass runs on empty partitions and the result comes from
+    the hot emit alone (with and without a TopN on it)."""
+    rng = np.random.default_rng(23)
+    n = 1_000_000
+    k = rng.integers(0, n_keys, n).astype(np.int64) * 1_000_003 - 5
+    x = rng.normal(50, 10, n)
+    aggs = [("count_star", -1), ("sum", 1)]
+    err, _, _ = check([BIGINT, DOUBLE], [0], aggs, [k, x], est_groups=2_000_000, mode=RADIX, device=True)
+    assert err <= REL_TOL
+    gpu = run_gpu([BIGINT, DOUBLE], [0], aggs, [k, x], topn=(1, False, 5), est_groups=2_000_000, mode=RADIX,
+                  device=True)
+    orc = oracle.run_query([BIGINT, DOUBLE], [0], aggs, [k, x])
+    order = np.lexsort((orc["keys"][0], -orc["aggs"][0][0]))[:5]
+    assert np.array_equal(gpu["keys"][0], orc["keys"][0][order])
+    assert np.array_equal(gpu["aggs"][0][0], orc["aggs"][0][0][order])
+
+
 @pytest.mark.parametrize("mode", [HASH, RADIX])
 def test_zipf_topn_count_desc(mode):
     k, x = datagen.zipf(2_000_000, seed=1, n_values=400_000)

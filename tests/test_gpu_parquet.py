@@ -14,7 +14,7 @@ pytestmark = [pytest.mark.gpu, pytest.mark.usefixtures("oracle_lib", "gblib")]
 
 
 def run_pq(data, col_types, col_map, group_cols, aggs, filters=(), est_groups=0, device=False, batches=1,
-           mode=0, nullable=()):
+           mode=0, nullable=(), pruned=None):
     pf = capi.ParquetFile(data)
     if device:
         pf.upload()
@@ -25,6 +25,8 @@ def run_pq(data, col_types, col_map, group_cols, aggs, filters=(), est_groups=0,
         step = max(1, (nrg + batches - 1) // batches)
         for b in range(0, nrg, step):
             capi.ingest_parquet(g, pf, col_map, b, min(nrg, b + step), device=device)
+        if pruned is not None:
+            pruned.append(g.row_groups_pruned())
         g.finalize()
         res = g.result()
     finally:
@@ -260,3 +262,38 @@ def test_corrupt_snappy_block_is_reported():
     finally:
         g.close()
         pf.close()
+
+
+@pytest.mark.parametrize("key", ["int", "varchar"])
+def test_zone_map_pruning_against_the_oracle(key):
+    """Row groups whose statistics rule out the WHERE clause are skipped
+    (none, some, all of them) and the result still equals the oracle's over
+    the whole file; a numeric and a dictionary-encoded VARCHAR key (whose
+    dictionaries of skipped row groups are not encoded), one or several
+    batches, host and resident files."""
+    n, rg = 240_000, 40_000
+    rng = np.random.default_rng(41)
+    f = (np.arange(n) // rg * 100 + rng.integers(0, 100, n)).astype(np.int32)  # row group g: [100g, 100g + 100)
+    v = rng.integers(-10**6, 10**6, n, dtype=np.int64)
+    idx = rng.integers(0, 1500, n).astype(np.uint32)
+    if key == "int":
+        d = rng.integers(-(2**31), 2**31 - 1, 1500, dtype=np.int64).astype(np.int32)
+        kcol = pq.Column("k", pq.T_INT32, dictionary=d, indices=idx)
+        types, kvals = [INTEGER, INTEGER, BIGINT], d[idx]
+    else:
+        d = [b"name-%05d" % i * (1 + i % 3) for i in range(1500)]
+        kcol = pq.Column("k", pq.T_BYTE_ARRAY, dictionary=d, indices=idx, shuffle_seed=3)
+        types, kvals = [capi.VARCHAR, INTEGER, BIGINT], pq.strings_of(d, idx)
+    # f is an INTEGER column: the reference reads no statistics for SMALLINT
+    data = pq.write([kcol, pq.Column("f", pq.T_INT32, values=f), pq.Column("v", pq.T_INT64, values=v)],
+                    row_group_rows=rg, page_rows=8192, stats=True)
+    aggs = [("count_star", -1), ("sum", 2), ("max", 2)]
+    for filters, n_pruned in (([(1, "<", 1000)], 0), ([(1, "<", 250)], 3), ([(1, ">=", 300), (1, "<", 420)], 4),
+                              ([(1, ">", 5000)], 6)):
+        orc = oracle.run_query(types, [0], aggs, [kvals, f, v], filters=filters)
+        for device, batches in ((False, 1), (True, 1), (False, 4), (True, 6)):
+            got = []
+            gpu = run_pq(data, types, [0, 1, 2], [0], aggs, filters=filters, est_groups=1500, device=device,
+                         batches=batches, pruned=got)
+            assert got == [n_pruned], (filters, device, batches, got)
+            compare(gpu, orc)
