@@ -587,6 +587,8 @@ struct gb_agg {
     int smem_probe = 8;
     int gmax_probe = 256;
     bool precombine = true;
+    bool precombine_set = false;  // the "precombine" option was given (else the fast path chooses)
+    bool fast_ingest = true;      // integer plans take the register-resident fast kernel
     u32 tile_rows = 8192;
     // profiling (CUDA events around each kernel, resolved at sync points)
     bool profiling = false;
@@ -856,6 +858,11 @@ static gb_status dist_clear(gb_agg *h, cudaStream_t st) {
     return GB_OK;
 }
 
+// defined with the fast tile path (gb_batch.cuh): launches the
+// single-query fast ingest when the plan allows it (*launched = true)
+static gb_status launch_ingest_fast(gb_agg *h, const TableRef &T, IngestArgs A, int grid, cudaStream_t st,
+                                    bool *launched);
+
 static gb_status run_ingest(gb_agg *h, u64 n_rows, cudaStream_t st) {
     if (n_rows == 0) return GB_OK;
     if (h->plan.n_dist) {
@@ -905,7 +912,9 @@ static gb_status run_ingest(gb_agg *h, u64 n_rows, cudaStream_t st) {
         A.pad = 0;
         TableRef T = table_ref(h);
         int g = (int)std::min<u64>((u64)grid, n_tiles_total - first);
-        {
+        bool fast = false;
+        if (gb_status fs = launch_ingest_fast(h, T, A, g, st, &fast)) return fs;
+        if (!fast) {
             ProfScope ps(h, "k_ingest", st);
             if (h->precombine) k_ingest<true><<<g, h->block, smem, st>>>(h->plan, T, A);
             else k_ingest<false><<<g, h->block, smem, st>>>(h->plan, T, A);
@@ -2193,6 +2202,10 @@ gb_status gb_agg_set_option(gb_agg *h, const char *name, int64_t value) {
         h->smem_slots = (int)value;
     } else if (n == "precombine") {
         h->precombine = value != 0;
+        h->precombine_set = true;
+    } else if (n == "fast_ingest") {
+        if (value < 0 || value > 1) return GB_ERR_INVALID;
+        h->fast_ingest = value != 0;
     } else if (n == "ctas_per_sm") {
         if (value < 1 || value > 4) return GB_ERR_INVALID;
         h->ctas_per_sm = (int)value;

@@ -22,7 +22,8 @@
 // dictionary growth) is re-run on its own handle afterwards.
 
 #define BATCH_TILE 16384  // default rows per work item (option "tile_rows")
-#define FAST_MAX_OPS 2
+#define FAST_MAX_OPS 4        // ops a register-resident plan holds (single-query kernels)
+#define BATCH_FAST_MAX_OPS 2  // ops of the batch's fast plan classes
 #define FAST_MAX_FILTERS 2
 
 // Integer-plan description kept in registers by the fast tile path (up to
@@ -187,6 +188,20 @@ __device__ __forceinline__ void fast_global(const FastPlan &F, const TableRef &T
     fast_apply_global<NOPS>(F, T.slots + (u64)s * (u64)T.stride + 1, cnt, v);
 }
 
+// As fast_global, for the single-query kernel: a key that finds no slot
+// within the probe bound becomes a spill record (the host grows the table and
+// merges the records) instead of a re-run.
+template <int NOPS>
+__device__ __forceinline__ void fast_global_spill(const FastPlan &F, const Plan &P, const TableRef &T, u64 pk, u64 cnt,
+                                                  const u64 *v, u32 *new_groups) {
+    const long long s = g_slot(T, pk, mix64(pk), new_groups);
+    if (s < 0) {
+        spill_record(P, T, pk, cnt, v);
+        return;
+    }
+    fast_apply_global<NOPS>(F, T.slots + (u64)s * (u64)T.stride + 1, cnt, v);
+}
+
 // Narrow shared states: count u32; ADD as a (lo, hi) u32 pair with carry;
 // CNT_NN u32; MIN/MAX s32 over SMALLINT/INTEGER, s64 over BIGINT.  Every
 // update is a native 32-bit shared atomic except the 64-bit MIN/MAX.
@@ -248,9 +263,9 @@ __device__ __forceinline__ void fast_smem_init(const FastPlan &F, u64 *keys, u32
     }
 }
 
-template <int NOPS>
+template <int NOPS, bool SPILL = false>
 __device__ __forceinline__ void fast_smem_flush(const FastPlan &F, const TableRef &T, const u64 *keys, const u32 *st,
-                                                int S, u32 *new_groups) {
+                                                int S, u32 *new_groups, const Plan *SP = nullptr) {
     for (int i = threadIdx.x; i < S; i += blockDim.x) {
         const u64 k = keys[i];
         if (k == EMPTY_KEY) continue;
@@ -266,7 +281,8 @@ __device__ __forceinline__ void fast_smem_flush(const FastPlan &F, const TableRe
             else if (kind == OP_MIN_I || kind == OP_MAX_I) v[j] = wide ? *(const u64 *)x : (u64)(i64)(int)x[0];
             else v[j] = x[0];
         }
-        fast_global<NOPS>(F, T, k, w[0], v, new_groups);
+        if (SPILL) fast_global_spill<NOPS>(F, *SP, T, k, w[0], v, new_groups);
+        else fast_global<NOPS>(F, T, k, w[0], v, new_groups);
     }
 }
 
@@ -353,9 +369,10 @@ __device__ __forceinline__ int fast_key_of(u32 kd, i64 a_, i64 b_, u32 vbits, u6
 }
 
 // One warp step of the fast path on fetched rows.
-template <bool PRECOMBINE, int NOPS, bool FILT>
+template <bool PRECOMBINE, int NOPS, bool FILT, bool SPILL = false>
 __device__ __forceinline__ void fast_rows(const FastPlan &F, const FastFilters &FF, const TableRef &T, u64 *keys,
-                                          u32 *st, int S, const FastRaw<NOPS, FILT> &w, u32 *new_groups) {
+                                          u32 *st, int S, const FastRaw<NOPS, FILT> &w, u32 *new_groups,
+                                          const Plan *SP = nullptr) {
     const int lane = threadIdx.x & 31;
     bool act = w.act && (!FILT || fast_pass(F, FF, w.f, w.vbits));
     u64 pk = 0;
@@ -412,7 +429,8 @@ __device__ __forceinline__ void fast_rows(const FastPlan &F, const FastFilters &
             s = (s + 1) & (u32)(S - 1);
         }
     }
-    fast_global<NOPS>(F, T, pk, cnt, v, new_groups);
+    if (SPILL) fast_global_spill<NOPS>(F, *SP, T, pk, cnt, v, new_groups);
+    else fast_global<NOPS>(F, T, pk, cnt, v, new_groups);
 }
 
 // One tile of the fast path (inlined into its class's kernel: the plan's
@@ -627,13 +645,16 @@ struct gb_batch {
 };
 
 // The fast-path description of a query's plan (eligible = 0 when the plan
-// has filters, a full-width pair key, floating-point ops or more than
-// FAST_MAX_OPS ops: such queries take the generic tile path).
-static FastPlan make_fast_plan(const Plan &P, FastFilters &FF) {
+// has more than FAST_MAX_FILTERS predicates or an IN / VARCHAR predicate, a
+// full-width pair key, floating-point ops or more than max_ops ops: such
+// queries take the generic tile path).
+static FastPlan make_fast_plan(const Plan &P, FastFilters &FF, int max_ops = BATCH_FAST_MAX_OPS) {
     FastPlan F;
     memset(&F, 0, sizeof F);
     memset(&FF, 0, sizeof FF);
-    if (P.n_filters > FAST_MAX_FILTERS || P.key_mode == KEY_WIDE || P.n_ops > FAST_MAX_OPS) return F;
+    if (P.n_filters > FAST_MAX_FILTERS || P.key_mode == KEY_WIDE || P.n_ops > max_ops ||
+        P.n_ops > FAST_MAX_OPS)
+        return F;
     auto is_int = [](int t) { return t == GB_T_SMALLINT || t == GB_T_INTEGER || t == GB_T_BIGINT; };
     for (int k = 0; k < P.n_keys; k++)
         if (!is_int(P.cols[P.key_col[k]].type)) return F;
@@ -677,6 +698,113 @@ static FastPlan make_fast_plan(const Plan &P, FastFilters &FF) {
     F.n_ops = P.n_ops;
     F.eligible = 1;
     return F;
+}
+
+// ----------------------------------------------------- single-query fast ingest
+// The hash ingest of one query whose plan compiles into registers (integer
+// keys and ops, up to FAST_MAX_OPS ops and FAST_MAX_FILTERS numeric
+// predicates): the batch's fast tile path as a persistent kernel over the
+// query's tiles, with one narrow shared table per CTA for the whole launch
+// and spill records instead of re-runs.  Same tile-claim / spill-threshold
+// protocol as k_ingest, so run_ingest drives both.
+template <bool PRE, int NOPS, bool NULLS, bool FILT>
+__global__ void __launch_bounds__(512, 2)
+    k_ingest_fast(const __grid_constant__ Plan P, const __grid_constant__ FastPlan F,
+                  const __grid_constant__ FastFilters FF, const TableRef T, const IngestArgs A) {
+    extern __shared__ u64 bsm[];
+    __shared__ u32 s_tile, s_new;
+    const int S = A.smem_slots;
+    u64 *keys = bsm;
+    u32 *st = (u32 *)(bsm + S);
+    if (threadIdx.x == 0) s_new = 0;
+    fast_smem_init<NOPS>(F, keys, st, S);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const u64 step = (u64)(blockDim.x >> 5) * 32;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            u32 t = ~0u;
+            if (*(volatile u32 *)&T.ctl->stop == 0) {
+                const u32 c = atomicAdd(&T.ctl->tile_counter, 1u);
+                if (c < A.n_tiles) t = c;
+            }
+            s_tile = t;
+        }
+        __syncthreads();
+        const u32 t = s_tile;
+        __syncthreads();
+        if (t == ~0u) break;
+        const u64 t0 = (u64)(A.first_tile + t) * A.tile_rows;
+        const u64 t1 = min(A.n_rows, t0 + A.tile_rows);
+        u64 base = t0 + (u64)warp * 32;
+        FastRaw<NOPS, FILT> cur, nxt;
+        fast_fetch<NOPS, NULLS, FILT>(F, FF, base + lane, t1, cur);
+        for (; base < t1; base += step) {
+            fast_fetch<NOPS, NULLS, FILT>(F, FF, base + step + lane, t1, nxt);
+            fast_rows<PRE, NOPS, FILT, true>(F, FF, T, keys, st, S, cur, &s_new, &P);
+            cur = nxt;
+        }
+        if (threadIdx.x == 0 && *(volatile u32 *)&T.ctl->spill_count > T.spill_threshold)
+            atomicExch(&T.ctl->stop, 1u);
+    }
+    __syncthreads();
+    fast_smem_flush<NOPS, true>(F, T, keys, st, S, &s_new, &P);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_new) atomicAdd(&T.ctl->n_groups, s_new);
+}
+
+typedef void (*FastIngestKernel)(Plan, FastPlan, FastFilters, TableRef, IngestArgs);
+
+#define GB_FI4(PRE_, N_)                                                                        \
+    {                                                                                           \
+        {k_ingest_fast<PRE_, N_, false, false>, k_ingest_fast<PRE_, N_, false, true>},          \
+        {                                                                                       \
+            k_ingest_fast<PRE_, N_, true, false>, k_ingest_fast<PRE_, N_, true, true>           \
+        }                                                                                       \
+    }
+
+static FastIngestKernel fast_ingest_kernel(int pre, int nops, int nulls, int filt) {
+    static const FastIngestKernel tab[2][FAST_MAX_OPS + 1][2][2] = {
+        {GB_FI4(false, 0), GB_FI4(false, 1), GB_FI4(false, 2), GB_FI4(false, 3), GB_FI4(false, 4)},
+        {GB_FI4(true, 0), GB_FI4(true, 1), GB_FI4(true, 2), GB_FI4(true, 3), GB_FI4(true, 4)},
+    };
+    return tab[pre][nops][nulls][filt];
+}
+#undef GB_FI4
+
+static gb_status launch_ingest_fast(gb_agg *h, const TableRef &T, IngestArgs A, int grid, cudaStream_t st,
+                                    bool *launched) {
+    *launched = false;
+    if (!h->fast_ingest || h->plan.n_dist || h->plan.str_key >= 0) return GB_OK;
+    FastFilters FF;
+    const FastPlan F = make_fast_plan(h->plan, FF, FAST_MAX_OPS);
+    if (!F.eligible) return GB_OK;
+    // the shared table pays when the estimated groups fit it; otherwise rows
+    // go straight to the HBM table (no probe of a full shared table)
+    const int S = h->est_groups <= (u64)A.smem_slots ? A.smem_slots : 0;
+    // narrow shared atomics beat the warp key match; without a shared table,
+    // few groups mean hot HBM slots, which the match relieves
+    const bool pre = h->precombine_set ? h->precombine : (S == 0 && h->est_groups <= 4096);
+    A.smem_slots = S;
+    const size_t smem = (size_t)S * (8 + 4 * (size_t)F.swords);
+    static bool attr_set = false;
+    if (!attr_set) {
+        for (int a = 0; a < 2; a++)
+            for (int n = 0; n <= FAST_MAX_OPS; n++)
+                for (int u = 0; u < 2; u++)
+                    for (int f = 0; f < 2; f++)
+                        GB_CUDA(cudaFuncSetAttribute(fast_ingest_kernel(a, n, u, f),
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        attr_set = true;
+    }
+    {
+        ProfScope ps(h, "k_ingest_fast", st);
+        fast_ingest_kernel(pre, F.n_ops, F.nulls != 0, F.n_filters != 0)<<<grid, 512, smem, st>>>(h->plan, F, FF, T,
+                                                                                                   A);
+    }
+    GB_CUDA(cudaGetLastError());
+    *launched = true;
+    return GB_OK;
 }
 
 // Dynamic shared memory of one k_batch_ingest CTA so that `ctas` CTAs fit on
