@@ -173,19 +173,20 @@ __global__ void k_merge_records(const __grid_constant__ Plan P, const u64 *recs,
 
 // Compact used slots into dense result columns (the direct emit of
 // physical_planner.cpp:8027-8173 with agg_emit_helpers.cpp:26-165 rules).
-// Each CTA takes chunks of COMPACT_PER * blockDim slots; one output
-// reservation per chunk.
+// Each CTA takes chunks of `per` * blockDim slots (per <= COMPACT_PER; small
+// tables use fewer slots per thread so that more CTAs share them); one
+// output reservation per chunk.
 #define COMPACT_PER 8
 __global__ void k_compact(const __grid_constant__ Plan P, const u64 *slots, u64 cap, int stride,
-                          const __grid_constant__ EmitArgs E, Ctl *ctl) {
+                          const __grid_constant__ EmitArgs E, Ctl *ctl, int per) {
     const u64 total = cap + 2;
-    const u64 chunk = (u64)COMPACT_PER * blockDim.x;
+    const u64 chunk = (u64)per * blockDim.x;
     for (u64 c0 = blockIdx.x * chunk; c0 < total; c0 += (u64)gridDim.x * chunk) {
         u32 mine = 0;
 #pragma unroll
         for (int j = 0; j < COMPACT_PER; j++) {
             const u64 s = c0 + (u64)j * blockDim.x + threadIdx.x;
-            if (s >= total) break;
+            if (j >= per || s >= total) break;
             const u64 *sl = slots + s * (u64)stride;
             mine += (s < cap) ? (sl[0] != EMPTY_KEY) : (sl[1] != 0);
         }
@@ -193,7 +194,7 @@ __global__ void k_compact(const __grid_constant__ Plan P, const u64 *slots, u64 
 #pragma unroll
         for (int j = 0; j < COMPACT_PER; j++) {
             const u64 s = c0 + (u64)j * blockDim.x + threadIdx.x;
-            if (s >= total) break;
+            if (j >= per || s >= total) break;
             const u64 *sl = slots + s * (u64)stride;
             const bool occ = (s < cap) ? (sl[0] != EMPTY_KEY) : (sl[1] != 0);
             if (!occ) continue;
@@ -1447,6 +1448,7 @@ static gb_status compile_plan(gb_agg *h) {
         P.key_type[i] = t;
     }
     P.n_keys = ng;
+    P.str_key = -1;
     if (ng == 1) {
         P.key_mode = (h->col_types[P.key_col[0]] == GB_T_VARCHAR) ? KEY_STRING : KEY_SINGLE;
         if (P.key_mode == KEY_STRING) {
@@ -1999,8 +2001,13 @@ gb_status gb_agg_finalize(gb_agg *h, void *stream) {
     fill_emit(h, E, h->out_cols, h->out_valid, h->out_cap);
     {
         ProfScope ps(h, "k_compact", st);
-        k_compact<<<grid_for((h->cap + 2 + COMPACT_PER - 1) / COMPACT_PER, 256, sm_count() * 4), 256, 0, st>>>(
-            h->plan, (const u64 *)h->table.p, h->cap, h->plan.stride, E, dctl);
+        // slots per thread: up to COMPACT_PER, fewer where the table would
+        // otherwise occupy under two CTAs per SM
+        const u64 slots_n = h->cap + 2;
+        int per = COMPACT_PER;
+        while (per > 1 && slots_n / ((u64)per * 256) < (u64)sm_count() * 2) per >>= 1;
+        k_compact<<<grid_for((slots_n + per - 1) / per, 256, sm_count() * 4), 256, 0, st>>>(
+            h->plan, (const u64 *)h->table.p, h->cap, h->plan.stride, E, dctl, per);
     }
     h->launches++;
     GB_CUDA(cudaGetLastError());

@@ -64,6 +64,12 @@ struct BQuery {
     const int64_t *soffs;
     const uint64_t *svalid;
     long long *ids;
+    // VARCHAR results emitted inside the batch: per-row lengths, offsets
+    // (n + 1), bytes, and per-chunk sums then bases
+    int64_t *str_lens;
+    int64_t *str_offs;
+    uint8_t *str_out;
+    int64_t *str_chunk;
     u32 *sretry;
     u64 n_rows;
     u64 table_words;
@@ -612,14 +618,157 @@ __global__ void k_batch_compact(const BQuery *qs, const BItem *items, u32 n_item
     }
 }
 
+// ------------------------------------------------------- VARCHAR results
+// The string ids a VARCHAR query emitted become offsets + bytes inside the
+// batch (no per-query host round trip): lengths and per-chunk sums, one scan
+// of the chunk sums per query, then offsets and a byte gather per chunk.
+// The row count is the query's out_count, read on the device.
+#define STR_EMIT_CHUNK 4096
+
+__device__ __forceinline__ long long block_sum_ll(long long x, long long *s_part) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(FULL, x, o);
+    if (lane == 0) s_part[warp] = x;
+    __syncthreads();
+    long long t = 0;
+    if (threadIdx.x == 0)
+        for (int w = 0; w < nwarps; w++) t += s_part[w];
+    __syncthreads();
+    return t;  // valid in thread 0
+}
+
+__global__ void k_batch_str_len(const BQuery *qs, const BItem *items, u32 n_items) {
+    __shared__ long long s_part[32];
+    for (u32 it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const BItem w = items[it];
+        const BQuery &q = qs[w.q];
+        const u64 n = min((u64)q.T.ctl->out_count, q.E.out_cap);  // an overflow re-runs on the handle
+        const u64 lo = (u64)w.idx * STR_EMIT_CHUNK, hi = min(n, lo + STR_EMIT_CHUNK);
+        const long long *ids = (const long long *)q.E.out[0];
+        long long local = 0;
+        for (u64 r = lo + threadIdx.x; r < hi; r += blockDim.x) {
+            const long long id = ids[r];
+            const int64_t len = id < 0 ? 0 : (int64_t)(q.D.ref_by_id[id] & 0xffffffu);
+            if (id < 0) atomicAnd((unsigned long long *)&q.E.valid[0][r >> 6], ~(1ull << (r & 63)));
+            q.str_lens[r] = len;
+            local += len;
+        }
+        const long long t = block_sum_ll(local, s_part);
+        if (threadIdx.x == 0) q.str_chunk[w.idx] = t;
+    }
+}
+
+// One block per VARCHAR query: exclusive scan of its chunk sums (in place)
+// and the final offset.
+__global__ void k_batch_str_scan(const BQuery *qs, const u32 *str_queries, u32 n_q) {
+    __shared__ long long s_part[32];
+    __shared__ long long s_carry;
+    for (u32 i = blockIdx.x; i < n_q; i += gridDim.x) {
+        const BQuery &q = qs[str_queries[i]];
+        const u64 n = min((u64)q.T.ctl->out_count, q.E.out_cap);  // an overflow re-runs on the handle
+        const u64 nch = (n + STR_EMIT_CHUNK - 1) / STR_EMIT_CHUNK;
+        if (threadIdx.x == 0) s_carry = 0;
+        __syncthreads();
+        for (u64 c0 = 0; c0 < nch; c0 += blockDim.x) {
+            const u64 c = c0 + threadIdx.x;
+            const long long x = c < nch ? q.str_chunk[c] : 0;
+            // block inclusive scan
+            const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+            long long incl = x;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long y = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane == 31) s_part[warp] = incl;
+            __syncthreads();
+            if (warp == 0) {
+                const long long wv = lane < nwarps ? s_part[lane] : 0;
+                long long wi = wv;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const long long y = __shfl_up_sync(FULL, wi, o);
+                    if (lane >= o) wi += y;
+                }
+                if (lane < nwarps) s_part[lane] = wi - wv;
+            }
+            __syncthreads();
+            const long long base = s_carry + s_part[warp];
+            if (c < nch) q.str_chunk[c] = base + incl - x;
+            __syncthreads();
+            if (threadIdx.x == blockDim.x - 1) s_carry = base + incl;
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) q.str_offs[n] = s_carry;
+        __syncthreads();
+    }
+}
+
+__global__ void k_batch_str_gather(const BQuery *qs, const BItem *items, u32 n_items) {
+    __shared__ long long s_part[32];
+    __shared__ long long s_run;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (u32 it = blockIdx.x; it < n_items; it += gridDim.x) {
+        const BItem w = items[it];
+        const BQuery &q = qs[w.q];
+        const u64 n = min((u64)q.T.ctl->out_count, q.E.out_cap);  // an overflow re-runs on the handle
+        const u64 lo = (u64)w.idx * STR_EMIT_CHUNK, hi = min(n, lo + STR_EMIT_CHUNK);
+        if (lo >= hi) continue;  // uniform across the block
+        if (threadIdx.x == 0) s_run = q.str_chunk[w.idx];
+        __syncthreads();
+        // offsets: block-wide exclusive scan of the lengths, blockDim rows at a time
+        for (u64 r0 = lo; r0 < hi; r0 += blockDim.x) {
+            const u64 r = r0 + threadIdx.x;
+            const long long x = r < hi ? q.str_lens[r] : 0;
+            long long incl = x;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const long long y = __shfl_up_sync(FULL, incl, o);
+                if (lane >= o) incl += y;
+            }
+            if (lane == 31) s_part[warp] = incl;
+            __syncthreads();
+            if (warp == 0) {
+                const long long wv = lane < nwarps ? s_part[lane] : 0;
+                long long wi = wv;
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const long long y = __shfl_up_sync(FULL, wi, o);
+                    if (lane >= o) wi += y;
+                }
+                if (lane < nwarps) s_part[lane] = wi - wv;
+            }
+            __syncthreads();
+            const long long off = s_run + s_part[warp] + incl - x;
+            if (r < hi) q.str_offs[r] = off;
+            __syncthreads();
+            if (threadIdx.x == blockDim.x - 1) s_run = off + x;
+            __syncthreads();
+        }
+        // bytes: one warp per string
+        const long long *ids = (const long long *)q.E.out[0];
+        for (u64 r = lo + warp; r < hi; r += nwarps) {
+            const long long id = ids[r];
+            if (id < 0) continue;
+            const u64 ref = q.D.ref_by_id[id];
+            const u32 len = (u32)(ref & 0xffffffu);
+            const uint8_t *src = q.D.arena + (ref >> 24);
+            uint8_t *dst = q.str_out + q.str_offs[r];
+            for (u32 b = lane; b < len; b += 32) dst[b] = src[b];
+        }
+        __syncthreads();
+    }
+}
+
 // ================================================================== host
 struct gb_batch {
     std::vector<gb_agg *> handles;
     std::vector<std::vector<gb_col>> cols;
     std::vector<u64> rows;
-    DevBuf qdesc, items_init, items_str, items_ingest, items_compact, bctl, qctl;
+    DevBuf qdesc, items_init, items_str, items_ingest, items_compact, items_semit, str_queries, bctl, qctl;
     HostBuf qctl_host;
-    u32 n_init = 0, n_str = 0, n_ingest = 0, n_compact = 0;
+    u32 n_init = 0, n_str = 0, n_ingest = 0, n_compact = 0, n_semit = 0, n_strq = 0;
     u32 cls_off[BATCH_CLASSES] = {}, cls_n[BATCH_CLASSES] = {};  // ingest items per plan class
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -818,7 +967,8 @@ static int batch_smem_bytes(int ctas) {
 static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
     const u32 nq = (u32)b->handles.size();
     std::vector<BQuery> qs(nq);
-    std::vector<BItem> it_init, it_str, it_ing, it_cmp;
+    std::vector<BItem> it_init, it_str, it_ing, it_cmp, it_semit;
+    std::vector<u32> strq;
     gb_status s;
     if ((s = b->qctl.ensure((size_t)nq * sizeof(Ctl) + 64)) || (s = b->bctl.ensure(BATCH_CLASSES * sizeof(Ctl))) ||
         (s = b->qctl_host.ensure((size_t)nq * sizeof(Ctl) + 64)))
@@ -899,6 +1049,20 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
         d.tile_rows = b->tile_rows;
         for (u64 c = 0; c * b->tile_rows < n; c++) it_ing.push_back({q, (u32)c});
         for (u64 c = 0; c * (COMPACT_PER * 256) < h->cap + 2; c++) it_cmp.push_back({q, (u32)c});
+        if (d.is_str) {
+            // string results for up to out_cap groups; their bytes are at most
+            // the dictionary arena's (each distinct string is stored once)
+            const u64 nch = (h->out_cap + STR_EMIT_CHUNK - 1) / STR_EMIT_CHUNK;
+            if ((s = h->str_lens.ensure(h->out_cap * 8 + 8)) || (s = h->out_str_offs.ensure(h->out_cap * 8 + 16)) ||
+                (s = h->out_str_bytes.ensure(h->sd_arena_cap + 16)) || (s = h->scan_tmp.ensure(nch * 8 + 16)))
+                return s;
+            d.str_lens = (int64_t *)h->str_lens.p;
+            d.str_offs = (int64_t *)h->out_str_offs.p;
+            d.str_out = (uint8_t *)h->out_str_bytes.p;
+            d.str_chunk = (int64_t *)h->scan_tmp.p;
+            for (u64 c = 0; c < nch; c++) it_semit.push_back({q, (u32)c});
+            strq.push_back(q);
+        }
     }
     // Tile order: query-major by default (the CTAs sweep one query's table
     // at a time, which keeps it in L2); "order" 1 interleaves the queries.
@@ -941,7 +1105,9 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
         (s = b->items_init.ensure(it_init.size() * sizeof(BItem) + 64)) ||
         (s = b->items_str.ensure(it_str.size() * sizeof(BItem) + 64)) ||
         (s = b->items_ingest.ensure(it_ing.size() * sizeof(BItem) + 64)) ||
-        (s = b->items_compact.ensure(it_cmp.size() * sizeof(BItem) + 64)))
+        (s = b->items_compact.ensure(it_cmp.size() * sizeof(BItem) + 64)) ||
+        (s = b->items_semit.ensure(it_semit.size() * sizeof(BItem) + 64)) ||
+        (s = b->str_queries.ensure(strq.size() * sizeof(u32) + 64)))
         return s;
     GB_CUDA(cudaMemcpy(b->qdesc.p, qs.data(), qs.size() * sizeof(BQuery), cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(b->items_init.p, it_init.data(), it_init.size() * sizeof(BItem), cudaMemcpyHostToDevice));
@@ -949,6 +1115,12 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
         GB_CUDA(cudaMemcpy(b->items_str.p, it_str.data(), it_str.size() * sizeof(BItem), cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(b->items_ingest.p, it_ing.data(), it_ing.size() * sizeof(BItem), cudaMemcpyHostToDevice));
     GB_CUDA(cudaMemcpy(b->items_compact.p, it_cmp.data(), it_cmp.size() * sizeof(BItem), cudaMemcpyHostToDevice));
+    if (!strq.empty()) {
+        GB_CUDA(cudaMemcpy(b->items_semit.p, it_semit.data(), it_semit.size() * sizeof(BItem), cudaMemcpyHostToDevice));
+        GB_CUDA(cudaMemcpy(b->str_queries.p, strq.data(), strq.size() * sizeof(u32), cudaMemcpyHostToDevice));
+    }
+    b->n_semit = (u32)it_semit.size();
+    b->n_strq = (u32)strq.size();
     b->n_init = (u32)it_init.size();
     b->n_str = (u32)it_str.size();
     b->n_ingest = (u32)it_ing.size();
@@ -1025,6 +1197,16 @@ static gb_status batch_enqueue(gb_batch *b, cudaStream_t st) {
     k_batch_compact<<<std::max(1, std::min((int)b->n_compact, sms * 8)), 256, 0, st>>>(
         (const BQuery *)b->qdesc.p, (const BItem *)b->items_compact.p, b->n_compact);
     GB_CUDA(cudaGetLastError());
+    if (b->n_strq) {
+        const BQuery *qd = (const BQuery *)b->qdesc.p;
+        const BItem *si = (const BItem *)b->items_semit.p;
+        const int g = std::max(1, std::min((int)b->n_semit, sms * 8));
+        k_batch_str_len<<<g, 256, 0, st>>>(qd, si, b->n_semit);
+        k_batch_str_scan<<<std::min((int)b->n_strq, sms * 4), 1024, 0, st>>>(qd, (const u32 *)b->str_queries.p,
+                                                                            b->n_strq);
+        k_batch_str_gather<<<g, 256, 0, st>>>(qd, si, b->n_semit);
+        GB_CUDA(cudaGetLastError());
+    }
     batch_prof(b, 3, st, false);
     GB_CUDA(cudaMemcpyAsync(b->qctl_host.p, b->qctl.p, (size_t)nq * sizeof(Ctl), cudaMemcpyDeviceToHost, st));
     return GB_OK;
@@ -1231,7 +1413,7 @@ gb_status gb_batch_run(gb_batch *b, void *stream) {
     }
     u32 ncls = 0;
     for (int c = 0; c < BATCH_CLASSES; c++) ncls += b->cls_n[c] ? 1 : 0;
-    b->launches += 2 + ncls + (b->n_str ? 1 : 0);
+    b->launches += 2 + ncls + (b->n_str ? 1 : 0) + (b->n_strq ? 3 : 0);
     GB_CUDA(cudaStreamSynchronize(st));
     batch_prof_collect(b);
     const Ctl *qc = (const Ctl *)b->qctl_host.p;
@@ -1253,8 +1435,7 @@ gb_status gb_batch_run(gb_batch *b, void *stream) {
         h->n_rows_out = c.out_count;
         h->topn_applied = false;
         h->finalized = true;
-        h->has_result = false;
-        if (h->str_col >= 0 && (s = strdict_emit(h, (const long long *)h->out_cols[0].p, h->n_rows_out, st))) return s;
+        h->has_result = false;  // a VARCHAR key's strings were emitted inside the batch
     }
     if (b->handles.size() && b->slow.size() < nq) GB_CUDA(cudaStreamSynchronize(st));
     if (!b->slow.empty()) {
@@ -1312,7 +1493,8 @@ void gb_batch_destroy(gb_batch *b) {
     }
     for (auto *h : b->handles) gb_agg_destroy(h);
     for (auto &e : b->pool) gb_agg_destroy(e.second);
-    for (DevBuf *d : {&b->qdesc, &b->items_init, &b->items_str, &b->items_ingest, &b->items_compact, &b->bctl, &b->qctl})
+    for (DevBuf *d : {&b->qdesc, &b->items_init, &b->items_str, &b->items_ingest, &b->items_compact, &b->items_semit,
+                      &b->str_queries, &b->bctl, &b->qctl})
         d->release();
     b->qctl_host.release();
     delete b;
