@@ -66,6 +66,8 @@ def parse():
     ap.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")
     ap.add_argument("--scale", type=float, default=1.0, help="serve: resident table scale (1.0 = ~66 GB)")
     ap.add_argument("--budget-gb", type=float, default=40.0, help="serve: admission budget")
+    ap.add_argument("--capacity-queries", type=int, default=3000,
+                    help="serve: queries of the stream submitted at once to measure each mode's capacity")
     return ap.parse_args()
 
 
@@ -765,11 +767,14 @@ def run_batch_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def _serve_stream(srv, queries, t0_wall):
-    """Submit `queries` at their arrival times (seconds after t0_wall) and
-    wait for all of them; returns (tickets, submit wall times)."""
+def _serve_stream(srv, queries, t0_wall, on_done):
+    """Submit `queries` at their arrival times (seconds after t0_wall) from a
+    thread while this thread waits for each ticket in submission order and
+    hands it to on_done(i, ticket), which releases it (results are not held
+    for the whole stream)."""
     import threading
     tickets = [None] * len(queries)
+    ready = threading.Semaphore(0)
     errors = []
 
     def submitter():
@@ -780,17 +785,32 @@ def _serve_stream(srv, queries, t0_wall):
                     time.sleep(delay)
                 tickets[i] = srv.submit(q["table"], q["r0"], q["r1"], q["group_cols"], q["aggs"],
                                         filters=q["filters"], est_groups=q["est_groups"])
+                ready.release()
         except Exception as e:  # surfaced below
             errors.append(e)
+            ready.release()
 
     th = threading.Thread(target=submitter)
     th.start()
+    for i in range(len(queries)):
+        ready.acquire()
+        if errors:
+            break
+        srv.wait(tickets[i])
+        on_done(i, tickets[i])
     th.join()
     if errors:
         raise errors[0]
-    for t in tickets:
-        srv.wait(t)
-    return tickets
+
+
+def results_mismatch(rb, ra, nk):
+    """None when two results of one query (lists of (values, valid), keys
+    first) hold the same groups with equal integers and DOUBLE values within
+    REL_TOL_F64 of each other; else the first difference."""
+    ref = {"n_groups": len(ra[0][0]), "keys": [ra[j][0] for j in range(nk)],
+           "key_null": [~np.asarray(ra[j][1], bool) for j in range(nk)],
+           "aggs": [(v, ~np.asarray(m, bool), v) for v, m in ra[nk:]]}
+    return oracle_mismatch(rb, ref, nk)
 
 
 def run_serve(args):
@@ -840,15 +860,10 @@ def run_serve(args):
             srv.wait(t)
             srv.release(t)
         st0 = srv.stats()
-        clocks = Clocks(local)
-        clocks.start()
-        w0 = time.perf_counter()
-        tickets = _serve_stream(srv, queries, w0)
-        w1 = time.perf_counter()
-        clk = clocks.stop()
         lat = []
         exec_by_shape = {}
-        for i, t in enumerate(tickets):
+
+        def on_done(i, t):
             qm, em, bs = srv.times(t)
             lat.append(qm + em)
             if mode == 1:
@@ -856,6 +871,13 @@ def run_serve(args):
             if i in sample:
                 results.setdefault(i, []).append(srv.result(t))
             srv.release(t)
+
+        clocks = Clocks(local)
+        clocks.start()
+        w0 = time.perf_counter()
+        _serve_stream(srv, queries, w0, on_done)
+        w1 = time.perf_counter()
+        clk = clocks.stop()
         st = srv.stats()
         lat = np.array(lat)
         out[name] = {"queries_per_s": len(queries) / (w1 - w0), "wall_s": w1 - w0,
@@ -866,6 +888,18 @@ def run_serve(args):
                      "peak_admitted_GB": st["peak_admitted_bytes"] / 2**30,
                      "kernel_launches": st["kernel_launches"] - st0["kernel_launches"],
                      "result_bytes": st["result_bytes"] - st0["result_bytes"], "clocks": clk}
+        # capacity: the first --capacity-queries queries of the stream, all
+        # submitted at once (the server saturated; latency is queueing here)
+        capq = [dict(q, at=0.0) for q in queries[:args.capacity_queries]]
+        if capq:
+            c_st0 = srv.stats()
+            c0 = time.perf_counter()
+            _serve_stream(srv, capq, c0, lambda i, t: srv.release(t))
+            c1 = time.perf_counter()
+            c_st = srv.stats()
+            out[name]["capacity"] = {"queries": len(capq), "wall_s": c1 - c0, "queries_per_s": len(capq) / (c1 - c0),
+                                     "busy_ms": c_st["busy_ms"] - c_st0["busy_ms"],
+                                     "batches": c_st["batches"] - c_st0["batches"]}
         if mode == 1:
             out[name]["per_shape"] = {
                 str(k): {"queries": len(v), "mean_exec_ms": float(np.mean([e for e, _ in v])),
@@ -875,32 +909,12 @@ def run_serve(args):
     # per-result identity, mixed (batched) vs alone: integer columns
     # bit-exact, DOUBLE columns within 1e-12 relative (their sums are
     # accumulated in a different order on each run)
-    same, worst, why = 0, 0.0, []
+    same, why = 0, []
     for i, (rb, ra) in results.items():
-        ok = len(rb[0][0]) == len(ra[0][0])
-        if not ok:
-            why.append("q%d shape %d: %d vs %d groups" % (i, queries[i]["shape"], len(rb[0][0]), len(ra[0][0])))
-        if ok:
-            nk = len(queries[i]["group_cols"])
-            def order(r):
-                return sorted(range(len(r[0][0])), key=lambda j: tuple(
-                    (bool(r[c][1][j]), r[c][0][j] if r[c][1][j] else 0) for c in range(nk)))
-            ob, oa = order(rb), order(ra)
-            for (vb, nb), (va, na) in zip(rb, ra):
-                vb, nb, va, na = vb[ob], nb[ob], va[oa], na[oa]
-                if not np.array_equal(nb, na):
-                    ok = False
-                elif vb.dtype == np.float64:
-                    m = nb
-                    d = np.abs(vb[m] - va[m]) / np.maximum(np.abs(va[m]), 1e-300)
-                    w = float(d.max()) if d.size else 0.0
-                    worst = max(worst, w)
-                    ok = ok and w <= 1e-12
-                else:
-                    ok = ok and bool(np.array_equal(vb[nb], va[na]))
-            if not ok:
-                why.append("q%d shape %d: values differ" % (i, queries[i]["shape"]))
-        same += ok
+        d = results_mismatch(rb, ra, len(queries[i]["group_cols"]))
+        if d:
+            why.append("q%d shape %d: %s" % (i, queries[i]["shape"], d))
+        same += d is None
     # oracle parity of the sampled queries (their row ranges copied to the
     # host); the same oracle pass, all host threads per query, is the timed
     # CPU baseline on that sample of the mix
@@ -948,8 +962,11 @@ def run_serve(args):
             "p50_ms": b["p50_ms"], "p95_ms": b["p95_ms"], "p99_ms": b["p99_ms"],
             "batched": b, "one_at_a_time": out["one_at_a_time"],
             "speedup_vs_one_at_a_time": out["one_at_a_time"]["wall_s"] / b["wall_s"],
-            "identity_alone_vs_mixed": "%d/%d sampled results identical (integers bit-exact, DOUBLE max rel "
-                                        "diff %.1e)" % (same, len(results), worst),
+            "capacity_speedup_vs_one_at_a_time": (b["capacity"]["queries_per_s"] /
+                                                  out["one_at_a_time"]["capacity"]["queries_per_s"])
+            if "capacity" in b else None,
+            "identity_alone_vs_mixed": "%d/%d sampled results identical (integers bit-exact, DOUBLE within "
+                                        "1e-12 relative)" % (same, len(results)),
             "identity_mismatches": why[:6],
             "parity": {"oracle_mismatches": len(orc_diffs), "sampled": len(results), "first": orc_diffs[:4]},
             "roofline": roofline, "cpu_baseline": cpu,

@@ -746,16 +746,22 @@ __global__ void k_batch_str_gather(const BQuery *qs, const BItem *items, u32 n_i
             if (threadIdx.x == blockDim.x - 1) s_run = off + x;
             __syncthreads();
         }
-        // bytes: one warp per string
+        // bytes: one thread per string (the id → ref → bytes chains of a
+        // block's rows overlap); arena entries are 8-byte aligned and padded,
+        // so the source is read in whole words
         const long long *ids = (const long long *)q.E.out[0];
-        for (u64 r = lo + warp; r < hi; r += nwarps) {
+        for (u64 r = lo + threadIdx.x; r < hi; r += blockDim.x) {
             const long long id = ids[r];
             if (id < 0) continue;
             const u64 ref = q.D.ref_by_id[id];
             const u32 len = (u32)(ref & 0xffffffu);
-            const uint8_t *src = q.D.arena + (ref >> 24);
+            const u64 *src = (const u64 *)(q.D.arena + (ref >> 24));
             uint8_t *dst = q.str_out + q.str_offs[r];
-            for (u32 b = lane; b < len; b += 32) dst[b] = src[b];
+            for (u32 b = 0; b < len; b += 8) {
+                const u64 x = src[b >> 3];
+                const u32 m = min(8u, len - b);
+                for (u32 j = 0; j < m; j++) dst[b + j] = (uint8_t)(x >> (8 * j));
+            }
         }
         __syncthreads();
     }
