@@ -1763,6 +1763,18 @@ gb_status gb_agg_set_filters(gb_agg *h, const gb_filter *filters, uint32_t n_fil
         compile_filters(h);
         return s;
     }
+    // a radix handle's partition pass depends on the predicates: re-prepare
+    // when they change which pass it takes
+    if (h->mode == 1 && radix_spec_of(h->plan, h->rplan, h->nullable_mask) != h->rplan.spec) {
+        RadixPlan R;
+        if (gb_status s = radix_prepare(h->plan, R, std::max<u64>(h->est_groups, 1u << 16), h->nullable_mask)) {
+            h->filters = old;
+            compile_filters(h);
+            set_error("these filters do not fit the handle's radix plan");
+            return s;
+        }
+        h->rplan = R;
+    }
     return GB_OK;
 }
 

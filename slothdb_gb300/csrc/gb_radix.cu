@@ -586,8 +586,9 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
 
 // ------------------------------------------------------------- P1, one key + one SUM
 // The specialised P1 for the plan "one non-NULL BIGINT key, one non-NULL
-// value column, one SUM (DOUBLE: OPK = OP_ADD_F, BIGINT: OP_ADD_I), no
-// predicates".  Nothing in its row loop waits on other warps: each warp
+// value column, one SUM (DOUBLE: OPK = OP_ADD_F, BIGINT: OP_ADD_I), at most
+// one numeric predicate on the value column (FILT)".  A row that fails the
+// predicate is dropped before its hot-table probe.  Nothing in its row loop waits on other warps: each warp
 // claims P1D_CLAIM steps of P1D_RUN rows at a time and streams them with
 // 128-bit loads (4 rows per lane).  A hot row (its key in the 2-way bucket
 // table) counts in registers (the REG_HOT hottest keys) or in a shared u32
@@ -606,7 +607,7 @@ size_t radix_p1d_smem(const RadixPlan &R) {
     return HB * 16 + NP * 8 + HB * 4 + NP * 4 + (size_t)R.nh * 4;
 }
 
-template <int OPK>
+template <int OPK, bool FILT>
 __global__ void __launch_bounds__(P1_WARPS * 32, 1)
     k_partition_direct(const __grid_constant__ Plan P, const __grid_constant__ RadixPlan R, const RadixRef X,
                        const TableRef T, const RadixTile A) {
@@ -634,6 +635,9 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
     u64 *hsum = X.hot_part + (u64)blockIdx.x * NH * W + P.ops[0].word;  // this CTA's hot slice, SUM word
     u64 *oob = T.slots + T.cap * (u64)T.stride + 1;  // state words of the key equal to EMPTY_KEY
     const u64 n = A.n_rows;
+    const int fop = FILT ? P.filters[0].op : 0;
+    const double fdc = FILT ? P.filters[0].dc : 0.0;
+    const i64 fic = FILT ? P.filters[0].ic : 0;
     u32 rc[REG_HOT];
 #pragma unroll
     for (int q = 0; q < REG_HOT; q++) rc[q] = 0;
@@ -673,6 +677,14 @@ __global__ void __launch_bounds__(P1_WARPS * 32, 1)
                         v[j] = vcol[r];
                         live |= 1u << j;
                     }
+                }
+            }
+            if (FILT) {
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const bool pass = OPK == OP_ADD_F ? cmp_f(fop, __longlong_as_double((i64)v[j]), fdc)
+                                                      : cmp_i(fop, (i64)v[j], fic);
+                    if (!pass) live &= ~(1u << j);
                 }
             }
             u32 cp[4];  // partition + 1 of a cold row, 0 otherwise
@@ -1084,12 +1096,16 @@ u64 radix_inflight_rows(const RadixPlan &R, int grid) {
 static int p1_spec(const Plan &P, const RadixPlan &R, u64 nullable_mask) {
     if (P.key_mode != KEY_SINGLE || P.cols[P.key_col[0]].type != GB_T_BIGINT) return 0;
     if ((nullable_mask >> P.key_col[0]) & 1ull) return 0;
-    if (R.V != 1 || P.n_ops != 1 || P.n_filters || ((nullable_mask >> R.vcol[0]) & 1ull)) return 0;
+    if (R.V != 1 || P.n_ops != 1 || P.n_filters > 1 || ((nullable_mask >> R.vcol[0]) & 1ull)) return 0;
+    // one compare on the value column itself (its type is the op's)
+    if (P.n_filters && (P.filters[0].col != R.vcol[0] || P.filters[0].op > GB_CMP_GE)) return 0;
     const int t = P.cols[R.vcol[0]].type;
     if (P.ops[0].kind == OP_ADD_F && t == GB_T_DOUBLE) return OP_ADD_F;
     if (P.ops[0].kind == OP_ADD_I && t == GB_T_BIGINT) return OP_ADD_I;
     return 0;
 }
+
+int radix_spec_of(const Plan &P, const RadixPlan &R, u64 nullable_mask) { return p1_spec(P, R, nullable_mask); }
 
 static const size_t kSmemBudget = 224 * 1024;  // <= the 227 KiB opt-in minus static shared memory
 
@@ -1230,7 +1246,7 @@ static void fill_tables(P1Fn *t1, P2Fn *t2) {
 
 static P1Fn g_p1[4 * (RADIX_MAX_OPS + 1)];
 static P2Fn g_p2[4 * (RADIX_MAX_OPS + 1)];
-static P1Fn g_p1_spec_f, g_p1_spec_i;  // specialised P1: BIGINT key, one SUM (DOUBLE / integer)
+static P1Fn g_p1_spec[2][2];  // specialised P1: BIGINT key, one SUM [integer, DOUBLE][predicate]
 static P2Fn g_p2_gw[RADIX_MAX_OPS + 1];  // P2 with the state words in L2 (ops all DOUBLE SUM), one value column
 
 static gb_status radix_set_attributes() {
@@ -1239,11 +1255,13 @@ static gb_status radix_set_attributes() {
     fill_tables<1>(g_p1, g_p2);
     fill_tables<2>(g_p1, g_p2);
     fill_tables<3>(g_p1, g_p2);
-    g_p1_spec_f = (P1Fn)k_partition_direct<OP_ADD_F>;
-    g_p1_spec_i = (P1Fn)k_partition_direct<OP_ADD_I>;
+    g_p1_spec[0][0] = (P1Fn)k_partition_direct<OP_ADD_I, false>;
+    g_p1_spec[0][1] = (P1Fn)k_partition_direct<OP_ADD_I, true>;
+    g_p1_spec[1][0] = (P1Fn)k_partition_direct<OP_ADD_F, false>;
+    g_p1_spec[1][1] = (P1Fn)k_partition_direct<OP_ADD_F, true>;
     g_p2_gw[1] = (P2Fn)k_part_agg_sum<1>;
     g_p2_gw[2] = (P2Fn)k_part_agg_sum<2>;
-    for (P1Fn f : {g_p1_spec_f, g_p1_spec_i})
+    for (P1Fn f : {g_p1_spec[0][0], g_p1_spec[0][1], g_p1_spec[1][0], g_p1_spec[1][1]})
         if (gb_status s = allow_max_smem(f)) return s;
     if (gb_status s = allow_max_smem(k_hot_rank)) return s;
     for (int o = 1; o <= 2; o++)
@@ -1270,7 +1288,7 @@ gb_status radix_launch_p1(const Plan &P, const RadixPlan &R, const RadixRef &X, 
             set_error("radix plan: a NOT NULL column carries a validity mask");
             return GB_ERR_INVALID;
         }
-        f = R.spec == OP_ADD_F ? g_p1_spec_f : g_p1_spec_i;
+        f = g_p1_spec[R.spec == OP_ADD_F ? 1 : 0][P.n_filters ? 1 : 0];
         smem = radix_p1d_smem(R);
     }
     f<<<grid, P1_WARPS * 32, smem, st>>>(P, R, X, T, A);

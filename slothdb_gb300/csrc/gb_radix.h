@@ -56,6 +56,9 @@ struct RadixTile {
 gb_status radix_prepare(const Plan &P, RadixPlan &R, u64 est_groups, u64 nullable_mask);
 size_t radix_p1_smem(const Plan &P, const RadixPlan &R);
 gb_status radix_set_bits(const Plan &P, RadixPlan &R, int bits);
+// The specialised-P1 kind radix_prepare would pick for P now (0: none); a
+// plan whose predicates changed re-prepares when it differs from R.spec.
+int radix_spec_of(const Plan &P, const RadixPlan &R, u64 nullable_mask);
 size_t radix_p2_smem(const Plan &P, const RadixPlan &R);
 bool radix_p2_global_words(const Plan &P, const RadixPlan &R);
 u32 radix_tile_rows(const RadixPlan &R);

@@ -180,6 +180,39 @@ def test_radix_hot_table_full_key_range(vtype):
     assert err <= REL_TOL
 
 
+@pytest.mark.parametrize("vtype", [DOUBLE, BIGINT])
+def test_radix_predicate_on_the_value_column(vtype):
+    """The specialised partition pass with one compare on the value column
+    (the served Zipf shape), and a radix handle whose predicates are
+    replaced after reset: none, on the value column, on another column
+    (the generic pass) and back, each against the oracle."""
+    import torch
+    k, x = datagen.zipf(1_500_000, seed=8, n_values=300_000)
+    if vtype == BIGINT:
+        x = np.random.default_rng(8).integers(-10**6, 10**6, len(k), dtype=np.int64)
+    f = np.random.default_rng(9).integers(0, 1000, len(k)).astype(np.int32)
+    thr = 95.0 if vtype == DOUBLE else 0
+    aggs = [("count_star", -1), ("sum", 1), ("avg", 1)]
+    types = [BIGINT, vtype, INTEGER]
+    for op in ("<", ">=", "!="):
+        err, _, _ = check(types, [0], aggs, [k, x, f], est_groups=300_000, mode=RADIX, filters=[(1, op, thr)],
+                          device=True)
+        assert err <= REL_TOL
+    dk, dx, df = (torch.from_numpy(a).cuda() for a in (k, x, f))
+    g = capi.GroupBy(types, [0], aggs, est_groups=300_000, options={"mode": RADIX})
+    try:
+        for filters in ([], [(1, "<", thr)], [(2, "<", 300)], [(1, ">", thr)], []):
+            g.reset()
+            g.set_filters(filters)
+            g.ingest([dk, dx, df], nrows=len(k), device=True)
+            g.finalize()
+            gpu = gpu_to_dict(g.result(), 1, [BIGINT, BIGINT, vtype if vtype == DOUBLE else BIGINT, DOUBLE])
+            orc = oracle.run_query(types, [0], aggs, [k, x, f], filters=filters)
+            assert compare(gpu, orc, rel_tol=REL_TOL) <= REL_TOL
+    finally:
+        g.close()
+
+
 @pytest.mark.parametrize("n_keys", [1, 700])
 def test_radix_specialised_pass_all_keys_hot(n_keys):
     """The specialised partition pass (one BIGINT key, one DOUBLE SUM) when
