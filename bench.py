@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--rate", type=float, default=200.0, help="serve: arrivals per second")
     ap.add_argument("--scale", type=float, default=1.0, help="serve: resident table scale (1.0 = ~66 GB)")
     ap.add_argument("--budget-gb", type=float, default=40.0, help="serve: admission budget")
+    ap.add_argument("--lanes", type=int, default=2, help="serve: execution lanes of the batched server")
     ap.add_argument("--capacity-queries", type=int, default=3000,
                     help="serve: queries of the stream submitted at once to measure each mode's capacity")
     return ap.parse_args()
@@ -849,7 +850,8 @@ def run_serve(args):
     results = {}
     sample = list(range(0, len(queries), max(1, len(queries) // 24)))
     for mode, name in [(0, "batched"), (1, "one_at_a_time")]:
-        srv = capi.Server(budget_bytes=int(args.budget_gb * (1 << 30)), max_batch=256, mode=mode)
+        srv = capi.Server(budget_bytes=int(args.budget_gb * (1 << 30)), max_batch=256, mode=mode,
+                          lanes=args.lanes if mode == 0 else 1)
         for types, cols, n in tabs:
             srv.add_table(types, cols, n)
         # warm-up: a few queries of every shape
@@ -956,7 +958,7 @@ def run_serve(args):
             "vs_baseline": None, "dtype": "int64+f64", "data": "synthetic",
             "config": {"workload": "serve-10-tables", "resident_GB": res_bytes / 1e9, "scale": args.scale,
                        "queries": len(queries), "rate_qps": args.rate, "duration_s": args.duration,
-                       "budget_GB": args.budget_gb, "scanned_GB": scanned / 1e9,
+                       "budget_GB": args.budget_gb, "scanned_GB": scanned / 1e9, "lanes": args.lanes,
                        "shapes": "1M plain / 100M zipf / 200M filtered / 1e4-1e7 composite|varchar",
                        "datagen_s": round(gen_s, 1)},
             "p50_ms": b["p50_ms"], "p95_ms": b["p95_ms"], "p99_ms": b["p99_ms"],

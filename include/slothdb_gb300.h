@@ -358,6 +358,12 @@ typedef struct gb_server_stat {
     uint64_t result_bytes; /* device→host bytes of the results copied so far */
 } gb_server_stat;
 gb_status gb_server_create(uint64_t budget_bytes, uint32_t max_batch, int32_t mode, gb_server **out);
+/* Execution lanes (1..8, before the first submit; continuous batching
+ * defaults to 2, one-at-a-time mode runs 1): each lane is a thread with its
+ * own stream that admits work from the shared queue, so the lanes' kernels,
+ * result copies and host round trips overlap on the device.  The budget
+ * bounds the estimated bytes of every lane's work together. */
+gb_status gb_server_set_lanes(gb_server *s, uint32_t lanes);
 gb_status gb_server_add_table(gb_server *s, const int32_t *col_types, uint32_t n_cols, const gb_col *cols,
                               uint64_t nrows, uint32_t *table_id);
 gb_status gb_server_submit(gb_server *s, uint32_t table_id, uint64_t row_begin, uint64_t row_end,

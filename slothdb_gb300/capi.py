@@ -148,6 +148,7 @@ _SIGS = {
     "gb_server_query_times": (C.c_int, [C.c_void_p, C.c_uint64, C.POINTER(C.c_double), C.POINTER(C.c_double),
                                         C.POINTER(C.c_uint32)]),
     "gb_server_release": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "gb_server_set_lanes": (C.c_int, [C.c_void_p, C.c_uint32]),
     "gb_server_stats": (C.c_int, [C.c_void_p, C.POINTER(ServerStat)]),
     "gb_server_destroy": (None, [C.c_void_p]),
     "gb_hash_aggregate_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p,
@@ -495,13 +496,15 @@ class Server:
     """A served query stream over HBM-resident tables (gb_server).  mode 0 =
     continuous batching, 1 = one query at a time."""
 
-    def __init__(self, budget_bytes, max_batch=256, mode=0):
+    def __init__(self, budget_bytes, max_batch=256, mode=0, lanes=None):
         self.lib = load()
         h = C.c_void_p()
         check(self.lib.gb_server_create(int(budget_bytes), int(max_batch), int(mode), C.byref(h)))
         self.h = h
         self._keep = []
         self.tables = []
+        if lanes is not None:
+            check(self.lib.gb_server_set_lanes(self.h, int(lanes)))
 
     def add_table(self, col_types, cols, nrows, validity=None):
         """cols: torch CUDA tensors / device pointers (VARCHAR: (offsets, bytes))."""

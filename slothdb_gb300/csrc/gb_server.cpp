@@ -179,6 +179,16 @@ struct Query {
 };
 
 
+// One execution lane: its own stream, batch object and pool of lone
+// handles; lanes run on their own threads, so a lane's host work (result
+// copies, reservations, syncs) overlaps another lane's kernels.
+struct Lane {
+    cudaStream_t stream = nullptr;
+    gb_batch *batch = nullptr;                              // reused: gb_batch_clear keeps its handles pooled
+    std::unordered_multimap<std::string, gb_agg *> alone;   // idle handles of queries run alone, by plan shape
+    std::deque<std::string> alone_order;
+};
+
 }  // namespace
 
 struct gb_server {
@@ -191,15 +201,16 @@ struct gb_server {
     u64 next_ticket = 1;
     std::mutex mu;
     std::condition_variable cv_work, cv_done;
-    std::thread worker;
+    std::vector<std::thread> workers;
     bool stopping = false;
     bool started = false;
-    cudaStream_t stream = nullptr;
     int device = 0;
-    PinnedPool pinned;                                      // host result blocks
-    gb_batch *batch = nullptr;                              // reused: gb_batch_clear keeps its handles pooled
-    std::unordered_multimap<std::string, gb_agg *> alone;   // idle handles of queries run alone, by plan shape
-    std::deque<std::string> alone_order;
+    uint32_t n_lanes = 1;
+    std::vector<Lane> lanes;
+    PinnedPool pinned;  // host result blocks
+    u64 inflight_bytes = 0;  // estimated bytes of the queries the lanes are running
+    int active = 0;          // lanes running work (busy time is the union)
+    u64 busy_since = 0;
     // statistics
     u64 n_batches = 0, n_done = 0, n_rejected = 0, n_failed = 0, peak_admitted = 0, busy_ns = 0;
     // written by the dispatcher outside the lock, read by gb_server_stats
@@ -327,15 +338,15 @@ constexpr size_t ALONE_POOL_MAX = 8;  // idle lone handles kept (a radix handle 
 // One query on its own handle (the radix path for high-cardinality keys,
 // and every query in one-at-a-time mode).  Handles are pooled by plan shape
 // and reused with new predicates (gb_agg_reset + gb_agg_set_filters).
-void run_alone(gb_server *s, Query *q) {
+void run_alone(gb_server *s, Lane &L, Query *q) {
     const gb_agg_spec sp = q->spec();
     gb_agg *h = nullptr;
     gb_status st = GB_OK;
     const std::string key = alone_key(q);
-    auto it = s->alone.find(key);
-    if (it != s->alone.end()) {
+    auto it = L.alone.find(key);
+    if (it != L.alone.end()) {
         h = it->second;
-        s->alone.erase(it);
+        L.alone.erase(it);
         st = gb_agg_reset(h);
         if (st == GB_OK) st = gb_agg_set_filters(h, sp.filters, sp.n_filters);
     } else {
@@ -343,11 +354,11 @@ void run_alone(gb_server *s, Query *q) {
     }
     if (st == GB_OK) {
         std::vector<gb_col> cols = slice_cols(s->tables[q->table], q->r0);
-        st = gb_agg_ingest(h, cols.data(), q->r1 - q->r0, GB_MEM_DEVICE, s->stream);
-        if (st == GB_OK) st = gb_agg_finalize(h, s->stream);
+        st = gb_agg_ingest(h, cols.data(), q->r1 - q->r0, GB_MEM_DEVICE, L.stream);
+        if (st == GB_OK) st = gb_agg_finalize(h, L.stream);
         gb_result r{};
         if (st == GB_OK) st = gb_agg_result_device(h, &r);
-        if (st == GB_OK) st = copy_result_device(r, q->res, s->pinned, s->stream);
+        if (st == GB_OK) st = copy_result_device(r, q->res, s->pinned, L.stream);
         if (st == GB_OK) s->result_bytes += q->res.bytes;
         s->launches += gb_agg_kernel_launches(h);
     }
@@ -357,31 +368,31 @@ void run_alone(gb_server *s, Query *q) {
         gb_agg_destroy(h);
         return;
     }
-    s->alone.emplace(key, h);
-    s->alone_order.push_back(key);
-    while (s->alone.size() > ALONE_POOL_MAX && !s->alone_order.empty()) {
-        auto e = s->alone.find(s->alone_order.front());
-        s->alone_order.pop_front();
-        if (e != s->alone.end()) {
+    L.alone.emplace(key, h);
+    L.alone_order.push_back(key);
+    while (L.alone.size() > ALONE_POOL_MAX && !L.alone_order.empty()) {
+        auto e = L.alone.find(L.alone_order.front());
+        L.alone_order.pop_front();
+        if (e != L.alone.end()) {
             gb_agg_destroy(e->second);
-            s->alone.erase(e);
+            L.alone.erase(e);
         }
     }
 }
 
-void run_batch(gb_server *s, std::vector<Query *> &qs) {
+void run_batch(gb_server *s, Lane &L, std::vector<Query *> &qs) {
     gb_status st = GB_OK;
-    if (!s->batch) {
-        st = gb_batch_create(&s->batch);
-        if (st == GB_OK) gb_batch_set_option(s->batch, "graph", 0);  // one-off batches: capture costs more
+    if (!L.batch) {
+        st = gb_batch_create(&L.batch);
+        if (st == GB_OK) gb_batch_set_option(L.batch, "graph", 0);  // one-off batches: capture costs more
     } else {
-        st = gb_batch_clear(s->batch);
+        st = gb_batch_clear(L.batch);
     }
     if (st) {
         for (Query *q : qs) finish(q, st, gb_last_error());
         return;
     }
-    gb_batch *b = s->batch;
+    gb_batch *b = L.batch;
     std::vector<Query *> in;
     for (Query *q : qs) {
         const gb_agg_spec sp = q->spec();
@@ -393,11 +404,11 @@ void run_batch(gb_server *s, std::vector<Query *> &qs) {
     }
     if (!in.empty()) {
         const u64 l0 = gb_batch_kernel_launches(b);
-        st = gb_batch_run(b, s->stream);
+        st = gb_batch_run(b, L.stream);
         for (size_t i = 0; i < in.size(); i++) {
             gb_result r{};
             gb_status rs = st ? st : gb_batch_result_device(b, (uint32_t)i, &r);
-            if (rs == GB_OK) rs = copy_result_device(r, in[i]->res, s->pinned, s->stream);
+            if (rs == GB_OK) rs = copy_result_device(r, in[i]->res, s->pinned, L.stream);
             if (rs == GB_OK) s->result_bytes += in[i]->res.bytes;
             finish(in[i], rs, rs ? gb_last_error() : nullptr);
         }
@@ -405,34 +416,53 @@ void run_batch(gb_server *s, std::vector<Query *> &qs) {
     }
 }
 
-void dispatcher(gb_server *s) {
+// A query that takes the lone-handle path (radix-sized estimate,
+// COUNT(DISTINCT), a VARCHAR in a pair key, or one-at-a-time mode).
+bool runs_alone(const gb_server *s, const Query *q) {
+    return s->mode == 1 || q->est_groups >= RADIX_GROUPS || q->distinct();
+}
+
+// One lane's loop: admit queries from the front of the queue (FIFO) while
+// their estimated bytes fit the budget beside what the other lanes run — at
+// most max_batch small queries (one batch) and at most one lone query per
+// turn, so lanes share the large queries — then run them.
+void dispatcher(gb_server *s, int lane) {
     cudaSetDevice(s->device);
+    Lane &L = s->lanes[lane];
     for (;;) {
-        std::vector<Query *> take;
+        std::vector<Query *> big, small;
+        u64 sum = 0;
         {
             std::unique_lock<std::mutex> lk(s->mu);
-            s->cv_work.wait(lk, [&] { return s->stopping || !s->queue.empty(); });
-            if (s->queue.empty()) break;  // stopping and drained
-            u64 sum = 0;
-            while (!s->queue.empty() && take.size() < s->max_batch) {
-                Query *q = s->queue.front();
-                if (q->est_bytes > s->budget) {
+            for (;;) {
+                // reject what can never fit, then admit what fits now
+                while (!s->queue.empty() && s->queue.front()->est_bytes > s->budget) {
+                    Query *q = s->queue.front();
                     s->queue.pop_front();
                     finish(q, GB_ERR_BUDGET, "estimated device bytes exceed the admission budget");
                     q->t_start = q->t_done = now_ns();
                     q->done = true;
                     s->n_rejected++;
-                    continue;
                 }
-                if (sum + q->est_bytes > s->budget) break;
-                s->queue.pop_front();
-                take.push_back(q);
-                sum += q->est_bytes;
+                while (!s->queue.empty() && small.size() < s->max_batch) {
+                    Query *q = s->queue.front();
+                    if (q->est_bytes > s->budget) break;  // rejected on the next pass
+                    if (s->inflight_bytes + sum + q->est_bytes > s->budget) break;
+                    const bool alone = runs_alone(s, q);
+                    if (alone && !big.empty()) break;
+                    s->queue.pop_front();
+                    (alone ? big : small).push_back(q);
+                    sum += q->est_bytes;
+                }
+                s->cv_done.notify_all();
+                if (!big.empty() || !small.empty()) break;
+                if (s->stopping && s->queue.empty()) return;  // stopping and drained
+                s->cv_work.wait(lk);
             }
-            s->peak_admitted = std::max(s->peak_admitted, sum);
-            s->cv_done.notify_all();
+            s->inflight_bytes += sum;
+            s->peak_admitted = std::max(s->peak_admitted, s->inflight_bytes);
+            if (s->active++ == 0) s->busy_since = now_ns();
         }
-        if (take.empty()) continue;
         const u64 t0 = now_ns();
         // a query's start / done times: its batch's, or its own when it runs alone
         auto complete = [&](std::vector<Query *> &qs, u64 ts, u64 td) {
@@ -445,12 +475,9 @@ void dispatcher(gb_server *s) {
                 s->n_done++;
             }
         };
-        std::vector<Query *> big, small;
-        for (Query *q : take)
-            (s->mode == 1 || q->est_groups >= RADIX_GROUPS || q->distinct() ? big : small).push_back(q);
         if (!small.empty()) {
             for (Query *q : small) q->batch_size = (uint32_t)small.size();
-            run_batch(s, small);
+            run_batch(s, L, small);
             complete(small, t0, now_ns());
             s->cv_done.notify_all();
         }
@@ -458,16 +485,17 @@ void dispatcher(gb_server *s) {
             std::vector<Query *> one{q};
             q->batch_size = 1;
             const u64 ts = now_ns();
-            run_alone(s, q);
+            run_alone(s, L, q);
             complete(one, ts, now_ns());
             s->cv_done.notify_all();
         }
-        const u64 t1 = now_ns();
         {
             std::lock_guard<std::mutex> lk(s->mu);
             s->n_batches++;
-            s->busy_ns += t1 - t0;
+            s->inflight_bytes -= sum;
+            if (--s->active == 0) s->busy_ns += now_ns() - s->busy_since;
         }
+        s->cv_work.notify_all();  // budget freed: another lane may admit
     }
 }
 
@@ -484,13 +512,27 @@ gb_status gb_server_create(uint64_t budget_bytes, uint32_t max_batch, int32_t mo
     s->budget = budget_bytes;
     s->max_batch = max_batch;
     s->mode = mode;
+    s->n_lanes = mode == 0 ? 2 : 1;
     cudaGetDevice(&s->device);
-    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
-        delete s;
-        set_error("cudaStreamCreate failed");
-        return GB_ERR_CUDA;
-    }
     *out = s;
+    return GB_OK;
+}
+
+gb_status gb_server_set_lanes(gb_server *s, uint32_t lanes) {
+    if (!s || lanes == 0 || lanes > 8) {
+        set_error("lanes must be 1..8");
+        return GB_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->started) {
+        set_error("lanes are set before the first query");
+        return GB_ERR_STATE;
+    }
+    if (s->mode == 1 && lanes != 1) {
+        set_error("one-at-a-time mode runs one lane");
+        return GB_ERR_INVALID;
+    }
+    s->n_lanes = lanes;
     return GB_OK;
 }
 
@@ -564,8 +606,16 @@ gb_status gb_server_submit(gb_server *s, uint32_t table_id, uint64_t row_begin, 
     s->queue.push_back(q.get());
     s->all[q->ticket] = std::move(q);
     if (!s->started) {
+        s->lanes.resize(s->n_lanes);
+        for (Lane &L : s->lanes)
+            if (cudaStreamCreateWithFlags(&L.stream, cudaStreamNonBlocking) != cudaSuccess) {
+                s->all.erase(*ticket);
+                s->queue.pop_back();
+                set_error("cudaStreamCreate failed");
+                return GB_ERR_CUDA;
+            }
         s->started = true;
-        s->worker = std::thread(dispatcher, s);
+        for (uint32_t i = 0; i < s->n_lanes; i++) s->workers.emplace_back(dispatcher, s, (int)i);
     }
     s->cv_work.notify_one();
     return GB_OK;
@@ -652,11 +702,14 @@ void gb_server_destroy(gb_server *s) {
         s->stopping = true;
     }
     s->cv_work.notify_all();
-    if (s->worker.joinable()) s->worker.join();
-    if (s->batch) gb_batch_destroy(s->batch);
-    for (auto &e : s->alone) gb_agg_destroy(e.second);
+    for (std::thread &t : s->workers)
+        if (t.joinable()) t.join();
+    for (Lane &L : s->lanes) {
+        if (L.batch) gb_batch_destroy(L.batch);
+        for (auto &e : L.alone) gb_agg_destroy(e.second);
+        if (L.stream) cudaStreamDestroy(L.stream);
+    }
     for (auto &e : s->all) release_result(e.second->res, s->pinned);
-    if (s->stream) cudaStreamDestroy(s->stream);
     delete s;
 }
 

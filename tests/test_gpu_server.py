@@ -70,7 +70,10 @@ def _queries(rng, n, tabs):
             q = COMP if t == 0 else STR
             group_cols, aggs = q["group_cols"], q["aggs"]
             filters = [(2 if t == 0 else 1, "<", int(sel * 10**6))]
-        qs.append(dict(table=t, r0=r0, r1=r1, group_cols=group_cols, aggs=aggs, filters=filters))
+        # every fifth query estimates radix-sized group counts: it runs alone,
+        # on the partitioned path, beside the other lanes' batches
+        est = (1 << 20) if i % 5 == 4 and t != 1 else 0
+        qs.append(dict(table=t, r0=r0, r1=r1, group_cols=group_cols, aggs=aggs, filters=filters, est=est))
     return qs
 
 
@@ -92,11 +95,14 @@ def _alone(types, dcols, q):
         g.close()
 
 
-@pytest.mark.parametrize("mode", [0, 1])
-def test_mixed_results_equal_alone(tables, mode):
+@pytest.mark.parametrize("mode,lanes", [(0, None), (0, 1), (0, 3), (1, None)])
+def test_mixed_results_equal_alone(tables, mode, lanes):
+    """Every result equals the query run alone (and the oracle's on a
+    sample), with one, two (the default) or three execution lanes, and in
+    one-at-a-time mode."""
     rng = np.random.default_rng(70 + mode)
     dtabs = [_dev(cols, types) for types, cols in tables]
-    srv = capi.Server(budget_bytes=8 << 30, max_batch=64, mode=mode)
+    srv = capi.Server(budget_bytes=8 << 30, max_batch=64, mode=mode, lanes=lanes)
     try:
         for (types, cols), d in zip(tables, dtabs):
             n = len(cols[1]) if types[0] == capi.VARCHAR else len(cols[0])
@@ -108,7 +114,7 @@ def test_mixed_results_equal_alone(tables, mode):
             for i in range(lo, hi):
                 q = qs[i]
                 tickets[i] = srv.submit(q["table"], q["r0"], q["r1"], q["group_cols"], q["aggs"],
-                                        filters=q["filters"])
+                                        filters=q["filters"], est_groups=q["est"])
 
         th = [threading.Thread(target=submit, args=(i * 10, i * 10 + 10)) for i in range(4)]
         for t in th:
@@ -201,5 +207,27 @@ def test_submit_errors(tables):
         assert srv.wait(t)
         with pytest.raises(capi.GbError):
             srv.add_table(types, d, n)                  # tables are registered before the first query
+    finally:
+        srv.close()
+
+
+def test_lane_settings(tables):
+    """Lanes are 1..8, set before the first submit; one-at-a-time mode runs
+    one lane."""
+    with pytest.raises(capi.GbError):
+        capi.Server(budget_bytes=1 << 30, lanes=0)
+    with pytest.raises(capi.GbError):
+        capi.Server(budget_bytes=1 << 30, lanes=9)
+    with pytest.raises(capi.GbError):
+        capi.Server(budget_bytes=1 << 30, mode=1, lanes=2)
+    types, cols = tables[2]
+    srv = capi.Server(budget_bytes=1 << 30, lanes=4)
+    try:
+        srv.add_table(types, _dev(cols, types), len(cols[0]))
+        t = srv.submit(0, 0, 1000, [0], [("count_star", -1)])
+        assert srv.wait(t)
+        srv.release(t)
+        with pytest.raises(capi.GbError):
+            capi.check(srv.lib.gb_server_set_lanes(srv.h, 2))  # after the first submit
     finally:
         srv.close()
