@@ -15,11 +15,6 @@
 namespace slothdb_gb300 {
 namespace engine {
 
-void ValidityMask::SetInvalid(idx_t i, idx_t capacity) {
-    if (words_.empty()) words_.assign((capacity + 63) / 64, ~0ull);
-    words_[i >> 6] &= ~(1ull << (i & 63));
-}
-
 static int type_width(LogicalTypeId t) {
     switch (t) {
     case LogicalTypeId::SMALLINT: return 2;
@@ -27,6 +22,12 @@ static int type_width(LogicalTypeId t) {
     case LogicalTypeId::VARCHAR: return 0;
     default: return 8;
     }
+}
+
+#ifndef SLOTHDB_GB300_ENGINE_HEADERS
+void ValidityMask::SetInvalid(idx_t i, idx_t capacity) {
+    if (words_.empty()) words_.assign((capacity + 63) / 64, ~0ull);
+    words_[i >> 6] &= ~(1ull << (i & 63));
 }
 
 Vector::Vector(LogicalType type, idx_t capacity) : type_(type), capacity_(capacity) {
@@ -44,6 +45,7 @@ void DataChunk::Reset() {
     for (auto &v : data) v.GetValidity().Reset();
     count_ = 0;
 }
+#endif
 
 }  // namespace engine
 
@@ -85,10 +87,10 @@ PhysicalGpuHashAggregate::PhysicalGpuHashAggregate(std::vector<idx_t> groups, st
                                                    std::vector<LogicalType> result_types,
                                                    std::vector<LogicalType> input_types,
                                                    std::vector<GpuPredicate> filters, uint64_t est_groups)
-    : PhysicalOperator(std::move(result_types)), groups_(std::move(groups)), aggregates_(std::move(aggregates)),
+    : GB300_OPERATOR_BASE(std::move(result_types)), groups_(std::move(groups)), aggregates_(std::move(aggregates)),
       input_types_(std::move(input_types)), filters_(std::move(filters)) {
     std::vector<int32_t> ct, gc;
-    for (const auto &t : input_types_) ct.push_back(to_gb(t.id));
+    for (const auto &t : input_types_) ct.push_back(to_gb(type_id(t)));
     for (idx_t g : groups_) gc.push_back((int32_t)g);
     std::vector<gb_agg_desc> ad;
     for (const auto &a : aggregates_) ad.push_back({a.kind, a.column});
@@ -133,7 +135,7 @@ void PhysicalGpuHashAggregate::Flush() {
     for (size_t c = 0; c < nc; c++) {
         cols[c].data = S.cols[c];
         cols[c].validity = S.has_null[c] ? S.valid[c] : nullptr;
-        cols[c].offsets = input_types_[c].id == LogicalTypeId::VARCHAR ? S.offs[c] : nullptr;
+        cols[c].offsets = type_id(input_types_[c]) == LogicalTypeId::VARCHAR ? S.offs[c] : nullptr;
     }
     check(gb_agg_ingest(h_, cols.data(), S.rows, GB_MEM_HOST, nullptr), "gb_agg_ingest");
     S.rows = 0;
@@ -157,8 +159,8 @@ void PhysicalGpuHashAggregate::ComputeAggregates() {
         S.has_null.assign(nc, false);
         S.str_used.assign(nc, 0);
         for (size_t c = 0; c < nc; c++) {
-            const bool str = input_types_[c].id == LogicalTypeId::VARCHAR;
-            size_t bytes = str ? (size_t)STAGE_ROWS * 16 : (size_t)STAGE_ROWS * type_width(input_types_[c].id);
+            const bool str = type_id(input_types_[c]) == LogicalTypeId::VARCHAR;
+            size_t bytes = str ? (size_t)STAGE_ROWS * 16 : (size_t)STAGE_ROWS * type_width(type_id(input_types_[c]));
             check(gb_host_alloc(&S.cols[c], bytes), "gb_host_alloc");
             S.col_cap[c] = bytes;
             if (str) {
@@ -185,10 +187,12 @@ void PhysicalGpuHashAggregate::ComputeAggregates() {
                 const idx_t take = std::min<idx_t>(n - r0, STAGE_ROWS - S.rows);
                 for (size_t c = 0; c < nc; c++) {
                     const Vector &v = chunk.GetVector(c);
-                    if (input_types_[c].id == LogicalTypeId::VARCHAR) {
+                    if (type_id(input_types_[c]) == LogicalTypeId::VARCHAR) {
                         for (idx_t i = 0; i < take; i++) {
-                            const std::string &str = v.Strings()[r0 + i];
-                            size_t need = (size_t)S.str_used[c] + str.size();
+                            const char *sp = nullptr;
+                            size_t sn = 0;
+                            string_at(v, r0 + i, &sp, &sn);
+                            size_t need = (size_t)S.str_used[c] + sn;
                             if (need > S.col_cap[c]) {  // grow the pinned byte buffer
                                 void *p = nullptr;
                                 check(gb_host_alloc(&p, need * 2), "gb_host_alloc");
@@ -197,12 +201,12 @@ void PhysicalGpuHashAggregate::ComputeAggregates() {
                                 S.cols[c] = p;
                                 S.col_cap[c] = need * 2;
                             }
-                            memcpy((char *)S.cols[c] + S.str_used[c], str.data(), str.size());
-                            S.str_used[c] += (int64_t)str.size();
+                            if (sn) memcpy((char *)S.cols[c] + S.str_used[c], sp, sn);
+                            S.str_used[c] += (int64_t)sn;
                             S.offs[c][S.rows + i + 1] = S.str_used[c];
                         }
                     } else {
-                        const int w = type_width(input_types_[c].id);
+                        const int w = type_width(type_id(input_types_[c]));
                         memcpy((char *)S.cols[c] + S.rows * w, v.GetData<char>() + r0 * w, take * w);
                     }
                     if (!v.GetValidity().AllValid()) {
@@ -227,7 +231,7 @@ void PhysicalGpuHashAggregate::ComputeAggregates() {
     const auto &rt = GetTypes();
     if (rt.size() != res_.n_cols) throw GpuAggregateError(GB_ERR_INVALID, "result_types width differs from the plan's");
     for (uint32_t c = 0; c < res_.n_cols; c++)
-        if (to_gb(rt[c].id) != res_.types[c])
+        if (to_gb(type_id(rt[c])) != res_.types[c])
             throw GpuAggregateError(GB_ERR_INVALID, "result type of output slot " + std::to_string(c) +
                                                         " differs from the plan's");
 }
@@ -248,7 +252,7 @@ bool PhysicalGpuHashAggregate::GetData(DataChunk &result) {
             const int64_t *o = res_.offsets[c];
             const char *b = (const char *)res_.data[c];
             for (idx_t i = 0; i < count; i++)
-                v.Strings()[i].assign(b + o[emit_pos_ + i], (size_t)(o[emit_pos_ + i + 1] - o[emit_pos_ + i]));
+                set_string(v, i, b + o[emit_pos_ + i], (size_t)(o[emit_pos_ + i + 1] - o[emit_pos_ + i]));
         } else {
             const int w = t == GB_T_SMALLINT ? 2 : (t == GB_T_INTEGER ? 4 : 8);
             memcpy(v.GetData<char>(), (const char *)res_.data[c] + emit_pos_ * w, count * w);
@@ -257,7 +261,7 @@ bool PhysicalGpuHashAggregate::GetData(DataChunk &result) {
         if (vw)
             for (idx_t i = 0; i < count; i++) {
                 const idx_t r = emit_pos_ + i;
-                if (!((vw[r >> 6] >> (r & 63)) & 1ull)) v.GetValidity().SetInvalid(i, VECTOR_SIZE);
+                if (!((vw[r >> 6] >> (r & 63)) & 1ull)) set_invalid(v.GetValidity(), i, VECTOR_SIZE);
             }
     }
     emit_pos_ += count;

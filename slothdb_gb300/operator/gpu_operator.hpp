@@ -16,8 +16,12 @@
 //   ValidityMask            vector.hpp:65-120, validity_mask.hpp:9-69
 //
 // The engine types below are minimal stand-ins with the reference's names so
-// that this operator and its tests compile on their own; inside SlothDB the
-// operator uses the engine's own types in their place.
+// that this operator and its tests compile on their own.  Built with
+// SLOTHDB_GB300_ENGINE_HEADERS defined and the engine's include directory on
+// the path, the operator uses the engine's own types instead
+// (include/slothdb/common/types/data_chunk.hpp, vector.hpp, validity_mask.hpp,
+// string_type.hpp, include/slothdb/execution/physical_operator.hpp); the few
+// places where the two differ go through the adapters below.
 // Group keys and aggregate arguments are input column indices — the planner
 // places a projection below the operator for expressions.  Failures throw
 // GpuAggregateError (SlothDB converts it to InternalException); there is no
@@ -32,6 +36,41 @@
 
 #include "../../include/slothdb_gb300.h"
 
+#ifdef SLOTHDB_GB300_ENGINE_HEADERS
+#include "slothdb/common/types/data_chunk.hpp"
+#include "slothdb/execution/physical_operator.hpp"
+
+namespace slothdb_gb300 {
+namespace engine {
+
+using slothdb::DataChunk;
+using slothdb::idx_t;
+using slothdb::LogicalType;
+using slothdb::LogicalTypeId;
+using slothdb::PhysicalOperator;
+using slothdb::ValidityMask;
+using slothdb::Vector;
+using slothdb::VECTOR_SIZE;
+
+inline LogicalTypeId type_id(const LogicalType &t) { return t.id(); }
+// VARCHAR values are string_t views; written strings live in the vector's
+// string buffer
+inline void string_at(const Vector &v, idx_t i, const char **p, size_t *n) {
+    const slothdb::string_t &s = v.GetData<slothdb::string_t>()[i];
+    *p = s.GetData();
+    *n = s.GetSize();
+}
+inline void set_string(Vector &v, idx_t i, const char *p, size_t n) {
+    const char *q = v.GetStringBuffer().AddString(p, (idx_t)n);
+    v.GetData<slothdb::string_t>()[i] = slothdb::string_t(q, (uint32_t)n);
+}
+inline void set_invalid(ValidityMask &m, idx_t i, idx_t) { m.SetInvalid(i); }
+
+}  // namespace engine
+// PhysicalHashAggregate passes TABLE_SCAN (physical_planner.cpp:6014): the
+// engine's PhysicalOperatorType has no aggregate member
+#define GB300_OPERATOR_BASE(types) engine::PhysicalOperator(slothdb::PhysicalOperatorType::TABLE_SCAN, types)
+#else
 namespace slothdb_gb300 {
 namespace engine {
 
@@ -112,6 +151,19 @@ private:
 };
 
 }  // namespace engine
+
+namespace engine {
+inline LogicalTypeId type_id(const LogicalType &t) { return t.id; }
+inline void string_at(const Vector &v, idx_t i, const char **p, size_t *n) {
+    const std::string &s = v.Strings()[i];
+    *p = s.data();
+    *n = s.size();
+}
+inline void set_string(Vector &v, idx_t i, const char *p, size_t n) { v.Strings()[i].assign(p, n); }
+inline void set_invalid(ValidityMask &m, idx_t i, idx_t capacity) { m.SetInvalid(i, capacity); }
+}  // namespace engine
+#define GB300_OPERATOR_BASE(types) engine::PhysicalOperator(types)
+#endif
 
 class GpuAggregateError : public std::runtime_error {
 public:
