@@ -225,6 +225,10 @@ __device__ __forceinline__ long long strdict_warp_encode(const StrDictRef &D, co
         for (int p = 0; p < D.max_probe; p++) {
             u64 *hk = D.hash + slot;
             u64 k = *(volatile u64 *)hk;
+            // the slot's ref is loaded beside its key (the acquire orders the
+            // arena and id loads after it), so a hit costs two round trips:
+            // key + ref, then arena bytes + id
+            u64 r = ld_acquire(D.ref + slot);
             if (k == EMPTY_KEY) {
                 const u64 old = atomicCAS((unsigned long long *)hk, EMPTY_KEY, hv);
                 if (old == EMPTY_KEY) {
@@ -232,16 +236,17 @@ __device__ __forceinline__ long long strdict_warp_encode(const StrDictRef &D, co
                     break;
                 }
                 k = old;
+                r = ld_acquire(D.ref + slot);  // claimed by another thread meanwhile
             }
             if (k == hv) {
-                const u64 r = ld_acquire(D.ref + slot);
                 if (r == REF_PENDING) {
                     waitslot = (long long)slot;
                     waitp = p;
                     break;
                 }
+                const long long sid = (long long)D.id[slot];  // written before the ref was published
                 if (shrt ? short_arena_equal(D, r, c, len) : arena_equal(D, r, s, len)) {
-                    id = (long long)D.id[slot];
+                    id = sid;
                     break;
                 }
             }
