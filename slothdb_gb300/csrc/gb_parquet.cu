@@ -25,6 +25,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "gb_agg_host.h"
@@ -691,10 +692,12 @@ __global__ void k_pq_runs(const uint8_t *file, const DPage *pages, const RunJob 
 // ------------------------------------------------- VARCHAR dictionary pages
 // A BYTE_ARRAY dictionary page holds its values PLAIN: a 4-byte little-endian
 // length, then the bytes, per value (ReadDictionaryPage / the VARCHAR branch
-// of DecodeDataPageTyped, parquet.cpp:2340-2471, 2229-2331).  A batch's
-// dictionary strings are compacted into one offsets + bytes array and
-// encoded once into the handle's string dictionary; the data pages' indices
-// then gather string ids instead of values.
+// of DecodeDataPageTyped, parquet.cpp:2340-2471, 2229-2331), and so does a
+// PLAIN BYTE_ARRAY data page (its defined values only; parquet.cpp:
+// 1742-1854).  A batch's dictionary strings and PLAIN-page strings are
+// compacted into one offsets + bytes array and encoded once into the
+// handle's string dictionary; a dictionary-encoded data page's indices then
+// gather string ids, and value j of a PLAIN page is its page's entry j.
 struct DDict {
     uint64_t off;           // payload offset in the device file
     uint64_t entry_base;    // index of the page's first value in the batch's entries
@@ -707,7 +710,11 @@ struct DDict {
 // address and compacted offset.  Every length is checked against the
 // payload, and the walk must end exactly at the payload's end; anything else
 // sets ERR_CORRUPT (and the host stops before using the entries).
-__global__ void k_pq_dict_walk(const uint8_t *file, const DDict *dicts, u64 *src, int64_t *offs, Ctl *ctl) {
+// counts != nullptr (a PLAIN page, whose value count the levels decide): d.n
+// only bounds the values, nothing is written but counts[page], and the walk
+// ends at the payload's end.
+__global__ void k_pq_dict_walk(const uint8_t *file, const DDict *dicts, u64 *src, int64_t *offs, Ctl *ctl,
+                               uint32_t *counts) {
     __shared__ uint8_t win[PQ_WIN];
     __shared__ u64 s_pos;
     __shared__ uint32_t s_i;
@@ -730,6 +737,7 @@ __global__ void k_pq_dict_walk(const uint8_t *file, const DDict *dicts, u64 *src
             uint32_t i = s_i;
             int state = 0;
             while (i < d.n) {
+                if (counts && pos == d.bytes) break;  // every value of the payload walked
                 if (pos + 4 > w0 + wn) {
                     if (pos + 4 > d.bytes) state = 2;  // no room for the length
                     break;
@@ -741,12 +749,14 @@ __global__ void k_pq_dict_walk(const uint8_t *file, const DDict *dicts, u64 *src
                     state = 2;  // the value runs past the payload
                     break;
                 }
-                src[d.entry_base + i] = d.off + pos + 4;
-                offs[d.entry_base + i] = (int64_t)(d.compact_base + pos - 4 * (u64)i);
+                if (!counts) {
+                    src[d.entry_base + i] = d.off + pos + 4;
+                    offs[d.entry_base + i] = (int64_t)(d.compact_base + pos - 4 * (u64)i);
+                }
                 pos += 4 + (u64)len;
                 i++;
             }
-            if (state == 0 && i == d.n) state = pos == d.bytes ? 1 : 2;
+            if (state == 0 && (i == d.n || (counts && pos == d.bytes))) state = pos == d.bytes ? 1 : 2;
             if (state == 0 && pos == w0) state = 2;  // no progress (cannot happen with a valid window)
             s_pos = pos;
             s_i = i;
@@ -755,6 +765,7 @@ __global__ void k_pq_dict_walk(const uint8_t *file, const DDict *dicts, u64 *src
         __syncthreads();
     }
     if (threadIdx.x == 0 && s_state != 1) atomicOr(&ctl->err, (u32)ERR_CORRUPT);
+    if (threadIdx.x == 0 && counts) counts[blockIdx.x] = s_i;
 }
 
 // Copy each dictionary value's bytes to its compacted offset (the walk has
@@ -858,7 +869,14 @@ __device__ __forceinline__ bool level_at(const uint8_t *file, const DPage &pg, c
 // string-predicate flag instead of its string id.
 __device__ __forceinline__ u64 decode_at(const uint8_t *file, const DPage &pg, const DRun *runs,
                                          const uint32_t *page_runs, uint32_t pidx, uint32_t i, bool match = false) {
-    if (pg.kind == 0) return load_plain(file + pg.off + (u64)i * pg.width, pg.width);
+    if (pg.kind == 0) {
+        if (pg.dict_ids) {  // a PLAIN BYTE_ARRAY page: value i is entry i of its walked strings
+            if (i >= pg.dict_n) return match ? 0ull : ~0ull;  // more defined rows than values: NULL id
+            if (match) return pg.dict_match ? (u64)__ldg((const uint8_t *)pg.dict_match + i) : 1ull;
+            return (u64)__ldg((const long long *)pg.dict_ids + i);
+        }
+        return load_plain(file + pg.off + (u64)i * pg.width, pg.width);
+    }
     const uint32_t nr = page_runs[PQ_PR * pidx], bw = page_runs[PQ_PR * pidx + 1];
     const DRun *rr = runs + pg.run_base;
     uint32_t lo = 0, hi = nr;  // last run with start <= i
@@ -1435,8 +1453,9 @@ struct PqScratch {
     size_t out_valid_cap[GB_MAX_COLS] = {};
     // VARCHAR dictionary pages of a batch: descriptors, value sources,
     // compacted offsets and bytes
-    void *dicts = nullptr, *dsrc = nullptr, *doffs = nullptr, *dbytes = nullptr, *dmatch = nullptr;
-    size_t dicts_cap = 0, dsrc_cap = 0, doffs_cap = 0, dbytes_cap = 0, dmatch_cap = 0;
+    void *dicts = nullptr, *dsrc = nullptr, *doffs = nullptr, *dbytes = nullptr, *dmatch = nullptr,
+         *dcounts = nullptr;  // value counts of PLAIN BYTE_ARRAY pages
+    size_t dicts_cap = 0, dsrc_cap = 0, doffs_cap = 0, dbytes_cap = 0, dmatch_cap = 0, dcounts_cap = 0;
     // compressed batches: the decompressed image, its jobs, the level lengths found inside
     void *img = nullptr, *ijobs = nullptr, *ilvl = nullptr;
     size_t img_cap = 0, ijobs_cap = 0, ilvl_cap = 0;
@@ -1479,7 +1498,7 @@ void gb_pq_release_scratch(gb_agg *h) {
         g_pq_scratch.erase(it);
     }
     for (void *p : {s->file_dev, s->pages, s->runs, s->page_runs, s->dict_pages, s->col_pages, s->chunks, s->ctl,
-                    s->dicts, s->dsrc, s->doffs, s->dbytes, s->dmatch, s->img, s->ijobs, s->ilvl})
+                    s->dicts, s->dsrc, s->doffs, s->dbytes, s->dmatch, s->dcounts, s->img, s->ijobs, s->ilvl})
         if (p) cudaFree(p);
     for (void *p : s->out)
         if (p) cudaFree(p);
@@ -1512,35 +1531,86 @@ __global__ void k_pq_dict_match(const uint8_t *bytes, const int64_t *offs, u64 n
     }
 }
 
+// The batch's VARCHAR-key strings: each live row group's dictionary page,
+// then its PLAIN data pages (plain_at[page] = {first entry, values} for
+// every PLAIN page, page = index into V.pages).
 static gb_status pq_varchar_dict(gb_agg *h, const PqView &V, PqScratch *S, const uint8_t *dfile, uint64_t base,
                                  uint32_t rg_begin, uint32_t rg_end, const std::vector<char> &live, int fcol,
                                  Ctl *dctl, cudaStream_t st, const int64_t **ids, const PqStrFilters &SF,
-                                 const uint8_t **match) {
-    std::vector<DDict> dd;
-    uint64_t D = 0, B = 0;
+                                 const uint8_t **match, std::unordered_map<uint32_t, std::pair<uint64_t, uint32_t>> &plain_at) {
+    gb_status s;
+    // PLAIN pages: their value counts first (a walk that only counts)
+    std::vector<uint32_t> plain_pages;
+    std::vector<DDict> pd;
     for (uint32_t g = rg_begin; g < rg_end; g++) {
         if (!live[g - rg_begin]) continue;
         const PqChunk &ch = (*V.chunks)[g][fcol];
-        if (ch.dict_off < 0) {
-            if (ch.page_begin != ch.page_end) return pq_corrupt("VARCHAR column chunk without a dictionary page");
-            continue;
+        for (uint32_t p = ch.page_begin; p < ch.page_end; p++) {
+            const PqPage &pg = (*V.pages)[p];
+            if (pg.kind != 0) continue;
+            DDict d{};
+            d.off = pg.off - base;
+            d.n = pg.bytes / 4;  // a bound: every value has a 4-byte length
+            d.bytes = pg.bytes;
+            pd.push_back(d);
+            plain_pages.push_back(p);
         }
-        if ((uint64_t)ch.dict_n * 4 > ch.dict_bytes) return pq_corrupt("dictionary size");
-        DDict d{};
-        d.off = (uint64_t)ch.dict_off - base;
-        d.entry_base = D;
-        d.compact_base = B;
-        d.n = ch.dict_n;
-        d.bytes = ch.dict_bytes;
-        D += d.n;
-        B += (uint64_t)d.bytes - 4 * (uint64_t)d.n;
-        dd.push_back(d);
+    }
+    std::vector<uint32_t> counts(pd.size(), 0);
+    if (!pd.empty()) {
+        if ((s = grow(S->dicts, S->dicts_cap, pd.size() * sizeof(DDict) + 16)) ||
+            (s = grow(S->dcounts, S->dcounts_cap, pd.size() * 4 + 16)))
+            return s;
+        GB_CUDA(cudaMemcpyAsync(S->dicts, pd.data(), pd.size() * sizeof(DDict), cudaMemcpyHostToDevice, st));
+        k_pq_dict_walk<<<(unsigned)pd.size(), 128, 0, st>>>(dfile, (const DDict *)S->dicts, nullptr, nullptr, dctl,
+                                                            (uint32_t *)S->dcounts);
+        GB_CUDA(cudaGetLastError());
+        gb_agg_count_launch(h, 1);
+        Ctl c;
+        GB_CUDA(cudaMemcpyAsync(counts.data(), S->dcounts, pd.size() * 4, cudaMemcpyDeviceToHost, st));
+        GB_CUDA(cudaMemcpyAsync(&c, dctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
+        GB_CUDA(cudaStreamSynchronize(st));
+        if ((s = pq_fail_if_err(c))) return s;
+        for (size_t i = 0; i < pd.size(); i++) {
+            const PqPage &pg = (*V.pages)[plain_pages[i]];
+            // a REQUIRED page holds one value per row; an OPTIONAL one at most
+            if (pg.def_bytes == 0 ? counts[i] != pg.n_values : counts[i] > pg.n_values)
+                return pq_corrupt("PLAIN BYTE_ARRAY value count");
+        }
+    }
+    std::vector<DDict> dd;
+    uint64_t D = 0, B = 0;
+    size_t pi = 0;
+    for (uint32_t g = rg_begin; g < rg_end; g++) {
+        if (!live[g - rg_begin]) continue;
+        const PqChunk &ch = (*V.chunks)[g][fcol];
+        if (ch.dict_off >= 0) {
+            if ((uint64_t)ch.dict_n * 4 > ch.dict_bytes) return pq_corrupt("dictionary size");
+            DDict d{};
+            d.off = (uint64_t)ch.dict_off - base;
+            d.entry_base = D;
+            d.compact_base = B;
+            d.n = ch.dict_n;
+            d.bytes = ch.dict_bytes;
+            D += d.n;
+            B += (uint64_t)d.bytes - 4 * (uint64_t)d.n;
+            dd.push_back(d);
+        }
+        for (; pi < plain_pages.size() && (*V.pages)[plain_pages[pi]].rg == g; pi++) {
+            DDict d = pd[pi];
+            d.entry_base = D;
+            d.compact_base = B;
+            d.n = counts[pi];
+            plain_at[plain_pages[pi]] = {D, counts[pi]};
+            D += d.n;
+            B += (uint64_t)d.bytes - 4 * (uint64_t)d.n;
+            dd.push_back(d);
+        }
     }
     if (D == 0) {
         set_error("VARCHAR column with an empty dictionary");
         return GB_ERR_UNSUPPORTED;
     }
-    gb_status s;
     if ((s = grow(S->dicts, S->dicts_cap, dd.size() * sizeof(DDict) + 16)) ||
         (s = grow(S->dsrc, S->dsrc_cap, D * 8 + 16)) || (s = grow(S->doffs, S->doffs_cap, (D + 1) * 8 + 16)) ||
         (s = grow(S->dbytes, S->dbytes_cap, B + 16)))
@@ -1549,7 +1619,7 @@ static gb_status pq_varchar_dict(gb_agg *h, const PqView &V, PqScratch *S, const
     GB_CUDA(cudaMemcpyAsync(S->dicts, dd.data(), dd.size() * sizeof(DDict), cudaMemcpyHostToDevice, st));
     GB_CUDA(cudaMemcpyAsync((int64_t *)S->doffs + D, &total, 8, cudaMemcpyHostToDevice, st));
     k_pq_dict_walk<<<(unsigned)dd.size(), 128, 0, st>>>(dfile, (const DDict *)S->dicts, (u64 *)S->dsrc,
-                                                        (int64_t *)S->doffs, dctl);
+                                                        (int64_t *)S->doffs, dctl, nullptr);
     GB_CUDA(cudaGetLastError());
     Ctl c;
     GB_CUDA(cudaMemcpyAsync(&c, dctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
@@ -1836,11 +1906,6 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
             set_error("VARCHAR column %d is not the group key", c);
             return GB_ERR_UNSUPPORTED;
         }
-        if (f->cols[col_map[c]].plain_strings) {
-            set_error("Parquet column '%s' has PLAIN BYTE_ARRAY pages; the GPU path decodes dictionary-encoded "
-                      "VARCHAR columns", f->cols[col_map[c]].name.c_str());
-            return GB_ERR_UNSUPPORTED;
-        }
         vc = c;
     }
     // string predicates must be on the VARCHAR key (tested per dictionary entry)
@@ -1956,20 +2021,37 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
             // each row group's dictionary entries start at its running base
             const int64_t *ids = nullptr;
             const uint8_t *match = nullptr;
+            std::unordered_map<uint32_t, std::pair<uint64_t, uint32_t>> plain_at;
             if ((s = pq_varchar_dict(h, V, S, dfile, base, rg_begin, rg_end, live, col_map[vc], dctl, st, &ids, SF,
-                                     &match)))
+                                     &match, plain_at)))
                 return s;
             uint64_t eb = 0;
             for (uint32_t g = rg_begin; g < rg_end; g++) {
                 if (!live[g - rg_begin]) continue;
                 const PqChunk &ch = (*V.chunks)[g][col_map[vc]];
                 const uint32_t k = (g - rg_begin) * (uint32_t)nc + (uint32_t)vc;
-                for (uint32_t p = col_pages[2 * k]; p < col_pages[2 * k + 1]; p++)
+                if (col_pages[2 * k + 1] - col_pages[2 * k] != ch.page_end - ch.page_begin) {
+                    set_error("page table of the VARCHAR key out of step with its chunk");
+                    return GB_ERR_INVALID;
+                }
+                for (uint32_t p = col_pages[2 * k]; p < col_pages[2 * k + 1]; p++) {
                     if (pages[p].kind == 1) {
                         pages[p].dict_ids = (uint64_t)(uintptr_t)(ids + eb);
                         pages[p].dict_match = match ? (uint64_t)(uintptr_t)(match + eb) : 0;
+                    } else {  // PLAIN: value j is entry j of the page's strings
+                        const auto it = plain_at.find(ch.page_begin + (p - col_pages[2 * k]));
+                        if (it == plain_at.end()) {
+                            set_error("PLAIN BYTE_ARRAY page without its strings");
+                            return GB_ERR_INVALID;
+                        }
+                        pages[p].dict_ids = (uint64_t)(uintptr_t)(ids + it->second.first);
+                        pages[p].dict_match = match ? (uint64_t)(uintptr_t)(match + it->second.first) : 0;
+                        pages[p].dict_n = it->second.second;
                     }
+                }
                 if (ch.dict_off >= 0) eb += ch.dict_n;
+                for (const auto &e : plain_at)
+                    if ((*V.pages)[e.first].rg == g) eb += e.second.second;
             }
         }
         if ((s = grow(S->pages, S->pages_cap, pages.size() * sizeof(DPage) + 16)) ||

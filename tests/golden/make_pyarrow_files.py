@@ -11,7 +11,9 @@ value columns, written as data page v1 and v2, with dictionary encoding on
 every column (values falling back to PLAIN pages once the dictionary page
 limit is reached), on no column, or on the key only, uncompressed or with
 pyarrow's default SNAPPY codec; a dictionary-encoded VARCHAR key with NULL
-keys (uncompressed and SNAPPY); OPTIONAL columns without NULLs.
+keys (uncompressed and SNAPPY), also with PLAIN BYTE_ARRAY pages (no
+dictionary, or pyarrow's fallback once the dictionary page limit is reached);
+OPTIONAL columns without NULLs.
 """
 from __future__ import annotations
 
@@ -93,6 +95,13 @@ def main():
                    "v": pa.array(v2, pa.int64(), mask=vn2)})
     _write("pa_varchar_nulls", t2, row_group_size=8_000, data_page_size=4 * 1024)
     _write("pa_varchar_nulls_snappy", t2, compression="snappy", row_group_size=8_000, data_page_size=4 * 1024)
+    # PLAIN BYTE_ARRAY data pages: no dictionary at all, and a dictionary
+    # whose page limit is reached (pyarrow falls back to PLAIN pages)
+    _write("pa_varchar_plain", t2, row_group_size=8_000, data_page_size=4 * 1024, use_dictionary=False)
+    _write("pa_varchar_fallback_v2", t2, row_group_size=8_000, data_page_size=4 * 1024,
+           dictionary_pagesize_limit=4 * 1024, data_page_version="2.0")
+    _write("pa_varchar_fallback_snappy", t2, compression="snappy", row_group_size=8_000, data_page_size=4 * 1024,
+           dictionary_pagesize_limit=4 * 1024)
     t3 = pa.table({"k": pa.array(np.arange(1000, dtype=np.int32) % 7), "v": pa.array(np.arange(1000, dtype=np.int64))})
     _write("pa_optional_nonnull", t3)
 

@@ -147,16 +147,19 @@ def test_pyarrow_files_with_nulls(name):
             compare(gpu, orc)
 
 
-@pytest.mark.parametrize("name", ["pa_varchar_nulls", "pa_varchar_nulls_snappy"])
+@pytest.mark.parametrize("name", ["pa_varchar_nulls", "pa_varchar_nulls_snappy", "pa_varchar_plain",
+                                  "pa_varchar_fallback_v2", "pa_varchar_fallback_snappy"])
 def test_pyarrow_varchar_key_with_nulls(name):
-    """A pyarrow-written dictionary-encoded VARCHAR key with NULL keys (one
-    NULL group) and a nullable value column; a LIKE on the key; uncompressed
-    and SNAPPY pages."""
+    """A pyarrow-written VARCHAR key with NULL keys (one NULL group) and a
+    nullable value column; a LIKE and an equality on the key; dictionary
+    pages, PLAIN BYTE_ARRAY pages (no dictionary, or pyarrow's fallback to
+    PLAIN once the dictionary page limit is reached: both encodings in one
+    chunk), data page v1 and v2, uncompressed and SNAPPY."""
     data = paf.load(name)
     _, names, v, kn, vn = paf.varchar_columns()
     types = [capi.VARCHAR, BIGINT]
     aggs = [("count_star", -1), ("count", 1), ("sum", 1)]
-    for filters in ([], [(0, "like", b"k001")]):
+    for filters in ([], [(0, "like", b"k001")], [(0, "==", b"k00042")]):
         orc = oracle.run_query(types, [0], aggs, [names, v], filters=filters, nulls=[kn, vn])
         for device in (False, True):
             gpu = run_pq(data, types, [0, 1], [0], aggs, filters=filters, est_groups=1500, device=device,

@@ -299,3 +299,13 @@ def test_pyarrow_fixtures_match_their_columns():
         pf = capi.ParquetFile(paf.load(name))
         assert pf.columns() == [("key", capi.INTEGER), ("f", capi.SMALLINT), ("v", capi.BIGINT), ("x", capi.DOUBLE)]
         pf.close()
+    strs, _, v, kn, vn = paf.varchar_columns()
+    for name in ("pa_varchar_nulls", "pa_varchar_nulls_snappy", "pa_varchar_plain", "pa_varchar_fallback_v2",
+                 "pa_varchar_fallback_snappy"):
+        t = pq_.read_table(io.BytesIO(paf.load(name)))
+        got = t.column("name").to_pylist()
+        assert [None if n else s_.decode() for s_, n in zip(strs, kn)] == got
+        assert np.array_equal(t.column("v").is_null().to_numpy(zero_copy_only=False), vn)
+        pf = capi.ParquetFile(paf.load(name))
+        assert pf.columns() == [("name", capi.VARCHAR), ("v", capi.BIGINT)]
+        pf.close()
