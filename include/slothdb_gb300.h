@@ -273,6 +273,23 @@ gb_status gb_pq_column_info(const gb_pq_file *f, uint32_t col, char *name, uint3
  * (physical_planner.cpp:1142-1150, src/storage/parquet.cpp:3200-3240).
  * INTEGER, BIGINT and DOUBLE statistics are read (the reference reads none
  * for SMALLINT).  gb_agg_ingest_parquet skips the row groups this rules out. */
+/* Ungrouped SUM and COUNT of one INT64 dictionary-encoded column over row
+ * groups [rg_begin, rg_end) without decoding it: a histogram of each row
+ * group's dictionary indices, then sum_idx count[idx] * dict[idx]
+ * (TryDictHistogramAgg, include/slothdb/execution/dict_histogram.hpp:34, per
+ * row group ParquetReader::DecodeBigintColumnHistogram,
+ * src/storage/parquet.cpp:2726-2897, the fast path of
+ * SELECT SUM(c) / AVG(c) / COUNT(c) FROM file, physical_planner.cpp:
+ * 8745-8790).  PLAIN pages of the column (dictionary fallback) are summed as
+ * they are; indices past the dictionary are not counted, as there.  *count =
+ * the values counted, *sum = their exact sum rounded once to double.
+ * GB_ERR_UNSUPPORTED — the reference's `false`, after which the engine takes
+ * the fused path — when the column is not INT64, a row group has no
+ * dictionary page, a page holds NULLs, or a chunk is compressed.  mem:
+ * GB_MEM_DEVICE reads the uploaded file (gb_pq_upload), GB_MEM_HOST copies
+ * the column's byte range. */
+gb_status gb_pq_dict_sum(gb_pq_file *f, uint32_t col, uint32_t rg_begin, uint32_t rg_end, int32_t mem, void *stream,
+                         int64_t *count, double *sum);
 gb_status gb_pq_row_group_might_match(const gb_pq_file *f, uint32_t rg, const int32_t *col_map, uint32_t n_cols,
                                       const gb_filter *filters, uint32_t n_filters, int32_t *might);
 /* Copies the whole file into HBM once (a resident table). */

@@ -158,6 +158,8 @@ _SIGS = {
     "gb_pq_num_rows": (C.c_uint64, [C.c_void_p]),
     "gb_pq_num_columns": (C.c_uint32, [C.c_void_p]),
     "gb_pq_column_info": (C.c_int, [C.c_void_p, C.c_uint32, C.c_char_p, C.c_uint32, C.POINTER(C.c_int32)]),
+    "gb_pq_dict_sum": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_int32, C.c_void_p,
+                                 C.POINTER(C.c_int64), C.POINTER(C.c_double)]),
     "gb_pq_row_group_might_match": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_int32), C.c_uint32,
                                               C.c_void_p, C.c_uint32, C.POINTER(C.c_int32)]),
     "gb_pq_upload": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -595,6 +597,16 @@ class ParquetFile:
     @property
     def num_rows(self):
         return int(self.lib.gb_pq_num_rows(self.h))
+
+    def dict_sum(self, col, rg_begin=0, rg_end=None, device=False, stream=None):
+        """(count, sum) of INT64 file column `col` through the dictionary
+        histogram (gb_pq_dict_sum); raises GbError(GB_ERR_UNSUPPORTED) where
+        the reference would take the fused path."""
+        rg_end = self.num_row_groups if rg_end is None else rg_end
+        n, sm = C.c_int64(), C.c_double()
+        check(self.lib.gb_pq_dict_sum(self.h, int(col), int(rg_begin), int(rg_end), MEM_DEVICE if device else MEM_HOST,
+                                      C.c_void_p(stream) if stream else None, C.byref(n), C.byref(sm)))
+        return int(n.value), float(sm.value)
 
     def row_group_might_match(self, rg, col_map, filters):
         """Zone map of row group `rg`: False when its column statistics rule

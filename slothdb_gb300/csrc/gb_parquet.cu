@@ -1349,6 +1349,103 @@ static gb_status pq_build_index(gb_pq_file *f, cudaStream_t st) {
     return GB_OK;
 }
 
+// ------------------------------------------------ ungrouped dictionary histogram
+// SUM / COUNT of one INT64 column without decoding it (TryDictHistogramAgg,
+// include/slothdb/execution/dict_histogram.hpp:34, per row group
+// ParquetReader::DecodeBigintColumnHistogram, src/storage/parquet.cpp:
+// 2726-2897): a histogram of each row group's dictionary indices, then
+// sum_idx count[idx] * dict[idx]; PLAIN pages of the column are summed as
+// they are.  Sums are exact (128-bit) until the one rounding to double.
+struct DHGroup {
+    uint64_t dict_off;   // dictionary values (INT64, PLAIN) in the device file
+    uint32_t dict_n;     // dictionary entries
+    uint32_t hist_base;  // the row group's first histogram slot
+};
+
+__device__ __forceinline__ void block_add_i128(__int128 x, u64 cnt, u64 *out3) {
+    __shared__ __int128 s_v[32];
+    __shared__ u64 s_c[32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        const u64 lo = __shfl_down_sync(FULL, (u64)x, o), hi = __shfl_down_sync(FULL, (u64)(x >> 64), o);
+        x += (__int128)(((unsigned __int128)hi << 64) | lo);
+        cnt += __shfl_down_sync(FULL, cnt, o);
+    }
+    if (lane == 0) {
+        s_v[warp] = x;
+        s_c[warp] = cnt;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __int128 t = 0;
+        u64 c = 0;
+        for (int w = 0; w < nwarps; w++) {
+            t += s_v[w];
+            c += s_c[w];
+        }
+        out3[0] = (u64)t;
+        out3[1] = (u64)(t >> 64);
+        out3[2] = c;
+    }
+}
+
+// One CTA per page of the column.  Dictionary pages: every index entry
+// below the page's value count bumps its row group's histogram (an RLE run
+// once, by its length; indices past the dictionary are skipped, as the
+// reference does).  PLAIN pages: their values and count go to part[3 * page].
+// A page with NULLs sets *nulls (the reference then takes the fused path).
+__global__ void k_pq_dict_hist(const uint8_t *file, const DPage *pages, const DRun *runs, const uint32_t *page_runs,
+                               const uint32_t *page_group, const DHGroup *groups, uint32_t *hist, u64 *part,
+                               uint32_t *nulls) {
+    const uint32_t p = blockIdx.x;
+    const DPage pg = pages[p];
+    u64 *out3 = part + 3 * (u64)p;
+    if (pg.def_bytes && page_runs[PQ_PR * p + 3] != pg.n_values) {
+        if (threadIdx.x == 0) {
+            atomicOr(nulls, 1u);
+            out3[0] = out3[1] = out3[2] = 0;
+        }
+        return;
+    }
+    const uint32_t total = pg.n_values;
+    if (pg.kind == 1) {
+        const uint32_t nr = page_runs[PQ_PR * p], bw = page_runs[PQ_PR * p + 1];
+        const DRun *rr = runs + pg.run_base;
+        const DHGroup G = groups[page_group[p]];
+        for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) {
+            if (nr == 0) break;
+            const DRun rn = rr[run_search(rr, 0, nr, i)];
+            if (i < rn.start || i >= rn.start + rn.cnt) continue;  // past the decoded entries
+            if (rn.off == 0xffffffffu) {
+                if (i == rn.start && rn.val < G.dict_n)
+                    atomicAdd(&hist[G.hist_base + rn.val], min(rn.cnt, total - rn.start));
+            } else {
+                const uint32_t idx = load_bits(file + pg.off + rn.off, (u64)(i - rn.start) * bw, bw);
+                if (idx < G.dict_n) atomicAdd(&hist[G.hist_base + idx], 1u);
+            }
+        }
+        if (threadIdx.x == 0) out3[0] = out3[1] = out3[2] = 0;
+    } else {
+        __int128 acc = 0;
+        for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) acc += (i64)load_plain(file + pg.off + 8 * (u64)i, 8);
+        block_add_i128(acc, threadIdx.x == 0 ? total : 0, out3);
+    }
+}
+
+// One CTA per row group: sum_idx count[idx] * dict[idx] and sum_idx count[idx].
+__global__ void k_pq_dict_reduce(const uint8_t *file, const DHGroup *groups, const uint32_t *hist, u64 *part) {
+    const DHGroup G = groups[blockIdx.x];
+    __int128 acc = 0;
+    u64 cnt = 0;
+    for (uint32_t e = threadIdx.x; e < G.dict_n; e += blockDim.x) {
+        const uint32_t c = hist[G.hist_base + e];
+        if (!c) continue;
+        acc += (__int128)c * (i64)load_plain(file + G.dict_off + 8 * (u64)e, 8);
+        cnt += c;
+    }
+    block_add_i128(acc, cnt, part + 3 * (u64)blockIdx.x);
+}
+
 extern "C" {
 
 gb_status gb_pq_open(const uint8_t *bytes, uint64_t size, gb_pq_file **out) {
@@ -1414,6 +1511,132 @@ gb_status gb_pq_row_group_might_match(const gb_pq_file *f, uint32_t rg, const in
         }
     }
     return GB_OK;
+}
+
+gb_status gb_pq_dict_sum(gb_pq_file *f, uint32_t col, uint32_t rg_begin, uint32_t rg_end, int32_t mem, void *stream,
+                         int64_t *count, double *sum) {
+    if (!f || !count || !sum || col >= f->cols.size() || rg_begin > rg_end || rg_end > f->rg_rows.size()) {
+        set_error("invalid arguments to gb_pq_dict_sum");
+        return GB_ERR_INVALID;
+    }
+    *count = 0;
+    *sum = 0.0;
+    if (f->cols[col].gtype != GB_T_BIGINT) {
+        set_error("the dictionary histogram sums INT64 columns");
+        return GB_ERR_UNSUPPORTED;
+    }
+    if (rg_begin == rg_end) return GB_OK;
+    for (uint32_t g = rg_begin; g < rg_end; g++) {
+        const PqChunk &ch = f->chunks[g][col];
+        if (ch.dict_off < 0) {
+            set_error("row group %u of the column has no dictionary page", g);
+            return GB_ERR_UNSUPPORTED;
+        }
+        if (ch.codec != 0) {
+            set_error("the dictionary histogram reads uncompressed column chunks");
+            return GB_ERR_UNSUPPORTED;
+        }
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    gb_status s = GB_OK;
+    // the column's bytes: the resident file, or its row groups' byte range
+    const uint8_t *dfile = nullptr;
+    uint64_t base = 0, lo = ~0ull, hi = 0;
+    void *copy = nullptr;
+    if (mem == GB_MEM_DEVICE) {
+        if (!f->dev) {
+            set_error("gb_pq_upload the file before summing with GB_MEM_DEVICE");
+            return GB_ERR_STATE;
+        }
+        dfile = (const uint8_t *)f->dev;
+    } else {
+        for (uint32_t g = rg_begin; g < rg_end; g++) {
+            lo = std::min(lo, f->chunks[g][col].start);
+            hi = std::max(hi, f->chunks[g][col].start + f->chunks[g][col].size);
+        }
+        GB_CUDA(cudaMalloc(&copy, hi - lo + 64));
+        dfile = (const uint8_t *)copy;
+        base = lo;
+    }
+    std::vector<DPage> pages;
+    std::vector<RunJob> jobs;
+    std::vector<uint32_t> col_pages;
+    uint32_t run_total = 0;
+    const int32_t cols[1] = {(int32_t)col};
+    std::vector<DHGroup> groups;
+    std::vector<uint32_t> page_group;
+    uint64_t hist_n = 0;
+    void *d_pages = nullptr, *d_runs = nullptr, *d_page_runs = nullptr, *d_jobs = nullptr, *d_pg = nullptr,
+         *d_groups = nullptr, *d_hist = nullptr, *d_part = nullptr, *d_ctl = nullptr;
+    auto done = [&](gb_status r) {
+        for (void *q : {copy, d_pages, d_runs, d_page_runs, d_jobs, d_pg, d_groups, d_hist, d_part, d_ctl})
+            if (q) cudaFree(q);
+        return r;
+    };
+    if (copy && cudaMemcpyAsync(copy, f->host + lo, hi - lo, cudaMemcpyHostToDevice, st) != cudaSuccess)
+        return done(cuda_fail(cudaGetLastError(), "cudaMemcpyAsync"));
+    if ((s = pq_page_table(f, PqView{&f->chunks, &f->pages}, rg_begin, rg_end, cols, 1, base, nullptr, pages, jobs,
+                           col_pages, run_total)))
+        return done(s);
+    for (uint32_t g = rg_begin; g < rg_end; g++) {
+        const PqChunk &ch = f->chunks[g][col];
+        if (hist_n + ch.dict_n > 0xffffffffull) return done(GB_ERR_UNSUPPORTED);
+        groups.push_back({(uint64_t)ch.dict_off - base, ch.dict_n, (uint32_t)hist_n});
+        hist_n += ch.dict_n;
+        const uint32_t k = g - rg_begin;
+        for (uint32_t q = col_pages[2 * k]; q < col_pages[2 * k + 1]; q++) page_group.push_back(k);
+    }
+    const size_t np = pages.size(), ng = groups.size();
+    cudaError_t e;
+    if ((e = cudaMalloc(&d_pages, np * sizeof(DPage) + 16)) || (e = cudaMalloc(&d_runs, (size_t)run_total * sizeof(DRun) + 16)) ||
+        (e = cudaMalloc(&d_page_runs, np * PQ_PR * 4 + 16)) || (e = cudaMalloc(&d_jobs, jobs.size() * sizeof(RunJob) + 16)) ||
+        (e = cudaMalloc(&d_pg, np * 4 + 16)) || (e = cudaMalloc(&d_groups, ng * sizeof(DHGroup) + 16)) ||
+        (e = cudaMalloc(&d_hist, hist_n * 4 + 16)) || (e = cudaMalloc(&d_part, (np + ng) * 24 + 16)) ||
+        (e = cudaMalloc(&d_ctl, sizeof(Ctl))))
+        return done(cuda_fail(e, "cudaMalloc (dictionary histogram)"));
+    if ((e = cudaMemcpyAsync(d_pages, pages.data(), np * sizeof(DPage), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(RunJob), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(d_pg, page_group.data(), np * 4, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(d_groups, groups.data(), ng * sizeof(DHGroup), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemsetAsync(d_page_runs, 0, np * PQ_PR * 4 + 16, st)) || (e = cudaMemsetAsync(d_hist, 0, hist_n * 4 + 16, st)) ||
+        (e = cudaMemsetAsync(d_ctl, 0, sizeof(Ctl), st)))
+        return done(cuda_fail(e, "cudaMemcpyAsync (dictionary histogram)"));
+    if (!jobs.empty())
+        k_pq_runs<<<(unsigned)jobs.size(), 128, 0, st>>>(dfile, (const DPage *)d_pages, (const RunJob *)d_jobs,
+                                                         (DRun *)d_runs, (uint32_t *)d_page_runs, (Ctl *)d_ctl);
+    Ctl c;
+    if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&c, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st)) ||
+        (e = cudaStreamSynchronize(st)))
+        return done(cuda_fail(e, "k_pq_runs"));
+    if ((s = pq_fail_if_err(c))) return done(s);
+    uint32_t *nulls = (uint32_t *)d_ctl;  // the control block's first word, zeroed above
+    if ((e = cudaMemsetAsync(nulls, 0, 4, st))) return done(cuda_fail(e, "cudaMemsetAsync"));
+    if (np)
+        k_pq_dict_hist<<<(unsigned)np, 256, 0, st>>>(dfile, (const DPage *)d_pages, (const DRun *)d_runs,
+                                                    (const uint32_t *)d_page_runs, (const uint32_t *)d_pg,
+                                                    (const DHGroup *)d_groups, (uint32_t *)d_hist, (u64 *)d_part,
+                                                    nulls);
+    k_pq_dict_reduce<<<(unsigned)ng, 256, 0, st>>>(dfile, (const DHGroup *)d_groups, (const uint32_t *)d_hist,
+                                                  (u64 *)d_part + 3 * np);
+    std::vector<u64> part(3 * (np + ng));
+    uint32_t has_nulls = 0;
+    if ((e = cudaGetLastError()) ||
+        (e = cudaMemcpyAsync(part.data(), d_part, part.size() * 8, cudaMemcpyDeviceToHost, st)) ||
+        (e = cudaMemcpyAsync(&has_nulls, nulls, 4, cudaMemcpyDeviceToHost, st)) || (e = cudaStreamSynchronize(st)))
+        return done(cuda_fail(e, "k_pq_dict_hist"));
+    if (has_nulls) {
+        set_error("a page of the column holds NULLs (the histogram sums every row)");
+        return done(GB_ERR_UNSUPPORTED);
+    }
+    __int128 t = 0;
+    unsigned long long n = 0;
+    for (size_t i = 0; i < np + ng; i++) {
+        t += (__int128)(((unsigned __int128)part[3 * i + 1] << 64) | part[3 * i]);
+        n += part[3 * i + 2];
+    }
+    *count = (int64_t)n;
+    *sum = (double)t;
+    return done(GB_OK);
 }
 
 gb_status gb_pq_upload(gb_pq_file *f, void *stream) {

@@ -13,7 +13,8 @@ limit is reached), on no column, or on the key only, uncompressed or with
 pyarrow's default SNAPPY codec; a dictionary-encoded VARCHAR key with NULL
 keys (uncompressed and SNAPPY), also with PLAIN BYTE_ARRAY pages (no
 dictionary, or pyarrow's fallback once the dictionary page limit is reached);
-OPTIONAL columns without NULLs.
+OPTIONAL columns without NULLs; an INT64 column whose dictionary falls back
+to PLAIN pages.
 """
 from __future__ import annotations
 
@@ -64,6 +65,14 @@ def varchar_columns(seed=32, n=N_ROWS):
     return strs, (offs, blob), v, kn, vn
 
 
+def int64_column(seed=33, n=N_ROWS):
+    """An INT64 column of 20,000 distinct values (its dictionary outgrows a
+    16 KB dictionary page, so pyarrow falls back to PLAIN pages)."""
+    rng = np.random.default_rng(seed)
+    vals = rng.integers(-10**6, 10**6, 20_000, dtype=np.int64)
+    return vals[rng.integers(0, len(vals), n)]
+
+
 def load(name):
     """The committed file's bytes."""
     with gzip.open(os.path.join(OUT, name + ".parquet.gz"), "rb") as fh:
@@ -104,6 +113,9 @@ def main():
            dictionary_pagesize_limit=4 * 1024)
     t3 = pa.table({"k": pa.array(np.arange(1000, dtype=np.int32) % 7), "v": pa.array(np.arange(1000, dtype=np.int64))})
     _write("pa_optional_nonnull", t3)
+    t4 = pa.table({"c": pa.array(int64_column(), pa.int64())})
+    _write("pa_int64_fallback", t4, row_group_size=8_000, data_page_size=8 * 1024,
+           dictionary_pagesize_limit=16 * 1024)
 
 
 if __name__ == "__main__":

@@ -300,3 +300,58 @@ def test_zone_map_pruning_against_the_oracle(key):
                          batches=batches, pruned=got)
             assert got == [n_pruned], (filters, device, batches, got)
             compare(gpu, orc)
+
+
+def _exact(vals):
+    return int(np.asarray(vals, dtype=np.int64).astype(object).sum())
+
+
+def _near(got, vals):
+    """(count, sum) equal to the values' count and exact sum rounded once."""
+    cnt, sm = got
+    ex = _exact(vals)
+    return cnt == len(vals) and abs(sm - ex) <= abs(ex) * 2.0 ** -52
+
+def test_dictionary_histogram_sum():
+    """Ungrouped SUM / COUNT of an INT64 dictionary column through the
+    dictionary histogram (no decode), host and resident files, a row-group
+    range, a dictionary that falls back to PLAIN pages (pyarrow), OPTIONAL
+    without NULLs; the shapes the reference leaves to its fused path (NULLs,
+    no dictionary, not INT64) are GB_ERR_UNSUPPORTED."""
+    rng = np.random.default_rng(91)
+    n = 300_007
+    d = rng.integers(-10**12, 10**12, 5000, dtype=np.int64)
+    lens = rng.geometric(0.2, n)
+    idx = np.repeat(rng.integers(0, len(d), len(lens)).astype(np.uint32), lens)[:n]
+    plain = rng.integers(0, 10**6, n, dtype=np.int64)
+    data = pq.write([pq.Column("k", pq.T_INT32, values=(idx % 97).astype(np.int32)),
+                     pq.Column("c", pq.T_INT64, dictionary=d, indices=idx),
+                     pq.Column("p", pq.T_INT64, values=plain)], row_group_rows=50_000, page_rows=7_001)
+    vals = d[idx]
+    pf = capi.ParquetFile(data)
+    try:
+        pf.upload()
+        for device in (False, True):
+            assert _near(pf.dict_sum(1, device=device), vals)
+            assert _near(pf.dict_sum(1, 2, 4, device=device), vals[100_000:200_000])
+        assert pf.dict_sum(1, 3, 3) == (0, 0.0)
+        for col in (0, 2):  # INT32; INT64 without a dictionary
+            with pytest.raises(capi.GbError) as e:
+                pf.dict_sum(col)
+            assert e.value.status == capi.GB_ERR_UNSUPPORTED
+    finally:
+        pf.close()
+    for name, col, expect in (("pa_optional_nonnull", 1, np.arange(1000, dtype=np.int64)),
+                              ("pa_int64_fallback", 0, paf.int64_column())):
+        pf = capi.ParquetFile(paf.load(name))
+        try:
+            assert _near(pf.dict_sum(col), expect)
+        finally:
+            pf.close()
+    pf = capi.ParquetFile(paf.load("pa_nulls_v1_dict"))  # v holds NULLs
+    try:
+        with pytest.raises(capi.GbError) as e:
+            pf.dict_sum(2)
+        assert e.value.status == capi.GB_ERR_UNSUPPORTED
+    finally:
+        pf.close()

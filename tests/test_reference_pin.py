@@ -270,3 +270,29 @@ def test_golden_fixtures_are_reference_results():
             if m.any():
                 assert rel_err(z["agg%d" % a][m], comp[m]).max() <= REL_TOL_F64, n
             a += 1
+
+
+def test_dictionary_histogram_sum_and_count():
+    """The reference's ungrouped SUM / COUNT over INT64 dictionary columns
+    (its dictionary-histogram fast path, one aggregate per query) equal the
+    values' count and sum: a project-writer file and a pyarrow file whose
+    dictionary falls back to PLAIN pages."""
+    import sys
+    from slothdb_gb300 import parquet as gpq
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_pyarrow_files as paf
+    rng = np.random.default_rng(92)
+    d = rng.integers(-10**6, 10**6, 3000, dtype=np.int64)
+    idx = rng.integers(0, len(d), 120_000).astype(np.uint32)
+    files = [(gpq.write([gpq.Column("c", gpq.T_INT64, dictionary=d, indices=idx)], row_group_rows=40_000,
+                        page_rows=9_000), d[idx]),
+             (paf.load("pa_int64_fallback"), paf.int64_column())]
+    with tempfile.TemporaryDirectory() as tmp:
+        for i, (data, vals) in enumerate(files):
+            path = os.path.join(tmp, "f%d.parquet" % i)
+            with open(path, "wb") as fh:
+                fh.write(data)
+            s, _ = reference.query("SELECT SUM(c) FROM '%s'" % path)
+            n, _ = reference.query("SELECT COUNT(c) FROM '%s'" % path)
+            assert int(s[0][1][0]) == int(vals.astype(object).sum())
+            assert int(n[0][1][0]) == len(vals)
