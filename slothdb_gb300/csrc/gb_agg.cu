@@ -420,6 +420,107 @@ __global__ void __launch_bounds__(512) k_topn(const __grid_constant__ TopnArgs A
     if (threadIdx.x == 0) out_n[blockIdx.x] = nb;
 }
 
+// TopN for K <= 32: each warp keeps its best K rows in registers, sorted
+// (lane i holds the i-th best; lanes >= K hold nothing); a row better than
+// the warp's K-th enters by one shuffle insertion.  Warp 0 then merges the
+// block's warp lists the same way.  Items: result rows (ids == nullptr) or a
+// candidate list of row ids (~0u = none).  Output: the block's best K ids in
+// out_ids[blockIdx.x * K + i] (~0u past out_n[blockIdx.x]).
+struct TopItem {
+    u64 p, s;
+    u32 id;
+};
+
+// Insert (p, s, id) into the warp's sorted list (every lane calls it with the
+// same item); returns the new K-th best.
+__device__ __forceinline__ void warp_list_insert(TopItem &mine, int K, u64 p, u64 s, u32 id) {
+    const int lane = threadIdx.x & 31;
+    const bool better = lane < K && code_less(mine.p, mine.s, p, s);  // my slot stays ahead of the item
+    const int pos = __popc(__ballot_sync(FULL, better));
+    const u64 up = __shfl_up_sync(FULL, mine.p, 1), us = __shfl_up_sync(FULL, mine.s, 1);
+    const u32 ui = __shfl_up_sync(FULL, mine.id, 1);
+    if (lane < K) {
+        if (lane == pos) {
+            mine.p = p;
+            mine.s = s;
+            mine.id = id;
+        } else if (lane > pos) {
+            mine.p = up;
+            mine.s = us;
+            mine.id = ui;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(512) k_topn_small(const __grid_constant__ TopnArgs A, const u32 *ids, u64 n,
+                                                    u32 *out_ids, u32 *out_n) {
+    __shared__ TopItem s_list[16][32];
+    const int K = A.K;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    TopItem mine{~0ull, ~0ull, ~0u};
+    const u64 per = (n + gridDim.x - 1) / gridDim.x;
+    const u64 lo = blockIdx.x * per, hi = min(n, lo + per);
+    constexpr int TR = 4;  // rows per lane per step: their loads are issued together
+    u64 tp = ~0ull, ts = ~0ull;  // the warp's K-th best
+    bool full = false;           // K rows held: only better rows enter
+    for (u64 base = lo + (u64)warp * 32 * TR; base < hi; base += (u64)nwarps * 32 * TR) {
+        u64 cp[TR], cs[TR];
+        u32 row[TR];
+#pragma unroll
+        for (int j = 0; j < TR; j++) {
+            const u64 it = base + (u64)j * 32 + lane;
+            cp[j] = cs[j] = ~0ull;
+            row[j] = ~0u;
+            if (it < hi) {
+                row[j] = ids ? ids[it] : (u32)it;
+                if (row[j] != ~0u) topn_code(A, row[j], cp[j], cs[j]);
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < TR; j++) {
+            bool want = row[j] != ~0u && (!full || code_less(cp[j], cs[j], tp, ts));
+            unsigned m;
+            while ((m = __ballot_sync(FULL, want))) {
+                const int src = __ffs(m) - 1;
+                const u64 p = __shfl_sync(FULL, cp[j], src), s = __shfl_sync(FULL, cs[j], src);
+                const u32 id = __shfl_sync(FULL, row[j], src);
+                warp_list_insert(mine, K, p, s, id);
+                tp = __shfl_sync(FULL, mine.p, K - 1);
+                ts = __shfl_sync(FULL, mine.s, K - 1);
+                full = __shfl_sync(FULL, mine.id, K - 1) != ~0u;
+                if (lane == src) want = false;
+                want = want && (!full || code_less(cp[j], cs[j], tp, ts));
+            }
+        }
+    }
+    s_list[warp][lane] = mine;
+    __syncthreads();
+    if (warp == 0) {
+        TopItem best{~0ull, ~0ull, ~0u};
+        u64 bp = ~0ull, bs = ~0ull;
+        bool bfull = false;
+        for (int w = 0; w < nwarps; w++) {
+            const TopItem c = s_list[w][lane];
+            bool want = lane < K && c.id != ~0u && (!bfull || code_less(c.p, c.s, bp, bs));
+            unsigned m;
+            while ((m = __ballot_sync(FULL, want))) {
+                const int src = __ffs(m) - 1;
+                const u64 p = __shfl_sync(FULL, c.p, src), s = __shfl_sync(FULL, c.s, src);
+                const u32 id = __shfl_sync(FULL, c.id, src);
+                warp_list_insert(best, K, p, s, id);
+                bp = __shfl_sync(FULL, best.p, K - 1);
+                bs = __shfl_sync(FULL, best.s, K - 1);
+                bfull = __shfl_sync(FULL, best.id, K - 1) != ~0u;
+                if (lane == src) want = false;
+                want = want && (!bfull || code_less(c.p, c.s, bp, bs));
+            }
+        }
+        if (lane < K) out_ids[(u64)blockIdx.x * K + lane] = best.id;
+        const unsigned have = __ballot_sync(FULL, lane < K && best.id != ~0u);
+        if (lane == 0) out_n[blockIdx.x] = (u32)__popc(have);
+    }
+}
+
 // Gather rows `ids[0..k)` of the dense result into TopN output buffers.
 __global__ void k_gather_rows(const u32 *ids, u32 k, int ncols, const __grid_constant__ EmitArgs src,
                               const __grid_constant__ EmitArgs dst, const int32_t *types) {
@@ -590,6 +691,7 @@ struct gb_agg {
     bool precombine = true;
     bool precombine_set = false;  // the "precombine" option was given (else the fast path chooses)
     bool fast_ingest = true;      // integer plans take the register-resident fast kernel
+    bool topn_small = true;       // K <= 32: warp-register TopN lists
     u32 tile_rows = 8192;
     // profiling (CUDA events around each kernel, resolved at sync points)
     bool profiling = false;
@@ -1678,15 +1780,21 @@ static gb_status run_topn(gb_agg *h, cudaStream_t st) {
     if ((s = h->topn_ids_b.ensure((size_t)K * 4 + 64))) return s;
     if ((s = h->topn_cnt.ensure((size_t)grid * 4 + 64))) return s;
     GB_CUDA(cudaMemsetAsync(h->topn_ids_a.p, 0xff, (size_t)grid * K * 4, st));
+    const bool small = K <= 32 && h->topn_small;  // warp-register lists
     {
         ProfScope ps(h, "k_topn", st);
-        k_topn<<<grid, 512, smem, st>>>(A, nullptr, n, (u32 *)h->topn_ids_a.p, (u32 *)h->topn_cnt.p, sortn);
+        if (small) k_topn_small<<<grid, 512, 0, st>>>(A, nullptr, n, (u32 *)h->topn_ids_a.p, (u32 *)h->topn_cnt.p);
+        else k_topn<<<grid, 512, smem, st>>>(A, nullptr, n, (u32 *)h->topn_ids_a.p, (u32 *)h->topn_cnt.p, sortn);
     }
     h->launches++;
     GB_CUDA(cudaGetLastError());
     // second pass over the grid*K candidate ids (padding ids are skipped)
-    k_topn<<<1, 512, smem, st>>>(A, (const u32 *)h->topn_ids_a.p, (u64)grid * K, (u32 *)h->topn_ids_b.p,
-                                 (u32 *)h->topn_cnt.p, sortn);
+    if (small)
+        k_topn_small<<<1, 512, 0, st>>>(A, (const u32 *)h->topn_ids_a.p, (u64)grid * K, (u32 *)h->topn_ids_b.p,
+                                        (u32 *)h->topn_cnt.p);
+    else
+        k_topn<<<1, 512, smem, st>>>(A, (const u32 *)h->topn_ids_a.p, (u64)grid * K, (u32 *)h->topn_ids_b.p,
+                                     (u32 *)h->topn_cnt.p, sortn);
     h->launches++;
     GB_CUDA(cudaGetLastError());
     u32 kf = 0;
@@ -2222,6 +2330,9 @@ gb_status gb_agg_set_option(gb_agg *h, const char *name, int64_t value) {
     } else if (n == "precombine") {
         h->precombine = value != 0;
         h->precombine_set = true;
+    } else if (n == "topn_small") {
+        if (value < 0 || value > 1) return GB_ERR_INVALID;
+        h->topn_small = value != 0;
     } else if (n == "fast_ingest") {
         if (value < 0 || value > 1) return GB_ERR_INVALID;
         h->fast_ingest = value != 0;

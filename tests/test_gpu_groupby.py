@@ -259,6 +259,51 @@ def test_topn_ties_key_ascending_and_asc_order():
     assert gpu["keys"][0].tolist() == [7, 9]
 
 
+def _expected_topn(orc, col, asc, K):
+    """Rows of the oracle's result in TopN order: the order column's value
+    (NULL first ascending, last descending), then the key ascending."""
+    n = orc["n_groups"]
+    vals, nul, _ = orc["aggs"][col - 1]
+    keys = orc["keys"][0].astype(np.int64)
+    big = 1 << 64
+
+    def code(i):
+        prim = 0 if nul[i] else (int(vals[i]) + (1 << 63))
+        return (prim if asc else (big - 1 - prim), int(keys[i]))
+    return sorted(range(n), key=code)[:K]
+
+
+@pytest.mark.parametrize("small", [0, 1])
+def test_topn_limits_orders_and_nulls(small):
+    """TopN for K from 1 to 64 (warp-register lists up to 32, the
+    shared-memory select beyond, and with the small path switched off) on
+    COUNT DESC with many ties, MIN ASC with NULL results, and a result with
+    fewer groups than K that holds a NULL order value and the key INT64_MAX."""
+    rng = np.random.default_rng(12)
+    n = 400_000
+    k = rng.integers(0, 30_000, n).astype(np.int64)
+    v = rng.integers(-1000, 1000, n, dtype=np.int64)
+    vn = rng.random(n) < 0.3
+    vn[k % 97 == 0] = True  # groups whose values are all NULL
+    aggs = [("count_star", -1), ("min", 1)]
+    orc = oracle.run_query([BIGINT, BIGINT], [0], aggs, [k, v], nulls=[None, vn])
+    for K in (1, 5, 10, 32, 33, 64):
+        for col, asc in ((1, False), (2, True), (2, False)):
+            gpu = run_gpu([BIGINT, BIGINT], [0], aggs, [k, v], nulls=[None, vn], topn=(col, asc, K),
+                          options={"topn_small": small})
+            want = _expected_topn(orc, col, asc, K)
+            assert gpu["keys"][0].astype(np.int64).tolist() == orc["keys"][0][want].astype(np.int64).tolist(), (K, col)
+    kk = np.array([np.iinfo(np.int64).max, 3, 3, 5], dtype=np.int64)
+    vv = np.array([1, 2, 3, 4], dtype=np.int64)
+    vnn = np.array([True, False, False, False])
+    orc = oracle.run_query([BIGINT, BIGINT], [0], aggs, [kk, vv], nulls=[None, vnn])
+    for K in (3, 10):
+        gpu = run_gpu([BIGINT, BIGINT], [0], aggs, [kk, vv], nulls=[None, vnn], topn=(2, False, K),
+                      options={"topn_small": small})
+        want = _expected_topn(orc, 2, False, K)
+        assert gpu["keys"][0].astype(np.int64).tolist() == orc["keys"][0][want].astype(np.int64).tolist()
+
+
 def test_nulls_in_keys_and_values():
     n = 200_000
     rng = np.random.default_rng(6)
