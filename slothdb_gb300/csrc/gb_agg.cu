@@ -265,7 +265,10 @@ __device__ void smem_bitonic(u64 *P_, u64 *S_, u32 *I_, int n) {
                 int ixj = i ^ j;
                 if (ixj > i) {
                     bool up = ((i & k) == 0);
-                    bool gt = code_less(P_[ixj], S_[ixj], P_[i], S_[i]);
+                    // ties on the code order by id, so a real row whose code
+                    // is all ones still sorts before the empty entries (~0u)
+                    bool gt = code_less(P_[ixj], S_[ixj], P_[i], S_[i]) ||
+                              (P_[ixj] == P_[i] && S_[ixj] == S_[i] && I_[ixj] < I_[i]);
                     if (gt == up) {
                         u64 tp = P_[i]; P_[i] = P_[ixj]; P_[ixj] = tp;
                         u64 ts = S_[i]; S_[i] = S_[ixj]; S_[ixj] = ts;
