@@ -59,7 +59,8 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--cpu-sample", type=int, default=20_000_000)
     ap.add_argument("--workload", default="zipf100m", choices=["zipf100m", "plain1m", "batch256", "serve",
-                                                                      "parquet200m", "distinct100m"])
+                                                                      "parquet200m", "parquet200m_snappy",
+                                                                      "dictsum200m", "distinct100m"])
     ap.add_argument("--pq-rows", type=int, default=200_000_000, help="parquet200m: rows in the file")
     ap.add_argument("--tables", type=int, default=256)
     ap.add_argument("--duration", type=float, default=120.0, help="serve: seconds of Poisson arrivals")
@@ -1066,8 +1067,11 @@ def run_parquet(args):
     if args.impl == "reference" and rank != 0:
         return  # rank 0 alone runs the reference arm
     rows = args.pq_rows
+    snappy = args.workload == "parquet200m_snappy"
     t0 = time.time()
-    data, key, f, v = pq.filter_groupby_file(n_rows=rows, row_group_rows=1_000_000)
+    data, key, f, v = pq.filter_groupby_file(n_rows=rows, row_group_rows=1_000_000,
+                                             codec="snappy" if snappy else None)
+    raw_bytes = len(pq.filter_groupby_file(n_rows=rows, row_group_rows=1_000_000)[0]) if snappy else len(data)
     gen_s = time.time() - t0
     if args.impl == "reference":
         return run_parquet_reference(args, key, f, v, rows)
@@ -1126,9 +1130,17 @@ def run_parquet(args):
     clk = clocks.stop()
     ms = e0.elapsed_time(e1) / args.steps
     scan_ms = prof.get("k_pq_scan", float("nan"))
-    achieved = file_bytes / (scan_ms / 1e3) / 1e9
+    # the scan reads the (decompressed) page bytes; the inflate reads the
+    # compressed pages and writes the decompressed image
+    achieved = raw_bytes / (scan_ms / 1e3) / 1e9
+    if snappy:
+        inf_ms = prof.get("k_pq_inflate", float("nan"))
+        if inf_ms > scan_ms:
+            scan_ms = inf_ms
+            achieved = (file_bytes + raw_bytes) / (inf_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "traffic": None, "kernel": "k_pq_scan", "kernel_ms": scan_ms,
+                "traffic": None, "kernel": ("k_pq_inflate" if snappy and scan_ms == prof.get("k_pq_inflate")
+                                            else "k_pq_scan"), "kernel_ms": scan_ms,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                 "step_GBps": file_bytes / (ms / 1e3) / 1e9, "step_frac": file_bytes / (ms / 1e3) / 1e9 / hbm_peak,
                 "kernels_ms": prof}
@@ -1160,12 +1172,14 @@ def run_parquet(args):
         dt = time.perf_counter() - tc
         cpu = {"value": n / dt, "unit": "rows/s", "cores": thr, "kind": "port",
                "sample": "first %d decoded rows, filter + GROUP BY (no page decode), %d threads" % (n, thr)}
-    line = {"metric": "fused Parquet decode+filter+GROUP BY rows/s (200M rows, 1M-row RGs)",
+    line = {"metric": "fused Parquet decode+filter+GROUP BY rows/s (200M rows, 1M-row RGs%s)" % (
+                ", SNAPPY" if snappy else ""),
             "value": rows / (ms / 1e3), "unit": "rows/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32+int64", "data": "synthetic",
-            "config": {"workload": "parquet-filter-groupby-%dM" % (rows // 1_000_000), "rows": rows,
-                       "file_bytes": file_bytes, "row_group_rows": 1_000_000, "dict": 65_536,
+            "config": {"workload": "parquet-filter-groupby-%dM%s" % (rows // 1_000_000, "-snappy" if snappy else ""),
+                       "rows": rows, "file_bytes": file_bytes, "page_bytes_uncompressed": raw_bytes,
+                       "codec": "SNAPPY" if snappy else "UNCOMPRESSED", "row_group_rows": 1_000_000, "dict": 65_536,
                        "predicate": "f < 100", "l2": "file %.1f GB > L2 129 MB (no flush needed)" % (file_bytes / 1e9),
                        "datagen_s": round(gen_s, 1)},
             "parity": "bit-exact vs oracle" if ok else "MISMATCH vs oracle",
@@ -1195,7 +1209,8 @@ def run_parquet_reference(args, key, f, v, rows):
             times.append(time.perf_counter() - t)
     per = statistics.mean(times)
     val = n / per
-    line = {"impl": "reference", "metric": "fused Parquet decode+filter+GROUP BY rows/s (200M rows, 1M-row RGs)",
+    line = {"impl": "reference", "metric": "fused Parquet decode+filter+GROUP BY rows/s (200M rows, 1M-row RGs%s)" % (
+                ", SNAPPY" if args.workload == "parquet200m_snappy" else ""),
             "value": val, "unit": "rows/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32+int64", "data": "synthetic",
@@ -1204,6 +1219,116 @@ def run_parquet_reference(args, key, f, v, rows):
                              "sample": "first %d decoded rows per step" % n},
             "e2e": {"value": val, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def dictsum_cpu(dictionary, idx, rg_rows, rows):
+    """The dictionary histogram on the host (the reference's
+    DecodeBigintColumnHistogram per row group, on already-decoded indices:
+    no RLE decode), over the first `rows` rows; returns (count, sum, s)."""
+    t = time.perf_counter()
+    cnt, tot = 0, 0.0
+    for r0 in range(0, rows, rg_rows):
+        h = np.bincount(idx[r0:min(rows, r0 + rg_rows)], minlength=len(dictionary))
+        cnt += int(h.sum())
+        tot += float(np.dot(h.astype(np.float64), dictionary.astype(np.float64)))
+    return cnt, tot, time.perf_counter() - t
+
+
+def run_dictsum(args):
+    """Ungrouped SUM/COUNT of an INT64 dictionary column through the
+    dictionary histogram (gb_pq_dict_sum): --pq-rows rows in 1M-row row
+    groups, 65,536 dictionary values, RLE/bit-packed indices (bit width 16,
+    runs of mean 4).  value = rows/s with the file resident in HBM (the
+    public call: index run tables, histogram, reduce, result to the host);
+    e2e = rows/s from the file in host memory (the column's bytes copied
+    inside the call)."""
+    ws, rank, local = dist_env()
+    from slothdb_gb300 import parquet as pq
+    if rank != 0:
+        return
+    rows = args.pq_rows
+    t0 = time.time()
+    data, dictionary, idx = pq.dict_int64_file(n_rows=rows, row_group_rows=1_000_000)
+    gen_s = time.time() - t0
+    thr = ref_threads("parquet")
+    n_cpu = min(args.cpu_sample, rows)
+    metric = "ungrouped SUM/COUNT rows/s of an INT64 dictionary column (dictionary histogram, 200M rows)"
+    if args.impl == "reference":
+        times = []
+        for i in range(args.warmup + args.steps):
+            _, _, dt = dictsum_cpu(dictionary, idx, 1_000_000, n_cpu)
+            if i >= args.warmup:
+                times.append(dt)
+        per = statistics.mean(times)
+        val = n_cpu / per
+        print(json.dumps({"impl": "reference", "metric": metric, "value": val, "unit": "rows/s", "n_gpus": 1,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": per * 1e3,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64",
+                          "data": "synthetic", "config": {"workload": "dictsum-%dM (bounded sample of %d rows)" % (
+                              rows // 1_000_000, n_cpu)},
+                          "cpu_baseline": {"value": val, "unit": "rows/s", "cores": 1, "kind": "port",
+                                           "sample": "first %d rows: per-row-group histogram of the decoded "
+                                                     "indices + dot product, 1 thread" % n_cpu},
+                          "e2e": {"value": val, "unit": "rows/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+              flush=True)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    from slothdb_gb300 import capi
+    capi.load(build_if_missing=True)
+    hbm_peak, peak_src = hbm_peak_gbs()
+    pf = capi.ParquetFile(data)
+    pf.upload()
+    exact = int((np.bincount(idx, minlength=len(dictionary)).astype(object) * dictionary.astype(object)).sum())
+    for _ in range(args.warmup):
+        got = pf.dict_sum(0, device=True)
+    parity = {"count_equal": got[0] == rows, "sum_rel_err": abs(got[1] - exact) / max(1.0, abs(exact)),
+              "tol_f64": REL_TOL_F64}
+    clocks = Clocks(local)
+    clocks.start()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        pf.dict_sum(0, device=True)
+    ms = (time.perf_counter() - t) / args.steps * 1e3
+    clk = clocks.stop()
+    # the dominant kernel on its own (CUDA events around one call's work:
+    # the histogram and its reduce dominate; the run walk is the rest)
+    st = torch.cuda.current_stream()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    pf.dict_sum(0, device=True, stream=st.cuda_stream)
+    e1.record(st)
+    torch.cuda.synchronize()
+    call_ms = e0.elapsed_time(e1)
+    te = time.perf_counter()
+    ne = max(1, args.steps // 2)
+    for _ in range(ne):
+        pf.dict_sum(0, device=False)
+    e2e_s = (time.perf_counter() - te) / ne
+    pf.close()
+    _, _, cpu_s = dictsum_cpu(dictionary, idx, 1_000_000, n_cpu)
+    file_bytes = len(data)
+    achieved = file_bytes / (call_ms / 1e3) / 1e9
+    print(json.dumps({"metric": metric, "value": rows / (ms / 1e3), "unit": "rows/s", "n_gpus": 1,
+                      "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+                      "scaling": "weak", "vs_baseline": None, "dtype": "int64", "data": "synthetic",
+                      "config": {"workload": "dictsum-%dM" % (rows // 1_000_000), "rows": rows,
+                                 "file_bytes": file_bytes, "row_group_rows": 1_000_000, "dict": len(dictionary),
+                                 "l2": "file %.1f GB > L2 129 MB (no flush needed)" % (file_bytes / 1e9),
+                                 "datagen_s": round(gen_s, 1)},
+                      "parity": parity,
+                      "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                                   "frac": achieved / hbm_peak, "traffic": None,
+                                   "kernel": "one gb_pq_dict_sum call (k_pq_runs + k_pq_dict_hist + k_pq_dict_reduce)",
+                                   "kernel_ms": call_ms, "peak_source": peak_src,
+                                   "note": "algorithmic bytes = the column chunks' bytes (index pages + dictionaries)"},
+                      "cpu_baseline": {"value": n_cpu / cpu_s, "unit": "rows/s", "cores": 1, "kind": "port",
+                                       "sample": "first %d rows: per-row-group histogram of the decoded indices + "
+                                                 "dot product, 1 thread" % n_cpu},
+                      "e2e": {"value": rows / e2e_s, "unit": "rows/s", "h2d_bytes_per_step": file_bytes,
+                              "d2h_bytes_per_step": 16, "ms_per_step": e2e_s * 1e3},
+                      "clocks": clk, "gpu_launches": 3 * args.steps}), flush=True)
 
 
 DISTINCT_GROUPS, DISTINCT_VALUES = 100_000, 2000
@@ -1383,8 +1508,11 @@ def main():
     if args.workload == "serve":
         run_serve(args)
         return
-    if args.workload == "parquet200m":
+    if args.workload in ("parquet200m", "parquet200m_snappy"):
         run_parquet(args)
+        return
+    if args.workload == "dictsum200m":
+        run_dictsum(args)
         return
     if args.impl == "reference":
         run_reference(args)

@@ -365,7 +365,8 @@ def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="sloth
     return b"".join(parts)
 
 
-def filter_groupby_file(n_rows=200_000_000, seed=2, n_dict=65_536, row_group_rows=1_000_000, page_rows=65_536):
+def filter_groupby_file(n_rows=200_000_000, seed=2, n_dict=65_536, row_group_rows=1_000_000, page_rows=65_536,
+                        codec=None):
     """The fused decode + filter + aggregate workload's file: key INT32
     dictionary-encoded (n_dict entries uniform in [0, 2^31), RLE/bit-packed
     indices at bit width 16, run lengths geometric with mean 4, run value
@@ -385,8 +386,27 @@ def filter_groupby_file(n_rows=200_000_000, seed=2, n_dict=65_536, row_group_row
     cols = [Column("key", T_INT32, dictionary=dictionary, indices=idx),
             Column("f", T_INT32, values=f, int16=True),
             Column("v", T_INT64, values=v)]
-    data = write(cols, row_group_rows=row_group_rows, page_rows=page_rows)
+    data = write(cols, row_group_rows=row_group_rows, page_rows=page_rows, codec=codec)
     return data, dictionary[idx], f, v
+
+
+def dict_int64_file(n_rows=200_000_000, seed=7, n_dict=65_536, row_group_rows=1_000_000, page_rows=65_536):
+    """One INT64 column, dictionary-encoded: n_dict entries uniform in
+    [-10^9, 10^9], indices in runs of geometric length (mean 4), run value
+    uniform (the shape of the fused workload's key, as an INT64 measure for
+    the ungrouped dictionary histogram).  Returns (file bytes, dictionary,
+    indices)."""
+    rng = np.random.default_rng(seed)
+    dictionary = rng.integers(-10**9, 10**9 + 1, n_dict, dtype=np.int64)
+    m = n_rows // 4 + 1024
+    lens = rng.geometric(0.25, m)
+    while lens.sum() < n_rows:
+        lens = np.concatenate([lens, rng.geometric(0.25, m)])
+    vals = rng.integers(0, n_dict, len(lens), dtype=np.int64)
+    idx = np.repeat(vals.astype(np.uint32), lens)[:n_rows]
+    data = write([Column("c", T_INT64, dictionary=dictionary, indices=idx)], row_group_rows=row_group_rows,
+                 page_rows=page_rows)
+    return data, dictionary, idx
 
 
 def varchar_groupby_file(n_rows=200_000, seed=6, n_dict=3000, row_group_rows=50_000, page_rows=8192):

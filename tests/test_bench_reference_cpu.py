@@ -16,6 +16,8 @@ CASES = {
     "zipf100m": ["--rows", "200000", "--cpu-sample", "200000"],
     "distinct100m": ["--rows", "200000", "--cpu-sample", "100000"],
     "parquet200m": ["--pq-rows", "300000", "--cpu-sample", "100000"],
+    "parquet200m_snappy": ["--pq-rows", "300000", "--cpu-sample", "100000"],
+    "dictsum200m": ["--pq-rows", "300000", "--cpu-sample", "100000"],
     "batch256": ["--tables", "1"],
     "serve": ["--duration", "0.05", "--scale", "0.001"],
 }
