@@ -1884,9 +1884,12 @@ struct InflateJob {
 // the bytes (an overlapping copy in rounds of at most `offset` bytes).  Every
 // length and offset is checked against the piece's bounds; a malformed block
 // sets ERR_CORRUPT and stops.
-__global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *file, const InflateJob *jobs, uint32_t n,
-                                                    uint8_t *img, uint32_t *lvl, Ctl *ctl) {
-    const int lane = threadIdx.x & 31;
+#define PQ_INF_WIN 4096  // bytes of a warp's shared window on its block's tag stream
+
+__global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *__restrict__ file, const InflateJob *jobs,
+                                                    uint32_t n, uint8_t *__restrict__ img, uint32_t *lvl, Ctl *ctl) {
+    __shared__ uint8_t s_win[4][PQ_INF_WIN];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (j >= n) return;  // the whole warp
     const InflateJob J = jobs[j];
@@ -1896,16 +1899,28 @@ __global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *file, const I
     if (J.mode == 0) {
         for (uint32_t i = lane; i < J.src_len; i += 32) dst[i] = src[i];
     } else {
+        // lane 0 parses the tags from a shared window of the block (refilled
+        // by the warp whenever a tag and its 4 extra bytes might not fit);
+        // literal bytes are copied straight from the file
+        uint8_t *w = s_win[warp];
+        uint32_t wbeg = 0, wend = 0;
+        auto refill = [&](uint32_t at) {
+            wbeg = at;
+            wend = min(J.src_len, at + (uint32_t)PQ_INF_WIN);
+            for (uint32_t k = lane; k < wend - wbeg; k += 32) w[k] = src[wbeg + k];
+            __syncwarp();
+        };
+        refill(0);
         uint32_t ip = 0, op = 0;
         if (lane == 0) {
             uint64_t ulen = 0;
             int sh = 0;
             for (;;) {
-                if (ip >= J.src_len || sh > 28) {
+                if (ip >= wend || sh > 28) {
                     bad = true;
                     break;
                 }
-                const uint8_t b = src[ip++];
+                const uint8_t b = w[ip++ - wbeg];
                 ulen |= (uint64_t)(b & 0x7f) << sh;
                 if (!(b & 0x80)) break;
                 sh += 7;
@@ -1915,12 +1930,13 @@ __global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *file, const I
         bad = __shfl_sync(FULL, (int)bad, 0) != 0;
         ip = __shfl_sync(FULL, ip, 0);
         while (!bad && op < J.dst_len) {
+            if (ip + 5 > wend && wend < J.src_len) refill(ip);
             uint32_t kind = 0, len = 0, from = 0;  // kind 0: literal at src[from]; 1: copy of dst[from]
             if (lane == 0) {
                 if (ip >= J.src_len) {
                     bad = true;
                 } else {
-                    const uint32_t tag = src[ip++];
+                    const uint32_t tag = w[ip++ - wbeg];
                     const uint32_t t = tag & 3u;
                     uint32_t off = 0;
                     if (t == 0) {
@@ -1929,7 +1945,7 @@ __global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *file, const I
                             const uint32_t nb = l - 59;
                             if (ip + nb > J.src_len) bad = true;
                             l = 0;
-                            for (uint32_t b = 0; b < nb && !bad; b++) l |= (uint32_t)src[ip + b] << (8 * b);
+                            for (uint32_t b = 0; b < nb && !bad; b++) l |= (uint32_t)w[ip + b - wbeg] << (8 * b);
                             ip += nb;
                         }
                         len = l + 1;
@@ -1943,7 +1959,7 @@ __global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *file, const I
                         if (ip + nb > J.src_len) {
                             bad = true;
                         } else {
-                            for (uint32_t b = 0; b < nb; b++) off |= (uint32_t)src[ip + b] << (8 * b);
+                            for (uint32_t b = 0; b < nb; b++) off |= (uint32_t)w[ip + b - wbeg] << (8 * b);
                             if (t == 1) off = ((tag >> 5) << 8) | (off & 0xffu);
                             ip += nb;
                         }
@@ -1960,7 +1976,15 @@ __global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *file, const I
             from = __shfl_sync(FULL, from, 0);
             ip = __shfl_sync(FULL, ip, 0);
             if (kind == 0) {
-                for (uint32_t i = lane; i < len; i += 32) dst[op + i] = src[from + i];
+                // 8 bytes per lane per round: their loads are issued together
+                for (uint32_t i0 = (uint32_t)lane * 8; i0 < len; i0 += 256) {
+                    uint8_t b[8];
+#pragma unroll
+                    for (int k = 0; k < 8; k++) b[k] = i0 + k < len ? src[from + i0 + k] : 0;
+#pragma unroll
+                    for (int k = 0; k < 8; k++)
+                        if (i0 + k < len) dst[op + i0 + k] = b[k];
+                }
             } else {
                 const uint32_t step = min(op - from, 32u);  // bytes of one round: all written before it
                 for (uint32_t b0 = 0; b0 < len; b0 += step) {
