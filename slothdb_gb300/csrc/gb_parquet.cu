@@ -1884,11 +1884,13 @@ struct InflateJob {
 // the bytes (an overlapping copy in rounds of at most `offset` bytes).  Every
 // length and offset is checked against the piece's bounds; a malformed block
 // sets ERR_CORRUPT and stops.
-#define PQ_INF_WIN 4096  // bytes of a warp's shared window on its block's tag stream
+#define PQ_INF_WIN 4096   // bytes of a warp's shared window on its block's tag stream
+#define PQ_INF_RING 1024  // the warp's last output bytes, kept in shared memory for short-offset copies
 
 __global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *__restrict__ file, const InflateJob *jobs,
                                                     uint32_t n, uint8_t *__restrict__ img, uint32_t *lvl, Ctl *ctl) {
     __shared__ uint8_t s_win[4][PQ_INF_WIN];
+    __shared__ uint8_t s_ring[4][PQ_INF_RING];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (j >= n) return;  // the whole warp
@@ -1903,6 +1905,7 @@ __global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *__restrict__ 
         // by the warp whenever a tag and its 4 extra bytes might not fit);
         // literal bytes are copied straight from the file
         uint8_t *w = s_win[warp];
+        uint8_t *ring = s_ring[warp];  // output byte o at ring[o % PQ_INF_RING]
         uint32_t wbeg = 0, wend = 0;
         auto refill = [&](uint32_t at) {
             wbeg = at;
@@ -1983,14 +1986,24 @@ __global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *__restrict__ 
                     for (int k = 0; k < 8; k++) b[k] = i0 + k < len ? src[from + i0 + k] : 0;
 #pragma unroll
                     for (int k = 0; k < 8; k++)
-                        if (i0 + k < len) dst[op + i0 + k] = b[k];
+                        if (i0 + k < len) {
+                            dst[op + i0 + k] = b[k];
+                            ring[(op + i0 + k) % PQ_INF_RING] = b[k];
+                        }
                 }
             } else {
-                const uint32_t step = min(op - from, 32u);  // bytes of one round: all written before it
-                for (uint32_t b0 = 0; b0 < len; b0 += step) {
-                    const uint32_t i = b0 + (uint32_t)lane;
-                    if ((uint32_t)lane < step && i < len) dst[op + i] = dst[from + i];
-                    __syncwarp();
+                // output byte op + i repeats byte from + (i mod off), which is
+                // older than op: a short offset reads the shared ring (no slot
+                // it reads is one this element writes while off + len fits
+                // the ring), a long one the image (written before this
+                // element; no overlap, as len <= 64 < off)
+                const uint32_t off = op - from;
+                const bool in_ring = off + len <= PQ_INF_RING;
+                for (uint32_t i = lane; i < len; i += 32) {
+                    const uint32_t o = from + (i % off);
+                    const uint8_t b = in_ring ? ring[o % PQ_INF_RING] : dst[o];
+                    dst[op + i] = b;
+                    ring[(op + i) % PQ_INF_RING] = b;
                 }
             }
             op += len;
