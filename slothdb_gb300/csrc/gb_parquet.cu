@@ -1979,11 +1979,16 @@ __global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *__restrict__ 
             from = __shfl_sync(FULL, from, 0);
             ip = __shfl_sync(FULL, ip, 0);
             if (kind == 0) {
-                // 8 bytes per lane per round: their loads are issued together
+                // literal bytes inside the shared window are read there (no
+                // global round trip per element); the rest 8 bytes per lane
+                // per round, their loads issued together
                 for (uint32_t i0 = (uint32_t)lane * 8; i0 < len; i0 += 256) {
                     uint8_t b[8];
 #pragma unroll
-                    for (int k = 0; k < 8; k++) b[k] = i0 + k < len ? src[from + i0 + k] : 0;
+                    for (int k = 0; k < 8; k++) {
+                        const uint32_t q = from + i0 + k;
+                        b[k] = i0 + k < len ? (q < wend ? w[q - wbeg] : src[q]) : 0;
+                    }
 #pragma unroll
                     for (int k = 0; k < 8; k++)
                         if (i0 + k < len) {
