@@ -1880,139 +1880,149 @@ struct InflateJob {
 // uncompressed length, then elements whose tag's low 2 bits say literal (00:
 // length in the tag or in 1-4 following bytes), or copy with a 1-, 2- or
 // 4-byte offset (01/10/11) of an earlier output position, possibly
-// overlapping the bytes it writes.  Lane 0 parses the tags; the warp moves
-// the bytes (an overlapping copy in rounds of at most `offset` bytes).  Every
-// length and offset is checked against the piece's bounds; a malformed block
-// sets ERR_CORRUPT and stops.
-#define PQ_INF_WIN 4096   // bytes of a warp's shared window on its block's tag stream
-#define PQ_INF_RING 1024  // the warp's last output bytes, kept in shared memory for short-offset copies
+// overlapping the bytes it writes.
+//
+// The warp decodes a round of elements at a time.  Lane L reads the 8
+// compressed bytes at ip + L (one aligned word per lane, redistributed by
+// shuffles) and decodes the element a tag there would be; the chain of real
+// tags from ip (each start plus its element's compressed size) is walked with
+// shuffles over the lanes' sizes, up to the first start at or past ip + 32.
+// An exclusive scan of the starts' lengths places each element in the output.
+// Each output byte of the round gets its source in a per-warp shared map: a
+// compressed position (literal) or an earlier output position (copy; an
+// overlapping copy repeats its first `offset` bytes).  A source inside the
+// round is followed through the map to a byte written before the round or a
+// literal byte, so that all bytes of a round are independent and the warp
+// writes them with one load and one store each.  A literal longer than 64
+// bytes (the last element of its round) is copied by the whole warp after
+// the round.  Every length and offset is checked against the piece's bounds;
+// a malformed block sets ERR_CORRUPT and stops.
+#define PQ_INF_MAP 1024   // output bytes of one round: at most 16 elements of at most 64 bytes
+#define PQ_INF_LONG 64    // literals longer than this are copied by the warp
+#define PQ_INF_LIT 0x80000000u
 
-__global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *__restrict__ file, const InflateJob *jobs,
-                                                    uint32_t n, uint8_t *__restrict__ img, uint32_t *lvl, Ctl *ctl) {
-    __shared__ uint8_t s_win[4][PQ_INF_WIN];
-    __shared__ uint8_t s_ring[4][PQ_INF_RING];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    if (j >= n) return;  // the whole warp
-    const InflateJob J = jobs[j];
+__device__ __forceinline__ void pq_inflate_piece(const uint8_t *__restrict__ file, const InflateJob J, uint8_t *img,
+                                                 uint32_t *lvl, Ctl *ctl, uint32_t *map, const int lane) {
     const uint8_t *src = file + J.src;
     uint8_t *dst = img + J.dst;
     bool bad = false;
     if (J.mode == 0) {
         for (uint32_t i = lane; i < J.src_len; i += 32) dst[i] = src[i];
     } else {
-        // lane 0 parses the tags from a shared window of the block (refilled
-        // by the warp whenever a tag and its 4 extra bytes might not fit);
-        // literal bytes are copied straight from the file
-        uint8_t *w = s_win[warp];
-        uint8_t *ring = s_ring[warp];  // output byte o at ring[o % PQ_INF_RING]
-        uint32_t wbeg = 0, wend = 0;
-        auto refill = [&](uint32_t at) {
-            wbeg = at;
-            wend = min(J.src_len, at + (uint32_t)PQ_INF_WIN);
-            for (uint32_t k = lane; k < wend - wbeg; k += 32) w[k] = src[wbeg + k];
-            __syncwarp();
-        };
-        refill(0);
+        const uint32_t slen = J.src_len, dlen = J.dst_len;
         uint32_t ip = 0, op = 0;
-        if (lane == 0) {
+        if (lane == 0) {  // the preamble: the uncompressed length
             uint64_t ulen = 0;
             int sh = 0;
             for (;;) {
-                if (ip >= wend || sh > 28) {
+                if (ip >= slen || sh > 28) {
                     bad = true;
                     break;
                 }
-                const uint8_t b = w[ip++ - wbeg];
+                const uint8_t b = src[ip++];
                 ulen |= (uint64_t)(b & 0x7f) << sh;
                 if (!(b & 0x80)) break;
                 sh += 7;
             }
-            if (ulen != J.dst_len) bad = true;
+            if (ulen != dlen) bad = true;
         }
         bad = __shfl_sync(FULL, (int)bad, 0) != 0;
         ip = __shfl_sync(FULL, ip, 0);
-        while (!bad && op < J.dst_len) {
-            if (ip + 5 > wend && wend < J.src_len) refill(ip);
-            uint32_t kind = 0, len = 0, from = 0;  // kind 0: literal at src[from]; 1: copy of dst[from]
-            if (lane == 0) {
-                if (ip >= J.src_len) {
-                    bad = true;
+        while (!bad && op < dlen) {
+            if (ip >= slen) {
+                bad = true;
+                break;
+            }
+            // bytes [ip + lane, ip + lane + 8): lanes 0..10 load the aligned words over
+            // [ip, ip + 40) and the warp redistributes them
+            const uint8_t *blk = (const uint8_t *)((uintptr_t)(src + ip) & ~(uintptr_t)3);
+            uint32_t word = 0;
+            if (lane < 11) {
+                const uint8_t *wp = blk + 4 * lane;
+                if (blk >= src && blk + 44 <= src + slen) {
+                    word = __ldg((const uint32_t *)wp);
                 } else {
-                    const uint32_t tag = w[ip++ - wbeg];
-                    const uint32_t t = tag & 3u;
-                    uint32_t off = 0;
-                    if (t == 0) {
-                        uint32_t l = tag >> 2;
-                        if (l >= 60) {
-                            const uint32_t nb = l - 59;
-                            if (ip + nb > J.src_len) bad = true;
-                            l = 0;
-                            for (uint32_t b = 0; b < nb && !bad; b++) l |= (uint32_t)w[ip + b - wbeg] << (8 * b);
-                            ip += nb;
-                        }
-                        len = l + 1;
-                        if (!bad && (len > J.src_len - ip || len == 0)) bad = true;
-                        from = ip;
-                        ip += len;
-                    } else {
-                        kind = 1;
-                        const uint32_t nb = t == 1 ? 1 : (t == 2 ? 2 : 4);
-                        len = t == 1 ? 4 + ((tag >> 2) & 7u) : (tag >> 2) + 1;
-                        if (ip + nb > J.src_len) {
-                            bad = true;
-                        } else {
-                            for (uint32_t b = 0; b < nb; b++) off |= (uint32_t)w[ip + b - wbeg] << (8 * b);
-                            if (t == 1) off = ((tag >> 5) << 8) | (off & 0xffu);
-                            ip += nb;
-                        }
-                        if (!bad && (off == 0 || off > op)) bad = true;
-                        from = op - off;
-                    }
-                    if (!bad && len > J.dst_len - op) bad = true;
+                    for (int k = 0; k < 4; k++)
+                        if (wp + k >= src && wp + k < src + slen) word |= (uint32_t)__ldg(wp + k) << (8 * k);
                 }
             }
-            bad = __shfl_sync(FULL, (int)bad, 0) != 0;
-            if (bad) break;
-            kind = __shfl_sync(FULL, kind, 0);
-            len = __shfl_sync(FULL, len, 0);
-            from = __shfl_sync(FULL, from, 0);
-            ip = __shfl_sync(FULL, ip, 0);
-            if (kind == 0) {
-                // literal bytes inside the shared window are read there (no
-                // global round trip per element); the rest 8 bytes per lane
-                // per round, their loads issued together
-                for (uint32_t i0 = (uint32_t)lane * 8; i0 < len; i0 += 256) {
-                    uint8_t b[8];
-#pragma unroll
-                    for (int k = 0; k < 8; k++) {
-                        const uint32_t q = from + i0 + k;
-                        b[k] = i0 + k < len ? (q < wend ? w[q - wbeg] : src[q]) : 0;
-                    }
-#pragma unroll
-                    for (int k = 0; k < 8; k++)
-                        if (i0 + k < len) {
-                            dst[op + i0 + k] = b[k];
-                            ring[(op + i0 + k) % PQ_INF_RING] = b[k];
-                        }
-                }
-            } else {
-                // output byte op + i repeats byte from + (i mod off), which is
-                // older than op: a short offset reads the shared ring (no slot
-                // it reads is one this element writes while off + len fits
-                // the ring), a long one the image (written before this
-                // element; no overlap, as len <= 64 < off)
-                const uint32_t off = op - from;
-                const bool in_ring = off + len <= PQ_INF_RING;
-                for (uint32_t i = lane; i < len; i += 32) {
-                    const uint32_t o = from + (i % off);
-                    const uint8_t b = in_ring ? ring[o % PQ_INF_RING] : dst[o];
-                    dst[op + i] = b;
-                    ring[(op + i) % PQ_INF_RING] = b;
+            const uint32_t sh0 = (uint32_t)((uintptr_t)(src + ip) & 3) + (uint32_t)lane;
+            const uint32_t w0 = __shfl_sync(FULL, word, sh0 >> 2);
+            const uint32_t w1 = __shfl_sync(FULL, word, (sh0 >> 2) + 1);
+            const uint32_t w2 = __shfl_sync(FULL, word, (sh0 >> 2) + 2);
+            const uint32_t lo = __funnelshift_r(w0, w1, 8 * (sh0 & 3)), hi = __funnelshift_r(w1, w2, 8 * (sh0 & 3));
+            // the element a tag at ip + lane would be (selects, no branches)
+            const uint32_t tag = lo & 0xffu, t = tag & 3u, l6 = tag >> 2;
+            const uint32_t rest = (lo >> 8) | (hi << 24);  // bytes 1..4 after the tag
+            const uint32_t nb = l6 >= 60 ? l6 - 59 : 0;     // a literal's length bytes
+            const uint32_t lraw = nb ? rest & (0xffffffffu >> (32 - 8 * nb)) : l6;
+            const uint32_t hdr = t == 0 ? 1 + nb : (t == 1 ? 2 : (t == 2 ? 3 : 5));
+            const uint32_t len = t == 0 ? lraw + 1 : (t == 1 ? 4 + (l6 & 7u) : l6 + 1);  // 0 after a wrap
+            const uint32_t off = t == 1 ? ((tag >> 5) << 8) | (rest & 0xffu) : (t == 2 ? rest & 0xffffu : rest);
+            const uint32_t cs = t != 0 ? hdr : (lraw >= 0x7fff0000u ? 0x7fffffffu : hdr + lraw + 1);
+            // the chain of starts from ip
+            const uint32_t avail = min(32u, slen - ip);
+            uint32_t pos = 0, mask = 0;
+            while (pos < avail) {
+                mask |= 1u << pos;
+                pos += __shfl_sync(FULL, cs, pos);
+            }
+            const bool start = (mask >> lane) & 1u;
+            // lengths clamped in the scan (16 starts of at most 2^26 cannot wrap); the one
+            // element that may be longer, a long literal, is the round's last start
+            uint32_t mylen = start ? min(len, 1u << 26) : 0, incl = mylen;
+            for (int d = 1; d < 32; d <<= 1) {
+                const uint32_t y = __shfl_up_sync(FULL, incl, d);
+                if (lane >= d) incl += y;
+            }
+            const uint32_t excl = incl - mylen;  // round-relative output position
+            uint32_t total = __shfl_sync(FULL, incl, 31);
+            const uint32_t p = ip + (uint32_t)lane;  // compressed position of this lane's tag
+            const uint64_t o = (uint64_t)op + excl;
+            const bool live = start && o < dlen;  // elements after the last output byte are ignored
+            const bool mybad = live && ((uint64_t)p + cs > slen || len == 0 || o + len > dlen ||
+                                        (t != 0 && (off == 0 || off > o)));
+            if (__any_sync(FULL, mybad)) {
+                bad = true;
+                break;
+            }
+            // outputs past dlen (trailing elements) and the long literal are not mapped
+            if (total > dlen - op) total = dlen - op;
+            const uint32_t lmask = __ballot_sync(FULL, live && t == 0 && len > PQ_INF_LONG);
+            uint32_t mapped = total, lit_at = 0, lit_len = 0, lit_src = 0;
+            if (lmask) {
+                const int ll = __ffs(lmask) - 1;
+                mapped = __shfl_sync(FULL, excl, ll);
+                lit_len = __shfl_sync(FULL, len, ll);
+                lit_src = __shfl_sync(FULL, p + hdr, ll);
+                lit_at = op + mapped;
+                total = mapped + lit_len;
+            }
+            if (mapped > PQ_INF_MAP) {  // unreachable: 16 starts of at most 64 bytes
+                bad = true;
+                break;
+            }
+            if (start && excl < mapped) {
+                // a literal's byte b comes from q + b; a copy's from o - off + (b mod off)
+                const uint32_t base = t == 0 ? PQ_INF_LIT | (p + hdr) : (uint32_t)o - off;
+                const uint32_t per = t == 0 ? 0xffffffffu : off;
+                for (uint32_t b = 0, r = 0; b < len; b++) {
+                    map[excl + b] = base + r;
+                    r = r + 1 == per ? 0 : r + 1;
                 }
             }
-            op += len;
             __syncwarp();
+            for (uint32_t k = lane; k < mapped; k += 32) {
+                uint32_t s = map[k];
+                while (!(s & PQ_INF_LIT) && s >= op) s = map[s - op];
+                dst[op + k] = (s & PQ_INF_LIT) ? __ldg(src + (s & ~PQ_INF_LIT)) : dst[s];
+            }
+            if (lit_len) {
+                for (uint32_t b = lane; b < lit_len; b += 32) dst[lit_at + b] = __ldg(src + lit_src + b);
+            }
+            __syncwarp();
+            op += total;
+            ip += pos;
         }
     }
     if (bad && lane == 0) atomicOr(&ctl->err, (u32)ERR_CORRUPT);
@@ -2022,6 +2032,23 @@ __global__ void __launch_bounds__(128) k_pq_inflate(const uint8_t *__restrict__ 
         if (!bad && J.dst_len >= 4)
             l4 = (uint32_t)dst[0] | ((uint32_t)dst[1] << 8) | ((uint32_t)dst[2] << 16) | ((uint32_t)dst[3] << 24);
         lvl[J.lvl_slot] = l4;
+    }
+}
+
+// Each warp claims pieces from a counter (the word after the last job, zero
+// at launch) until none is left; the host lists the pieces longest first, so
+// that the long pages start early and no warp idles beside a long one.
+__global__ void __launch_bounds__(256) k_pq_inflate(const uint8_t *__restrict__ file, InflateJob *jobs,
+                                                    uint32_t n, uint8_t *img, uint32_t *lvl, Ctl *ctl) {
+    __shared__ uint32_t s_map[8][PQ_INF_MAP];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t *next = (uint32_t *)(jobs + n);
+    for (;;) {
+        uint32_t j = 0;
+        if (lane == 0) j = atomicAdd(next, 1u);
+        j = __shfl_sync(FULL, j, 0);
+        if (j >= n) return;  // the whole warp
+        pq_inflate_piece(file, jobs[j], img, lvl, ctl, s_map[warp], lane);
     }
 }
 
@@ -2085,16 +2112,23 @@ static gb_status pq_inflate_batch(gb_agg *h, const gb_pq_file *f, PqScratch *S, 
             }
         }
     }
+    // longest first (a stored piece costs about a sixteenth of an inflated
+    // one per byte), then a zero word: the kernel's claim counter
+    std::stable_sort(jobs.begin(), jobs.end(), [](const InflateJob &a, const InflateJob &b) {
+        return (a.mode ? (uint64_t)a.dst_len * 16 : a.dst_len) > (b.mode ? (uint64_t)b.dst_len * 16 : b.dst_len);
+    });
+    const size_t n_jobs = jobs.size();
+    jobs.push_back({0, 0, 0, 0, 0, 0});
     gb_status s;
     if ((s = grow(S->img, S->img_cap, pos + 64)) || (s = grow(S->ijobs, S->ijobs_cap, jobs.size() * sizeof(InflateJob) + 16)) ||
         (s = grow(S->ilvl, S->ilvl_cap, pending.size() * 4 + 16)))
         return s;
-    if (!jobs.empty()) {
+    if (n_jobs) {
         GB_CUDA(cudaMemcpyAsync(S->ijobs, jobs.data(), jobs.size() * sizeof(InflateJob), cudaMemcpyHostToDevice, st));
         gb_prof_mark *pm = gb_agg_prof_begin(h, "k_pq_inflate", st);
-        k_pq_inflate<<<(unsigned)((jobs.size() + 3) / 4), 128, 0, st>>>(dfile, (const InflateJob *)S->ijobs,
-                                                                       (uint32_t)jobs.size(), (uint8_t *)S->img,
-                                                                       (uint32_t *)S->ilvl, dctl);
+        const unsigned grid = (unsigned)std::min<size_t>((n_jobs + 7) / 8, (size_t)sm_count() * 6);
+        k_pq_inflate<<<grid, 256, 0, st>>>(dfile, (InflateJob *)S->ijobs, (uint32_t)n_jobs, (uint8_t *)S->img,
+                                           (uint32_t *)S->ilvl, dctl);
         gb_agg_prof_end(h, pm, st);
         GB_CUDA(cudaGetLastError());
         gb_agg_count_launch(h, 1);

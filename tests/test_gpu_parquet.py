@@ -238,6 +238,37 @@ def test_snappy_pages_from_the_project_writer(device):
                        batches=batches), orc)
 
 
+def test_snappy_byte_patterns():
+    """SNAPPY pages whose blocks exercise every element shape of the
+    inflate: incompressible values (literals longer than a round, copied by
+    the whole warp), constant and short-period runs (overlapping copies of
+    up to 64 bytes, sources inside the same round), small values in runs
+    (short literals followed by copies of them), pages whose block ends
+    inside a round; the decoded values against the oracle bit for bit
+    (magnitudes below 2^44: every group's SUM stays below 2^53, where the
+    reference's double accumulator is exact)."""
+    rng = np.random.default_rng(31)
+    seg = 24_576
+    v = np.concatenate([
+        rng.integers(-2**44, 2**44, seg, dtype=np.int64),                           # incompressible
+        np.zeros(seg, dtype=np.int64),                                               # one long run
+        np.tile(np.array([7, -3, 2**40], dtype=np.int64), seg // 3),                 # period 24 bytes
+        np.repeat(rng.integers(0, 256, seg // 4, dtype=np.int64), 4),                # short runs
+        rng.integers(0, 4, seg, dtype=np.int64),                                     # tiny alphabet
+        np.repeat(rng.integers(-2**44, 2**44, seg // 64, dtype=np.int64), 64),       # long runs of random words
+        rng.integers(-1000, 1000, 5_000, dtype=np.int64),                            # a ragged tail
+    ])
+    n = len(v)
+    key = (np.arange(n) % 97).astype(np.int32)
+    cols = [pq.Column("key", pq.T_INT32, values=key), pq.Column("v", pq.T_INT64, values=v)]
+    for page_rows in (8192, 3000):
+        data = pq.write(cols, row_group_rows=40_000, page_rows=page_rows, codec="snappy")
+        types = [INTEGER, BIGINT]
+        aggs = [("sum", 1), ("min", 1), ("max", 1), ("count_star", -1)]
+        orc = oracle.run_query(types, [0], aggs, [key, v])
+        compare(run_pq(data, types, [0, 1], [0], aggs, est_groups=97, device=True), orc)
+
+
 def test_corrupt_snappy_block_is_reported():
     """A page whose Snappy block is damaged (a copy reaching before the
     start of the output) is reported as a corrupt file, not decoded."""
