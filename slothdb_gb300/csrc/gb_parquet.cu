@@ -201,6 +201,10 @@ struct gb_pq_file {
     bool idx_ready = false;
     void *idx_pages = nullptr, *idx_runs = nullptr, *idx_page_runs = nullptr;
     std::vector<uint32_t> idx_col_pages;  // [(rg * n_cols + col) * 2] = {begin, end}
+    // device buffers of gb_pq_dict_sum, kept (grow-only) for the next call
+    std::mutex ds_mu;
+    void *ds_buf[10] = {};
+    size_t ds_cap[10] = {};
 };
 
 static gb_status pq_corrupt(const char *what) {
@@ -1392,8 +1396,13 @@ __device__ __forceinline__ void block_add_i128(__int128 x, u64 cnt, u64 *out3) {
 // One CTA per page of the column.  Dictionary pages: every index entry
 // below the page's value count bumps its row group's histogram (an RLE run
 // once, by its length; indices past the dictionary are skipped, as the
-// reference does).  PLAIN pages: their values and count go to part[3 * page].
-// A page with NULLs sets *nulls (the reference then takes the fused path).
+// reference does).  Each warp walks the runs over its slice of the page's
+// entries: an RLE run is one atomic; a bit-packed run is unpacked 32 entries
+// at a time, and lanes holding the same index as their left neighbour hand
+// their count to the first lane of the group, so that a run of equal indices
+// costs one atomic.  PLAIN pages: their values and count go to
+// part[3 * page].  A page with NULLs sets *nulls (the reference then takes
+// the fused path).
 __global__ void k_pq_dict_hist(const uint8_t *file, const DPage *pages, const DRun *runs, const uint32_t *page_runs,
                                const uint32_t *page_group, const DHGroup *groups, uint32_t *hist, u64 *part,
                                uint32_t *nulls) {
@@ -1412,16 +1421,37 @@ __global__ void k_pq_dict_hist(const uint8_t *file, const DPage *pages, const DR
         const uint32_t nr = page_runs[PQ_PR * p], bw = page_runs[PQ_PR * p + 1];
         const DRun *rr = runs + pg.run_base;
         const DHGroup G = groups[page_group[p]];
-        for (uint32_t i = threadIdx.x; i < total; i += blockDim.x) {
-            if (nr == 0) break;
-            const DRun rn = rr[run_search(rr, 0, nr, i)];
-            if (i < rn.start || i >= rn.start + rn.cnt) continue;  // past the decoded entries
-            if (rn.off == 0xffffffffu) {
-                if (i == rn.start && rn.val < G.dict_n)
-                    atomicAdd(&hist[G.hist_base + rn.val], min(rn.cnt, total - rn.start));
-            } else {
-                const uint32_t idx = load_bits(file + pg.off + rn.off, (u64)(i - rn.start) * bw, bw);
-                if (idx < G.dict_n) atomicAdd(&hist[G.hist_base + idx], 1u);
+        uint32_t *h = hist + G.hist_base;
+        const uint32_t lane = threadIdx.x & 31, nw = blockDim.x >> 5, w = threadIdx.x >> 5;
+        const uint32_t per = (total + nw - 1) / nw;
+        const uint32_t a = min(total, w * per), b = min(total, a + per);  // this warp's entries
+        if (nr > 0 && a < b) {
+            for (uint32_t r = run_search(rr, 0, nr, a); r < nr; r++) {
+                const DRun rn = rr[r];
+                if (rn.start >= b) break;
+                const uint32_t s0 = max(rn.start, a);
+                const uint32_t s1 = (uint32_t)min((u64)rn.start + rn.cnt, (u64)b);
+                if (s0 >= s1) continue;  // entries past the decoded ones
+                if (rn.off == 0xffffffffu) {
+                    if (lane == 0 && rn.val < G.dict_n) atomicAdd(&h[rn.val], s1 - s0);
+                    continue;
+                }
+                const uint8_t *payload = file + pg.off + rn.off;
+                for (uint32_t i0 = s0; i0 < s1; i0 += 32) {
+                    const uint32_t i = i0 + lane;
+                    uint32_t key = 0xffffffffu;  // no entry, or an index past the dictionary
+                    if (i < s1) {
+                        const uint32_t idx = load_bits(payload, (u64)(i - rn.start) * bw, bw);
+                        if (idx < G.dict_n) key = idx;
+                    }
+                    const uint32_t left = __shfl_up_sync(FULL, key, 1);
+                    const uint32_t heads = __ballot_sync(FULL, lane == 0 || key != left);
+                    if (key != 0xffffffffu && (heads >> lane & 1u)) {
+                        const uint32_t above = lane == 31 ? 0u : heads >> (lane + 1);
+                        const uint32_t n = above ? (uint32_t)__ffs(above) : 32u - lane;
+                        atomicAdd(&h[key], n);
+                    }
+                }
             }
         }
         if (threadIdx.x == 0) out3[0] = out3[1] = out3[2] = 0;
@@ -1431,6 +1461,8 @@ __global__ void k_pq_dict_hist(const uint8_t *file, const DPage *pages, const DR
         block_add_i128(acc, threadIdx.x == 0 ? total : 0, out3);
     }
 }
+
+static gb_status grow(void *&p, size_t &cap, size_t need);
 
 // One CTA per row group: sum_idx count[idx] * dict[idx] and sum_idx count[idx].
 __global__ void k_pq_dict_reduce(const uint8_t *file, const DHGroup *groups, const uint32_t *hist, u64 *part) {
@@ -1539,6 +1571,9 @@ gb_status gb_pq_dict_sum(gb_pq_file *f, uint32_t col, uint32_t rg_begin, uint32_
     }
     cudaStream_t st = (cudaStream_t)stream;
     gb_status s = GB_OK;
+    std::lock_guard<std::mutex> lk(f->ds_mu);
+    void **B = f->ds_buf;
+    size_t *C = f->ds_cap;
     // the column's bytes: the resident file, or its row groups' byte range
     const uint8_t *dfile = nullptr;
     uint64_t base = 0, lo = ~0ull, hi = 0;
@@ -1554,7 +1589,8 @@ gb_status gb_pq_dict_sum(gb_pq_file *f, uint32_t col, uint32_t rg_begin, uint32_
             lo = std::min(lo, f->chunks[g][col].start);
             hi = std::max(hi, f->chunks[g][col].start + f->chunks[g][col].size);
         }
-        GB_CUDA(cudaMalloc(&copy, hi - lo + 64));
+        if ((s = grow(B[9], C[9], hi - lo + 64))) return s;
+        copy = B[9];
         dfile = (const uint8_t *)copy;
         base = lo;
     }
@@ -1568,11 +1604,7 @@ gb_status gb_pq_dict_sum(gb_pq_file *f, uint32_t col, uint32_t rg_begin, uint32_
     uint64_t hist_n = 0;
     void *d_pages = nullptr, *d_runs = nullptr, *d_page_runs = nullptr, *d_jobs = nullptr, *d_pg = nullptr,
          *d_groups = nullptr, *d_hist = nullptr, *d_part = nullptr, *d_ctl = nullptr;
-    auto done = [&](gb_status r) {
-        for (void *q : {copy, d_pages, d_runs, d_page_runs, d_jobs, d_pg, d_groups, d_hist, d_part, d_ctl})
-            if (q) cudaFree(q);
-        return r;
-    };
+    auto done = [&](gb_status r) { return r; };
     if (copy && cudaMemcpyAsync(copy, f->host + lo, hi - lo, cudaMemcpyHostToDevice, st) != cudaSuccess)
         return done(cuda_fail(cudaGetLastError(), "cudaMemcpyAsync"));
     if ((s = pq_page_table(f, PqView{&f->chunks, &f->pages}, rg_begin, rg_end, cols, 1, base, nullptr, pages, jobs,
@@ -1588,12 +1620,14 @@ gb_status gb_pq_dict_sum(gb_pq_file *f, uint32_t col, uint32_t rg_begin, uint32_
     }
     const size_t np = pages.size(), ng = groups.size();
     cudaError_t e;
-    if ((e = cudaMalloc(&d_pages, np * sizeof(DPage) + 16)) || (e = cudaMalloc(&d_runs, (size_t)run_total * sizeof(DRun) + 16)) ||
-        (e = cudaMalloc(&d_page_runs, np * PQ_PR * 4 + 16)) || (e = cudaMalloc(&d_jobs, jobs.size() * sizeof(RunJob) + 16)) ||
-        (e = cudaMalloc(&d_pg, np * 4 + 16)) || (e = cudaMalloc(&d_groups, ng * sizeof(DHGroup) + 16)) ||
-        (e = cudaMalloc(&d_hist, hist_n * 4 + 16)) || (e = cudaMalloc(&d_part, (np + ng) * 24 + 16)) ||
-        (e = cudaMalloc(&d_ctl, sizeof(Ctl))))
-        return done(cuda_fail(e, "cudaMalloc (dictionary histogram)"));
+    if ((s = grow(B[0], C[0], np * sizeof(DPage) + 16)) || (s = grow(B[1], C[1], (size_t)run_total * sizeof(DRun) + 16)) ||
+        (s = grow(B[2], C[2], np * PQ_PR * 4 + 16)) || (s = grow(B[3], C[3], jobs.size() * sizeof(RunJob) + 16)) ||
+        (s = grow(B[4], C[4], np * 4 + 16)) || (s = grow(B[5], C[5], ng * sizeof(DHGroup) + 16)) ||
+        (s = grow(B[6], C[6], hist_n * 4 + 16)) || (s = grow(B[7], C[7], (np + ng) * 24 + 16)) ||
+        (s = grow(B[8], C[8], sizeof(Ctl))))
+        return s;
+    d_pages = B[0], d_runs = B[1], d_page_runs = B[2], d_jobs = B[3], d_pg = B[4], d_groups = B[5], d_hist = B[6],
+    d_part = B[7], d_ctl = B[8];
     if ((e = cudaMemcpyAsync(d_pages, pages.data(), np * sizeof(DPage), cudaMemcpyHostToDevice, st)) ||
         (e = cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(RunJob), cudaMemcpyHostToDevice, st)) ||
         (e = cudaMemcpyAsync(d_pg, page_group.data(), np * 4, cudaMemcpyHostToDevice, st)) ||
@@ -1654,6 +1688,8 @@ void gb_pq_close(gb_pq_file *f) {
     if (!f) return;
     if (f->dev) cudaFree(f->dev);
     for (void *p : {f->idx_pages, f->idx_runs, f->idx_page_runs})
+        if (p) cudaFree(p);
+    for (void *p : f->ds_buf)
         if (p) cudaFree(p);
     delete f;
 }
