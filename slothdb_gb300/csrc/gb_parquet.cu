@@ -10,6 +10,9 @@
 //   k_pq_runs   one CTA per dictionary-encoded data page: the page is staged in
 //               shared memory and its RLE / bit-packed run headers are walked
 //               into a run table (RleDecoder::FetchRun, parquet.cpp:485-512).
+//   k_pq_views  per row chunk: each column's pages over the chunk and the run
+//               window of the dictionary column the scan stages (searched for
+//               every chunk in parallel before the scan).
 //   k_pq_scan   row chunks: every needed column is decoded at each row — PLAIN
 //               values loaded in place from the page, dictionary indices
 //               located through the run table and bit-unpacked from the page
@@ -949,13 +952,24 @@ __device__ __forceinline__ u64 decode_col(const uint8_t *file, const DPage *page
 #define PQ_MAXR 1024
 
 
+#define PQ_FASTC 4  // columns of a chunk decoded by the straight-line path
+
 struct PqChunkView {
     uint32_t np[GB_MAX_COLS];              // pages overlapping the chunk (0 = fallback)
     uint32_t pfirst[GB_MAX_COLS][PQ_MAXP];  // their first rows
     uint32_t pidx[GB_MAX_COLS][PQ_MAXP];    // their page indices
     int32_t dcol;                           // dictionary column with staged runs (-1: none)
+    uint32_t fast;                          // 1: every column REQUIRED in one page, PLAIN fixed-width or dcol
+    uint32_t rlo[PQ_MAXP];                  // first run of each page of dcol in the run table
     uint32_t rbeg[PQ_MAXP], rcnt[PQ_MAXP];  // staged run windows per page of dcol
 };
+
+// A chunk's view as k_pq_views writes it (u32 words, n_cols columns):
+// [0] dcol, [1] fast, [2, 2 + n_cols) np, then per column pfirst[PQ_MAXP] and
+// pidx[PQ_MAXP], then rlo, rbeg, rcnt [PQ_MAXP] each.
+__host__ __device__ __forceinline__ uint32_t pq_view_words(int n_cols) {
+    return 2u + (uint32_t)n_cols * (1u + 2u * PQ_MAXP) + 3u * PQ_MAXP;
+}
 
 __device__ __forceinline__ uint32_t run_search(const DRun *rr, uint32_t lo, uint32_t hi, uint32_t i) {
     while (hi - lo > 1) {  // last run with start <= i
@@ -1007,74 +1021,131 @@ __device__ __forceinline__ u64 decode_staged(const uint8_t *file, const DPage *p
     return decode_at(file, pg, runs, page_runs, pi, j, match);
 }
 
-__global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPage *pages, const DRun *runs,
-                                                 const uint32_t *page_runs, const uint32_t *col_pages,
-                                                 const PqChunkArg *chunks, uint32_t n_chunks,
-                                                 const __grid_constant__ PqScan S, Ctl *ctl) {
-    constexpr int PER = PQ_CHUNK / 256;
-    __shared__ PqChunkView V;
-    __shared__ DRun srun[PQ_MAXR];
-    __shared__ uint32_t s_surv[8][PER * 32];  // per warp: its surviving rows
-    __shared__ uint32_t s_rlo[PQ_MAXP];
-    for (uint32_t ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
+// One thread per chunk: each column's pages overlapping the chunk (a
+// fallback to per-row page search past PQ_MAXP pages), the first dictionary
+// column whose runs the scan stages in shared memory with each page's run
+// window (none past PQ_MAXR runs), and whether the chunk takes the
+// straight-line decode.  Every chunk's searches run here in parallel, before
+// the scan, instead of in one thread of each scan block while it waits.
+__global__ void k_pq_views(const DPage *pages, const DRun *runs, const uint32_t *page_runs,
+                           const uint32_t *col_pages, const PqChunkArg *chunks, uint32_t n_chunks, int n_cols,
+                           int id_col, uint32_t *views) {
+    const uint32_t W = pq_view_words(n_cols);
+    for (uint32_t ci = blockIdx.x * blockDim.x + threadIdx.x; ci < n_chunks; ci += gridDim.x * blockDim.x) {
         const PqChunkArg ch = chunks[ci];
         const uint32_t rlast = ch.row0 + (ch.nrows ? ch.nrows - 1 : 0);
-        // (a) each column's pages overlapping the chunk
-        if (threadIdx.x < (unsigned)S.n_cols) {
-            const int c = threadIdx.x;
-            const uint32_t pb = col_pages[2 * (ch.rg * S.n_cols + c)], pe = col_pages[2 * (ch.rg * S.n_cols + c) + 1];
-            uint32_t n = 0;
+        uint32_t *rec = views + (u64)ci * W;
+        uint32_t *npw = rec + 2, *pw = rec + 2 + n_cols;
+        uint32_t *rw = pw + (uint32_t)n_cols * 2 * PQ_MAXP;
+        int dc = -1;
+        bool fast = n_cols <= PQ_FASTC;
+        for (int c = 0; c < n_cols; c++) {
+            const uint32_t pb = col_pages[2 * (ch.rg * n_cols + c)], pe = col_pages[2 * (ch.rg * n_cols + c) + 1];
+            uint32_t n = 0, p0 = 0;
             if (pe > pb) {
                 uint32_t p = find_page(pages, pb, pe, ch.row0);
+                p0 = p;
                 for (; p < pe && pages[p].first_row <= rlast; p++) {
                     if (n == PQ_MAXP) {
                         n = 0;  // too many pages: per-row global search
                         break;
                     }
-                    V.pfirst[c][n] = pages[p].first_row;
-                    V.pidx[c][n] = p;
+                    pw[c * 2 * PQ_MAXP + n] = pages[p].first_row;
+                    pw[c * 2 * PQ_MAXP + PQ_MAXP + n] = p;
                     n++;
                 }
             }
-            V.np[c] = n;
+            npw[c] = n;
+            const bool dict = n && pages[p0].kind != 0 && pages[p0].def_bytes == 0;
+            if (dc < 0 && dict) dc = c;
+            // straight-line decode: one REQUIRED page, PLAIN fixed-width (or the staged dictionary column)
+            if (n != 1 || pages[p0].def_bytes != 0 || (c == id_col && !dict) ||
+                (!dict && (pages[p0].kind != 0 || pages[p0].dict_ids)))
+                fast = false;
+            if (dict && c != dc) fast = false;
         }
-        if (threadIdx.x == 0) V.dcol = -1;
-        __syncthreads();
-        // (b) the first dictionary column's runs overlapping the chunk
-        if (threadIdx.x == 0) {
-            int dc = -1;
-            for (int c = 0; c < S.n_cols && dc < 0; c++)
-                if (V.np[c] && pages[V.pidx[c][0]].kind != 0 && pages[V.pidx[c][0]].def_bytes == 0) dc = c;
+        int dcol = -1;
+        if (dc >= 0) {
             uint32_t tot = 0;
-            if (dc >= 0) {
-                for (uint32_t k = 0; k < V.np[dc]; k++) {
-                    const uint32_t pi = V.pidx[dc][k];
-                    const DPage &pg = pages[pi];
-                    if (pg.kind == 0) {  // a PLAIN page of the column has no runs
-                        s_rlo[k] = 0;
-                        V.rbeg[k] = tot;
-                        V.rcnt[k] = 0;
-                        continue;
-                    }
-                    const uint32_t nr = page_runs[PQ_PR * pi];
-                    const DRun *rr = runs + pg.run_base;
-                    const uint32_t i0 = ch.row0 > pg.first_row ? ch.row0 - pg.first_row : 0;
-                    const uint32_t i1 = rlast - pg.first_row;  // inclusive (clipped by the run search)
-                    uint32_t lo = nr ? run_search(rr, 0, nr, i0) : 0;
-                    uint32_t hi = nr ? run_search(rr, 0, nr, i1) + 1 : 0;
-                    s_rlo[k] = pg.run_base + lo;
-                    V.rbeg[k] = tot;
-                    V.rcnt[k] = hi - lo;
-                    tot += hi - lo;
+            for (uint32_t k = 0; k < npw[dc]; k++) {
+                const uint32_t pi = pw[dc * 2 * PQ_MAXP + PQ_MAXP + k];
+                const DPage &pg = pages[pi];
+                if (pg.kind == 0) {  // a PLAIN page of the column has no runs
+                    rw[k] = 0;
+                    rw[PQ_MAXP + k] = tot;
+                    rw[2 * PQ_MAXP + k] = 0;
+                    continue;
                 }
-                if (tot <= PQ_MAXR) V.dcol = dc;
+                const uint32_t nr = page_runs[PQ_PR * pi];
+                const DRun *rr = runs + pg.run_base;
+                const uint32_t i0 = ch.row0 > pg.first_row ? ch.row0 - pg.first_row : 0;
+                const uint32_t i1 = rlast - pg.first_row;  // inclusive (clipped by the run search)
+                const uint32_t lo = nr ? run_search(rr, 0, nr, i0) : 0;
+                const uint32_t hi = nr ? run_search(rr, lo, nr, i1) + 1 : 0;
+                rw[k] = pg.run_base + lo;
+                rw[PQ_MAXP + k] = tot;
+                rw[2 * PQ_MAXP + k] = hi - lo;
+                tot += hi - lo;
+            }
+            if (tot <= PQ_MAXR) dcol = dc;
+        }
+        if (dc >= 0 && dcol < 0) fast = false;  // its runs are not staged
+        rec[0] = (uint32_t)dcol;
+        rec[1] = fast ? 1u : 0u;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPage *pages, const DRun *runs,
+                                                 const uint32_t *page_runs, const uint32_t *col_pages,
+                                                 const PqChunkArg *chunks, uint32_t n_chunks,
+                                                 const uint32_t *views, const __grid_constant__ PqScan S,
+                                                 Ctl *ctl) {
+    constexpr int PER = PQ_CHUNK / 256;
+    __shared__ PqChunkView V;
+    __shared__ DRun srun[PQ_MAXR];
+    __shared__ uint32_t s_surv[8][PER * 32];  // per warp: its surviving rows
+    __shared__ u64 s_poff[PQ_FASTC];
+    __shared__ int s_pwid[PQ_FASTC];
+    const int nc = S.n_cols;
+    const uint32_t W = pq_view_words(nc), PW = 2 + (uint32_t)nc + (uint32_t)nc * 2 * PQ_MAXP;
+    for (uint32_t ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
+        const PqChunkArg ch = chunks[ci];
+        // the chunk's view (k_pq_views)
+        const uint32_t *rec = views + (u64)ci * W;
+        for (uint32_t w = threadIdx.x; w < W; w += blockDim.x) {
+            const uint32_t x = rec[w];
+            if (w == 0) {
+                V.dcol = (int32_t)x;
+            } else if (w == 1) {
+                V.fast = x;
+            } else if (w < 2 + (uint32_t)nc) {
+                V.np[w - 2] = x;
+            } else if (w < PW) {
+                const uint32_t q = w - 2 - nc, c = q / (2 * PQ_MAXP), k = q % (2 * PQ_MAXP);
+                if (k < PQ_MAXP) V.pfirst[c][k] = x;
+                else V.pidx[c][k - PQ_MAXP] = x;
+            } else {
+                const uint32_t q = w - PW;
+                if (q < PQ_MAXP) V.rlo[q] = x;
+                else if (q < 2 * PQ_MAXP) V.rbeg[q - PQ_MAXP] = x;
+                else V.rcnt[q - 2 * PQ_MAXP] = x;
             }
         }
         __syncthreads();
+        if (threadIdx.x < PQ_FASTC) {  // the straight-line decode's PLAIN columns
+            const int c = threadIdx.x;
+            s_poff[c] = 0;  // file offset of row 0 of the row group in the column's page (mod 2^64)
+            s_pwid[c] = 0;  // 0: not a PLAIN column
+            if (V.fast && c < nc && c != V.dcol) {
+                const DPage &pg = pages[V.pidx[c][0]];
+                s_pwid[c] = pg.width;
+                s_poff[c] = pg.off - (u64)V.pfirst[c][0] * (u64)pg.width;
+            }
+        }
         if (V.dcol >= 0) {
             const int dc = V.dcol;
             for (uint32_t k = 0; k < V.np[dc]; k++)
-                for (uint32_t t = threadIdx.x; t < V.rcnt[k]; t += blockDim.x) srun[V.rbeg[k] + t] = runs[s_rlo[k] + t];
+                for (uint32_t t = threadIdx.x; t < V.rcnt[k]; t += blockDim.x) srun[V.rbeg[k] + t] = runs[V.rlo[k] + t];
         }
         __syncthreads();
         bool keep[PER];
@@ -1145,6 +1216,37 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
         u64 o = block_out_base(ctl, lane == 0 ? cnt : 0u);
         o = __shfl_sync(FULL, o, 0);
         __syncwarp();
+        if (V.fast) {
+            // every column in one REQUIRED page: the PLAIN loads of a survivor are
+            // issued together, beside the dictionary column's run -> bits -> value chain
+            const int dc = V.dcol;
+            const uint32_t dpi = dc >= 0 ? V.pidx[dc][0] : 0, dfirst = dc >= 0 ? V.pfirst[dc][0] : 0;
+            const uint32_t dbw = dc >= 0 ? page_runs[PQ_PR * dpi + 1] : 0;
+            for (u32 e = lane; e < cnt; e += 32) {
+                const u64 oe = o + e;
+                if (oe >= S.out_cap) {
+                    atomicOr(&ctl->err, (u32)ERR_OUT_OVERFLOW);
+                    continue;
+                }
+                const uint32_t r = s_surv[wid][e];
+                u64 x[PQ_FASTC];
+#pragma unroll
+                for (int c = 0; c < PQ_FASTC; c++)
+                    x[c] = s_pwid[c] ? load_plain(file + (s_poff[c] + (u64)r * (u64)s_pwid[c]), s_pwid[c]) : 0;
+                const u64 xk = dc >= 0 ? dict_value(file, pages[dpi], srun + V.rbeg[0], 0, V.rcnt[0], dbw, r - dfirst)
+                                       : 0;
+#pragma unroll
+                for (int c = 0; c < PQ_FASTC; c++) {
+                    if (c < nc) {
+                        const u64 val = c == dc ? xk : x[c];
+                        const int t = S.out_type[c];
+                        if (t == GB_T_SMALLINT) ((int16_t *)S.out[c])[oe] = (int16_t)(i64)val;
+                        else if (t == GB_T_INTEGER) ((int32_t *)S.out[c])[oe] = (int32_t)(i64)val;
+                        else ((u64 *)S.out[c])[oe] = val;
+                    }
+                }
+            }
+        } else
         for (u32 e = lane; e < cnt; e += 32) {
             const u64 oe = o + e;
             if (oe >= S.out_cap) {
@@ -1718,6 +1820,8 @@ struct PqScratch {
     // compressed batches: the decompressed image, its jobs, the level lengths found inside
     void *img = nullptr, *ijobs = nullptr, *ilvl = nullptr;
     size_t img_cap = 0, ijobs_cap = 0, ilvl_cap = 0;
+    void *views = nullptr;  // per chunk of the batch: its view (k_pq_views)
+    size_t views_cap = 0;
 };
 
 static gb_status grow(void *&p, size_t &cap, size_t need) {
@@ -1757,7 +1861,7 @@ void gb_pq_release_scratch(gb_agg *h) {
         g_pq_scratch.erase(it);
     }
     for (void *p : {s->file_dev, s->pages, s->runs, s->page_runs, s->dict_pages, s->col_pages, s->chunks, s->ctl,
-                    s->dicts, s->dsrc, s->doffs, s->dbytes, s->dmatch, s->dcounts, s->img, s->ijobs, s->ilvl})
+                    s->dicts, s->dsrc, s->doffs, s->dbytes, s->dmatch, s->dcounts, s->img, s->ijobs, s->ilvl, s->views})
         if (p) cudaFree(p);
     for (void *p : s->out)
         if (p) cudaFree(p);
@@ -2496,14 +2600,23 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
     for (int q = 0; q < v.n_filters; q++) P.filters[q] = v.filters[q];
     P.out_cap = S->out_cap_rows;
     {
+        if ((s = grow(S->views, S->views_cap, chunks.size() * pq_view_words(nc) * 4 + 16))) return s;
+        const int vgrid = (int)std::min<size_t>((chunks.size() + 127) / 128, (size_t)sm_count() * 8);
+        gb_prof_mark *pv = gb_agg_prof_begin(h, "k_pq_views", st);
+        k_pq_views<<<std::max(vgrid, 1), 128, 0, st>>>((const DPage *)d_pages, (const DRun *)d_runs,
+                                                       (const uint32_t *)d_page_runs, (const uint32_t *)S->col_pages,
+                                                       (const PqChunkArg *)S->chunks, (uint32_t)chunks.size(), nc, vc,
+                                                       (uint32_t *)S->views);
+        gb_agg_prof_end(h, pv, st);
         const int grid = (int)std::min<size_t>(chunks.size(), (size_t)sm_count() * 8);
         gb_prof_mark *pm = gb_agg_prof_begin(h, "k_pq_scan", st);
         k_pq_scan<<<std::max(grid, 1), 256, 0, st>>>(dfile, (const DPage *)d_pages, (const DRun *)d_runs,
                                                      (const uint32_t *)d_page_runs, (const uint32_t *)S->col_pages,
-                                                     (const PqChunkArg *)S->chunks, (uint32_t)chunks.size(), P, dctl);
+                                                     (const PqChunkArg *)S->chunks, (uint32_t)chunks.size(),
+                                                     (const uint32_t *)S->views, P, dctl);
         gb_agg_prof_end(h, pm, st);
         GB_CUDA(cudaGetLastError());
-        gb_agg_count_launch(h, 1);
+        gb_agg_count_launch(h, 2);
     }
     Ctl c;
     GB_CUDA(cudaMemcpyAsync(&c, dctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st));
