@@ -1095,7 +1095,7 @@ __global__ void k_pq_views(const DPage *pages, const DRun *runs, const uint32_t 
     }
 }
 
-__global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPage *pages, const DRun *runs,
+__global__ void __launch_bounds__(256, 4) k_pq_scan(const uint8_t *file, const DPage *pages, const DRun *runs,
                                                  const uint32_t *page_runs, const uint32_t *col_pages,
                                                  const PqChunkArg *chunks, uint32_t n_chunks,
                                                  const uint32_t *views, const __grid_constant__ PqScan S,
@@ -1106,14 +1106,25 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
     __shared__ uint32_t s_surv[8][PER * 32];  // per warp: its surviving rows
     __shared__ u64 s_poff[PQ_FASTC];
     __shared__ int s_pwid[PQ_FASTC];
+    __shared__ DPage s_dpg;  // the straight-line decode's dictionary page
+    __shared__ uint32_t s_dbw;
     const int nc = S.n_cols;
     const uint32_t W = pq_view_words(nc), PW = 2 + (uint32_t)nc + (uint32_t)nc * 2 * PQ_MAXP;
+    // each thread holds words threadIdx.x and threadIdx.x + 256 of the next
+    // chunk's view, and its row range, loaded while the block works on the
+    // current chunk
+    uint32_t rw[2] = {0, 0};
+    PqChunkArg ch = {0, 0, 0};
+    if (blockIdx.x < n_chunks) {
+        ch = chunks[blockIdx.x];
+        for (int h = 0; h < 2; h++)
+            if (threadIdx.x + 256u * h < W) rw[h] = views[(u64)blockIdx.x * W + threadIdx.x + 256u * h];
+    }
     for (uint32_t ci = blockIdx.x; ci < n_chunks; ci += gridDim.x) {
-        const PqChunkArg ch = chunks[ci];
         // the chunk's view (k_pq_views)
-        const uint32_t *rec = views + (u64)ci * W;
-        for (uint32_t w = threadIdx.x; w < W; w += blockDim.x) {
-            const uint32_t x = rec[w];
+        for (int h = 0; h < 2; h++) {
+            const uint32_t w = threadIdx.x + 256u * h, x = rw[h];
+            if (w >= W) continue;
             if (w == 0) {
                 V.dcol = (int32_t)x;
             } else if (w == 1) {
@@ -1131,7 +1142,19 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
                 else V.rcnt[q - 2 * PQ_MAXP] = x;
             }
         }
+        const PqChunkArg chc = ch;
+        if (ci + gridDim.x < n_chunks) {
+            const uint32_t cn = ci + gridDim.x;
+            ch = chunks[cn];
+            for (int h = 0; h < 2; h++)
+                if (threadIdx.x + 256u * h < W) rw[h] = views[(u64)cn * W + threadIdx.x + 256u * h];
+        }
         __syncthreads();
+        if (threadIdx.x == PQ_FASTC && V.fast && V.dcol >= 0) {  // the staged dictionary column's page
+            const uint32_t pi = V.pidx[V.dcol][0];
+            s_dpg = pages[pi];
+            s_dbw = page_runs[PQ_PR * pi + 1];
+        }
         if (threadIdx.x < PQ_FASTC) {  // the straight-line decode's PLAIN columns
             const int c = threadIdx.x;
             s_poff[c] = 0;  // file offset of row 0 of the row group in the column's page (mod 2^64)
@@ -1142,37 +1165,53 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
                 s_poff[c] = pg.off - (u64)V.pfirst[c][0] * (u64)pg.width;
             }
         }
-        if (V.dcol >= 0) {
-            const int dc = V.dcol;
-            for (uint32_t k = 0; k < V.np[dc]; k++)
-                for (uint32_t t = threadIdx.x; t < V.rcnt[k]; t += blockDim.x) srun[V.rbeg[k] + t] = runs[V.rlo[k] + t];
-        }
-        __syncthreads();
-        bool keep[PER];
-        u32 mine = 0;
         // one predicate on a PLAIN column inside one page (the common case):
-        // every load of the chunk is issued before any compare
+        // every load of the chunk is issued before any compare, and before the
+        // run staging below
         const int fc = (S.n_filters == 1 && S.filters[0].op <= GB_CMP_GE) ? S.filters[0].col : -1;
-        if (fc >= 0 && V.np[fc] == 1 && pages[V.pidx[fc][0]].kind == 0 && pages[V.pidx[fc][0]].def_bytes == 0) {
-            const DPage pg = pages[V.pidx[fc][0]];
-            const Filter f = S.filters[0];
+        const bool fastf =
+            fc >= 0 && V.np[fc] == 1 && pages[V.pidx[fc][0]].kind == 0 && pages[V.pidx[fc][0]].def_bytes == 0;
+        u32 kmask = 0;  // the fast predicate's result, row j * 256 + threadIdx.x in bit j
+        if (fastf) {
+            const DPage &pg = pages[V.pidx[fc][0]];
             const uint8_t *base = file + pg.off;  // page payloads start at any byte
+            const int wd = pg.width;
+            const uint32_t first = pg.first_row;
             u64 xv[PER];
 #pragma unroll
             for (int j = 0; j < PER; j++) {
                 const uint32_t rr = (uint32_t)j * 256 + threadIdx.x;
                 xv[j] = 0;
-                if (rr < ch.nrows) {
-                    const uint32_t i = ch.row0 + rr - pg.first_row;
-                    xv[j] = load_plain(base + (u64)i * pg.width, pg.width);
-                }
+                if (rr < chc.nrows) xv[j] = load_plain(base + (u64)(chc.row0 + rr - first) * wd, wd);
             }
+            if (V.dcol >= 0 && threadIdx.x < V.rcnt[0]) {  // the first staged run while the loads fly
+                const uint32_t t = threadIdx.x;
+                srun[V.rbeg[0] + t] = runs[V.rlo[0] + t];
+            }
+            const Filter f = S.filters[0];
+            const bool dbl = S.out_type[fc] == GB_T_DOUBLE;
 #pragma unroll
             for (int j = 0; j < PER; j++) {
                 const uint32_t rr = (uint32_t)j * 256 + threadIdx.x;
-                keep[j] = rr < ch.nrows && (S.out_type[fc] == GB_T_DOUBLE
-                                                ? cmp_f(f.op, __longlong_as_double((i64)xv[j]), f.dc)
-                                                : cmp_i(f.op, (i64)xv[j], f.ic));
+                const bool k = rr < chc.nrows && (dbl ? cmp_f(f.op, __longlong_as_double((i64)xv[j]), f.dc)
+                                                      : cmp_i(f.op, (i64)xv[j], f.ic));
+                kmask |= (u32)k << j;
+            }
+        }
+        if (V.dcol >= 0) {
+            const int dc = V.dcol;
+            for (uint32_t k = 0; k < V.np[dc]; k++)
+                for (uint32_t t = threadIdx.x + (fastf && k == 0 ? blockDim.x : 0); t < V.rcnt[k]; t += blockDim.x)
+                    srun[V.rbeg[k] + t] = runs[V.rlo[k] + t];
+        }
+        __syncthreads();
+        const PqChunkArg ch = chc;
+        bool keep[PER];
+        u32 mine = 0;
+        if (fastf) {
+#pragma unroll
+            for (int j = 0; j < PER; j++) {
+                keep[j] = (kmask >> j) & 1u;
                 mine += keep[j];
             }
         } else {
@@ -1220,8 +1259,7 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
             // every column in one REQUIRED page: the PLAIN loads of a survivor are
             // issued together, beside the dictionary column's run -> bits -> value chain
             const int dc = V.dcol;
-            const uint32_t dpi = dc >= 0 ? V.pidx[dc][0] : 0, dfirst = dc >= 0 ? V.pfirst[dc][0] : 0;
-            const uint32_t dbw = dc >= 0 ? page_runs[PQ_PR * dpi + 1] : 0;
+            const uint32_t dfirst = dc >= 0 ? V.pfirst[dc][0] : 0;
             for (u32 e = lane; e < cnt; e += 32) {
                 const u64 oe = o + e;
                 if (oe >= S.out_cap) {
@@ -1233,8 +1271,7 @@ __global__ void __launch_bounds__(256) k_pq_scan(const uint8_t *file, const DPag
 #pragma unroll
                 for (int c = 0; c < PQ_FASTC; c++)
                     x[c] = s_pwid[c] ? load_plain(file + (s_poff[c] + (u64)r * (u64)s_pwid[c]), s_pwid[c]) : 0;
-                const u64 xk = dc >= 0 ? dict_value(file, pages[dpi], srun + V.rbeg[0], 0, V.rcnt[0], dbw, r - dfirst)
-                                       : 0;
+                const u64 xk = dc >= 0 ? dict_value(file, s_dpg, srun + V.rbeg[0], 0, V.rcnt[0], s_dbw, r - dfirst) : 0;
 #pragma unroll
                 for (int c = 0; c < PQ_FASTC; c++) {
                     if (c < nc) {
