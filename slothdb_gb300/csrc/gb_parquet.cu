@@ -2645,7 +2645,8 @@ extern "C" gb_status gb_agg_ingest_parquet(gb_agg *h, gb_pq_file *f, uint32_t rg
                                                        (const PqChunkArg *)S->chunks, (uint32_t)chunks.size(), nc, vc,
                                                        (uint32_t *)S->views);
         gb_agg_prof_end(h, pv, st);
-        const int grid = (int)std::min<size_t>(chunks.size(), (size_t)sm_count() * 8);
+        // one wave: the blocks that fit on the SMs at once (4 each) loop over the chunks
+        const int grid = (int)std::min<size_t>(chunks.size(), (size_t)sm_count() * 4);
         gb_prof_mark *pm = gb_agg_prof_begin(h, "k_pq_scan", st);
         k_pq_scan<<<std::max(grid, 1), 256, 0, st>>>(dfile, (const DPage *)d_pages, (const DRun *)d_runs,
                                                      (const uint32_t *)d_page_runs, (const uint32_t *)S->col_pages,
