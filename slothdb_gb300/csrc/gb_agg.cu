@@ -115,13 +115,18 @@ __global__ void __launch_bounds__(512) k_ingest(const __grid_constant__ Plan P, 
 
 // Re-insert every pair of the old sets into the new (larger, emptied) ones.
 __global__ void k_dset_rehash(const u64 *old_sets, u64 old_mask, int n_sets, u64 *new_sets, u64 new_mask,
-                              unsigned long long *meta) {
+                              unsigned long long *meta, int narrow) {
     const u64 old_slots = old_mask + 1, new_slots = new_mask + 1;
     const u64 total = old_slots * (u64)n_sets;
     for (u64 i = blockIdx.x * (u64)blockDim.x + threadIdx.x; i < total; i += (u64)gridDim.x * blockDim.x) {
+        const int d = (int)(i / old_slots);
+        if (narrow) {
+            const u64 e = old_sets[i];
+            if (e != ~0ull) dset_insert_narrow(new_sets + new_slots * d, new_mask, e, meta, d);
+            continue;
+        }
         const u64 g = old_sets[2 * i], v = old_sets[2 * i + 1];
         if (g == EMPTY_KEY && v == EMPTY_KEY) continue;
-        const int d = (int)(i / old_slots);
         dset_insert(new_sets + 2 * new_slots * d, new_mask, g, v, meta, d);
     }
 }
@@ -917,25 +922,28 @@ static gb_status dist_reserve(gb_agg *h, u64 n_rows, cudaStream_t st) {
     if (h->dslots == 0) GB_CUDA(cudaMemsetAsync(h->dmeta.p, 0, sizeof(h->dmeta_host), st));
     u64 slots = std::max<u64>(1024, h->dslots);
     while (slots < 2 * (h->dpairs + n_rows)) slots *= 2;
-    const size_t bytes = (size_t)slots * 16 * nd;
+    const u64 wps = P.dnarrow ? 1 : 2;  // words per slot
+    const u64 empty = P.dnarrow ? ~0ull : EMPTY_KEY;
+    const size_t bytes = (size_t)slots * 8 * wps * nd;
     if (slots != h->dslots) {
         std::swap(h->dsets, h->dsets_old);
         std::swap(h->null_sets, h->null_sets_old);
         if ((s = h->dsets.ensure(bytes))) return s;
-        if ((s = radix_fill_u64((u64 *)h->dsets.p, (u64)slots * 2 * nd, EMPTY_KEY, st))) return s;
+        if ((s = radix_fill_u64((u64 *)h->dsets.p, (u64)slots * wps * nd, empty, st))) return s;
         if (h->dist_null_sets) {
             if ((s = h->null_sets.ensure(bytes))) return s;
-            if ((s = radix_fill_u64((u64 *)h->null_sets.p, (u64)slots * 2 * nd, EMPTY_KEY, st))) return s;
+            if ((s = radix_fill_u64((u64 *)h->null_sets.p, (u64)slots * wps * nd, empty, st))) return s;
         }
         if (h->dslots) {
             const u64 old_mask = h->dslots - 1, total = h->dslots * (u64)nd;
             const int grid = grid_for(total, 256, sm_count() * 8);
             k_dset_rehash<<<grid, 256, 0, st>>>((const u64 *)h->dsets_old.p, old_mask, nd, (u64 *)h->dsets.p,
-                                                slots - 1, (unsigned long long *)h->dmeta.p);
+                                                slots - 1, (unsigned long long *)h->dmeta.p, P.dnarrow);
             h->launches++;
             if (h->dist_null_sets) {
                 k_dset_rehash<<<grid, 256, 0, st>>>((const u64 *)h->null_sets_old.p, old_mask, nd,
-                                                    (u64 *)h->null_sets.p, slots - 1, (unsigned long long *)h->dmeta.p);
+                                                    (u64 *)h->null_sets.p, slots - 1, (unsigned long long *)h->dmeta.p,
+                                                    P.dnarrow);
                 h->launches++;
             }
             GB_CUDA(cudaGetLastError());
@@ -956,10 +964,11 @@ static gb_status dist_clear(gb_agg *h, cudaStream_t st) {
     h->dpairs = 0;
     memset(h->dmeta_host, 0, sizeof(h->dmeta_host));
     if (!h->dslots) return GB_OK;
-    const u64 words = h->dslots * 2 * (u64)h->plan.n_dist;
+    const u64 words = h->dslots * (h->plan.dnarrow ? 1 : 2) * (u64)h->plan.n_dist;
+    const u64 empty = h->plan.dnarrow ? ~0ull : EMPTY_KEY;
     gb_status s;
-    if ((s = radix_fill_u64((u64 *)h->dsets.p, words, EMPTY_KEY, st))) return s;
-    if (h->dist_null_sets && (s = radix_fill_u64((u64 *)h->null_sets.p, words, EMPTY_KEY, st))) return s;
+    if ((s = radix_fill_u64((u64 *)h->dsets.p, words, empty, st))) return s;
+    if (h->dist_null_sets && (s = radix_fill_u64((u64 *)h->null_sets.p, words, empty, st))) return s;
     GB_CUDA(cudaMemsetAsync(h->dmeta.p, 0, sizeof(h->dmeta_host), st));
     return GB_OK;
 }
@@ -1710,6 +1719,17 @@ static gb_status compile_plan(gb_agg *h) {
     // the NULL-key group of a nullable BIGINT key has no spare key value
     h->dist_null_sets = P.n_dist && P.key_mode == KEY_SINGLE && P.key_type[0] == GB_T_BIGINT &&
                         ((h->nullable_mask >> P.key_col[0]) & 1ull);
+    // a non-NULL 16/32-bit key and 16/32-bit distinct columns: 8-byte pair slots
+    P.dnarrow = 0;
+    if (P.n_dist && P.key_mode == KEY_SINGLE && h->str_col < 0 &&
+        (P.key_type[0] == GB_T_SMALLINT || P.key_type[0] == GB_T_INTEGER) &&
+        !((h->nullable_mask >> P.key_col[0]) & 1ull)) {
+        P.dnarrow = 1;
+        for (int i = 0; i < P.n_ops; i++)
+            if (P.ops[i].kind == OP_DIST && h->col_types[P.ops[i].col] != GB_T_SMALLINT &&
+                h->col_types[P.ops[i].col] != GB_T_INTEGER)
+                P.dnarrow = 0;
+    }
     if (h->str_col >= 0) P.n_cols = nc + 1;
     {
         int need = words + 1;

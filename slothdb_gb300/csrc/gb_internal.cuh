@@ -100,11 +100,13 @@ struct Plan {
     int32_t words;        // state words (word 0 = row count)
     int32_t stride;       // words per table slot incl. key, power of two
     int32_t n_dist;       // OP_DIST ops (COUNT(DISTINCT) columns)
+    int32_t dnarrow;      // 1: pair sets of 8-byte slots (a non-NULL 16/32-bit key, 16/32-bit values)
     int32_t str_key;      // a pair key's VARCHAR position (its 32-bit string ids are packed), -1: none
     uint64_t word_init[GB_MAX_WORDS];
     // COUNT(DISTINCT): per OP_DIST op a set of (group key, value) pairs,
-    // 16-byte slots of which dmask + 1 per set; the NULL-key group of a
-    // nullable BIGINT key keeps its pairs in twin sets (null_sets, or null)
+    // 16-byte slots (8-byte when dnarrow) of which dmask + 1 per set; the
+    // NULL-key group of a nullable BIGINT key keeps its pairs in twin sets
+    // (null_sets, or null)
     u64 *dsets;
     u64 *null_sets;
     unsigned long long *dmeta;  // [0] pairs inserted, [1] overflow flag, [2 + d] marker pair of set d seen

@@ -155,6 +155,23 @@ __device__ __forceinline__ bool dset_insert(u64 *set, u64 mask, u64 g, u64 v, un
     return false;
 }
 
+// The narrow form: a 16/32-bit key and a 16/32-bit value packed into one
+// 8-byte slot (key in the high half), claimed by one 64-bit compare-and-swap;
+// the empty marker is all ones, and the real pair equal to it (key -1, value
+// -1) is tracked by the same flag word as the wide form's marker pair.
+__device__ __forceinline__ bool dset_insert_narrow(u64 *set, u64 mask, u64 e, unsigned long long *meta, int d) {
+    if (e == ~0ull) return atomicExch(meta + 2 + d, 1ull) == 0ull;
+    u64 s = mix64(e) & mask;
+    for (u64 q = 0; q <= mask; q++) {
+        const u64 old = atomicCAS((unsigned long long *)(set + s), ~0ull, e);
+        if (old == ~0ull) return true;
+        if (old == e) return false;
+        s = (s + 1) & mask;
+    }
+    atomicExch(meta + 1, 1ull);  // full: the host sized it wrongly
+    return false;
+}
+
 // Replace each OP_DIST contribution of row r (key pk of kind `kind`, as
 // make_key returns) by 1 if its (group, value) pair is new, else 0.
 __device__ __forceinline__ void dist_vals(const Plan &P, u64 r, int kind, u64 pk, u64 *v, u32 *new_pairs) {
@@ -164,7 +181,13 @@ __device__ __forceinline__ void dist_vals(const Plan &P, u64 r, int kind, u64 pk
             const Op o = P.ops[i];
             const DevCol &c = P.cols[o.col];
             u64 x = 0;
-            if (row_valid(c.valid, r)) {
+            if (row_valid(c.valid, r) && P.dnarrow) {
+                const u64 e = ((u64)(uint32_t)pk << 32) | (uint32_t)load_int(c, r);
+                if (dset_insert_narrow(P.dsets + (P.dmask + 1) * o.dset, P.dmask, e, P.dmeta, o.dset)) {
+                    x = 1;
+                    atomicAdd(new_pairs, 1u);
+                }
+            } else if (row_valid(c.valid, r)) {
                 const u64 val = (u64)load_int(c, r);
                 const u64 slots = P.dmask + 1;
                 u64 *set = P.dsets + 2 * slots * o.dset;

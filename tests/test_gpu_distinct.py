@@ -107,6 +107,55 @@ def test_reset_reuses_pair_sets():
     assert int(outs[1][2][0].sum()) == 120_000
 
 
+@pytest.mark.parametrize("key_type", [INTEGER, SMALLINT])
+def test_narrow_pair_sets(key_type):
+    """A non-NULL 16/32-bit key with 16/32-bit distinct columns packs each
+    pair into one 8-byte slot: negative keys and values, the pair equal to
+    the empty marker (key -1, value -1), two distinct columns (one of them
+    nullable), a WHERE clause, and 12 ingests that grow the sets (rehash of
+    the 8-byte slots) while the table spills."""
+    n = 600_000
+    rng = np.random.default_rng(41 + key_type)
+    k = rng.integers(-25_000, 25_000, n).astype(np.int16 if key_type == SMALLINT else np.int32)
+    if key_type == INTEGER:
+        k[-2:] = [-(2**31), 2**31 - 1]
+    k[:5000] = -1
+    x = rng.integers(-1000, 1000, n).astype(np.int32)
+    x[:2500] = -1  # the marker pair
+    x[-3:] = [-(2**31), 2**31 - 1, 0]
+    y = rng.integers(-30_000, 30_000, n).astype(np.int16)
+    yn = rng.random(n) < 0.05
+    f = rng.integers(0, 100, n).astype(np.int16)
+    aggs = [("count_distinct", 1), ("count_distinct", 2), ("count_star", -1), ("sum", 1)]
+    types = [key_type, INTEGER, SMALLINT, SMALLINT]
+    check(types, [0], aggs, [k, x, y, f], nulls=[None, None, yn, None], est_groups=16, chunks=49_984)
+    check(types, [0], aggs, [k, x, y, f], nulls=[None, None, yn, None], filters=[(3, "<", 70)])
+
+
+def test_narrow_pair_sets_reset_and_resident():
+    """The 8-byte pair sets emptied by reset (same results on the same
+    rows) and fed from device-resident columns."""
+    rng = np.random.default_rng(44)
+    n = 300_000
+    k = rng.integers(0, 7000, n).astype(np.int32)
+    v = rng.integers(-50, 50, n).astype(np.int32)
+    aggs = [("count_distinct", 1), ("count_star", -1)]
+    check([INTEGER, INTEGER], [0], aggs, [k, v], device=True)
+    g = capi.GroupBy([INTEGER, INTEGER], [0], aggs)
+    try:
+        outs = []
+        for m in (n, 100_000, n):
+            g.ingest([k[:m], v[:m]])
+            g.finalize()
+            outs.append(g.result())
+            g.reset()
+    finally:
+        g.close()
+    o0, o2 = (np.argsort(o[0][0]) for o in (outs[0], outs[2]))
+    for c in range(3):
+        assert np.array_equal(outs[0][c][0][o0], outs[2][c][0][o2])
+
+
 def test_rejections():
     k = np.arange(10, dtype=np.int32)
     with pytest.raises(capi.GbError):
