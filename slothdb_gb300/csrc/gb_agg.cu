@@ -997,7 +997,10 @@ static gb_status run_ingest(gb_agg *h, u64 n_rows, cudaStream_t st) {
     }
     const u64 n_tiles_total = (n_rows + tile_rows - 1) / tile_rows;
     int grid = (int)std::min<u64>((u64)max_ctas, n_tiles_total);
+    // the shared table pays when the estimated groups fit it; past that every
+    // row would probe a full table before its HBM fold
     int S = h->smem_slots;
+    if (h->est_groups > (u64)S) S = 0;
     size_t smem = (size_t)S * 8 * (1 + words);
     // spill capacity: threshold + what in-flight tiles and the final flush can add
     u64 margin = (u64)grid * ((u64)tile_rows + (u64)S) + 1024;
