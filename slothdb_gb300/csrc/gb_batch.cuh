@@ -1046,8 +1046,8 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
             // narrow shared atomics beat the warp key match; without a shared
             // table, few groups mean hot HBM slots, which the match relieves
             d.pre = b->precombine == 2 || (b->precombine == 1 && d.smem_slots == 0 && h->est_groups <= 4096);
-        } else if (h->est_groups > 65536) {
-            d.smem_slots = 0;  // a shared table only pays for small group counts
+        } else if (h->est_groups > (u64)d.smem_slots) {
+            d.smem_slots = 0;  // a shared table only pays when the estimated groups fit it
         }
         d.init_words = d.table_words + (u64)(d.E.n_keys + d.E.n_aggs) * ((d.E.out_cap + 63) / 64) +
                        (d.is_str ? 2 * d.D.cap + 8 : 0);
