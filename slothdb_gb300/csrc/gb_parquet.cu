@@ -2059,45 +2059,27 @@ struct InflateJob {
 // 4-byte offset (01/10/11) of an earlier output position, possibly
 // overlapping the bytes it writes.
 //
-// The warp decodes a round of elements at a time.  Lane L reads the bytes at
-// ip + 2L and ip + 2L + 1 (aligned words over the round's 76 bytes,
-// redistributed by shuffles) and decodes the element a tag at each would
-// be; the chain of real tags from ip (each start plus its element's
-// compressed size) is walked with shuffles, up to the first start at or past
-// ip + 64.  A scan of the starts' lengths places each element in the
-// output.  Then every output byte of the round is written by one lane: a
-// binary search over the lanes' running lengths finds its element, whose
-// byte is a literal byte or an earlier output byte (an overlapping copy
-// repeats its first `offset` bytes); a source inside the round is followed
-// back the same way to a byte written before the round or to a literal
-// byte, so that the bytes of a round are independent.  A literal longer than
-// 64 bytes (the last element of its round) is copied by the whole warp after
+// The warp decodes a round of elements at a time.  Lane L reads the 8
+// compressed bytes at ip + L (one aligned word per lane, redistributed by
+// shuffles) and decodes the element a tag there would be; the chain of real
+// tags from ip (each start plus its element's compressed size) is walked with
+// shuffles over the lanes' sizes, up to the first start at or past ip + 32.
+// An exclusive scan of the starts' lengths places each element in the output.
+// Each output byte of the round gets its source in a per-warp shared map: a
+// compressed position (literal) or an earlier output position (copy; an
+// overlapping copy repeats its first `offset` bytes).  A source inside the
+// round is followed through the map to a byte written before the round or a
+// literal byte, so that all bytes of a round are independent and the warp
+// writes them with one load and one store each.  A literal longer than 64
+// bytes (the last element of its round) is copied by the whole warp after
 // the round.  Every length and offset is checked against the piece's bounds;
 // a malformed block sets ERR_CORRUPT and stops.
-#define PQ_INF_LONG 64  // literals longer than this are copied by the warp
+#define PQ_INF_MAP 1024   // output bytes of one round: at most 16 elements of at most 64 bytes
+#define PQ_INF_LONG 64    // literals longer than this are copied by the warp
 #define PQ_INF_LIT 0x80000000u
 
-// The element a tag at the first of the 8 bytes (lo, hi) would be.
-struct SnapEl {
-    uint32_t t, hdr, len, off, cs;
-};
-
-__device__ __forceinline__ SnapEl snap_el(uint32_t lo, uint32_t hi) {
-    SnapEl e;
-    const uint32_t tag = lo & 0xffu, l6 = tag >> 2;
-    const uint32_t rest = (lo >> 8) | (hi << 24);  // bytes 1..4 after the tag
-    const uint32_t nb = l6 >= 60 ? l6 - 59 : 0;     // a literal's length bytes
-    const uint32_t lraw = nb ? rest & (0xffffffffu >> (32 - 8 * nb)) : l6;
-    e.t = tag & 3u;
-    e.hdr = e.t == 0 ? 1 + nb : (e.t == 1 ? 2 : (e.t == 2 ? 3 : 5));
-    e.len = e.t == 0 ? lraw + 1 : (e.t == 1 ? 4 + (l6 & 7u) : l6 + 1);  // 0 after a wrap
-    e.off = e.t == 1 ? ((tag >> 5) << 8) | (rest & 0xffu) : (e.t == 2 ? rest & 0xffffu : rest);
-    e.cs = e.t != 0 ? e.hdr : (lraw >= 0x7fff0000u ? 0x7fffffffu : e.hdr + lraw + 1);
-    return e;
-}
-
 __device__ __forceinline__ void pq_inflate_piece(const uint8_t *__restrict__ file, const InflateJob J, uint8_t *img,
-                                                 uint32_t *lvl, Ctl *ctl, const int lane) {
+                                                 uint32_t *lvl, Ctl *ctl, uint32_t *map, const int lane) {
     const uint8_t *src = file + J.src;
     uint8_t *dst = img + J.dst;
     bool bad = false;
@@ -2128,116 +2110,89 @@ __device__ __forceinline__ void pq_inflate_piece(const uint8_t *__restrict__ fil
                 bad = true;
                 break;
             }
-            // lanes 0..18 load the aligned words over [ip, ip + 72)
+            // bytes [ip + lane, ip + lane + 8): lanes 0..10 load the aligned words over
+            // [ip, ip + 40) and the warp redistributes them
             const uint8_t *blk = (const uint8_t *)((uintptr_t)(src + ip) & ~(uintptr_t)3);
             uint32_t word = 0;
-            if (lane < 19) {
+            if (lane < 11) {
                 const uint8_t *wp = blk + 4 * lane;
-                if (blk >= src && blk + 76 <= src + slen) {
+                if (blk >= src && blk + 44 <= src + slen) {
                     word = __ldg((const uint32_t *)wp);
                 } else {
                     for (int k = 0; k < 4; k++)
                         if (wp + k >= src && wp + k < src + slen) word |= (uint32_t)__ldg(wp + k) << (8 * k);
                 }
             }
-            // bytes [ip + 2L, ip + 2L + 9) lie in words i .. i + 2
-            const uint32_t sh0 = (uint32_t)((uintptr_t)(src + ip) & 3) + 2u * (uint32_t)lane;
-            const uint32_t wi = sh0 >> 2, bs = 8 * (sh0 & 3);
-            const uint32_t w0 = __shfl_sync(FULL, word, wi);
-            const uint32_t w1 = __shfl_sync(FULL, word, wi + 1);
-            const uint32_t w2 = __shfl_sync(FULL, word, wi + 2);
-            const SnapEl ea = snap_el(__funnelshift_r(w0, w1, bs), __funnelshift_r(w1, w2, bs));
-            const SnapEl eb = snap_el(__funnelshift_rc(w0, w1, bs + 8), __funnelshift_rc(w1, w2, bs + 8));
-            // the chain of starts from ip: position 2L in lane L's a, 2L + 1 in its b
-            const uint32_t avail = min(64u, slen - ip);
-            uint32_t pos = 0, mska = 0, mskb = 0;  // starts at even / odd positions, by lane
+            const uint32_t sh0 = (uint32_t)((uintptr_t)(src + ip) & 3) + (uint32_t)lane;
+            const uint32_t w0 = __shfl_sync(FULL, word, sh0 >> 2);
+            const uint32_t w1 = __shfl_sync(FULL, word, (sh0 >> 2) + 1);
+            const uint32_t w2 = __shfl_sync(FULL, word, (sh0 >> 2) + 2);
+            const uint32_t lo = __funnelshift_r(w0, w1, 8 * (sh0 & 3)), hi = __funnelshift_r(w1, w2, 8 * (sh0 & 3));
+            // the element a tag at ip + lane would be (selects, no branches)
+            const uint32_t tag = lo & 0xffu, t = tag & 3u, l6 = tag >> 2;
+            const uint32_t rest = (lo >> 8) | (hi << 24);  // bytes 1..4 after the tag
+            const uint32_t nb = l6 >= 60 ? l6 - 59 : 0;     // a literal's length bytes
+            const uint32_t lraw = nb ? rest & (0xffffffffu >> (32 - 8 * nb)) : l6;
+            const uint32_t hdr = t == 0 ? 1 + nb : (t == 1 ? 2 : (t == 2 ? 3 : 5));
+            const uint32_t len = t == 0 ? lraw + 1 : (t == 1 ? 4 + (l6 & 7u) : l6 + 1);  // 0 after a wrap
+            const uint32_t off = t == 1 ? ((tag >> 5) << 8) | (rest & 0xffu) : (t == 2 ? rest & 0xffffu : rest);
+            const uint32_t cs = t != 0 ? hdr : (lraw >= 0x7fff0000u ? 0x7fffffffu : hdr + lraw + 1);
+            // the chain of starts from ip
+            const uint32_t avail = min(32u, slen - ip);
+            uint32_t pos = 0, mask = 0;
             while (pos < avail) {
-                const uint32_t bit = 1u << (pos >> 1);
-                if (pos & 1) mskb |= bit;
-                else mska |= bit;
-                pos += __shfl_sync(FULL, (pos & 1) ? eb.cs : ea.cs, pos >> 1);
+                mask |= 1u << pos;
+                pos += __shfl_sync(FULL, cs, pos);
             }
-            const bool sa = (mska >> lane) & 1u, sb = (mskb >> lane) & 1u;
-            // lengths clamped in the scan (32 starts of at most 2^26 cannot wrap); the one
+            const bool start = (mask >> lane) & 1u;
+            // lengths clamped in the scan (16 starts of at most 2^26 cannot wrap); the one
             // element that may be longer, a long literal, is the round's last start
-            const uint32_t ma = sa ? min(ea.len, 1u << 26) : 0, mb = sb ? min(eb.len, 1u << 26) : 0;
-            uint32_t incl = ma + mb;
+            uint32_t mylen = start ? min(len, 1u << 26) : 0, incl = mylen;
             for (int d = 1; d < 32; d <<= 1) {
                 const uint32_t y = __shfl_up_sync(FULL, incl, d);
                 if (lane >= d) incl += y;
             }
-            const uint32_t xa = incl - ma - mb, xb = xa + ma;  // round-relative output positions
+            const uint32_t excl = incl - mylen;  // round-relative output position
             uint32_t total = __shfl_sync(FULL, incl, 31);
-            const uint32_t pa = ip + 2u * (uint32_t)lane, pb = pa + 1;  // below slen for a start
-            const uint32_t rem = dlen - op;
-            // elements after the last output byte are ignored; for the others op + x < dlen
-            const bool la = sa && xa < rem, lb = sb && xb < rem;
-            const uint32_t oa = op + xa, ob = op + xb;
-            const bool mybad = (la && (ea.cs > slen - pa || ea.len == 0 || ea.len > rem - xa ||
-                                       (ea.t != 0 && (ea.off == 0 || ea.off > oa)))) ||
-                               (lb && (eb.cs > slen - pb || eb.len == 0 || eb.len > rem - xb ||
-                                       (eb.t != 0 && (eb.off == 0 || eb.off > ob))));
+            const uint32_t p = ip + (uint32_t)lane;  // compressed position of this lane's tag
+            const uint64_t o = (uint64_t)op + excl;
+            const bool live = start && o < dlen;  // elements after the last output byte are ignored
+            const bool mybad = live && ((uint64_t)p + cs > slen || len == 0 || o + len > dlen ||
+                                        (t != 0 && (off == 0 || off > o)));
             if (__any_sync(FULL, mybad)) {
                 bad = true;
                 break;
             }
-            if (total > rem) total = rem;
-            const bool longa = la && ea.t == 0 && ea.len > PQ_INF_LONG;
-            const bool longb = lb && eb.t == 0 && eb.len > PQ_INF_LONG;
-            const uint32_t lmask = __ballot_sync(FULL, longa || longb);
+            // outputs past dlen (trailing elements) and the long literal are not mapped
+            if (total > dlen - op) total = dlen - op;
+            const uint32_t lmask = __ballot_sync(FULL, live && t == 0 && len > PQ_INF_LONG);
             uint32_t mapped = total, lit_at = 0, lit_len = 0, lit_src = 0;
             if (lmask) {
                 const int ll = __ffs(lmask) - 1;
-                const uint32_t x = longa ? xa : xb, ln = longa ? ea.len : eb.len, q = longa ? pa + ea.hdr : pb + eb.hdr;
-                mapped = __shfl_sync(FULL, x, ll);
-                lit_len = __shfl_sync(FULL, ln, ll);
-                lit_src = __shfl_sync(FULL, q, ll);
+                mapped = __shfl_sync(FULL, excl, ll);
+                lit_len = __shfl_sync(FULL, len, ll);
+                lit_src = __shfl_sync(FULL, p + hdr, ll);
                 lit_at = op + mapped;
                 total = mapped + lit_len;
             }
-            // each element's byte r comes from base + (r mod per): a literal's from its
-            // compressed bytes (PQ_INF_LIT set), a copy's from the output
-            const uint32_t basea = ea.t == 0 ? PQ_INF_LIT | (pa + ea.hdr) : oa - ea.off;
-            const uint32_t baseb = eb.t == 0 ? PQ_INF_LIT | (pb + eb.hdr) : ob - eb.off;
-            // an overlapping copy (offset below its length, so below 64) repeats its first
-            // `offset` bytes: its period, else 0
-            const uint32_t pera = la && ea.t != 0 && ea.off < ea.len ? ea.off : 0;
-            const uint32_t perb = lb && eb.t != 0 && eb.off < eb.len ? eb.off : 0;
-            const bool periodic = __any_sync(FULL, (pera | perb) != 0);
-            for (uint32_t k0 = 0; k0 < mapped; k0 += 32) {
-                uint32_t k = k0 + (uint32_t)lane;  // the round-relative output byte to resolve
-                bool want = k < mapped;
-                uint32_t s = 0;
-                for (;;) {
-                    // the lane whose elements cover byte k: the first with incl > k
-                    uint32_t lo = 0;
-#pragma unroll
-                    for (int st = 16; st > 0; st >>= 1)
-                        if (__shfl_sync(FULL, incl, lo + st - 1) <= k) lo += st;
-                    const uint32_t ex = __shfl_sync(FULL, xa, lo), mal = __shfl_sync(FULL, ma, lo);
-                    const uint32_t ba = __shfl_sync(FULL, basea, lo), bb = __shfl_sync(FULL, baseb, lo);
-                    uint32_t qa = 0, qb = 0;
-                    if (periodic) {  // warp-uniform
-                        qa = __shfl_sync(FULL, pera, lo);
-                        qb = __shfl_sync(FULL, perb, lo);
-                    }
-                    if (want) {
-                        const bool inb = k - ex >= mal;
-                        uint32_t r = inb ? k - ex - mal : k - ex;
-                        const uint32_t per = inb ? qb : qa;
-                        if (r >= per && per) {  // r < 64, per < 64: r mod per through a float quotient
-                            r -= per * __float2uint_rz(__fdividef((float)r, (float)per));
-                            if (r >= per) r -= per;
-                        }
-                        s = (inb ? bb : ba) + r;
-                        // a copy whose source lies in this round resolves that byte next
-                        want = !(s & PQ_INF_LIT) && s >= op;
-                        if (want) k = s - op;
-                    }
-                    if (!__any_sync(FULL, want)) break;
+            if (mapped > PQ_INF_MAP) {  // unreachable: 16 starts of at most 64 bytes
+                bad = true;
+                break;
+            }
+            if (start && excl < mapped) {
+                // a literal's byte b comes from q + b; a copy's from o - off + (b mod off)
+                const uint32_t base = t == 0 ? PQ_INF_LIT | (p + hdr) : (uint32_t)o - off;
+                const uint32_t per = t == 0 ? 0xffffffffu : off;
+                for (uint32_t b = 0, r = 0; b < len; b++) {
+                    map[excl + b] = base + r;
+                    r = r + 1 == per ? 0 : r + 1;
                 }
-                if (k0 + lane < mapped)
-                    dst[op + k0 + lane] = (s & PQ_INF_LIT) ? __ldg(src + (s & ~PQ_INF_LIT)) : dst[s];
+            }
+            __syncwarp();
+            for (uint32_t k = lane; k < mapped; k += 32) {
+                uint32_t s = map[k];
+                while (!(s & PQ_INF_LIT) && s >= op) s = map[s - op];
+                dst[op + k] = (s & PQ_INF_LIT) ? __ldg(src + (s & ~PQ_INF_LIT)) : dst[s];
             }
             if (lit_len) {
                 for (uint32_t b = lane; b < lit_len; b += 32) dst[lit_at + b] = __ldg(src + lit_src + b);
@@ -2262,14 +2217,15 @@ __device__ __forceinline__ void pq_inflate_piece(const uint8_t *__restrict__ fil
 // that the long pages start early and no warp idles beside a long one.
 __global__ void __launch_bounds__(256) k_pq_inflate(const uint8_t *__restrict__ file, InflateJob *jobs,
                                                     uint32_t n, uint8_t *img, uint32_t *lvl, Ctl *ctl) {
-    const int lane = threadIdx.x & 31;
+    __shared__ uint32_t s_map[8][PQ_INF_MAP];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t *next = (uint32_t *)(jobs + n);
     for (;;) {
         uint32_t j = 0;
         if (lane == 0) j = atomicAdd(next, 1u);
         j = __shfl_sync(FULL, j, 0);
         if (j >= n) return;  // the whole warp
-        pq_inflate_piece(file, jobs[j], img, lvl, ctl, lane);
+        pq_inflate_piece(file, jobs[j], img, lvl, ctl, s_map[warp], lane);
     }
 }
 
