@@ -206,8 +206,8 @@ struct gb_pq_file {
     std::vector<uint32_t> idx_col_pages;  // [(rg * n_cols + col) * 2] = {begin, end}
     // device buffers of gb_pq_dict_sum, kept (grow-only) for the next call
     std::mutex ds_mu;
-    void *ds_buf[10] = {};
-    size_t ds_cap[10] = {};
+    void *ds_buf[11] = {};
+    size_t ds_cap[11] = {};
 };
 
 static gb_status pq_corrupt(const char *what) {
@@ -1542,12 +1542,12 @@ __device__ __forceinline__ void block_add_i128(__int128 x, u64 cnt, u64 *out3) {
 // costs one atomic.  PLAIN pages: their values and count go to
 // part[3 * page].  A page with NULLs sets *nulls (the reference then takes
 // the fused path).
-__global__ void k_pq_dict_hist(const uint8_t *file, const DPage *pages, const DRun *runs, const uint32_t *page_runs,
-                               const uint32_t *page_group, const DHGroup *groups, uint32_t *hist, u64 *part,
-                               uint32_t *nulls) {
-    const uint32_t p = blockIdx.x;
+__global__ void k_pq_dict_hist(const uint8_t *file, const DPage *pages, const uint32_t *pidx, const DRun *runs,
+                               const uint32_t *page_runs, const uint32_t *page_group, const DHGroup *groups,
+                               uint32_t *hist, u64 *part, uint32_t *nulls) {
+    const uint32_t p = pidx ? pidx[blockIdx.x] : blockIdx.x;  // pidx: the column's pages in a file's page index
     const DPage pg = pages[p];
-    u64 *out3 = part + 3 * (u64)p;
+    u64 *out3 = part + 3 * (u64)blockIdx.x;
     if (pg.def_bytes && page_runs[PQ_PR * p + 3] != pg.n_values) {
         if (threadIdx.x == 0) {
             atomicOr(nulls, 1u);
@@ -1559,7 +1559,7 @@ __global__ void k_pq_dict_hist(const uint8_t *file, const DPage *pages, const DR
     if (pg.kind == 1) {
         const uint32_t nr = page_runs[PQ_PR * p], bw = page_runs[PQ_PR * p + 1];
         const DRun *rr = runs + pg.run_base;
-        const DHGroup G = groups[page_group[p]];
+        const DHGroup G = groups[page_group[blockIdx.x]];
         uint32_t *h = hist + G.hist_base;
         const uint32_t lane = threadIdx.x & 31, nw = blockDim.x >> 5, w = threadIdx.x >> 5;
         const uint32_t per = (total + nw - 1) / nw;
@@ -1746,9 +1746,23 @@ gb_status gb_pq_dict_sum(gb_pq_file *f, uint32_t col, uint32_t rg_begin, uint32_
     auto done = [&](gb_status r) { return r; };
     if (copy && cudaMemcpyAsync(copy, f->host + lo, hi - lo, cudaMemcpyHostToDevice, st) != cudaSuccess)
         return done(cuda_fail(cudaGetLastError(), "cudaMemcpyAsync"));
-    if ((s = pq_page_table(f, PqView{&f->chunks, &f->pages}, rg_begin, rg_end, cols, 1, base, nullptr, pages, jobs,
-                           col_pages, run_total)))
+    // a resident uncompressed file: its page index (descriptors and run
+    // tables, built once for every column; a file it cannot index is tabled
+    // per call)
+    const bool indexed = mem == GB_MEM_DEVICE && !f->compressed && pq_build_index(f, st) == GB_OK;
+    std::vector<uint32_t> pidx;
+    if (indexed) {
+        const size_t nfc = f->cols.size();
+        for (uint32_t g = rg_begin; g < rg_end; g++) {
+            col_pages.push_back((uint32_t)pidx.size());
+            for (uint32_t q = f->idx_col_pages[2 * (g * nfc + col)]; q < f->idx_col_pages[2 * (g * nfc + col) + 1]; q++)
+                pidx.push_back(q);
+            col_pages.push_back((uint32_t)pidx.size());
+        }
+    } else if ((s = pq_page_table(f, PqView{&f->chunks, &f->pages}, rg_begin, rg_end, cols, 1, base, nullptr, pages,
+                                  jobs, col_pages, run_total))) {
         return done(s);
+    }
     for (uint32_t g = rg_begin; g < rg_end; g++) {
         const PqChunk &ch = f->chunks[g][col];
         if (hist_n + ch.dict_n > 0xffffffffull) return done(GB_ERR_UNSUPPORTED);
@@ -1757,38 +1771,46 @@ gb_status gb_pq_dict_sum(gb_pq_file *f, uint32_t col, uint32_t rg_begin, uint32_
         const uint32_t k = g - rg_begin;
         for (uint32_t q = col_pages[2 * k]; q < col_pages[2 * k + 1]; q++) page_group.push_back(k);
     }
-    const size_t np = pages.size(), ng = groups.size();
+    const size_t np = indexed ? pidx.size() : pages.size(), ng = groups.size();
     cudaError_t e;
     if ((s = grow(B[0], C[0], np * sizeof(DPage) + 16)) || (s = grow(B[1], C[1], (size_t)run_total * sizeof(DRun) + 16)) ||
         (s = grow(B[2], C[2], np * PQ_PR * 4 + 16)) || (s = grow(B[3], C[3], jobs.size() * sizeof(RunJob) + 16)) ||
         (s = grow(B[4], C[4], np * 4 + 16)) || (s = grow(B[5], C[5], ng * sizeof(DHGroup) + 16)) ||
         (s = grow(B[6], C[6], hist_n * 4 + 16)) || (s = grow(B[7], C[7], (np + ng) * 24 + 16)) ||
-        (s = grow(B[8], C[8], sizeof(Ctl))))
+        (s = grow(B[8], C[8], sizeof(Ctl))) || (s = grow(B[10], C[10], pidx.size() * 4 + 16)))
         return s;
     d_pages = B[0], d_runs = B[1], d_page_runs = B[2], d_jobs = B[3], d_pg = B[4], d_groups = B[5], d_hist = B[6],
     d_part = B[7], d_ctl = B[8];
-    if ((e = cudaMemcpyAsync(d_pages, pages.data(), np * sizeof(DPage), cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(RunJob), cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(d_pg, page_group.data(), np * 4, cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemcpyAsync(d_groups, groups.data(), ng * sizeof(DHGroup), cudaMemcpyHostToDevice, st)) ||
-        (e = cudaMemsetAsync(d_page_runs, 0, np * PQ_PR * 4 + 16, st)) || (e = cudaMemsetAsync(d_hist, 0, hist_n * 4 + 16, st)) ||
-        (e = cudaMemsetAsync(d_ctl, 0, sizeof(Ctl), st)))
+    if (indexed) {
+        d_pages = f->idx_pages, d_runs = f->idx_runs, d_page_runs = f->idx_page_runs;
+        if ((e = cudaMemcpyAsync(B[10], pidx.data(), pidx.size() * 4, cudaMemcpyHostToDevice, st)))
+            return done(cuda_fail(e, "cudaMemcpyAsync (dictionary histogram)"));
+    } else if ((e = cudaMemcpyAsync(d_pages, pages.data(), np * sizeof(DPage), cudaMemcpyHostToDevice, st)) ||
+               (e = cudaMemcpyAsync(d_jobs, jobs.data(), jobs.size() * sizeof(RunJob), cudaMemcpyHostToDevice, st)) ||
+               (e = cudaMemsetAsync(d_page_runs, 0, np * PQ_PR * 4 + 16, st))) {
         return done(cuda_fail(e, "cudaMemcpyAsync (dictionary histogram)"));
-    if (!jobs.empty())
+    }
+    if ((e = cudaMemcpyAsync(d_pg, page_group.data(), np * 4, cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemcpyAsync(d_groups, groups.data(), ng * sizeof(DHGroup), cudaMemcpyHostToDevice, st)) ||
+        (e = cudaMemsetAsync(d_hist, 0, hist_n * 4 + 16, st)) || (e = cudaMemsetAsync(d_ctl, 0, sizeof(Ctl), st)))
+        return done(cuda_fail(e, "cudaMemcpyAsync (dictionary histogram)"));
+    if (!jobs.empty()) {  // a batch's own run tables (the file in host memory)
         k_pq_runs<<<(unsigned)jobs.size(), 128, 0, st>>>(dfile, (const DPage *)d_pages, (const RunJob *)d_jobs,
                                                          (DRun *)d_runs, (uint32_t *)d_page_runs, (Ctl *)d_ctl);
-    Ctl c;
-    if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&c, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st)) ||
-        (e = cudaStreamSynchronize(st)))
-        return done(cuda_fail(e, "k_pq_runs"));
-    if ((s = pq_fail_if_err(c))) return done(s);
+        Ctl c;
+        if ((e = cudaGetLastError()) || (e = cudaMemcpyAsync(&c, d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st)) ||
+            (e = cudaStreamSynchronize(st)))
+            return done(cuda_fail(e, "k_pq_runs"));
+        if ((s = pq_fail_if_err(c))) return done(s);
+    }
     uint32_t *nulls = (uint32_t *)d_ctl;  // the control block's first word, zeroed above
     if ((e = cudaMemsetAsync(nulls, 0, 4, st))) return done(cuda_fail(e, "cudaMemsetAsync"));
     if (np)
-        k_pq_dict_hist<<<(unsigned)np, 256, 0, st>>>(dfile, (const DPage *)d_pages, (const DRun *)d_runs,
-                                                    (const uint32_t *)d_page_runs, (const uint32_t *)d_pg,
-                                                    (const DHGroup *)d_groups, (uint32_t *)d_hist, (u64 *)d_part,
-                                                    nulls);
+        k_pq_dict_hist<<<(unsigned)np, 256, 0, st>>>(dfile, (const DPage *)d_pages,
+                                                    indexed ? (const uint32_t *)B[10] : nullptr,
+                                                    (const DRun *)d_runs, (const uint32_t *)d_page_runs,
+                                                    (const uint32_t *)d_pg, (const DHGroup *)d_groups,
+                                                    (uint32_t *)d_hist, (u64 *)d_part, nulls);
     k_pq_dict_reduce<<<(unsigned)ng, 256, 0, st>>>(dfile, (const DHGroup *)d_groups, (const uint32_t *)d_hist,
                                                   (u64 *)d_part + 3 * np);
     std::vector<u64> part(3 * (np + ng));
