@@ -31,6 +31,7 @@
 #include <unordered_map>
 #include <vector>
 
+#include "gb_zstd.h"
 #include "gb_agg_host.h"
 #include "gb_kernels.cuh"
 
@@ -1631,9 +1632,9 @@ gb_status gb_pq_open(const uint8_t *bytes, uint64_t size, gb_pq_file **out) {
     gb_status s = parse_footer(f);
     for (uint32_t g = 0; !s && g < f->chunks.size(); g++)
         for (uint32_t c = 0; !s && c < f->cols.size(); c++) {
-            if (f->chunks[g][c].codec != 0 && f->chunks[g][c].codec != 1) {
+            if (f->chunks[g][c].codec != 0 && f->chunks[g][c].codec != 1 && f->chunks[g][c].codec != 6) {
                 set_error("Parquet column chunks compressed with codec %d are not supported on the GPU path "
-                          "(uncompressed and SNAPPY are)", f->chunks[g][c].codec);
+                          "(uncompressed, SNAPPY and ZSTD are)", f->chunks[g][c].codec);
                 s = GB_ERR_UNSUPPORTED;
                 break;
             }
@@ -1881,6 +1882,8 @@ struct PqScratch {
     size_t img_cap = 0, ijobs_cap = 0, ilvl_cap = 0;
     void *views = nullptr;  // per chunk of the batch: its view (k_pq_views)
     size_t views_cap = 0;
+    void *zjobs = nullptr, *zscratch = nullptr;  // ZSTD pieces and their decoders' tables
+    size_t zjobs_cap = 0, zscratch_cap = 0;
 };
 
 static gb_status grow(void *&p, size_t &cap, size_t need) {
@@ -1920,7 +1923,8 @@ void gb_pq_release_scratch(gb_agg *h) {
         g_pq_scratch.erase(it);
     }
     for (void *p : {s->file_dev, s->pages, s->runs, s->page_runs, s->dict_pages, s->col_pages, s->chunks, s->ctl,
-                    s->dicts, s->dsrc, s->doffs, s->dbytes, s->dmatch, s->dcounts, s->img, s->ijobs, s->ilvl, s->views})
+                    s->dicts, s->dsrc, s->doffs, s->dbytes, s->dmatch, s->dcounts, s->img, s->ijobs, s->ilvl, s->views, s->zjobs,
+                    s->zscratch})
         if (p) cudaFree(p);
     for (void *p : s->out)
         if (p) cudaFree(p);
@@ -2065,9 +2069,9 @@ static gb_status pq_varchar_dict(gb_agg *h, const PqView &V, PqScratch *S, const
 
 // ------------------------------------------------ compressed column chunks
 // One piece of a batch's decompressed image: `src_len` bytes at file offset
-// `src` copied (mode 0) or inflated from a raw Snappy block (mode 1, the
-// codec of parquet.cpp:44-90, the vendored snappy 1.2.1) into `dst_len`
-// bytes at image offset `dst`.  lvl_slot != ~0: the piece is a page v1 of an
+// `src` copied (mode 0), inflated from a raw Snappy block (mode 1, the codec
+// of parquet.cpp:44-90, the vendored snappy 1.2.1) or from ZSTD frames (mode
+// 2, parquet.cpp:693-736) into `dst_len` bytes at image offset `dst`.  lvl_slot != ~0: the piece is a page v1 of an
 // OPTIONAL column, whose first 4 bytes (the level length) go to lvl[slot].
 struct InflateJob {
     uint64_t src, dst;
@@ -2251,6 +2255,31 @@ __global__ void __launch_bounds__(256) k_pq_inflate(const uint8_t *__restrict__ 
     }
 }
 
+// ZSTD pieces (mode 2): one thread per piece, claimed from a counter (the
+// word after the last job) longest first; each thread decodes with its own
+// 9.5 KB of tables in `scratch`.  A frame that does not decode to exactly
+// dst_len bytes sets ERR_CORRUPT.
+__global__ void __launch_bounds__(128) k_pq_unzstd(const uint8_t *__restrict__ file, InflateJob *jobs, uint32_t n,
+                                                   uint8_t *img, uint32_t *lvl, Ctl *ctl, gbz::ZsScratch *scratch) {
+    gbz::ZsScratch &Z = scratch[blockIdx.x * (u64)blockDim.x + threadIdx.x];
+    uint32_t *next = (uint32_t *)(jobs + n);
+    for (;;) {
+        const uint32_t j = atomicAdd(next, 1u);
+        if (j >= n) return;
+        const InflateJob J = jobs[j];
+        uint8_t *dst = img + J.dst;
+        const int64_t got = gbz::zstd_decompress(file + J.src, J.src_len, dst, J.dst_len, Z);
+        const bool bad = got != (int64_t)J.dst_len;
+        if (bad) atomicOr(&ctl->err, (u32)ERR_CORRUPT);
+        if (J.lvl_slot != ~0u) {
+            uint32_t l4 = ~0u;  // too short to hold a level length: corrupt
+            if (!bad && J.dst_len >= 4)
+                l4 = (uint32_t)dst[0] | ((uint32_t)dst[1] << 8) | ((uint32_t)dst[2] << 16) | ((uint32_t)dst[3] << 24);
+            lvl[J.lvl_slot] = l4;
+        }
+    }
+}
+
 // Build a batch's decompressed image: per live row group and mapped file
 // column, an uncompressed chunk is copied whole, a SNAPPY chunk's
 // dictionary page and data pages are inflated (page v2 levels copied as
@@ -2290,9 +2319,10 @@ static gb_status pq_inflate_batch(gb_agg *h, const gb_pq_file *f, PqScratch *S, 
                 }
                 continue;
             }
+            const uint32_t cm = ch.codec == 6 ? 2u : 1u;  // ZSTD or SNAPPY
             if (ch.dict_off >= 0) {
                 const uint64_t at = place(ch.dict_bytes);
-                jobs.push_back({ch.dict_src - base, at, ch.dict_src_bytes, ch.dict_bytes, 1u, ~0u});
+                jobs.push_back({ch.dict_src - base, at, ch.dict_src_bytes, ch.dict_bytes, cm, ~0u});
                 ch.dict_off = (int64_t)at;
             }
             for (uint32_t p = ch.page_begin; p < ch.page_end; p++) {
@@ -2303,7 +2333,7 @@ static gb_status pq_inflate_batch(gb_agg *h, const gb_pq_file *f, PqScratch *S, 
                     pg.def_off = at;
                     pg.def_bytes = pg.lvl_copy;
                 }
-                jobs.push_back({pg.src_off - base, at + pg.lvl_copy, pg.src_bytes, pg.raw_bytes, pg.stored ? 0u : 1u,
+                jobs.push_back({pg.src_off - base, at + pg.lvl_copy, pg.src_bytes, pg.raw_bytes, pg.stored ? 0u : cm,
                                 pg.lvl_pending ? (uint32_t)pending.size() : ~0u});
                 if (pg.lvl_pending) pending.push_back(p);
                 pg.off = at + pg.lvl_copy;
@@ -2311,17 +2341,44 @@ static gb_status pq_inflate_batch(gb_agg *h, const gb_pq_file *f, PqScratch *S, 
             }
         }
     }
+    // the ZSTD pieces in a list of their own (a kernel of their own)
+    std::vector<InflateJob> zjobs;
+    for (size_t k = 0; k < jobs.size();) {
+        if (jobs[k].mode == 2) {
+            zjobs.push_back(jobs[k]);
+            jobs[k] = jobs.back();
+            jobs.pop_back();
+        } else {
+            k++;
+        }
+    }
     // longest first (a stored piece costs about a sixteenth of an inflated
-    // one per byte), then a zero word: the kernel's claim counter
-    std::stable_sort(jobs.begin(), jobs.end(), [](const InflateJob &a, const InflateJob &b) {
+    // one per byte), then a zero word: the kernels' claim counters
+    auto longest = [](const InflateJob &a, const InflateJob &b) {
         return (a.mode ? (uint64_t)a.dst_len * 16 : a.dst_len) > (b.mode ? (uint64_t)b.dst_len * 16 : b.dst_len);
-    });
-    const size_t n_jobs = jobs.size();
+    };
+    std::stable_sort(jobs.begin(), jobs.end(), longest);
+    std::stable_sort(zjobs.begin(), zjobs.end(), longest);
+    const size_t n_jobs = jobs.size(), n_z = zjobs.size();
     jobs.push_back({0, 0, 0, 0, 0, 0});
+    zjobs.push_back({0, 0, 0, 0, 0, 0});
+    const size_t z_threads = std::min<size_t>(((n_z + 127) / 128) * 128, (size_t)sm_count() * 64);
     gb_status s;
     if ((s = grow(S->img, S->img_cap, pos + 64)) || (s = grow(S->ijobs, S->ijobs_cap, jobs.size() * sizeof(InflateJob) + 16)) ||
-        (s = grow(S->ilvl, S->ilvl_cap, pending.size() * 4 + 16)))
+        (s = grow(S->ilvl, S->ilvl_cap, pending.size() * 4 + 16)) ||
+        (n_z && ((s = grow(S->zjobs, S->zjobs_cap, zjobs.size() * sizeof(InflateJob) + 16)) ||
+                 (s = grow(S->zscratch, S->zscratch_cap, z_threads * sizeof(gbz::ZsScratch))))))
         return s;
+    if (n_z) {
+        GB_CUDA(cudaMemcpyAsync(S->zjobs, zjobs.data(), zjobs.size() * sizeof(InflateJob), cudaMemcpyHostToDevice, st));
+        gb_prof_mark *pm = gb_agg_prof_begin(h, "k_pq_unzstd", st);
+        k_pq_unzstd<<<(unsigned)(z_threads / 128), 128, 0, st>>>(dfile, (InflateJob *)S->zjobs, (uint32_t)n_z,
+                                                                  (uint8_t *)S->img, (uint32_t *)S->ilvl, dctl,
+                                                                  (gbz::ZsScratch *)S->zscratch);
+        gb_agg_prof_end(h, pm, st);
+        GB_CUDA(cudaGetLastError());
+        gb_agg_count_launch(h, 1);
+    }
     if (n_jobs) {
         GB_CUDA(cudaMemcpyAsync(S->ijobs, jobs.data(), jobs.size() * sizeof(InflateJob), cudaMemcpyHostToDevice, st));
         gb_prof_mark *pm = gb_agg_prof_begin(h, "k_pq_inflate", st);

@@ -35,6 +35,9 @@ CASES = {
     # pyarrow's default codec: SNAPPY pages (inflated on the GPU)
     "pa_nulls_v1_snappy": dict(version="1.0", dictionary=True, compression="snappy"),
     "pa_nulls_v2_snappy": dict(version="2.0", dictionary=["key"], compression="snappy"),
+    # ZSTD pages (decoded on the GPU, one thread per page)
+    "pa_nulls_v1_zstd": dict(version="1.0", dictionary=True, compression="zstd"),
+    "pa_nulls_v2_zstd": dict(version="2.0", dictionary=["key"], compression="zstd"),
 }
 
 
@@ -111,6 +114,9 @@ def main():
            dictionary_pagesize_limit=4 * 1024, data_page_version="2.0")
     _write("pa_varchar_fallback_snappy", t2, compression="snappy", row_group_size=8_000, data_page_size=4 * 1024,
            dictionary_pagesize_limit=4 * 1024)
+    _write("pa_varchar_nulls_zstd", t2, compression="zstd", row_group_size=8_000, data_page_size=4 * 1024)
+    _write("pa_varchar_fallback_zstd", t2, compression="zstd", row_group_size=8_000, data_page_size=4 * 1024,
+           dictionary_pagesize_limit=4 * 1024, data_page_version="2.0")
     t3 = pa.table({"k": pa.array(np.arange(1000, dtype=np.int32) % 7), "v": pa.array(np.arange(1000, dtype=np.int64))})
     _write("pa_optional_nonnull", t3)
     t4 = pa.table({"c": pa.array(int64_column(), pa.int64())})

@@ -132,7 +132,8 @@ import make_pyarrow_files as paf  # noqa: E402
 def test_pyarrow_files_with_nulls(name):
     """Files written by pyarrow (an independent writer: OPTIONAL columns with
     definition levels, data page v1 and v2, its own page splits, dictionary
-    fallback to PLAIN pages; committed under tests/golden/) through the GPU
+    fallback to PLAIN pages, SNAPPY and ZSTD pages; committed under
+    tests/golden/) through the GPU
     decoder: NULLs in the key, the filter column and the value columns,
     against the oracle on the same logical columns."""
     data = paf.load(name)
@@ -148,7 +149,8 @@ def test_pyarrow_files_with_nulls(name):
 
 
 @pytest.mark.parametrize("name", ["pa_varchar_nulls", "pa_varchar_nulls_snappy", "pa_varchar_plain",
-                                  "pa_varchar_fallback_v2", "pa_varchar_fallback_snappy"])
+                                  "pa_varchar_fallback_v2", "pa_varchar_fallback_snappy",
+                                  "pa_varchar_nulls_zstd", "pa_varchar_fallback_zstd"])
 def test_pyarrow_varchar_key_with_nulls(name):
     """A pyarrow-written VARCHAR key with NULL keys (one NULL group) and a
     nullable value column; a LIKE and an equality on the key; dictionary
@@ -292,6 +294,23 @@ def test_corrupt_snappy_block_is_reported():
     try:
         with pytest.raises(capi.GbError) as e:
             capi.ingest_parquet(g, pf, [0])
+        assert e.value.status == 6  # GB_ERR_CORRUPT
+    finally:
+        g.close()
+        pf.close()
+
+
+def test_corrupt_zstd_page_is_reported():
+    """A ZSTD page whose frame is damaged (its magic number zeroed) is
+    reported as a corrupt file, not decoded."""
+    data = bytearray(paf.load("pa_nulls_v1_zstd"))
+    at = bytes(data).index(b"\x28\xb5\x2f\xfd", 4)  # the first frame
+    data[at:at + 4] = bytes(4)
+    pf = capi.ParquetFile(bytes(data))
+    g = capi.GroupBy([INTEGER, SMALLINT, BIGINT, DOUBLE], [0], [("count_star", -1)], nullable=[0, 1, 2, 3])
+    try:
+        with pytest.raises(capi.GbError) as e:
+            capi.ingest_parquet(g, pf, [0, 1, 2, 3])
         assert e.value.status == 6  # GB_ERR_CORRUPT
     finally:
         g.close()

@@ -301,7 +301,7 @@ def test_pyarrow_fixtures_match_their_columns():
         pf.close()
     strs, _, v, kn, vn = paf.varchar_columns()
     for name in ("pa_varchar_nulls", "pa_varchar_nulls_snappy", "pa_varchar_plain", "pa_varchar_fallback_v2",
-                 "pa_varchar_fallback_snappy"):
+                 "pa_varchar_fallback_snappy", "pa_varchar_nulls_zstd", "pa_varchar_fallback_zstd"):
         t = pq_.read_table(io.BytesIO(paf.load(name)))
         got = t.column("name").to_pylist()
         assert [None if n else s_.decode() for s_, n in zip(strs, kn)] == got
