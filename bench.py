@@ -60,7 +60,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=20_000_000)
     ap.add_argument("--workload", default="zipf100m", choices=["zipf100m", "plain1m", "batch256", "serve",
                                                                       "parquet200m", "parquet200m_snappy",
-                                                                      "dictsum200m", "distinct100m"])
+                                                                      "parquet200m_zstd", "dictsum200m",
+                                                                      "distinct100m"])
     ap.add_argument("--pq-rows", type=int, default=200_000_000, help="parquet200m: rows in the file")
     ap.add_argument("--tables", type=int, default=256)
     ap.add_argument("--duration", type=float, default=120.0, help="serve: seconds of Poisson arrivals")
@@ -1067,10 +1068,13 @@ def run_parquet(args):
     if args.impl == "reference" and rank != 0:
         return  # rank 0 alone runs the reference arm
     rows = args.pq_rows
-    snappy = args.workload == "parquet200m_snappy"
+    codec = {"parquet200m_snappy": "snappy", "parquet200m_zstd": "zstd"}.get(args.workload)
+    snappy = codec is not None  # compressed pages: decompressed on the GPU per batch
+    inflate = "k_pq_unzstd" if codec == "zstd" else "k_pq_inflate"
+    cname = {None: "UNCOMPRESSED", "snappy": "SNAPPY", "zstd": "ZSTD"}[codec]
     t0 = time.time()
     data, key, f, v = pq.filter_groupby_file(n_rows=rows, row_group_rows=1_000_000,
-                                             codec="snappy" if snappy else None)
+                                             codec=codec)
     raw_bytes = len(pq.filter_groupby_file(n_rows=rows, row_group_rows=1_000_000)[0]) if snappy else len(data)
     gen_s = time.time() - t0
     if args.impl == "reference":
@@ -1134,12 +1138,12 @@ def run_parquet(args):
     # compressed pages and writes the decompressed image
     achieved = raw_bytes / (scan_ms / 1e3) / 1e9
     if snappy:
-        inf_ms = prof.get("k_pq_inflate", float("nan"))
+        inf_ms = prof.get(inflate, float("nan"))
         if inf_ms > scan_ms:
             scan_ms = inf_ms
             achieved = (file_bytes + raw_bytes) / (inf_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "traffic": None, "kernel": ("k_pq_inflate" if snappy and scan_ms == prof.get("k_pq_inflate")
+                "traffic": None, "kernel": (inflate if snappy and scan_ms == prof.get(inflate)
                                             else "k_pq_scan"), "kernel_ms": scan_ms,
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
                 "step_GBps": file_bytes / (ms / 1e3) / 1e9, "step_frac": file_bytes / (ms / 1e3) / 1e9 / hbm_peak,
@@ -1173,13 +1177,13 @@ def run_parquet(args):
         cpu = {"value": n / dt, "unit": "rows/s", "cores": thr, "kind": "port",
                "sample": "first %d decoded rows, filter + GROUP BY (no page decode), %d threads" % (n, thr)}
     line = {"metric": "fused Parquet decode+filter+GROUP BY rows/s (200M rows, 1M-row RGs%s)" % (
-                ", SNAPPY" if snappy else ""),
+                ", " + cname if snappy else ""),
             "value": rows / (ms / 1e3), "unit": "rows/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32+int64", "data": "synthetic",
-            "config": {"workload": "parquet-filter-groupby-%dM%s" % (rows // 1_000_000, "-snappy" if snappy else ""),
+            "config": {"workload": "parquet-filter-groupby-%dM%s" % (rows // 1_000_000, "-" + codec if snappy else ""),
                        "rows": rows, "file_bytes": file_bytes, "page_bytes_uncompressed": raw_bytes,
-                       "codec": "SNAPPY" if snappy else "UNCOMPRESSED", "row_group_rows": 1_000_000, "dict": 65_536,
+                       "codec": cname, "row_group_rows": 1_000_000, "dict": 65_536,
                        "predicate": "f < 100", "l2": "file %.1f GB > L2 129 MB (no flush needed)" % (file_bytes / 1e9),
                        "datagen_s": round(gen_s, 1)},
             "parity": "bit-exact vs oracle" if ok else "MISMATCH vs oracle",
@@ -1210,7 +1214,7 @@ def run_parquet_reference(args, key, f, v, rows):
     per = statistics.mean(times)
     val = n / per
     line = {"impl": "reference", "metric": "fused Parquet decode+filter+GROUP BY rows/s (200M rows, 1M-row RGs%s)" % (
-                ", SNAPPY" if args.workload == "parquet200m_snappy" else ""),
+                {"parquet200m_snappy": ", SNAPPY", "parquet200m_zstd": ", ZSTD"}.get(args.workload, "")),
             "value": val, "unit": "rows/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": per * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "int32+int64", "data": "synthetic",
@@ -1508,7 +1512,7 @@ def main():
     if args.workload == "serve":
         run_serve(args)
         return
-    if args.workload in ("parquet200m", "parquet200m_snappy"):
+    if args.workload in ("parquet200m", "parquet200m_snappy", "parquet200m_zstd"):
         run_parquet(args)
         return
     if args.workload == "dictsum200m":

@@ -2255,13 +2255,17 @@ __global__ void __launch_bounds__(256) k_pq_inflate(const uint8_t *__restrict__ 
     }
 }
 
-// ZSTD pieces (mode 2): one thread per piece, claimed from a counter (the
-// word after the last job) longest first; each thread decodes with its own
-// 9.5 KB of tables in `scratch`.  A frame that does not decode to exactly
-// dst_len bytes sets ERR_CORRUPT.
+// ZSTD pieces (mode 2): one warp per piece, claimed from a counter (the word
+// after the last job) longest first, decoded by its first lane with the
+// warp's 9.5 KB of tables in `scratch` (a frame is one serial stream;
+// pieces on the lanes of one warp would serialise on their divergent
+// branches).  The tables stay in global memory, so that 64 warps per SM
+// decode at once (in shared memory only 24 fit).  A frame that does not
+// decode to exactly dst_len bytes sets ERR_CORRUPT.
 __global__ void __launch_bounds__(128) k_pq_unzstd(const uint8_t *__restrict__ file, InflateJob *jobs, uint32_t n,
                                                    uint8_t *img, uint32_t *lvl, Ctl *ctl, gbz::ZsScratch *scratch) {
-    gbz::ZsScratch &Z = scratch[blockIdx.x * (u64)blockDim.x + threadIdx.x];
+    if ((threadIdx.x & 31) != 0) return;
+    gbz::ZsScratch &Z = scratch[(blockIdx.x * blockDim.x + threadIdx.x) >> 5];
     uint32_t *next = (uint32_t *)(jobs + n);
     for (;;) {
         const uint32_t j = atomicAdd(next, 1u);
@@ -2362,19 +2366,19 @@ static gb_status pq_inflate_batch(gb_agg *h, const gb_pq_file *f, PqScratch *S, 
     const size_t n_jobs = jobs.size(), n_z = zjobs.size();
     jobs.push_back({0, 0, 0, 0, 0, 0});
     zjobs.push_back({0, 0, 0, 0, 0, 0});
-    const size_t z_threads = std::min<size_t>(((n_z + 127) / 128) * 128, (size_t)sm_count() * 64);
+    const size_t z_blocks = std::min<size_t>((n_z + 3) / 4, (size_t)sm_count() * 16);  // 4 warps per block
     gb_status s;
     if ((s = grow(S->img, S->img_cap, pos + 64)) || (s = grow(S->ijobs, S->ijobs_cap, jobs.size() * sizeof(InflateJob) + 16)) ||
         (s = grow(S->ilvl, S->ilvl_cap, pending.size() * 4 + 16)) ||
         (n_z && ((s = grow(S->zjobs, S->zjobs_cap, zjobs.size() * sizeof(InflateJob) + 16)) ||
-                 (s = grow(S->zscratch, S->zscratch_cap, z_threads * sizeof(gbz::ZsScratch))))))
+                 (s = grow(S->zscratch, S->zscratch_cap, z_blocks * 4 * sizeof(gbz::ZsScratch))))))
         return s;
     if (n_z) {
         GB_CUDA(cudaMemcpyAsync(S->zjobs, zjobs.data(), zjobs.size() * sizeof(InflateJob), cudaMemcpyHostToDevice, st));
         gb_prof_mark *pm = gb_agg_prof_begin(h, "k_pq_unzstd", st);
-        k_pq_unzstd<<<(unsigned)(z_threads / 128), 128, 0, st>>>(dfile, (InflateJob *)S->zjobs, (uint32_t)n_z,
-                                                                  (uint8_t *)S->img, (uint32_t *)S->ilvl, dctl,
-                                                                  (gbz::ZsScratch *)S->zscratch);
+        k_pq_unzstd<<<(unsigned)z_blocks, 128, 0, st>>>(dfile, (InflateJob *)S->zjobs, (uint32_t)n_z,
+                                                         (uint8_t *)S->img, (uint32_t *)S->ilvl, dctl,
+                                                         (gbz::ZsScratch *)S->zscratch);
         gb_agg_prof_end(h, pm, st);
         GB_CUDA(cudaGetLastError());
         gb_agg_count_launch(h, 1);

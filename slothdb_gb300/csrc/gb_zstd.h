@@ -69,27 +69,56 @@ ZS_HD uint32_t zs_bits(const uint8_t *src, int64_t size, int64_t pos, int n) {
 }
 
 // A backward bit stream (FSE and Huffman streams): read from its end, below
-// the highest set bit of its last byte.
+// the highest set bit of its last byte.  The 64 bits [wlo, wlo + 64) are
+// kept in `win` (bits outside the stream as 0) and reloaded, 8 bytes at a
+// time, when a read leaves them.
 struct ZsBack {
     const uint8_t *src;
     int64_t size;
     int64_t pos;  // bits not yet read; < 0 once more were read than the stream holds
+    int64_t wlo;  // first bit of the window (a multiple of 8)
+    uint64_t win;
 };
+
+ZS_HD void zs_back_load(ZsBack &b, int64_t top) {  // a window that holds the bits below `top`
+    int64_t lo = top - 64;  // rounded up to a byte: the window still reaches `top`
+    lo = lo >= 0 ? ((lo + 7) >> 3) << 3 : -((-lo) >> 3) * 8;
+    b.wlo = lo;
+    uint64_t v = 0;
+    const int64_t b0 = lo >> 3;  // exact: lo is a multiple of 8
+    if (b0 >= 0 && b0 + 8 <= b.size) {
+        for (int k = 0; k < 8; k++) v |= (uint64_t)b.src[b0 + k] << (8 * k);
+    } else {
+        for (int k = 0; k < 8; k++) {
+            const int64_t i = b0 + k;
+            if (i >= 0 && i < b.size) v |= (uint64_t)b.src[i] << (8 * k);
+        }
+    }
+    b.win = v;
+}
 
 ZS_HD bool zs_back_init(ZsBack &b, const uint8_t *src, int64_t size) {
     b.src = src;
     b.size = size;
     if (size <= 0 || src[size - 1] == 0) return false;
     b.pos = (size - 1) * 8 + zs_highbit(src[size - 1]);
+    zs_back_load(b, b.pos);
     return true;
+}
+
+// Bits [p, p + n) of the stream, n <= 32.
+ZS_HD uint32_t zs_back_bits(ZsBack &b, int64_t p, int n) {
+    if (n == 0) return 0;
+    if (p < b.wlo || p + n > b.wlo + 64) zs_back_load(b, p + n);
+    return (uint32_t)((b.win >> (p - b.wlo)) & ((1ull << n) - 1));
 }
 
 ZS_HD uint32_t zs_read(ZsBack &b, int n) {
     b.pos -= n;
-    return zs_bits(b.src, b.size, b.pos, n);
+    return zs_back_bits(b, b.pos, n);
 }
 
-ZS_HD uint32_t zs_peek(const ZsBack &b, int n) { return zs_bits(b.src, b.size, b.pos - n, n); }
+ZS_HD uint32_t zs_peek(ZsBack &b, int n) { return zs_back_bits(b, b.pos - n, n); }
 
 // FSE decoding table of `log` accuracy from normalized counts (-1: "less
 // than one", a cell of its own at the top of the table).
@@ -341,6 +370,34 @@ ZS_HD bool zs_huf_stream(const uint8_t *src, int64_t n, const ZsScratch &S, int 
     return b.pos == 0;
 }
 
+// d[0, n) = s[0, n) copied forward.  The bytes are loaded 8 at a time
+// before they are stored (one memory round trip per 8 bytes instead of per
+// byte) when a chunk cannot read what it writes: no overlap, or a source at
+// least 8 bytes behind (`gap`), or a source ahead of the destination (the
+// literals, gap 8).  An overlapping match closer than 8 bytes repeats its
+// first `gap` bytes, loaded once.
+ZS_HD void zs_copy(uint8_t *d, const uint8_t *s, int64_t n, int64_t gap) {
+    if (gap >= 8 || gap >= n) {
+        for (int64_t i = 0; i < n; i += 8) {
+            const int64_t m = n - i < 8 ? n - i : 8;
+            uint8_t t[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                if (k < m) t[k] = s[i + k];
+#pragma unroll
+            for (int k = 0; k < 8; k++)
+                if (k < m) d[i + k] = t[k];
+        }
+        return;
+    }
+    uint8_t t[8];
+    for (int64_t k = 0; k < gap; k++) t[k] = s[k];
+    for (int64_t i = 0, r = 0; i < n; i++) {
+        d[i] = t[r];
+        r = r + 1 == gap ? 0 : r + 1;
+    }
+}
+
 // The state a frame carries from block to block.
 struct ZsFrame {
     int huf_bits;  // 0: no Huffman table yet
@@ -382,7 +439,7 @@ ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap, in
     uint8_t *lit = dst + (cap - lsize);
     if (ltype == 0) {
         if (pos + lsize > n) return false;
-        for (int64_t i = 0; i < lsize; i++) lit[i] = src[pos + i];
+        zs_copy(lit, src + pos, lsize, 8);  // src and dst are different buffers
         pos += lsize;
     } else if (ltype == 1) {
         if (pos + 1 > n) return false;
@@ -490,10 +547,10 @@ ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap, in
             if (b.pos < 0) return false;
             // execute: ll literals, then ml bytes from off back
             if (ll > lsize - lp || ll + ml > cap - *op || off == 0 || (int64_t)off > *op + ll) return false;
-            for (int64_t i = 0; i < ll; i++) dst[*op + i] = lit[lp + i];  // forward: never ahead of the literal read
+            zs_copy(dst + *op, lit + lp, ll, 8);  // forward: never ahead of the literal read
             *op += ll;
             lp += ll;
-            for (int64_t i = 0; i < ml; i++) dst[*op + i] = dst[*op + i - off];
+            zs_copy(dst + *op, dst + *op - off, ml, off);
             *op += ml;
         }
         if (b.pos != 0) return false;
@@ -550,7 +607,7 @@ ZS_HD int64_t zstd_decompress(const uint8_t *src, int64_t n, uint8_t *dst, int64
             const int64_t bsize = bh >> 3;
             if (type == 0) {  // raw
                 if (bsize > n - ip || bsize > cap - op) return -1;
-                for (int64_t i = 0; i < bsize; i++) dst[op + i] = src[ip + i];
+                zs_copy(dst + op, src + ip, bsize, 8);
                 ip += bsize;
                 op += bsize;
             } else if (type == 1) {  // RLE: one byte, bsize times

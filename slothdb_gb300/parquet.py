@@ -50,6 +50,8 @@ def _encoder():
     lib.pq_rle_encode.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_void_p]
     lib.pq_snappy_compress.restype = C.c_int64
     lib.pq_snappy_compress.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]
+    lib.pq_zstd_compress.restype = C.c_int64
+    lib.pq_zstd_compress.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p]
     _enc = lib
     return lib
 
@@ -63,6 +65,19 @@ def snappy_compress(data: bytes) -> bytes:
     got = _encoder().pq_snappy_compress(src.ctypes.data, len(data), out.ctypes.data, cap, table.ctypes.data)
     if got < 0:
         raise RuntimeError("Snappy compress buffer overflow")
+    return out[:got].tobytes()
+
+
+def zstd_compress(data: bytes) -> bytes:
+    """One ZSTD frame of `data` (the writer's ZSTD pages: greedy matches, raw
+    literals, sequences coded with the format's predefined tables)."""
+    src = np.frombuffer(data, dtype=np.uint8) if data else np.zeros(1, np.uint8)
+    cap = len(data) + len(data) // 128 + 64
+    out = np.empty(cap, dtype=np.uint8)
+    table = np.empty(1 << 16, dtype=np.int32)
+    got = _encoder().pq_zstd_compress(src.ctypes.data, len(data), out.ctypes.data, cap, table.ctypes.data)
+    if got < 0:
+        raise RuntimeError("ZSTD compress buffer overflow")
     return out[:got].tobytes()
 
 
@@ -163,7 +178,7 @@ class TWriter:
         self.buf.append(0)
 
 
-CODEC_UNCOMPRESSED, CODEC_SNAPPY = 0, 1
+CODEC_UNCOMPRESSED, CODEC_SNAPPY, CODEC_ZSTD = 0, 1, 6
 
 
 def _page_header(ptype, size, num_values=None, encoding=None, dict_values=None, compressed_size=None):
@@ -237,14 +252,14 @@ def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="sloth
           stats=False):
     """Return the bytes of a Parquet file holding `columns` (equal lengths);
     codec "snappy" compresses every page (dictionary and data) as one raw
-    Snappy block; stats writes each numeric column chunk's min / max
-    (Statistics min_value / max_value)."""
-    snappy = codec == "snappy"
+    Snappy block, codec "zstd" as one ZSTD frame; stats writes each numeric
+    column chunk's min / max (Statistics min_value / max_value)."""
+    assert codec in (None, "snappy", "zstd")
 
     def page(ptype, payload, **kw):
-        if not snappy:
+        if codec is None:
             return _page_header(ptype, len(payload), **kw), payload, len(payload)
-        body = snappy_compress(payload)
+        body = snappy_compress(payload) if codec == "snappy" else zstd_compress(payload)
         return _page_header(ptype, len(payload), compressed_size=len(body), **kw), body, len(payload)
     n = columns[0].n()
     for c in columns:
@@ -332,7 +347,7 @@ def write(columns, row_group_rows=1_000_000, page_rows=65_536, created_by="sloth
                 w.list_i32(e)
             w.begin_list(3, CT_BINARY, 1)
             w.list_binary(c.name)
-            w.i32(4, CODEC_SNAPPY if snappy else CODEC_UNCOMPRESSED)
+            w.i32(4, {None: CODEC_UNCOMPRESSED, "snappy": CODEC_SNAPPY, "zstd": CODEC_ZSTD}[codec])
             w.i64(5, rows)
             w.i64(6, unc)
             w.i64(7, size)

@@ -17,6 +17,7 @@ CASES = {
     "distinct100m": ["--rows", "200000", "--cpu-sample", "100000"],
     "parquet200m": ["--pq-rows", "300000", "--cpu-sample", "100000"],
     "parquet200m_snappy": ["--pq-rows", "300000", "--cpu-sample", "100000"],
+    "parquet200m_zstd": ["--pq-rows", "300000", "--cpu-sample", "100000"],
     "dictsum200m": ["--pq-rows", "300000", "--cpu-sample", "100000"],
     "batch256": ["--tables", "1"],
     "serve": ["--duration", "0.05", "--scale", "0.001"],

@@ -72,3 +72,36 @@ def test_zstd_damaged_frames(zs):
             m[int(rng.integers(0, len(m)))] = int(rng.integers(0, 256))
         r = zs.zstd_host_decompress(bytes(m), len(m), out, len(raw))
         assert -1 <= r <= len(raw)
+
+
+def test_writer_zstd_frames(zs):
+    """The writer's ZSTD frames (slothdb_gb300/pq_encode.c) decode to the
+    same bytes with pyarrow's zstd and with the page decoder."""
+    pa = pytest.importorskip("pyarrow")
+    from slothdb_gb300 import parquet as pq
+    for name, raw in _cases().items():
+        c = pq.zstd_compress(raw)
+        if raw:
+            assert pa.decompress(c, decompressed_size=len(raw), codec="zstd", asbytes=True) == raw, name
+        out = ctypes.create_string_buffer(max(len(raw), 1))
+        assert zs.zstd_host_decompress(c, len(c), out, len(raw)) == len(raw), name
+        assert out.raw[:len(raw)] == raw, name
+
+
+def test_writer_zstd_file_read_by_pyarrow():
+    """A ZSTD Parquet file from the writer: pyarrow reads the same values,
+    and the library's parser opens it."""
+    pq_ = pytest.importorskip("pyarrow.parquet")
+    import io
+    from slothdb_gb300 import capi
+    from slothdb_gb300 import parquet as pq
+    _, key, f, v = pq.filter_groupby_file(n_rows=30_000, row_group_rows=10_000, page_rows=4096, n_dict=512)
+    cols = [pq.Column("key", pq.T_INT32, values=key), pq.Column("f", pq.T_INT32, values=f, int16=True),
+            pq.Column("v", pq.T_INT64, values=v)]
+    data = pq.write(cols, row_group_rows=10_000, page_rows=4096, codec="zstd")
+    t = pq_.read_table(io.BytesIO(data))
+    assert np.array_equal(t.column("key").to_numpy(), key) and np.array_equal(t.column("v").to_numpy(), v)
+    assert np.array_equal(t.column("f").to_numpy(), f.astype(np.int16))
+    pf = capi.ParquetFile(data)
+    assert pf.num_rows == 30_000
+    pf.close()
