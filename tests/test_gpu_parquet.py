@@ -223,15 +223,16 @@ def test_parquet_int_varchar_pair_key():
                 orc)
 
 
+@pytest.mark.parametrize("codec", ["snappy", "zstd"])
 @pytest.mark.parametrize("device", [False, True])
-def test_snappy_pages_from_the_project_writer(device):
-    """SNAPPY column chunks (dictionary and data pages) inflated on the GPU
-    per batch and decoded from the image, against the oracle; several
-    batches, with a filter that the zone maps do not prune."""
+def test_compressed_pages_from_the_project_writer(device, codec):
+    """SNAPPY or ZSTD column chunks (dictionary and data pages) decompressed
+    on the GPU per batch and decoded from the image, against the oracle;
+    several batches, with a filter that the zone maps do not prune."""
     _, key, f, v = pq.filter_groupby_file(n_rows=300_000, row_group_rows=50_000, page_rows=8192, n_dict=4096)
     cols = [pq.Column("key", pq.T_INT32, values=key), pq.Column("f", pq.T_INT32, values=f, int16=True),
             pq.Column("v", pq.T_INT64, values=v)]
-    data = pq.write(cols, row_group_rows=50_000, page_rows=8192, codec="snappy")
+    data = pq.write(cols, row_group_rows=50_000, page_rows=8192, codec=codec)
     types = [INTEGER, SMALLINT, BIGINT]
     aggs = [("sum", 2), ("count_star", -1), ("max", 2)]
     for filters, batches in (([], 1), ([(1, "<", 300)], 3)):

@@ -125,6 +125,35 @@ def test_parquet_filter_groupby_project_writer_file():
               filters=[(1, "<", 100)], ref_file=path)
 
 
+@pytest.mark.parametrize("codec", ["snappy", "zstd"])
+def test_parquet_compressed_pages(codec):
+    """The fused workload's shape with SNAPPY or ZSTD pages, written by
+    pyarrow and by the project writer (its own compressors), read by the
+    reference's Parquet reader (its vendored snappy and zstd) with WHERE f <
+    100, against the oracle on the decoded columns."""
+    pa = pytest.importorskip("pyarrow")
+    pq = pytest.importorskip("pyarrow.parquet")
+    from slothdb_gb300 import parquet as gpq
+    _, key, f, v = gpq.filter_groupby_file(n_rows=300_000, seed=2, n_dict=65_536, row_group_rows=100_000,
+                                           page_rows=16_384)
+    cols = [gpq.Column("key", gpq.T_INT32, values=key), gpq.Column("f", gpq.T_INT32, values=f, int16=True),
+            gpq.Column("v", gpq.T_INT64, values=v)]
+    ours = gpq.write(cols, row_group_rows=100_000, page_rows=16_384, codec=codec)
+    tbl = pa.table({"key": pa.array(key, pa.int32()), "f": pa.array(f.astype(np.int16), pa.int16()),
+                    "v": pa.array(v, pa.int64())})
+    with tempfile.TemporaryDirectory() as d:
+        for name in ("pyarrow", "project"):
+            path = os.path.join(d, name + ".parquet")
+            if name == "pyarrow":
+                pq.write_table(tbl, path, row_group_size=100_000, compression=codec.upper(), use_dictionary=["key"])
+            else:
+                with open(path, "wb") as fh:
+                    fh.write(ours)
+            check("SELECT \"key\", SUM(v), COUNT(*) FROM '{file}' WHERE f < 100 GROUP BY \"key\"",
+                  [INTEGER, SMALLINT, BIGINT], [0], [("sum", 2), ("count_star", -1)], [key, f.astype(np.int16), v],
+                  filters=[(1, "<", 100)], ref_file=path)
+
+
 def test_parquet_optional_columns_with_nulls():
     """pyarrow OPTIONAL columns with NULL values (definition levels), read by
     the reference's own Parquet reader, against the oracle with the same
