@@ -56,8 +56,8 @@ typedef enum gb_type {
  * COUNT(DISTINCT col) → BIGINT: the number of distinct non-NULL values of an
  * integer column in the group (the per-group value sets of
  * src/execution/int_group_agg.cpp:89-92, union sizes at 154-270); 0 for a
- * group whose values are all NULL.  It runs in hash mode only (not radix,
- * not gb_batch_*); at most GB_MAX_DISTINCT distinct columns per query. */
+ * group whose values are all NULL.  It runs in hash mode and in batches
+ * (not in radix mode); at most GB_MAX_DISTINCT distinct columns per query. */
 typedef enum gb_agg_kind {
     GB_AGG_COUNT_STAR = 0,
     GB_AGG_COUNT = 1,

@@ -93,7 +93,8 @@ __device__ __forceinline__ void copy_words(void *dst, const void *src, int bytes
 
 // Item (q, idx) covers words [idx * 65536, (idx+1) * 65536) of the query's
 // init range: the table words, then the validity words of every output column
-// (all ones; the emit clears the bits of NULL results), then for a VARCHAR
+// (all ones; the emit clears the bits of NULL results), then (COUNT(DISTINCT))
+// the pair sets, their NULL-key twins and the pair counters, after, for a VARCHAR
 // key the dictionary's hash slots (free), ref slots (unpublished) and its
 // eight counter words (zero).
 __global__ void k_batch_init(const BQuery *qs, const BItem *items, u32 n_items) {
@@ -104,6 +105,10 @@ __global__ void k_batch_init(const BQuery *qs, const BItem *items, u32 n_items) 
         const u64 vwords = (q.E.out_cap + 63) / 64;
         const u64 n0 = q.table_words, n1 = n0 + (u64)(q.E.n_keys + q.E.n_aggs) * vwords;
         const u64 dc = q.is_str ? q.D.cap : 0;
+        const u64 n2 = n1 + (q.is_str ? 2 * dc + 8 : 0);
+        const u64 sw = q.P.n_dist ? (q.P.dmask + 1) * (q.P.dnarrow ? 1 : 2) * (u64)q.P.n_dist : 0;
+        const u64 nw = q.P.null_sets ? sw : 0;
+        const u64 dempty = q.P.dnarrow ? ~0ull : EMPTY_KEY;
         const u64 lo = (u64)w.idx * 65536, hi = min(q.init_words, lo + 65536);
         for (u64 i = lo + threadIdx.x; i < hi; i += blockDim.x) {
             if (i < n0) {
@@ -120,8 +125,14 @@ __global__ void k_batch_init(const BQuery *qs, const BItem *items, u32 n_items) 
                 q.D.hash[i - n1] = EMPTY_KEY;
             } else if (i < n1 + 2 * dc) {
                 q.D.ref[i - n1 - dc] = REF_PENDING;
-            } else {
+            } else if (i < n2) {
                 q.D.next_id[i - n1 - 2 * dc] = 0;  // next id, arena used, error word, spare
+            } else if (i < n2 + sw) {
+                q.P.dsets[i - n2] = dempty;  // COUNT(DISTINCT) pair sets: empty
+            } else if (i < n2 + sw + nw) {
+                q.P.null_sets[i - n2 - sw] = dempty;
+            } else {
+                q.P.dmeta[i - n2 - sw - nw] = 0;  // pairs, overflow flag, marker flags
             }
         }
     }
@@ -474,12 +485,15 @@ __device__ __noinline__ void generic_tile(const Plan &sP, const TableRef &sT, u6
     sm.probe = 8;
     sm.keys = bsm;
     sm.st = bsm + sm.S;
+    __shared__ u32 s_pairs;  // COUNT(DISTINCT): new pairs of this tile
+    if (threadIdx.x == 0) s_pairs = 0;
     smem_init(sP, sm);
     __syncthreads();
     for (u64 base = t0 + (u64)warp * 32; base < t1; base += (u64)nwarps * 32)
-        warp_rows<PRECOMBINE>(sP, sT, sm, base, t1, new_groups, nullptr);  // no OP_DIST in a batch
+        warp_rows<PRECOMBINE>(sP, sT, sm, base, t1, new_groups, &s_pairs);
     __syncthreads();
     smem_flush(sP, sT, sm, new_groups);
+    if (threadIdx.x == 0 && s_pairs) atomicAdd(sP.dmeta, (unsigned long long)s_pairs);
 }
 
 // The persistent loop shared by the ingest kernels: claim the next item of
@@ -1027,6 +1041,11 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
             h->spill_cap = (u32)need_spill;
         }
         if ((s = alloc_outputs(h, h->cap + 2))) return s;
+        if (h->plan.n_dist) {
+            // pair sets for this query's rows, emptied by the batch's init
+            h->dpairs = 0;
+            if ((s = dist_reserve(h, n, st))) return s;
+        }
         d.P = h->plan;
         if (b->fast) d.F = make_fast_plan(h->plan, d.FF);
         d.T = table_ref(h);
@@ -1051,6 +1070,10 @@ static gb_status batch_prepare(gb_batch *b, cudaStream_t st) {
         }
         d.init_words = d.table_words + (u64)(d.E.n_keys + d.E.n_aggs) * ((d.E.out_cap + 63) / 64) +
                        (d.is_str ? 2 * d.D.cap + 8 : 0);
+        if (h->plan.n_dist) {
+            const u64 sw = (h->plan.dmask + 1) * (h->plan.dnarrow ? 1 : 2) * (u64)h->plan.n_dist;
+            d.init_words += sw * (h->plan.null_sets ? 2 : 1) + 2 + GB_MAX_DISTINCT;
+        }
         for (u64 c = 0; c * 65536 < d.init_words; c++) it_init.push_back({q, (u32)c});
         d.tile_rows = b->tile_rows;
         for (u64 c = 0; c * b->tile_rows < n; c++) it_ing.push_back({q, (u32)c});
@@ -1294,11 +1317,6 @@ gb_status gb_batch_create(gb_batch **out) {
 
 gb_status gb_batch_add(gb_batch *b, const gb_agg_spec *spec, const gb_col *cols, uint64_t nrows, uint32_t *qidx) {
     if (!b || !spec || (!cols && nrows)) return GB_ERR_INVALID;
-    for (uint32_t a = 0; a < spec->n_aggs && spec->aggs; a++)
-        if (spec->aggs[a].kind == GB_AGG_COUNT_DISTINCT) {
-            set_error("COUNT(DISTINCT) runs on its own handle (gb_agg_*), not in a batch");
-            return GB_ERR_UNSUPPORTED;
-        }
     if (spec->n_groups == 2 && spec->group_cols && spec->col_types)
         for (uint32_t g = 0; g < 2; g++)
             if (spec->group_cols[g] >= 0 && (uint32_t)spec->group_cols[g] < spec->n_cols &&
@@ -1427,7 +1445,12 @@ gb_status gb_batch_run(gb_batch *b, void *stream) {
     for (u32 q = 0; q < nq; q++) {
         gb_agg *h = b->handles[q];
         const Ctl &c = qc[q];
-        const bool bad = c.spill_count || c.err || c.aux1 || c.out_count > h->out_cap;
+        bool bad = c.spill_count || c.err || c.aux1 || c.out_count > h->out_cap;
+        if (!bad && h->plan.n_dist) {  // the pair sets' counters
+            GB_CUDA(cudaMemcpy(h->dmeta_host, h->dmeta.p, sizeof(h->dmeta_host), cudaMemcpyDeviceToHost));
+            bad = h->dmeta_host[1] != 0;
+            h->dpairs = h->dmeta_host[0];
+        }
         if (bad) {
             // host decisions needed (spill / dictionary growth): the whole query
             // re-runs on its own handle

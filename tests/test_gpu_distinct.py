@@ -157,7 +157,6 @@ def test_narrow_pair_sets_reset_and_resident():
 
 
 def test_rejections():
-    k = np.arange(10, dtype=np.int32)
     with pytest.raises(capi.GbError):
         capi.GroupBy([INTEGER, DOUBLE], [0], [("count_distinct", 1)])
     with pytest.raises(capi.GbError):
@@ -165,9 +164,57 @@ def test_rejections():
                      [("count_distinct", 1), ("count_distinct", 2), ("count_distinct", 3)])
     with pytest.raises(capi.GbError):
         capi.GroupBy([BIGINT, BIGINT], [0], [("count_distinct", 1)], options={"mode": RADIX})
+
+
+def test_batch_with_count_distinct():
+    """COUNT(DISTINCT) queries in a batch (generic tiles, pair sets emptied
+    by the batch's init): 8-byte sets (INTEGER key and value), 16-byte sets
+    with NULL keys (a nullable BIGINT key: twin sets), a VARCHAR key, next to
+    a plain query; every result against the oracle, on the first run and on
+    the graph's replay."""
+    import torch
+    import oracle
+    from util import compare, gpu_to_dict
+    rng = np.random.default_rng(61)
+    n = 250_000
+    k1 = rng.integers(-3000, 3000, n).astype(np.int32)
+    v1 = rng.integers(-500, 500, n).astype(np.int32)
+    k2 = rng.integers(0, 9000, n).astype(np.int64)
+    v2 = rng.integers(0, 10**9, n).astype(np.int64)
+    kn2 = rng.random(n) < 0.03
+    (offs, data), s3, m3 = datagen.varchar_table(80_000, 2000, seed=62)
+    m3 = (m3 % 300).astype(np.int32)
+    qs = [
+        ([INTEGER, INTEGER], [0], [("count_distinct", 1), ("count_star", -1)], [k1, v1], None, 6000),
+        ([BIGINT, BIGINT], [0], [("count_distinct", 1), ("sum", 1)], [k2, v2], [kn2, None], 9000),
+        ([VARCHAR, BIGINT, INTEGER], [0], [("count_distinct", 2), ("max", 1)], [(offs, data), s3, m3], None, 2000),
+        ([INTEGER, INTEGER], [0], [("count_star", -1), ("sum", 1)], [k1, v1], None, 6000),
+    ]
+
+    def dev(c):
+        if isinstance(c, tuple):
+            return (torch.from_numpy(c[0]).cuda(), torch.from_numpy(c[1]).cuda())
+        return torch.from_numpy(np.ascontiguousarray(c)).cuda()
+
     b = capi.Batch()
     try:
-        with pytest.raises(capi.GbError):
-            b.add([INTEGER, BIGINT], [0], [("count_distinct", 1)], [k, k.astype(np.int64)], len(k))
+        for types, gcols, aggs, cols, nulls, est in qs:
+            d = [dev(c) for c in cols]
+            vd = None
+            nullable = ()
+            if nulls is not None:
+                vd = [torch.from_numpy(capi.validity_words(~m).view(np.int64)).cuda() if m is not None else None
+                      for m in nulls]
+                nullable = [i for i, m in enumerate(nulls) if m is not None]
+            rows = len(cols[-1])
+            b.add(types, gcols, aggs, d, rows, validity=vd, nullable=nullable, est_groups=est)
+        torch.cuda.synchronize()
+        for _ in range(2):  # the first run and the graph's replay
+            b.run()
+            for i, (types, gcols, aggs, cols, nulls, est) in enumerate(qs):
+                orc = oracle.run_query(types, gcols, aggs, cols, nulls=nulls)
+                out_types = [types[c] for c in gcols] + [
+                    oracle.agg_out_type(oracle.AGG_NAMES[kd], types[c] if c >= 0 else 0) for kd, c in aggs]
+                compare(gpu_to_dict(b.result(i), len(gcols), out_types), orc)
     finally:
         b.close()
