@@ -16,9 +16,9 @@
 //   execute  the admitted queries run as one gb_batch (one pass of a few
 //            persistent kernels), except high-cardinality queries (estimated
 //            groups >= 2^20), which run one by one on their own handle (the
-//            radix path), and COUNT(DISTINCT) queries, which run alone on a
-//            hash handle; in mode 1 every query runs alone on its own handle
-//            (the one-at-a-time baseline);
+//            radix path), and queries with a VARCHAR in a pair key, which run
+//            alone on a hash handle; in mode 1 every query runs alone on its
+//            own handle (the one-at-a-time baseline);
 //   complete results are copied to host memory owned by the ticket, the
 //            ticket records queue / execution times, and waiters wake up.
 //
@@ -151,11 +151,9 @@ struct Query {
     u64 t_submit = 0, t_start = 0, t_done = 0;
     uint32_t batch_size = 0;
 
-    // queries the batch kernels do not take (COUNT(DISTINCT), a VARCHAR in a
-    // pair key) run alone on their own handle
-    bool distinct() const {
-        for (const gb_agg_desc &a : aggs)
-            if (a.kind == GB_AGG_COUNT_DISTINCT) return true;
+    // queries the batch kernels do not take (a VARCHAR in a pair key) run
+    // alone on their own handle
+    bool batch_refused() const {
         if (group_cols.size() == 2)
             for (int32_t g : group_cols)
                 if (col_types[g] == GB_T_VARCHAR) return true;
@@ -416,10 +414,10 @@ void run_batch(gb_server *s, Lane &L, std::vector<Query *> &qs) {
     }
 }
 
-// A query that takes the lone-handle path (radix-sized estimate,
-// COUNT(DISTINCT), a VARCHAR in a pair key, or one-at-a-time mode).
+// A query that takes the lone-handle path (radix-sized estimate, a VARCHAR
+// in a pair key, or one-at-a-time mode).
 bool runs_alone(const gb_server *s, const Query *q) {
-    return s->mode == 1 || q->est_groups >= RADIX_GROUPS || q->distinct();
+    return s->mode == 1 || q->est_groups >= RADIX_GROUPS || q->batch_refused();
 }
 
 // One lane's loop: admit queries from the front of the queue (FIFO) while

@@ -65,6 +65,8 @@ def _queries(rng, n, tabs):
         sel = float(rng.uniform(0.01, 1.0))
         if t == 2:
             group_cols, aggs = [0], [("count_star", -1), ("sum", 1), ("min", 1), ("max", 1)]
+            if i % 3 == 0:  # COUNT(DISTINCT), batched beside the others
+                aggs = [("count_distinct", 1), ("count_star", -1), ("sum", 1)]
             filters = [(1, "<", int(sel * 10**6))]
         else:
             q = COMP if t == 0 else STR
