@@ -19,8 +19,12 @@
 
 #ifdef __CUDACC__
 #define ZS_HD __host__ __device__ __forceinline__
+// Table builders run once per block: kept out of line on the device so
+// that their registers do not add to the sequence loop's
+#define ZS_COLD __host__ __device__ __noinline__
 #else
 #define ZS_HD inline
+#define ZS_COLD inline
 #endif
 
 namespace gbz {
@@ -74,23 +78,23 @@ ZS_HD uint32_t zs_bits(const uint8_t *src, int64_t size, int64_t pos, int n) {
 // time, when a read leaves them.
 struct ZsBack {
     const uint8_t *src;
-    int64_t size;
-    int64_t pos;  // bits not yet read; < 0 once more were read than the stream holds
-    int64_t wlo;  // first bit of the window (a multiple of 8)
+    int32_t size;  // bytes (a stream lies inside one block: at most 128 KB)
+    int32_t pos;   // bits not yet read; < 0 once more were read than the stream holds
+    int32_t wlo;   // first bit of the window (a multiple of 8)
     uint64_t win;
 };
 
-ZS_HD void zs_back_load(ZsBack &b, int64_t top) {  // a window that holds the bits below `top`
-    int64_t lo = top - 64;  // rounded up to a byte: the window still reaches `top`
+ZS_HD void zs_back_load(ZsBack &b, int32_t top) {  // a window that holds the bits below `top`
+    int32_t lo = top - 64;  // rounded up to a byte: the window still reaches `top`
     lo = lo >= 0 ? ((lo + 7) >> 3) << 3 : -((-lo) >> 3) * 8;
     b.wlo = lo;
     uint64_t v = 0;
-    const int64_t b0 = lo >> 3;  // exact: lo is a multiple of 8
+    const int32_t b0 = lo >> 3;  // exact: lo is a multiple of 8
     if (b0 >= 0 && b0 + 8 <= b.size) {
         for (int k = 0; k < 8; k++) v |= (uint64_t)b.src[b0 + k] << (8 * k);
     } else {
         for (int k = 0; k < 8; k++) {
-            const int64_t i = b0 + k;
+            const int32_t i = b0 + k;
             if (i >= 0 && i < b.size) v |= (uint64_t)b.src[i] << (8 * k);
         }
     }
@@ -98,16 +102,16 @@ ZS_HD void zs_back_load(ZsBack &b, int64_t top) {  // a window that holds the bi
 }
 
 ZS_HD bool zs_back_init(ZsBack &b, const uint8_t *src, int64_t size) {
+    if (size <= 0 || size > (int64_t)ZS_BLOCK_MAX || src[size - 1] == 0) return false;
     b.src = src;
-    b.size = size;
-    if (size <= 0 || src[size - 1] == 0) return false;
-    b.pos = (size - 1) * 8 + zs_highbit(src[size - 1]);
+    b.size = (int32_t)size;
+    b.pos = (b.size - 1) * 8 + zs_highbit(src[size - 1]);
     zs_back_load(b, b.pos);
     return true;
 }
 
 // Bits [p, p + n) of the stream, n <= 32.
-ZS_HD uint32_t zs_back_bits(ZsBack &b, int64_t p, int n) {
+ZS_HD uint32_t zs_back_bits(ZsBack &b, int32_t p, int n) {
     if (n == 0) return 0;
     if (p < b.wlo || p + n > b.wlo + 64) zs_back_load(b, p + n);
     return (uint32_t)((b.win >> (p - b.wlo)) & ((1ull << n) - 1));
@@ -254,7 +258,7 @@ ZS_HD void zs_ml(uint32_t code, uint32_t *base, int *bits) {
 
 // A sequence table from its mode: 0 predefined, 1 RLE, 2 described here, 3
 // the previous one.  Returns the bytes used, or -1.
-ZS_HD int64_t zs_seq_table(int mode, int which, const uint8_t *src, int64_t n, uint32_t *tab, int *log, int max_log,
+ZS_COLD int64_t zs_seq_table(int mode, int which, const uint8_t *src, int64_t n, uint32_t *tab, int *log, int max_log,
                            int max_sym, bool *have) {
     int16_t norm[64];
     int nsym, al;
@@ -285,7 +289,7 @@ ZS_HD int64_t zs_seq_table(int mode, int which, const uint8_t *src, int64_t n, u
 
 // The Huffman table of a literals section: returns the bytes of its
 // description, or -1.
-ZS_HD int64_t zs_huf_table(const uint8_t *src, int64_t n, ZsScratch &S, int *maxbits) {
+ZS_COLD int64_t zs_huf_table(const uint8_t *src, int64_t n, ZsScratch &S, int *maxbits) {
     if (n < 1) return -1;
     uint8_t w[256];
     int nw = 0;
@@ -359,7 +363,7 @@ ZS_HD int64_t zs_huf_table(const uint8_t *src, int64_t n, ZsScratch &S, int *max
     return used;
 }
 
-ZS_HD bool zs_huf_stream(const uint8_t *src, int64_t n, const ZsScratch &S, int mb, uint8_t *out, int64_t count) {
+ZS_COLD bool zs_huf_stream(const uint8_t *src, int64_t n, const ZsScratch &S, int mb, uint8_t *out, int64_t count) {
     ZsBack b;
     if (!zs_back_init(b, src, n)) return false;
     for (int64_t i = 0; i < count; i++) {
@@ -376,10 +380,10 @@ ZS_HD bool zs_huf_stream(const uint8_t *src, int64_t n, const ZsScratch &S, int 
 // least 8 bytes behind (`gap`), or a source ahead of the destination (the
 // literals, gap 8).  An overlapping match closer than 8 bytes repeats its
 // first `gap` bytes, loaded once.
-ZS_HD void zs_copy(uint8_t *d, const uint8_t *s, int64_t n, int64_t gap) {
+ZS_HD void zs_copy(uint8_t *d, const uint8_t *s, int32_t n, int32_t gap) {
     if (gap >= 8 || gap >= n) {
-        for (int64_t i = 0; i < n; i += 8) {
-            const int64_t m = n - i < 8 ? n - i : 8;
+        for (int32_t i = 0; i < n; i += 8) {
+            const int32_t m = n - i < 8 ? n - i : 8;
             uint8_t t[8];
 #pragma unroll
             for (int k = 0; k < 8; k++)
@@ -391,8 +395,8 @@ ZS_HD void zs_copy(uint8_t *d, const uint8_t *s, int64_t n, int64_t gap) {
         return;
     }
     uint8_t t[8];
-    for (int64_t k = 0; k < gap; k++) t[k] = s[k];
-    for (int64_t i = 0, r = 0; i < n; i++) {
+    for (int32_t k = 0; k < gap; k++) t[k] = s[k];
+    for (int32_t i = 0, r = 0; i < n; i++) {
         d[i] = t[r];
         r = r + 1 == gap ? 0 : r + 1;
     }
@@ -520,8 +524,8 @@ ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap, in
             int mln, lln;
             zs_ml(mlc, &mlb, &mln);
             zs_ll(llc, &llb, &lln);
-            const int64_t ml = mlb + zs_read(b, mln);
-            const int64_t ll = llb + zs_read(b, lln);
+            const uint32_t ml = mlb + zs_read(b, mln);
+            const uint32_t ll = llb + zs_read(b, lln);
             uint32_t off;
             if (ofv > 3) {
                 off = ofv - 3;
@@ -546,7 +550,8 @@ ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap, in
             }
             if (b.pos < 0) return false;
             // execute: ll literals, then ml bytes from off back
-            if (ll > lsize - lp || ll + ml > cap - *op || off == 0 || (int64_t)off > *op + ll) return false;
+            if ((int64_t)ll > lsize - lp || (int64_t)(ll + ml) > cap - *op || off == 0 || (int64_t)off > *op + ll)
+                return false;
             zs_copy(dst + *op, lit + lp, ll, 8);  // forward: never ahead of the literal read
             *op += ll;
             lp += ll;
