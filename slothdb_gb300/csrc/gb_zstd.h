@@ -37,8 +37,9 @@ enum : uint32_t {
     ZS_BLOCK_MAX = 131072,
 };
 
-// Scratch of one decode (9.5 KB): the Huffman table, the three sequence
-// tables and the Huffman weights' table.  A block's literals are decoded
+// Scratch of one decode (13.3 KB): the Huffman table, the three sequence
+// tables with the lengths' baselines per cell, and the Huffman weights'
+// table.  A block's literals are decoded
 // into the end of the destination, dst[cap - literals, cap): the sequences
 // write at or below the next literal they read (their output before the
 // block's end is at most cap - literals + the literals read so far), so the
@@ -46,6 +47,8 @@ enum : uint32_t {
 struct ZsScratch {
     uint16_t huf[1u << ZS_HUF_LOG];  // (symbol << 8) | code length
     uint32_t ll[1u << ZS_LL_LOG], ml[1u << ZS_ML_LOG], of[1u << ZS_OF_LOG];
+    // per cell of ll / ml: the length's baseline | its extra bits << 24
+    uint32_t llx[1u << ZS_LL_LOG], mlx[1u << ZS_ML_LOG];
     uint32_t wt[64];                 // the Huffman weights' FSE table (accuracy <= 6)
 };
 
@@ -258,33 +261,39 @@ ZS_HD void zs_ml(uint32_t code, uint32_t *base, int *bits) {
 
 // A sequence table from its mode: 0 predefined, 1 RLE, 2 described here, 3
 // the previous one.  Returns the bytes used, or -1.
-ZS_COLD int64_t zs_seq_table(int mode, int which, const uint8_t *src, int64_t n, uint32_t *tab, int *log, int max_log,
-                           int max_sym, bool *have) {
+ZS_COLD int64_t zs_seq_table(int mode, int which, const uint8_t *src, int64_t n, uint32_t *tab, uint32_t *xtab,
+                             int *log, int max_log, int max_sym, bool *have) {
     int16_t norm[64];
     int nsym, al;
+    int64_t used;
     if (mode == 0) {
         const int16_t *p = zs_predef(which, &nsym, &al);
         for (int s = 0; s < nsym; s++) norm[s] = p[s];
         if (!zs_fse_build(tab, al, norm, nsym)) return -1;
-        *log = al;
-        *have = true;
-        return 0;
-    }
-    if (mode == 1) {
+        used = 0;
+    } else if (mode == 1) {
         if (n < 1 || src[0] >= max_sym) return -1;
         tab[0] = zs_cell(src[0], 0, 0);
-        *log = 0;
-        *have = true;
-        return 1;
-    }
-    if (mode == 2) {
-        const int64_t used = zs_read_ncount(src, n, max_log, max_sym, norm, &nsym, &al);
+        al = 0;
+        used = 1;
+    } else if (mode == 2) {
+        used = zs_read_ncount(src, n, max_log, max_sym, norm, &nsym, &al);
         if (used < 0 || !zs_fse_build(tab, al, norm, nsym)) return -1;
-        *log = al;
-        *have = true;
-        return used;
+    } else {
+        return *have ? 0 : -1;  // repeat: the previous block's table
     }
-    return *have ? 0 : -1;  // repeat: the previous block's table
+    *log = al;
+    *have = true;
+    if (xtab) {  // literal / match lengths: each cell's baseline and extra bits
+        for (uint32_t i = 0; i < (1u << al); i++) {
+            uint32_t base;
+            int bits;
+            if (which == 0) zs_ll(tab[i] & 0xffu, &base, &bits);
+            else zs_ml(tab[i] & 0xffu, &base, &bits);
+            xtab[i] = base | ((uint32_t)bits << 24);
+        }
+    }
+    return used;
 }
 
 // The Huffman table of a literals section: returns the bytes of its
@@ -411,22 +420,23 @@ struct ZsFrame {
 };
 
 // One compressed block src[0, n) appended to dst at *op (capacity cap).
-ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap, int64_t *op, ZsScratch &S, ZsFrame &F) {
+ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int32_t cap, int32_t *op, ZsScratch &S, ZsFrame &F) {
     // literals section
     if (n < 1) return false;
     const uint32_t b0 = src[0], ltype = b0 & 3, sf = (b0 >> 2) & 3;
-    int64_t pos, lsize, csize = 0;
+    int64_t pos, csize = 0;
+    int32_t lsize;
     if (ltype < 2) {
         if (sf == 0 || sf == 2) {
-            lsize = b0 >> 3;
+            lsize = (int32_t)(b0 >> 3);
             pos = 1;
         } else if (sf == 1) {
             if (n < 2) return false;
-            lsize = (b0 >> 4) + ((int64_t)src[1] << 4);
+            lsize = (int32_t)((b0 >> 4) + ((uint32_t)src[1] << 4));
             pos = 2;
         } else {
             if (n < 3) return false;
-            lsize = (b0 >> 4) + ((int64_t)src[1] << 4) + ((int64_t)src[2] << 12);
+            lsize = (int32_t)((b0 >> 4) + ((uint32_t)src[1] << 4) + ((uint32_t)src[2] << 12));
             pos = 3;
         }
     } else {
@@ -435,11 +445,11 @@ ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap, in
         uint64_t v = 0;
         for (int k = 0; k < hb; k++) v |= (uint64_t)src[k] << (8 * k);
         const int bits = sf < 2 ? 10 : (sf == 2 ? 14 : 18);
-        lsize = (int64_t)((v >> 4) & ((1ull << bits) - 1));
+        lsize = (int32_t)((v >> 4) & ((1ull << bits) - 1));
         csize = (int64_t)((v >> (4 + bits)) & ((1ull << bits) - 1));
         pos = hb;
     }
-    if (lsize > ZS_BLOCK_MAX || lsize > cap - *op) return false;
+    if (lsize > (int32_t)ZS_BLOCK_MAX || lsize > cap - *op) return false;
     uint8_t *lit = dst + (cap - lsize);
     if (ltype == 0) {
         if (pos + lsize > n) return false;
@@ -447,7 +457,7 @@ ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap, in
         pos += lsize;
     } else if (ltype == 1) {
         if (pos + 1 > n) return false;
-        for (int64_t i = 0; i < lsize; i++) lit[i] = src[pos];
+        for (int32_t i = 0; i < lsize; i++) lit[i] = src[pos];
         pos += 1;
     } else {
         if (pos + csize > n) return false;
@@ -496,19 +506,19 @@ ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap, in
         nseq = src[pos + 1] + ((int64_t)src[pos + 2] << 8) + 0x7F00;
         pos += 3;
     }
-    int64_t lp = 0;  // literals copied so far
+    int32_t lp = 0;  // literals copied so far
     if (nseq > 0) {
         if (pos >= n) return false;
         const uint32_t modes = src[pos++];
         if (modes & 3) return false;
         int64_t u;
-        if ((u = zs_seq_table((modes >> 6) & 3, 0, src + pos, n - pos, S.ll, &F.ll_log, ZS_LL_LOG, 36, &F.have_ll)) < 0)
+        if ((u = zs_seq_table((modes >> 6) & 3, 0, src + pos, n - pos, S.ll, S.llx, &F.ll_log, ZS_LL_LOG, 36, &F.have_ll)) < 0)
             return false;
         pos += u;
-        if ((u = zs_seq_table((modes >> 4) & 3, 1, src + pos, n - pos, S.of, &F.of_log, ZS_OF_LOG, 32, &F.have_of)) < 0)
+        if ((u = zs_seq_table((modes >> 4) & 3, 1, src + pos, n - pos, S.of, nullptr, &F.of_log, ZS_OF_LOG, 32, &F.have_of)) < 0)
             return false;
         pos += u;
-        if ((u = zs_seq_table((modes >> 2) & 3, 2, src + pos, n - pos, S.ml, &F.ml_log, ZS_ML_LOG, 53, &F.have_ml)) < 0)
+        if ((u = zs_seq_table((modes >> 2) & 3, 2, src + pos, n - pos, S.ml, S.mlx, &F.ml_log, ZS_ML_LOG, 53, &F.have_ml)) < 0)
             return false;
         pos += u;
         ZsBack b;
@@ -516,16 +526,13 @@ ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap, in
         uint32_t sll = zs_read(b, F.ll_log), sof = zs_read(b, F.of_log), sml = zs_read(b, F.ml_log);
         for (int64_t q = 0; q < nseq; q++) {
             const uint32_t cl = S.ll[sll], co = S.of[sof], cm = S.ml[sml];
-            const uint32_t llc = cl & 0xff, ofc = co & 0xff, mlc = cm & 0xff;
-            if (llc > 35 || mlc > 52 || ofc > 31) return false;
+            const uint32_t xl = S.llx[sll], xm = S.mlx[sml];
+            const uint32_t ofc = co & 0xff;
+            if (ofc > 31) return false;
             // offset bits first, then match length, then literal length
             uint32_t ofv = (1u << ofc) + (ofc ? zs_read(b, (int)ofc) : 0u);
-            uint32_t mlb, llb;
-            int mln, lln;
-            zs_ml(mlc, &mlb, &mln);
-            zs_ll(llc, &llb, &lln);
-            const uint32_t ml = mlb + zs_read(b, mln);
-            const uint32_t ll = llb + zs_read(b, lln);
+            const uint32_t ml = (xm & 0xffffffu) + zs_read(b, (int)(xm >> 24));
+            const uint32_t ll = (xl & 0xffffffu) + zs_read(b, (int)(xl >> 24));
             uint32_t off;
             if (ofv > 3) {
                 off = ofv - 3;
@@ -550,13 +557,14 @@ ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap, in
             }
             if (b.pos < 0) return false;
             // execute: ll literals, then ml bytes from off back
-            if ((int64_t)ll > lsize - lp || (int64_t)(ll + ml) > cap - *op || off == 0 || (int64_t)off > *op + ll)
+            // ll <= lsize - lp and ll + ml <= cap - op (< 2^31) before op + ll is formed
+            if (ll > (uint32_t)(lsize - lp) || ll + ml > (uint32_t)(cap - *op) || off == 0 || off > (uint32_t)*op + ll)
                 return false;
-            zs_copy(dst + *op, lit + lp, ll, 8);  // forward: never ahead of the literal read
-            *op += ll;
-            lp += ll;
-            zs_copy(dst + *op, dst + *op - off, ml, off);
-            *op += ml;
+            zs_copy(dst + *op, lit + lp, (int32_t)ll, 8);  // forward: never ahead of the literal read
+            *op += (int32_t)ll;
+            lp += (int32_t)ll;
+            zs_copy(dst + *op, dst + *op - off, (int32_t)ml, (int32_t)off);
+            *op += (int32_t)ml;
         }
         if (b.pos != 0) return false;
     } else if (pos != n) {
@@ -564,14 +572,17 @@ ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap, in
     }
     // the remaining literals
     if (lsize - lp > cap - *op) return false;
-    for (int64_t i = lp; i < lsize; i++) dst[(*op)++] = lit[i];
+    for (int32_t i = lp; i < lsize; i++) dst[(*op)++] = lit[i];
     return true;
 }
 
 // Decompress the frames of src[0, n) into dst (capacity cap): the bytes
 // written, or -1 for a malformed or oversized frame.
-ZS_HD int64_t zstd_decompress(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap, ZsScratch &S) {
-    int64_t ip = 0, op = 0;
+ZS_HD int64_t zstd_decompress(const uint8_t *src, int64_t n, uint8_t *dst, int64_t cap64, ZsScratch &S) {
+    // output positions are 32-bit: a page holds less than 2 GB
+    const int32_t cap = cap64 > 0x7fffffff ? 0x7fffffff : (int32_t)cap64;
+    int64_t ip = 0;
+    int32_t op = 0;
     while (ip < n) {
         if (n - ip < 4) return -1;
         const uint32_t magic = src[ip] | (src[ip + 1] << 8) | (src[ip + 2] << 16) | ((uint32_t)src[ip + 3] << 24);
@@ -612,14 +623,14 @@ ZS_HD int64_t zstd_decompress(const uint8_t *src, int64_t n, uint8_t *dst, int64
             const int64_t bsize = bh >> 3;
             if (type == 0) {  // raw
                 if (bsize > n - ip || bsize > cap - op) return -1;
-                zs_copy(dst + op, src + ip, bsize, 8);
+                zs_copy(dst + op, src + ip, (int32_t)bsize, 8);
                 ip += bsize;
-                op += bsize;
+                op += (int32_t)bsize;
             } else if (type == 1) {  // RLE: one byte, bsize times
                 if (ip >= n || bsize > cap - op) return -1;
-                for (int64_t i = 0; i < bsize; i++) dst[op + i] = src[ip];
+                for (int32_t i = 0; i < (int32_t)bsize; i++) dst[op + i] = src[ip];
                 ip += 1;
-                op += bsize;
+                op += (int32_t)bsize;
             } else if (type == 2) {
                 if (bsize > n - ip || bsize > ZS_BLOCK_MAX) return -1;
                 if (!zs_block(src + ip, bsize, dst, cap, &op, S, F)) return -1;
