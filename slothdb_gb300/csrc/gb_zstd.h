@@ -39,11 +39,12 @@ enum : uint32_t {
 
 // Scratch of one decode (13.3 KB): the Huffman table, the three sequence
 // tables with the lengths' baselines per cell, and the Huffman weights'
-// table.  A block's literals are decoded
-// into the end of the destination, dst[cap - literals, cap): the sequences
-// write at or below the next literal they read (their output before the
-// block's end is at most cap - literals + the literals read so far), so the
-// literals are consumed before they are overwritten.
+// table.  A block's Huffman or RLE literals are decoded into the end of the
+// destination, dst[cap - literals, cap) (raw literals are read where they
+// lie in the frame): the sequences write at or below the next literal they
+// read (their output before the block's end is at most cap - literals + the
+// literals read so far), so the literals are consumed before they are
+// overwritten.
 struct ZsScratch {
     uint16_t huf[1u << ZS_HUF_LOG];  // (symbol << 8) | code length
     uint32_t ll[1u << ZS_LL_LOG], ml[1u << ZS_ML_LOG], of[1u << ZS_OF_LOG];
@@ -450,14 +451,17 @@ ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int32_t cap, in
         pos = hb;
     }
     if (lsize > (int32_t)ZS_BLOCK_MAX || lsize > cap - *op) return false;
-    uint8_t *lit = dst + (cap - lsize);
+    // raw literals are read where they lie in the frame (src and dst are
+    // different buffers); the others are decoded into the end of dst
+    uint8_t *lbuf = dst + (cap - lsize);
+    const uint8_t *lit = lbuf;
     if (ltype == 0) {
         if (pos + lsize > n) return false;
-        zs_copy(lit, src + pos, lsize, 8);  // src and dst are different buffers
+        lit = src + pos;
         pos += lsize;
     } else if (ltype == 1) {
         if (pos + 1 > n) return false;
-        for (int32_t i = 0; i < lsize; i++) lit[i] = src[pos];
+        for (int32_t i = 0; i < lsize; i++) lbuf[i] = src[pos];
         pos += 1;
     } else {
         if (pos + csize > n) return false;
@@ -475,7 +479,7 @@ ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int32_t cap, in
         }
         const bool four = sf != 0;
         if (!four) {
-            if (!zs_huf_stream(c, cn, S, F.huf_bits, lit, lsize)) return false;
+            if (!zs_huf_stream(c, cn, S, F.huf_bits, lbuf, lsize)) return false;
         } else {
             if (cn < 6) return false;
             const int64_t s1 = c[0] | (c[1] << 8), s2 = c[2] | (c[3] << 8), s3 = c[4] | (c[5] << 8);
@@ -484,10 +488,10 @@ ZS_HD bool zs_block(const uint8_t *src, int64_t n, uint8_t *dst, int32_t cap, in
             const int64_t seg = (lsize + 3) / 4;
             if (3 * seg > lsize) return false;
             const uint8_t *p = c + 6;
-            if (!zs_huf_stream(p, s1, S, F.huf_bits, lit, seg) ||
-                !zs_huf_stream(p + s1, s2, S, F.huf_bits, lit + seg, seg) ||
-                !zs_huf_stream(p + s1 + s2, s3, S, F.huf_bits, lit + 2 * seg, seg) ||
-                !zs_huf_stream(p + s1 + s2 + s3, s4, S, F.huf_bits, lit + 3 * seg, lsize - 3 * seg))
+            if (!zs_huf_stream(p, s1, S, F.huf_bits, lbuf, seg) ||
+                !zs_huf_stream(p + s1, s2, S, F.huf_bits, lbuf + seg, seg) ||
+                !zs_huf_stream(p + s1 + s2, s3, S, F.huf_bits, lbuf + 2 * seg, seg) ||
+                !zs_huf_stream(p + s1 + s2 + s3, s4, S, F.huf_bits, lbuf + 3 * seg, lsize - 3 * seg))
                 return false;
         }
         pos += csize;
