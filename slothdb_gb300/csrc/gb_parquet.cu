@@ -2259,11 +2259,12 @@ __global__ void __launch_bounds__(256) k_pq_inflate(const uint8_t *__restrict__ 
 // after the last job) longest first, decoded by its first lane with the
 // warp's 13.3 KB of tables in `scratch` (a frame is one serial stream;
 // pieces on the lanes of one warp would serialise on their divergent
-// branches).  The tables stay in global memory.  At 128 registers a thread
-// 16 warps per SM decode at once; launch bounds that fit 24 or 32 warps
-// spill, and measured slower.  A frame that does not
+// branches).  The tables stay in global memory.  Launch bounds of 5 blocks
+// an SM hold a thread to 96 registers: 20 warps per SM decode at once, which
+// measured faster than 16 warps at 128 registers and than 24 or 32 warps,
+// whose tighter bounds spill.  A frame that does not
 // decode to exactly dst_len bytes sets ERR_CORRUPT.
-__global__ void __launch_bounds__(128) k_pq_unzstd(const uint8_t *__restrict__ file, InflateJob *jobs, uint32_t n,
+__global__ void __launch_bounds__(128, 5) k_pq_unzstd(const uint8_t *__restrict__ file, InflateJob *jobs, uint32_t n,
                                                    uint8_t *img, uint32_t *lvl, Ctl *ctl, gbz::ZsScratch *scratch) {
     if ((threadIdx.x & 31) != 0) return;
     gbz::ZsScratch &Z = scratch[(blockIdx.x * blockDim.x + threadIdx.x) >> 5];
