@@ -1,5 +1,5 @@
 """The ZSTD page decoder (slothdb_gb300/csrc/gb_zstd.h, the same code the
-GPU runs one thread per page) built for the host and checked against
+GPU runs on one lane per page) built for the host and checked against
 pyarrow's zstd on the same frames: compression levels from fast to high,
 incompressible, constant, run-heavy, integer and text data, frames of
 several blocks, the output capacity exactly the decoded size; damaged frames
